@@ -1,0 +1,114 @@
+/*
+ * spand_gb300.h -- C ABI of the GB300 spaND factorization and solve.
+ *
+ * This is the drop-in boundary for the reference's Tree::partition / assemble /
+ * factorize / solve (leopoldcambier/spaND_public include/tree.h) and its CG driver
+ * (include/is.h).  Plain pointers and sizes only: column-major dense data, CSC sparse
+ * matrices with 0-based sorted int32 row indices, FP64 vectors.  Every function
+ * returns a spand_status; spand_last_error() returns the message of the last failure
+ * on the calling thread.  No function aborts or traps.
+ *
+ * Threading: one spand_tree is used by one thread at a time (the reference Tree is not
+ * re-entrant either: solve() mutates the cluster vectors, include/tree.h:192).
+ */
+#ifndef SPAND_GB300_H
+#define SPAND_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    SPAND_OK = 0,
+    SPAND_ERR_ARG = 1,            /* invalid argument */
+    SPAND_ERR_STATE = 2,          /* call out of order (e.g. solve before factorize) */
+    SPAND_ERR_CUDA = 3,           /* CUDA runtime failure */
+    SPAND_ERR_NOT_SPD = 4,        /* non-SPD pivot: the reference throws "Error: Non-SPD Pivot" (src/tree.cpp:587-590) */
+    SPAND_ERR_UNSUPPORTED = 5,    /* configuration not implemented on the device path */
+    SPAND_ERR_NO_CONVERGENCE = 6
+} spand_status;
+
+typedef struct spand_tree spand_tree;
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* spand_last_error(void);
+
+/* Tree(int lvl)                                    -- include/tree.h:173, src/tree.cpp:113 */
+int spand_tree_create(spand_tree** out, int nlevels);
+/* ~Tree()                                                                              */
+int spand_tree_destroy(spand_tree* t);
+
+/* Setters                                          -- include/tree.h:133-147            */
+int spand_tree_set_verb(spand_tree* t, int verb);                   /* set_verb          */
+int spand_tree_set_use_geo(spand_tree* t, int geo);                 /* set_use_geo       */
+int spand_tree_set_Xcoo(spand_tree* t, const double* X, int dim, int n); /* set_Xcoo: dim x n col-major */
+int spand_tree_set_tol(spand_tree* t, double tol);                  /* set_tol           */
+int spand_tree_set_skip(spand_tree* t, int skip);                   /* set_skip          */
+/* ScalingKind {SVD=0, PLU=1, PLUQ=2, EVD=3, LLT=4, LDLT=5} (include/spaND.h:19)         */
+int spand_tree_set_scaling_kind(spand_tree* t, int kind);           /* set_scaling_kind  */
+/* SymmKind {SPD=0, SYM=1, GEN=2} (include/spaND.h:21)                                   */
+int spand_tree_set_symm_kind(spand_tree* t, int kind);              /* set_symm_kind     */
+/* PartKind {MND=0, RB=1} (include/spaND.h:20)                                           */
+int spand_tree_set_part_kind(spand_tree* t, int kind);              /* set_part_kind     */
+int spand_tree_set_use_sparsify(spand_tree* t, int use);            /* set_use_sparsify  */
+/* No reference counterpart: factor storage and arithmetic in FP32 (1) or FP64 (0).      */
+int spand_tree_set_fp32(spand_tree* t, int fp32);
+
+/* std::vector<ClusterID> partition(SpMat&)         -- include/tree.h:176, src/tree.cpp:306-419
+ * A: n x n pattern in CSC.  sepids (optional, 6*n ints): per dof in natural ordering
+ * self.lvl self.sep l.lvl l.sep r.lvl r.sep. */
+int spand_tree_partition(spand_tree* t, int n, const int* colptr, const int* rowval, int* sepids);
+
+/* void assemble(SpMat&)                            -- include/tree.h:182, src/tree.cpp:505-575
+ * Also builds the symbolic plan of the factorization and uploads the blocks. */
+int spand_tree_assemble(spand_tree* t, int n, const int* colptr, const int* rowval, const double* vals);
+
+/* void factorize()                                 -- include/tree.h:186, src/tree.cpp:1447-1551 */
+int spand_tree_factorize(spand_tree* t);
+
+/* void solve(Eigen::VectorXd&) const               -- include/tree.h:192, src/tree.cpp:1610-1635
+ * x: host buffer n x nrhs (leading dimension ld >= n), natural ordering, in place. */
+int spand_tree_solve(spand_tree* t, double* x, int nrhs, int ld);
+/* Same on a device buffer; runs on the tree's stream and returns without synchronising. */
+int spand_tree_solve_device(spand_tree* t, double* x_dev, int nrhs, int ld);
+
+/* int cg(const SpMat&, const VectorXd& rhs, VectorXd& x, const Tree&, int iters, double tol, bool verb)
+ *                                                  -- include/is.h:12, src/is.cpp:39-121
+ * The matrix is the one given to assemble().  b, x: host vectors (x holds the initial
+ * guess).  iters_out: the reference's return value (i+1); relres_out: |r|/|b| of the
+ * recurrence residual. */
+int spand_cg(spand_tree* t, const double* b, double* x, int iters, double tol, int verb, int* iters_out,
+             double* relres_out);
+/* Same with device vectors. */
+int spand_cg_device(spand_tree* t, const double* b_dev, double* x_dev, int iters, double tol, int* iters_out,
+                    double* relres_out);
+
+/* Introspection (reference: get_N, get_assembly_perm, nnz, get_stop, print_log fields;
+ * include/tree.h:150-165, src/tree.cpp:1645-1727) */
+int spand_tree_get_N(spand_tree* t, int* n);
+int spand_tree_get_perm(spand_tree* t, int* perm);
+int spand_tree_nnz(spand_tree* t, long long* nnz);
+int spand_tree_get_stop(spand_tree* t, int* stop);
+/* 11 values per level: dofs_nd dofs_left_nd dofs_left_elim dofs_left_spars rank_before_sum
+ * rank_after_sum rank_after_count ignored nbrs_sum nbrs_count fact_nnz */
+int spand_tree_level_log(spand_tree* t, long long* out);
+/* (level, cluster order, rows, rank) per sparsified cluster */
+int spand_tree_num_ranks(spand_tree* t, int* n);
+int spand_tree_get_ranks(spand_tree* t, int* out);
+/* Operation list in recording order: kind level self nbr ns nn rows cols (8 ints each);
+ * kind: 0 ScalingLLT 1 GemmSymmOut 2 GemmSymmIn 3 Orthogonal 4 Merge 5 Split */
+int spand_tree_num_ops(spand_tree* t, int* n);
+int spand_tree_get_ops(spand_tree* t, int* out);
+int spand_tree_get_op_matrix(spand_tree* t, int idx, double* out);
+int spand_tree_get_op_tau(spand_tree* t, int idx, double* out);
+/* seconds: partition, assemble, factorize */
+int spand_tree_timings(spand_tree* t, double* out);
+/* kernels launched by this tree since the last reset */
+int spand_tree_launches(spand_tree* t, long long* n, int reset);
+int spand_tree_device_bytes(spand_tree* t, long long* bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPAND_GB300_H */

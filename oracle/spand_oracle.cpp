@@ -1,0 +1,1588 @@
+// spaND CPU oracle -- TEST INFRASTRUCTURE ONLY.
+//
+// A plain C++ restatement of the reference hot path (leopoldcambier/spaND_public):
+// ordering (geometric modified nested dissection), assembly, the level loop of
+// Tree::factorize (eliminate / scale / sparsify / merge), the op-replay solve and the
+// CG / IR drivers.  Only the test-suite, smoke() and bench.py's CPU baseline legs may
+// load this library; the product path never does.
+//
+// Dense arithmetic: the reference calls OpenBLAS/MKL (dpotrf, dtrsm, dgemm, dsyrk,
+// dgeqp3, dormqr, dtrsv, dgemv, dgetrf).  Those libraries are not part of the
+// reference tree, so their published algorithms (LAPACK 3.x dpotf2, dgetf2, dlaqp2 with
+// the LAWN 176 partial-norm downdating safeguard, dlarfg/dlarf, reference BLAS loops)
+// are restated below.  They agree with LAPACK up to rounding; tests compare them with
+// scipy's LAPACK on random inputs.
+//
+// Structure is mirrored exactly (std::list edge lists, insertion and sort orders), since
+// edge order decides the column order of the sparsification matrix and therefore the
+// QRCP pivot sequence.
+//
+// Citations are path:line into the reference project.
+
+#include <algorithm>
+#include <array>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <limits>
+#include <list>
+#include <map>
+#include <memory>
+#include <numeric>
+#include <set>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace orc {
+
+// ---------------------------------------------------------------------------------
+// Dense column-major matrix
+// ---------------------------------------------------------------------------------
+struct Mat {
+    int r = 0, c = 0;
+    std::vector<double> v;
+    Mat() {}
+    Mat(int r_, int c_) : r(r_), c(c_), v((size_t)r_ * (size_t)c_, 0.0) {}
+    double& operator()(int i, int j) { return v[(size_t)i + (size_t)j * r]; }
+    double operator()(int i, int j) const { return v[(size_t)i + (size_t)j * r]; }
+    double* col(int j) { return v.data() + (size_t)j * r; }
+    const double* col(int j) const { return v.data() + (size_t)j * r; }
+    static Mat eye(int n) {
+        Mat I(n, n);
+        for (int i = 0; i < n; i++) I(i, i) = 1.0;
+        return I;
+    }
+};
+using pMat = std::unique_ptr<Mat>;
+
+static double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// ---------------------------------------------------------------------------------
+// Restated dense kernels (util.cpp:122-452 call sites)
+// ---------------------------------------------------------------------------------
+
+// Euclidean norm, scaled sum of squares (reference BLAS dnrm2).
+static double nrm2(int n, const double* x) {
+    if (n < 1) return 0.0;
+    if (n == 1) return std::fabs(x[0]);
+    double scale = 0.0, ssq = 1.0;
+    for (int i = 0; i < n; i++) {
+        if (x[i] != 0.0) {
+            double a = std::fabs(x[i]);
+            if (scale < a) {
+                ssq = 1.0 + ssq * (scale / a) * (scale / a);
+                scale = a;
+            } else {
+                ssq += (a / scale) * (a / scale);
+            }
+        }
+    }
+    return scale * std::sqrt(ssq);
+}
+
+// Lower Cholesky, A = L L^T in place (dpotrf 'L'); util.cpp:158-165.  Returns LAPACK info.
+static int potf(Mat& A) {
+    int n = A.r;
+    for (int j = 0; j < n; j++) {
+        double ajj = A(j, j);
+        if (!(ajj > 0.0) || std::isnan(ajj)) return j + 1;
+        ajj = std::sqrt(ajj);
+        A(j, j) = ajj;
+        double* cj = A.col(j);
+        for (int i = j + 1; i < n; i++) cj[i] /= ajj;
+        for (int k = j + 1; k < n; k++) {
+            double f = cj[k];
+            if (f == 0.0) continue;
+            double* ck = A.col(k);
+            for (int i = k; i < n; i++) ck[i] -= cj[i] * f;
+        }
+    }
+    return 0;
+}
+
+// B <- L^{-1} B, L lower non-unit (dtrsm Left Lower NoTrans); util.cpp:266-274.
+static void trsm_left_lower(const Mat& L, Mat& B) {
+    int m = B.r, n = B.c;
+    for (int j = 0; j < n; j++) {
+        double* b = B.col(j);
+        for (int k = 0; k < m; k++) {
+            if (b[k] == 0.0) continue;
+            b[k] /= L(k, k);
+            const double* lk = L.col(k);
+            double bk = b[k];
+            for (int i = k + 1; i < m; i++) b[i] -= bk * lk[i];
+        }
+    }
+}
+
+// B <- B L^{-T}, L lower non-unit (dtrsm Right Lower Trans); util.cpp:256-264.
+static void trsm_right_lower_trans(const Mat& L, Mat& B) {
+    int m = B.r, n = B.c;
+    for (int j = 0; j < n; j++) {
+        double* bj = B.col(j);
+        double d = 1.0 / L(j, j);
+        for (int i = 0; i < m; i++) bj[i] *= d;
+        for (int k = j + 1; k < n; k++) {
+            double f = L(k, j);
+            if (f == 0.0) continue;
+            double* bk = B.col(k);
+            for (int i = 0; i < m; i++) bk[i] -= bj[i] * f;
+        }
+    }
+}
+
+// B <- B U^{-1}, U upper non-unit (dtrsm Right Upper NoTrans).
+static void trsm_right_upper(const Mat& U, Mat& B) {
+    int m = B.r, n = B.c;
+    for (int j = 0; j < n; j++) {
+        double* bj = B.col(j);
+        for (int k = 0; k < j; k++) {
+            double f = U(k, j);
+            if (f == 0.0) continue;
+            const double* bk = B.col(k);
+            for (int i = 0; i < m; i++) bj[i] -= f * bk[i];
+        }
+        double d = 1.0 / U(j, j);
+        for (int i = 0; i < m; i++) bj[i] *= d;
+    }
+}
+
+// C <- C - op(A) op(B)  (dgemm alpha=-1, beta=1); util.cpp:122-138.
+static void gemm_sub(const Mat& A, bool tA, const Mat& B, bool tB, Mat& C) {
+    int m = C.r, n = C.c;
+    int k = tA ? A.r : A.c;
+    if (m == 0 || n == 0 || k == 0) return;
+    for (int j = 0; j < n; j++) {
+        double* cj = C.col(j);
+        if (!tA) {
+            for (int l = 0; l < k; l++) {
+                double b = tB ? B(j, l) : B(l, j);
+                if (b == 0.0) continue;
+                const double* al = A.col(l);
+                for (int i = 0; i < m; i++) cj[i] -= al[i] * b;
+            }
+        } else {
+            for (int i = 0; i < m; i++) {
+                const double* ai = A.col(i);
+                double s = 0.0;
+                if (!tB) {
+                    const double* bj = B.col(j);
+                    for (int l = 0; l < k; l++) s += ai[l] * bj[l];
+                } else {
+                    for (int l = 0; l < k; l++) s += ai[l] * B(j, l);
+                }
+                cj[i] -= s;
+            }
+        }
+    }
+}
+
+// lower(C) <- lower(C) - op(A) op(A)^T (dsyrk Lower, alpha=-1, beta=1); util.cpp:148-156.
+static void syrk_sub_lower(const Mat& A, bool tA, Mat& C) {
+    int n = C.r;
+    int k = tA ? A.r : A.c;
+    if (n == 0 || k == 0) return;
+    for (int j = 0; j < n; j++) {
+        double* cj = C.col(j);
+        if (!tA) {
+            for (int l = 0; l < k; l++) {
+                double b = A(j, l);
+                if (b == 0.0) continue;
+                const double* al = A.col(l);
+                for (int i = j; i < n; i++) cj[i] -= al[i] * b;
+            }
+        } else {
+            const double* aj = A.col(j);
+            for (int i = j; i < n; i++) {
+                const double* ai = A.col(i);
+                double s = 0.0;
+                for (int l = 0; l < k; l++) s += ai[l] * aj[l];
+                cj[i] -= s;
+            }
+        }
+    }
+}
+
+// x <- L^{-1} x or L^{-T} x (dtrsv Lower NonUnit); util.cpp:276-283.
+static void trsv_lower(const Mat& L, double* x, int n, bool trans) {
+    if (!trans) {
+        for (int k = 0; k < n; k++) {
+            x[k] /= L(k, k);
+            double xk = x[k];
+            const double* lk = L.col(k);
+            for (int i = k + 1; i < n; i++) x[i] -= xk * lk[i];
+        }
+    } else {
+        for (int k = n - 1; k >= 0; k--) {
+            const double* lk = L.col(k);
+            double s = x[k];
+            for (int i = k + 1; i < n; i++) s -= lk[i] * x[i];
+            x[k] = s / L(k, k);
+        }
+    }
+}
+
+// x <- U^{-1} x, U upper non-unit (dtrsv Upper NoTrans NonUnit).
+static void trsv_upper(const Mat& U, double* x, int n) {
+    for (int k = n - 1; k >= 0; k--) {
+        x[k] /= U(k, k);
+        double xk = x[k];
+        const double* uk = U.col(k);
+        for (int i = 0; i < k; i++) x[i] -= xk * uk[i];
+    }
+}
+
+// x2 <- x2 - A x1 (gemv_notrans, util.cpp:306-315) ; x2 <- x2 - A^T x1 (gemv_trans, util.cpp:317-326)
+static void gemv_sub(const Mat& A, bool trans, const double* x1, double* x2) {
+    int m = A.r, n = A.c;
+    if (m == 0 || n == 0) return;
+    if (!trans) {
+        for (int j = 0; j < n; j++) {
+            double xj = x1[j];
+            const double* aj = A.col(j);
+            for (int i = 0; i < m; i++) x2[i] -= aj[i] * xj;
+        }
+    } else {
+        for (int j = 0; j < n; j++) {
+            const double* aj = A.col(j);
+            double s = 0.0;
+            for (int i = 0; i < m; i++) s += aj[i] * x1[i];
+            x2[j] -= s;
+        }
+    }
+}
+
+// Householder reflector generation (LAPACK dlarfg).  alpha is updated to beta.
+static void larfg(int n, double& alpha, double* x, double& tau) {
+    if (n <= 1) { tau = 0.0; return; }
+    double xnorm = nrm2(n - 1, x);
+    if (xnorm == 0.0) { tau = 0.0; return; }
+    double beta = -std::copysign(std::hypot(alpha, xnorm), alpha);
+    const double safmin = std::numeric_limits<double>::min() / std::numeric_limits<double>::epsilon();
+    int knt = 0;
+    if (std::fabs(beta) < safmin) {
+        double rsafmn = 1.0 / safmin;
+        do {
+            knt++;
+            for (int i = 0; i < n - 1; i++) x[i] *= rsafmn;
+            beta *= rsafmn;
+            alpha *= rsafmn;
+        } while (std::fabs(beta) < safmin && knt < 20);
+        xnorm = nrm2(n - 1, x);
+        beta = -std::copysign(std::hypot(alpha, xnorm), alpha);
+    }
+    tau = (beta - alpha) / beta;
+    double scal = 1.0 / (alpha - beta);
+    for (int i = 0; i < n - 1; i++) x[i] *= scal;
+    for (int j = 0; j < knt; j++) beta *= safmin;
+    alpha = beta;
+}
+
+// Relative window inside which two partial column norms count as tied (see geqp3).
+static const double QRCP_TIE = 1e-7;
+
+// QR with column pivoting, A P = Q R (dgeqp3 -> dlaqp2); util.cpp:383-394.
+// jpvt is 0-based on output (util.cpp:392-393 decrements LAPACK's 1-based pivots).
+static void geqp3(Mat& A, std::vector<int>& jpvt, std::vector<double>& tau) {
+    int m = A.r, n = A.c;
+    jpvt.resize(n);
+    tau.assign(std::min(m, n), 0.0);
+    if (m == 0 || n == 0) return;
+    for (int j = 0; j < n; j++) jpvt[j] = j;
+    std::vector<double> vn1(n), vn2(n), work(n);
+    for (int j = 0; j < n; j++) { vn1[j] = nrm2(m, A.col(j)); vn2[j] = vn1[j]; }
+    const double tol3z = std::sqrt(std::numeric_limits<double>::epsilon());
+    int mn = std::min(m, n);
+    for (int i = 0; i < mn; i++) {
+        // pivot: first column whose partial norm is within QRCP_TIE of the largest.
+        // Plain idamax (first exact maximum) lets rounding noise decide between columns
+        // whose norms are equal in exact arithmetic (mirror-symmetric stencil columns),
+        // so any two implementations could pivot differently; the relative tie window
+        // makes the choice reproducible across summation orders.
+        double best = 0.0;
+        for (int j = i; j < n; j++) best = std::max(best, std::fabs(vn1[j]));
+        int pvt = i;
+        for (int j = i; j < n; j++)
+            if (std::fabs(vn1[j]) >= best * (1.0 - QRCP_TIE)) { pvt = j; break; }
+        if (pvt != i) {
+            std::swap_ranges(A.col(pvt), A.col(pvt) + m, A.col(i));
+            std::swap(jpvt[pvt], jpvt[i]);
+            vn1[pvt] = vn1[i];
+            vn2[pvt] = vn2[i];
+        }
+        double* ci = A.col(i);
+        if (i < m - 1) larfg(m - i, ci[i], ci + i + 1, tau[i]);
+        else larfg(1, ci[m - 1], ci + m - 1, tau[i]);
+        if (i < n - 1 && tau[i] != 0.0) {
+            // apply H(i)^T = H(i) to A(i:m, i+1:n) from the left (dlarf)
+            double aii = ci[i];
+            ci[i] = 1.0;
+            for (int j = i + 1; j < n; j++) {
+                double* cj = A.col(j);
+                double s = 0.0;
+                for (int r = i; r < m; r++) s += ci[r] * cj[r];
+                s *= tau[i];
+                for (int r = i; r < m; r++) cj[r] -= s * ci[r];
+            }
+            ci[i] = aii;
+        }
+        // partial column norm downdating (LAWN 176 safeguard)
+        for (int j = i + 1; j < n; j++) {
+            if (vn1[j] != 0.0) {
+                double temp = std::fabs(A(i, j)) / vn1[j];
+                temp = 1.0 - temp * temp;
+                temp = std::max(temp, 0.0);
+                double r = vn1[j] / vn2[j];
+                double temp2 = temp * r * r;
+                if (temp2 <= tol3z) {
+                    if (i < m - 1) {
+                        vn1[j] = nrm2(m - i - 1, A.col(j) + i + 1);
+                        vn2[j] = vn1[j];
+                    } else {
+                        vn1[j] = 0.0;
+                        vn2[j] = 0.0;
+                    }
+                } else {
+                    vn1[j] *= std::sqrt(temp);
+                }
+            }
+        }
+    }
+}
+
+// Apply Q (trans=false) or Q^T (trans=true) of k reflectors stored in v (m x >=k) to x
+// (dormqr Left, nrhs=1); util.cpp:328-351.
+static void ormqr_vec(const Mat& v, const std::vector<double>& h, int k, double* x, bool trans) {
+    int m = v.r;
+    if (m == 0 || k == 0) return;
+    auto apply = [&](int i) {
+        if (h[i] == 0.0) return;
+        const double* vi = v.col(i);
+        double s = x[i];
+        for (int r = i + 1; r < m; r++) s += vi[r] * x[r];
+        s *= h[i];
+        x[i] -= s;
+        for (int r = i + 1; r < m; r++) x[r] -= s * vi[r];
+    };
+    if (trans) for (int i = 0; i < k; i++) apply(i);
+    else for (int i = k - 1; i >= 0; i--) apply(i);
+}
+
+// Partial-pivot LU (dgetrf -> dgetf2); returns info; swap is 0-based; util.cpp:183-200.
+static int getf(Mat& A, std::vector<int>& perm) {
+    int n = A.r;
+    std::vector<int> swp(n);
+    int info = 0;
+    for (int j = 0; j < n; j++) {
+        int p = j;
+        double best = std::fabs(A(j, j));
+        for (int i = j + 1; i < n; i++)
+            if (std::fabs(A(i, j)) > best) { best = std::fabs(A(i, j)); p = i; }
+        swp[j] = p;
+        if (A(p, j) != 0.0) {
+            if (p != j)
+                for (int c = 0; c < n; c++) std::swap(A(j, c), A(p, c));
+            double d = 1.0 / A(j, j);
+            for (int i = j + 1; i < n; i++) A(i, j) *= d;
+        } else if (info == 0) {
+            info = j + 1;
+        }
+        for (int c = j + 1; c < n; c++) {
+            double f = A(j, c);
+            if (f == 0.0) continue;
+            for (int i = j + 1; i < n; i++) A(i, c) -= A(i, j) * f;
+        }
+    }
+    if (info != 0) return info;
+    // swap2perm (util.cpp:76-88)
+    perm.resize(n);
+    for (int i = 0; i < n; i++) perm[i] = i;
+    for (int i = 0; i < n; i++) std::swap(perm[swp[i]], perm[i]);
+    return 0;
+}
+
+// A = L (D + U') -> L |D|^1/2 and |D|^1/2 sign(D) (I + D^-1 U'); util.cpp:212-227.
+static void split_LU(const Mat& A, Mat& L, Mat& U) {
+    int n = A.r;
+    L = Mat(n, n);
+    U = Mat(n, n);
+    for (int j = 0; j < n; j++) {
+        double dj = A(j, j);
+        double sj = std::sqrt(std::fabs(dj));
+        for (int i = j + 1; i < n; i++) L(i, j) = A(i, j) * sj;
+        L(j, j) = sj;
+    }
+    for (int j = 0; j < n; j++) {
+        for (int i = 0; i < j; i++) {
+            double di = A(i, i);
+            double sgn = (di > 0) - (di < 0);
+            U(i, j) = sgn * std::sqrt(std::fabs(di)) * (A(i, j) / di);
+        }
+        double dj = A(j, j);
+        double sgn = (dj > 0) - (dj < 0);
+        U(j, j) = sgn * std::sqrt(std::fabs(dj));
+    }
+}
+
+// Rank from |R_ii| / |R_00| >= tol (prefix); util.cpp:434-452.
+static int choose_rank(const std::vector<double>& s, double tol) {
+    int n = (int)s.size();
+    if (tol == 0) return n;
+    if (tol >= 1.0) return 0;
+    if (n <= 1) return n;
+    double sref = std::fabs(s[0]);
+    int rank = 1;
+    while (rank < n && std::fabs(s[rank]) / sref >= tol) rank++;
+    return rank;
+}
+
+// ---------------------------------------------------------------------------------
+// Sparse matrix (CSC, sorted rows, no duplicates)
+// ---------------------------------------------------------------------------------
+struct CSC {
+    int n = 0;
+    std::vector<int> colptr, rowval;
+    std::vector<double> val;
+};
+
+// A[p,p]: App(i,j) = A(p[i], p[j]); util.cpp:519-546.
+static CSC symm_perm(const CSC& A, const std::vector<int>& p) {
+    int n = A.n;
+    std::vector<int> pinv(n);
+    for (int i = 0; i < n; i++) pinv[p[i]] = i;
+    std::vector<int> cnt(n + 1, 0);
+    for (int j = 0; j < n; j++) cnt[pinv[j] + 1] += A.colptr[j + 1] - A.colptr[j];
+    CSC B;
+    B.n = n;
+    B.colptr.assign(n + 1, 0);
+    for (int j = 0; j < n; j++) B.colptr[j + 1] = B.colptr[j] + cnt[j + 1];
+    B.rowval.resize(A.rowval.size());
+    B.val.resize(A.val.size());
+    std::vector<std::pair<int, double>> tmp;
+    for (int jn = 0; jn < n; jn++) {
+        int j = p[jn];
+        tmp.clear();
+        for (int k = A.colptr[j]; k < A.colptr[j + 1]; k++) tmp.push_back({pinv[A.rowval[k]], A.val[k]});
+        std::sort(tmp.begin(), tmp.end(), [](auto& a, auto& b) { return a.first < b.first; });
+        int o = B.colptr[jn];
+        for (size_t t = 0; t < tmp.size(); t++) { B.rowval[o + t] = tmp[t].first; B.val[o + t] = tmp[t].second; }
+    }
+    return B;
+}
+
+// ---------------------------------------------------------------------------------
+// Partitioning (partition.h:23-75, partition.cpp)
+// ---------------------------------------------------------------------------------
+struct SepID {
+    int lvl = -1, sep = 0;
+    SepID() {}
+    SepID(int l, int s) : lvl(l), sep(s) {}
+    bool operator==(const SepID& o) const { return lvl == o.lvl && sep == o.sep; }
+    bool operator<(const SepID& o) const { return lvl < o.lvl || (lvl == o.lvl && sep < o.sep); }
+};
+struct ClusterID {
+    SepID self, l, r;
+    ClusterID() {}
+    ClusterID(SepID s, SepID a, SepID b) : self(s), l(a), r(b) {}
+    bool operator==(const ClusterID& o) const { return self == o.self && l == o.l && r == o.r; }
+    bool operator<(const ClusterID& o) const {
+        return (self < o.self) || (self == o.self && l < o.l) || (self == o.self && l == o.l && r < o.r);
+    }
+};
+// partition.cpp:8-16
+static SepID merge_sep(const SepID& s) { return SepID(s.lvl + 1, s.sep / 2); }
+static ClusterID merge_if(const ClusterID& c, int lvl) {
+    SepID left = c.l.lvl < lvl ? merge_sep(c.l) : c.l;
+    SepID right = c.r.lvl < lvl ? merge_sep(c.r) : c.r;
+    return ClusterID(c.self, left, right);
+}
+
+// Geometric ND bisection with one-sided vertex separator; partition.cpp:139-210.
+// X is dim x N column-major (X[d + dim*i]).
+static void partition_nd_geo(const std::vector<int>& colptr, const std::vector<int>& rowval, const std::vector<int>& dofs,
+                             std::vector<int>& parts, const double* X, int dim, std::vector<int>& invp) {
+    int N = (int)dofs.size();
+    if (N == 0) return;
+    int bestdim = -1;
+    double maxrange = -1.0;
+    for (int d = 0; d < dim; d++) {
+        double maxi = std::numeric_limits<double>::lowest();
+        double mini = std::numeric_limits<double>::max();
+        for (int i = 0; i < N; i++) {
+            double x = X[d + (size_t)dim * dofs[i]];
+            maxi = std::max(maxi, x);
+            mini = std::min(mini, x);
+        }
+        double range = maxi - mini;
+        if (range > maxrange) { bestdim = d; maxrange = range; }
+    }
+    // the value at the median position of the sorted coordinates (ties do not matter)
+    std::vector<double> xs(N);
+    for (int i = 0; i < N; i++) xs[i] = X[bestdim + (size_t)dim * dofs[i]];
+    std::nth_element(xs.begin(), xs.begin() + N / 2, xs.end());
+    double midv = xs[N / 2];
+    for (int i = 0; i < N; i++) {
+        int dof = dofs[i];
+        invp[dof] = -1;
+        for (int k = colptr[dof]; k < colptr[dof + 1]; k++) invp[rowval[k]] = -1;
+    }
+    for (int i = 0; i < N; i++) {
+        int dof = dofs[i];
+        invp[dof] = i;
+        parts[i] = (X[bestdim + (size_t)dim * dof] < midv) ? 0 : 1;
+    }
+    for (int i = 0; i < N; i++) {
+        int dof = dofs[i];
+        if (parts[i] == 0) continue;
+        for (int k = colptr[dof]; k < colptr[dof + 1]; k++) {
+            int in = invp[rowval[k]];
+            if (in == -1) continue;
+            if (parts[in] == 0) { parts[i] = 2; break; }
+        }
+    }
+}
+
+// Modified nested dissection; partition.cpp:384-478 (geometric branch).
+static std::vector<ClusterID> partition_modifiedND(const CSC& A, int nlevels, const double* X, int dim) {
+    int N = A.n;
+    // SpMat2CSC: the graph without self loops (partition.cpp:21-39)
+    std::vector<int> colptr(N + 1, 0), rowval;
+    for (int i = 0; i < N; i++) {
+        colptr[i + 1] = colptr[i];
+        for (int k = A.colptr[i]; k < A.colptr[i + 1]; k++) {
+            int j = A.rowval[k];
+            if (i != j) { rowval.push_back(j); colptr[i + 1]++; }
+        }
+    }
+    std::vector<int> invp(N + 1), parttmp(N);
+    std::vector<std::vector<int>> doms(1, std::vector<int>(N));
+    std::iota(doms[0].begin(), doms[0].end(), 0);
+    std::vector<ClusterID> part(N, ClusterID(SepID(nlevels - 1, 0), SepID(nlevels - 1, 0), SepID(nlevels - 1, 0)));
+    for (int depth = 0; depth < nlevels - 1; depth++) {
+        int level = nlevels - depth - 1;
+        std::vector<std::vector<int>> newdoms((size_t)1 << (depth + 1));
+        for (int sep = 0; sep < (1 << depth); sep++) {
+            SepID idself(level, sep);
+            std::vector<int> dofssep = doms[sep];
+            std::sort(dofssep.begin(), dofssep.end());
+            partition_nd_geo(colptr, rowval, dofssep, parttmp, X, dim, invp);
+            SepID idleft(level - 1, 2 * sep), idright(level - 1, 2 * sep + 1);
+            for (size_t i = 0; i < dofssep.size(); i++) {
+                int j = dofssep[i];
+                if (part[j].self == idself) {
+                    if (parttmp[i] == 0) part[j].self = idleft;
+                    else if (parttmp[i] == 1) part[j].self = idright;
+                }
+                if (parttmp[i] == 0) {
+                    if (part[j].l == idself) part[j].l = idleft;
+                    if (part[j].r == idself) part[j].r = idleft;
+                } else if (parttmp[i] == 1) {
+                    if (part[j].l == idself) part[j].l = idright;
+                    if (part[j].r == idself) part[j].r = idright;
+                } else if (parttmp[i] == 2) {
+                    if (part[j].self == idself) { part[j].l = idleft; part[j].r = idright; }
+                }
+            }
+            std::vector<int> newleft, newright;
+            for (int i : dofssep) {
+                const ClusterID& c = part[i];
+                if (c.self == idleft || c.l == idleft || c.r == idleft) newleft.push_back(i);
+                if (c.self == idright || c.l == idright || c.r == idright) newright.push_back(i);
+            }
+            newdoms[2 * sep] = newleft;
+            newdoms[2 * sep + 1] = newright;
+        }
+        doms = newdoms;
+    }
+    return part;
+}
+
+// ---------------------------------------------------------------------------------
+// Cluster / Edge (cluster.h:16-116, edge.h:32-44, cluster.cpp, edge.cpp)
+// ---------------------------------------------------------------------------------
+struct Cluster;
+struct Edge {
+    Cluster* n1;
+    Cluster* n2;
+    pMat A;  // rows n2->size, cols n1->size
+    bool original;
+};
+using pEdge = std::unique_ptr<Edge>;
+
+struct Cluster {
+    int start, size, level, order;
+    bool eliminated = false, sparsify;
+    Cluster* parent = nullptr;
+    std::vector<Cluster*> children;
+    std::list<pEdge> edgesOut;   // pivot first
+    std::list<Edge*> edgesIn;
+    std::vector<double> x;       // x_ ; original_size() == x.size()
+    Cluster(int st, int sz, int lv, int ord, bool sp) : start(st), size(sz), level(lv), order(ord), sparsify(sp) {
+        reset_size(sz);
+    }
+    void reset_size(int s) { size = s; x.assign(s, 0.0); }
+    int original_size() const { return (int)x.size(); }
+    Edge* pivot() { return edgesOut.begin()->get(); }
+    // cluster.cpp:113-123
+    void add_edge(pEdge e) {
+        if (e->n1 == e->n2) {
+            edgesOut.push_front(std::move(e));
+        } else {
+            e->n2->edgesIn.push_back(e.get());
+            edgesOut.push_back(std::move(e));
+        }
+    }
+    // cluster.cpp:161-176 (std::list::sort is stable)
+    void sort_edges() {
+        edgesOut.sort([](const pEdge& a, const pEdge& b) {
+            if (a->n1 == a->n2) return true;
+            if (b->n1 == b->n2) return false;
+            return a->n2->order < b->n2->order;
+        });
+        edgesIn.sort([](const Edge* a, const Edge* b) { return a->n1->order < b->n1->order; });
+    }
+    // cluster.cpp:32-45
+    void set_eliminated() {
+        for (auto& e : edgesOut) {
+            Cluster* me = this;
+            e->n2->edgesIn.remove_if([me](Edge* e2) { return e2->n1 == me; });
+        }
+        for (auto e : edgesIn) {
+            Cluster* me = this;
+            e->n1->edgesOut.remove_if([me](const pEdge& e2) { return e2->n2 == me; });
+        }
+        edgesIn.clear();
+        edgesOut.clear();
+        eliminated = true;
+    }
+    std::vector<Edge*> out_nbr() {
+        std::vector<Edge*> r;
+        auto it = edgesOut.begin();
+        if (it != edgesOut.end()) ++it;
+        for (; it != edgesOut.end(); ++it) r.push_back(it->get());
+        return r;
+    }
+    std::vector<Edge*> out_all() {
+        std::vector<Edge*> r;
+        for (auto& e : edgesOut) r.push_back(e.get());
+        return r;
+    }
+    std::vector<Edge*> in_nbr() { return std::vector<Edge*>(edgesIn.begin(), edgesIn.end()); }
+};
+using pCluster = std::unique_ptr<Cluster>;
+
+// ---------------------------------------------------------------------------------
+// Operations (operations.h:32-163, operations.cpp)
+// ---------------------------------------------------------------------------------
+enum OpKind {
+    OP_SCALING_LLT = 0,
+    OP_GEMM_SYMM_OUT = 1,
+    OP_GEMM_SYMM_IN = 2,
+    OP_ORTHOGONAL = 3,
+    OP_MERGE = 4,
+    OP_SPLIT = 5,
+    OP_GEMM_OUT = 6,
+    OP_GEMM_IN = 7,
+    OP_SCALING_PLUQ = 8,
+};
+
+struct Op {
+    OpKind kind;
+    Cluster* self = nullptr;
+    Cluster* nbr = nullptr;
+    int ns = 0, nn = 0;          // Segment lengths captured at construction (head_x())
+    pMat A;                      // LLT, Gemm block, v (Orthogonal), L (PLUQ)
+    pMat U;                      // PLUQ
+    std::vector<double> h;       // Orthogonal
+    std::vector<int> p, q;       // PLUQ
+    int ilvl = 0;                // level at which the op was recorded
+
+    long long nnz() const {
+        switch (kind) {
+            case OP_SCALING_LLT: return (long long)ns * (ns + 1) / 2;
+            case OP_GEMM_SYMM_OUT: case OP_GEMM_SYMM_IN: case OP_GEMM_OUT: case OP_GEMM_IN:
+                return (long long)ns * nn;
+            case OP_ORTHOGONAL: return (long long)ns * ns;
+            case OP_SCALING_PLUQ: return (long long)ns * ns + 2LL * ns;
+            default: return 0;
+        }
+    }
+    void fwd() {
+        double* xs = self ? self->x.data() : nullptr;
+        switch (kind) {
+            case OP_SCALING_LLT: trsv_lower(*A, xs, ns, false); break;
+            case OP_GEMM_SYMM_OUT: case OP_GEMM_OUT:
+                if (nn > 0 && ns > 0) gemv_sub(*A, false, xs, nbr->x.data());
+                break;
+            case OP_GEMM_SYMM_IN:
+                if (nn > 0 && ns > 0) gemv_sub(*A, true, xs, nbr->x.data());
+                break;
+            case OP_GEMM_IN: break;
+            case OP_ORTHOGONAL: ormqr_vec(*A, h, A->c, xs, true); break;
+            case OP_MERGE: {
+                int k = 0;
+                for (auto c : self->children)
+                    for (int i = 0; i < c->size; i++) self->x[k++] = c->x[i];
+                break;
+            }
+            case OP_SPLIT: {
+                Cluster* sib = nbr;
+                for (int i = 0; i < sib->size; i++) sib->x[i] = self->x[self->size + i];
+                break;
+            }
+            case OP_SCALING_PLUQ: {
+                std::vector<double> t(ns);
+                for (int i = 0; i < ns; i++) t[i] = xs[p[i]];
+                std::copy(t.begin(), t.end(), xs);
+                trsv_lower(*A, xs, ns, false);
+                break;
+            }
+        }
+    }
+    void bwd() {
+        double* xs = self ? self->x.data() : nullptr;
+        switch (kind) {
+            case OP_SCALING_LLT: trsv_lower(*A, xs, ns, true); break;
+            case OP_GEMM_SYMM_OUT:
+                if (nn > 0 && ns > 0) gemv_sub(*A, true, nbr->x.data(), xs);
+                break;
+            case OP_GEMM_SYMM_IN: case OP_GEMM_IN:
+                if (nn > 0 && ns > 0) gemv_sub(*A, false, nbr->x.data(), xs);
+                break;
+            case OP_GEMM_OUT: break;
+            case OP_ORTHOGONAL: ormqr_vec(*A, h, A->c, xs, false); break;
+            case OP_MERGE: {
+                int k = 0;
+                for (auto c : self->children)
+                    for (int i = 0; i < c->size; i++) c->x[i] = self->x[k++];
+                break;
+            }
+            case OP_SPLIT: {
+                Cluster* sib = nbr;
+                for (int i = 0; i < sib->size; i++) self->x[self->size + i] = sib->x[i];
+                break;
+            }
+            case OP_SCALING_PLUQ: {
+                trsv_upper(*U, xs, ns);
+                std::vector<double> t(ns);
+                for (int i = 0; i < ns; i++) t[i] = xs[q[i]];
+                std::copy(t.begin(), t.end(), xs);
+                break;
+            }
+        }
+    }
+};
+using pOp = std::unique_ptr<Op>;
+
+// ---------------------------------------------------------------------------------
+// Per-level log and flop log (util.h:262-401)
+// ---------------------------------------------------------------------------------
+struct IStats {
+    long long sum = 0;
+    int count = 0, mn = INT32_MAX, mx = INT32_MIN;
+    void add(int v) { sum += v; count++; mn = std::min(mn, v); mx = std::max(mx, v); }
+};
+struct LevelLog {
+    int dofs_nd = 0, dofs_left_nd = 0, dofs_left_elim = 0, dofs_left_spars = 0;
+    long long fact_nnz = 0;
+    IStats rank_before, rank_after, nbrs;
+    int ignored = 0;
+    double t_elim = 0, t_scale = 0, t_spars = 0, t_merge = 0;
+    double flops_potf = 0, flops_trsm = 0, flops_gemm = 0, flops_geqp3 = 0;
+};
+
+enum SymmKind { SPD = 0, SYM = 1, GEN = 2 };
+enum ScalingKind { S_LLT = 0, S_PLU = 3, S_PLUQ = 4, S_LDLT = 5 };
+
+// ---------------------------------------------------------------------------------
+// Tree (tree.h, tree.cpp)
+// ---------------------------------------------------------------------------------
+struct Tree {
+    bool verb = false;
+    bool geo = false;
+    int ilvl = 0;
+    int nlevels;
+    double tol = 10.0;       // tree.cpp:94
+    int skip = 0;
+    int symm = SPD;
+    int scale_kind = S_LLT;
+    bool use_want_sparsify = true;
+    const double* X = nullptr;
+    int dim = 0;
+    int max_order = 0;
+    std::vector<int> perm;
+    std::list<pOp> ops;
+    int current_bottom = 0;
+    std::vector<std::list<pCluster>> bottoms;
+    std::vector<pCluster> others;
+    std::vector<LevelLog> log;
+    std::vector<ClusterID> part;  // natural ordering
+    double t_partition = 0, t_assemble = 0, t_factorize = 0;
+    // ranks for parity: (level, cluster order, rows, rank) of every sparsified cluster
+    std::vector<std::array<int, 4>> rank_log;
+
+    explicit Tree(int nl) : nlevels(nl), bottoms(nl), log(nl) {}
+    bool symmetry() const { return symm == SPD || symm == SYM; }
+    int get_new_order() { return max_order++; }
+    std::list<pCluster>& bottom_current() { return bottoms[current_bottom]; }
+    std::list<pCluster>& bottom_original() { return bottoms[0]; }
+    int N() const { return (int)perm.size(); }
+
+    int ndofs_left() {
+        int n = 0;
+        for (auto& s : bottom_current())
+            if (!s->eliminated) n += s->size;
+        return n;
+    }
+    int nclusters_left() {
+        int n = 0;
+        for (auto& s : bottom_current())
+            if (!s->eliminated) n++;
+        return n;
+    }
+    long long nnz() const {
+        long long n = 0;
+        for (auto& op : ops) n += op->nnz();
+        return n;
+    }
+    int get_stop() const {  // tree.cpp:158-169
+        int stop = (int)perm.size();
+        for (auto& l : log) {
+            if (l.dofs_left_elim > 0) stop = std::min(stop, l.dofs_left_elim);
+            if (l.dofs_left_spars > 0) stop = std::min(stop, l.dofs_left_spars);
+        }
+        return stop;
+    }
+
+    // tree.cpp:306-419
+    void partition(const CSC& A) {
+        double t0 = now_s();
+        int N = A.n;
+        if (geo) {
+            part = partition_modifiedND(A, nlevels, X, dim);
+        } else {
+            throw std::runtime_error("oracle: algebraic (METIS) ordering is not restated; set geometry");
+        }
+        for (int i = 0; i < N; i++) log[part[i].self.lvl].dofs_nd += 1;
+        log[nlevels - 1].dofs_left_nd = 0;
+        for (int l = nlevels - 2; l >= 0; l--) log[l].dofs_left_nd = log[l + 1].dofs_nd + log[l + 1].dofs_left_nd;
+        perm.resize(N);
+        std::iota(perm.begin(), perm.end(), 0);
+        std::vector<ClusterID> pm = part;
+        auto cmp = [&pm](int i, int j) { return pm[i] < pm[j]; };
+        std::stable_sort(perm.begin(), perm.end(), cmp);
+        for (int lvl = 1; lvl < nlevels; lvl++) {
+            for (auto& c : pm) c = merge_if(c, lvl);
+            std::stable_sort(perm.begin(), perm.end(), cmp);
+        }
+        std::map<Cluster*, ClusterID> ids;
+        for (int k = 0; k < N;) {
+            int knext = k + 1;
+            ClusterID id = part[perm[k]];
+            while (knext < N && part[perm[knext]] == id) knext++;
+            auto self = std::make_unique<Cluster>(k, knext - k, id.self.lvl, get_new_order(), id.l.lvl == 0 && id.r.lvl == 0);
+            ids[self.get()] = id;
+            bottoms[0].push_back(std::move(self));
+            k = knext;
+        }
+        for (int lvl = 1; lvl < nlevels; lvl++) {
+            auto begin = std::find_if(bottoms[lvl - 1].begin(), bottoms[lvl - 1].end(),
+                                      [lvl](const pCluster& s) { return s->level >= lvl; });
+            auto end = bottoms[lvl - 1].end();
+            std::map<Cluster*, ClusterID> pids;
+            for (auto it = begin; it != end; ++it) pids[it->get()] = merge_if(ids.at(it->get()), lvl);
+            for (auto k = begin; k != end;) {
+                ClusterID idp = pids.at(k->get());
+                std::vector<Cluster*> ch;
+                ch.push_back(k->get());
+                int cstart = (*k)->start, csize = (*k)->size;
+                ++k;
+                while (k != end && idp == pids.at(k->get())) {
+                    ch.push_back(k->get());
+                    csize += (*k)->size;
+                    ++k;
+                }
+                auto parent = std::make_unique<Cluster>(cstart, csize, idp.self.lvl, get_new_order(),
+                                                        idp.l.lvl == lvl && idp.r.lvl == lvl);
+                for (auto c : ch) { c->parent = parent.get(); parent->children.push_back(c); }
+                ids[parent.get()] = idp;
+                bottoms[lvl].push_back(std::move(parent));
+            }
+        }
+        t_partition = now_s() - t0;
+    }
+
+    // tree.cpp:505-575
+    void assemble(const CSC& A) {
+        double t0 = now_s();
+        int N = this->N();
+        CSC App = symm_perm(A, perm);
+        std::vector<Cluster*> cmap(N);
+        for (auto& s : bottom_original())
+            for (int k = s->start; k < s->start + s->size; k++) cmap[k] = s.get();
+        for (auto& sp : bottom_original()) {
+            Cluster* self = sp.get();
+            std::set<int> nbr_orders;
+            std::map<int, Cluster*> by_order;
+            for (int j = self->start; j < self->start + self->size; j++) {
+                for (int k = App.colptr[j]; k < App.colptr[j + 1]; k++) {
+                    int row = App.rowval[k];
+                    if (symmetry() && row < j) continue;
+                    Cluster* n = cmap[row];
+                    nbr_orders.insert(n->order);
+                    by_order[n->order] = n;
+                }
+            }
+            nbr_orders.insert(self->order);
+            by_order[self->order] = self;
+            for (int o : nbr_orders) {
+                Cluster* nbr = by_order[o];
+                auto M = std::make_unique<Mat>(nbr->size, self->size);
+                // block2dense (util.cpp:454-486)
+                for (int col = 0; col < self->size; col++) {
+                    int j = self->start + col;
+                    for (int k = App.colptr[j]; k < App.colptr[j + 1]; k++) {
+                        int row = App.rowval[k];
+                        if (row >= nbr->start && row < nbr->start + nbr->size) (*M)(row - nbr->start, col) = App.val[k];
+                    }
+                }
+                self->add_edge(std::make_unique<Edge>(Edge{self, nbr, std::move(M), true}));
+            }
+            self->sort_edges();
+        }
+        t_assemble = now_s() - t0;
+    }
+
+    // ---- elimination kernels ----------------------------------------------------
+    void potf_cluster(Cluster* self) {  // tree.cpp:582-593
+        Mat* Ass = self->pivot()->A.get();
+        int info = potf(*Ass);
+        if (info != 0) throw std::runtime_error("Error: Non-SPD Pivot");
+        double n = Ass->r;
+        log[ilvl].flops_potf += n * n * n / 3.0;
+    }
+    void getf_cluster(Cluster* self, pMat& L, pMat& U, std::vector<int>& p, std::vector<int>& q) {  // tree.cpp:614-635
+        Mat* Ass = self->pivot()->A.get();
+        if (scale_kind == S_PLUQ) throw std::runtime_error("oracle: PLUQ (full pivoting) is not restated");
+        int info = getf(*Ass, p);
+        if (info != 0) throw std::runtime_error("Error: Singular Pivot");
+        q.resize(self->size);
+        std::iota(q.begin(), q.end(), 0);
+        L = std::make_unique<Mat>();
+        U = std::make_unique<Mat>();
+        split_LU(*Ass, *L, *U);
+        double n = Ass->r;
+        log[ilvl].flops_potf += 2.0 * n * n * n / 3.0;
+    }
+    void panel_potf(Cluster* self) {  // tree.cpp:717-724, 640-663
+        Mat& L = *self->pivot()->A;
+        for (auto e : self->in_nbr()) {
+            trsm_left_lower(L, *e->A);
+            log[ilvl].flops_trsm += (double)e->A->c * e->A->r * e->A->r;
+        }
+        for (auto e : self->out_nbr()) {
+            trsm_right_lower_trans(L, *e->A);
+            log[ilvl].flops_trsm += (double)e->A->r * e->A->c * e->A->c;
+        }
+    }
+    void panel_getf(Cluster* self, Mat& L, Mat& U, std::vector<int>& p) {  // tree.cpp:668-689, 735-742
+        for (auto e : self->in_nbr()) {
+            Mat& Asn = *e->A;
+            Mat T(Asn.r, Asn.c);
+            for (int j = 0; j < Asn.c; j++)
+                for (int i = 0; i < Asn.r; i++) T(i, j) = Asn(p[i], j);
+            Asn = std::move(T);
+            trsm_left_lower(L, Asn);
+            log[ilvl].flops_trsm += (double)Asn.c * Asn.r * Asn.r;
+        }
+        for (auto e : self->out_nbr()) {
+            // q is the identity for PLU
+            trsm_right_upper(U, *e->A);
+            log[ilvl].flops_trsm += (double)e->A->r * e->A->c * e->A->c;
+        }
+    }
+    // tree.cpp:748-793
+    void gemm_edges(Edge* e1, Edge* e2, bool t1, bool t2) {
+        Cluster* s = t1 ? e1->n2 : e1->n1;
+        Cluster* n1 = t1 ? e1->n1 : e1->n2;
+        Cluster* n2 = t2 ? e2->n2 : e2->n1;
+        Edge* found = nullptr;
+        for (auto& e : n2->edgesOut)
+            if (e->n2 == n1) { found = e.get(); break; }
+        if (!found) {
+            n2->add_edge(std::make_unique<Edge>(Edge{n2, n1, std::make_unique<Mat>(n1->size, n2->size), false}));
+            for (auto& e : n2->edgesOut)
+                if (e->n2 == n1) { found = e.get(); break; }
+        }
+        Mat& C = *found->A;
+        if (n1 == n2 && symmetry()) {
+            syrk_sub_lower(*e1->A, t1, C);
+            log[ilvl].flops_gemm += (double)C.r * C.r * s->size;
+        } else {
+            gemm_sub(*e1->A, t1, *e2->A, t2, C);
+            log[ilvl].flops_gemm += 2.0 * C.r * C.c * s->size;
+        }
+    }
+    void schur_symmetric(Cluster* self) {  // tree.cpp:862-883
+        auto outs = self->out_nbr();
+        auto ins = self->in_nbr();
+        for (auto e1 : outs)
+            for (auto e2 : outs)
+                if (e1->n2->order >= e2->n2->order) gemm_edges(e1, e2, false, true);
+        for (auto e1 : ins)
+            for (auto e2 : ins)
+                if (e1->n1->order >= e2->n1->order) gemm_edges(e1, e2, true, false);
+        for (auto e1 : outs)
+            for (auto e2 : ins) gemm_edges(e1, e2, false, false);
+    }
+    void push_op(pOp op) { op->ilvl = ilvl; ops.push_back(std::move(op)); }
+    pOp make_op(OpKind k, Cluster* self, Cluster* nbr, pMat A) {
+        auto op = std::make_unique<Op>();
+        op->kind = k;
+        op->self = self;
+        op->nbr = nbr;
+        op->ns = self ? self->size : 0;
+        op->nn = nbr ? nbr->size : 0;
+        op->A = std::move(A);
+        return op;
+    }
+    // tree.cpp:895-967
+    void eliminate_cluster(Cluster* self) {
+        if (scale_kind == S_LLT) {
+            potf_cluster(self);
+            panel_potf(self);
+            schur_symmetric(self);
+            push_op(make_op(OP_SCALING_LLT, self, nullptr, std::move(self->pivot()->A)));
+            for (auto e : self->out_nbr()) push_op(make_op(OP_GEMM_SYMM_OUT, self, e->n2, std::move(e->A)));
+            for (auto e : self->in_nbr()) push_op(make_op(OP_GEMM_SYMM_IN, self, e->n1, std::move(e->A)));
+        } else if (scale_kind == S_PLU || scale_kind == S_PLUQ) {
+            pMat L, U;
+            std::vector<int> p, q;
+            getf_cluster(self, L, U, p, q);
+            panel_getf(self, *L, *U, p);
+            for (auto e1 : self->out_nbr())
+                for (auto e2 : self->in_nbr()) gemm_edges(e1, e2, false, false);
+            auto op = make_op(OP_SCALING_PLUQ, self, nullptr, std::move(L));
+            op->U = std::move(U);
+            op->p = p;
+            op->q = q;
+            push_op(std::move(op));
+            for (auto e : self->out_nbr()) push_op(make_op(OP_GEMM_OUT, self, e->n2, std::move(e->A)));
+            for (auto e : self->in_nbr()) push_op(make_op(OP_GEMM_IN, self, e->n1, std::move(e->A)));
+        } else {
+            throw std::runtime_error("oracle: scaling kind not restated");
+        }
+        self->set_eliminated();
+    }
+    // tree.cpp:796-856
+    void scale_cluster(Cluster* self) {
+        if (scale_kind == S_LLT) {
+            potf_cluster(self);
+            panel_potf(self);
+            push_op(make_op(OP_SCALING_LLT, self, nullptr, std::move(self->pivot()->A)));
+        } else {
+            pMat L, U;
+            std::vector<int> p, q;
+            getf_cluster(self, L, U, p, q);
+            panel_getf(self, *L, *U, p);
+            auto op = make_op(OP_SCALING_PLUQ, self, nullptr, std::move(L));
+            op->U = std::move(U);
+            op->p = p;
+            op->q = q;
+            push_op(std::move(op));
+        }
+        self->pivot()->A = std::make_unique<Mat>(Mat::eye(self->size));
+    }
+
+    // ---- sparsification ---------------------------------------------------------
+    // tree.cpp:1189-1224 (pred == true)
+    pMat assemble_Asn(Cluster* self) {
+        int rows = self->size, cols = 0;
+        auto ins = self->in_nbr();
+        auto outs = self->out_nbr();
+        for (auto e : ins) cols += e->n1->size;
+        for (auto e : outs) cols += e->n2->size;
+        auto Asn = std::make_unique<Mat>(rows, cols);
+        int c = 0;
+        for (auto e : ins) {
+            for (int j = 0; j < e->n1->size; j++)
+                for (int i = 0; i < rows; i++) (*Asn)(i, c + j) = (*e->A)(i, j);
+            c += e->n1->size;
+        }
+        for (auto e : outs) {
+            for (int j = 0; j < e->n2->size; j++)
+                for (int i = 0; i < rows; i++) (*Asn)(i, c + j) = (*e->A)(j, i);
+            c += e->n2->size;
+        }
+        log[ilvl].nbrs.add(cols);
+        return Asn;
+    }
+    // tree.cpp:980-1104 (pred == true branch, is_pivot_I == true)
+    Cluster* shrink_split(Cluster* original, int osize, Mat& AsnP) {
+        int sib_size = original->size - osize;
+        auto psib = std::make_unique<Cluster>(original->start + osize, sib_size, original->level, get_new_order(),
+                                              original->sparsify);
+        Cluster* sib = psib.get();
+        original->size = osize;  // set_size keeps x
+        int col = 0;
+        for (auto e : original->in_nbr()) {
+            int cols = e->n1->size;
+            auto M = std::make_unique<Mat>(osize, cols);
+            for (int j = 0; j < cols; j++)
+                for (int i = 0; i < osize; i++) (*M)(i, j) = AsnP(i, col + j);
+            e->A = std::move(M);
+            col += cols;
+        }
+        for (auto e : original->out_nbr()) {
+            int cols = e->n2->size;
+            auto M = std::make_unique<Mat>(cols, osize);
+            for (int j = 0; j < cols; j++)
+                for (int i = 0; i < osize; i++) (*M)(j, i) = AsnP(i, col + j);
+            e->A = std::move(M);
+            col += cols;
+        }
+        // pivot is identity: Aoo = I_osize, Ass = I_sib
+        sib->add_edge(std::make_unique<Edge>(Edge{sib, sib, std::make_unique<Mat>(Mat::eye(sib_size)), true}));
+        original->pivot()->A = std::make_unique<Mat>(Mat::eye(osize));
+        others.push_back(std::move(psib));
+        push_op(make_op(OP_SPLIT, original, sib, nullptr));
+        return sib;
+    }
+    // tree.cpp:1292-1347
+    void sparsify_adaptive_only(Cluster* self) {
+        auto Asn = assemble_Asn(self);
+        int rows = Asn->r, cols = Asn->c;
+        std::vector<int> jpvt;
+        std::vector<double> ht;
+        geqp3(*Asn, jpvt, ht);
+        std::vector<double> diag(std::min(rows, cols));
+        for (size_t i = 0; i < diag.size(); i++) diag[i] = (*Asn)((int)i, (int)i);
+        int rank = choose_rank(diag, tol);
+        rank_log.push_back({ilvl, self->order, rows, rank});
+        {
+            double m = rows, n = cols, k = std::min(rank, (int)diag.size());
+            log[ilvl].flops_geqp3 += 4.0 * m * n * k - 2.0 * k * k * (m + n) + 4.0 * k * k * k / 3.0;
+        }
+        if (rank >= rows) return;
+        auto v = std::make_unique<Mat>(rows, rank);
+        for (int j = 0; j < rank; j++)
+            for (int i = 0; i < rows; i++) (*v)(i, j) = (*Asn)(i, j);
+        auto op = make_op(OP_ORTHOGONAL, self, nullptr, std::move(v));
+        op->h.assign(ht.begin(), ht.begin() + rank);
+        push_op(std::move(op));
+        // AsnP = triu(R[:rank,:]) P^T : column jpvt[j] of AsnP is column j of triu(R)
+        Mat AsnP(rank, cols);
+        for (int j = 0; j < cols; j++)
+            for (int i = 0; i < rank && i <= j; i++) AsnP(i, jpvt[j]) = (*Asn)(i, j);
+        Cluster* sib = shrink_split(self, rank, AsnP);
+        eliminate_cluster(sib);
+    }
+    void sparsify_cluster(Cluster* self) {  // tree.cpp:1417-1433
+        if (!use_want_sparsify || self->sparsify) {
+            log[ilvl].rank_before.add(self->size);
+            sparsify_adaptive_only(self);
+            log[ilvl].rank_after.add(self->size);
+        } else {
+            log[ilvl].ignored++;
+        }
+    }
+
+    // ---- merge ------------------------------------------------------------------
+    // tree.cpp:1106-1131
+    void reset_size(Cluster* snew, std::map<Cluster*, int>& posparent) {
+        int size = 0;
+        for (auto sold : snew->children) { posparent[sold] = size; size += sold->size; }
+        snew->reset_size(size);
+        push_op(make_op(OP_MERGE, snew, nullptr, nullptr));
+    }
+    // tree.cpp:1133-1184
+    void update_edges(Cluster* snew, std::map<Cluster*, int>& posparent) {
+        std::map<int, std::pair<Cluster*, bool>> merged;  // keyed by order: iteration order only affects list order pre-sort
+        for (auto sold : snew->children)
+            for (auto& eold : sold->edgesOut) {
+                Cluster* nnew = eold->n2->parent;
+                auto it = merged.find(nnew->order);
+                if (it == merged.end()) merged[nnew->order] = {nnew, eold->original};
+                else if (!it->second.second) it->second.second = eold->original;
+            }
+        for (auto& kv : merged) {
+            Cluster* nnew = kv.second.first;
+            snew->add_edge(std::make_unique<Edge>(Edge{snew, nnew, std::make_unique<Mat>(nnew->size, snew->size), kv.second.second}));
+        }
+        snew->sort_edges();
+        for (auto sold : snew->children) {
+            for (auto& eold : sold->edgesOut) {
+                Cluster* nold = eold->n2;
+                Cluster* nnew = nold->parent;
+                Edge* found = nullptr;
+                for (auto& e : snew->edgesOut)
+                    if (e->n2 == nnew) { found = e.get(); break; }
+                int r0 = posparent[nold], c0 = posparent[sold];
+                Mat& D = *found->A;
+                Mat& S = *eold->A;
+                for (int j = 0; j < S.c; j++)
+                    for (int i = 0; i < S.r; i++) D(r0 + i, c0 + j) = S(i, j);
+            }
+            sold->edgesOut.clear();
+            sold->edgesIn.clear();
+        }
+    }
+    void merge_all() {  // tree.cpp:1435-1445
+        current_bottom++;
+        std::map<Cluster*, int> posparent;
+        for (auto& s : bottom_current()) reset_size(s.get(), posparent);
+        for (auto& s : bottom_current()) update_edges(s.get(), posparent);
+    }
+
+    // tree.cpp:1447-1551
+    void factorize() {
+        double t0 = now_s();
+        for (ilvl = 0; ilvl < nlevels; ilvl++) {
+            double ta = now_s();
+            {
+                std::vector<Cluster*> elim;
+                for (auto& s : bottom_current())
+                    if (s->level == ilvl) elim.push_back(s.get());
+                for (auto s : elim) eliminate_cluster(s);
+                log[ilvl].dofs_left_elim = ndofs_left();
+            }
+            double tb = now_s();
+            log[ilvl].t_elim = tb - ta;
+            if (ilvl >= skip) {
+                for (auto& s : bottom_current())
+                    if (s->level > ilvl) scale_cluster(s.get());
+                double tc = now_s();
+                log[ilvl].t_scale = tc - tb;
+                std::vector<Cluster*> sp;
+                for (auto& s : bottom_current())
+                    if (s->level > ilvl) sp.push_back(s.get());
+                for (auto s : sp) sparsify_cluster(s);
+                log[ilvl].t_spars = now_s() - tc;
+            }
+            double td = now_s();
+            if (ilvl < nlevels - 1) merge_all();
+            log[ilvl].t_merge = now_s() - td;
+            log[ilvl].dofs_left_spars = ndofs_left();
+            log[ilvl].fact_nnz = nnz();
+        }
+        t_factorize = now_s() - t0;
+    }
+
+    // tree.cpp:1610-1635
+    void solve(double* xnat) {
+        int n = N();
+        std::vector<double> b(n);
+        for (int i = 0; i < n; i++) b[i] = xnat[perm[i]];
+        for (auto& c : bottom_original()) {
+            if (c->children.empty()) std::copy(b.begin() + c->start, b.begin() + c->start + c->x.size(), c->x.begin());
+            else std::fill(c->x.begin(), c->x.end(), 0.0);
+        }
+        for (auto& op : ops) op->fwd();
+        for (auto it = ops.rbegin(); it != ops.rend(); ++it) (*it)->bwd();
+        for (auto& c : bottom_original())
+            if (c->children.empty()) std::copy(c->x.begin(), c->x.end(), b.begin() + c->start);
+        for (int i = 0; i < n; i++) xnat[perm[i]] = b[i];
+    }
+
+    // Current trailing matrix in permuted ordering as dense-coordinate triplets; tree.cpp:1730-1763
+    void trailing(std::vector<int>& I, std::vector<int>& J, std::vector<double>& V) {
+        for (auto& s : bottom_current()) {
+            if (s->eliminated) continue;
+            for (auto& e : s->edgesOut) {
+                int n1 = e->n2->start, n2 = e->n2->size, s1 = s->start, s2 = s->size;
+                for (int i_ = 0; i_ < n2; i_++)
+                    for (int j_ = 0; j_ < s2; j_++) {
+                        int i = n1 + i_, j = s1 + j_;
+                        double v = (*e->A)(i_, j_);
+                        if (symmetry() && i > j) { I.push_back(j); J.push_back(i); V.push_back(v); I.push_back(i); J.push_back(j); V.push_back(v); }
+                        else if (symmetry() && i == j) { I.push_back(i); J.push_back(i); V.push_back(v); }
+                        else if (!symmetry()) { I.push_back(i); J.push_back(j); V.push_back(v); }
+                    }
+            }
+        }
+    }
+};
+
+// y = A x (CSC, column traversal as in Eigen's sparse * dense)
+static void spmv(const CSC& A, const double* x, double* y) {
+    std::fill(y, y + A.n, 0.0);
+    for (int j = 0; j < A.n; j++) {
+        double xj = x[j];
+        for (int k = A.colptr[j]; k < A.colptr[j + 1]; k++) y[A.rowval[k]] += A.val[k] * xj;
+    }
+}
+static double dot(int n, const double* a, const double* b) {
+    double s = 0;
+    for (int i = 0; i < n; i++) s += a[i] * b[i];
+    return s;
+}
+
+// Preconditioned CG; is.cpp:39-121.  Returns the iteration count (i+1).
+static int cg(const CSC& A, const double* rhs, double* x, Tree& M, int iters, double tol, double* relres_out) {
+    int n = A.n;
+    std::vector<double> r(n), p(n), z(n), tmp(n);
+    spmv(A, x, tmp.data());
+    for (int i = 0; i < n; i++) r[i] = rhs[i] - tmp[i];
+    double rhsNorm2 = dot(n, rhs, rhs);
+    if (rhsNorm2 == 0) { std::fill(x, x + n, 0.0); return 0; }
+    double threshold = tol * tol * rhsNorm2;
+    double resNorm2 = dot(n, r.data(), r.data());
+    if (relres_out) *relres_out = std::sqrt(resNorm2 / rhsNorm2);
+    if (resNorm2 < threshold) return 0;
+    p = r;
+    M.solve(p.data());
+    double absNew = dot(n, r.data(), p.data());
+    int i = 0;
+    while (i < iters) {
+        spmv(A, p.data(), tmp.data());
+        double alpha = absNew / dot(n, p.data(), tmp.data());
+        for (int k = 0; k < n; k++) x[k] += alpha * p[k];
+        for (int k = 0; k < n; k++) r[k] -= alpha * tmp[k];
+        resNorm2 = dot(n, r.data(), r.data());
+        if (resNorm2 < threshold) break;
+        z = r;
+        M.solve(z.data());
+        double absOld = absNew;
+        absNew = dot(n, r.data(), z.data());
+        double beta = absNew / absOld;
+        for (int k = 0; k < n; k++) p[k] = z[k] + beta * p[k];
+        i++;
+    }
+    if (relres_out) *relres_out = std::sqrt(resNorm2 / rhsNorm2);
+    return i + 1;
+}
+
+// Iterative refinement; is.cpp:12-37.
+static int ir(const CSC& A, const double* rhs, double* x, Tree& M, int iters, double tol) {
+    int n = A.n;
+    std::vector<double> res(n), tmp(n);
+    spmv(A, x, tmp.data());
+    for (int k = 0; k < n; k++) res[k] = rhs[k] - tmp[k];
+    double rhsNorm2 = dot(n, rhs, rhs);
+    if (rhsNorm2 == 0) { std::fill(x, x + n, 0.0); return 0; }
+    double threshold = tol * tol * rhsNorm2;
+    double resNorm2 = dot(n, res.data(), res.data());
+    int i = 1;
+    while (resNorm2 >= threshold && i < iters) {
+        M.solve(res.data());
+        for (int k = 0; k < n; k++) x[k] += res[k];
+        spmv(A, x, tmp.data());
+        for (int k = 0; k < n; k++) res[k] = rhs[k] - tmp[k];
+        resNorm2 = dot(n, res.data(), res.data());
+        if (resNorm2 < threshold) break;
+        i++;
+    }
+    return i;
+}
+
+}  // namespace orc
+
+// =================================================================================
+// C API (ctypes), oracle only
+// =================================================================================
+using namespace orc;
+
+struct OrcHandle {
+    std::unique_ptr<Tree> t;
+    CSC A;
+    std::vector<double> X;
+    std::string err;
+};
+
+static CSC make_csc(int n, const int* colptr, const int* rowval, const double* val) {
+    CSC A;
+    A.n = n;
+    A.colptr.assign(colptr, colptr + n + 1);
+    int nnz = colptr[n];
+    A.rowval.assign(rowval, rowval + nnz);
+    if (val) A.val.assign(val, val + nnz);
+    else A.val.assign(nnz, 1.0);
+    return A;
+}
+
+extern "C" {
+
+void* orc_create(int nlevels) {
+    auto h = new OrcHandle();
+    h->t = std::make_unique<Tree>(nlevels);
+    return h;
+}
+void orc_destroy(void* p) { delete (OrcHandle*)p; }
+const char* orc_error(void* p) { return ((OrcHandle*)p)->err.c_str(); }
+void orc_set_tol(void* p, double tol) { ((OrcHandle*)p)->t->tol = tol; }
+void orc_set_skip(void* p, int skip) { ((OrcHandle*)p)->t->skip = skip; }
+void orc_set_symm_kind(void* p, int k) { ((OrcHandle*)p)->t->symm = k; }
+void orc_set_scaling_kind(void* p, int k) { ((OrcHandle*)p)->t->scale_kind = k; }
+void orc_set_use_sparsify(void* p, int u) { ((OrcHandle*)p)->t->use_want_sparsify = u != 0; }
+void orc_set_Xcoo(void* p, const double* X, int dim, int n) {
+    auto h = (OrcHandle*)p;
+    h->X.assign(X, X + (size_t)dim * n);
+    h->t->X = h->X.data();
+    h->t->dim = dim;
+    h->t->geo = true;
+}
+
+int orc_partition(void* p, int n, const int* colptr, const int* rowval) {
+    auto h = (OrcHandle*)p;
+    try {
+        h->t->partition(make_csc(n, colptr, rowval, nullptr));
+    } catch (std::exception& e) { h->err = e.what(); return -1; }
+    return 0;
+}
+// out: 6*N ints: self.lvl self.sep l.lvl l.sep r.lvl r.sep per dof (natural ordering)
+void orc_get_partition(void* p, int* out) {
+    auto& part = ((OrcHandle*)p)->t->part;
+    for (size_t i = 0; i < part.size(); i++) {
+        out[6 * i + 0] = part[i].self.lvl; out[6 * i + 1] = part[i].self.sep;
+        out[6 * i + 2] = part[i].l.lvl;    out[6 * i + 3] = part[i].l.sep;
+        out[6 * i + 4] = part[i].r.lvl;    out[6 * i + 5] = part[i].r.sep;
+    }
+}
+void orc_get_perm(void* p, int* perm) {
+    auto& v = ((OrcHandle*)p)->t->perm;
+    std::copy(v.begin(), v.end(), perm);
+}
+int orc_num_clusters(void* p, int lvl) { return (int)((OrcHandle*)p)->t->bottoms[lvl].size(); }
+// per cluster at hierarchy level lvl: start size level order sparsify parent_order
+void orc_get_clusters(void* p, int lvl, int* out) {
+    int k = 0;
+    for (auto& c : ((OrcHandle*)p)->t->bottoms[lvl]) {
+        out[6 * k + 0] = c->start; out[6 * k + 1] = c->size; out[6 * k + 2] = c->level;
+        out[6 * k + 3] = c->order; out[6 * k + 4] = c->sparsify; out[6 * k + 5] = c->parent ? c->parent->order : -1;
+        k++;
+    }
+}
+int orc_assemble(void* p, int n, const int* colptr, const int* rowval, const double* val) {
+    auto h = (OrcHandle*)p;
+    try {
+        h->A = make_csc(n, colptr, rowval, val);
+        h->t->assemble(h->A);
+    } catch (std::exception& e) { h->err = e.what(); return -1; }
+    return 0;
+}
+// trailing matrix triplets; returns count, fills when buffers non-null
+int orc_trailing(void* p, int* I, int* J, double* V) {
+    std::vector<int> i, j;
+    std::vector<double> v;
+    ((OrcHandle*)p)->t->trailing(i, j, v);
+    if (I) { std::copy(i.begin(), i.end(), I); std::copy(j.begin(), j.end(), J); std::copy(v.begin(), v.end(), V); }
+    return (int)i.size();
+}
+int orc_factorize(void* p) {
+    auto h = (OrcHandle*)p;
+    try {
+        h->t->factorize();
+    } catch (std::exception& e) { h->err = e.what(); return -1; }
+    return 0;
+}
+void orc_solve(void* p, double* x) { ((OrcHandle*)p)->t->solve(x); }
+void orc_solve_multi(void* p, double* x, int nrhs, int ld) {
+    for (int k = 0; k < nrhs; k++) ((OrcHandle*)p)->t->solve(x + (size_t)k * ld);
+}
+int orc_cg(void* p, const double* b, double* x, int iters, double tol, double* relres) {
+    auto h = (OrcHandle*)p;
+    return cg(h->A, b, x, *h->t, iters, tol, relres);
+}
+int orc_ir(void* p, const double* b, double* x, int iters, double tol) {
+    auto h = (OrcHandle*)p;
+    return ir(h->A, b, x, *h->t, iters, tol);
+}
+long long orc_nnz(void* p) { return ((OrcHandle*)p)->t->nnz(); }
+int orc_get_stop(void* p) { return ((OrcHandle*)p)->t->get_stop(); }
+// per level: dofs_nd dofs_left_nd dofs_left_elim dofs_left_spars rank_before_sum rank_after_sum
+//            rank_after_count ignored nbrs_sum nbrs_count
+void orc_get_log(void* p, long long* out) {
+    auto& L = ((OrcHandle*)p)->t->log;
+    for (size_t l = 0; l < L.size(); l++) {
+        long long* o = out + 11 * l;
+        o[0] = L[l].dofs_nd; o[1] = L[l].dofs_left_nd; o[2] = L[l].dofs_left_elim; o[3] = L[l].dofs_left_spars;
+        o[4] = L[l].rank_before.sum; o[5] = L[l].rank_after.sum; o[6] = L[l].rank_after.count; o[7] = L[l].ignored;
+        o[8] = L[l].nbrs.sum; o[9] = L[l].nbrs.count; o[10] = L[l].fact_nnz;
+    }
+}
+// per level: t_elim t_scale t_spars t_merge flops_potf flops_trsm flops_gemm flops_geqp3
+void orc_get_prof(void* p, double* out) {
+    auto& L = ((OrcHandle*)p)->t->log;
+    for (size_t l = 0; l < L.size(); l++) {
+        double* o = out + 8 * l;
+        o[0] = L[l].t_elim; o[1] = L[l].t_scale; o[2] = L[l].t_spars; o[3] = L[l].t_merge;
+        o[4] = L[l].flops_potf; o[5] = L[l].flops_trsm; o[6] = L[l].flops_gemm; o[7] = L[l].flops_geqp3;
+    }
+}
+void orc_get_times(void* p, double* out) {
+    auto t = ((OrcHandle*)p)->t.get();
+    out[0] = t->t_partition; out[1] = t->t_assemble; out[2] = t->t_factorize;
+}
+int orc_num_ranks(void* p) { return (int)((OrcHandle*)p)->t->rank_log.size(); }
+void orc_get_ranks(void* p, int* out) {
+    auto& r = ((OrcHandle*)p)->t->rank_log;
+    for (size_t i = 0; i < r.size(); i++)
+        for (int k = 0; k < 4; k++) out[4 * i + k] = r[i][k];
+}
+// Op list introspection: per op kind, level, self order, nbr order, ns, nn, rows(A), cols(A)
+int orc_num_ops(void* p) { return (int)((OrcHandle*)p)->t->ops.size(); }
+void orc_get_ops(void* p, int* out) {
+    int k = 0;
+    for (auto& op : ((OrcHandle*)p)->t->ops) {
+        int* o = out + 8 * k;
+        o[0] = op->kind; o[1] = op->ilvl; o[2] = op->self ? op->self->order : -1; o[3] = op->nbr ? op->nbr->order : -1;
+        o[4] = op->ns; o[5] = op->nn; o[6] = op->A ? op->A->r : 0; o[7] = op->A ? op->A->c : 0;
+        k++;
+    }
+}
+// Copy the A matrix of op #idx (column-major) into out; returns number of entries
+long long orc_get_op_matrix(void* p, int idx, double* out) {
+    auto it = ((OrcHandle*)p)->t->ops.begin();
+    std::advance(it, idx);
+    if (!(*it)->A) return 0;
+    auto& v = (*it)->A->v;
+    if (out) std::copy(v.begin(), v.end(), out);
+    return (long long)v.size();
+}
+int orc_get_op_tau(void* p, int idx, double* out) {
+    auto it = ((OrcHandle*)p)->t->ops.begin();
+    std::advance(it, idx);
+    auto& h = (*it)->h;
+    if (out) std::copy(h.begin(), h.end(), out);
+    return (int)h.size();
+}
+
+// Dense kernels exposed for cross-checks against LAPACK
+int orc_dense_potf(int n, double* A) {
+    Mat M(n, n);
+    std::copy(A, A + (size_t)n * n, M.v.begin());
+    int info = potf(M);
+    std::copy(M.v.begin(), M.v.end(), A);
+    return info;
+}
+void orc_dense_geqp3(int m, int n, double* A, int* jpvt, double* tau) {
+    Mat M(m, n);
+    std::copy(A, A + (size_t)m * n, M.v.begin());
+    std::vector<int> jp;
+    std::vector<double> t;
+    geqp3(M, jp, t);
+    std::copy(M.v.begin(), M.v.end(), A);
+    std::copy(jp.begin(), jp.end(), jpvt);
+    std::copy(t.begin(), t.end(), tau);
+}
+int orc_dense_getf(int n, double* A, int* perm) {
+    Mat M(n, n);
+    std::copy(A, A + (size_t)n * n, M.v.begin());
+    std::vector<int> p;
+    int info = getf(M, p);
+    std::copy(M.v.begin(), M.v.end(), A);
+    if (info == 0) std::copy(p.begin(), p.end(), perm);
+    return info;
+}
+int orc_choose_rank(const double* s, int n, double tol) {
+    return choose_rank(std::vector<double>(s, s + n), tol);
+}
+void orc_spmv(void* p, const double* x, double* y) { spmv(((OrcHandle*)p)->A, x, y); }
+
+}  // extern "C"

@@ -1,0 +1,258 @@
+"""spaND factorization and solve on GB300: Python binding of the C ABI.
+
+``Tree`` mirrors ``spaND::Tree`` of leopoldcambier/spaND_public (include/tree.h:133-197:
+set_* options, partition, assemble, factorize, solve) and ``cg`` mirrors its CG driver
+(include/is.h:12).  Every call goes through ``lib/libspand_gb300.so`` (include/spand_gb300.h);
+there is no CPU fallback: a missing library or a missing GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libspand_gb300.so")
+
+# ScalingKind / SymmKind / PartKind enumerators of include/spaND.h:19-21
+SVD, PLU, PLUQ, EVD, LLT, LDLT = range(6)
+SPD, SYM, GEN = range(3)
+MND, RB = range(2)
+
+OP_NAMES = {0: "ScalingLLT", 1: "GemmSymmOut", 2: "GemmSymmIn", 3: "Orthogonal", 4: "Merge", 5: "Split"}
+
+_lib = None
+
+
+class SpandError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"[{status}] {msg}")
+        self.status = status
+
+
+_PROTOS = {
+    "spand_last_error": (C.c_char_p, []),
+    "spand_tree_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int]),
+    "spand_tree_destroy": (C.c_int, [C.c_void_p]),
+    "spand_tree_set_verb": (C.c_int, [C.c_void_p, C.c_int]),
+    "spand_tree_set_use_geo": (C.c_int, [C.c_void_p, C.c_int]),
+    "spand_tree_set_Xcoo": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
+    "spand_tree_set_tol": (C.c_int, [C.c_void_p, C.c_double]),
+    "spand_tree_set_skip": (C.c_int, [C.c_void_p, C.c_int]),
+    "spand_tree_set_scaling_kind": (C.c_int, [C.c_void_p, C.c_int]),
+    "spand_tree_set_symm_kind": (C.c_int, [C.c_void_p, C.c_int]),
+    "spand_tree_set_part_kind": (C.c_int, [C.c_void_p, C.c_int]),
+    "spand_tree_set_use_sparsify": (C.c_int, [C.c_void_p, C.c_int]),
+    "spand_tree_set_fp32": (C.c_int, [C.c_void_p, C.c_int]),
+    "spand_tree_partition": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "spand_tree_assemble": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "spand_tree_factorize": (C.c_int, [C.c_void_p]),
+    "spand_tree_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
+    "spand_tree_solve_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
+    "spand_cg": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int,
+                           C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "spand_cg_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
+                                  C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "spand_tree_get_N": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "spand_tree_get_perm": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "spand_tree_nnz": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
+    "spand_tree_get_stop": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "spand_tree_level_log": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "spand_tree_num_ranks": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "spand_tree_get_ranks": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "spand_tree_num_ops": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "spand_tree_get_ops": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "spand_tree_get_op_matrix": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "spand_tree_get_op_tau": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "spand_tree_timings": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "spand_tree_launches": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.c_int]),
+    "spand_tree_device_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
+}
+
+
+def exported_symbols():
+    return list(_PROTOS)
+
+
+def lib():
+    """Load the in-tree C-ABI library; raise if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _PROTOS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise SpandError(rc, lib().spand_last_error().decode())
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _csc(A):
+    A = A.tocsc()
+    cp = np.ascontiguousarray(A.indptr, dtype=np.int32)
+    rv = np.ascontiguousarray(A.indices, dtype=np.int32)
+    vv = np.ascontiguousarray(A.data, dtype=np.float64)
+    return A.shape[0], cp, rv, vv
+
+
+LOG_KEYS = ["dofs_nd", "dofs_left_nd", "dofs_left_elim", "dofs_left_spars", "rank_before_sum", "rank_after_sum",
+            "rank_after_count", "ignored", "nbrs_sum", "nbrs_count", "fact_nnz"]
+
+
+class Tree:
+    """spaND::Tree on one GB300 (include/tree.h:133-197)."""
+
+    def __init__(self, nlevels: int):
+        self.L = lib()
+        h = C.c_void_p()
+        _check(self.L.spand_tree_create(C.byref(h), int(nlevels)))
+        self.h = h
+        self.nlevels = int(nlevels)
+        self._A = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.spand_tree_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # setters (include/tree.h:133-147)
+    def set_verb(self, v): _check(self.L.spand_tree_set_verb(self.h, int(bool(v))))
+    def set_use_geo(self, g): _check(self.L.spand_tree_set_use_geo(self.h, int(bool(g))))
+    def set_tol(self, tol): _check(self.L.spand_tree_set_tol(self.h, float(tol)))
+    def set_skip(self, s): _check(self.L.spand_tree_set_skip(self.h, int(s)))
+    def set_scaling_kind(self, k): _check(self.L.spand_tree_set_scaling_kind(self.h, int(k)))
+    def set_symm_kind(self, k): _check(self.L.spand_tree_set_symm_kind(self.h, int(k)))
+    def set_part_kind(self, k): _check(self.L.spand_tree_set_part_kind(self.h, int(k)))
+    def set_use_sparsify(self, u): _check(self.L.spand_tree_set_use_sparsify(self.h, int(bool(u))))
+    def set_fp32(self, f): _check(self.L.spand_tree_set_fp32(self.h, int(bool(f))))
+
+    def set_Xcoo(self, X):
+        X = np.asfortranarray(X, dtype=np.float64)
+        self._X = X
+        _check(self.L.spand_tree_set_Xcoo(self.h, _ptr(X), X.shape[0], X.shape[1]))
+
+    def partition(self, A):
+        n, cp, rv, _ = _csc(A)
+        out = np.zeros((n, 6), dtype=np.int32)
+        _check(self.L.spand_tree_partition(self.h, n, _ptr(cp), _ptr(rv), _ptr(out)))
+        self.n = n
+        return out
+
+    def assemble(self, A):
+        n, cp, rv, vv = _csc(A)
+        _check(self.L.spand_tree_assemble(self.h, n, _ptr(cp), _ptr(rv), _ptr(vv)))
+        self._A = A
+
+    def factorize(self):
+        _check(self.L.spand_tree_factorize(self.h))
+
+    def solve(self, x):
+        """Return M^{-1} x for a vector or an (n, nrhs) array (src/tree.cpp:1610-1635)."""
+        y = np.array(x, dtype=np.float64, order="F", copy=True)
+        nrhs = 1 if y.ndim == 1 else y.shape[1]
+        _check(self.L.spand_tree_solve(self.h, _ptr(y), nrhs, y.shape[0]))
+        return y
+
+    def solve_device(self, ptr: int, nrhs: int, ld: int):
+        _check(self.L.spand_tree_solve_device(self.h, C.c_void_p(ptr), int(nrhs), int(ld)))
+
+    def cg(self, b, iters=100, tol=1e-12, x0=None, verb=False):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.float64)
+        it = C.c_int()
+        rr = C.c_double()
+        _check(self.L.spand_cg(self.h, _ptr(b), _ptr(x), int(iters), float(tol), int(bool(verb)), C.byref(it),
+                               C.byref(rr)))
+        return x, it.value, rr.value
+
+    def cg_device(self, b_ptr: int, x_ptr: int, iters=100, tol=1e-12):
+        it = C.c_int()
+        rr = C.c_double()
+        _check(self.L.spand_cg_device(self.h, C.c_void_p(b_ptr), C.c_void_p(x_ptr), int(iters), float(tol),
+                                      C.byref(it), C.byref(rr)))
+        return it.value, rr.value
+
+    # introspection
+    def get_N(self):
+        n = C.c_int()
+        _check(self.L.spand_tree_get_N(self.h, C.byref(n)))
+        return n.value
+
+    def get_assembly_perm(self):
+        p = np.zeros(self.get_N(), dtype=np.int32)
+        _check(self.L.spand_tree_get_perm(self.h, _ptr(p)))
+        return p
+
+    def nnz(self):
+        v = C.c_longlong()
+        _check(self.L.spand_tree_nnz(self.h, C.byref(v)))
+        return v.value
+
+    def get_stop(self):
+        v = C.c_int()
+        _check(self.L.spand_tree_get_stop(self.h, C.byref(v)))
+        return v.value
+
+    def level_log(self):
+        out = np.zeros((self.nlevels, 11), dtype=np.int64)
+        _check(self.L.spand_tree_level_log(self.h, _ptr(out)))
+        return [dict(zip(LOG_KEYS, map(int, r))) for r in out]
+
+    def ranks(self):
+        n = C.c_int()
+        _check(self.L.spand_tree_num_ranks(self.h, C.byref(n)))
+        out = np.zeros((n.value, 4), dtype=np.int32)
+        if n.value:
+            _check(self.L.spand_tree_get_ranks(self.h, _ptr(out)))
+        return out
+
+    def ops(self):
+        n = C.c_int()
+        _check(self.L.spand_tree_num_ops(self.h, C.byref(n)))
+        out = np.zeros((n.value, 8), dtype=np.int32)
+        if n.value:
+            _check(self.L.spand_tree_get_ops(self.h, _ptr(out)))
+        return out
+
+    def op_matrix(self, idx, rows, cols):
+        buf = np.zeros(max(rows * cols, 1))
+        _check(self.L.spand_tree_get_op_matrix(self.h, int(idx), _ptr(buf)))
+        return buf[: rows * cols].reshape((cols, rows)).T
+
+    def op_tau(self, idx, k):
+        buf = np.zeros(max(k, 1))
+        _check(self.L.spand_tree_get_op_tau(self.h, int(idx), _ptr(buf)))
+        return buf[:k]
+
+    def timings(self):
+        out = np.zeros(3)
+        _check(self.L.spand_tree_timings(self.h, _ptr(out)))
+        return dict(partition=out[0], assemble=out[1], factorize=out[2])
+
+    def launches(self, reset=False):
+        v = C.c_longlong()
+        _check(self.L.spand_tree_launches(self.h, C.byref(v), int(bool(reset))))
+        return v.value
+
+    def device_bytes(self):
+        v = C.c_longlong()
+        _check(self.L.spand_tree_device_bytes(self.h, C.byref(v)))
+        return v.value

@@ -1,0 +1,244 @@
+// extern "C" boundary (include/spand_gb300.h) over spaND::Tree.
+#include <cstring>
+#include <exception>
+#include <string>
+
+#include "../../include/spand_gb300.h"
+#include "tree.h"
+
+struct spand_tree {
+    spaND::Tree* t;
+    int geo = 0;
+};
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+template <typename F>
+static int guard(F&& f) {
+    try {
+        f();
+        g_err.clear();
+        return SPAND_OK;
+    } catch (std::invalid_argument& e) {
+        return fail(SPAND_ERR_ARG, e.what());
+    } catch (std::logic_error& e) {
+        return fail(SPAND_ERR_STATE, e.what());
+    } catch (std::runtime_error& e) {
+        std::string m = e.what();
+        if (m.find("Non-SPD") != std::string::npos) return fail(SPAND_ERR_NOT_SPD, m);
+        if (m.find("cuda") != std::string::npos || m.find("CUDA") != std::string::npos) return fail(SPAND_ERR_CUDA, m);
+        return fail(SPAND_ERR_UNSUPPORTED, m);
+    } catch (spand::DeviceError& e) {
+        return fail(e.status, e.msg);
+    } catch (std::exception& e) {
+        return fail(SPAND_ERR_CUDA, e.what());
+    }
+}
+
+static spand::Csc make_csc(int n, const int* colptr, const int* rowval, const double* vals) {
+    if (n < 0 || !colptr || (!rowval && colptr[n] > 0)) throw std::invalid_argument("invalid CSC arrays");
+    spand::Csc A;
+    A.n = n;
+    A.colptr.assign(colptr, colptr + n + 1);
+    const int nnz = colptr[n];
+    A.rowval.assign(rowval, rowval + nnz);
+    if (vals) A.val.assign(vals, vals + nnz);
+    else A.val.assign(nnz, 1.0);
+    for (int j = 0; j < n; j++) {
+        if (colptr[j + 1] < colptr[j]) throw std::invalid_argument("colptr must be non-decreasing");
+        for (int k = colptr[j]; k < colptr[j + 1]; k++) {
+            if (rowval[k] < 0 || rowval[k] >= n) throw std::invalid_argument("row index out of range");
+            if (k > colptr[j] && rowval[k] <= rowval[k - 1]) throw std::invalid_argument("row indices must be sorted and unique");
+        }
+    }
+    return A;
+}
+
+#define CHECK_T(t) \
+    if (!(t) || !(t)->t) return fail(SPAND_ERR_ARG, "null tree")
+
+extern "C" {
+
+const char* spand_last_error(void) { return g_err.c_str(); }
+
+int spand_tree_create(spand_tree** out, int nlevels) {
+    if (!out) return fail(SPAND_ERR_ARG, "null output pointer");
+    return guard([&] {
+        auto* h = new spand_tree();
+        h->t = new spaND::Tree(nlevels);
+        *out = h;
+    });
+}
+
+int spand_tree_destroy(spand_tree* t) {
+    if (!t) return SPAND_OK;
+    return guard([&] {
+        delete t->t;
+        delete t;
+    });
+}
+
+int spand_tree_set_verb(spand_tree* t, int v) { CHECK_T(t); t->t->set_verb(v != 0); return SPAND_OK; }
+int spand_tree_set_use_geo(spand_tree* t, int g) { CHECK_T(t); t->t->set_use_geo(g != 0); return SPAND_OK; }
+int spand_tree_set_Xcoo(spand_tree* t, const double* X, int dim, int n) {
+    CHECK_T(t);
+    if (!X || dim <= 0 || n < 0) return fail(SPAND_ERR_ARG, "invalid coordinates");
+    return guard([&] { t->t->set_Xcoo(X, dim, n); });
+}
+int spand_tree_set_tol(spand_tree* t, double tol) { CHECK_T(t); t->t->set_tol(tol); return SPAND_OK; }
+int spand_tree_set_skip(spand_tree* t, int skip) { CHECK_T(t); t->t->set_skip(skip); return SPAND_OK; }
+int spand_tree_set_scaling_kind(spand_tree* t, int k) {
+    CHECK_T(t);
+    if (k < 0 || k > 5) return fail(SPAND_ERR_ARG, "unknown scaling kind");
+    t->t->set_scaling_kind((spaND::ScalingKind)k);
+    return SPAND_OK;
+}
+int spand_tree_set_symm_kind(spand_tree* t, int k) {
+    CHECK_T(t);
+    if (k < 0 || k > 2) return fail(SPAND_ERR_ARG, "unknown symmetry kind");
+    t->t->set_symm_kind((spaND::SymmKind)k);
+    return SPAND_OK;
+}
+int spand_tree_set_part_kind(spand_tree* t, int k) {
+    CHECK_T(t);
+    if (k < 0 || k > 1) return fail(SPAND_ERR_ARG, "unknown partition kind");
+    t->t->set_part_kind((spaND::PartKind)k);
+    return SPAND_OK;
+}
+int spand_tree_set_use_sparsify(spand_tree* t, int u) { CHECK_T(t); t->t->set_use_sparsify(u != 0); return SPAND_OK; }
+int spand_tree_set_fp32(spand_tree* t, int f) { CHECK_T(t); t->t->set_fp32(f != 0); return SPAND_OK; }
+
+int spand_tree_partition(spand_tree* t, int n, const int* colptr, const int* rowval, int* sepids) {
+    CHECK_T(t);
+    return guard([&] {
+        auto part = t->t->partition(make_csc(n, colptr, rowval, nullptr));
+        if (sepids)
+            for (int i = 0; i < n; i++) {
+                sepids[6 * i + 0] = part[i].self.lvl; sepids[6 * i + 1] = part[i].self.sep;
+                sepids[6 * i + 2] = part[i].l.lvl;    sepids[6 * i + 3] = part[i].l.sep;
+                sepids[6 * i + 4] = part[i].r.lvl;    sepids[6 * i + 5] = part[i].r.sep;
+            }
+    });
+}
+
+int spand_tree_assemble(spand_tree* t, int n, const int* colptr, const int* rowval, const double* vals) {
+    CHECK_T(t);
+    if (!vals) return fail(SPAND_ERR_ARG, "null values");
+    return guard([&] { t->t->assemble(make_csc(n, colptr, rowval, vals)); });
+}
+
+int spand_tree_factorize(spand_tree* t) {
+    CHECK_T(t);
+    return guard([&] { t->t->factorize(); });
+}
+
+int spand_tree_solve(spand_tree* t, double* x, int nrhs, int ld) {
+    CHECK_T(t);
+    if (!x || nrhs < 1 || ld < t->t->get_N()) return fail(SPAND_ERR_ARG, "invalid vector arguments");
+    return guard([&] { t->t->solve(x, nrhs, ld); });
+}
+
+int spand_tree_solve_device(spand_tree* t, double* x, int nrhs, int ld) {
+    CHECK_T(t);
+    if (!x || nrhs < 1 || ld < t->t->get_N()) return fail(SPAND_ERR_ARG, "invalid vector arguments");
+    return guard([&] { t->t->solve_device(x, nrhs, ld); });
+}
+
+int spand_cg(spand_tree* t, const double* b, double* x, int iters, double tol, int verb, int* iters_out,
+             double* relres_out) {
+    CHECK_T(t);
+    if (!b || !x) return fail(SPAND_ERR_ARG, "null vector");
+    return guard([&] {
+        double rr = 0;
+        int it = spaND::cg(t->t->matrix(), b, x, *t->t, iters, tol, verb != 0, &rr);
+        if (iters_out) *iters_out = it;
+        if (relres_out) *relres_out = rr;
+    });
+}
+
+int spand_cg_device(spand_tree* t, const double* b, double* x, int iters, double tol, int* iters_out,
+                    double* relres_out) {
+    CHECK_T(t);
+    if (!b || !x) return fail(SPAND_ERR_ARG, "null vector");
+    return guard([&] {
+        if (!t->t->device()) throw std::logic_error("cg before factorize");
+        spand::PcgResult r = spand::device_pcg(*t->t->device(), t->t->device_csr(), b, x, iters, tol, true);
+        if (iters_out) *iters_out = r.iterations;
+        if (relres_out) *relres_out = r.relres;
+    });
+}
+
+int spand_tree_get_N(spand_tree* t, int* n) { CHECK_T(t); *n = t->t->get_N(); return SPAND_OK; }
+int spand_tree_get_perm(spand_tree* t, int* perm) {
+    CHECK_T(t);
+    const auto& p = t->t->get_assembly_perm();
+    std::memcpy(perm, p.data(), p.size() * sizeof(int));
+    return SPAND_OK;
+}
+int spand_tree_nnz(spand_tree* t, long long* nnz) { CHECK_T(t); *nnz = t->t->nnz(); return SPAND_OK; }
+int spand_tree_get_stop(spand_tree* t, int* stop) { CHECK_T(t); *stop = t->t->get_stop(); return SPAND_OK; }
+int spand_tree_level_log(spand_tree* t, long long* out) {
+    CHECK_T(t);
+    const auto& L = t->t->log();
+    for (size_t l = 0; l < L.size(); l++) {
+        long long* o = out + 11 * l;
+        o[0] = L[l].dofs_nd; o[1] = L[l].dofs_left_nd; o[2] = L[l].dofs_left_elim; o[3] = L[l].dofs_left_spars;
+        o[4] = L[l].rank_before_sum; o[5] = L[l].rank_after_sum; o[6] = L[l].rank_after_count; o[7] = L[l].ignored;
+        o[8] = L[l].nbrs_sum; o[9] = L[l].nbrs_count; o[10] = L[l].fact_nnz;
+    }
+    return SPAND_OK;
+}
+int spand_tree_num_ranks(spand_tree* t, int* n) { CHECK_T(t); *n = (int)t->t->ranks().size(); return SPAND_OK; }
+int spand_tree_get_ranks(spand_tree* t, int* out) {
+    CHECK_T(t);
+    auto r = t->t->ranks();
+    for (size_t i = 0; i < r.size(); i++)
+        for (int k = 0; k < 4; k++) out[4 * i + k] = r[i][k];
+    return SPAND_OK;
+}
+int spand_tree_num_ops(spand_tree* t, int* n) { CHECK_T(t); *n = (int)t->t->ops().size(); return SPAND_OK; }
+int spand_tree_get_ops(spand_tree* t, int* out) {
+    CHECK_T(t);
+    const auto& ops = t->t->ops();
+    for (size_t i = 0; i < ops.size(); i++) {
+        int* o = out + 8 * i;
+        o[0] = ops[i].kind; o[1] = ops[i].level; o[2] = ops[i].self; o[3] = ops[i].nbr;
+        o[4] = ops[i].ns; o[5] = ops[i].nn; o[6] = ops[i].rows; o[7] = ops[i].cols;
+    }
+    return SPAND_OK;
+}
+int spand_tree_get_op_matrix(spand_tree* t, int idx, double* out) {
+    CHECK_T(t);
+    return guard([&] {
+        std::vector<double> m;
+        t->t->op_matrix(idx, m);
+        std::memcpy(out, m.data(), m.size() * sizeof(double));
+    });
+}
+int spand_tree_get_op_tau(spand_tree* t, int idx, double* out) {
+    CHECK_T(t);
+    return guard([&] {
+        std::vector<double> m;
+        t->t->op_tau(idx, m);
+        std::memcpy(out, m.data(), m.size() * sizeof(double));
+    });
+}
+int spand_tree_timings(spand_tree* t, double* out) {
+    CHECK_T(t);
+    out[0] = t->t->t_partition; out[1] = t->t->t_assemble; out[2] = t->t->t_factorize;
+    return SPAND_OK;
+}
+int spand_tree_launches(spand_tree* t, long long* n, int reset) {
+    CHECK_T(t);
+    *n = t->t->launches();
+    if (reset) t->t->reset_launches();
+    return SPAND_OK;
+}
+int spand_tree_device_bytes(spand_tree* t, long long* b) { CHECK_T(t); *b = (long long)t->t->device_bytes(); return SPAND_OK; }
+
+}  // extern "C"

@@ -1,0 +1,81 @@
+// Device numeric factorization and solve for the GB300 spaND path.
+//
+// The plan (host.h) fixes every work list; this layer uploads them once and runs the
+// factorization as a fixed launch sequence on one stream.  Cluster sizes live in device
+// memory: the QRCP kernels shrink them, later kernels read them, so no host round trip
+// happens inside factorize().  T is the storage/arithmetic type of the factor (double
+// for the plain path, float for the mixed path).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "host.h"
+
+namespace spand {
+
+// Status codes shared with the C ABI.
+enum Status : int {
+    SPAND_OK = 0,
+    SPAND_ERR_ARG = 1,
+    SPAND_ERR_STATE = 2,
+    SPAND_ERR_CUDA = 3,
+    SPAND_ERR_NOT_SPD = 4,
+    SPAND_ERR_UNSUPPORTED = 5,
+    SPAND_ERR_NO_CONVERGENCE = 6,
+};
+
+struct DeviceError {
+    int status;
+    std::string msg;
+};
+
+// Per-launch counters: how many kernels ran, for the bench's gpu_launches claim.
+struct LaunchCounter {
+    int64_t launches = 0;
+};
+
+class DeviceFactorBase {
+   public:
+    virtual ~DeviceFactorBase() {}
+    virtual void upload(const Plan& P, const std::vector<double>& assembled) = 0;
+    virtual void factorize(double tol) = 0;  // throws DeviceError
+    // x: device pointer, natural ordering, n x nrhs (ld), FP64; in-place M^{-1} x
+    virtual void solve_device(double* x, int nrhs, int ld) = 0;
+    virtual void sizes(std::vector<int>& csize, std::vector<int>& rows0) = 0;
+    virtual void block(int b, std::vector<double>& out) = 0;  // host copy (ld layout)
+    virtual void ortho(int c, std::vector<double>& v, std::vector<double>& tau) = 0;
+    virtual int precision_bytes() const = 0;
+    virtual cudaStream_t stream() const = 0;
+    virtual int64_t launches() const = 0;
+    virtual void reset_launches() = 0;
+    virtual void capture_solve_graph(int nrhs) = 0;
+    virtual size_t device_bytes() const = 0;
+};
+
+// perm: assembly permutation (b = P^T x <=> b[i] = x[perm[i]])
+std::unique_ptr<DeviceFactorBase> make_device_factor(bool fp32, cudaStream_t stream, const std::vector<int>& perm);
+
+// FP64 preconditioned CG on the device (src/is.cpp:39-121), A in CSR on the device.
+struct DeviceCsr {
+    int n = 0;
+    int* rowptr = nullptr;
+    int* colind = nullptr;
+    double* val = nullptr;
+};
+
+struct PcgResult {
+    int iterations = 0;
+    double relres = 0.0;  // recurrence residual |r|/|b|
+};
+
+PcgResult device_pcg(DeviceFactorBase& M, const DeviceCsr& A, const double* b, double* x, int maxit, double tol,
+                     bool use_graph);
+
+void device_spmv(const DeviceCsr& A, const double* x, double* y, cudaStream_t s);
+
+}  // namespace spand

@@ -1,0 +1,324 @@
+// spaND::Tree on the GB300 device path.  Citations are path:line into
+// leopoldcambier/spaND_public.
+#include "tree.h"
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+
+namespace spaND {
+
+static double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+static void cuda_check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+Tree::Tree(int nlevels) : nlevels_(nlevels) {
+    if (nlevels <= 0) throw std::invalid_argument("nlevels must be > 0");  // tree.cpp:87
+}
+
+Tree::~Tree() {
+    dev_.reset();
+    if (dx_) cudaFree(dx_);
+    if (dA_.rowptr) cudaFree(dA_.rowptr);
+    if (dA_.colind) cudaFree(dA_.colind);
+    if (dA_.val) cudaFree(dA_.val);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+void Tree::set_Xcoo(const double* X, int dim, int n) {
+    X_.assign(X, X + (size_t)dim * n);
+    dim_ = dim;
+}
+
+// tree.cpp:306-419
+std::vector<ClusterID> Tree::partition(const Csc& A) {
+    if (partitioned_) throw std::logic_error("partition() called twice");
+    double t0 = now_s();
+    const int N = A.n;
+    if (part_kind_ != PartKind::MND) throw std::invalid_argument("only modified nested dissection (MND) is supported");
+    if (geo_) {
+        if ((int)X_.size() != dim_ * N || dim_ <= 0) throw std::invalid_argument("set_Xcoo: coordinates must be dim x N");
+        part_ = spand::partition_modified_nd(A, nlevels_, X_.data(), dim_);
+    } else {
+        std::string err;
+        if (!spand::partition_modified_nd_metis(A, nlevels_, part_, err)) throw std::runtime_error(err);
+    }
+    H_ = spand::build_hierarchy(part_, nlevels_, perm_);
+    log_.assign(nlevels_, LevelLog());
+    for (int i = 0; i < N; i++) log_[part_[i].self.lvl].dofs_nd += 1;
+    log_[nlevels_ - 1].dofs_left_nd = 0;
+    for (int l = nlevels_ - 2; l >= 0; l--) log_[l].dofs_left_nd = log_[l + 1].dofs_nd + log_[l + 1].dofs_left_nd;
+    partitioned_ = true;
+    t_partition = now_s() - t0;
+    return part_;
+}
+
+// tree.cpp:505-575, plus the symbolic plan of factorize() and the device upload.
+void Tree::assemble(const Csc& A) {
+    if (!partitioned_) throw std::logic_error("assemble() before partition()");
+    if (symm_ != SymmKind::SPD || scaling_ != ScalingKind::LLT)
+        throw std::invalid_argument("the device path implements the SPD / LLT configuration");
+    if (A.n != get_N()) throw std::invalid_argument("matrix size does not match the partition");
+    double t0 = now_s();
+    A_ = A;
+    Csc App = spand::symm_perm(A, perm_);
+    asmb_ = spand::assembly_structure(H_, App, true);
+    plan_ = spand::build_plan(H_, asmb_, skip_, use_want_sparsify_);
+    spand::fill_assembled_blocks(plan_, H_, asmb_, App, assembled_);
+    if (!stream_) cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    dev_ = spand::make_device_factor(fp32_, stream_, perm_);
+    try {
+        dev_->upload(plan_, assembled_);
+    } catch (spand::DeviceError& e) {
+        throw std::runtime_error(e.msg);
+    }
+    // CSR of A for the device Krylov solvers (A is structurally symmetric; store A^T's CSC = A's CSR)
+    {
+        const int n = A.n;
+        std::vector<int> rp(n + 1, 0), ci(A.rowval.size());
+        std::vector<double> vv(A.rowval.size());
+        for (int j = 0; j < n; j++)
+            for (int k = A.colptr[j]; k < A.colptr[j + 1]; k++) rp[A.rowval[k] + 1]++;
+        for (int i = 0; i < n; i++) rp[i + 1] += rp[i];
+        std::vector<int> fill(rp.begin(), rp.end() - 1);
+        for (int j = 0; j < n; j++)
+            for (int k = A.colptr[j]; k < A.colptr[j + 1]; k++) {
+                int r = A.rowval[k];
+                ci[fill[r]] = j;
+                vv[fill[r]] = A.val[k];
+                fill[r]++;
+            }
+        if (dA_.rowptr) { cudaFree(dA_.rowptr); cudaFree(dA_.colind); cudaFree(dA_.val); }
+        dA_.n = n;
+        cuda_check(cudaMalloc(&dA_.rowptr, rp.size() * sizeof(int)), "cudaMalloc");
+        cuda_check(cudaMalloc(&dA_.colind, std::max<size_t>(ci.size(), 1) * sizeof(int)), "cudaMalloc");
+        cuda_check(cudaMalloc(&dA_.val, std::max<size_t>(vv.size(), 1) * sizeof(double)), "cudaMalloc");
+        cuda_check(cudaMemcpy(dA_.rowptr, rp.data(), rp.size() * sizeof(int), cudaMemcpyHostToDevice), "H2D");
+        cuda_check(cudaMemcpy(dA_.colind, ci.data(), ci.size() * sizeof(int), cudaMemcpyHostToDevice), "H2D");
+        cuda_check(cudaMemcpy(dA_.val, vv.data(), vv.size() * sizeof(double), cudaMemcpyHostToDevice), "H2D");
+    }
+    assembled_ok_ = true;
+    factored_ = false;
+    t_assemble = now_s() - t0;
+}
+
+// tree.cpp:1447-1551
+void Tree::factorize() {
+    if (!assembled_ok_) throw std::logic_error("factorize() before assemble()");
+    double t0 = now_s();
+    try {
+        if (factored_) {
+            // re-factorize from the assembled values
+            dev_.reset();
+            dev_ = spand::make_device_factor(fp32_, stream_, perm_);
+            dev_->upload(plan_, assembled_);
+        }
+        dev_->factorize(tol_);
+    } catch (spand::DeviceError& e) {
+        if (e.status == spand::SPAND_ERR_NOT_SPD) {
+            if (verb_) printf("Not SPD!\n");
+            throw std::runtime_error("Error: Non-SPD Pivot\n");
+        }
+        throw std::runtime_error(e.msg);
+    }
+    t_factorize = now_s() - t0;
+    factored_ = true;
+    dev_->sizes(csize_, rows0_);
+    build_ops_and_log();
+}
+
+void Tree::solve_device(double* x, int nrhs, int ld) const {
+    if (!factored_) throw std::logic_error("solve() before factorize()");
+    try {
+        dev_->solve_device(x, nrhs, ld);
+    } catch (spand::DeviceError& e) {
+        throw std::runtime_error(e.msg);
+    }
+}
+
+void Tree::solve(double* x, int nrhs, int ld) const {
+    if (ld < 0) ld = get_N();
+    const size_t len = (size_t)ld * nrhs;
+    if (dx_len_ < len) {
+        if (dx_) cudaFree(dx_);
+        cuda_check(cudaMalloc(&dx_, len * sizeof(double)), "cudaMalloc");
+        dx_len_ = len;
+    }
+    cuda_check(cudaMemcpyAsync(dx_, x, len * sizeof(double), cudaMemcpyHostToDevice, stream_), "H2D");
+    solve_device(dx_, nrhs, ld);
+    cuda_check(cudaMemcpyAsync(x, dx_, len * sizeof(double), cudaMemcpyDeviceToHost, stream_), "D2H");
+    cuda_check(cudaStreamSynchronize(stream_), "sync");
+}
+
+size_t Tree::device_bytes() const { return dev_ ? dev_->device_bytes() : 0; }
+
+// Op list and per-level log reconstructed from the plan and the device sizes, in the
+// reference's recording order (tree.cpp:909-910, 885-892, 810, 1331, 1102, 1342, 1439).
+void Tree::build_ops_and_log() {
+    ops_.clear();
+    const spand::Plan& P = plan_;
+    int next_order = P.nclusters;  // siblings are numbered after all clusters
+    long long nnz = 0;
+    auto push = [&](OpRecord r) {
+        switch (r.kind) {
+            case 0: nnz += (long long)r.ns * (r.ns + 1) / 2; break;
+            case 1: case 2: nnz += (long long)r.ns * r.nn; break;
+            case 3: nnz += (long long)r.ns * r.ns; break;
+            default: break;
+        }
+        ops_.push_back(r);
+    };
+    for (int l = 0; l < P.nlevels; l++) {
+        const spand::LevelPlan& L = P.levels[l];
+        LevelLog& G = log_[l];
+        size_t g = 0;
+        for (size_t k = 0; k < L.op_elim_llt.size(); k++) {
+            int s = L.op_elim_llt[k];
+            push({0, l, s, -1, rows0_[s], 0, rows0_[s], rows0_[s], L.op_elim_llt_block[k]});
+            while (g < L.op_gemm.size() && L.op_gemm[g].self == s) {
+                const spand::GemmOpItem& it = L.op_gemm[g];
+                int ns = rows0_[s], nn = rows0_[it.nbr];
+                if (it.kind == 1) push({1, l, s, it.nbr, ns, nn, nn, ns, it.block});
+                else push({2, l, s, it.nbr, ns, nn, ns, nn, it.block});
+                g++;
+            }
+        }
+        long long left_elim = 0;
+        for (int c : H_.bottoms[l])
+            if (H_.level[c] > l) left_elim += rows0_[c];
+        G.dofs_left_elim = left_elim;
+        for (size_t k = 0; k < L.op_scale_llt.size(); k++) {
+            int c = L.op_scale_llt[k];
+            push({0, l, c, -1, rows0_[c], 0, rows0_[c], rows0_[c], L.op_scale_llt_block[k]});
+        }
+        // wave index of every sparsified cluster of this level, for the Asn widths
+        std::vector<int> wave_of;
+        std::map<int, int> wmap;
+        for (size_t w = 0; w < L.waves.size(); w++)
+            for (const spand::SparsifyItem& it : L.waves[w]) wmap[it.cluster] = (int)w;
+        for (int c : L.op_ortho) {
+            int rows = rows0_[c], k = csize_[c];
+            G.rank_before_sum += rows;
+            G.rank_after_sum += k;
+            G.rank_after_count += 1;
+            // Asn width at this cluster's turn
+            const spand::SparsifyItem* item = nullptr;
+            for (const auto& wave : L.waves)
+                for (const auto& it : wave)
+                    if (it.cluster == c) item = &it;
+            long long cols = 0;
+            for (int p = 0; p < item->count; p++) {
+                int n = P.asn_pieces[item->first + p].nbr;
+                auto wn = wmap.find(n);
+                bool before = wn != wmap.end() && wn->second < wmap[c];
+                cols += before ? csize_[n] : rows0_[n];
+            }
+            G.nbrs_sum += cols;
+            G.nbrs_count += 1;
+            if (k < rows) {
+                push({3, l, c, -1, rows, 0, rows, k, c});
+                int sib = next_order++;
+                push({5, l, c, sib, k, rows - k, 0, 0, -1});
+                push({0, l, sib, -1, rows - k, 0, rows - k, rows - k, -1});
+            }
+        }
+        G.ignored = L.ignored;
+        for (int p : L.op_merge) push({4, l, p, -1, rows0_[p], 0, 0, 0, -1});
+        long long left_spars = 0;
+        if (l + 1 < P.nlevels) {
+            for (int p : H_.bottoms[l + 1]) left_spars += rows0_[p];
+        }
+        G.dofs_left_spars = left_spars;
+        G.fact_nnz = nnz;
+    }
+}
+
+long long Tree::nnz() const {
+    return log_.empty() ? 0 : log_.back().fact_nnz;
+}
+
+// tree.cpp:158-169
+int Tree::get_stop() const {
+    int stop = get_N();
+    for (const LevelLog& l : log_) {
+        if (l.dofs_left_elim > 0) stop = std::min<long long>(stop, l.dofs_left_elim);
+        if (l.dofs_left_spars > 0) stop = std::min<long long>(stop, l.dofs_left_spars);
+    }
+    return stop;
+}
+
+std::vector<std::array<int, 4>> Tree::ranks() const {
+    std::vector<std::array<int, 4>> r;
+    for (int l = 0; l < plan_.nlevels; l++)
+        for (int c : plan_.levels[l].op_ortho) r.push_back({l, c, rows0_[c], csize_[c]});
+    return r;
+}
+
+void Tree::op_matrix(int idx, std::vector<double>& out) const {
+    const OpRecord& r = ops_.at(idx);
+    out.clear();
+    if (r.kind == 0 || r.kind == 1 || r.kind == 2) {
+        if (r.block < 0) {  // sibling identity
+            out.assign((size_t)r.rows * r.cols, 0.0);
+            for (int i = 0; i < r.rows; i++) out[i + (size_t)i * r.rows] = 1.0;
+            return;
+        }
+        std::vector<double> full;
+        dev_->block(r.block, full);
+        const int ld = plan_.blocks[r.block].ld;
+        out.resize((size_t)r.rows * r.cols);
+        for (int j = 0; j < r.cols; j++)
+            for (int i = 0; i < r.rows; i++) out[i + (size_t)j * r.rows] = full[i + (size_t)j * ld];
+    } else if (r.kind == 3) {
+        std::vector<double> v, tau;
+        dev_->ortho(r.block, v, tau);
+        const int ld = plan_.c_cap[r.block];
+        out.resize((size_t)r.rows * r.cols);
+        for (int j = 0; j < r.cols; j++)
+            for (int i = 0; i < r.rows; i++) out[i + (size_t)j * r.rows] = v[i + (size_t)j * ld];
+    }
+}
+
+void Tree::op_tau(int idx, std::vector<double>& out) const {
+    const OpRecord& r = ops_.at(idx);
+    out.clear();
+    if (r.kind != 3) return;
+    std::vector<double> v, tau;
+    dev_->ortho(r.block, v, tau);
+    out.assign(tau.begin(), tau.begin() + r.cols);
+}
+
+int cg(const Csc& A, const double* rhs, double* x, const Tree& precond, int iters, double tol, bool verb,
+       double* relres) {
+    (void)A;  // the tree holds the device copy of the assembled matrix
+    const int n = precond.get_N();
+    double *db, *dx;
+    cuda_check(cudaMalloc(&db, n * sizeof(double)), "cudaMalloc");
+    cuda_check(cudaMalloc(&dx, n * sizeof(double)), "cudaMalloc");
+    cudaStream_t s = precond.stream();
+    cuda_check(cudaMemcpyAsync(db, rhs, n * sizeof(double), cudaMemcpyHostToDevice, s), "H2D");
+    cuda_check(cudaMemcpyAsync(dx, x, n * sizeof(double), cudaMemcpyHostToDevice, s), "H2D");
+    spand::PcgResult r;
+    try {
+        r = spand::device_pcg(*precond.device(), precond.device_csr(), db, dx, iters, tol, true);
+    } catch (spand::DeviceError& e) {
+        cudaFree(db);
+        cudaFree(dx);
+        throw std::runtime_error(e.msg);
+    }
+    cuda_check(cudaMemcpyAsync(x, dx, n * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
+    cuda_check(cudaStreamSynchronize(s), "sync");
+    cudaFree(db);
+    cudaFree(dx);
+    if (verb) printf("# of iter:  %d\n", r.iterations);
+    if (relres) *relres = r.relres;
+    return r.iterations;
+}
+
+}  // namespace spaND

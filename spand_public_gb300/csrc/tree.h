@@ -1,0 +1,124 @@
+// C++ drop-in for spaND::Tree (include/tree.h:25-197) and the CG driver
+// (include/is.h:12-14), backed by the GB300 device factorization.
+//
+// Eigen types of the reference signatures are replaced by plain CSC arrays and raw
+// vectors; names, argument meaning and error behaviour (std::runtime_error on a
+// non-SPD pivot, tree.cpp:587-590) follow the reference.
+#pragma once
+
+#include <array>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "device.h"
+#include "host.h"
+
+namespace spaND {
+
+using spand::ClusterID;
+using spand::Csc;
+using spand::SepID;
+
+enum class ScalingKind { SVD, PLU, PLUQ, EVD, LLT, LDLT };
+enum class PartKind { MND, RB };
+enum class SymmKind { SPD, SYM, GEN };
+
+// Per-level record, as Log in include/util.h:366-401 (fields used for parity).
+struct LevelLog {
+    long long dofs_nd = 0, dofs_left_nd = 0, dofs_left_elim = 0, dofs_left_spars = 0;
+    long long rank_before_sum = 0, rank_after_sum = 0, rank_after_count = 0, ignored = 0;
+    long long nbrs_sum = 0, nbrs_count = 0, fact_nnz = 0;
+};
+
+// One recorded operation of the factor, in the reference's op-list order
+// (operations.h:32-163): kind 0 ScalingLLT, 1 GemmSymmOut, 2 GemmSymmIn, 3 Orthogonal,
+// 4 Merge, 5 Split.
+struct OpRecord {
+    int kind, level, self, nbr, ns, nn, rows, cols;
+    int block;  // device block (ScalingLLT / Gemm), or sparsified cluster (Orthogonal), or -1
+};
+
+class Tree {
+   public:
+    explicit Tree(int nlevels);
+    ~Tree();
+
+    void set_verb(bool v) { verb_ = v; }
+    void set_Xcoo(const double* X, int dim, int n);
+    void set_use_geo(bool g) { geo_ = g; }
+    void set_tol(double t) { tol_ = t; }
+    void set_skip(int s) { skip_ = s; }
+    void set_scaling_kind(ScalingKind k) { scaling_ = k; }
+    void set_symm_kind(SymmKind k) { symm_ = k; }
+    void set_part_kind(PartKind k) { part_kind_ = k; }
+    void set_use_sparsify(bool u) { use_want_sparsify_ = u; }
+    // No reference counterpart: storage/arithmetic type of the factor (false: FP64).
+    void set_fp32(bool f) { fp32_ = f; }
+
+    std::vector<ClusterID> partition(const Csc& A);
+    void assemble(const Csc& A);
+    void factorize();
+    // x <- M^{-1} x, host vector(s) in natural ordering (tree.cpp:1610-1635)
+    void solve(double* x, int nrhs = 1, int ld = -1) const;
+    // device vector(s)
+    void solve_device(double* x, int nrhs, int ld) const;
+
+    int get_N() const { return (int)perm_.size(); }
+    const std::vector<int>& get_assembly_perm() const { return perm_; }
+    long long nnz() const;
+    int get_stop() const;
+    int get_nlevels() const { return nlevels_; }
+    const std::vector<LevelLog>& log() const { return log_; }
+    // (level, cluster order, rows, rank) for every sparsified cluster, reference order
+    std::vector<std::array<int, 4>> ranks() const;
+    const std::vector<OpRecord>& ops() const { return ops_; }
+    void op_matrix(int idx, std::vector<double>& out) const;
+    void op_tau(int idx, std::vector<double>& out) const;
+    double t_partition = 0, t_assemble = 0, t_factorize = 0;
+    int64_t launches() const { return dev_ ? dev_->launches() : 0; }
+    void reset_launches() { if (dev_) dev_->reset_launches(); }
+    spand::DeviceFactorBase* device() const { return dev_.get(); }
+    const Csc& matrix() const { return A_; }
+    const spand::Plan& plan() const { return plan_; }
+    cudaStream_t stream() const { return stream_; }
+    spand::DeviceCsr device_csr() const { return dA_; }
+    size_t device_bytes() const;
+
+   private:
+    void build_ops_and_log();
+
+    int nlevels_;
+    bool verb_ = true, geo_ = false, use_want_sparsify_ = true, fp32_ = false;
+    double tol_ = 10.0;  // tree.cpp:94
+    int skip_ = 0;
+    ScalingKind scaling_ = ScalingKind::LLT;
+    SymmKind symm_ = SymmKind::SPD;
+    PartKind part_kind_ = PartKind::MND;
+    std::vector<double> X_;
+    int dim_ = 0;
+    std::vector<ClusterID> part_;
+    std::vector<int> perm_;
+    spand::Hierarchy H_;
+    spand::Assembly asmb_;
+    spand::Plan plan_;
+    Csc A_;
+    std::vector<double> assembled_;
+    std::unique_ptr<spand::DeviceFactorBase> dev_;
+    cudaStream_t stream_ = nullptr;
+    spand::DeviceCsr dA_;
+    mutable double* dx_ = nullptr;
+    mutable size_t dx_len_ = 0;
+    bool partitioned_ = false, assembled_ok_ = false, factored_ = false;
+    std::vector<LevelLog> log_;
+    std::vector<OpRecord> ops_;
+    std::vector<int> csize_, rows0_;
+};
+
+// Preconditioned CG (is.cpp:39-121) on the device; b and x are host vectors.
+int cg(const Csc& A, const double* rhs, double* x, const Tree& precond, int iters, double tol, bool verb,
+       double* relres = nullptr);
+
+}  // namespace spaND

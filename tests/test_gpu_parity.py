@@ -1,0 +1,165 @@
+"""Device path vs the CPU oracle (plain FP64 and mixed FP32 factor).
+
+Bars: partition and permutation identical; per-cluster ranks identical; every recorded
+factor block (ScalingLLT lower triangles, Gemm panels, Householder reflectors) within
+1e-12 relative (Frobenius, per block) of the oracle; M^{-1}b within 1e-12 relative; CG
+iteration count equal.  The FP32 factor must reach the same FP64 residual with at most
+15% more CG iterations.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL_BLOCK = 1e-12   # relative Frobenius error per factor block, FP64 path
+TOL_SOLVE = 1e-12   # relative error of M^{-1} b, FP64 path
+
+
+def _build(n, dim, nlevels, tol, skip=0, fp32=False, A=None):
+    import spand_public_gb300 as pkg
+    from oracle.oracle import OracleTree
+    from spand_public_gb300 import problems as P
+
+    A = P.neglapl(n, dim) if A is None else A
+    X = P.linspace_nd(n, dim)
+    t = pkg.Tree(nlevels)
+    t.set_verb(False)
+    t.set_use_geo(True)
+    t.set_Xcoo(X)
+    t.set_tol(tol)
+    t.set_skip(skip)
+    t.set_fp32(fp32)
+    pt = t.partition(A)
+    t.assemble(A)
+    t.factorize()
+    o = OracleTree(nlevels)
+    o.set_Xcoo(X)
+    o.set_tol(tol)
+    o.set_skip(skip)
+    po = o.partition(A)
+    o.assemble(A)
+    o.factorize()
+    assert np.array_equal(pt, po)
+    return A, t, o
+
+
+CASES = [
+    (5, 2, 3, 1e-2, 0),
+    (20, 2, 4, 1e-14, 0),
+    (32, 2, 5, 1e-2, 0),
+    (64, 2, 7, 1e-2, 0),    # 2D 5-point -Laplacian 64x64, 7 levels, eps = 1e-2
+    (64, 2, 7, 1e-2, 2),
+    (10, 3, 4, 1e-2, 0),
+    (16, 3, 6, 1e-2, 0),
+    (16, 3, 6, 0.0, 0),
+    (20, 2, 4, 10.0, 0),    # tol >= 1: every sparsified cluster drops to rank 0
+]
+
+
+@pytest.mark.parametrize("n,dim,nlevels,tol,skip", CASES)
+def test_factor_parity_fp64(n, dim, nlevels, tol, skip):
+    A, t, o = _build(n, dim, nlevels, tol, skip)
+    assert np.array_equal(t.get_assembly_perm(), o.get_assembly_perm())
+    # ranks
+    rt, ro = t.ranks(), o.ranks()
+    assert np.array_equal(rt, ro), "per-cluster ranks differ"
+    # op structure (kind, level, self, nbr, sizes)
+    opt, opo = t.ops(), o.ops()
+    assert opt.shape == opo.shape
+    assert np.array_equal(opt[:, :6], opo[:, :6])
+    # factor blocks
+    worst = 0.0
+    for k in range(opt.shape[0]):
+        kind, rows, cols = opt[k, 0], opt[k, 6], opt[k, 7]
+        if kind not in (0, 1, 2, 3) or rows * cols == 0:
+            continue
+        mt = t.op_matrix(k, rows, cols)
+        mo = o.op_matrix(k, opo[k, 6], opo[k, 7])
+        if kind == 0:
+            mt, mo = np.tril(mt), np.tril(mo)
+        if kind == 3:
+            mt, mo = np.tril(mt, -1), np.tril(mo, -1)
+            ht, ho = t.op_tau(k, cols), o.op_tau(k, cols)
+            worst = max(worst, np.linalg.norm(ht - ho) / max(np.linalg.norm(ho), 1e-300))
+        den = max(np.linalg.norm(mo), 1e-300)
+        worst = max(worst, np.linalg.norm(mt - mo) / den)
+    assert worst < TOL_BLOCK, worst
+    # per-level log
+    lt, lo = t.level_log(), o.level_log()
+    for a, b in zip(lt, lo):
+        for key in ("dofs_nd", "dofs_left_nd", "dofs_left_elim", "dofs_left_spars", "rank_before_sum",
+                    "rank_after_sum", "rank_after_count", "ignored", "nbrs_sum", "fact_nnz"):
+            assert a[key] == b[key], (key, a[key], b[key])
+    assert t.nnz() == o.nnz()
+    assert t.get_stop() == o.get_stop()
+    # solve
+    from spand_public_gb300 import problems as P
+    b = P.rhs(A.shape[0], 2, seed=3)
+    xt, xo = t.solve(b), o.solve(b)
+    assert np.linalg.norm(xt - xo) / np.linalg.norm(xo) < TOL_SOLVE
+
+
+@pytest.mark.parametrize("n,dim,nlevels,tol", [(64, 2, 7, 1e-2), (16, 3, 6, 1e-2), (24, 3, 7, 1e-3)])
+def test_pcg_iterations_match(n, dim, nlevels, tol):
+    from spand_public_gb300 import problems as P
+    A, t, o = _build(n, dim, nlevels, tol)
+    b = P.rhs(A.shape[0], 1, seed=11)[:, 0]
+    xt, it, rel = t.cg(b, iters=200, tol=1e-12)
+    xo, ito = o.cg(b, iters=200, tol=1e-12)
+    assert it == ito, (it, ito)
+    res = np.linalg.norm(A @ xt - b) / np.linalg.norm(b)
+    assert res < 1e-11
+    assert np.linalg.norm(xt - xo) / np.linalg.norm(xo) < 1e-9
+
+
+@pytest.mark.parametrize("n,dim,nlevels,tol", [(64, 2, 7, 1e-2), (16, 3, 6, 1e-2), (24, 3, 7, 1e-3)])
+def test_mixed_precision_pcg(n, dim, nlevels, tol):
+    """FP32 factor + FP64 PCG reaches 1e-10 with <= 15% more iterations than FP64."""
+    from spand_public_gb300 import problems as P
+    A, t64, o = _build(n, dim, nlevels, tol)
+    _, t32, _ = _build(n, dim, nlevels, tol, fp32=True)
+    b = P.rhs(A.shape[0], 1, seed=5)[:, 0]
+    x64, it64, _ = t64.cg(b, iters=200, tol=1e-10)
+    x32, it32, _ = t32.cg(b, iters=200, tol=1e-10)
+    assert np.linalg.norm(A @ x32 - b) / np.linalg.norm(b) < 1e-9
+    assert it32 <= max(it64 + 1, int(np.ceil(1.15 * it64))), (it32, it64)
+    # the FP32 preconditioner against the FP64 oracle's (error stated: ~FP32 epsilon x conditioning)
+    xt = t32.solve(b)
+    xo = o.solve(b)
+    assert np.linalg.norm(xt - xo) / np.linalg.norm(xo) < 1e-3
+
+
+def test_reproducible():
+    """Bit-identical results across runs (tests/tests.cpp:917-994)."""
+    from spand_public_gb300 import problems as P
+    A, t, _ = _build(32, 2, 5, 1e-5, skip=1)
+    b = P.rhs(A.shape[0], 1, seed=1)[:, 0]
+    x0 = t.solve(b)
+    for _ in range(3):
+        _, t2, _ = _build(32, 2, 5, 1e-5, skip=1)
+        assert np.array_equal(t2.solve(b), x0)
+
+
+def test_not_spd_error():
+    """A non-SPD pivot is reported as an error (tree.cpp:587-590), not a crash."""
+    import spand_public_gb300 as pkg
+    from spand_public_gb300 import problems as P
+    A = -P.neglapl(10, 2)
+    X = P.linspace_nd(10, 2)
+    t = pkg.Tree(3)
+    t.set_verb(False)
+    t.set_use_geo(True)
+    t.set_Xcoo(X)
+    t.partition(A)
+    t.assemble(A)
+    with pytest.raises(pkg.SpandError) as e:
+        t.factorize()
+    assert e.value.status == 4
+    # the context is still usable
+    t2 = pkg.Tree(3)
+    t2.set_use_geo(True)
+    t2.set_Xcoo(X)
+    t2.set_verb(False)
+    t2.partition(-A)
+    t2.assemble(-A)
+    t2.factorize()
