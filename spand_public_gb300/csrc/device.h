@@ -39,10 +39,46 @@ struct LaunchCounter {
     int64_t launches = 0;
 };
 
+// Per-kernel-class device time, recorded with CUDA events on the launching stream
+// around every launch while enabled.
+class KernelProfiler {
+   public:
+    ~KernelProfiler();
+    void enable(bool on) { on_ = on; }
+    bool enabled() const { return on_; }
+    void begin(cudaStream_t s, const char* cls);
+    void end(cudaStream_t s);
+    // accumulate recorded pairs into per-class totals (synchronises the events)
+    void collect();
+    void clear();
+    struct Entry {
+        std::string cls;
+        int64_t launches = 0;
+        double ms = 0.0;
+    };
+    const std::vector<Entry>& totals() const { return totals_; }
+
+   private:
+    cudaEvent_t take();
+    bool on_ = false;
+    std::vector<cudaEvent_t> pool_;
+    size_t used_ = 0;
+    struct Rec {
+        std::string cls;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec> recs_;
+    std::string cur_;
+    cudaEvent_t cur_a_ = nullptr;
+    std::vector<Entry> totals_;
+};
+
 class DeviceFactorBase {
    public:
     virtual ~DeviceFactorBase() {}
     virtual void upload(const Plan& P, const std::vector<double>& assembled) = 0;
+    // replace the assembled block values (same plan)
+    virtual void upload_values(const std::vector<double>& assembled) = 0;
     virtual void factorize(double tol) = 0;  // throws DeviceError
     // x: device pointer, natural ordering, n x nrhs (ld), FP64; in-place M^{-1} x
     virtual void solve_device(double* x, int nrhs, int ld) = 0;
@@ -51,10 +87,17 @@ class DeviceFactorBase {
     virtual void ortho(int c, std::vector<double>& v, std::vector<double>& tau) = 0;
     virtual int precision_bytes() const = 0;
     virtual cudaStream_t stream() const = 0;
-    virtual int64_t launches() const = 0;
-    virtual void reset_launches() = 0;
-    virtual void capture_solve_graph(int nrhs) = 0;
     virtual size_t device_bytes() const = 0;
+    int64_t launches() const { return launches_; }
+    void reset_launches() { launches_ = 0; }
+    void add_launches(int64_t k) { launches_ += k; }
+    KernelProfiler& profiler() { return prof_; }
+    // capture the solve on buffer x as a CUDA graph; solve_device(x, ...) then replays it
+    virtual void capture_solve(double* x, int nrhs, int ld) = 0;
+
+   protected:
+    int64_t launches_ = 0;
+    KernelProfiler prof_;
 };
 
 // perm: assembly permutation (b = P^T x <=> b[i] = x[perm[i]])

@@ -884,15 +884,70 @@ __global__ void sub_kernel(int n, const double* a, const double* b, double* y) {
 }
 
 // ------------------------------------------------------------------------------------
+// Kernel profiler
+// ------------------------------------------------------------------------------------
+KernelProfiler::~KernelProfiler() {
+    for (cudaEvent_t e : pool_) cudaEventDestroy(e);
+}
+
+cudaEvent_t KernelProfiler::take() {
+    if (used_ == pool_.size()) {
+        cudaEvent_t e;
+        SPAND_CUDA(cudaEventCreate(&e));
+        pool_.push_back(e);
+    }
+    return pool_[used_++];
+}
+
+void KernelProfiler::begin(cudaStream_t s, const char* cls) {
+    if (!on_) return;
+    cur_ = cls;
+    cur_a_ = take();
+    SPAND_CUDA(cudaEventRecord(cur_a_, s));
+}
+
+void KernelProfiler::end(cudaStream_t s) {
+    if (!on_) return;
+    cudaEvent_t b = take();
+    SPAND_CUDA(cudaEventRecord(b, s));
+    recs_.push_back({cur_, cur_a_, b});
+}
+
+void KernelProfiler::collect() {
+    for (const Rec& r : recs_) {
+        SPAND_CUDA(cudaEventSynchronize(r.b));
+        float ms = 0;
+        SPAND_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+        auto it = std::find_if(totals_.begin(), totals_.end(), [&](const Entry& e) { return e.cls == r.cls; });
+        if (it == totals_.end()) {
+            totals_.push_back({r.cls, 0, 0.0});
+            it = totals_.end() - 1;
+        }
+        it->launches++;
+        it->ms += ms;
+    }
+    recs_.clear();
+    used_ = 0;
+}
+
+void KernelProfiler::clear() {
+    recs_.clear();
+    used_ = 0;
+    totals_.clear();
+}
+
+// ------------------------------------------------------------------------------------
 // Host driver
 // ------------------------------------------------------------------------------------
 template <typename V>
-static V* dev_upload(const std::vector<V>& h, std::vector<void*>& owned, cudaStream_t s) {
+static V* dev_upload(const std::vector<V>& h, std::vector<void*>& owned, size_t& bytes, cudaStream_t s) {
     if (h.empty()) return nullptr;
     V* d = nullptr;
     SPAND_CUDA(cudaMalloc(&d, h.size() * sizeof(V)));
     owned.push_back(d);
+    bytes += h.size() * sizeof(V);
     SPAND_CUDA(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(V), cudaMemcpyHostToDevice, s));
+    SPAND_CUDA(cudaStreamSynchronize(s));
     return d;
 }
 
@@ -912,31 +967,25 @@ class DeviceFactor : public DeviceFactorBase {
     ~DeviceFactor() override {
         if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
         if (graph_) cudaGraphDestroy(graph_);
+        if (xs_) cudaFree(xs_);
         for (void* p : owned_) cudaFree(p);
     }
 
     int precision_bytes() const override { return sizeof(T); }
     cudaStream_t stream() const override { return s_; }
-    int64_t launches() const override { return launches_; }
-    void reset_launches() override { launches_ = 0; }
     size_t device_bytes() const override { return bytes_; }
 
     void upload(const Plan& P, const std::vector<double>& assembled) override {
         P_ = &P;
         nc_ = P.nclusters;
-        // arena
-        arena_len_ = P.arena_len;
-        arena_ = alloc<T>(arena_len_);
-        {
-            std::vector<T> tmp(assembled.begin(), assembled.end());
-            SPAND_CUDA(cudaMemcpyAsync(arena_, tmp.data(), tmp.size() * sizeof(T), cudaMemcpyHostToDevice, s_));
-            SPAND_CUDA(cudaStreamSynchronize(s_));
-        }
+        arena_ = alloc<T>(P.arena_len);
+        pristine_ = alloc<T>(P.assembled_len);
+        upload_values(assembled);
         std::vector<DBlock> blk(P.blocks.size());
         for (size_t b = 0; b < P.blocks.size(); b++)
             blk[b] = {(long long)P.blocks[b].off, P.blocks[b].ld, P.blocks[b].rowc, P.blocks[b].colc, P.blocks[b].flag};
-        d_blk_ = dev_upload(blk, owned_, s_);
-        d_cap_ = dev_upload(P.c_cap, owned_, s_);
+        d_blk_ = up(blk);
+        d_cap_ = up(P.c_cap);
         csize_ = alloc<int>(nc_);
         rows0_ = alloc<int>(nc_);
         rank_ = alloc<int>(nc_);
@@ -946,7 +995,14 @@ class DeviceFactor : public DeviceFactorBase {
         taustore_ = alloc<T>(std::max<int64_t>(P.tau_len, 1));
         tauws_ = alloc<T>(std::max<int64_t>(P.tau_len, 1));
         ws_ = alloc<T>(std::max<int64_t>(P.ws_len, 1));
-        // per-level device lists
+        {
+            std::vector<DUpd> u;
+            for (const SchurUpdate& su : P.schur_updates) u.push_back({su.b1, su.t1, su.b2, su.t2, su.s});
+            d_ups_ = up(u);
+            std::vector<DAsn> a;
+            for (const AsnPiece& ap : P.asn_pieces) a.push_back({ap.block, ap.nbr, ap.transposed});
+            pieces_ = up(a);
+        }
         int64_t max_cols = 1;
         int max_items = 1;
         levels_.resize(P.nlevels);
@@ -954,11 +1010,10 @@ class DeviceFactor : public DeviceFactorBase {
             const LevelPlan& L = P.levels[l];
             LevelDev& D = levels_[l];
             D.n_elim = (int)L.elim_clusters.size();
-            D.elim_clusters = dev_upload(L.elim_clusters, owned_, s_);
-            D.elim_pivots = dev_upload(L.elim_pivots, owned_, s_);
+            D.elim_clusters = up(L.elim_clusters);
+            D.elim_pivots = up(L.elim_pivots);
             D.elim_smem = smem_for(L.elim_clusters, P);
             build_trsm(L.elim_trsm, L.elim_pivots, L.elim_clusters, P, D.elim_trsm0, D.elim_trsm1);
-            // schur
             {
                 std::vector<DTarget> tg;
                 std::vector<DTile> tiles;
@@ -971,27 +1026,23 @@ class DeviceFactor : public DeviceFactorBase {
                         for (int b = 0; b < tj; b++)
                             if (!st.syrk || a >= b) tiles.push_back({t, a, b});
                 }
-                D.schur_targets = dev_upload(tg, owned_, s_);
-                D.schur_tiles = dev_upload(tiles, owned_, s_);
+                D.schur_targets = up(tg);
+                D.schur_tiles = up(tiles);
                 D.n_schur_tiles = (int)tiles.size();
             }
-            D.fill_off = L.fill_off;
-            D.fill_len = L.fill_len;
             D.scaled = L.scaled;
             D.n_scale = (int)L.scale_clusters.size();
-            D.scale_clusters = dev_upload(L.scale_clusters, owned_, s_);
-            D.scale_pivots = dev_upload(L.scale_pivots, owned_, s_);
+            D.scale_clusters = up(L.scale_clusters);
+            D.scale_pivots = up(L.scale_pivots);
             D.scale_smem = smem_for(L.scale_clusters, P);
             build_trsm(L.scale_trsm, L.scale_pivots, L.scale_clusters, P, D.scale_trsm0, D.scale_trsm1);
-            // snapshot clusters: everything in this hierarchy level
             {
                 std::vector<int> all;
                 for (int cl = 0; cl < nc_; cl++)
                     if (P.c_hlevel[cl] == l) all.push_back(cl);
                 D.n_level = (int)all.size();
-                D.level_clusters = dev_upload(all, owned_, s_);
+                D.level_clusters = up(all);
             }
-            // sparsify waves
             for (const auto& wave : L.waves) {
                 WaveDev W;
                 std::vector<DSpars> items;
@@ -1003,14 +1054,15 @@ class DeviceFactor : public DeviceFactorBase {
                     coloff += std::max(it.cap_cols, 1);
                     maxcap = std::max(maxcap, P.c_cap[it.cluster]);
                 }
+                if ((int64_t)maxcap * (int64_t)sizeof(T) > 200 * 1024)
+                    throw DeviceError{SPAND_ERR_UNSUPPORTED, "cluster too large for the QRCP kernel"};
                 max_cols = std::max(max_cols, coloff);
                 max_items = std::max(max_items, (int)items.size());
                 W.n = (int)items.size();
-                W.items = dev_upload(items, owned_, s_);
+                W.items = up(items);
                 W.maxcap = maxcap;
                 D.waves.push_back(W);
             }
-            // merge
             D.merged = L.merged;
             if (L.merged) {
                 std::vector<int> cptr(1, 0), cidx, parent_of;
@@ -1022,10 +1074,10 @@ class DeviceFactor : public DeviceFactorBase {
                     cptr.push_back((int)cidx.size());
                 }
                 D.n_parents = (int)L.merge_parents.size();
-                D.parents = dev_upload(L.merge_parents, owned_, s_);
-                D.child_ptr = dev_upload(cptr, owned_, s_);
-                D.child_idx = dev_upload(cidx, owned_, s_);
-                D.child_parent = dev_upload(parent_of, owned_, s_);
+                D.parents = up(L.merge_parents);
+                D.child_ptr = up(cptr);
+                D.child_idx = up(cidx);
+                D.child_parent = up(parent_of);
                 D.n_children = (int)cidx.size();
                 std::vector<DMerge> mc;
                 std::vector<DTile> tiles;
@@ -1036,23 +1088,21 @@ class DeviceFactor : public DeviceFactorBase {
                     for (int a = 0; a < ti; a++)
                         for (int b = 0; b < tj; b++) tiles.push_back({(int)k, a, b});
                 }
-                D.merge_items = dev_upload(mc, owned_, s_);
-                D.merge_tiles = dev_upload(tiles, owned_, s_);
+                D.merge_items = up(mc);
+                D.merge_tiles = up(tiles);
                 D.n_merge_tiles = (int)tiles.size();
-                D.merge_off = L.merge_off;
-                D.merge_len = L.merge_len;
             }
-            // solve ops
             D.n_elim_llt = (int)L.op_elim_llt.size();
-            D.elim_llt = dev_upload(L.op_elim_llt, owned_, s_);
-            D.elim_llt_blk = dev_upload(L.op_elim_llt_block, owned_, s_);
+            D.elim_llt = up(L.op_elim_llt);
+            D.elim_llt_blk = up(L.op_elim_llt_block);
             D.n_scale_llt = (int)L.op_scale_llt.size();
-            D.scale_llt = dev_upload(L.op_scale_llt, owned_, s_);
-            D.scale_llt_blk = dev_upload(L.op_scale_llt_block, owned_, s_);
+            D.scale_llt = up(L.op_scale_llt);
+            D.scale_llt_blk = up(L.op_scale_llt_block);
             D.x_smem_elim = xsmem_for(L.op_elim_llt, P);
             D.x_smem_scale = xsmem_for(L.op_scale_llt, P);
             {
-                // group gemm ops: fwd by nbr (op order), bwd by self (reverse op order)
+                // Gemm ops grouped: forward by neighbour in op order, backward by
+                // eliminated cluster in reverse op order.
                 std::map<int, std::vector<DGemmOp>> fwd, bwd;
                 std::vector<int> fkeys, bkeys;
                 for (const GemmOpItem& g : L.op_gemm) {
@@ -1075,10 +1125,10 @@ class DeviceFactor : public DeviceFactorBase {
                 }
                 D.n_gf = (int)fg.size();
                 D.n_gb = (int)bg.size();
-                D.gf = dev_upload(fg, owned_, s_);
-                D.gb = dev_upload(bg, owned_, s_);
-                D.gfo = dev_upload(fo, owned_, s_);
-                D.gbo = dev_upload(bo, owned_, s_);
+                D.gf = up(fg);
+                D.gb = up(bg);
+                D.gfo = up(fo);
+                D.gbo = up(bo);
             }
             {
                 std::vector<DOrtho> ot;
@@ -1089,7 +1139,7 @@ class DeviceFactor : public DeviceFactorBase {
                         mx = std::max(mx, P.c_cap[it.cluster]);
                     }
                 D.n_ortho = (int)ot.size();
-                D.ortho = dev_upload(ot, owned_, s_);
+                D.ortho = up(ot);
                 D.x_smem_ortho = mx * (int)sizeof(T);
             }
         }
@@ -1097,77 +1147,94 @@ class DeviceFactor : public DeviceFactorBase {
         jpvt_ = alloc<int>(max_cols);
         ipvt_ = alloc<int>(max_cols);
         colcount_ = alloc<int>(max_items);
-        pieces_ = dev_upload(std::vector<DAsn>(toasn(P)), owned_, s_);
-        // solve-vector layout
-        d_xoff_ = dev_upload(std::vector<long long>(P.c_xoff.begin(), P.c_xoff.end()), owned_, s_);
+        d_xoff_ = up(std::vector<long long>(P.c_xoff.begin(), P.c_xoff.end()));
         xld_ = P.x_len;
         {
             std::vector<long long> slot(perm_h_.size());
             for (int c0 = 0; c0 < nc_; c0++)
                 if (P.c_hlevel[c0] == 0)
                     for (int i = 0; i < P.c_cap[c0]; i++) slot[P.c_start[c0] + i] = P.c_xoff[c0] + i;
-            d_slot_ = dev_upload(slot, owned_, s_);
-            d_perm_ = dev_upload(perm_h_, owned_, s_);
+            d_slot_ = up(slot);
+            d_perm_ = up(perm_h_);
         }
-        SPAND_CUDA(cudaStreamSynchronize(s_));
         ctx_ = Ctx<T>{arena_, d_blk_, csize_, rows0_, d_cap_, status_};
-        // opt in to large dynamic shared memory
         SPAND_CUDA(cudaFuncSetAttribute(potrf_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(qrcp_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(trsv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(ortho_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        caps_h_ = P.c_cap;
+    }
+
+    void upload_values(const std::vector<double>& assembled) override {
+        if ((int64_t)assembled.size() != P_->assembled_len)
+            throw DeviceError{SPAND_ERR_ARG, "assembled values do not match the plan"};
+        if (!assembled.empty()) {
+            std::vector<T> tmp(assembled.begin(), assembled.end());
+            SPAND_CUDA(cudaMemcpyAsync(pristine_, tmp.data(), tmp.size() * sizeof(T), cudaMemcpyHostToDevice, s_));
+            SPAND_CUDA(cudaStreamSynchronize(s_));
+        }
+        factored_ = false;
     }
 
     void factorize(double tol) override {
         const Plan& P = *P_;
-        // reset state: sizes, status, assembled values are restored by re-upload only
-        std::vector<int> caps(P.c_cap);
-        SPAND_CUDA(cudaMemcpyAsync(csize_, caps.data(), nc_ * sizeof(int), cudaMemcpyHostToDevice, s_));
-        SPAND_CUDA(cudaMemcpyAsync(rows0_, caps.data(), nc_ * sizeof(int), cudaMemcpyHostToDevice, s_));
-        SPAND_CUDA(cudaMemsetAsync(status_, 0, sizeof(DStatus), s_));
-        SPAND_CUDA(cudaMemsetAsync(rank_, 0x7f, nc_ * sizeof(int), s_));
-        if (P.arena_len > P.assembled_len)
-            SPAND_CUDA(cudaMemsetAsync(arena_ + P.assembled_len, 0, (P.arena_len - P.assembled_len) * sizeof(T), s_));
+        // inputs: the assembled blocks (device copy) and the initial cluster sizes
+        launch("restore", [&] {
+            if (P.assembled_len)
+                SPAND_CUDA(cudaMemcpyAsync(arena_, pristine_, P.assembled_len * sizeof(T), cudaMemcpyDeviceToDevice, s_));
+            if (P.arena_len > P.assembled_len)
+                SPAND_CUDA(cudaMemsetAsync(arena_ + P.assembled_len, 0, (P.arena_len - P.assembled_len) * sizeof(T), s_));
+            SPAND_CUDA(cudaMemcpyAsync(csize_, d_cap_, nc_ * sizeof(int), cudaMemcpyDeviceToDevice, s_));
+            SPAND_CUDA(cudaMemcpyAsync(rows0_, d_cap_, nc_ * sizeof(int), cudaMemcpyDeviceToDevice, s_));
+            SPAND_CUDA(cudaMemsetAsync(status_, 0, sizeof(DStatus), s_));
+            SPAND_CUDA(cudaMemsetAsync(rank_, 0x7f, nc_ * sizeof(int), s_));
+        }, 0);
         for (int l = 0; l < P.nlevels; l++) {
             LevelDev& D = levels_[l];
-            // eliminate interiors
             if (D.n_elim) {
                 launch_potrf(D.elim_pivots, D.elim_clusters, D.n_elim, D.elim_smem);
                 launch_trsm(D.elim_trsm0);
                 launch_trsm(D.elim_trsm1);
-                if (D.n_schur_tiles) {
-                    schur_kernel<T><<<D.n_schur_tiles, 256, 0, s_>>>(ctx_, D.schur_targets, schur_ups(), D.schur_tiles,
-                                                                     D.n_schur_tiles);
-                    count_launch();
-                }
+                if (D.n_schur_tiles)
+                    launch("schur", [&] {
+                        schur_kernel<T><<<D.n_schur_tiles, 256, 0, s_>>>(ctx_, D.schur_targets, d_ups_, D.schur_tiles,
+                                                                         D.n_schur_tiles);
+                    });
             }
             if (D.scaled && D.n_scale) {
                 launch_potrf(D.scale_pivots, D.scale_clusters, D.n_scale, D.scale_smem);
                 launch_trsm(D.scale_trsm0);
                 launch_trsm(D.scale_trsm1);
             }
-            // rows0 of this hierarchy level: sizes before sparsification
-            if (D.n_level) {
-                snapshot_kernel<<<(D.n_level + 255) / 256, 256, 0, s_>>>(csize_, rows0_, D.level_clusters, D.n_level);
-                count_launch();
-            }
+            if (D.n_level)
+                launch("snapshot", [&] {
+                    snapshot_kernel<<<(D.n_level + 255) / 256, 256, 0, s_>>>(csize_, rows0_, D.level_clusters,
+                                                                             D.n_level);
+                });
             for (WaveDev& W : D.waves) {
-                asn_gather_kernel<T><<<W.n, 256, 0, s_>>>(ctx_, W.items, pieces_, ws_, colcount_);
-                qrcp_kernel<T><<<W.n, 512, W.maxcap * sizeof(T), s_>>>(ctx_, W.items, ws_, norms_, jpvt_, colcount_,
-                                                                        tauws_, rank_, tol);
-                sparsify_scatter_kernel<T><<<W.n, 256, 0, s_>>>(ctx_, W.items, pieces_, ws_, jpvt_, ipvt_, rank_,
-                                                                 vstore_, tauws_, taustore_, colcount_);
-                count_launch(3);
+                launch("asn_gather", [&] {
+                    asn_gather_kernel<T><<<W.n, 256, 0, s_>>>(ctx_, W.items, pieces_, ws_, colcount_);
+                });
+                launch("qrcp", [&] {
+                    qrcp_kernel<T><<<W.n, 512, W.maxcap * sizeof(T), s_>>>(ctx_, W.items, ws_, norms_, jpvt_,
+                                                                            colcount_, tauws_, rank_, tol);
+                });
+                launch("sparsify_scatter", [&] {
+                    sparsify_scatter_kernel<T><<<W.n, 256, 0, s_>>>(ctx_, W.items, pieces_, ws_, jpvt_, ipvt_, rank_,
+                                                                     vstore_, tauws_, taustore_, colcount_);
+                });
             }
             if (D.merged) {
-                merge_sizes_kernel<<<(D.n_parents + 127) / 128, 128, 0, s_>>>(csize_, rows0_, cpos_, D.parents,
-                                                                                D.n_parents, D.child_ptr, D.child_idx);
-                count_launch();
-                if (D.n_merge_tiles) {
-                    merge_copy_kernel<T><<<D.n_merge_tiles, 256, 0, s_>>>(ctx_, D.merge_items, D.merge_tiles,
-                                                                          D.n_merge_tiles, cpos_);
-                    count_launch();
-                }
+                launch("merge_sizes", [&] {
+                    merge_sizes_kernel<<<(D.n_parents + 127) / 128, 128, 0, s_>>>(csize_, rows0_, cpos_, D.parents,
+                                                                                    D.n_parents, D.child_ptr,
+                                                                                    D.child_idx);
+                });
+                if (D.n_merge_tiles)
+                    launch("merge_copy", [&] {
+                        merge_copy_kernel<T><<<D.n_merge_tiles, 256, 0, s_>>>(ctx_, D.merge_items, D.merge_tiles,
+                                                                              D.n_merge_tiles, cpos_);
+                    });
             }
         }
         SPAND_CUDA(cudaGetLastError());
@@ -1179,16 +1246,9 @@ class DeviceFactor : public DeviceFactorBase {
         factored_ = true;
     }
 
-    void ensure_x(int nrhs) {
-        if (nrhs <= x_nrhs_) return;
-        if (xs_) cudaFree(xs_);
-        SPAND_CUDA(cudaMalloc(&xs_, (size_t)xld_ * nrhs * sizeof(T)));
-        x_nrhs_ = nrhs;
-    }
-
     void solve_device(double* x, int nrhs, int ld) override {
         if (!factored_) throw DeviceError{SPAND_ERR_STATE, "solve before factorize"};
-        if (graph_exec_ && graph_x_ == x && graph_nrhs_ == nrhs && graph_ld_ == ld) {
+        if (graph_exec_ && graph_x_ == x && graph_nrhs_ == nrhs && graph_ld_ == ld && !prof_.enabled()) {
             SPAND_CUDA(cudaGraphLaunch(graph_exec_, s_));
             launches_ += graph_kernels_;
             return;
@@ -1197,13 +1257,8 @@ class DeviceFactor : public DeviceFactorBase {
         run_solve(x, nrhs, ld);
     }
 
-    void capture_solve_graph(int nrhs) override {
-        // Captured against a fixed FP64 buffer; solve_device() replays it when called
-        // with that buffer (the PCG driver does).
-        (void)nrhs;
-    }
-
-    void capture_for(double* x, int nrhs, int ld) {
+    void capture_solve(double* x, int nrhs, int ld) override {
+        if (!factored_) throw DeviceError{SPAND_ERR_STATE, "solve before factorize"};
         ensure_x(nrhs);
         if (graph_exec_) {
             cudaGraphExecDestroy(graph_exec_);
@@ -1211,11 +1266,22 @@ class DeviceFactor : public DeviceFactorBase {
             graph_exec_ = nullptr;
             graph_ = nullptr;
         }
+        const bool was_on = prof_.enabled();
+        prof_.enable(false);
         int64_t before = launches_;
         SPAND_CUDA(cudaStreamBeginCapture(s_, cudaStreamCaptureModeThreadLocal));
-        run_solve(x, nrhs, ld);
+        try {
+            run_solve(x, nrhs, ld);
+        } catch (...) {
+            cudaGraph_t g;
+            cudaStreamEndCapture(s_, &g);
+            if (g) cudaGraphDestroy(g);
+            prof_.enable(was_on);
+            throw;
+        }
         SPAND_CUDA(cudaStreamEndCapture(s_, &graph_));
         SPAND_CUDA(cudaGraphInstantiate(&graph_exec_, graph_, 0));
+        prof_.enable(was_on);
         graph_kernels_ = launches_ - before;
         launches_ = before;
         graph_x_ = x;
@@ -1249,7 +1315,8 @@ class DeviceFactor : public DeviceFactorBase {
                     if (it.cluster == cl) {
                         size_t n = (size_t)P_->c_cap[cl] * P_->c_cap[cl];
                         std::vector<T> tv(n), tt(P_->c_cap[cl]);
-                        SPAND_CUDA(cudaMemcpyAsync(tv.data(), vstore_ + it.v_off, n * sizeof(T), cudaMemcpyDeviceToHost, s_));
+                        SPAND_CUDA(cudaMemcpyAsync(tv.data(), vstore_ + it.v_off, n * sizeof(T), cudaMemcpyDeviceToHost,
+                                                   s_));
                         SPAND_CUDA(cudaMemcpyAsync(tt.data(), taustore_ + it.tau_off, tt.size() * sizeof(T),
                                                    cudaMemcpyDeviceToHost, s_));
                         SPAND_CUDA(cudaStreamSynchronize(s_));
@@ -1282,7 +1349,6 @@ class DeviceFactor : public DeviceFactorBase {
         DTarget* schur_targets = nullptr;
         DTile* schur_tiles = nullptr;
         int n_schur_tiles = 0;
-        int64_t fill_off = 0, fill_len = 0;
         bool scaled = false;
         int n_scale = 0;
         int* scale_clusters = nullptr;
@@ -1298,7 +1364,6 @@ class DeviceFactor : public DeviceFactorBase {
         DMerge* merge_items = nullptr;
         DTile* merge_tiles = nullptr;
         int n_merge_tiles = 0;
-        int64_t merge_off = 0, merge_len = 0;
         int n_elim_llt = 0, n_scale_llt = 0;
         int *elim_llt = nullptr, *elim_llt_blk = nullptr, *scale_llt = nullptr, *scale_llt_blk = nullptr;
         int x_smem_elim = 0, x_smem_scale = 0, x_smem_ortho = 0;
@@ -1317,20 +1382,24 @@ class DeviceFactor : public DeviceFactorBase {
         bytes_ += std::max<int64_t>(n, 1) * sizeof(V);
         return p;
     }
-    void count_launch(int k = 1) { launches_ += k; }
-
-    std::vector<DAsn> toasn(const Plan& P) {
-        std::vector<DAsn> v;
-        for (const AsnPiece& a : P.asn_pieces) v.push_back({a.block, a.nbr, a.transposed});
-        return v;
+    template <typename V>
+    V* up(const std::vector<V>& h) {
+        return dev_upload(h, owned_, bytes_, s_);
     }
-    DUpd* schur_ups() {
-        if (!d_ups_) {
-            std::vector<DUpd> u;
-            for (const SchurUpdate& s : P_->schur_updates) u.push_back({s.b1, s.t1, s.b2, s.t2, s.s});
-            d_ups_ = dev_upload(u, owned_, s_);
-        }
-        return d_ups_;
+    // one kernel (or copy) launch: counted, and timed when the profiler is on
+    template <typename F>
+    void launch(const char* cls, F&& f, int kernels = 1) {
+        prof_.begin(s_, cls);
+        f();
+        prof_.end(s_);
+        launches_ += kernels;
+    }
+    void ensure_x(int nrhs) {
+        if (nrhs <= x_nrhs_) return;
+        if (xs_) cudaFree(xs_);
+        xs_ = nullptr;
+        SPAND_CUDA(cudaMalloc(&xs_, (size_t)xld_ * nrhs * sizeof(T)));
+        x_nrhs_ = nrhs;
     }
     int smem_for(const std::vector<int>& clusters, const Plan& P) {
         int mx = 0;
@@ -1341,6 +1410,8 @@ class DeviceFactor : public DeviceFactorBase {
     int xsmem_for(const std::vector<int>& clusters, const Plan& P) {
         int mx = 1;
         for (int c0 : clusters) mx = std::max(mx, P.c_cap[c0]);
+        if ((int64_t)mx * (int64_t)sizeof(T) > 200 * 1024)
+            throw DeviceError{SPAND_ERR_UNSUPPORTED, "cluster too large for the solve kernels"};
         return mx * (int)sizeof(T);
     }
     void build_trsm(const std::vector<TrsmItem>& items, const std::vector<int>& pivots, const std::vector<int>& clusters,
@@ -1362,18 +1433,18 @@ class DeviceFactor : public DeviceFactorBase {
         }
         auto t0 = tiles_1d(ext0, TRSM_COLS);
         auto t1 = tiles_1d(ext1, TRSM_ROWS);
-        side0 = {dev_upload(it0, owned_, s_), dev_upload(t0, owned_, s_), (int)t0.size(), 0};
-        side1 = {dev_upload(it1, owned_, s_), dev_upload(t1, owned_, s_), (int)t1.size(), 1};
+        side0 = {up(it0), up(t0), (int)t0.size(), 0};
+        side1 = {up(it1), up(t1), (int)t1.size(), 1};
     }
     void launch_potrf(int* pivots, int* clusters, int n, int smem) {
-        potrf_kernel<T><<<n, 256, smem, s_>>>(ctx_, pivots, clusters, n, smem / (int)sizeof(T));
-        count_launch();
+        launch("potrf", [&] { potrf_kernel<T><<<n, 256, smem, s_>>>(ctx_, pivots, clusters, n, smem / (int)sizeof(T)); });
     }
     void launch_trsm(const TrsmDev& t) {
         if (!t.ntiles) return;
-        if (t.side == 1) trsm_kernel<T><<<t.ntiles, TRSM_ROWS, 0, s_>>>(ctx_, t.items, t.tiles, t.ntiles);
-        else trsm_kernel<T><<<t.ntiles, TRSM_COLS * 32, 0, s_>>>(ctx_, t.items, t.tiles, t.ntiles);
-        count_launch();
+        launch("trsm", [&] {
+            if (t.side == 1) trsm_kernel<T><<<t.ntiles, TRSM_ROWS, 0, s_>>>(ctx_, t.items, t.tiles, t.ntiles);
+            else trsm_kernel<T><<<t.ntiles, TRSM_COLS * 32, 0, s_>>>(ctx_, t.items, t.tiles, t.ntiles);
+        });
     }
 
     void run_solve(double* x, int nrhs, int ld) {
@@ -1381,75 +1452,74 @@ class DeviceFactor : public DeviceFactorBase {
         XCtx<T> X{xs_, (long long)xld_, d_xoff_, nrhs};
         const int n = (int)perm_h_.size();
         const long long tot = (long long)n * nrhs;
-        perm_in_kernel<T><<<(unsigned)((tot + 255) / 256), 256, 0, s_>>>(x, ld, X, d_perm_, d_slot_, n);
-        count_launch();
+        launch("perm", [&] {
+            perm_in_kernel<T><<<(unsigned)((tot + 255) / 256), 256, 0, s_>>>(x, ld, X, d_perm_, d_slot_, n);
+        });
         for (int l = 0; l < P.nlevels; l++) {
             LevelDev& D = levels_[l];
-            if (D.n_elim_llt) {
-                trsv_kernel<T><<<D.n_elim_llt * nrhs, 128, D.x_smem_elim, s_>>>(ctx_, X, D.elim_llt, D.elim_llt_blk,
-                                                                                D.n_elim_llt, 0);
-                count_launch();
-            }
-            if (D.n_gf) {
-                gemm_fwd_kernel<T><<<D.n_gf * nrhs, 128, 0, s_>>>(ctx_, X, D.gf, D.gfo, D.n_gf);
-                count_launch();
-            }
-            if (D.n_scale_llt) {
-                trsv_kernel<T><<<D.n_scale_llt * nrhs, 128, D.x_smem_scale, s_>>>(ctx_, X, D.scale_llt,
-                                                                                  D.scale_llt_blk, D.n_scale_llt, 0);
-                count_launch();
-            }
-            if (D.n_ortho) {
-                ortho_kernel<T><<<D.n_ortho * nrhs, 128, D.x_smem_ortho, s_>>>(ctx_, X, D.ortho, D.n_ortho, vstore_,
-                                                                               taustore_, 1);
-                count_launch();
-            }
-            if (D.merged && D.n_children) {
-                merge_x_kernel<T><<<D.n_children * nrhs, 128, 0, s_>>>(ctx_, X, D.child_idx, D.child_parent,
-                                                                       D.n_children, cpos_, 1);
-                count_launch();
-            }
+            if (D.n_elim_llt)
+                launch("trsv", [&] {
+                    trsv_kernel<T><<<D.n_elim_llt * nrhs, 128, D.x_smem_elim, s_>>>(ctx_, X, D.elim_llt,
+                                                                                    D.elim_llt_blk, D.n_elim_llt, 0);
+                });
+            if (D.n_gf)
+                launch("gemm_fwd", [&] { gemm_fwd_kernel<T><<<D.n_gf * nrhs, 128, 0, s_>>>(ctx_, X, D.gf, D.gfo, D.n_gf); });
+            if (D.n_scale_llt)
+                launch("trsv", [&] {
+                    trsv_kernel<T><<<D.n_scale_llt * nrhs, 128, D.x_smem_scale, s_>>>(ctx_, X, D.scale_llt,
+                                                                                      D.scale_llt_blk, D.n_scale_llt, 0);
+                });
+            if (D.n_ortho)
+                launch("ortho", [&] {
+                    ortho_kernel<T><<<D.n_ortho * nrhs, 128, D.x_smem_ortho, s_>>>(ctx_, X, D.ortho, D.n_ortho, vstore_,
+                                                                                   taustore_, 1);
+                });
+            if (D.merged && D.n_children)
+                launch("merge_x", [&] {
+                    merge_x_kernel<T><<<D.n_children * nrhs, 128, 0, s_>>>(ctx_, X, D.child_idx, D.child_parent,
+                                                                           D.n_children, cpos_, 1);
+                });
         }
         for (int l = P.nlevels - 1; l >= 0; l--) {
             LevelDev& D = levels_[l];
-            if (D.merged && D.n_children) {
-                merge_x_kernel<T><<<D.n_children * nrhs, 128, 0, s_>>>(ctx_, X, D.child_idx, D.child_parent,
-                                                                       D.n_children, cpos_, 0);
-                count_launch();
-            }
-            if (D.n_ortho) {
-                ortho_kernel<T><<<D.n_ortho * nrhs, 128, D.x_smem_ortho, s_>>>(ctx_, X, D.ortho, D.n_ortho, vstore_,
-                                                                               taustore_, 0);
-                count_launch();
-            }
-            if (D.n_scale_llt) {
-                trsv_kernel<T><<<D.n_scale_llt * nrhs, 128, D.x_smem_scale, s_>>>(ctx_, X, D.scale_llt,
-                                                                                  D.scale_llt_blk, D.n_scale_llt, 1);
-                count_launch();
-            }
-            if (D.n_gb) {
-                gemm_bwd_kernel<T><<<D.n_gb * nrhs, 128, 0, s_>>>(ctx_, X, D.gb, D.gbo, D.n_gb);
-                count_launch();
-            }
-            if (D.n_elim_llt) {
-                trsv_kernel<T><<<D.n_elim_llt * nrhs, 128, D.x_smem_elim, s_>>>(ctx_, X, D.elim_llt, D.elim_llt_blk,
-                                                                                D.n_elim_llt, 1);
-                count_launch();
-            }
+            if (D.merged && D.n_children)
+                launch("merge_x", [&] {
+                    merge_x_kernel<T><<<D.n_children * nrhs, 128, 0, s_>>>(ctx_, X, D.child_idx, D.child_parent,
+                                                                           D.n_children, cpos_, 0);
+                });
+            if (D.n_ortho)
+                launch("ortho", [&] {
+                    ortho_kernel<T><<<D.n_ortho * nrhs, 128, D.x_smem_ortho, s_>>>(ctx_, X, D.ortho, D.n_ortho, vstore_,
+                                                                                   taustore_, 0);
+                });
+            if (D.n_scale_llt)
+                launch("trsv", [&] {
+                    trsv_kernel<T><<<D.n_scale_llt * nrhs, 128, D.x_smem_scale, s_>>>(ctx_, X, D.scale_llt,
+                                                                                      D.scale_llt_blk, D.n_scale_llt, 1);
+                });
+            if (D.n_gb)
+                launch("gemm_bwd", [&] { gemm_bwd_kernel<T><<<D.n_gb * nrhs, 128, 0, s_>>>(ctx_, X, D.gb, D.gbo, D.n_gb); });
+            if (D.n_elim_llt)
+                launch("trsv", [&] {
+                    trsv_kernel<T><<<D.n_elim_llt * nrhs, 128, D.x_smem_elim, s_>>>(ctx_, X, D.elim_llt,
+                                                                                    D.elim_llt_blk, D.n_elim_llt, 1);
+                });
         }
-        perm_out_kernel<T><<<(unsigned)((tot + 255) / 256), 256, 0, s_>>>(x, ld, X, d_perm_, d_slot_, n);
-        count_launch();
+        launch("perm", [&] {
+            perm_out_kernel<T><<<(unsigned)((tot + 255) / 256), 256, 0, s_>>>(x, ld, X, d_perm_, d_slot_, n);
+        });
         SPAND_CUDA(cudaGetLastError());
     }
 
     cudaStream_t s_;
     std::vector<int> perm_h_;
+    std::vector<int> caps_h_;
     const Plan* P_ = nullptr;
     int nc_ = 0;
     std::vector<void*> owned_;
     size_t bytes_ = 0;
-    int64_t arena_len_ = 0;
     T* arena_ = nullptr;
+    T* pristine_ = nullptr;
     DBlock* d_blk_ = nullptr;
     int* d_cap_ = nullptr;
     int *csize_ = nullptr, *rows0_ = nullptr, *rank_ = nullptr, *cpos_ = nullptr;
@@ -1467,17 +1537,11 @@ class DeviceFactor : public DeviceFactorBase {
     int x_nrhs_ = 0;
     Ctx<T> ctx_{};
     bool factored_ = false;
-    int64_t launches_ = 0;
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t graph_exec_ = nullptr;
     int64_t graph_kernels_ = 0;
     double* graph_x_ = nullptr;
     int graph_nrhs_ = 0, graph_ld_ = 0;
-
-    friend PcgResult device_pcg(DeviceFactorBase&, const DeviceCsr&, const double*, double*, int, double, bool);
-
-   public:
-    void capture(double* x, int nrhs, int ld) { capture_for(x, nrhs, ld); }
 };
 
 std::unique_ptr<DeviceFactorBase> make_device_factor(bool fp32, cudaStream_t stream, const std::vector<int>& perm) {
@@ -1489,91 +1553,101 @@ void device_spmv(const DeviceCsr& A, const double* x, double* y, cudaStream_t s)
     spmv_kernel<<<(A.n + 255) / 256, 256, 0, s>>>(A.n, A.rowptr, A.colind, A.val, x, y);
 }
 
+// Workspace of the device CG, kept across calls for one matrix size.
+struct PcgWork {
+    int n = 0;
+    double *r = nullptr, *p = nullptr, *z = nullptr, *tmp = nullptr, *partial = nullptr, *sc = nullptr;
+    double* h_sc = nullptr;
+    ~PcgWork() { release(); }
+    void release() {
+        cudaFree(r); cudaFree(p); cudaFree(z); cudaFree(tmp); cudaFree(partial); cudaFree(sc);
+        if (h_sc) cudaFreeHost(h_sc);
+        r = p = z = tmp = partial = sc = h_sc = nullptr;
+        n = 0;
+    }
+    void ensure(int nn) {
+        if (nn == n) return;
+        release();
+        SPAND_CUDA(cudaMalloc(&r, nn * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&p, nn * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&z, nn * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&tmp, nn * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&partial, RED_BLOCKS * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&sc, 8 * sizeof(double)));
+        SPAND_CUDA(cudaMallocHost(&h_sc, 8 * sizeof(double)));
+        n = nn;
+    }
+};
+
+static thread_local PcgWork g_pcg;
+
 // Preconditioned CG (is.cpp:39-121) with all vectors and scalars on the device; one
 // scalar read back per iteration for the stopping test.
 PcgResult device_pcg(DeviceFactorBase& M, const DeviceCsr& A, const double* b, double* x, int maxit, double tol,
                      bool use_graph) {
     cudaStream_t s = M.stream();
+    KernelProfiler& prof = M.profiler();
     const int n = A.n;
     PcgResult res;
-    double *r, *p, *z, *tmp, *partial, *sc;
-    SPAND_CUDA(cudaMalloc(&r, n * sizeof(double)));
-    SPAND_CUDA(cudaMalloc(&p, n * sizeof(double)));
-    SPAND_CUDA(cudaMalloc(&z, n * sizeof(double)));
-    SPAND_CUDA(cudaMalloc(&tmp, n * sizeof(double)));
-    SPAND_CUDA(cudaMalloc(&partial, RED_BLOCKS * sizeof(double)));
-    SPAND_CUDA(cudaMalloc(&sc, 8 * sizeof(double)));
-    double* h_sc = nullptr;
-    SPAND_CUDA(cudaMallocHost(&h_sc, 8 * sizeof(double)));
-    auto dot = [&](const double* a, const double* bb, int slot) {
-        dot_partial_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, a, bb, partial);
-        dot_final_kernel<<<1, RED_THREADS, 0, s>>>(partial, RED_BLOCKS, sc + slot);
+    g_pcg.ensure(n);
+    double *r = g_pcg.r, *p = g_pcg.p, *z = g_pcg.z, *tmp = g_pcg.tmp, *partial = g_pcg.partial, *sc = g_pcg.sc;
+    double* h_sc = g_pcg.h_sc;
+    auto L = [&](const char* cls, auto&& f, int k = 1) {
+        prof.begin(s, cls);
+        f();
+        prof.end(s);
+        M.add_launches(k);
     };
     const unsigned gb = (unsigned)((n + 255) / 256);
-    auto cleanup = [&]() {
-        cudaFree(r);
-        cudaFree(p);
-        cudaFree(z);
-        cudaFree(tmp);
-        cudaFree(partial);
-        cudaFree(sc);
-        cudaFreeHost(h_sc);
+    auto dot = [&](const double* a, const double* bb, int slot) {
+        L("dot", [&] {
+            dot_partial_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, a, bb, partial);
+            dot_final_kernel<<<1, RED_THREADS, 0, s>>>(partial, RED_BLOCKS, sc + slot);
+        }, 2);
     };
-    try {
-        // r = b - A x ; rhsNorm2 ; residualNorm2
-        spmv_kernel<<<gb, 256, 0, s>>>(n, A.rowptr, A.colind, A.val, x, tmp);
-        sub_kernel<<<gb, 256, 0, s>>>(n, b, tmp, r);
-        dot(b, b, 4);
-        dot(r, r, 2);
-        SPAND_CUDA(cudaMemcpyAsync(h_sc, sc, 8 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    auto spmv = [&](const double* in, double* out) {
+        L("spmv", [&] { spmv_kernel<<<gb, 256, 0, s>>>(n, A.rowptr, A.colind, A.val, in, out); });
+    };
+    spmv(x, tmp);
+    L("axpy", [&] { sub_kernel<<<gb, 256, 0, s>>>(n, b, tmp, r); });
+    dot(b, b, 4);
+    dot(r, r, 2);
+    SPAND_CUDA(cudaMemcpyAsync(h_sc, sc, 8 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    SPAND_CUDA(cudaStreamSynchronize(s));
+    const double rhsNorm2 = h_sc[4];
+    if (rhsNorm2 == 0) {
+        SPAND_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
         SPAND_CUDA(cudaStreamSynchronize(s));
-        const double rhsNorm2 = h_sc[4];
-        if (rhsNorm2 == 0) {
-            SPAND_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
-            cleanup();
-            return res;
-        }
-        const double threshold = tol * tol * rhsNorm2;
-        double resNorm2 = h_sc[2];
-        res.relres = std::sqrt(resNorm2 / rhsNorm2);
-        if (resNorm2 < threshold) {
-            cleanup();
-            return res;
-        }
-        SPAND_CUDA(cudaMemcpyAsync(p, r, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-        M.solve_device(p, 1, n);
-        dot(r, p, 0);
-        DeviceFactor<double>* fd = dynamic_cast<DeviceFactor<double>*>(&M);
-        DeviceFactor<float>* ff = dynamic_cast<DeviceFactor<float>*>(&M);
-        if (use_graph) {
-            if (fd) fd->capture(z, 1, n);
-            if (ff) ff->capture(z, 1, n);
-        }
-        int i = 0;
-        while (i < maxit) {
-            spmv_kernel<<<gb, 256, 0, s>>>(n, A.rowptr, A.colind, A.val, p, tmp);
-            dot(p, tmp, 1);
-            cg_update_xr_kernel<<<gb, 256, 0, s>>>(n, x, r, p, tmp, sc);
-            dot(r, r, 2);
-            SPAND_CUDA(cudaMemcpyAsync(h_sc + 2, sc + 2, sizeof(double), cudaMemcpyDeviceToHost, s));
-            SPAND_CUDA(cudaStreamSynchronize(s));
-            resNorm2 = h_sc[2];
-            if (resNorm2 < threshold) break;
-            SPAND_CUDA(cudaMemcpyAsync(z, r, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-            M.solve_device(z, 1, n);
-            copy_scalar_kernel<<<1, 1, 0, s>>>(sc, 3, 0);
-            dot(r, z, 0);
-            cg_update_p_kernel<<<gb, 256, 0, s>>>(n, p, z, sc);
-            i++;
-        }
-        SPAND_CUDA(cudaGetLastError());
-        res.iterations = i + 1;
-        res.relres = std::sqrt(resNorm2 / rhsNorm2);
-    } catch (...) {
-        cleanup();
-        throw;
+        return res;
     }
-    cleanup();
+    const double threshold = tol * tol * rhsNorm2;
+    double resNorm2 = h_sc[2];
+    res.relres = std::sqrt(resNorm2 / rhsNorm2);
+    if (resNorm2 < threshold) return res;
+    SPAND_CUDA(cudaMemcpyAsync(p, r, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    M.solve_device(p, 1, n);
+    dot(r, p, 0);
+    if (use_graph) M.capture_solve(z, 1, n);
+    int i = 0;
+    while (i < maxit) {
+        spmv(p, tmp);
+        dot(p, tmp, 1);
+        L("axpy", [&] { cg_update_xr_kernel<<<gb, 256, 0, s>>>(n, x, r, p, tmp, sc); });
+        dot(r, r, 2);
+        SPAND_CUDA(cudaMemcpyAsync(h_sc + 2, sc + 2, sizeof(double), cudaMemcpyDeviceToHost, s));
+        SPAND_CUDA(cudaStreamSynchronize(s));
+        resNorm2 = h_sc[2];
+        if (resNorm2 < threshold) break;
+        SPAND_CUDA(cudaMemcpyAsync(z, r, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        M.solve_device(z, 1, n);
+        L("axpy", [&] { copy_scalar_kernel<<<1, 1, 0, s>>>(sc, 3, 0); });
+        dot(r, z, 0);
+        L("axpy", [&] { cg_update_p_kernel<<<gb, 256, 0, s>>>(n, p, z, sc); });
+        i++;
+    }
+    SPAND_CUDA(cudaGetLastError());
+    res.iterations = i + 1;
+    res.relres = std::sqrt(resNorm2 / rhsNorm2);
     return res;
 }
 

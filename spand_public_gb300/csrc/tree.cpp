@@ -59,6 +59,20 @@ std::vector<ClusterID> Tree::partition(const Csc& A) {
     return part_;
 }
 
+// Values of A in CSR order (A structurally symmetric: the CSR pattern is the transpose
+// of the CSC pattern).
+static std::vector<double> csr_val_of(const Csc& A) {
+    const int n = A.n;
+    std::vector<int> fill(n + 1, 0);
+    for (int j = 0; j < n; j++)
+        for (int k = A.colptr[j]; k < A.colptr[j + 1]; k++) fill[A.rowval[k] + 1]++;
+    for (int i = 0; i < n; i++) fill[i + 1] += fill[i];
+    std::vector<double> vv(A.rowval.size());
+    for (int j = 0; j < n; j++)
+        for (int k = A.colptr[j]; k < A.colptr[j + 1]; k++) vv[fill[A.rowval[k]]++] = A.val[k];
+    return vv;
+}
+
 // tree.cpp:505-575, plus the symbolic plan of factorize() and the device upload.
 void Tree::assemble(const Csc& A) {
     if (!partitioned_) throw std::logic_error("assemble() before partition()");
@@ -66,8 +80,25 @@ void Tree::assemble(const Csc& A) {
         throw std::invalid_argument("the device path implements the SPD / LLT configuration");
     if (A.n != get_N()) throw std::invalid_argument("matrix size does not match the partition");
     double t0 = now_s();
+    const bool same_pattern = assembled_ok_ && dev_ && A.colptr == A_.colptr && A.rowval == A_.rowval;
     A_ = A;
     Csc App = spand::symm_perm(A, perm_);
+    if (same_pattern) {
+        // same sparsity pattern: keep the symbolic plan and the device work lists,
+        // re-assemble the block values only
+        spand::fill_assembled_blocks(plan_, H_, asmb_, App, assembled_);
+        try {
+            dev_->upload_values(assembled_);
+        } catch (spand::DeviceError& e) {
+            throw std::runtime_error(e.msg);
+        }
+        cuda_check(cudaMemcpyAsync(dA_.val, csr_val_of(A).data(), A.rowval.size() * sizeof(double),
+                                   cudaMemcpyHostToDevice, stream_), "H2D");
+        cuda_check(cudaStreamSynchronize(stream_), "sync");
+        factored_ = false;
+        t_assemble = now_s() - t0;
+        return;
+    }
     asmb_ = spand::assembly_structure(H_, App, true);
     plan_ = spand::build_plan(H_, asmb_, skip_, use_want_sparsify_);
     spand::fill_assembled_blocks(plan_, H_, asmb_, App, assembled_);
@@ -113,12 +144,6 @@ void Tree::factorize() {
     if (!assembled_ok_) throw std::logic_error("factorize() before assemble()");
     double t0 = now_s();
     try {
-        if (factored_) {
-            // re-factorize from the assembled values
-            dev_.reset();
-            dev_ = spand::make_device_factor(fp32_, stream_, perm_);
-            dev_->upload(plan_, assembled_);
-        }
         dev_->factorize(tol_);
     } catch (spand::DeviceError& e) {
         if (e.status == spand::SPAND_ERR_NOT_SPD) {
@@ -292,6 +317,109 @@ void Tree::op_tau(int idx, std::vector<double>& out) const {
     std::vector<double> v, tau;
     dev_->ortho(r.block, v, tau);
     out.assign(tau.begin(), tau.begin() + r.cols);
+}
+
+static void add_work(std::vector<Tree::Work>& w, const char* cls, double bytes, double flops) {
+    for (auto& e : w)
+        if (e.cls == cls) {
+            e.bytes += bytes;
+            e.flops += flops;
+            return;
+        }
+    w.push_back({cls, bytes, flops});
+}
+
+std::vector<Tree::Work> Tree::work_factor() const {
+    std::vector<Work> w;
+    if (!factored_) return w;
+    const spand::Plan& P = plan_;
+    const double sz = dev_->precision_bytes();
+    auto r0 = [&](int c) { return (double)rows0_[c]; };
+    for (int l = 0; l < P.nlevels; l++) {
+        const spand::LevelPlan& L = P.levels[l];
+        auto potrf = [&](const std::vector<int>& cl) {
+            for (int c : cl) {
+                double n = r0(c);
+                add_work(w, "potrf", 2 * n * n * sz, n * n * n / 3);
+            }
+        };
+        auto trsm = [&](const std::vector<spand::TrsmItem>& items) {
+            for (const auto& t : items) {
+                const spand::PlanBlock& B = P.blocks[t.block];
+                double n = r0(t.cluster);
+                double m = t.side == 0 ? r0(B.colc) : r0(B.rowc);
+                add_work(w, "trsm", (2 * m * n + n * (n + 1) / 2) * sz, m * n * n);
+            }
+        };
+        potrf(L.elim_clusters);
+        trsm(L.elim_trsm);
+        for (int t = 0; t < L.schur_count; t++) {
+            const spand::SchurTarget& st = P.schur_targets[L.schur_first + t];
+            const spand::PlanBlock& B = P.blocks[st.target];
+            double M = r0(B.rowc), N = r0(B.colc);
+            double bytes = 2 * M * N * sz, flops = 0;
+            for (int u = 0; u < st.count; u++) {
+                double S = r0(P.schur_updates[st.first + u].s);
+                bytes += (M + N) * S * sz;
+                flops += st.syrk ? M * M * S : 2 * M * N * S;
+            }
+            add_work(w, "schur", bytes, flops);
+        }
+        potrf(L.scale_clusters);
+        trsm(L.scale_trsm);
+        std::map<int, int> wave_of;
+        for (size_t wv = 0; wv < L.waves.size(); wv++)
+            for (const auto& it : L.waves[wv]) wave_of[it.cluster] = (int)wv;
+        for (const auto& wave : L.waves)
+            for (const auto& it : wave) {
+                double rows = r0(it.cluster), k = csize_[it.cluster], cols = 0;
+                for (int p = 0; p < it.count; p++) {
+                    int n = P.asn_pieces[it.first + p].nbr;
+                    auto wn = wave_of.find(n);
+                    cols += (wn != wave_of.end() && wn->second < wave_of[it.cluster]) ? csize_[n] : rows0_[n];
+                }
+                double kk = std::min(k, std::min(rows, cols));
+                add_work(w, "asn_gather", 2 * rows * cols * sz, 0);
+                add_work(w, "qrcp", 2 * rows * cols * sz,
+                         4 * rows * cols * kk - 2 * kk * kk * (rows + cols) + 4 * kk * kk * kk / 3);
+                if (k < rows) add_work(w, "sparsify_scatter", (2 * rows * k + 2 * k * cols) * sz, 0);
+            }
+        for (const auto& m : L.merge_copies) add_work(w, "merge_copy", 2.0 * csize_[m.nold] * csize_[m.sold] * sz, 0);
+    }
+    return w;
+}
+
+std::vector<Tree::Work> Tree::work_solve() const {
+    std::vector<Work> w;
+    if (!factored_) return w;
+    const spand::Plan& P = plan_;
+    const double sz = dev_->precision_bytes();
+    // both sweeps
+    for (int l = 0; l < P.nlevels; l++) {
+        const spand::LevelPlan& L = P.levels[l];
+        for (int c : L.op_elim_llt) {
+            double n = rows0_[c];
+            add_work(w, "trsv", 2 * (n * (n + 1) / 2 + 2 * n) * sz, 2 * n * n);
+        }
+        for (int c : L.op_scale_llt) {
+            double n = rows0_[c];
+            add_work(w, "trsv", 2 * (n * (n + 1) / 2 + 2 * n) * sz, 2 * n * n);
+        }
+        for (const auto& g : L.op_gemm) {
+            double a = rows0_[g.self], b = rows0_[g.nbr];
+            add_work(w, "gemm_fwd", (a * b + a + 2 * b) * sz, 2 * a * b);
+            add_work(w, "gemm_bwd", (a * b + 2 * a + b) * sz, 2 * a * b);
+        }
+        for (int c : L.op_ortho) {
+            double rows = rows0_[c], k = csize_[c];
+            if (k < rows) add_work(w, "ortho", 2 * (rows * k + 2 * rows) * sz, 2 * 4 * rows * k);
+        }
+        for (int p : L.op_merge)
+            for (int ch : P.c_children[p]) add_work(w, "merge_x", 2 * 2.0 * csize_[ch] * sz, 0);
+    }
+    const double n = get_N();
+    add_work(w, "perm", 2 * n * (8 + 4 + 8 + sz), 0);
+    return w;
 }
 
 int cg(const Csc& A, const double* rhs, double* x, const Tree& precond, int iters, double tol, bool verb,

@@ -87,6 +87,16 @@ class Tree {
     spand::DeviceCsr device_csr() const { return dA_; }
     size_t device_bytes() const;
 
+    // Algorithmic work per kernel class for one factorization and for one solve with one
+    // right-hand side: (class, bytes, flops).  Bytes count each operand read or written
+    // once; flops use the standard LAPACK counts (QRCP truncated at the rank).
+    struct Work {
+        std::string cls;
+        double bytes = 0, flops = 0;
+    };
+    std::vector<Work> work_factor() const;
+    std::vector<Work> work_solve() const;
+
    private:
     void build_ops_and_log();
 
