@@ -1,0 +1,360 @@
+#!/usr/bin/env python
+"""Benchmark of the spaND factorization + PCG hot path on GB300.
+
+Metric: seconds for factorize + preconditioned CG to an FP64 relative residual of 1e-10
+on the 3D 7-point Laplacian 64^3 (n = 262,144), 12 nested-dissection levels,
+eps = 1e-2, one N(0,1) right-hand side -- the mixed-precision path (FP32 factor, FP64
+CG).  The plain FP64 path is timed beside it.  A step = one factorization (from the
+assembled blocks, resident in HBM) + one CG solve.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line.  Under torchrun (N > 1) every rank runs an independent replica on
+its own GPU (the path has no data exchange) and the time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "factor+PCG seconds to 1e-10 FP64 rel. residual (3D 7-pt Laplacian 64^3, eps=1e-2)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--levels", type=int, default=12)
+    ap.add_argument("--eps", type=float, default=1e-2)
+    ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--maxit", type=int, default=200)
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(args):
+    from spand_public_gb300 import problems as P
+
+    A = P.neglapl(args.n, 3)
+    X = P.linspace_nd(args.n, 3)
+    b = P.rhs(A.shape[0], 1, seed=0)[:, 0].copy()
+    return A, X, b
+
+
+def config(args, extra=None):
+    c = {"workload": f"3d 7-point -Laplacian {args.n}^3 (n={args.n ** 3}), {args.levels} ND levels, eps={args.eps:g}, "
+                     f"1 RHS N(0,1) seed 0, PCG to {args.tol:g}",
+         "grid": args.n, "levels": args.levels, "eps": args.eps, "nrhs": 1, "pcg_tol": args.tol,
+         "ordering": "geometric modified nested dissection",
+         "l2": "working set larger than L2 (factor arena of several GB)"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+# --------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p.get("hbm_gbs", 6800.0), p.get("bf16_tflops", 1900.0), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+def ncu_traffic(cls: str):
+    """DRAM bytes per launch of a kernel class from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(cls)
+    except Exception:
+        return None
+
+
+# --------------------------------------------------------------------------------------
+def make_tree(A, X, args, fp32: bool):
+    import spand_public_gb300 as pkg
+
+    t = pkg.Tree(args.levels)
+    t.set_verb(False)
+    t.set_use_geo(True)
+    t.set_Xcoo(X)
+    t.set_tol(args.eps)
+    t.set_fp32(fp32)
+    t.partition(A)
+    t.assemble(A)
+    return t
+
+
+def cpu_oracle_solve(A, X, b, args):
+    """The oracle (C++ restatement of the reference, one thread): factorize + CG."""
+    from oracle.oracle import OracleTree
+
+    o = OracleTree(args.levels)
+    o.set_Xcoo(X)
+    o.set_tol(args.eps)
+    o.partition(A)
+    o.assemble(A)
+    t0 = time.perf_counter()
+    o.factorize()
+    x, it = o.cg(b, args.maxit, args.tol)
+    t1 = time.perf_counter()
+    rel = float(np.linalg.norm(A @ x - b) / np.linalg.norm(b))
+    return t1 - t0, it, rel
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    A, X, b = workload(args)
+    # each step is one full factor + CG of the 64^3 problem (~10-20 s on one core);
+    # the run is capped at about three minutes
+    steps_run, times, its, rels = 0, [], [], []
+    budget = 180.0
+    t_start = time.perf_counter()
+    warm = min(args.warmup, 0)
+    for _ in range(warm):
+        cpu_oracle_solve(A, X, b, args)
+    while steps_run < args.steps:
+        s, it, rel = cpu_oracle_solve(A, X, b, args)
+        times.append(s)
+        its.append(it)
+        rels.append(rel)
+        steps_run += 1
+        if time.perf_counter() - t_start + s > budget:
+            break
+    v = float(np.mean(times))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": world, "steps": steps_run,
+            "warmup": warm, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config(args, {"pcg_iterations": its[-1], "true_relres": rels[-1]}),
+            "cpu_baseline": {"value": v, "unit": "s", "cores": 1, "kind": "port",
+                             "sample": f"{steps_run} full factor+CG solve(s) of the {args.n}^3 problem; the reference "
+                                       "cannot be built here (no Eigen/METIS/LAPACKE), so its C++ restatement runs, "
+                                       "single-threaded like the reference"},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args, rank, world, local_rank):
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+    A, X, b = workload(args)
+    N = A.shape[0]
+    t_analysis0 = time.perf_counter()
+    t32 = make_tree(A, X, args, fp32=True)
+    t_analysis = time.perf_counter() - t_analysis0
+    b_dev = torch.from_numpy(b).to(dev)
+    x_dev = torch.zeros_like(b_dev)
+    for _ in range(args.warmup):
+        t32.bench_step(b_dev.data_ptr(), x_dev.data_ptr(), args.maxit, args.tol)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t32.launches(reset=True)
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    steps = []
+    for _ in range(args.steps):
+        steps.append(t32.bench_step(b_dev.data_ptr(), x_dev.data_ptr(), args.maxit, args.tol))
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = t32.launches(reset=True) / max(args.steps, 1)
+    step_s = [(s["factor_ms"] + s["pcg_ms"]) / 1e3 for s in steps]
+    value = float(np.mean(step_s))
+    if dist:
+        tv = torch.tensor([value], device=dev, dtype=torch.float64)
+        dist.all_reduce(tv, op=dist.ReduceOp.MAX)
+        value = float(tv.item())
+    x = x_dev.cpu().numpy()
+    true_rel = float(np.linalg.norm(A @ x - b) / np.linalg.norm(b))
+    factor_ms = float(np.mean([s["factor_ms"] for s in steps]))
+    pcg_ms = float(np.mean([s["pcg_ms"] for s in steps]))
+    iters = steps[-1]["iterations"]
+
+    # profiled step (CUDA events around every launch): per-kernel-class time
+    t32.set_profiling(True)
+    prof_step = t32.bench_step(b_dev.data_ptr(), x_dev.data_ptr(), args.maxit, args.tol)
+    prof = t32.profile()
+    t32.set_profiling(False)
+    wf = t32.work("factor")
+    ws = t32.work("solve")
+    n_solves = prof.get("perm", {}).get("launches", 0) // 2
+    hbm, bf16, peak_kind = peaks()
+    kernels = {}
+    for cls, p in prof.items():
+        if cls in wf:
+            by, fl = wf[cls]["bytes"], wf[cls]["flops"]
+        elif cls in ws:
+            by, fl = ws[cls]["bytes"] * n_solves, ws[cls]["flops"] * n_solves
+        else:
+            by, fl = None, None
+        e = {"launches": p["launches"], "ms": round(p["ms"], 4)}
+        if by is not None and p["ms"] > 0:
+            e["gbs"] = round(by / (p["ms"] * 1e-3) / 1e9, 1)
+            e["gflops"] = round(fl / (p["ms"] * 1e-3) / 1e9, 1)
+        kernels[cls] = e
+    total_prof = sum(p["ms"] for p in prof.values())
+    dom = max((c for c in prof if c != "restore"), key=lambda c: prof[c]["ms"])
+    dom_by = wf[dom]["bytes"] if dom in wf else ws.get(dom, {}).get("bytes", 0) * n_solves
+    dom_launches = prof[dom]["launches"]
+    dom_avg_ms = prof[dom]["ms"] / max(dom_launches, 1)
+    achieved = (dom_by / max(dom_launches, 1)) / (dom_avg_ms * 1e-3) / 1e9 if dom_avg_ms > 0 else 0.0
+    traffic = ncu_traffic(dom)
+    roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 4), "peak_source": peak_kind,
+                "traffic": traffic, "bytes_per_launch": dom_by / max(dom_launches, 1),
+                "avg_launch_ms": dom_avg_ms, "share_of_step": round(prof[dom]["ms"] / max(total_prof, 1e-9), 3)}
+
+    # plain FP64 path, same workload
+    fp64 = None
+    if args.fp64_steps > 0:
+        t64 = make_tree(A, X, args, fp32=False)
+        t64.bench_step(b_dev.data_ptr(), x_dev.data_ptr(), args.maxit, args.tol)
+        s64 = [t64.bench_step(b_dev.data_ptr(), x_dev.data_ptr(), args.maxit, args.tol) for _ in range(args.fp64_steps)]
+        x64 = x_dev.cpu().numpy()
+        fp64 = {"seconds": float(np.mean([(s["factor_ms"] + s["pcg_ms"]) / 1e3 for s in s64])),
+                "factor_ms": float(np.mean([s["factor_ms"] for s in s64])),
+                "pcg_ms": float(np.mean([s["pcg_ms"] for s in s64])),
+                "pcg_iterations": s64[-1]["iterations"],
+                "true_relres": float(np.linalg.norm(A @ x64 - b) / np.linalg.norm(b))}
+        t64.close()
+
+    # end to end through the C ABI with host buffers: values upload (assemble on the
+    # cached plan), factorize, CG with host b -> host x
+    e2e_t = []
+    for k in range(max(args.steps, 1)):
+        t0 = time.perf_counter()
+        t32.assemble(A)
+        t32.factorize()
+        xh, it_h, _ = t32.cg(b, args.maxit, args.tol)
+        e2e_t.append(time.perf_counter() - t0)
+    h2d = t32.assembled_bytes() + A.nnz * 8 + b.nbytes * 2  # block values, CSR values, b and x0
+    d2h = xh.nbytes
+    e2e = {"value": float(np.mean(e2e_t)), "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+           "pcg_iterations": it_h, "true_relres": float(np.linalg.norm(A @ xh - b) / np.linalg.norm(b))}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        s, it_c, rel_c = cpu_oracle_solve(A, X, b, args)
+        cpu = {"value": s, "unit": "s", "cores": 1, "kind": "port",
+               "sample": f"one full factor+CG solve of the same {args.n}^3 problem by the oracle (C++ restatement "
+                         f"of the reference, one thread): {it_c} CG iterations, true relres {rel_c:.2e}"}
+
+    if rank == 0:
+        extra = {"pcg_iterations": iters, "true_relres": true_rel, "factor_ms": factor_ms, "pcg_ms": pcg_ms,
+                 "analysis_s": t_analysis, "precision": "FP32 factor (SIMT), FP64 CG/SpMV/dots",
+                 "plain_fp64": fp64,
+                 "speedup_vs_plain_fp64": (fp64["seconds"] / value) if fp64 else None,
+                 "kernels": kernels, "profiled_step_ms": prof_step["factor_ms"] + prof_step["pcg_ms"],
+                 "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"}
+        line = {"metric": METRIC, "value": value, "unit": "s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config(args, extra),
+                "e2e": e2e, "gpu_launches": int(round(launches)), "roofline": roofline, "cpu_baseline": cpu,
+                "clocks": clk}
+        print(json.dumps(line), flush=True)
+    t32.close()
+    return 0
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    try:
+        return run_gb300(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

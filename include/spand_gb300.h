@@ -107,6 +107,22 @@ int spand_tree_timings(spand_tree* t, double* out);
 int spand_tree_launches(spand_tree* t, long long* n, int reset);
 int spand_tree_device_bytes(spand_tree* t, long long* bytes);
 
+/* No reference counterpart -- measurement hooks used by bench.py:
+ * one factorize() + device CG on device vectors b_dev / x_dev (x_dev is zeroed first),
+ * timed with CUDA events on the tree's stream.  out[4]: factor ms, CG ms, iterations,
+ * |r|/|b| of the recurrence residual. */
+int spand_tree_bench_step(spand_tree* t, const double* b_dev, double* x_dev, int iters, double tol, double* out);
+/* Bytes uploaded by assemble() for the block values (the factorization's device input). */
+int spand_tree_assembled_bytes(spand_tree* t, long long* bytes);
+/* Per-kernel-class device time (CUDA events around every launch while enabled). */
+int spand_tree_set_profiling(spand_tree* t, int on);
+int spand_tree_profile_count(spand_tree* t, int* n); /* collects pending records */
+int spand_tree_profile_entry(spand_tree* t, int idx, char* name64, long long* launches, double* ms);
+int spand_tree_profile_reset(spand_tree* t);
+/* Algorithmic bytes and flops per kernel class: which = 0 one factorization, 1 one solve. */
+int spand_tree_work_count(spand_tree* t, int which, int* n);
+int spand_tree_work_entry(spand_tree* t, int which, int idx, char* name64, double* bytes, double* flops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -68,6 +68,16 @@ _PROTOS = {
     "spand_tree_timings": (C.c_int, [C.c_void_p, C.c_void_p]),
     "spand_tree_launches": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.c_int]),
     "spand_tree_device_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
+    "spand_tree_bench_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p]),
+    "spand_tree_assembled_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
+    "spand_tree_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "spand_tree_profile_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "spand_tree_profile_entry": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.POINTER(C.c_longlong),
+                                           C.POINTER(C.c_double)]),
+    "spand_tree_profile_reset": (C.c_int, [C.c_void_p]),
+    "spand_tree_work_count": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
+    "spand_tree_work_entry": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_char_p, C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double)]),
 }
 
 
@@ -251,6 +261,48 @@ class Tree:
         v = C.c_longlong()
         _check(self.L.spand_tree_launches(self.h, C.byref(v), int(bool(reset))))
         return v.value
+
+    def bench_step(self, b_ptr: int, x_ptr: int, iters=200, tol=1e-10):
+        """factorize + device CG, timed with CUDA events on the tree's stream."""
+        out = np.zeros(4)
+        _check(self.L.spand_tree_bench_step(self.h, C.c_void_p(b_ptr), C.c_void_p(x_ptr), int(iters), float(tol),
+                                            _ptr(out)))
+        return dict(factor_ms=out[0], pcg_ms=out[1], iterations=int(out[2]), relres=out[3])
+
+    def assembled_bytes(self):
+        v = C.c_longlong()
+        _check(self.L.spand_tree_assembled_bytes(self.h, C.byref(v)))
+        return v.value
+
+    def set_profiling(self, on: bool):
+        _check(self.L.spand_tree_set_profiling(self.h, int(bool(on))))
+
+    def profile(self, reset=True):
+        n = C.c_int()
+        _check(self.L.spand_tree_profile_count(self.h, C.byref(n)))
+        out = {}
+        for i in range(n.value):
+            name = C.create_string_buffer(64)
+            la = C.c_longlong()
+            ms = C.c_double()
+            _check(self.L.spand_tree_profile_entry(self.h, i, name, C.byref(la), C.byref(ms)))
+            out[name.value.decode()] = dict(launches=la.value, ms=ms.value)
+        if reset:
+            _check(self.L.spand_tree_profile_reset(self.h))
+        return out
+
+    def work(self, which: str = "factor"):
+        w = 0 if which == "factor" else 1
+        n = C.c_int()
+        _check(self.L.spand_tree_work_count(self.h, w, C.byref(n)))
+        out = {}
+        for i in range(n.value):
+            name = C.create_string_buffer(64)
+            b = C.c_double()
+            f = C.c_double()
+            _check(self.L.spand_tree_work_entry(self.h, w, i, name, C.byref(b), C.byref(f)))
+            out[name.value.decode()] = dict(bytes=b.value, flops=f.value)
+        return out
 
     def device_bytes(self):
         v = C.c_longlong()

@@ -241,4 +241,61 @@ int spand_tree_launches(spand_tree* t, long long* n, int reset) {
 }
 int spand_tree_device_bytes(spand_tree* t, long long* b) { CHECK_T(t); *b = (long long)t->t->device_bytes(); return SPAND_OK; }
 
+int spand_tree_bench_step(spand_tree* t, const double* b, double* x, int iters, double tol, double* out) {
+    CHECK_T(t);
+    if (!b || !x || !out) return fail(SPAND_ERR_ARG, "null argument");
+    return guard([&] { t->t->bench_step(b, x, iters, tol, out); });
+}
+int spand_tree_assembled_bytes(spand_tree* t, long long* b) {
+    CHECK_T(t);
+    if (!t->t->device()) return fail(SPAND_ERR_STATE, "before assemble");
+    *b = (long long)t->t->plan().assembled_len * t->t->device()->precision_bytes();
+    return SPAND_OK;
+}
+int spand_tree_set_profiling(spand_tree* t, int on) {
+    CHECK_T(t);
+    if (!t->t->device()) return fail(SPAND_ERR_STATE, "profiling before assemble");
+    t->t->device()->profiler().enable(on != 0);
+    return SPAND_OK;
+}
+int spand_tree_profile_count(spand_tree* t, int* n) {
+    CHECK_T(t);
+    if (!t->t->device()) return fail(SPAND_ERR_STATE, "profiling before assemble");
+    return guard([&] {
+        t->t->device()->profiler().collect();
+        *n = (int)t->t->device()->profiler().totals().size();
+    });
+}
+int spand_tree_profile_entry(spand_tree* t, int idx, char* name, long long* launches, double* ms) {
+    CHECK_T(t);
+    if (!t->t->device()) return fail(SPAND_ERR_STATE, "profiling before assemble");
+    const auto& v = t->t->device()->profiler().totals();
+    if (idx < 0 || idx >= (int)v.size()) return fail(SPAND_ERR_ARG, "index out of range");
+    std::strncpy(name, v[idx].cls.c_str(), 63);
+    name[63] = 0;
+    *launches = v[idx].launches;
+    *ms = v[idx].ms;
+    return SPAND_OK;
+}
+int spand_tree_profile_reset(spand_tree* t) {
+    CHECK_T(t);
+    if (t->t->device()) t->t->device()->profiler().clear();
+    return SPAND_OK;
+}
+int spand_tree_work_count(spand_tree* t, int which, int* n) {
+    CHECK_T(t);
+    return guard([&] { *n = (int)(which ? t->t->work_solve() : t->t->work_factor()).size(); });
+}
+int spand_tree_work_entry(spand_tree* t, int which, int idx, char* name, double* bytes, double* flops) {
+    CHECK_T(t);
+    return guard([&] {
+        auto v = which ? t->t->work_solve() : t->t->work_factor();
+        if (idx < 0 || idx >= (int)v.size()) throw std::invalid_argument("index out of range");
+        std::strncpy(name, v[idx].cls.c_str(), 63);
+        name[63] = 0;
+        *bytes = v[idx].bytes;
+        *flops = v[idx].flops;
+    });
+}
+
 }  // extern "C"

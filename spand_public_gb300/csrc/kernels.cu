@@ -1259,6 +1259,9 @@ class DeviceFactor : public DeviceFactorBase {
 
     void capture_solve(double* x, int nrhs, int ld) override {
         if (!factored_) throw DeviceError{SPAND_ERR_STATE, "solve before factorize"};
+        // the graph reads every size from device memory, so it stays valid across
+        // re-factorizations with the same plan
+        if (graph_exec_ && graph_x_ == x && graph_nrhs_ == nrhs && graph_ld_ == ld) return;
         ensure_x(nrhs);
         if (graph_exec_) {
             cudaGraphExecDestroy(graph_exec_);

@@ -154,8 +154,37 @@ void Tree::factorize() {
     }
     t_factorize = now_s() - t0;
     factored_ = true;
-    dev_->sizes(csize_, rows0_);
-    build_ops_and_log();
+    log_dirty_ = true;
+}
+
+void Tree::bench_step(const double* b_dev, double* x_dev, int iters, double tol, double out[4]) {
+    if (!assembled_ok_) throw std::logic_error("bench_step() before assemble()");
+    cudaEvent_t e[3];
+    for (auto& ev : e) cuda_check(cudaEventCreate(&ev), "cudaEventCreate");
+    spand::PcgResult r;
+    try {
+        cuda_check(cudaEventRecord(e[0], stream_), "cudaEventRecord");
+        dev_->factorize(tol_);
+        factored_ = true;
+        log_dirty_ = true;
+        cuda_check(cudaEventRecord(e[1], stream_), "cudaEventRecord");
+        cuda_check(cudaMemsetAsync(x_dev, 0, get_N() * sizeof(double), stream_), "cudaMemsetAsync");
+        r = spand::device_pcg(*dev_, dA_, b_dev, x_dev, iters, tol, true);
+        cuda_check(cudaEventRecord(e[2], stream_), "cudaEventRecord");
+        cuda_check(cudaEventSynchronize(e[2]), "cudaEventSynchronize");
+    } catch (spand::DeviceError& err) {
+        for (auto& ev : e) cudaEventDestroy(ev);
+        if (err.status == spand::SPAND_ERR_NOT_SPD) throw std::runtime_error("Error: Non-SPD Pivot\n");
+        throw std::runtime_error(err.msg);
+    }
+    float f = 0, p = 0;
+    cudaEventElapsedTime(&f, e[0], e[1]);
+    cudaEventElapsedTime(&p, e[1], e[2]);
+    for (auto& ev : e) cudaEventDestroy(ev);
+    out[0] = f;
+    out[1] = p;
+    out[2] = r.iterations;
+    out[3] = r.relres;
 }
 
 void Tree::solve_device(double* x, int nrhs, int ld) const {
@@ -186,7 +215,15 @@ size_t Tree::device_bytes() const { return dev_ ? dev_->device_bytes() : 0; }
 // Op list and per-level log reconstructed from the plan and the device sizes, in the
 // reference's recording order (tree.cpp:909-910, 885-892, 810, 1331, 1102, 1342, 1439).
 void Tree::build_ops_and_log() {
+    log_dirty_ = false;
+    dev_->sizes(csize_, rows0_);
     ops_.clear();
+    for (LevelLog& G : log_) {  // keep the partition counts, recompute the rest
+        LevelLog fresh;
+        fresh.dofs_nd = G.dofs_nd;
+        fresh.dofs_left_nd = G.dofs_left_nd;
+        G = fresh;
+    }
     const spand::Plan& P = plan_;
     int next_order = P.nclusters;  // siblings are numbered after all clusters
     long long nnz = 0;
@@ -265,11 +302,13 @@ void Tree::build_ops_and_log() {
 }
 
 long long Tree::nnz() const {
+    ensure_log();
     return log_.empty() ? 0 : log_.back().fact_nnz;
 }
 
 // tree.cpp:158-169
 int Tree::get_stop() const {
+    ensure_log();
     int stop = get_N();
     for (const LevelLog& l : log_) {
         if (l.dofs_left_elim > 0) stop = std::min<long long>(stop, l.dofs_left_elim);
@@ -279,6 +318,7 @@ int Tree::get_stop() const {
 }
 
 std::vector<std::array<int, 4>> Tree::ranks() const {
+    ensure_log();
     std::vector<std::array<int, 4>> r;
     for (int l = 0; l < plan_.nlevels; l++)
         for (int c : plan_.levels[l].op_ortho) r.push_back({l, c, rows0_[c], csize_[c]});
@@ -332,6 +372,7 @@ static void add_work(std::vector<Tree::Work>& w, const char* cls, double bytes, 
 std::vector<Tree::Work> Tree::work_factor() const {
     std::vector<Work> w;
     if (!factored_) return w;
+    ensure_log();
     const spand::Plan& P = plan_;
     const double sz = dev_->precision_bytes();
     auto r0 = [&](int c) { return (double)rows0_[c]; };
@@ -392,6 +433,7 @@ std::vector<Tree::Work> Tree::work_factor() const {
 std::vector<Tree::Work> Tree::work_solve() const {
     std::vector<Work> w;
     if (!factored_) return w;
+    ensure_log();
     const spand::Plan& P = plan_;
     const double sz = dev_->precision_bytes();
     // both sweeps

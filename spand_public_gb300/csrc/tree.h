@@ -71,10 +71,10 @@ class Tree {
     long long nnz() const;
     int get_stop() const;
     int get_nlevels() const { return nlevels_; }
-    const std::vector<LevelLog>& log() const { return log_; }
+    const std::vector<LevelLog>& log() const { ensure_log(); return log_; }
     // (level, cluster order, rows, rank) for every sparsified cluster, reference order
     std::vector<std::array<int, 4>> ranks() const;
-    const std::vector<OpRecord>& ops() const { return ops_; }
+    const std::vector<OpRecord>& ops() const { ensure_log(); return ops_; }
     void op_matrix(int idx, std::vector<double>& out) const;
     void op_tau(int idx, std::vector<double>& out) const;
     double t_partition = 0, t_assemble = 0, t_factorize = 0;
@@ -97,8 +97,15 @@ class Tree {
     std::vector<Work> work_factor() const;
     std::vector<Work> work_solve() const;
 
+    // No reference counterpart: factorize + device PCG on device vectors, timed with
+    // CUDA events on the tree's stream.  out: factor ms, PCG ms, iterations, |r|/|b|.
+    void bench_step(const double* b_dev, double* x_dev, int iters, double tol, double out[4]);
+
    private:
     void build_ops_and_log();
+    void ensure_log() const {
+        if (log_dirty_) const_cast<Tree*>(this)->build_ops_and_log();
+    }
 
     int nlevels_;
     bool verb_ = true, geo_ = false, use_want_sparsify_ = true, fp32_ = false;
@@ -125,6 +132,7 @@ class Tree {
     std::vector<LevelLog> log_;
     std::vector<OpRecord> ops_;
     std::vector<int> csize_, rows0_;
+    bool log_dirty_ = false;
 };
 
 // Preconditioned CG (is.cpp:39-121) on the device; b and x are host vectors.
