@@ -4,11 +4,14 @@
 // when the cluster's hierarchy level started).  Work lists are uploaded once from the
 // symbolic plan; grids are sized from capacities and surplus blocks exit early.
 // Citations are path:line into leopoldcambier/spaND_public.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
+#include <climits>
 #include <cstring>
 #include <map>
 #include <stdexcept>
@@ -118,20 +121,59 @@ __device__ T warp_sum(T v) {
 }
 
 // ------------------------------------------------------------------------------------
-// Cholesky of pivot blocks, one block per pivot (dpotrf 'L', tree.cpp:582-593)
-// Right-looking, column by column; the block is staged in shared memory when it fits.
+// Cholesky of pivot blocks, blocked (tree.cpp:582-593).  One block per pivot.  When the
+// whole block fits in shared memory it is factored there column by column; otherwise
+// 32-column panels are staged in shared memory, updated left-looking from the factored
+// columns (read from global memory, L1/L2 resident) and factored in place.
 // ------------------------------------------------------------------------------------
+constexpr int PNB = 32;
+
 template <typename T>
-__global__ void potrf_kernel(Ctx<T> c, const int* __restrict__ pivots, const int* __restrict__ clusters, int count,
-                             int smem_elems) {
-    extern __shared__ unsigned char smem_raw[];
+__device__ bool chol_inplace_smem(T* A, int ld, int m, int w, T* dsh, int* bad) {
+    // factor the leading w columns of an m x w panel (diagonal block on top)
+    for (int j = 0; j < w; j++) {
+        if (threadIdx.x == 0) {
+            T ajj = A[j + (size_t)j * ld];
+            if (!(ajj > T(0))) {
+                *bad = 1;
+                *dsh = T(1);
+            } else {
+                *dsh = dsqrt(ajj);
+            }
+            A[j + (size_t)j * ld] = *dsh;
+        }
+        __syncthreads();
+        if (*bad) return false;
+        const T inv = T(1) / *dsh;
+        for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) A[i + (size_t)j * ld] *= inv;
+        __syncthreads();
+        const int wc = w - j - 1;  // trailing columns inside the panel
+        const int mr = m - j - 1;
+        for (int idx = threadIdx.x; idx < mr * wc; idx += blockDim.x) {
+            int ii = idx % mr, kk = idx / mr;
+            if (ii < kk) continue;
+            int i = j + 1 + ii, k = j + 1 + kk;
+            A[i + (size_t)k * ld] -= A[i + (size_t)j * ld] * A[k + (size_t)j * ld];
+        }
+        __syncthreads();
+    }
+    return true;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) potrf2_kernel(Ctx<T> c, const int* __restrict__ pivots,
+                                                     const int* __restrict__ clusters, int count, int smem_elems) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
     const int item = blockIdx.x;
     if (item >= count) return;
-    // Another block of this launch may record a failure at any time: read the status
-    // once per block so that every thread takes the same branch.
     __shared__ int failed;
-    if (threadIdx.x == 0) failed = *(volatile int*)&c.status->not_spd;
+    __shared__ T dsh;
+    __shared__ int bad;
+    if (threadIdx.x == 0) {
+        failed = *(volatile int*)&c.status->not_spd;
+        bad = 0;
+    }
     __syncthreads();
     if (failed) return;
     const int cl = clusters[item];
@@ -139,68 +181,65 @@ __global__ void potrf_kernel(Ctx<T> c, const int* __restrict__ pivots, const int
     if (n == 0) return;
     T* G = bptr(c, pivots[item]);
     const int gld = c.blk[pivots[item]].ld;
-    const bool in_smem = (long long)n * n <= smem_elems;
-    T* A = in_smem ? sm : G;
-    const int ld = in_smem ? n : gld;
-    if (in_smem) {
+    if ((long long)n * n <= smem_elems) {
         for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
             int i = idx % n, j = idx / n;
-            sm[i + j * n] = G[i + (size_t)j * gld];
+            if (i >= j) sm[i + j * n] = G[i + (size_t)j * gld];
         }
-    }
-    __shared__ T dshared;
-    __shared__ int bad;
-    if (threadIdx.x == 0) bad = 0;
-    __syncthreads();
-    for (int j = 0; j < n; j++) {
-        if (threadIdx.x == 0) {
-            T ajj = A[j + (size_t)j * ld];
-            if (!(ajj > T(0))) {
-                bad = 1;
-                dshared = T(1);
-            } else {
-                dshared = dsqrt(ajj);
+        __syncthreads();
+        bool ok = chol_inplace_smem(sm, n, n, n, &dsh, &bad);
+        if (ok)
+            for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+                int i = idx % n, j = idx / n;
+                if (i >= j) G[i + (size_t)j * gld] = sm[i + j * n];
             }
-            A[j + (size_t)j * ld] = dshared;
+    } else if ((long long)n * PNB <= smem_elems) {
+        for (int jb = 0; jb < n && !bad; jb += PNB) {
+            const int w = min(PNB, n - jb), m = n - jb;
+            T* P = sm;  // m x w, ld m
+            for (int idx = threadIdx.x; idx < m * w; idx += blockDim.x) {
+                int i = idx % m, j = idx / m;
+                P[i + j * m] = G[(jb + i) + (size_t)(jb + j) * gld];
+            }
+            __syncthreads();
+            // left-looking update with the factored columns 0..jb
+            for (int idx = threadIdx.x; idx < m * w; idx += blockDim.x) {
+                int i = idx % m, j = idx / m;
+                if (i < j) continue;
+                T s = 0;
+                const T* ai = G + (jb + i);
+                const T* aj = G + (jb + j);
+                for (int k = 0; k < jb; k++) s += ai[(size_t)k * gld] * aj[(size_t)k * gld];
+                P[i + j * m] -= s;
+            }
+            __syncthreads();
+            if (!chol_inplace_smem(P, m, m, w, &dsh, &bad)) break;
+            for (int idx = threadIdx.x; idx < m * w; idx += blockDim.x) {
+                int i = idx % m, j = idx / m;
+                if (i >= j) G[(jb + i) + (size_t)(jb + j) * gld] = P[i + j * m];
+            }
+            __syncthreads();
         }
-        __syncthreads();
-        if (bad) break;
-        const T d = dshared;
-        const T inv = T(1) / d;
-        for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) A[i + (size_t)j * ld] *= inv;
-        __syncthreads();
-        // trailing lower update: A[i,k] -= A[i,j] A[k,j], j < k <= i
-        const int m = n - j - 1;
-        for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) {
-            int ii = idx % m, kk = idx / m;
-            if (ii < kk) continue;
-            int i = j + 1 + ii, k = j + 1 + kk;
-            A[i + (size_t)k * ld] -= A[i + (size_t)j * ld] * A[k + (size_t)j * ld];
-        }
-        __syncthreads();
+    } else {
+        // panel larger than the shared-memory budget: factor in global memory
+        chol_inplace_smem(G, gld, n, n, &dsh, &bad);
     }
-    if (bad) {
-        if (threadIdx.x == 0) atomicCAS(&c.status->not_spd, 0, cl + 1);
-        return;
-    }
-    if (in_smem) {
-        for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
-            int i = idx % n, j = idx / n;
-            G[i + (size_t)j * gld] = sm[i + j * n];
-        }
-    }
+    if (bad && threadIdx.x == 0) atomicCAS(&c.status->not_spd, 0, cl + 1);
 }
 
 // ------------------------------------------------------------------------------------
-// Triangular solves of edge blocks with a cluster's Cholesky factor (tree.cpp:640-663)
-// side 1: B (m x n) <- B L^{-T}; one thread per row of B.
-// side 0: B (n x m) <- L^{-1} B; one warp per column of B.
+// Triangular solves of edge blocks with a cluster's Cholesky factor (tree.cpp:640-663),
+// a tile of the block staged in shared memory.
+// side 1: B (m x n) <- B L^{-T}: tile of TRB rows; side 0: B (n x m) <- L^{-1} B: tile of
+// TRB columns.  Right-looking over the n columns / rows of L.
 // ------------------------------------------------------------------------------------
-constexpr int TRSM_ROWS = 128;   // rows of B per block, side 1
-constexpr int TRSM_COLS = 16;    // columns of B per block, side 0 (one warp each, 16 warps)
+constexpr int TRB = 32;
 
 template <typename T>
-__global__ void trsm_kernel(Ctx<T> c, const DTrsm* __restrict__ items, const DTile* __restrict__ tiles, int ntiles) {
+__global__ void __launch_bounds__(256) trsm2_kernel(Ctx<T> c, const DTrsm* __restrict__ items,
+                                                   const DTile* __restrict__ tiles, int ntiles, int smem_elems) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* X = reinterpret_cast<T*>(smem_raw);
     const int t = blockIdx.x;
     if (t >= ntiles || c.status->not_spd) return;
     const DTrsm it = items[tiles[t].item];
@@ -210,30 +249,66 @@ __global__ void trsm_kernel(Ctx<T> c, const DTrsm* __restrict__ items, const DTi
     const int lld = c.blk[it.lblock].ld;
     T* B = bptr(c, it.block);
     const int bld = c.blk[it.block].ld;
-    if (it.side == 1) {
-        const int m = c.csize[c.blk[it.block].rowc];
-        const int r = tiles[t].tile_i * TRSM_ROWS + threadIdx.x;
-        if (r >= m) return;
-        T* row = B + r;
-        for (int j = 0; j < n; j++) {
-            const T x = row[(size_t)j * bld] / L[j + (size_t)j * lld];
-            row[(size_t)j * bld] = x;
-            const T* lj = L + (size_t)j * lld;
-            for (int k = j + 1; k < n; k++) row[(size_t)k * bld] -= x * lj[k];
+    const int m = it.side == 1 ? c.csize[c.blk[it.block].rowc] : c.csize[c.blk[it.block].colc];
+    const int r0 = tiles[t].tile_i * TRB;
+    if (r0 >= m) return;
+    const int tr = min(TRB, m - r0);
+    // element (q, k): q the independent index (row of B for side 1, column for side 0),
+    // k the index solved over; staged in shared memory as X[q + k*tr] when it fits
+    const bool staged = (long long)tr * n <= smem_elems;
+    T* base;
+    long long sq, sk;
+    if (staged) {
+        base = X;
+        sq = 1;
+        sk = tr;
+        if (it.side == 1) {
+            for (int idx = threadIdx.x; idx < tr * n; idx += blockDim.x) {
+                int q = idx % tr, k = idx / tr;
+                X[q + k * tr] = B[(r0 + q) + (size_t)k * bld];
+            }
+        } else {
+            for (int idx = threadIdx.x; idx < tr * n; idx += blockDim.x) {
+                int k = idx % n, q = idx / n;
+                X[q + k * tr] = B[k + (size_t)(r0 + q) * bld];
+            }
         }
+        __syncthreads();
+    } else if (it.side == 1) {
+        base = B + r0;
+        sq = 1;
+        sk = bld;
     } else {
-        const int m = c.csize[c.blk[it.block].colc];
-        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-        const int col = tiles[t].tile_i * TRSM_COLS + w;
-        if (col >= m) return;
-        T* b = B + (size_t)col * bld;
-        for (int k = 0; k < n; k++) {
-            const T x = b[k] / L[k + (size_t)k * lld];
-            __syncwarp();
-            if (lane == 0) b[k] = x;
-            const T* lk = L + (size_t)k * lld;
-            for (int i = k + 1 + lane; i < n; i += 32) b[i] -= lk[i] * x;
-            __syncwarp();
+        base = B + (size_t)r0 * bld;
+        sq = bld;
+        sk = 1;
+    }
+    // both sides solve x L^T = b per independent index: x_j = (b_j - sum_{k<j} x_k L[j,k]) / L[j,j]
+    const int q = threadIdx.x % TRB;
+    const int lanes = blockDim.x / TRB;
+    const int sub = threadIdx.x / TRB;
+    for (int j = 0; j < n; j++) {
+        const T d = L[j + (size_t)j * lld];
+        if (sub == 0 && q < tr) base[q * sq + j * sk] /= d;
+        __syncthreads();
+        if (q < tr) {
+            const T xj = base[q * sq + j * sk];
+            const T* lj = L + (size_t)j * lld;
+            for (int k = j + 1 + sub; k < n; k += lanes) base[q * sq + k * sk] -= xj * lj[k];
+        }
+        __syncthreads();
+    }
+    if (staged) {
+        if (it.side == 1) {
+            for (int idx = threadIdx.x; idx < tr * n; idx += blockDim.x) {
+                int qq = idx % tr, k = idx / tr;
+                B[(r0 + qq) + (size_t)k * bld] = X[qq + k * tr];
+            }
+        } else {
+            for (int idx = threadIdx.x; idx < tr * n; idx += blockDim.x) {
+                int k = idx % n, qq = idx / n;
+                B[k + (size_t)(r0 + qq) * bld] = X[qq + k * tr];
+            }
         }
     }
 }
@@ -325,8 +400,8 @@ __global__ void __launch_bounds__(256) schur_kernel(Ctx<T> c, const DTarget* __r
 // Asn = [A_sn (in-edges) | A_ns^T (out-edges)], rows = size(c); ld = cap(c).
 template <typename T>
 __global__ void asn_gather_kernel(Ctx<T> c, const DSpars* __restrict__ items, const DAsn* __restrict__ pieces, T* ws,
-                                  int* colcount) {
-    if (c.status->not_spd) return;
+                                  int* colcount, const int* __restrict__ only) {
+    if (c.status->not_spd || (only && !only[blockIdx.x])) return;
     const DSpars it = items[blockIdx.x];
     const int rows = c.csize[it.cluster];
     const int ld = c.cap[it.cluster];
@@ -366,7 +441,7 @@ __device__ __forceinline__ T qrcp_tie() {
 template <typename T>
 __global__ void __launch_bounds__(512) qrcp_kernel(Ctx<T> c, const DSpars* __restrict__ items, T* ws, T* norms,
                                                     int* jpvt_ws, const int* __restrict__ colcount, T* taus,
-                                                    int* rank_out, double tol) {
+                                                    int* rank_out, double tol, const int* __restrict__ only) {
     extern __shared__ unsigned char smem_raw[];
     T* vsh = reinterpret_cast<T*>(smem_raw);  // cap(c) entries
     __shared__ T red[33];
@@ -375,7 +450,7 @@ __global__ void __launch_bounds__(512) qrcp_kernel(Ctx<T> c, const DSpars* __res
     __shared__ int s_pvt;
     __shared__ T s_beta, s_tau, s_scal;
     __shared__ int s_stop;
-    if (c.status->not_spd) return;
+    if (c.status->not_spd || (only && !only[blockIdx.x])) return;
     const DSpars it = items[blockIdx.x];
     const int rows = c.csize[it.cluster];
     const int cols = colcount[blockIdx.x];
@@ -542,6 +617,650 @@ __global__ void __launch_bounds__(512) qrcp_kernel(Ctx<T> c, const DSpars* __res
     if (threadIdx.x == 0) rank_out[it.cluster] = rank;
 }
 
+// QRCP with the sparsification matrix resident in the shared memory of a thread-block
+// cluster (CS CTAs, CS = 1..16).  CTA r of the cluster owns the column slab
+// [r*cpc, min(cols, (r+1)*cpc)) of Asn, gathered straight from the edge blocks.  Per
+// pivot step: the cluster-wide largest partial norm and the first column inside the tie
+// window are reduced through distributed shared memory; the owner of column i swaps in
+// the pivot column (remote read/write of the other slab) and builds the reflector; every
+// CTA then reads the reflector from the owner's slab and updates its own columns and
+// norms.  Three cluster barriers per step.  Arithmetic and pivot rule are those of
+// qrcp_kernel; the result (R, reflectors, jpvt, tau, rank) is written to the same global
+// workspace for sparsify_scatter_kernel.  Matrices too large for the cluster's shared
+// memory set fallback[item] and are handled by asn_gather_kernel + qrcp_kernel.
+constexpr int QC_THREADS = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, const DSpars* __restrict__ items,
+                                                                  const DAsn* __restrict__ pieces, T* ws,
+                                                                  int* jpvt_ws, T* taus, int* rank_out,
+                                                                  int* colcount, int* fallback, double tol,
+                                                                  int smem_bytes) {
+    namespace cgx = cooperative_groups;
+    cgx::cluster_group cl = cgx::this_cluster();
+    const int CS = (int)cl.num_blocks();
+    const int me = (int)cl.block_rank();
+    const int item = blockIdx.x / CS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ T red[33];
+    __shared__ int ired[33];
+    __shared__ T pub_max;
+    __shared__ int pub_idx;
+    __shared__ T pub_beta, pub_tau, pub_r00;
+    __shared__ int pub_stop;
+    if (c.status->not_spd) return;
+    const DSpars it = items[item];
+    const int rows = c.csize[it.cluster];
+    int cols = 0;
+    for (int p = 0; p < it.count; p++) cols += c.csize[pieces[it.first + p].nbr];
+    const int mn = min(rows, cols);
+    const int cpc = (cols + CS - 1) / CS;
+    // shared layout: A slab (rows x cpc), v (rows), vn1, vn2 (cpc), jp (cpc)
+    const long long need = ((long long)rows * cpc + rows + 2LL * cpc) * sizeof(T) + (long long)cpc * sizeof(int);
+    const bool fits = need <= smem_bytes;
+    if (threadIdx.x == 0 && me == 0) {
+        fallback[item] = (mn > 0 && tol < 1.0 && !fits) ? 1 : 0;
+        colcount[item] = cols;
+    }
+    int* jpg = jpvt_ws + it.col_off;
+    if (mn == 0 || tol >= 1.0) {
+        // choose_rank gives 0 for an empty diagonal and for tol >= 1: no reflectors
+        if (me == 0) {
+            for (int j = threadIdx.x; j < cols; j += blockDim.x) jpg[j] = j;
+            if (threadIdx.x == 0) rank_out[it.cluster] = 0;
+        }
+        return;
+    }
+    if (!fits) return;
+    T* A = reinterpret_cast<T*>(smem_raw);
+    T* vsh = A + (size_t)rows * cpc;
+    T* vn1 = vsh + rows;
+    T* vn2 = vn1 + cpc;
+    int* jp = reinterpret_cast<int*>(vn2 + cpc);
+    const int c0 = me * cpc;
+    const int c1 = min(cols, c0 + cpc);
+    const int nloc = max(0, c1 - c0);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    // gather this slab of Asn = [A_sn | A_ns^T] from the edge blocks
+    {
+        int col = 0;
+        for (int p = 0; p < it.count && col < c1; p++) {
+            const DAsn pc = pieces[it.first + p];
+            const int n = c.csize[pc.nbr];
+            const int lo = max(col, c0), hi = min(col + n, c1);
+            if (lo < hi) {
+                const T* B = bptr(c, pc.block);
+                const int bld = c.blk[pc.block].ld;
+                const int width = hi - lo;
+                if (!pc.transposed) {
+                    for (int idx = threadIdx.x; idx < rows * width; idx += blockDim.x) {
+                        int i = idx % rows, jj = idx / rows;
+                        A[i + (size_t)(lo - c0 + jj) * rows] = B[i + (size_t)(lo - col + jj) * bld];
+                    }
+                } else {
+                    for (int idx = threadIdx.x; idx < rows * width; idx += blockDim.x) {
+                        int jj = idx % width, i = idx / width;
+                        A[i + (size_t)(lo - c0 + jj) * rows] = B[(lo - col + jj) + (size_t)i * bld];
+                    }
+                }
+            }
+            col += n;
+        }
+    }
+    __syncthreads();
+    for (int j = w; j < nloc; j += nw) {
+        const T* a = A + (size_t)j * rows;
+        T s = 0;
+        for (int r = lane; r < rows; r += 32) s += a[r] * a[r];
+        s = warp_sum(s);
+        if (lane == 0) {
+            vn1[j] = dsqrt(s);
+            vn2[j] = vn1[j];
+            jp[j] = c0 + j;
+        }
+    }
+    const T tol3z = dsqrt(sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-07));
+    int rank = mn;
+    T r00 = 0;
+    for (int i = 0; i < mn; i++) {
+        __syncthreads();
+        // (1) cluster-wide largest partial norm over columns >= i
+        T bv = 0;
+        for (int j = max(i - c0, 0) + threadIdx.x; j < nloc; j += blockDim.x) bv = fmax(bv, vn1[j]);
+        for (int o = 16; o > 0; o >>= 1) bv = fmax(bv, __shfl_xor_sync(0xffffffffu, bv, o));
+        if (lane == 0) red[w] = bv;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            T m = red[0];
+            for (int k = 1; k < nw; k++) m = fmax(m, red[k]);
+            pub_max = m;
+        }
+        cl.sync();
+        T gmax = 0;
+        for (int q = 0; q < CS; q++) gmax = fmax(gmax, *cl.map_shared_rank(&pub_max, q));
+        const T thresh = gmax * (T(1) - qrcp_tie<T>());
+        // (2) first column >= i inside the tie window
+        int bi = cols;
+        for (int j = max(i - c0, 0) + threadIdx.x; j < nloc; j += blockDim.x)
+            if (vn1[j] >= thresh) { bi = c0 + j; break; }
+        for (int o = 16; o > 0; o >>= 1) bi = min(bi, __shfl_xor_sync(0xffffffffu, bi, o));
+        if (lane == 0) ired[w] = bi;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int m = ired[0];
+            for (int k = 1; k < nw; k++) m = min(m, ired[k]);
+            pub_idx = m;
+        }
+        cl.sync();
+        int pvt = cols;
+        for (int q = 0; q < CS; q++) pvt = min(pvt, *cl.map_shared_rank(&pub_idx, q));
+        if (pvt >= cols) pvt = i;  // all norms NaN: keep the current column
+        const int own_i = i / cpc;
+        // (3) the owner of column i swaps in the pivot column and builds the reflector
+        if (me == own_i) {
+            const int li = i - c0;
+            T* ai = A + (size_t)li * rows;
+            if (pvt != i) {
+                const int own_p = pvt / cpc;
+                const int lp = pvt - own_p * cpc;
+                T* Ap = cl.map_shared_rank(A, own_p) + (size_t)lp * rows;
+                for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+                    T t = ai[r];
+                    ai[r] = Ap[r];
+                    Ap[r] = t;
+                }
+                if (threadIdx.x == 0) {
+                    T* rvn1 = cl.map_shared_rank(vn1, own_p);
+                    T* rvn2 = cl.map_shared_rank(vn2, own_p);
+                    int* rjp = cl.map_shared_rank(jp, own_p);
+                    int t = jp[li];
+                    jp[li] = rjp[lp];
+                    rjp[lp] = t;
+                    rvn1[lp] = vn1[li];
+                    rvn2[lp] = vn2[li];
+                }
+                __syncthreads();
+            }
+            T part = 0;
+            for (int r = i + 1 + threadIdx.x; r < rows; r += blockDim.x) part += ai[r] * ai[r];
+            const T xnorm2 = block_sum(part, red);
+            if (threadIdx.x == 0) {
+                const T alpha = ai[i];
+                const T xnorm = dsqrt(xnorm2);
+                T beta, tu, sc;
+                if (xnorm == T(0)) {
+                    beta = alpha;
+                    tu = 0;
+                    sc = 0;
+                } else {
+                    beta = -copysign(hypot(alpha, xnorm), alpha);
+                    tu = (beta - alpha) / beta;
+                    sc = T(1) / (alpha - beta);
+                }
+                const T rii = fabs(beta);
+                T ref = (i == 0) ? rii : pub_r00;
+                int stop = 0;
+                if (tol != 0.0 && i >= 1 && !(rii / ref >= T(tol))) stop = 1;
+                pub_beta = beta;
+                pub_tau = tu;
+                pub_r00 = ref;
+                pub_stop = stop;
+                red[32] = sc;
+            }
+            __syncthreads();
+            if (!pub_stop) {
+                const T sc = red[32];
+                if (pub_tau != T(0))
+                    for (int r = i + 1 + threadIdx.x; r < rows; r += blockDim.x) ai[r] *= sc;
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    ai[i] = pub_beta;
+                    taus[it.tau_off + i] = pub_tau;
+                }
+            }
+        }
+        cl.sync();
+        const int stop = *cl.map_shared_rank(&pub_stop, own_i);
+        const T tu = *cl.map_shared_rank(&pub_tau, own_i);
+        if (me != own_i && threadIdx.x == 0) pub_r00 = *cl.map_shared_rank(&pub_r00, own_i);
+        if (stop) {
+            rank = i;
+            break;
+        }
+        // (4) reflector from the owner's slab, applied to this slab's columns > i
+        {
+            const T* vi = cl.map_shared_rank(A, own_i) + (size_t)(i - own_i * cpc) * rows;
+            for (int r = i + 1 + threadIdx.x; r < rows; r += blockDim.x) vsh[r] = vi[r];
+            if (threadIdx.x == 0) vsh[i] = T(1);
+        }
+        __syncthreads();
+        for (int j = max(i + 1 - c0, 0) + w; j < nloc; j += nw) {
+            T* aj = A + (size_t)j * rows;
+            if (tu != T(0)) {
+                T s = 0;
+                for (int r = i + lane; r < rows; r += 32) s += vsh[r] * aj[r];
+                s = warp_sum(s) * tu;
+                for (int r = i + lane; r < rows; r += 32) aj[r] -= s * vsh[r];
+            }
+            __syncwarp();
+            const T v1 = vn1[j];
+            if (v1 != T(0)) {
+                T temp = fabs(aj[i]) / v1;
+                temp = T(1) - temp * temp;
+                temp = temp > T(0) ? temp : T(0);
+                const T rr = v1 / vn2[j];
+                const T temp2 = temp * rr * rr;
+                if (temp2 <= tol3z) {
+                    T s = 0;
+                    for (int r = i + 1 + lane; r < rows; r += 32) s += aj[r] * aj[r];
+                    s = warp_sum(s);
+                    if (lane == 0) {
+                        if (i < rows - 1) {
+                            vn1[j] = dsqrt(s);
+                            vn2[j] = vn1[j];
+                        } else {
+                            vn1[j] = 0;
+                            vn2[j] = 0;
+                        }
+                    }
+                } else if (lane == 0) {
+                    vn1[j] = v1 * dsqrt(temp);
+                }
+            }
+            __syncwarp();
+        }
+    }
+    // no CTA leaves while another may still read its shared memory
+    cl.sync();
+    const int ld = c.cap[it.cluster];
+    T* W = ws + it.ws_off;
+    for (int idx = threadIdx.x; idx < rows * nloc; idx += blockDim.x) {
+        int i = idx % rows, j = idx / rows;
+        W[i + (size_t)(c0 + j) * ld] = A[i + (size_t)j * rows];
+    }
+    for (int j = threadIdx.x; j < nloc; j += blockDim.x) jpg[c0 + j] = jp[j];
+    if (me == 0 && threadIdx.x == 0) rank_out[it.cluster] = rank;
+}
+
+// QRCP, version without column movement.  The sparsification matrix stays in the shared
+// memory of a thread-block cluster (CS CTAs, column slabs); a column never moves: the
+// pivoting is tracked as a permutation (perm: position -> column, replicated in every
+// CTA; pos: column -> position for the slab's own columns).  Per pivot step i:
+//   1. every CTA reads the published (slab maximum m_q, first position f_q inside the tie
+//      window of m_q) of all slabs and derives the pivot; exact as long as no slab maximum
+//      lies inside the tie window below the global one (else one more barrier);
+//   2. every CTA reads the pivot column through distributed shared memory and builds the
+//      Householder reflector itself (identical arithmetic in every CTA);
+//   3. every CTA applies the reflector to its trailing columns (G threads per column) and
+//      downdates their norms (LAWN 176), then publishes its next (m, f) and arrives at the
+//      cluster barrier.
+// The owner writes the reflector into the pivot column one step later, once no CTA can
+// still be reading that column.  At the end the slabs are written to the global workspace
+// in LAPACK's column order (position p holds column perm[p]).
+template <typename T>
+__device__ __forceinline__ void qc_barrier(cooperative_groups::cluster_group& cl, int cs) {
+    if (cs > 1) cl.sync();
+    else __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(QC_THREADS) qrcp3_kernel(Ctx<T> c, const DSpars* __restrict__ items,
+                                                           const DAsn* __restrict__ pieces, T* ws, int* jpvt_ws,
+                                                           T* taus, int* rank_out, int* colcount, int* fallback,
+                                                           double tol, int smem_bytes, unsigned long long* probe) {
+    namespace cgx = cooperative_groups;
+    cgx::cluster_group cl = cgx::this_cluster();
+    const int CS = (int)cl.num_blocks();
+    const int me = (int)cl.block_rank();
+    const int item = blockIdx.x / CS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ T red[32];
+    __shared__ int ired[32];
+    __shared__ T pubm[2][16];
+    __shared__ int pubf[2][16];
+    __shared__ T s_alpha;
+    if (c.status->not_spd) return;
+    const DSpars it = items[item];
+    const int rows = c.csize[it.cluster];
+    int cols = 0;
+    for (int p = 0; p < it.count; p++) cols += c.csize[pieces[it.first + p].nbr];
+    const int mn = min(rows, cols);
+    const int cpc = (cols + CS - 1) / CS;
+    const int lda = rows | 1;
+    const long long need = ((long long)lda * cpc + rows + 2LL * cpc) * sizeof(T) + ((long long)cols + cpc) * sizeof(int);
+    const bool fits = need <= smem_bytes;
+    if (threadIdx.x == 0 && me == 0) {
+        fallback[item] = (mn > 0 && tol < 1.0 && !fits) ? 1 : 0;
+        colcount[item] = cols;
+    }
+    int* jpg = jpvt_ws + it.col_off;
+    if (mn == 0 || tol >= 1.0) {
+        if (me == 0) {
+            for (int j = threadIdx.x; j < cols; j += blockDim.x) jpg[j] = j;
+            if (threadIdx.x == 0) rank_out[it.cluster] = 0;
+        }
+        return;
+    }
+    if (!fits) return;
+    T* A = reinterpret_cast<T*>(smem_raw);
+    T* vsh = A + (size_t)lda * cpc;
+    T* vn1 = vsh + rows;
+    T* vn2 = vn1 + cpc;
+    int* perm = reinterpret_cast<int*>(vn2 + cpc);
+    int* pos = perm + cols;
+    const int c0 = me * cpc;
+    const int c1 = min(cols, c0 + cpc);
+    const int nloc = max(0, c1 - c0);
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const int lane = tid & 31, w = tid >> 5, nw = nth >> 5;
+    // gather the slab of Asn = [A_sn | A_ns^T]
+    {
+        int col = 0;
+        for (int p = 0; p < it.count && col < c1; p++) {
+            const DAsn pc = pieces[it.first + p];
+            const int n = c.csize[pc.nbr];
+            const int lo = max(col, c0), hi = min(col + n, c1);
+            if (lo < hi) {
+                const T* B = bptr(c, pc.block);
+                const int bld = c.blk[pc.block].ld;
+                const int width = hi - lo;
+                if (!pc.transposed) {
+                    for (int idx = tid; idx < rows * width; idx += nth) {
+                        int i = idx % rows, jj = idx / rows;
+                        A[i + (size_t)(lo - c0 + jj) * lda] = B[i + (size_t)(lo - col + jj) * bld];
+                    }
+                } else {
+                    for (int idx = tid; idx < rows * width; idx += nth) {
+                        int jj = idx % width, i = idx / width;
+                        A[i + (size_t)(lo - c0 + jj) * lda] = B[(lo - col + jj) + (size_t)i * bld];
+                    }
+                }
+            }
+            col += n;
+        }
+    }
+    for (int p = tid; p < cols; p += nth) perm[p] = p;
+    for (int j = tid; j < nloc; j += nth) pos[j] = c0 + j;
+    __syncthreads();
+    for (int j = w; j < nloc; j += nw) {
+        const T* a = A + (size_t)j * lda;
+        T s = 0;
+        for (int r = lane; r < rows; r += 32) s += a[r] * a[r];
+        s = warp_sum(s);
+        if (lane == 0) {
+            vn1[j] = dsqrt(s);
+            vn2[j] = vn1[j];
+        }
+    }
+    // threads per column for the trailing update
+    int G = 1;
+    while (G < 8 && (nloc * G * 2 <= nth || rows >= 64 * G)) G *= 2;
+    const int gid = tid / G, gl = tid % G, ngroups = nth / G;
+    const T tie = T(1) - qrcp_tie<T>();
+    const T tol3z = dsqrt(sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-07));
+
+    // publish (slab max over columns at positions >= from, first position inside its tie window)
+    auto publish = [&](int par, int from) {
+        __syncthreads();
+        T m = 0;
+        for (int j = tid; j < nloc; j += nth)
+            if (pos[j] >= from) m = fmax(m, vn1[j]);
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) red[w] = m;
+        __syncthreads();
+        m = red[0];
+        for (int k = 1; k < nw; k++) m = fmax(m, red[k]);
+        int f = INT_MAX;
+        for (int j = tid; j < nloc; j += nth)
+            if (pos[j] >= from && vn1[j] >= m * tie) f = min(f, pos[j]);
+        for (int o = 16; o > 0; o >>= 1) f = min(f, __shfl_xor_sync(0xffffffffu, f, o));
+        if (lane == 0) ired[w] = f;
+        __syncthreads();
+        if (tid == 0) {
+            for (int k = 1; k < nw; k++) f = min(f, ired[k]);
+            f = min(f, ired[0]);
+            for (int q = 0; q < CS; q++) {
+                *cl.map_shared_rank(&pubm[par][me], q) = m;
+                *cl.map_shared_rank(&pubf[par][me], q) = f;
+            }
+        }
+    };
+
+    const bool probing = probe && item == 0 && me == 0 && tid == 0;
+    long long tmark = probing ? clock64() : 0;
+    auto mark = [&](int k) {
+        if (probing) {
+            long long t = clock64();
+            probe[k] += (unsigned long long)(t - tmark);
+            tmark = t;
+        }
+    };
+    publish(0, 0);
+    qc_barrier<T>(cl, CS);
+    mark(0);
+    int rank = mn;
+    T r00 = 0;
+    int pend = -1;        // local column awaiting its reflector
+    T pend_beta = 0;
+    int pend_i = 0;
+    for (int i = 0; i < mn; i++) {
+        const int par = i & 1;
+        T gmax = 0;
+        for (int q = 0; q < CS; q++) gmax = fmax(gmax, pubm[par][q]);
+        bool amb = false;
+        for (int q = 0; q < CS; q++) amb |= (pubm[par][q] < gmax && pubm[par][q] >= gmax * tie);
+        int pvt = INT_MAX;
+        if (!amb) {
+            for (int q = 0; q < CS; q++)
+                if (pubm[par][q] == gmax) pvt = min(pvt, pubf[par][q]);
+        } else {
+            // a slab maximum inside the tie window below the global one: search every slab
+            // with the global threshold
+            int f = INT_MAX;
+            for (int j = tid; j < nloc; j += nth)
+                if (pos[j] >= i && vn1[j] >= gmax * tie) f = min(f, pos[j]);
+            for (int o = 16; o > 0; o >>= 1) f = min(f, __shfl_xor_sync(0xffffffffu, f, o));
+            if (lane == 0) ired[w] = f;
+            __syncthreads();
+            if (tid == 0) {
+                for (int k = 0; k < nw; k++) f = min(f, ired[k]);
+                for (int q = 0; q < CS; q++) *cl.map_shared_rank(&pubf[par][me], q) = f;
+            }
+            qc_barrier<T>(cl, CS);
+            for (int q = 0; q < CS; q++) pvt = min(pvt, pubf[par][q]);
+        }
+        if (pvt < i || pvt >= cols) pvt = i;  // all norms NaN: keep the current position
+        mark(1);
+        const int phys = perm[pvt];
+        const int phys_i = perm[i];
+        const int own = phys / cpc, lj = phys - own * cpc;
+        // reflector of the previous step into its column (no CTA reads it any more)
+        if (pend >= 0) {
+            T* a = A + (size_t)pend * lda;
+            for (int r = pend_i + 1 + tid; r < rows; r += nth) a[r] = vsh[r];
+            if (tid == 0) a[pend_i] = pend_beta;
+            pend = -1;
+        }
+        __syncthreads();
+        mark(2);
+        // pivot column -> vsh (rows >= i)
+        const T* src = (own == me ? A : cl.map_shared_rank(A, own)) + (size_t)lj * lda;
+        T part = 0;
+        for (int r = i + tid; r < rows; r += nth) {
+            const T v = src[r];
+            if (r == i) {
+                s_alpha = v;
+                vsh[r] = T(1);
+            } else {
+                vsh[r] = v;
+                part += v * v;
+            }
+        }
+        part = warp_sum(part);
+        if (lane == 0) red[w] = part;
+        __syncthreads();
+        T xnorm2 = 0;
+        for (int k = 0; k < nw; k++) xnorm2 += red[k];
+        const T alpha = s_alpha;
+        const T xnorm = dsqrt(xnorm2);
+        T beta, tu, sc;
+        if (xnorm == T(0)) {
+            beta = alpha;
+            tu = 0;
+            sc = 0;
+        } else {
+            beta = -copysign(hypot(alpha, xnorm), alpha);
+            tu = (beta - alpha) / beta;
+            sc = T(1) / (alpha - beta);
+        }
+        const T rii = fabs(beta);
+        if (i == 0) r00 = rii;
+        if (tol != 0.0 && i >= 1 && !(rii / r00 >= T(tol))) {
+            rank = i;
+            break;
+        }
+        if (tu != T(0))
+            for (int r = i + 1 + tid; r < rows; r += nth) vsh[r] *= sc;
+        if (me == 0 && tid == 0) taus[it.tau_off + i] = tu;
+        __syncthreads();  // vsh final; every thread has read perm
+        mark(3);
+        if (tid == 0) {
+            perm[i] = phys;
+            perm[pvt] = phys_i;
+        }
+        // trailing update of this slab's columns and their norms; positions after the swap.
+        // The loop runs the same number of times in every thread so that the group
+        // shuffles always see all 32 lanes.  The first lane of each group also keeps the
+        // largest new norm of its columns for the next pivot search.
+        T mloc = 0;
+        for (int base = 0; base < nloc; base += ngroups) {
+            const int j = base + gid;
+            const int ph = c0 + j;
+            const bool active = j < nloc && ph != phys && pos[j] >= i;
+            T* aj = A + (size_t)(active ? j : 0) * lda;
+            T s = 0;
+            if (active && tu != T(0)) {
+                // four independent partial sums so the shared-memory loads overlap
+                T s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+                int r = i + gl;
+                for (; r + 3 * G < rows; r += 4 * G) {
+                    s0 += vsh[r] * aj[r];
+                    s1 += vsh[r + G] * aj[r + G];
+                    s2 += vsh[r + 2 * G] * aj[r + 2 * G];
+                    s3 += vsh[r + 3 * G] * aj[r + 3 * G];
+                }
+                for (; r < rows; r += G) s0 += vsh[r] * aj[r];
+                s = (s0 + s1) + (s2 + s3);
+            }
+            for (int o = G >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (active && tu != T(0)) {
+                s *= tu;
+                int r = i + gl;
+                for (; r + 3 * G < rows; r += 4 * G) {
+                    const T a0 = aj[r], a1 = aj[r + G], a2 = aj[r + 2 * G], a3 = aj[r + 3 * G];
+                    aj[r] = a0 - s * vsh[r];
+                    aj[r + G] = a1 - s * vsh[r + G];
+                    aj[r + 2 * G] = a2 - s * vsh[r + 2 * G];
+                    aj[r + 3 * G] = a3 - s * vsh[r + 3 * G];
+                }
+                for (; r < rows; r += G) aj[r] -= s * vsh[r];
+            }
+            __syncwarp();
+            // norm downdating (LAWN 176), decided by the group's first lane
+            int recompute = 0;
+            T newv = 0;
+            if (active && gl == 0) {
+                const T v1 = vn1[j];
+                newv = v1;
+                if (v1 != T(0)) {
+                    T temp = fabs(aj[i]) / v1;
+                    temp = T(1) - temp * temp;
+                    temp = temp > T(0) ? temp : T(0);
+                    const T rr = v1 / vn2[j];
+                    if (temp * rr * rr <= tol3z) recompute = 1;
+                    else newv = v1 * dsqrt(temp);
+                }
+            }
+            recompute = __shfl_sync(0xffffffffu, recompute, (lane / G) * G);
+            T q2 = 0;
+            if (active && recompute) {
+                T q0 = 0, q1 = 0, q2b = 0, q3 = 0;
+                int r = i + 1 + gl;
+                for (; r + 3 * G < rows; r += 4 * G) {
+                    q0 += aj[r] * aj[r];
+                    q1 += aj[r + G] * aj[r + G];
+                    q2b += aj[r + 2 * G] * aj[r + 2 * G];
+                    q3 += aj[r + 3 * G] * aj[r + 3 * G];
+                }
+                for (; r < rows; r += G) q0 += aj[r] * aj[r];
+                q2 = (q0 + q1) + (q2b + q3);
+            }
+            for (int o = G >> 1; o > 0; o >>= 1) q2 += __shfl_xor_sync(0xffffffffu, q2, o);
+            if (active && gl == 0) {
+                if (recompute) {
+                    newv = (i < rows - 1) ? dsqrt(q2) : T(0);
+                    vn2[j] = newv;
+                }
+                vn1[j] = newv;
+                if (ph == phys_i) pos[j] = pvt;
+                mloc = fmax(mloc, newv);
+            }
+            if (j < nloc && gl == 0 && ph == phys) pos[j] = i;
+        }
+        mark(4);
+        if (own == me) {
+            pend = lj;
+            pend_beta = beta;
+            pend_i = i;
+        }
+        if (i + 1 < mn) {
+            // publish (slab maximum, first position inside its tie window) for step i+1;
+            // every thread rescans only the columns it updated itself
+            for (int o = 16; o > 0; o >>= 1) mloc = fmax(mloc, __shfl_xor_sync(0xffffffffu, mloc, o));
+            if (lane == 0) red[w] = mloc;
+            __syncthreads();
+            T m = red[0];
+            for (int k = 1; k < nw; k++) m = fmax(m, red[k]);
+            int f = INT_MAX;
+            if (gl == 0)
+                for (int j = gid; j < nloc; j += ngroups)
+                    if (pos[j] > i && vn1[j] >= m * tie) f = min(f, pos[j]);
+            for (int o = 16; o > 0; o >>= 1) f = min(f, __shfl_xor_sync(0xffffffffu, f, o));
+            if (lane == 0) ired[w] = f;
+            __syncthreads();
+            if (tid == 0) {
+                for (int k = 0; k < nw; k++) f = min(f, ired[k]);
+                for (int q = 0; q < CS; q++) {
+                    *cl.map_shared_rank(&pubm[par ^ 1][me], q) = m;
+                    *cl.map_shared_rank(&pubf[par ^ 1][me], q) = f;
+                }
+            }
+            mark(5);
+            qc_barrier<T>(cl, CS);
+            mark(6);
+        }
+        if (probing) probe[7] += 1;
+    }
+    if (pend >= 0) {
+        __syncthreads();
+        T* a = A + (size_t)pend * lda;
+        for (int r = pend_i + 1 + tid; r < rows; r += nth) a[r] = vsh[r];
+        if (tid == 0) a[pend_i] = pend_beta;
+    }
+    // no CTA leaves while another may still read its shared memory
+    qc_barrier<T>(cl, CS);
+    const int ld = c.cap[it.cluster];
+    T* W = ws + it.ws_off;
+    for (int j = w; j < nloc; j += nw) {
+        const int p = pos[j];
+        const T* a = A + (size_t)j * lda;
+        T* dst = W + (size_t)p * ld;
+        for (int r = lane; r < rows; r += 32) dst[r] = a[r];
+        if (lane == 0) jpg[p] = c0 + j;
+    }
+    if (me == 0 && tid == 0) rank_out[it.cluster] = rank;
+}
+
 // Compressed edges AsnP = triu(R[:k,:]) P^T written back into the cluster's edge blocks,
 // reflectors saved for the Orthogonal op, cluster size set to the rank.
 template <typename T>
@@ -665,10 +1384,14 @@ __global__ void perm_out_kernel(double* __restrict__ x, int ldx, XCtx<T> X, cons
     x[perm[p] + (size_t)r * ldx] = (double)X.xs[slot[p] + r * X.xld];
 }
 
-// x <- L^{-1} x (fwd) or L^{-T} x (bwd), ScalingLLT (operations.cpp:97-103)
+// ------------------------------------------------------------------------------------
+// Blocked triangular solve of the ScalingLLT ops (operations.cpp:97-103): 32x32
+// diagonal blocks solved by one warp with shuffles (block held in registers), the
+// off-diagonal panel applied by the whole block; two barriers per 32 columns.
+// ------------------------------------------------------------------------------------
 template <typename T>
-__global__ void trsv_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ clusters, const int* __restrict__ lblocks,
-                            int count, int trans) {
+__global__ void __launch_bounds__(256) trsv2_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ clusters,
+                                                   const int* __restrict__ lblocks, int count, int trans) {
     const int item = blockIdx.x % count;
     const int r = blockIdx.x / count;
     const int cl = clusters[item];
@@ -677,31 +1400,71 @@ __global__ void trsv_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ cluster
     const T* L = bptr(c, lblocks[item]);
     const int ld = c.blk[lblocks[item]].ld;
     T* x = X.xs + X.xoff[cl] + r * X.xld;
-    extern __shared__ unsigned char smem_raw[];
-    T* xsh = reinterpret_cast<T*>(smem_raw);
-    __shared__ T red[33];
-    for (int i = threadIdx.x; i < n; i += blockDim.x) xsh[i] = x[i];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* xs = reinterpret_cast<T*>(smem_raw);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) xs[i] = x[i];
     __syncthreads();
+    const int nb = (n + 31) / 32;
     if (!trans) {
-        for (int k = 0; k < n; k++) {
-            const T xk = xsh[k] / L[k + (size_t)k * ld];
+        for (int b = 0; b < nb; b++) {
+            const int kb = b * 32, bw = min(32, n - kb);
+            if (w == 0) {
+                // lane i holds row i of the diagonal block and x_{kb+i}
+                T lrow[32];
+#pragma unroll
+                for (int k = 0; k < 32; k++) lrow[k] = (lane < bw && k <= lane) ? L[(kb + lane) + (size_t)(kb + k) * ld] : T(0);
+                T xi = lane < bw ? xs[kb + lane] : T(0);
+#pragma unroll
+                for (int k = 0; k < 32; k++) {
+                    if (k < bw) {
+                        const T xk = __shfl_sync(0xffffffffu, lane == k ? xi / lrow[k] : T(0), k);
+                        if (lane == k) xi = xk;
+                        else if (lane > k) xi -= lrow[k] * xk;
+                    }
+                }
+                if (lane < bw) xs[kb + lane] = xi;
+            }
             __syncthreads();
-            if (threadIdx.x == 0) xsh[k] = xk;
-            const T* lk = L + (size_t)k * ld;
-            for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) xsh[i] -= lk[i] * xk;
+            for (int i = kb + bw + threadIdx.x; i < n; i += blockDim.x) {
+                T s = 0;
+                for (int k = 0; k < bw; k++) s += L[i + (size_t)(kb + k) * ld] * xs[kb + k];
+                xs[i] -= s;
+            }
             __syncthreads();
         }
     } else {
-        for (int k = n - 1; k >= 0; k--) {
-            const T* lk = L + (size_t)k * ld;
-            T part = 0;
-            for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) part += lk[i] * xsh[i];
-            T s = block_sum(part, red);
-            if (threadIdx.x == 0) xsh[k] = (xsh[k] - s) / lk[k];
+        for (int b = nb - 1; b >= 0; b--) {
+            const int kb = b * 32, bw = min(32, n - kb);
+            // x[kb+k] -= L[kb+bw:n, kb+k]^T x[kb+bw:n], warp per k
+            for (int k = w; k < bw; k += nw) {
+                const T* lk = L + (size_t)(kb + k) * ld;
+                T s = 0;
+                for (int i = kb + bw + lane; i < n; i += 32) s += lk[i] * xs[i];
+                s = warp_sum(s);
+                if (lane == 0) xs[kb + k] -= s;
+            }
+            __syncthreads();
+            if (w == 0) {
+                // lane i holds column i of the diagonal block (row i of L^T) and x_{kb+i}
+                T lcol[32];
+#pragma unroll
+                for (int k = 0; k < 32; k++) lcol[k] = (lane < bw && k < bw && k >= lane) ? L[(kb + k) + (size_t)(kb + lane) * ld] : T(0);
+                T xi = lane < bw ? xs[kb + lane] : T(0);
+#pragma unroll
+                for (int kk = 31; kk >= 0; kk--) {
+                    if (kk < bw) {
+                        T xk = __shfl_sync(0xffffffffu, lane == kk ? xi / lcol[kk] : T(0), kk);
+                        if (lane == kk) xi = xk;
+                        else if (lane < kk) xi -= lcol[kk] * xk;
+                    }
+                }
+                if (lane < bw) xs[kb + lane] = xi;
+            }
             __syncthreads();
         }
     }
-    for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = xsh[i];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = xs[i];
 }
 
 // Forward Gemm ops grouped by neighbour: x_n -= A_ns x_s (GemmSymmOut) or A_sn^T x_s (GemmSymmIn)
@@ -1061,6 +1824,13 @@ class DeviceFactor : public DeviceFactorBase {
                 W.n = (int)items.size();
                 W.items = up(items);
                 W.maxcap = maxcap;
+                W.host = wave;
+                {
+                    // capacity bound until the first factorization reports the actual sizes
+                    int64_t need = 0;
+                    for (const SparsifyItem& it : wave) need = std::max(need, qc_need(P.c_cap[it.cluster], it.cap_cols, 1));
+                    choose_cluster(W, need);
+                }
                 D.waves.push_back(W);
             }
             D.merged = L.merged;
@@ -1158,9 +1928,12 @@ class DeviceFactor : public DeviceFactorBase {
             d_perm_ = up(perm_h_);
         }
         ctx_ = Ctx<T>{arena_, d_blk_, csize_, rows0_, d_cap_, status_};
-        SPAND_CUDA(cudaFuncSetAttribute(potrf_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SPAND_CUDA(cudaFuncSetAttribute(potrf2_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SPAND_CUDA(cudaFuncSetAttribute(trsm2_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(qrcp_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        SPAND_CUDA(cudaFuncSetAttribute(trsv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SPAND_CUDA(cudaFuncSetAttribute(qrcp3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, QC_SMEM_MAX));
+        fallback_ = alloc<int>(max_items);
+        SPAND_CUDA(cudaFuncSetAttribute(trsv2_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(ortho_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         caps_h_ = P.c_cap;
     }
@@ -1179,6 +1952,11 @@ class DeviceFactor : public DeviceFactorBase {
     void factorize(double tol) override {
         const Plan& P = *P_;
         // inputs: the assembled blocks (device copy) and the initial cluster sizes
+        if (probe_level_ >= 0) {
+            if (!probe_) probe_ = alloc<unsigned long long>(8);
+            SPAND_CUDA(cudaMemsetAsync(probe_, 0, 8 * sizeof(unsigned long long), s_));
+            probe_waves_ = 0;
+        }
         launch("restore", [&] {
             if (P.assembled_len)
                 SPAND_CUDA(cudaMemcpyAsync(arena_, pristine_, P.assembled_len * sizeof(T), cudaMemcpyDeviceToDevice, s_));
@@ -1191,6 +1969,7 @@ class DeviceFactor : public DeviceFactorBase {
         }, 0);
         for (int l = 0; l < P.nlevels; l++) {
             LevelDev& D = levels_[l];
+            cur_level_ = l;
             if (D.n_elim) {
                 launch_potrf(D.elim_pivots, D.elim_clusters, D.n_elim, D.elim_smem);
                 launch_trsm(D.elim_trsm0);
@@ -1212,13 +1991,14 @@ class DeviceFactor : public DeviceFactorBase {
                                                                              D.n_level);
                 });
             for (WaveDev& W : D.waves) {
-                launch("asn_gather", [&] {
-                    asn_gather_kernel<T><<<W.n, 256, 0, s_>>>(ctx_, W.items, pieces_, ws_, colcount_);
-                });
-                launch("qrcp", [&] {
+                launch("qrcp", [&] { launch_qrcp_cluster(W, tol); });
+                // matrices larger than the cluster's shared memory: gather to global memory
+                // and factor there (blocks of other matrices exit at once)
+                launch("qrcp_fallback", [&] {
+                    asn_gather_kernel<T><<<W.n, 256, 0, s_>>>(ctx_, W.items, pieces_, ws_, colcount_, fallback_);
                     qrcp_kernel<T><<<W.n, 512, W.maxcap * sizeof(T), s_>>>(ctx_, W.items, ws_, norms_, jpvt_,
-                                                                            colcount_, tauws_, rank_, tol);
-                });
+                                                                            colcount_, tauws_, rank_, tol, fallback_);
+                }, 2);
                 launch("sparsify_scatter", [&] {
                     sparsify_scatter_kernel<T><<<W.n, 256, 0, s_>>>(ctx_, W.items, pieces_, ws_, jpvt_, ipvt_, rank_,
                                                                      vstore_, tauws_, taustore_, colcount_);
@@ -1237,13 +2017,68 @@ class DeviceFactor : public DeviceFactorBase {
                     });
             }
         }
+        cur_level_ = -1;
         SPAND_CUDA(cudaGetLastError());
+        if (probe_) {
+            unsigned long long h[8];
+            SPAND_CUDA(cudaMemcpyAsync(h, probe_, sizeof(h), cudaMemcpyDeviceToHost, s_));
+            SPAND_CUDA(cudaStreamSynchronize(s_));
+            fprintf(stderr, "qrcp probe level %d (%d waves, first cluster of each): steps %llu | cycles/step:", probe_level_,
+                    probe_waves_, h[7]);
+            const char* nm[7] = {"init", "pivot", "pend", "load+householder", "apply", "publish", "barrier"};
+            for (int k = 0; k < 7; k++) fprintf(stderr, " %s %.0f", nm[k], h[7] ? (double)h[k] / h[7] : 0.0);
+            fprintf(stderr, "\n");
+        }
         DStatus st;
         SPAND_CUDA(cudaMemcpyAsync(&st, status_, sizeof(st), cudaMemcpyDeviceToHost, s_));
         SPAND_CUDA(cudaStreamSynchronize(s_));
         if (st.not_spd)
             throw DeviceError{SPAND_ERR_NOT_SPD, "Error: Non-SPD Pivot (cluster " + std::to_string(st.not_spd - 1) + ")"};
         factored_ = true;
+        if (!tuned_) tune_qrcp();
+    }
+
+    // Size the QRCP clusters of every wave from the matrices of the last factorization
+    // (10% slack); a later factorization whose matrices outgrow them takes the fallback.
+    void tune_qrcp() {
+        std::vector<int> cs, r0;
+        sizes(cs, r0);
+        for (LevelDev& D : levels_) {
+            std::map<int, int> wave_of;
+            for (size_t w = 0; w < D.waves.size(); w++)
+                for (const SparsifyItem& it : D.waves[w].host) wave_of[it.cluster] = (int)w;
+            for (size_t w = 0; w < D.waves.size(); w++) {
+                int64_t need = 0;
+                for (const SparsifyItem& it : D.waves[w].host) {
+                    int64_t cols = 0;
+                    for (int p = 0; p < it.count; p++) {
+                        int n = P_->asn_pieces[it.first + p].nbr;
+                        auto wn = wave_of.find(n);
+                        cols += (wn != wave_of.end() && wn->second < (int)w) ? cs[n] : r0[n];
+                    }
+                    int rows = r0[it.cluster];
+                    need = std::max(need, qc_need(rows + rows / 10 + 1, (int)(cols + cols / 10 + 1), 1));
+                }
+                choose_cluster(D.waves[w], need);
+            }
+        }
+        // POTRF / TRSM shared memory from the actual pivot sizes (10% slack; larger
+        // pivots in a later factorization take the global-memory branch of the kernels)
+        for (size_t l = 0; l < levels_.size(); l++) {
+            LevelDev& D = levels_[l];
+            const LevelPlan& L = P_->levels[l];
+            auto nmax = [&](const std::vector<int>& cl) {
+                int m = 0;
+                for (int c0 : cl) m = std::max(m, r0[c0]);
+                return m + m / 10 + 1;
+            };
+            int ne = nmax(L.elim_clusters), ns = nmax(L.scale_clusters);
+            D.elim_smem = potrf_smem_n(ne);
+            D.scale_smem = potrf_smem_n(ns);
+            D.elim_trsm0.smem = D.elim_trsm1.smem = trsm_smem_n(ne);
+            D.scale_trsm0.smem = D.scale_trsm1.smem = trsm_smem_n(ns);
+        }
+        tuned_ = true;
     }
 
     void solve_device(double* x, int nrhs, int ld) override {
@@ -1337,11 +2172,15 @@ class DeviceFactor : public DeviceFactorBase {
         DTile* tiles = nullptr;
         int ntiles = 0;
         int side = 0;
+        int smem = 0;
     };
     struct WaveDev {
         int n = 0;
         DSpars* items = nullptr;
         int maxcap = 1;
+        int cs = 1;          // CTAs per thread-block cluster of the shared-memory QRCP
+        int smem = 0;        // dynamic shared memory per CTA
+        std::vector<SparsifyItem> host;  // plan items, for tuning
     };
     struct LevelDev {
         int n_elim = 0;
@@ -1392,7 +2231,12 @@ class DeviceFactor : public DeviceFactorBase {
     // one kernel (or copy) launch: counted, and timed when the profiler is on
     template <typename F>
     void launch(const char* cls, F&& f, int kernels = 1) {
-        prof_.begin(s_, cls);
+        if (prof_.enabled() && per_level_ && cur_level_ >= 0) {
+            const std::string name = std::string(cls) + "@L" + std::to_string(cur_level_);
+            prof_.begin(s_, name.c_str());
+        } else {
+            prof_.begin(s_, cls);
+        }
         f();
         prof_.end(s_);
         launches_ += kernels;
@@ -1407,8 +2251,7 @@ class DeviceFactor : public DeviceFactorBase {
     int smem_for(const std::vector<int>& clusters, const Plan& P) {
         int mx = 0;
         for (int c0 : clusters) mx = std::max(mx, P.c_cap[c0]);
-        long long bytes = (long long)mx * mx * sizeof(T);
-        return bytes <= 160 * 1024 ? (int)bytes : 0;
+        return potrf_smem_n(mx);
     }
     int xsmem_for(const std::vector<int>& clusters, const Plan& P) {
         int mx = 1;
@@ -1434,20 +2277,77 @@ class DeviceFactor : public DeviceFactorBase {
                 ext1.push_back(P.c_cap[B.rowc]);
             }
         }
-        auto t0 = tiles_1d(ext0, TRSM_COLS);
-        auto t1 = tiles_1d(ext1, TRSM_ROWS);
-        side0 = {up(it0), up(t0), (int)t0.size(), 0};
-        side1 = {up(it1), up(t1), (int)t1.size(), 1};
+        auto t0 = tiles_1d(ext0, TRB);
+        auto t1 = tiles_1d(ext1, TRB);
+        side0 = {up(it0), up(t0), (int)t0.size(), 0, trsm_smem(clusters, P)};
+        side1 = {up(it1), up(t1), (int)t1.size(), 1, trsm_smem(clusters, P)};
+    }
+    static constexpr int QC_SMEM_MAX = 200 * 1024;
+    static constexpr int QC_SMEM_SHARED = 96 * 1024;  // two CTAs per SM
+    // shared-memory bytes of one CTA holding a rows x ceil(cols/cs) slab
+    static int64_t qc_need(int rows, int cols, int cs) {
+        int64_t cpc = (cols + cs - 1) / cs;
+        return ((int64_t)(rows | 1) * cpc + rows + 2 * cpc) * (int64_t)sizeof(T) + (cols + cpc) * (int64_t)sizeof(int);
+    }
+    // smallest cluster whose shared memory holds `need` bytes (need computed for cs = 1)
+    void choose_cluster(WaveDev& W, int64_t need1) {
+        for (int cs = 1; cs <= 8; cs *= 2) {
+            int64_t per = need1 / cs + need1 / 8 + 2048;
+            if (per <= QC_SMEM_SHARED || (cs == 8 && per <= QC_SMEM_MAX)) {
+                W.cs = cs;
+                W.smem = (int)std::max<int64_t>(per, 4096);
+                return;
+            }
+        }
+        W.cs = 8;
+        W.smem = QC_SMEM_MAX;
+    }
+    void launch_qrcp_cluster(WaveDev& W, double tol) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)(W.n * W.cs));
+        cfg.blockDim = dim3(QC_THREADS);
+        cfg.dynamicSmemBytes = (size_t)W.smem;
+        cfg.stream = s_;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)W.cs;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        unsigned long long* probe = nullptr;
+        if (probe_level_ == cur_level_ && probe_) {
+            probe = probe_;
+            probe_waves_ += 1;
+        }
+        SPAND_CUDA(cudaLaunchKernelEx(&cfg, qrcp3_kernel<T>, ctx_, (const DSpars*)W.items,
+                                      (const DAsn*)pieces_, ws_, jpvt_, tauws_, rank_, colcount_, fallback_, tol,
+                                      W.smem, probe));
     }
     void launch_potrf(int* pivots, int* clusters, int n, int smem) {
-        launch("potrf", [&] { potrf_kernel<T><<<n, 256, smem, s_>>>(ctx_, pivots, clusters, n, smem / (int)sizeof(T)); });
+        launch("potrf", [&] { potrf2_kernel<T><<<n, 256, smem, s_>>>(ctx_, pivots, clusters, n, smem / (int)sizeof(T)); });
     }
     void launch_trsm(const TrsmDev& t) {
         if (!t.ntiles) return;
         launch("trsm", [&] {
-            if (t.side == 1) trsm_kernel<T><<<t.ntiles, TRSM_ROWS, 0, s_>>>(ctx_, t.items, t.tiles, t.ntiles);
-            else trsm_kernel<T><<<t.ntiles, TRSM_COLS * 32, 0, s_>>>(ctx_, t.items, t.tiles, t.ntiles);
+            trsm2_kernel<T><<<t.ntiles, 256, t.smem, s_>>>(ctx_, t.items, t.tiles, t.ntiles, t.smem / (int)sizeof(T));
         });
+    }
+    // shared memory of the POTRF kernel for pivots of size up to nmax: whole block, else one panel
+    static int potrf_smem_n(int nmax) {
+        int64_t full = (int64_t)nmax * nmax * sizeof(T), panel = (int64_t)nmax * PNB * sizeof(T);
+        if (full <= 200 * 1024) return (int)std::max<int64_t>(full, 16);
+        if (panel <= 200 * 1024) return (int)panel;
+        return 0;
+    }
+    static int trsm_smem_n(int nmax) {
+        int64_t b = (int64_t)TRB * nmax * sizeof(T);
+        return b <= 200 * 1024 ? (int)std::max<int64_t>(b, 16) : 0;
+    }
+    int trsm_smem(const std::vector<int>& clusters, const Plan& P) {
+        int mx = 0;
+        for (int c0 : clusters) mx = std::max(mx, P.c_cap[c0]);
+        return trsm_smem_n(mx);
     }
 
     void run_solve(double* x, int nrhs, int ld) {
@@ -1462,14 +2362,14 @@ class DeviceFactor : public DeviceFactorBase {
             LevelDev& D = levels_[l];
             if (D.n_elim_llt)
                 launch("trsv", [&] {
-                    trsv_kernel<T><<<D.n_elim_llt * nrhs, 128, D.x_smem_elim, s_>>>(ctx_, X, D.elim_llt,
+                    trsv2_kernel<T><<<D.n_elim_llt * nrhs, 256, D.x_smem_elim, s_>>>(ctx_, X, D.elim_llt,
                                                                                     D.elim_llt_blk, D.n_elim_llt, 0);
                 });
             if (D.n_gf)
                 launch("gemm_fwd", [&] { gemm_fwd_kernel<T><<<D.n_gf * nrhs, 128, 0, s_>>>(ctx_, X, D.gf, D.gfo, D.n_gf); });
             if (D.n_scale_llt)
                 launch("trsv", [&] {
-                    trsv_kernel<T><<<D.n_scale_llt * nrhs, 128, D.x_smem_scale, s_>>>(ctx_, X, D.scale_llt,
+                    trsv2_kernel<T><<<D.n_scale_llt * nrhs, 256, D.x_smem_scale, s_>>>(ctx_, X, D.scale_llt,
                                                                                       D.scale_llt_blk, D.n_scale_llt, 0);
                 });
             if (D.n_ortho)
@@ -1497,14 +2397,14 @@ class DeviceFactor : public DeviceFactorBase {
                 });
             if (D.n_scale_llt)
                 launch("trsv", [&] {
-                    trsv_kernel<T><<<D.n_scale_llt * nrhs, 128, D.x_smem_scale, s_>>>(ctx_, X, D.scale_llt,
+                    trsv2_kernel<T><<<D.n_scale_llt * nrhs, 256, D.x_smem_scale, s_>>>(ctx_, X, D.scale_llt,
                                                                                       D.scale_llt_blk, D.n_scale_llt, 1);
                 });
             if (D.n_gb)
                 launch("gemm_bwd", [&] { gemm_bwd_kernel<T><<<D.n_gb * nrhs, 128, 0, s_>>>(ctx_, X, D.gb, D.gbo, D.n_gb); });
             if (D.n_elim_llt)
                 launch("trsv", [&] {
-                    trsv_kernel<T><<<D.n_elim_llt * nrhs, 128, D.x_smem_elim, s_>>>(ctx_, X, D.elim_llt,
+                    trsv2_kernel<T><<<D.n_elim_llt * nrhs, 256, D.x_smem_elim, s_>>>(ctx_, X, D.elim_llt,
                                                                                     D.elim_llt_blk, D.n_elim_llt, 1);
                 });
         }
@@ -1528,7 +2428,15 @@ class DeviceFactor : public DeviceFactorBase {
     int *csize_ = nullptr, *rows0_ = nullptr, *rank_ = nullptr, *cpos_ = nullptr;
     DStatus* status_ = nullptr;
     T *vstore_ = nullptr, *taustore_ = nullptr, *tauws_ = nullptr, *ws_ = nullptr, *norms_ = nullptr;
-    int *jpvt_ = nullptr, *ipvt_ = nullptr, *colcount_ = nullptr;
+    int *jpvt_ = nullptr, *ipvt_ = nullptr, *colcount_ = nullptr, *fallback_ = nullptr;
+    bool tuned_ = false;
+    int cur_level_ = -1;
+    // in-kernel phase timing of the QRCP of one level (SPAND_QC_PROBE=<level>)
+    int probe_level_ = getenv("SPAND_QC_PROBE") ? atoi(getenv("SPAND_QC_PROBE")) : -2;
+    unsigned long long* probe_ = nullptr;
+    int probe_waves_ = 0;
+    // per-level kernel classes in the profile (SPAND_PROFILE_LEVELS=1)
+    bool per_level_ = getenv("SPAND_PROFILE_LEVELS") != nullptr;
     DAsn* pieces_ = nullptr;
     DUpd* d_ups_ = nullptr;
     std::vector<LevelDev> levels_;
