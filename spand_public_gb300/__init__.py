@@ -50,6 +50,7 @@ _PROTOS = {
     "spand_tree_factorize": (C.c_int, [C.c_void_p]),
     "spand_tree_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
     "spand_tree_solve_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
+    "spand_tree_solve_device_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
     "spand_cg": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int,
                            C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "spand_cg_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double,

@@ -149,6 +149,12 @@ int spand_tree_solve_device(spand_tree* t, double* x, int nrhs, int ld) {
     return guard([&] { t->t->solve_device(x, nrhs, ld); });
 }
 
+int spand_tree_solve_device_noalloc(spand_tree* t, double* x, int nrhs, int ld) {
+    CHECK_T(t);
+    if (!x || nrhs < 1 || ld < t->t->get_N()) return fail(SPAND_ERR_ARG, "invalid vector arguments");
+    return guard([&] { t->t->solve_device_noalloc(x, nrhs, ld); });
+}
+
 int spand_cg(spand_tree* t, const double* b, double* x, int iters, double tol, int verb, int* iters_out,
              double* relres_out) {
     CHECK_T(t);

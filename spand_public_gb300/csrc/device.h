@@ -94,6 +94,9 @@ class DeviceFactorBase {
     KernelProfiler& profiler() { return prof_; }
     // capture the solve on buffer x as a CUDA graph; solve_device(x, ...) then replays it
     virtual void capture_solve(double* x, int nrhs, int ld) = 0;
+    // solve_device with the per-cluster solve vectors in a fixed device array instead of
+    // memory allocated by this object (no allocation of any kind on this path)
+    virtual void solve_device_noalloc(double* x, int nrhs, int ld) = 0;
 
    protected:
     int64_t launches_ = 0;

@@ -14,6 +14,7 @@
 #include <climits>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -1700,6 +1701,45 @@ void KernelProfiler::clear() {
 }
 
 // ------------------------------------------------------------------------------------
+// Allocation-free solve: fixed scratch for the per-cluster solve vectors
+// ------------------------------------------------------------------------------------
+// Some callers cannot allocate device memory at the moment they need a solve: code that
+// is being captured into a CUDA graph (cudaMalloc is not allowed while a stream captures
+// in the global or thread-local mode), code running under a fixed memory budget that
+// preallocates everything up front, or a host framework that owns the device allocator.
+// For them the solve can use this array instead of vectors owned by the factor.  It is
+// part of the library image, so every GPU that loads the library holds these 16 MiB
+// until the process exits.  All calls share it: two allocation-free solves that overlap
+// on the GPU (different streams, or different trees on different streams) race on it.
+// Nothing in it has to start at zero: every slot a solve reads was written earlier in the
+// same solve.
+constexpr size_t kNoAllocSolveScratchBytes = size_t(16) << 20;
+static __device__ __align__(256) unsigned char g_noalloc_solve_scratch[kNoAllocSolveScratchBytes];
+
+constexpr int kMaxDevices = 64;
+static void* g_noalloc_scratch_addr[kMaxDevices];
+static std::once_flag g_noalloc_scratch_once[kMaxDevices];
+
+// Device address of the scratch array on the current device.  In host code the array's
+// name is only a host-side stand-in, so the address is looked up with
+// cudaGetSymbolAddress, once per device, with that device current (the first
+// allocation-free solve on a device does this; make that first call before any stream
+// capture).
+static void* noalloc_solve_scratch() {
+    int dev = 0;
+    SPAND_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) throw DeviceError{SPAND_ERR_UNSUPPORTED, "device index out of range"};
+    std::call_once(g_noalloc_scratch_once[dev], [dev] {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_solve_scratch);
+        if (e != cudaSuccess || p == nullptr)
+            throw DeviceError{SPAND_ERR_CUDA, std::string("cudaGetSymbolAddress(solve scratch): ") + cudaGetErrorString(e)};
+        g_noalloc_scratch_addr[dev] = p;
+    });
+    return g_noalloc_scratch_addr[dev];
+}
+
+// ------------------------------------------------------------------------------------
 // Host driver
 // ------------------------------------------------------------------------------------
 template <typename V>
@@ -2092,6 +2132,27 @@ class DeviceFactor : public DeviceFactorBase {
         run_solve(x, nrhs, ld);
     }
 
+    void solve_device_noalloc(double* x, int nrhs, int ld) override {
+        if (!factored_) throw DeviceError{SPAND_ERR_STATE, "solve before factorize"};
+        const size_t need = (size_t)xld_ * (size_t)nrhs * sizeof(T);
+        if (need > kNoAllocSolveScratchBytes)
+            throw DeviceError{SPAND_ERR_ARG, "allocation-free solve needs " + std::to_string(need) +
+                                                 " bytes of solve vectors (" + std::to_string(xld_) + " x " +
+                                                 std::to_string(nrhs) + " x " + std::to_string(sizeof(T)) +
+                                                 "); its fixed scratch holds " +
+                                                 std::to_string(kNoAllocSolveScratchBytes) + " bytes"};
+        T* slots = static_cast<T*>(noalloc_solve_scratch());
+        const bool was_on = prof_.enabled();  // the profiler creates CUDA events
+        prof_.enable(false);
+        try {
+            run_solve_slots(x, nrhs, ld, slots);
+        } catch (...) {
+            prof_.enable(was_on);
+            throw;
+        }
+        prof_.enable(was_on);
+    }
+
     void capture_solve(double* x, int nrhs, int ld) override {
         if (!factored_) throw DeviceError{SPAND_ERR_STATE, "solve before factorize"};
         // the graph reads every size from device memory, so it stays valid across
@@ -2350,9 +2411,11 @@ class DeviceFactor : public DeviceFactorBase {
         return trsm_smem_n(mx);
     }
 
-    void run_solve(double* x, int nrhs, int ld) {
+    void run_solve(double* x, int nrhs, int ld) { run_solve_slots(x, nrhs, ld, xs_); }
+
+    void run_solve_slots(double* x, int nrhs, int ld, T* slots) {
         const Plan& P = *P_;
-        XCtx<T> X{xs_, (long long)xld_, d_xoff_, nrhs};
+        XCtx<T> X{slots, (long long)xld_, d_xoff_, nrhs};
         const int n = (int)perm_h_.size();
         const long long tot = (long long)n * nrhs;
         launch("perm", [&] {

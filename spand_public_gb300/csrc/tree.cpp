@@ -196,6 +196,16 @@ void Tree::solve_device(double* x, int nrhs, int ld) const {
     }
 }
 
+void Tree::solve_device_noalloc(double* x, int nrhs, int ld) const {
+    if (!factored_) throw std::logic_error("solve() before factorize()");
+    try {
+        dev_->solve_device_noalloc(x, nrhs, ld);
+    } catch (spand::DeviceError& e) {
+        if (e.status == spand::SPAND_ERR_ARG) throw std::invalid_argument(e.msg);
+        throw std::runtime_error(e.msg);
+    }
+}
+
 void Tree::solve(double* x, int nrhs, int ld) const {
     if (ld < 0) ld = get_N();
     const size_t len = (size_t)ld * nrhs;

@@ -65,6 +65,8 @@ class Tree {
     void solve(double* x, int nrhs = 1, int ld = -1) const;
     // device vector(s)
     void solve_device(double* x, int nrhs, int ld) const;
+    // device vector(s), allocating nothing (fixed scratch shared by all such calls)
+    void solve_device_noalloc(double* x, int nrhs, int ld) const;
 
     int get_N() const { return (int)perm_.size(); }
     const std::vector<int>& get_assembly_perm() const { return perm_; }
