@@ -121,40 +121,101 @@ __device__ T warp_sum(T v) {
     return v;
 }
 
+// Inverse of a lower Cholesky factor, written transposed into the strictly upper triangle
+// of the same block: after the call, for i > j, A[j + i*ld] = (L^{-1})[i][j]; the diagonal
+// of L^{-1} is 1/L[i][i] and is not stored.  Right-looking forward substitution on all
+// columns of the identity at once (n steps, two barriers each).
+template <typename T>
+__device__ void trtri_to_upper(T* A, int ld, int n) {
+    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+        int j = idx % n, i = idx / n;
+        if (i > j) A[j + (size_t)i * ld] = T(0);
+    }
+    __syncthreads();
+    for (int k = 0; k < n; k++) {
+        const T dinv = T(1) / A[k + (size_t)k * ld];
+        for (int j = threadIdx.x; j < k; j += blockDim.x) A[j + (size_t)k * ld] *= dinv;
+        __syncthreads();
+        // R[i, j] -= L[i, k] * Y[k, j] for i > k, j <= k
+        const int m = n - k - 1, w = k + 1;
+        for (int idx = threadIdx.x; idx < m * w; idx += blockDim.x) {
+            const int j = idx % w, i = k + 1 + idx / w;
+            const T ykj = (j == k) ? dinv : A[j + (size_t)k * ld];
+            A[j + (size_t)i * ld] -= A[i + (size_t)k * ld] * ykj;
+        }
+        __syncthreads();
+    }
+}
+
 // ------------------------------------------------------------------------------------
-// Cholesky of pivot blocks, blocked (tree.cpp:582-593).  One block per pivot.  When the
-// whole block fits in shared memory it is factored there column by column; otherwise
-// 32-column panels are staged in shared memory, updated left-looking from the factored
-// columns (read from global memory, L1/L2 resident) and factored in place.
+// Cholesky of pivot blocks, blocked left-looking with 32-column panels (dpotrf 'L',
+// tree.cpp:582-593).  One block per pivot; the block is staged in shared memory when it
+// fits, else factored in place in global memory.  Per panel: (1) update by the factored
+// columns, (2) the 32x32 diagonal block by one warp with shuffles, (3) the rows below by
+// a triangular solve, one row per thread.  Three barriers per panel.
 // ------------------------------------------------------------------------------------
 constexpr int PNB = 32;
 
 template <typename T>
-__device__ bool chol_inplace_smem(T* A, int ld, int m, int w, T* dsh, int* bad) {
-    // factor the leading w columns of an m x w panel (diagonal block on top)
-    for (int j = 0; j < w; j++) {
-        if (threadIdx.x == 0) {
-            T ajj = A[j + (size_t)j * ld];
-            if (!(ajj > T(0))) {
-                *bad = 1;
-                *dsh = T(1);
-            } else {
-                *dsh = dsqrt(ajj);
+__device__ bool chol_blocked(T* A, int ld, int n, int* bad) {
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = blockDim.x >> 5;
+    for (int jb = 0; jb < n; jb += PNB) {
+        const int w = min(PNB, n - jb);
+        if (jb > 0) {
+            for (int jj = ty; jj < w; jj += nty) {
+                const int j = jb + jj;
+                for (int i = j + tx; i < n; i += 32) {
+                    T s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+                    int k = 0;
+                    for (; k + 3 < jb; k += 4) {
+                        s0 += A[i + (size_t)k * ld] * A[j + (size_t)k * ld];
+                        s1 += A[i + (size_t)(k + 1) * ld] * A[j + (size_t)(k + 1) * ld];
+                        s2 += A[i + (size_t)(k + 2) * ld] * A[j + (size_t)(k + 2) * ld];
+                        s3 += A[i + (size_t)(k + 3) * ld] * A[j + (size_t)(k + 3) * ld];
+                    }
+                    for (; k < jb; k++) s0 += A[i + (size_t)k * ld] * A[j + (size_t)k * ld];
+                    A[i + (size_t)j * ld] -= (s0 + s1) + (s2 + s3);
+                }
             }
-            A[j + (size_t)j * ld] = *dsh;
+            __syncthreads();
+        }
+        if (ty == 0) {
+            int fail = 0;
+            for (int j = 0; j < w; j++) {
+                T* cj = A + (size_t)(jb + j) * ld + jb;
+                T d = 0;
+                if (tx == j) {
+                    d = cj[j];
+                    if (!(d > T(0))) {
+                        fail = 1;
+                        d = T(1);
+                    } else {
+                        d = dsqrt(d);
+                    }
+                    cj[j] = d;
+                }
+                d = __shfl_sync(0xffffffffu, d, j);
+                fail = __shfl_sync(0xffffffffu, fail, j);
+                if (fail) break;
+                if (tx > j && tx < w) cj[tx] /= d;
+                __syncwarp();
+                if (tx > j && tx < w) {
+                    const T lij = cj[tx];
+                    for (int kk = j + 1; kk <= tx; kk++) A[(jb + tx) + (size_t)(jb + kk) * ld] -= lij * cj[kk];
+                }
+                __syncwarp();
+            }
+            if (tx == 0 && fail) *bad = 1;
         }
         __syncthreads();
         if (*bad) return false;
-        const T inv = T(1) / *dsh;
-        for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) A[i + (size_t)j * ld] *= inv;
-        __syncthreads();
-        const int wc = w - j - 1;  // trailing columns inside the panel
-        const int mr = m - j - 1;
-        for (int idx = threadIdx.x; idx < mr * wc; idx += blockDim.x) {
-            int ii = idx % mr, kk = idx / mr;
-            if (ii < kk) continue;
-            int i = j + 1 + ii, k = j + 1 + kk;
-            A[i + (size_t)k * ld] -= A[i + (size_t)j * ld] * A[k + (size_t)j * ld];
+        // rows below the diagonal block: x_j = (a_j - sum_{l<j} x_l L[jb+j][jb+l]) / L[jb+j][jb+j]
+        for (int i = jb + w + threadIdx.x; i < n; i += blockDim.x) {
+            for (int j = 0; j < w; j++) {
+                T x = A[i + (size_t)(jb + j) * ld];
+                for (int l = 0; l < j; l++) x -= A[i + (size_t)(jb + l) * ld] * A[(jb + j) + (size_t)(jb + l) * ld];
+                A[i + (size_t)(jb + j) * ld] = x / A[(jb + j) + (size_t)(jb + j) * ld];
+            }
         }
         __syncthreads();
     }
@@ -162,14 +223,14 @@ __device__ bool chol_inplace_smem(T* A, int ld, int m, int w, T* dsh, int* bad) 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) potrf2_kernel(Ctx<T> c, const int* __restrict__ pivots,
-                                                     const int* __restrict__ clusters, int count, int smem_elems) {
+__global__ void __launch_bounds__(256) potrf3_kernel(Ctx<T> c, const int* __restrict__ pivots,
+                                                     const int* __restrict__ clusters, int count, int smem_elems,
+                                                     int strip_max_n) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
     const int item = blockIdx.x;
     if (item >= count) return;
     __shared__ int failed;
-    __shared__ T dsh;
     __shared__ int bad;
     if (threadIdx.x == 0) {
         failed = *(volatile int*)&c.status->not_spd;
@@ -182,62 +243,94 @@ __global__ void __launch_bounds__(256) potrf2_kernel(Ctx<T> c, const int* __rest
     if (n == 0) return;
     T* G = bptr(c, pivots[item]);
     const int gld = c.blk[pivots[item]].ld;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = blockDim.x >> 5;
     if ((long long)n * n <= smem_elems) {
-        for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
-            int i = idx % n, j = idx / n;
-            if (i >= j) sm[i + j * n] = G[i + (size_t)j * gld];
-        }
+        for (int j = ty; j < n; j += nty)
+            for (int i = j + tx; i < n; i += 32) sm[i + j * n] = G[i + (size_t)j * gld];
         __syncthreads();
-        bool ok = chol_inplace_smem(sm, n, n, n, &dsh, &bad);
-        if (ok)
-            for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
-                int i = idx % n, j = idx / n;
-                if (i >= j) G[i + (size_t)j * gld] = sm[i + j * n];
-            }
-    } else if ((long long)n * PNB <= smem_elems) {
-        for (int jb = 0; jb < n && !bad; jb += PNB) {
-            const int w = min(PNB, n - jb), m = n - jb;
-            T* P = sm;  // m x w, ld m
-            for (int idx = threadIdx.x; idx < m * w; idx += blockDim.x) {
-                int i = idx % m, j = idx / m;
-                P[i + j * m] = G[(jb + i) + (size_t)(jb + j) * gld];
-            }
-            __syncthreads();
-            // left-looking update with the factored columns 0..jb
-            for (int idx = threadIdx.x; idx < m * w; idx += blockDim.x) {
-                int i = idx % m, j = idx / m;
-                if (i < j) continue;
-                T s = 0;
-                const T* ai = G + (jb + i);
-                const T* aj = G + (jb + j);
-                for (int k = 0; k < jb; k++) s += ai[(size_t)k * gld] * aj[(size_t)k * gld];
-                P[i + j * m] -= s;
-            }
-            __syncthreads();
-            if (!chol_inplace_smem(P, m, m, w, &dsh, &bad)) break;
-            for (int idx = threadIdx.x; idx < m * w; idx += blockDim.x) {
-                int i = idx % m, j = idx / m;
-                if (i >= j) G[(jb + i) + (size_t)(jb + j) * gld] = P[i + j * m];
-            }
-            __syncthreads();
+        if (chol_blocked(sm, n, n, &bad)) {
+            for (int j = ty; j < n; j += nty)
+                for (int i = j + tx; i < n; i += 32) G[i + (size_t)j * gld] = sm[i + j * n];
         }
     } else {
-        // panel larger than the shared-memory budget: factor in global memory
-        chol_inplace_smem(G, gld, n, n, &dsh, &bad);
+        chol_blocked(G, gld, n, &bad);
     }
+    __syncthreads();
+    // pivots too large for the strip-wise inverse kernel get their inverse here
+    if (!bad && n > strip_max_n) trtri_to_upper(G, gld, n);
     if (bad && threadIdx.x == 0) atomicCAS(&c.status->not_spd, 0, cl + 1);
 }
 
 // ------------------------------------------------------------------------------------
-// Triangular solves of edge blocks with a cluster's Cholesky factor (tree.cpp:640-663),
-// a tile of the block staged in shared memory.
-// side 1: B (m x n) <- B L^{-T}: tile of TRB rows; side 0: B (n x m) <- L^{-1} B: tile of
-// TRB columns.  Right-looking over the n columns / rows of L.
+// Inverse of the Cholesky factors, stored transposed in the strictly upper triangle of
+// the pivot block: A[j + i*ld] = (L^{-1})[i][j] for i > j (the diagonal, 1/L[i][i], is
+// not stored).  One block per 32-column strip of L^{-1}: row blocks of 32 in order, each
+// = L_ii^{-1} (E - L[ib, jb:ib] Y[jb:ib]) with the small triangular solves done by warps
+// with shuffles.  The strip (n x 32) lives in shared memory.
 // ------------------------------------------------------------------------------------
-constexpr int TRB = 32;
-
 template <typename T>
-__global__ void __launch_bounds__(256) trsm2_kernel(Ctx<T> c, const DTrsm* __restrict__ items,
+__global__ void __launch_bounds__(256) trtri_kernel(Ctx<T> c, const int* __restrict__ pivots,
+                                                    const int* __restrict__ clusters, const DTile* __restrict__ tiles,
+                                                    int ntiles, int smem_elems) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* Y = reinterpret_cast<T*>(smem_raw);  // Y[i + jj * n], rows i >= jb
+    const int t = blockIdx.x;
+    if (t >= ntiles || c.status->not_spd) return;
+    const int item = tiles[t].item;
+    const int cl = clusters[item];
+    const int n = c.csize[cl];
+    const int jb = tiles[t].tile_i * 32;
+    if (jb >= n || (long long)n * 32 > smem_elems) return;  // large pivots: inverted by potrf3_kernel
+    const int w = min(32, n - jb);
+    T* A = bptr(c, pivots[item]);
+    const int ld = c.blk[pivots[item]].ld;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = blockDim.x >> 5;
+    for (int ib = jb; ib < n; ib += 32) {
+        const int h = min(32, n - ib);
+        // R = E - L[ib:ib+h, jb:ib] Y[jb:ib, :]
+        for (int jj = ty; jj < w; jj += nty) {
+            if (tx < h) {
+                const int i = ib + tx;
+                T s0 = 0, s1 = 0;
+                int k = jb;
+                for (; k + 1 < ib; k += 2) {
+                    s0 += A[i + (size_t)k * ld] * Y[k + jj * n];
+                    s1 += A[i + (size_t)(k + 1) * ld] * Y[(k + 1) + jj * n];
+                }
+                for (; k < ib; k++) s0 += A[i + (size_t)k * ld] * Y[k + jj * n];
+                Y[i + jj * n] = T(i == jb + jj ? 1 : 0) - (s0 + s1);
+            }
+        }
+        __syncthreads();
+        // Y[ib:ib+h, jj] = L_ii^{-1} R[:, jj]: a warp per column, lanes are rows
+        const T dii = tx < h ? A[(ib + tx) + (size_t)(ib + tx) * ld] : T(1);
+        for (int jj = ty; jj < w; jj += nty) {
+            T acc = tx < h ? Y[(ib + tx) + jj * n] : T(0);
+            for (int r = 0; r < h; r++) {
+                const T yr = __shfl_sync(0xffffffffu, acc / dii, r);
+                if (tx == r) acc = yr;
+                else if (tx > r && tx < h) acc -= A[(ib + tx) + (size_t)(ib + r) * ld] * yr;
+            }
+            if (tx < h) Y[(ib + tx) + jj * n] = acc;
+        }
+        __syncthreads();
+    }
+    // strip -> strictly upper triangle, transposed
+    for (int jj = ty; jj < w; jj += nty)
+        for (int i = jb + jj + 1 + tx; i < n; i += 32) A[(jb + jj) + (size_t)i * ld] = Y[i + jj * n];
+}
+
+constexpr int TRB = 32;  // independent indices per TRSM tile
+
+// ------------------------------------------------------------------------------------
+// Triangular solves of edge blocks as triangular products with the inverse factor
+// (tree.cpp:640-663): out[q][c] = sum_{k<=c} X[q][k] * Linv[c][k], where q runs over the
+// independent index (row of B for side 1: B L^{-T}; column of B for side 0: L^{-1} B).
+// A tile of 32 independent indices is staged in shared memory; every thread computes
+// columns c of one q with four partial sums; no barrier after the staging.
+// ------------------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) trsm3_kernel(Ctx<T> c, const DTrsm* __restrict__ items,
                                                    const DTile* __restrict__ tiles, int ntiles, int smem_elems) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* X = reinterpret_cast<T*>(smem_raw);
@@ -254,61 +347,58 @@ __global__ void __launch_bounds__(256) trsm2_kernel(Ctx<T> c, const DTrsm* __res
     const int r0 = tiles[t].tile_i * TRB;
     if (r0 >= m) return;
     const int tr = min(TRB, m - r0);
-    // element (q, k): q the independent index (row of B for side 1, column for side 0),
-    // k the index solved over; staged in shared memory as X[q + k*tr] when it fits
+    // element (q, k) of B: side 1 B[(r0+q) + k*bld], side 0 B[k + (r0+q)*bld]
+    const long long sq = it.side == 1 ? 1 : bld, sk = it.side == 1 ? bld : 1;
+    T* Bt = B + (it.side == 1 ? (size_t)r0 : (size_t)r0 * bld);
     const bool staged = (long long)tr * n <= smem_elems;
-    T* base;
-    long long sq, sk;
+    const T* src;
+    long long xq, xk;
     if (staged) {
-        base = X;
-        sq = 1;
-        sk = tr;
-        if (it.side == 1) {
-            for (int idx = threadIdx.x; idx < tr * n; idx += blockDim.x) {
-                int q = idx % tr, k = idx / tr;
-                X[q + k * tr] = B[(r0 + q) + (size_t)k * bld];
-            }
-        } else {
-            for (int idx = threadIdx.x; idx < tr * n; idx += blockDim.x) {
-                int k = idx % n, q = idx / n;
-                X[q + k * tr] = B[k + (size_t)(r0 + q) * bld];
-            }
+        for (int idx = threadIdx.x; idx < tr * n; idx += blockDim.x) {
+            int q, k;
+            if (it.side == 1) { q = idx % tr; k = idx / tr; } else { k = idx % n; q = idx / n; }
+            X[q + k * TRB] = Bt[q * sq + k * sk];
         }
         __syncthreads();
-    } else if (it.side == 1) {
-        base = B + r0;
-        sq = 1;
-        sk = bld;
+        src = X;
+        xq = 1;
+        xk = TRB;
     } else {
-        base = B + (size_t)r0 * bld;
-        sq = bld;
-        sk = 1;
+        // too large for the shared-memory budget: a copy is needed since B is overwritten
+        // column by column; process the columns in decreasing order so that every column
+        // is read before it is written (out[., c] needs X[., k <= c] only)
+        src = nullptr;
+        xq = xk = 0;
     }
-    // both sides solve x L^T = b per independent index: x_j = (b_j - sum_{k<j} x_k L[j,k]) / L[j,j]
     const int q = threadIdx.x % TRB;
-    const int lanes = blockDim.x / TRB;
-    const int sub = threadIdx.x / TRB;
-    for (int j = 0; j < n; j++) {
-        const T d = L[j + (size_t)j * lld];
-        if (sub == 0 && q < tr) base[q * sq + j * sk] /= d;
-        __syncthreads();
-        if (q < tr) {
-            const T xj = base[q * sq + j * sk];
-            const T* lj = L + (size_t)j * lld;
-            for (int k = j + 1 + sub; k < n; k += lanes) base[q * sq + k * sk] -= xj * lj[k];
-        }
-        __syncthreads();
-    }
+    const int sub = threadIdx.x / TRB, lanes = blockDim.x / TRB;
     if (staged) {
-        if (it.side == 1) {
-            for (int idx = threadIdx.x; idx < tr * n; idx += blockDim.x) {
-                int qq = idx % tr, k = idx / tr;
-                B[(r0 + qq) + (size_t)k * bld] = X[qq + k * tr];
+        if (q < tr) {
+            for (int cc = sub; cc < n; cc += lanes) {
+                const T* lrow = L + (size_t)cc * lld;  // (L^{-1})[cc][k] = lrow[k], k < cc
+                const T* xr = src + q * xq;
+                T s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+                int k = 0;
+                for (; k + 3 < cc; k += 4) {
+                    s0 += xr[k * xk] * lrow[k];
+                    s1 += xr[(k + 1) * xk] * lrow[k + 1];
+                    s2 += xr[(k + 2) * xk] * lrow[k + 2];
+                    s3 += xr[(k + 3) * xk] * lrow[k + 3];
+                }
+                for (; k < cc; k++) s0 += xr[k * xk] * lrow[k];
+                const T diag = xr[cc * xk] / L[cc + (size_t)cc * lld];
+                Bt[q * sq + cc * sk] = (s0 + s1) + (s2 + s3) + diag;
             }
-        } else {
-            for (int idx = threadIdx.x; idx < tr * n; idx += blockDim.x) {
-                int k = idx % n, qq = idx / n;
-                B[k + (size_t)(r0 + qq) * bld] = X[qq + k * tr];
+        }
+    } else {
+        // in place from the last column down; one thread group per q, columns in sequence
+        if (sub == 0 && q < tr) {
+            T* xr = Bt + q * sq;
+            for (int cc = n - 1; cc >= 0; cc--) {
+                const T* lrow = L + (size_t)cc * lld;
+                T s = 0;
+                for (int k = 0; k < cc; k++) s += xr[k * sk] * lrow[k];
+                xr[cc * sk] = s + xr[cc * sk] / L[cc + (size_t)cc * lld];
             }
         }
     }
@@ -1262,12 +1352,53 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp3_kernel(Ctx<T> c, const DSpar
     if (me == 0 && tid == 0) rank_out[it.cluster] = rank;
 }
 
+// Blocked compact WY form of Q = H_0 ... H_{k-1}: reflectors in blocks of QB = 32,
+// Q = Q_0 Q_1 ..., Q_b = I - V_b T_b V_b^T with T_b the 32x32 upper triangular factor of
+// block b (LAPACK dlarft, forward, columnwise, per block).  One warp per block: lanes
+// compute Z_b = striu(V_b^T V_b) then the 32-step recurrence
+// T_b[j][i] = -tau_i sum_{l=j}^{i-1} T_b[j][l] Z_b[l][i].  T_b is stored in the diagonal
+// block b of the k x k T store (ld ldt); Z uses the same positions of the scratch zs.
+constexpr int QB = 32;
+
+template <typename T>
+__device__ void larft_blocks(const T* V, int ldv, int rows, int k, const T* tau, T* Tm, int ldt, T* zs) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int nb = (k + QB - 1) / QB;
+    for (int b = w; b < nb; b += nw) {
+        const int i0 = b * QB, bw = min(QB, k - i0);
+        T* Z = zs + (size_t)i0 + (size_t)i0 * ldt;
+        T* Tb = Tm + (size_t)i0 + (size_t)i0 * ldt;
+        // Z[j][i] = v_j^T v_i, j < i (overlap from row i0+i where v_i is 1)
+        for (int i = 1; i < bw; i++) {
+            const T* vi = V + (size_t)(i0 + i) * ldv;
+            for (int j = 0; j < i; j++) {
+                const T* vj = V + (size_t)(i0 + j) * ldv;
+                T s = 0;
+                for (int r = i0 + i + 1 + lane; r < rows; r += 32) s += vj[r] * vi[r];
+                s = warp_sum(s);
+                if (lane == 0) Z[j + (size_t)i * ldt] = vj[i0 + i] + s;
+            }
+        }
+        __syncwarp();
+        for (int i = 0; i < bw; i++) {
+            if (lane < i) {
+                T s = 0;
+                for (int l = lane; l < i; l++) s += Tb[lane + (size_t)l * ldt] * Z[l + (size_t)i * ldt];
+                Tb[lane + (size_t)i * ldt] = -tau[i0 + i] * s;
+            }
+            if (lane == i) Tb[i + (size_t)i * ldt] = tau[i0 + i];
+            __syncwarp();
+        }
+    }
+}
+
 // Compressed edges AsnP = triu(R[:k,:]) P^T written back into the cluster's edge blocks,
 // reflectors saved for the Orthogonal op, cluster size set to the rank.
 template <typename T>
 __global__ void sparsify_scatter_kernel(Ctx<T> c, const DSpars* __restrict__ items, const DAsn* __restrict__ pieces,
-                                        const T* ws, int* jpvt_ws, int* ipvt_ws, const int* __restrict__ rank_in,
-                                        T* vstore, const T* taus_ws, T* taustore, const int* __restrict__ colcount) {
+                                        T* ws, int* jpvt_ws, int* ipvt_ws, const int* __restrict__ rank_in,
+                                        T* vstore, const T* taus_ws, T* taustore, const int* __restrict__ colcount,
+                                        T* tstore) {
     if (c.status->not_spd) return;
     const DSpars it = items[blockIdx.x];
     const int rows = c.csize[it.cluster];
@@ -1278,6 +1409,7 @@ __global__ void sparsify_scatter_kernel(Ctx<T> c, const DSpars* __restrict__ ite
     const T* A = ws + it.ws_off;
     const int* jpvt = jpvt_ws + it.col_off;
     int* ipvt = ipvt_ws + it.col_off;
+    (void)0;
     if (k > 0)
         for (int j = threadIdx.x; j < cols; j += blockDim.x) {
             const int q = jpvt[j];
@@ -1307,6 +1439,9 @@ __global__ void sparsify_scatter_kernel(Ctx<T> c, const DSpars* __restrict__ ite
         col += n;
     }
     __syncthreads();
+    // WY triangular factor of the reflectors, for the solve; the QRCP workspace (R is no
+    // longer needed) holds the k x k scratch
+    larft_blocks(V, ld, rows, k, taus_ws + it.tau_off, tstore + it.v_off, ld, ws + it.ws_off);
     if (threadIdx.x == 0) c.csize[it.cluster] = k;
 }
 
@@ -1386,12 +1521,12 @@ __global__ void perm_out_kernel(double* __restrict__ x, int ldx, XCtx<T> X, cons
 }
 
 // ------------------------------------------------------------------------------------
-// Blocked triangular solve of the ScalingLLT ops (operations.cpp:97-103): 32x32
-// diagonal blocks solved by one warp with shuffles (block held in registers), the
-// off-diagonal panel applied by the whole block; two barriers per 32 columns.
+// ScalingLLT ops of the solve (operations.cpp:97-103) as triangular products with the
+// inverse factor: fwd y[c] = sum_{k<=c} Linv[c][k] x[k] (a warp per c), bwd
+// y[c] = sum_{k>=c} Linv[k][c] x[k] (a thread per c).  One barrier.
 // ------------------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(256) trsv2_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ clusters,
+__global__ void __launch_bounds__(512) trsv3_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ clusters,
                                                    const int* __restrict__ lblocks, int count, int trans) {
     const int item = blockIdx.x % count;
     const int r = blockIdx.x / count;
@@ -1406,172 +1541,176 @@ __global__ void __launch_bounds__(256) trsv2_kernel(Ctx<T> c, XCtx<T> X, const i
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int i = threadIdx.x; i < n; i += blockDim.x) xs[i] = x[i];
     __syncthreads();
-    const int nb = (n + 31) / 32;
     if (!trans) {
-        for (int b = 0; b < nb; b++) {
-            const int kb = b * 32, bw = min(32, n - kb);
-            if (w == 0) {
-                // lane i holds row i of the diagonal block and x_{kb+i}
-                T lrow[32];
-#pragma unroll
-                for (int k = 0; k < 32; k++) lrow[k] = (lane < bw && k <= lane) ? L[(kb + lane) + (size_t)(kb + k) * ld] : T(0);
-                T xi = lane < bw ? xs[kb + lane] : T(0);
-#pragma unroll
-                for (int k = 0; k < 32; k++) {
-                    if (k < bw) {
-                        const T xk = __shfl_sync(0xffffffffu, lane == k ? xi / lrow[k] : T(0), k);
-                        if (lane == k) xi = xk;
-                        else if (lane > k) xi -= lrow[k] * xk;
-                    }
-                }
-                if (lane < bw) xs[kb + lane] = xi;
-            }
-            __syncthreads();
-            for (int i = kb + bw + threadIdx.x; i < n; i += blockDim.x) {
-                T s = 0;
-                for (int k = 0; k < bw; k++) s += L[i + (size_t)(kb + k) * ld] * xs[kb + k];
-                xs[i] -= s;
-            }
-            __syncthreads();
+        for (int cc = w; cc < n; cc += nw) {
+            const T* lrow = L + (size_t)cc * ld;
+            T s = 0;
+            for (int k = lane; k < cc; k += 32) s += lrow[k] * xs[k];
+            s = warp_sum(s);
+            if (lane == 0) x[cc] = s + xs[cc] / L[cc + (size_t)cc * ld];
         }
     } else {
-        for (int b = nb - 1; b >= 0; b--) {
-            const int kb = b * 32, bw = min(32, n - kb);
-            // x[kb+k] -= L[kb+bw:n, kb+k]^T x[kb+bw:n], warp per k
-            for (int k = w; k < bw; k += nw) {
-                const T* lk = L + (size_t)(kb + k) * ld;
-                T s = 0;
-                for (int i = kb + bw + lane; i < n; i += 32) s += lk[i] * xs[i];
-                s = warp_sum(s);
-                if (lane == 0) xs[kb + k] -= s;
+        for (int cc = threadIdx.x; cc < n; cc += blockDim.x) {
+            T s0 = 0, s1 = 0;
+            int k = cc + 1;
+            for (; k + 1 < n; k += 2) {
+                s0 += L[cc + (size_t)k * ld] * xs[k];
+                s1 += L[cc + (size_t)(k + 1) * ld] * xs[k + 1];
             }
-            __syncthreads();
-            if (w == 0) {
-                // lane i holds column i of the diagonal block (row i of L^T) and x_{kb+i}
-                T lcol[32];
-#pragma unroll
-                for (int k = 0; k < 32; k++) lcol[k] = (lane < bw && k < bw && k >= lane) ? L[(kb + k) + (size_t)(kb + lane) * ld] : T(0);
-                T xi = lane < bw ? xs[kb + lane] : T(0);
-#pragma unroll
-                for (int kk = 31; kk >= 0; kk--) {
-                    if (kk < bw) {
-                        T xk = __shfl_sync(0xffffffffu, lane == kk ? xi / lcol[kk] : T(0), kk);
-                        if (lane == kk) xi = xk;
-                        else if (lane < kk) xi -= lcol[kk] * xk;
-                    }
-                }
-                if (lane < bw) xs[kb + lane] = xi;
-            }
-            __syncthreads();
+            for (; k < n; k++) s0 += L[cc + (size_t)k * ld] * xs[k];
+            x[cc] = (s0 + s1) + xs[cc] / L[cc + (size_t)cc * ld];
         }
     }
-    for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = xs[i];
 }
 
-// Forward Gemm ops grouped by neighbour: x_n -= A_ns x_s (GemmSymmOut) or A_sn^T x_s (GemmSymmIn)
+// Forward Gemm ops grouped by neighbour n (operations.cpp:55-93): x_n -= sum over the
+// group's ops of A_ns x_s (GemmSymmOut) or A_sn^T x_s (GemmSymmIn), in op order.  One
+// block per (group, 64 rows of x_n); 4 threads per row split the columns, partial sums
+// reduced in a fixed order.
+constexpr int GF_ROWS = 64;
+
 template <typename T>
-__global__ void gemm_fwd_kernel(Ctx<T> c, XCtx<T> X, const DGroup* __restrict__ groups, const DGemmOp* __restrict__ ops,
-                                int ngroups) {
-    const int g = blockIdx.x % ngroups;
-    const int r = blockIdx.x / ngroups;
-    const DGroup G = groups[g];
+__global__ void __launch_bounds__(256) gemm_fwd2_kernel(Ctx<T> c, XCtx<T> X, const DGroup* __restrict__ groups,
+                                                        const DGemmOp* __restrict__ ops, const DTile* __restrict__ tiles,
+                                                        int ntiles, int rhs_stride) {
+    const int t = blockIdx.x % ntiles;
+    const int r = blockIdx.x / ntiles;
+    const DGroup G = groups[tiles[t].item];
     const int nb = G.key;
     const int nn = c.rows0[nb];
+    const int i0 = tiles[t].tile_i * GF_ROWS;
+    if (i0 >= nn) return;
+    (void)rhs_stride;
+    __shared__ T part[4][GF_ROWS];
     T* xn = X.xs + X.xoff[nb] + r * X.xld;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int li = threadIdx.x % GF_ROWS, sp = threadIdx.x / GF_ROWS;
+    const int i = i0 + li;
+    T acc = 0;
     for (int o = 0; o < G.count; o++) {
         const DGemmOp op = ops[G.first + o];
         const int ns = c.csize[op.self];
         const T* xs = X.xs + X.xoff[op.self] + r * X.xld;
         const T* A = bptr(c, op.block);
         const int ld = c.blk[op.block].ld;
-        if (op.kind == 1) {
-            for (int i = threadIdx.x; i < nn; i += blockDim.x) {
-                T s = 0;
-                for (int j = 0; j < ns; j++) s += A[i + (size_t)j * ld] * xs[j];
-                xn[i] -= s;
-            }
-        } else {
-            for (int i = w; i < nn; i += nw) {
+        if (i < nn) {
+            T s0 = 0, s1 = 0;
+            if (op.kind == 1) {
+                int j = sp;
+                for (; j + 4 < ns; j += 8) {
+                    s0 += A[i + (size_t)j * ld] * xs[j];
+                    s1 += A[i + (size_t)(j + 4) * ld] * xs[j + 4];
+                }
+                for (; j < ns; j += 4) s0 += A[i + (size_t)j * ld] * xs[j];
+            } else {
                 const T* a = A + (size_t)i * ld;
-                T s = 0;
-                for (int j = lane; j < ns; j += 32) s += a[j] * xs[j];
-                s = warp_sum(s);
-                if (lane == 0) xn[i] -= s;
+                for (int j = sp; j < ns; j += 4) s0 += a[j] * xs[j];
             }
+            acc += s0 + s1;
         }
-        __syncthreads();
     }
+    part[sp][li] = acc;
+    __syncthreads();
+    if (sp == 0 && i < nn) xn[i] -= (part[0][li] + part[1][li]) + (part[2][li] + part[3][li]);
 }
 
-// Backward Gemm ops grouped by eliminated cluster: x_s -= A_ns^T x_n or A_sn x_n
+// Backward Gemm ops grouped by eliminated cluster s: x_s -= sum of A_ns^T x_n
+// (GemmSymmOut) or A_sn x_n (GemmSymmIn), ops in reverse recording order.  One block per
+// (s, 32 entries of x_s), a warp per entry.
+constexpr int GB_ROWS = 32;
+
 template <typename T>
-__global__ void gemm_bwd_kernel(Ctx<T> c, XCtx<T> X, const DGroup* __restrict__ groups, const DGemmOp* __restrict__ ops,
-                                int ngroups) {
-    const int g = blockIdx.x % ngroups;
-    const int r = blockIdx.x / ngroups;
-    const DGroup G = groups[g];
+__global__ void __launch_bounds__(256) gemm_bwd2_kernel(Ctx<T> c, XCtx<T> X, const DGroup* __restrict__ groups,
+                                                        const DGemmOp* __restrict__ ops, const DTile* __restrict__ tiles,
+                                                        int ntiles) {
+    const int t = blockIdx.x % ntiles;
+    const int r = blockIdx.x / ntiles;
+    const DGroup G = groups[tiles[t].item];
     const int sc = G.key;
     const int ns = c.csize[sc];
+    const int i0 = tiles[t].tile_i * GB_ROWS;
+    if (i0 >= ns) return;
     T* xs = X.xs + X.xoff[sc] + r * X.xld;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int o = 0; o < G.count; o++) {
-        const DGemmOp op = ops[G.first + o];
-        const int nn = c.rows0[op.nbr];
-        const T* xn = X.xs + X.xoff[op.nbr] + r * X.xld;
-        const T* A = bptr(c, op.block);
-        const int ld = c.blk[op.block].ld;
-        if (op.kind == 1) {
-            for (int i = w; i < ns; i += nw) {
+    for (int ii = w; ii < GB_ROWS; ii += nw) {
+        const int i = i0 + ii;
+        if (i >= ns) break;
+        T acc = 0;
+        for (int o = 0; o < G.count; o++) {
+            const DGemmOp op = ops[G.first + o];
+            const int nn = c.rows0[op.nbr];
+            const T* xn = X.xs + X.xoff[op.nbr] + r * X.xld;
+            const T* A = bptr(c, op.block);
+            const int ld = c.blk[op.block].ld;
+            T s = 0;
+            if (op.kind == 1) {
                 const T* a = A + (size_t)i * ld;
-                T s = 0;
                 for (int j = lane; j < nn; j += 32) s += a[j] * xn[j];
-                s = warp_sum(s);
-                if (lane == 0) xs[i] -= s;
+            } else {
+                for (int j = lane; j < nn; j += 32) s += A[i + (size_t)j * ld] * xn[j];
             }
-        } else {
-            for (int i = threadIdx.x; i < ns; i += blockDim.x) {
-                T s = 0;
-                for (int j = 0; j < nn; j++) s += A[i + (size_t)j * ld] * xn[j];
-                xs[i] -= s;
-            }
+            acc += warp_sum(s);
         }
-        __syncthreads();
+        if (lane == 0) xs[i] -= acc;
     }
 }
 
-// Orthogonal op: x <- Q^T x (fwd) or Q x (bwd), k = rank reflectors (operations.cpp:153-158)
+// Orthogonal op of the solve with the blocked WY form: fwd x <- Q^T x applies
+// Q_b^T = I - V_b T_b^T V_b^T for b = 0, 1, ...; bwd x <- Q x applies Q_b for b = nb-1 ... 0
+// (operations.cpp:153-158).  Three barriers per block of 32 reflectors.
 template <typename T>
-__global__ void ortho_kernel(Ctx<T> c, XCtx<T> X, const DOrtho* __restrict__ items, int count, const T* vstore,
-                             const T* taustore, int trans) {
+__global__ void __launch_bounds__(512) ortho_wyb_kernel(Ctx<T> c, XCtx<T> X, const DOrtho* __restrict__ items,
+                                                        int count, const T* vstore, const T* tstore, int trans) {
     const int item = blockIdx.x % count;
     const int r = blockIdx.x / count;
     const DOrtho it = items[item];
     const int rows = c.rows0[it.cluster];
     const int k = c.csize[it.cluster];
-    if (k >= rows) return;
+    if (k >= rows || k == 0) return;
     const int ld = c.cap[it.cluster];
     const T* V = vstore + it.v_off;
-    const T* tau = taustore + it.tau_off;
+    const T* Tm = tstore + it.v_off;
     T* x = X.xs + X.xoff[it.cluster] + r * X.xld;
-    extern __shared__ unsigned char smem_raw[];
-    T* xsh = reinterpret_cast<T*>(smem_raw);
-    __shared__ T red[33];
-    for (int i = threadIdx.x; i < rows; i += blockDim.x) xsh[i] = x[i];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* xs = reinterpret_cast<T*>(smem_raw);  // rows
+    __shared__ T wv[QB], yv[QB];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int i = threadIdx.x; i < rows; i += blockDim.x) xs[i] = x[i];
     __syncthreads();
-    for (int q = 0; q < k; q++) {
-        const int i = trans ? q : k - 1 - q;
-        const T* v = V + (size_t)i * ld;
-        T part = 0;
-        for (int rr = i + 1 + threadIdx.x; rr < rows; rr += blockDim.x) part += v[rr] * xsh[rr];
-        T s = block_sum(part, red);
-        s = (s + xsh[i]) * tau[i];
+    const int nb = (k + QB - 1) / QB;
+    for (int q = 0; q < nb; q++) {
+        const int b = trans ? q : nb - 1 - q;
+        const int i0 = b * QB, bw = min(QB, k - i0);
+        // w = V_b^T x
+        for (int i = w; i < bw; i += nw) {
+            const T* vi = V + (size_t)(i0 + i) * ld;
+            T s = 0;
+            for (int rr = i0 + i + 1 + lane; rr < rows; rr += 32) s += vi[rr] * xs[rr];
+            s = warp_sum(s);
+            if (lane == 0) wv[i] = xs[i0 + i] + s;
+        }
         __syncthreads();
-        if (threadIdx.x == 0) xsh[i] -= s;
-        for (int rr = i + 1 + threadIdx.x; rr < rows; rr += blockDim.x) xsh[rr] -= s * v[rr];
+        // y = T_b^T w (fwd) or T_b w (bwd)
+        if (threadIdx.x < bw) {
+            const int i = threadIdx.x;
+            T s = 0;
+            if (trans) {
+                for (int j = 0; j <= i; j++) s += Tm[(i0 + j) + (size_t)(i0 + i) * ld] * wv[j];
+            } else {
+                for (int j = i; j < bw; j++) s += Tm[(i0 + i) + (size_t)(i0 + j) * ld] * wv[j];
+            }
+            yv[i] = s;
+        }
+        __syncthreads();
+        // x -= V_b y
+        for (int rr = i0 + threadIdx.x; rr < rows; rr += blockDim.x) {
+            const int imax = min(rr - i0, bw - 1);
+            T s = 0;
+            for (int i = 0; i <= imax; i++) s += (i0 + i == rr ? T(1) : V[rr + (size_t)(i0 + i) * ld]) * yv[i];
+            xs[rr] -= s;
+        }
         __syncthreads();
     }
-    for (int i = threadIdx.x; i < rows; i += blockDim.x) x[i] = xsh[i];
+    for (int i = threadIdx.x; i < rows; i += blockDim.x) x[i] = xs[i];
 }
 
 // Merge op: parent x = children heads concatenated (fwd) and back (bwd)
@@ -1795,6 +1934,7 @@ class DeviceFactor : public DeviceFactorBase {
         cpos_ = alloc<int>(nc_);
         status_ = alloc<DStatus>(1);
         vstore_ = alloc<T>(std::max<int64_t>(P.v_len, 1));
+        tstore_ = alloc<T>(std::max<int64_t>(P.v_len, 1));
         taustore_ = alloc<T>(std::max<int64_t>(P.tau_len, 1));
         tauws_ = alloc<T>(std::max<int64_t>(P.tau_len, 1));
         ws_ = alloc<T>(std::max<int64_t>(P.ws_len, 1));
@@ -1816,6 +1956,7 @@ class DeviceFactor : public DeviceFactorBase {
             D.elim_clusters = up(L.elim_clusters);
             D.elim_pivots = up(L.elim_pivots);
             D.elim_smem = smem_for(L.elim_clusters, P);
+            D.elim_tri = build_trtri(L.elim_clusters, P);
             build_trsm(L.elim_trsm, L.elim_pivots, L.elim_clusters, P, D.elim_trsm0, D.elim_trsm1);
             {
                 std::vector<DTarget> tg;
@@ -1838,6 +1979,7 @@ class DeviceFactor : public DeviceFactorBase {
             D.scale_clusters = up(L.scale_clusters);
             D.scale_pivots = up(L.scale_pivots);
             D.scale_smem = smem_for(L.scale_clusters, P);
+            D.scale_tri = build_trtri(L.scale_clusters, P);
             build_trsm(L.scale_trsm, L.scale_pivots, L.scale_clusters, P, D.scale_trsm0, D.scale_trsm1);
             {
                 std::vector<int> all;
@@ -1939,6 +2081,14 @@ class DeviceFactor : public DeviceFactorBase {
                 D.gb = up(bg);
                 D.gfo = up(fo);
                 D.gbo = up(bo);
+                std::vector<int> ef, eb;
+                for (const DGroup& g : fg) ef.push_back(P.c_cap[g.key]);
+                for (const DGroup& g : bg) eb.push_back(P.c_cap[g.key]);
+                auto tf = tiles_1d(ef, GF_ROWS), tb = tiles_1d(eb, GB_ROWS);
+                D.gf_tiles = up(tf);
+                D.n_gf_tiles = (int)tf.size();
+                D.gb_tiles = up(tb);
+                D.n_gb_tiles = (int)tb.size();
             }
             {
                 std::vector<DOrtho> ot;
@@ -1968,13 +2118,14 @@ class DeviceFactor : public DeviceFactorBase {
             d_perm_ = up(perm_h_);
         }
         ctx_ = Ctx<T>{arena_, d_blk_, csize_, rows0_, d_cap_, status_};
-        SPAND_CUDA(cudaFuncSetAttribute(potrf2_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        SPAND_CUDA(cudaFuncSetAttribute(trsm2_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SPAND_CUDA(cudaFuncSetAttribute(potrf3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SPAND_CUDA(cudaFuncSetAttribute(trtri_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SPAND_CUDA(cudaFuncSetAttribute(trsm3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(qrcp_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(qrcp3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, QC_SMEM_MAX));
         fallback_ = alloc<int>(max_items);
-        SPAND_CUDA(cudaFuncSetAttribute(trsv2_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        SPAND_CUDA(cudaFuncSetAttribute(ortho_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SPAND_CUDA(cudaFuncSetAttribute(trsv3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SPAND_CUDA(cudaFuncSetAttribute(ortho_wyb_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         caps_h_ = P.c_cap;
     }
 
@@ -2011,7 +2162,7 @@ class DeviceFactor : public DeviceFactorBase {
             LevelDev& D = levels_[l];
             cur_level_ = l;
             if (D.n_elim) {
-                launch_potrf(D.elim_pivots, D.elim_clusters, D.n_elim, D.elim_smem);
+                launch_potrf(D.elim_pivots, D.elim_clusters, D.n_elim, D.elim_smem, D.elim_tri);
                 launch_trsm(D.elim_trsm0);
                 launch_trsm(D.elim_trsm1);
                 if (D.n_schur_tiles)
@@ -2021,7 +2172,7 @@ class DeviceFactor : public DeviceFactorBase {
                     });
             }
             if (D.scaled && D.n_scale) {
-                launch_potrf(D.scale_pivots, D.scale_clusters, D.n_scale, D.scale_smem);
+                launch_potrf(D.scale_pivots, D.scale_clusters, D.n_scale, D.scale_smem, D.scale_tri);
                 launch_trsm(D.scale_trsm0);
                 launch_trsm(D.scale_trsm1);
             }
@@ -2041,7 +2192,7 @@ class DeviceFactor : public DeviceFactorBase {
                 }, 2);
                 launch("sparsify_scatter", [&] {
                     sparsify_scatter_kernel<T><<<W.n, 256, 0, s_>>>(ctx_, W.items, pieces_, ws_, jpvt_, ipvt_, rank_,
-                                                                     vstore_, tauws_, taustore_, colcount_);
+                                                                     vstore_, tauws_, taustore_, colcount_, tstore_);
                 });
             }
             if (D.merged) {
@@ -2115,6 +2266,8 @@ class DeviceFactor : public DeviceFactorBase {
             int ne = nmax(L.elim_clusters), ns = nmax(L.scale_clusters);
             D.elim_smem = potrf_smem_n(ne);
             D.scale_smem = potrf_smem_n(ns);
+            D.elim_tri.smem = trtri_smem_n(ne);
+            D.scale_tri.smem = trtri_smem_n(ns);
             D.elim_trsm0.smem = D.elim_trsm1.smem = trsm_smem_n(ne);
             D.scale_trsm0.smem = D.scale_trsm1.smem = trsm_smem_n(ns);
         }
@@ -2235,6 +2388,11 @@ class DeviceFactor : public DeviceFactorBase {
         int side = 0;
         int smem = 0;
     };
+    struct TrtriDev {
+        DTile* tiles = nullptr;
+        int ntiles = 0;
+        int smem = 0;
+    };
     struct WaveDev {
         int n = 0;
         DSpars* items = nullptr;
@@ -2249,6 +2407,7 @@ class DeviceFactor : public DeviceFactorBase {
         int* elim_pivots = nullptr;
         int elim_smem = 0;
         TrsmDev elim_trsm0, elim_trsm1;
+        TrtriDev elim_tri, scale_tri;
         DTarget* schur_targets = nullptr;
         DTile* schur_tiles = nullptr;
         int n_schur_tiles = 0;
@@ -2272,6 +2431,8 @@ class DeviceFactor : public DeviceFactorBase {
         int x_smem_elim = 0, x_smem_scale = 0, x_smem_ortho = 0;
         int n_gf = 0, n_gb = 0;
         DGroup *gf = nullptr, *gb = nullptr;
+        DTile *gf_tiles = nullptr, *gb_tiles = nullptr;
+        int n_gf_tiles = 0, n_gb_tiles = 0;
         DGemmOp *gfo = nullptr, *gbo = nullptr;
         int n_ortho = 0;
         DOrtho* ortho = nullptr;
@@ -2385,21 +2546,41 @@ class DeviceFactor : public DeviceFactorBase {
                                       (const DAsn*)pieces_, ws_, jpvt_, tauws_, rank_, colcount_, fallback_, tol,
                                       W.smem, probe));
     }
-    void launch_potrf(int* pivots, int* clusters, int n, int smem) {
-        launch("potrf", [&] { potrf2_kernel<T><<<n, 256, smem, s_>>>(ctx_, pivots, clusters, n, smem / (int)sizeof(T)); });
+    void launch_potrf(int* pivots, int* clusters, int n, int smem, const TrtriDev& tri) {
+        launch("potrf", [&] {
+            potrf3_kernel<T><<<n, 256, smem, s_>>>(ctx_, pivots, clusters, n, smem / (int)sizeof(T),
+                                                   tri.smem / (32 * (int)sizeof(T)));
+        });
+        if (tri.ntiles)
+            launch("trtri", [&] {
+                trtri_kernel<T><<<tri.ntiles, 256, tri.smem, s_>>>(ctx_, pivots, clusters, tri.tiles, tri.ntiles,
+                                                                   tri.smem / (int)sizeof(T));
+            });
     }
     void launch_trsm(const TrsmDev& t) {
         if (!t.ntiles) return;
         launch("trsm", [&] {
-            trsm2_kernel<T><<<t.ntiles, 256, t.smem, s_>>>(ctx_, t.items, t.tiles, t.ntiles, t.smem / (int)sizeof(T));
+            trsm3_kernel<T><<<t.ntiles, 256, t.smem, s_>>>(ctx_, t.items, t.tiles, t.ntiles, t.smem / (int)sizeof(T));
         });
     }
     // shared memory of the POTRF kernel for pivots of size up to nmax: whole block, else one panel
     static int potrf_smem_n(int nmax) {
-        int64_t full = (int64_t)nmax * nmax * sizeof(T), panel = (int64_t)nmax * PNB * sizeof(T);
-        if (full <= 200 * 1024) return (int)std::max<int64_t>(full, 16);
-        if (panel <= 200 * 1024) return (int)panel;
-        return 0;
+        int64_t full = (int64_t)nmax * nmax * sizeof(T);
+        return full <= 200 * 1024 ? (int)std::max<int64_t>(full, 16) : 0;
+    }
+    static int trtri_smem_n(int nmax) {
+        int64_t b = (int64_t)32 * nmax * sizeof(T);
+        return (int)std::min<int64_t>(std::max<int64_t>(b, 16), 200 * 1024);
+    }
+    TrtriDev build_trtri(const std::vector<int>& clusters, const Plan& P) {
+        std::vector<int> ext;
+        int mx = 0;
+        for (int c0 : clusters) {
+            ext.push_back(P.c_cap[c0]);
+            mx = std::max(mx, P.c_cap[c0]);
+        }
+        auto t = tiles_1d(ext, 32);
+        return {up(t), (int)t.size(), trtri_smem_n(mx)};
     }
     static int trsm_smem_n(int nmax) {
         int64_t b = (int64_t)TRB * nmax * sizeof(T);
@@ -2423,22 +2604,26 @@ class DeviceFactor : public DeviceFactorBase {
         });
         for (int l = 0; l < P.nlevels; l++) {
             LevelDev& D = levels_[l];
+            cur_level_ = l;
             if (D.n_elim_llt)
                 launch("trsv", [&] {
-                    trsv2_kernel<T><<<D.n_elim_llt * nrhs, 256, D.x_smem_elim, s_>>>(ctx_, X, D.elim_llt,
+                    trsv3_kernel<T><<<D.n_elim_llt * nrhs, 512, D.x_smem_elim, s_>>>(ctx_, X, D.elim_llt,
                                                                                     D.elim_llt_blk, D.n_elim_llt, 0);
                 });
             if (D.n_gf)
-                launch("gemm_fwd", [&] { gemm_fwd_kernel<T><<<D.n_gf * nrhs, 128, 0, s_>>>(ctx_, X, D.gf, D.gfo, D.n_gf); });
+                launch("gemm_fwd", [&] {
+                    gemm_fwd2_kernel<T><<<D.n_gf_tiles * nrhs, 256, 0, s_>>>(ctx_, X, D.gf, D.gfo, D.gf_tiles,
+                                                                             D.n_gf_tiles, 0);
+                });
             if (D.n_scale_llt)
                 launch("trsv", [&] {
-                    trsv2_kernel<T><<<D.n_scale_llt * nrhs, 256, D.x_smem_scale, s_>>>(ctx_, X, D.scale_llt,
+                    trsv3_kernel<T><<<D.n_scale_llt * nrhs, 512, D.x_smem_scale, s_>>>(ctx_, X, D.scale_llt,
                                                                                       D.scale_llt_blk, D.n_scale_llt, 0);
                 });
             if (D.n_ortho)
                 launch("ortho", [&] {
-                    ortho_kernel<T><<<D.n_ortho * nrhs, 128, D.x_smem_ortho, s_>>>(ctx_, X, D.ortho, D.n_ortho, vstore_,
-                                                                                   taustore_, 1);
+                    ortho_wyb_kernel<T><<<D.n_ortho * nrhs, 512, D.x_smem_ortho, s_>>>(ctx_, X, D.ortho, D.n_ortho,
+                                                                                          vstore_, tstore_, 1);
                 });
             if (D.merged && D.n_children)
                 launch("merge_x", [&] {
@@ -2448,6 +2633,7 @@ class DeviceFactor : public DeviceFactorBase {
         }
         for (int l = P.nlevels - 1; l >= 0; l--) {
             LevelDev& D = levels_[l];
+            cur_level_ = l;
             if (D.merged && D.n_children)
                 launch("merge_x", [&] {
                     merge_x_kernel<T><<<D.n_children * nrhs, 128, 0, s_>>>(ctx_, X, D.child_idx, D.child_parent,
@@ -2455,22 +2641,26 @@ class DeviceFactor : public DeviceFactorBase {
                 });
             if (D.n_ortho)
                 launch("ortho", [&] {
-                    ortho_kernel<T><<<D.n_ortho * nrhs, 128, D.x_smem_ortho, s_>>>(ctx_, X, D.ortho, D.n_ortho, vstore_,
-                                                                                   taustore_, 0);
+                    ortho_wyb_kernel<T><<<D.n_ortho * nrhs, 512, D.x_smem_ortho, s_>>>(ctx_, X, D.ortho, D.n_ortho,
+                                                                                          vstore_, tstore_, 0);
                 });
             if (D.n_scale_llt)
                 launch("trsv", [&] {
-                    trsv2_kernel<T><<<D.n_scale_llt * nrhs, 256, D.x_smem_scale, s_>>>(ctx_, X, D.scale_llt,
+                    trsv3_kernel<T><<<D.n_scale_llt * nrhs, 512, D.x_smem_scale, s_>>>(ctx_, X, D.scale_llt,
                                                                                       D.scale_llt_blk, D.n_scale_llt, 1);
                 });
             if (D.n_gb)
-                launch("gemm_bwd", [&] { gemm_bwd_kernel<T><<<D.n_gb * nrhs, 128, 0, s_>>>(ctx_, X, D.gb, D.gbo, D.n_gb); });
+                launch("gemm_bwd", [&] {
+                    gemm_bwd2_kernel<T><<<D.n_gb_tiles * nrhs, 256, 0, s_>>>(ctx_, X, D.gb, D.gbo, D.gb_tiles,
+                                                                             D.n_gb_tiles);
+                });
             if (D.n_elim_llt)
                 launch("trsv", [&] {
-                    trsv2_kernel<T><<<D.n_elim_llt * nrhs, 256, D.x_smem_elim, s_>>>(ctx_, X, D.elim_llt,
+                    trsv3_kernel<T><<<D.n_elim_llt * nrhs, 512, D.x_smem_elim, s_>>>(ctx_, X, D.elim_llt,
                                                                                     D.elim_llt_blk, D.n_elim_llt, 1);
                 });
         }
+        cur_level_ = -1;
         launch("perm", [&] {
             perm_out_kernel<T><<<(unsigned)((tot + 255) / 256), 256, 0, s_>>>(x, ld, X, d_perm_, d_slot_, n);
         });
@@ -2490,6 +2680,7 @@ class DeviceFactor : public DeviceFactorBase {
     int* d_cap_ = nullptr;
     int *csize_ = nullptr, *rows0_ = nullptr, *rank_ = nullptr, *cpos_ = nullptr;
     DStatus* status_ = nullptr;
+    T* tstore_ = nullptr;
     T *vstore_ = nullptr, *taustore_ = nullptr, *tauws_ = nullptr, *ws_ = nullptr, *norms_ = nullptr;
     int *jpvt_ = nullptr, *ipvt_ = nullptr, *colcount_ = nullptr, *fallback_ = nullptr;
     bool tuned_ = false;
