@@ -255,7 +255,7 @@ int spand_tree_bench_step(spand_tree* t, const double* b, double* x, int iters, 
 int spand_tree_assembled_bytes(spand_tree* t, long long* b) {
     CHECK_T(t);
     if (!t->t->device()) return fail(SPAND_ERR_STATE, "before assemble");
-    *b = (long long)t->t->plan().assembled_len * t->t->device()->precision_bytes();
+    *b = (long long)t->t->matrix().val.size() * (long long)sizeof(double);
     return SPAND_OK;
 }
 int spand_tree_set_profiling(spand_tree* t, int on) {

@@ -76,9 +76,13 @@ class KernelProfiler {
 class DeviceFactorBase {
    public:
     virtual ~DeviceFactorBase() {}
-    virtual void upload(const Plan& P, const std::vector<double>& assembled) = 0;
-    // replace the assembled block values (same plan)
-    virtual void upload_values(const std::vector<double>& assembled) = 0;
+    // work lists and block storage of a plan; amap: assembly_map of the matrix pattern
+    virtual void upload(const Plan& P, const std::vector<int64_t>& amap) = 0;
+    // assemble the level-0 blocks from the values of A (host, CSC order of the pattern):
+    // one copy to the device and a scatter through the assembly map
+    virtual void assemble_values(const double* vals, int64_t nnz) = 0;
+    // device copy of the last uploaded values of A (CSC order)
+    virtual const double* device_values() const = 0;
     virtual void factorize(double tol) = 0;  // throws DeviceError
     // x: device pointer, natural ordering, n x nrhs (ld), FP64; in-place M^{-1} x
     virtual void solve_device(double* x, int nrhs, int ld) = 0;
@@ -123,5 +127,8 @@ PcgResult device_pcg(DeviceFactorBase& M, const DeviceCsr& A, const double* b, d
                      bool use_graph);
 
 void device_spmv(const DeviceCsr& A, const double* x, double* y, cudaStream_t s);
+
+// dst[map[k]] = src[k] for map[k] >= 0 (device arrays), on stream s
+void device_scatter(const double* src, const int* map, int64_t n, double* dst, cudaStream_t s);
 
 }  // namespace spand

@@ -567,26 +567,40 @@ Plan build_plan(const Hierarchy& H, const Assembly& asmb, int skip, bool use_wan
     return P;
 }
 
-void fill_assembled_blocks(const Plan& P, const Hierarchy& H, const Assembly& asmb, const Csc& App,
-                           std::vector<double>& dst) {
-    dst.assign((size_t)P.assembled_len, 0.0);
-    size_t bi = 0;
-    for (size_t li = 0; li < H.bottoms[0].size(); li++) {
-        int self = H.bottoms[0][li];
-        for (int nbr : asmb.nbrs[li]) {
-            const PlanBlock& B = P.blocks[P.initial_blocks[bi++]];
-            double* D = dst.data() + B.off;
-            const int r0 = H.start[nbr], r1 = r0 + H.size[nbr];
-            // block2dense (util.cpp:454-486)
-            for (int col = 0; col < H.size[self]; col++) {
-                int j = H.start[self] + col;
-                const int* rb = App.rowval.data() + App.colptr[j];
-                const int* re = App.rowval.data() + App.colptr[j + 1];
-                for (const int* p = std::lower_bound(rb, re, r0); p != re && *p < r1; ++p)
-                    D[(size_t)(*p - r0) + (size_t)col * B.ld] = App.val[p - App.rowval.data()];
+std::vector<int64_t> assembly_map(const Plan& P, const Hierarchy& H, const Assembly& asmb, const Csc& A,
+                                  const std::vector<int>& perm) {
+    const int N = A.n;
+    std::vector<int> pinv(N), owner(N);
+    for (int i = 0; i < N; i++) pinv[perm[i]] = i;
+    for (int c : H.bottoms[0])
+        for (int k = H.start[c]; k < H.start[c] + H.size[c]; k++) owner[k] = c;
+    // per leaf: (neighbour, block) in the order assembly created them (self first, then by order)
+    std::vector<int> leaf_index(H.start.size(), -1);
+    for (size_t li = 0; li < H.bottoms[0].size(); li++) leaf_index[H.bottoms[0][li]] = (int)li;
+    std::vector<size_t> first(H.bottoms[0].size() + 1, 0);
+    for (size_t li = 0; li < H.bottoms[0].size(); li++) first[li + 1] = first[li] + asmb.nbrs[li].size();
+    std::vector<int64_t> map(A.rowval.size(), -1);
+    for (int col = 0; col < N; col++) {
+        const int j = pinv[col];
+        const int self = owner[j];
+        const int li = leaf_index[self];
+        const std::vector<int>& nb = asmb.nbrs[li];
+        for (int k = A.colptr[col]; k < A.colptr[col + 1]; k++) {
+            const int i = pinv[A.rowval[k]];
+            const int nbr = owner[i];
+            int t = -1;
+            if (nbr == self) {
+                t = 0;
+            } else {
+                auto it = std::lower_bound(nb.begin() + 1, nb.end(), nbr);
+                if (it != nb.end() && *it == nbr) t = (int)(it - nb.begin());
             }
+            if (t < 0) continue;
+            const PlanBlock& B = P.blocks[P.initial_blocks[first[li] + t]];
+            map[k] = B.off + (int64_t)(i - H.start[nbr]) + (int64_t)(j - H.start[self]) * B.ld;
         }
     }
+    return map;
 }
 
 }  // namespace spand

@@ -188,9 +188,12 @@ Assembly assembly_structure(const Hierarchy& H, const Csc& App, bool symmetric);
 
 Plan build_plan(const Hierarchy& H, const Assembly& asmb, int skip, bool use_want_sparsify);
 
-// Fill the assembled level-0 blocks of the arena (host copy) from A[p,p].
-void fill_assembled_blocks(const Plan& P, const Hierarchy& H, const Assembly& asmb, const Csc& App,
-                           std::vector<double>& dst);
+// For every entry k of A (natural ordering, CSC order): the element offset of A(r, c) in
+// the assembled level-0 blocks, or -1 when the entry is not stored (upper triangle of the
+// symmetric path).  Reproduces block2dense (util.cpp:454-486) on A[p,p] as a gather map,
+// so that re-assembly with new values is one scatter on the device.
+std::vector<int64_t> assembly_map(const Plan& P, const Hierarchy& H, const Assembly& asmb, const Csc& A,
+                                  const std::vector<int>& perm);
 
 Csc symm_perm(const Csc& A, const std::vector<int>& perm);
 

@@ -1484,6 +1484,23 @@ __global__ void merge_copy_kernel(Ctx<T> c, const DMerge* __restrict__ items, co
     }
 }
 
+// Assembly of the level-0 blocks on the device: blocks[map[k]] = vals[k] (block2dense,
+// util.cpp:454-486, as a scatter; the blocks are zeroed first).
+template <typename T>
+__global__ void assemble_scatter_kernel(const double* __restrict__ vals, const long long* __restrict__ map,
+                                        long long n, T* blocks) {
+    long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const long long d = map[k];
+    if (d >= 0) blocks[d] = (T)vals[k];
+}
+
+__global__ void scatter_f64_kernel(const double* __restrict__ src, const int* __restrict__ map, long long n,
+                                   double* dst) {
+    long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (k < n && map[k] >= 0) dst[map[k]] = src[k];
+}
+
 __global__ void snapshot_kernel(const int* csize, int* rows0, const int* __restrict__ clusters, int n) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n) rows0[clusters[k]] = csize[clusters[k]];
@@ -1917,12 +1934,14 @@ class DeviceFactor : public DeviceFactorBase {
     cudaStream_t stream() const override { return s_; }
     size_t device_bytes() const override { return bytes_; }
 
-    void upload(const Plan& P, const std::vector<double>& assembled) override {
+    void upload(const Plan& P, const std::vector<int64_t>& amap) override {
         P_ = &P;
         nc_ = P.nclusters;
         arena_ = alloc<T>(P.arena_len);
         pristine_ = alloc<T>(P.assembled_len);
-        upload_values(assembled);
+        amap_n_ = (int64_t)amap.size();
+        d_amap_ = up(std::vector<long long>(amap.begin(), amap.end()));
+        d_vals_ = alloc<double>(std::max<int64_t>(amap_n_, 1));
         std::vector<DBlock> blk(P.blocks.size());
         for (size_t b = 0; b < P.blocks.size(); b++)
             blk[b] = {(long long)P.blocks[b].off, P.blocks[b].ld, P.blocks[b].rowc, P.blocks[b].colc, P.blocks[b].flag};
@@ -2129,16 +2148,17 @@ class DeviceFactor : public DeviceFactorBase {
         caps_h_ = P.c_cap;
     }
 
-    void upload_values(const std::vector<double>& assembled) override {
-        if ((int64_t)assembled.size() != P_->assembled_len)
-            throw DeviceError{SPAND_ERR_ARG, "assembled values do not match the plan"};
-        if (!assembled.empty()) {
-            std::vector<T> tmp(assembled.begin(), assembled.end());
-            SPAND_CUDA(cudaMemcpyAsync(pristine_, tmp.data(), tmp.size() * sizeof(T), cudaMemcpyHostToDevice, s_));
-            SPAND_CUDA(cudaStreamSynchronize(s_));
+    void assemble_values(const double* vals, int64_t nnz) override {
+        if (nnz != amap_n_) throw DeviceError{SPAND_ERR_ARG, "values do not match the assembled pattern"};
+        if (nnz > 0) SPAND_CUDA(cudaMemcpyAsync(d_vals_, vals, nnz * sizeof(double), cudaMemcpyHostToDevice, s_));
+        if (P_->assembled_len) SPAND_CUDA(cudaMemsetAsync(pristine_, 0, P_->assembled_len * sizeof(T), s_));
+        if (nnz > 0) {
+            assemble_scatter_kernel<T><<<(unsigned)((nnz + 255) / 256), 256, 0, s_>>>(d_vals_, d_amap_, nnz, pristine_);
+            SPAND_CUDA(cudaGetLastError());
         }
         factored_ = false;
     }
+    const double* device_values() const override { return d_vals_; }
 
     void factorize(double tol) override {
         const Plan& P = *P_;
@@ -2676,6 +2696,9 @@ class DeviceFactor : public DeviceFactorBase {
     size_t bytes_ = 0;
     T* arena_ = nullptr;
     T* pristine_ = nullptr;
+    long long* d_amap_ = nullptr;
+    int64_t amap_n_ = 0;
+    double* d_vals_ = nullptr;
     DBlock* d_blk_ = nullptr;
     int* d_cap_ = nullptr;
     int *csize_ = nullptr, *rows0_ = nullptr, *rank_ = nullptr, *cpos_ = nullptr;
@@ -2716,6 +2739,10 @@ std::unique_ptr<DeviceFactorBase> make_device_factor(bool fp32, cudaStream_t str
 
 void device_spmv(const DeviceCsr& A, const double* x, double* y, cudaStream_t s) {
     spmv_kernel<<<(A.n + 255) / 256, 256, 0, s>>>(A.n, A.rowptr, A.colind, A.val, x, y);
+}
+
+void device_scatter(const double* src, const int* map, int64_t n, double* dst, cudaStream_t s) {
+    if (n > 0) scatter_f64_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, map, n, dst);
 }
 
 // Workspace of the device CG, kept across calls for one matrix size.

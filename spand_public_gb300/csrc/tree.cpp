@@ -22,8 +22,23 @@ Tree::Tree(int nlevels) : nlevels_(nlevels) {
     if (nlevels <= 0) throw std::invalid_argument("nlevels must be > 0");  // tree.cpp:87
 }
 
+double* Tree::cg_buffer(int which, int n) const {
+    if (cg_len_ < (size_t)n) {
+        for (auto& p : cg_buf_)
+            if (p) cudaFree(p);
+        cg_buf_[0] = cg_buf_[1] = nullptr;
+        cuda_check(cudaMalloc(&cg_buf_[0], n * sizeof(double)), "cudaMalloc");
+        cuda_check(cudaMalloc(&cg_buf_[1], n * sizeof(double)), "cudaMalloc");
+        cg_len_ = n;
+    }
+    return cg_buf_[which];
+}
+
 Tree::~Tree() {
     dev_.reset();
+    for (auto& p : cg_buf_)
+        if (p) cudaFree(p);
+    if (d_cmap_) cudaFree(d_cmap_);
     if (dx_) cudaFree(dx_);
     if (dA_.rowptr) cudaFree(dA_.rowptr);
     if (dA_.colind) cudaFree(dA_.colind);
@@ -59,81 +74,67 @@ std::vector<ClusterID> Tree::partition(const Csc& A) {
     return part_;
 }
 
-// Values of A in CSR order (A structurally symmetric: the CSR pattern is the transpose
-// of the CSC pattern).
-static std::vector<double> csr_val_of(const Csc& A) {
-    const int n = A.n;
-    std::vector<int> fill(n + 1, 0);
-    for (int j = 0; j < n; j++)
-        for (int k = A.colptr[j]; k < A.colptr[j + 1]; k++) fill[A.rowval[k] + 1]++;
-    for (int i = 0; i < n; i++) fill[i + 1] += fill[i];
-    std::vector<double> vv(A.rowval.size());
-    for (int j = 0; j < n; j++)
-        for (int k = A.colptr[j]; k < A.colptr[j + 1]; k++) vv[fill[A.rowval[k]]++] = A.val[k];
-    return vv;
-}
-
-// tree.cpp:505-575, plus the symbolic plan of factorize() and the device upload.
+// tree.cpp:505-575, plus the symbolic plan of factorize() and the device upload.  The
+// block values are assembled on the device: the first call builds the map from every
+// entry of A to its place in the level-0 blocks; later calls with the same sparsity
+// pattern only copy the new values and scatter them.
 void Tree::assemble(const Csc& A) {
     if (!partitioned_) throw std::logic_error("assemble() before partition()");
     if (symm_ != SymmKind::SPD || scaling_ != ScalingKind::LLT)
         throw std::invalid_argument("the device path implements the SPD / LLT configuration");
     if (A.n != get_N()) throw std::invalid_argument("matrix size does not match the partition");
+    if ((int64_t)A.val.size() != (int64_t)A.rowval.size()) throw std::invalid_argument("values do not match the pattern");
     double t0 = now_s();
     const bool same_pattern = assembled_ok_ && dev_ && A.colptr == A_.colptr && A.rowval == A_.rowval;
-    A_ = A;
-    Csc App = spand::symm_perm(A, perm_);
-    if (same_pattern) {
-        // same sparsity pattern: keep the symbolic plan and the device work lists,
-        // re-assemble the block values only
-        spand::fill_assembled_blocks(plan_, H_, asmb_, App, assembled_);
+    if (!same_pattern) {
+        A_ = A;
+        Csc App = spand::symm_perm(A, perm_);
+        asmb_ = spand::assembly_structure(H_, App, true);
+        plan_ = spand::build_plan(H_, asmb_, skip_, use_want_sparsify_);
+        std::vector<int64_t> amap = spand::assembly_map(plan_, H_, asmb_, A, perm_);
+        if (!stream_) cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+        dev_ = spand::make_device_factor(fp32_, stream_, perm_);
         try {
-            dev_->upload_values(assembled_);
+            dev_->upload(plan_, amap);
         } catch (spand::DeviceError& e) {
             throw std::runtime_error(e.msg);
         }
-        cuda_check(cudaMemcpyAsync(dA_.val, csr_val_of(A).data(), A.rowval.size() * sizeof(double),
-                                   cudaMemcpyHostToDevice, stream_), "H2D");
-        cuda_check(cudaStreamSynchronize(stream_), "sync");
-        factored_ = false;
-        t_assemble = now_s() - t0;
-        return;
-    }
-    asmb_ = spand::assembly_structure(H_, App, true);
-    plan_ = spand::build_plan(H_, asmb_, skip_, use_want_sparsify_);
-    spand::fill_assembled_blocks(plan_, H_, asmb_, App, assembled_);
-    if (!stream_) cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
-    dev_ = spand::make_device_factor(fp32_, stream_, perm_);
-    try {
-        dev_->upload(plan_, assembled_);
-    } catch (spand::DeviceError& e) {
-        throw std::runtime_error(e.msg);
-    }
-    // CSR of A for the device Krylov solvers (A is structurally symmetric; store A^T's CSC = A's CSR)
-    {
+        // CSR pattern of A for the device Krylov solvers (A structurally symmetric) and the
+        // position of every CSC entry in it
         const int n = A.n;
-        std::vector<int> rp(n + 1, 0), ci(A.rowval.size());
-        std::vector<double> vv(A.rowval.size());
+        const size_t nnz = A.rowval.size();
+        std::vector<int> rp(n + 1, 0), ci(nnz), cmap(nnz);
         for (int j = 0; j < n; j++)
             for (int k = A.colptr[j]; k < A.colptr[j + 1]; k++) rp[A.rowval[k] + 1]++;
         for (int i = 0; i < n; i++) rp[i + 1] += rp[i];
         std::vector<int> fill(rp.begin(), rp.end() - 1);
         for (int j = 0; j < n; j++)
             for (int k = A.colptr[j]; k < A.colptr[j + 1]; k++) {
-                int r = A.rowval[k];
+                const int r = A.rowval[k];
                 ci[fill[r]] = j;
-                vv[fill[r]] = A.val[k];
-                fill[r]++;
+                cmap[k] = fill[r]++;
             }
         if (dA_.rowptr) { cudaFree(dA_.rowptr); cudaFree(dA_.colind); cudaFree(dA_.val); }
+        if (d_cmap_) cudaFree(d_cmap_);
         dA_.n = n;
         cuda_check(cudaMalloc(&dA_.rowptr, rp.size() * sizeof(int)), "cudaMalloc");
-        cuda_check(cudaMalloc(&dA_.colind, std::max<size_t>(ci.size(), 1) * sizeof(int)), "cudaMalloc");
-        cuda_check(cudaMalloc(&dA_.val, std::max<size_t>(vv.size(), 1) * sizeof(double)), "cudaMalloc");
+        cuda_check(cudaMalloc(&dA_.colind, std::max<size_t>(nnz, 1) * sizeof(int)), "cudaMalloc");
+        cuda_check(cudaMalloc(&dA_.val, std::max<size_t>(nnz, 1) * sizeof(double)), "cudaMalloc");
+        cuda_check(cudaMalloc(&d_cmap_, std::max<size_t>(nnz, 1) * sizeof(int)), "cudaMalloc");
         cuda_check(cudaMemcpy(dA_.rowptr, rp.data(), rp.size() * sizeof(int), cudaMemcpyHostToDevice), "H2D");
-        cuda_check(cudaMemcpy(dA_.colind, ci.data(), ci.size() * sizeof(int), cudaMemcpyHostToDevice), "H2D");
-        cuda_check(cudaMemcpy(dA_.val, vv.data(), vv.size() * sizeof(double), cudaMemcpyHostToDevice), "H2D");
+        cuda_check(cudaMemcpy(dA_.colind, ci.data(), nnz * sizeof(int), cudaMemcpyHostToDevice), "H2D");
+        cuda_check(cudaMemcpy(d_cmap_, cmap.data(), nnz * sizeof(int), cudaMemcpyHostToDevice), "H2D");
+    } else {
+        A_.val = A.val;
     }
+    try {
+        dev_->assemble_values(A.val.data(), (int64_t)A.val.size());
+    } catch (spand::DeviceError& e) {
+        throw std::runtime_error(e.msg);
+    }
+    spand::device_scatter(dev_->device_values(), d_cmap_, (int64_t)A.val.size(), dA_.val, stream_);
+    cuda_check(cudaGetLastError(), "assembly scatter");
+    cuda_check(cudaStreamSynchronize(stream_), "sync");
     assembled_ok_ = true;
     factored_ = false;
     t_assemble = now_s() - t0;
@@ -478,9 +479,8 @@ int cg(const Csc& A, const double* rhs, double* x, const Tree& precond, int iter
        double* relres) {
     (void)A;  // the tree holds the device copy of the assembled matrix
     const int n = precond.get_N();
-    double *db, *dx;
-    cuda_check(cudaMalloc(&db, n * sizeof(double)), "cudaMalloc");
-    cuda_check(cudaMalloc(&dx, n * sizeof(double)), "cudaMalloc");
+    double* db = precond.cg_buffer(0, n);
+    double* dx = precond.cg_buffer(1, n);
     cudaStream_t s = precond.stream();
     cuda_check(cudaMemcpyAsync(db, rhs, n * sizeof(double), cudaMemcpyHostToDevice, s), "H2D");
     cuda_check(cudaMemcpyAsync(dx, x, n * sizeof(double), cudaMemcpyHostToDevice, s), "H2D");
@@ -488,14 +488,10 @@ int cg(const Csc& A, const double* rhs, double* x, const Tree& precond, int iter
     try {
         r = spand::device_pcg(*precond.device(), precond.device_csr(), db, dx, iters, tol, true);
     } catch (spand::DeviceError& e) {
-        cudaFree(db);
-        cudaFree(dx);
         throw std::runtime_error(e.msg);
     }
     cuda_check(cudaMemcpyAsync(x, dx, n * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
     cuda_check(cudaStreamSynchronize(s), "sync");
-    cudaFree(db);
-    cudaFree(dx);
     if (verb) printf("# of iter:  %d\n", r.iterations);
     if (relres) *relres = r.relres;
     return r.iterations;

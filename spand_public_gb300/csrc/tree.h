@@ -88,6 +88,8 @@ class Tree {
     cudaStream_t stream() const { return stream_; }
     spand::DeviceCsr device_csr() const { return dA_; }
     size_t device_bytes() const;
+    // device vectors of the CG driver (b, x), kept across calls
+    double* cg_buffer(int which, int n) const;
 
     // Algorithmic work per kernel class for one factorization and for one solve with one
     // right-hand side: (class, bytes, flops).  Bytes count each operand read or written
@@ -124,12 +126,15 @@ class Tree {
     spand::Assembly asmb_;
     spand::Plan plan_;
     Csc A_;
-    std::vector<double> assembled_;
+
     std::unique_ptr<spand::DeviceFactorBase> dev_;
     cudaStream_t stream_ = nullptr;
     spand::DeviceCsr dA_;
     mutable double* dx_ = nullptr;
     mutable size_t dx_len_ = 0;
+    mutable double* cg_buf_[2] = {nullptr, nullptr};
+    mutable size_t cg_len_ = 0;
+    int* d_cmap_ = nullptr;  // CSC entry -> CSR position
     bool partitioned_ = false, assembled_ok_ = false, factored_ = false;
     std::vector<LevelLog> log_;
     std::vector<OpRecord> ops_;

@@ -163,3 +163,37 @@ def test_not_spd_error():
     t2.partition(-A)
     t2.assemble(-A)
     t2.factorize()
+
+
+def test_reassemble_same_pattern():
+    """assemble() again with new values on the same pattern reuses the plan and the
+    device work lists (values scattered on the device) and factors the new matrix."""
+    import spand_public_gb300 as pkg
+    from oracle.oracle import OracleTree
+    from spand_public_gb300 import problems as P
+
+    n, dim, nl, tol = 16, 3, 6, 1e-2
+    A1 = P.neglapl(n, dim)
+    A2 = P.reaction_diffusion3d(n, 0.37)
+    assert np.array_equal(A1.indptr, A2.indptr) and np.array_equal(A1.indices, A2.indices)
+    X = P.linspace_nd(n, dim)
+    t = pkg.Tree(nl)
+    t.set_verb(False)
+    t.set_use_geo(True)
+    t.set_Xcoo(X)
+    t.set_tol(tol)
+    t.partition(A1)
+    t.assemble(A1)
+    t.factorize()
+    t.assemble(A2)
+    t.factorize()
+    o = OracleTree(nl)
+    o.set_Xcoo(X)
+    o.set_tol(tol)
+    o.partition(A2)
+    o.assemble(A2)
+    o.factorize()
+    assert np.array_equal(t.ranks(), o.ranks())
+    b = P.rhs(A2.shape[0], 1, seed=4)[:, 0]
+    xt, xo = t.solve(b), o.solve(b)
+    assert np.linalg.norm(xt - xo) / np.linalg.norm(xo) < TOL_SOLVE
