@@ -1,0 +1,118 @@
+// Definitions shared by the CUDA translation units: device work-list records, the
+// device context of the factorization, error checking and warp/block reductions.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "device.h"
+
+namespace spand {
+
+#define SPAND_CUDA(call)                                                                        \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess)                                                                  \
+            throw DeviceError{SPAND_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)}; \
+    } while (0)
+
+// ------------------------------------------------------------------------------------
+// Device work-list records
+// ------------------------------------------------------------------------------------
+struct DBlock {
+    long long off;
+    int ld, rowc, colc, flag;
+};
+struct DTrsm {
+    int block, lblock, cluster, side;
+};
+struct DTile {
+    int item, tile_i, tile_j;
+};
+struct DTarget {
+    int target, syrk, first, count;
+};
+struct DUpd {
+    int b1, t1, b2, t2, s;
+};
+struct DAsn {
+    int block, nbr, transposed;
+};
+struct DSpars {
+    int cluster, first, count, cap_cols;
+    long long ws_off, col_off, v_off, tau_off;
+};
+struct DMerge {
+    int src, dst, nold, sold;
+};
+struct DGemmOp {
+    int self, nbr, block, kind;
+};
+struct DGroup {
+    int key, first, count;
+};
+struct DOrtho {
+    int cluster;
+    long long v_off, tau_off;
+};
+
+// Status word: first failing cluster + 1 for a non-SPD pivot.
+struct DStatus {
+    int not_spd;
+};
+
+template <typename T>
+struct Ctx {
+    T* arena;
+    const DBlock* blk;
+    int* csize;
+    int* rows0;
+    const int* cap;
+    DStatus* status;
+};
+
+template <typename T>
+__device__ __forceinline__ T* bptr(const Ctx<T>& c, int b) {
+    return c.arena + c.blk[b].off;
+}
+
+template <typename T>
+__device__ __forceinline__ T dsqrt(T x) {
+    return sqrt(x);
+}
+
+// ------------------------------------------------------------------------------------
+// Block reductions (fixed order, deterministic)
+// ------------------------------------------------------------------------------------
+template <typename T>
+__device__ T block_sum(T v, T* red) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    T s = 0;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < nw; i++) s += red[i];
+        red[32] = s;
+    }
+    __syncthreads();
+    s = red[32];
+    return s;
+}
+
+template <typename T>
+__device__ T warp_sum(T v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Relative window inside which partial column norms count as tied (same rule as the
+// oracle's restated dgeqp3).
+template <typename T>
+__device__ __forceinline__ T qrcp_tie() {
+    return sizeof(T) == 8 ? T(1e-7) : T(1e-4);
+}
+
+}  // namespace spand

@@ -20,106 +20,10 @@
 #include <vector>
 
 #include "device.h"
+#include "kcommon.cuh"
+#include "qrcp.cuh"
 
 namespace spand {
-
-#define SPAND_CUDA(call)                                                                        \
-    do {                                                                                        \
-        cudaError_t e_ = (call);                                                                \
-        if (e_ != cudaSuccess)                                                                  \
-            throw DeviceError{SPAND_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)}; \
-    } while (0)
-
-// ------------------------------------------------------------------------------------
-// Device work-list records
-// ------------------------------------------------------------------------------------
-struct DBlock {
-    long long off;
-    int ld, rowc, colc, flag;
-};
-struct DTrsm {
-    int block, lblock, cluster, side;
-};
-struct DTile {
-    int item, tile_i, tile_j;
-};
-struct DTarget {
-    int target, syrk, first, count;
-};
-struct DUpd {
-    int b1, t1, b2, t2, s;
-};
-struct DAsn {
-    int block, nbr, transposed;
-};
-struct DSpars {
-    int cluster, first, count, cap_cols;
-    long long ws_off, col_off, v_off, tau_off;
-};
-struct DMerge {
-    int src, dst, nold, sold;
-};
-struct DGemmOp {
-    int self, nbr, block, kind;
-};
-struct DGroup {
-    int key, first, count;
-};
-struct DOrtho {
-    int cluster;
-    long long v_off, tau_off;
-};
-
-// Status word: first failing cluster + 1 for a non-SPD pivot.
-struct DStatus {
-    int not_spd;
-};
-
-template <typename T>
-struct Ctx {
-    T* arena;
-    const DBlock* blk;
-    int* csize;
-    int* rows0;
-    const int* cap;
-    DStatus* status;
-};
-
-template <typename T>
-__device__ __forceinline__ T* bptr(const Ctx<T>& c, int b) {
-    return c.arena + c.blk[b].off;
-}
-
-template <typename T>
-__device__ __forceinline__ T dsqrt(T x) {
-    return sqrt(x);
-}
-
-// ------------------------------------------------------------------------------------
-// Block reductions (fixed order, deterministic)
-// ------------------------------------------------------------------------------------
-template <typename T>
-__device__ T block_sum(T v, T* red) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    __syncthreads();
-    if (lane == 0) red[w] = v;
-    __syncthreads();
-    T s = 0;
-    if (threadIdx.x == 0) {
-        for (int i = 0; i < nw; i++) s += red[i];
-        red[32] = s;
-    }
-    __syncthreads();
-    s = red[32];
-    return s;
-}
-
-template <typename T>
-__device__ T warp_sum(T v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
 
 // Inverse of a lower Cholesky factor, written transposed into the strictly upper triangle
 // of the same block: after the call, for i > j, A[j + i*ld] = (L^{-1})[i][j]; the diagonal
@@ -519,20 +423,13 @@ __global__ void asn_gather_kernel(Ctx<T> c, const DSpars* __restrict__ items, co
     if (threadIdx.x == 0) colcount[blockIdx.x] = col;
 }
 
-// Relative window inside which partial column norms count as tied (same rule as the
-// oracle's restated dgeqp3).
-template <typename T>
-__device__ __forceinline__ T qrcp_tie() {
-    return sizeof(T) == 8 ? T(1e-7) : T(1e-4);
-}
-
 // Householder QR with column pivoting (LAPACK dgeqp3/dlaqp2 with LAWN 176 norm
 // downdating), stopped as soon as |R_ii| / |R_00| < tol (choose_rank, util.cpp:434-452).
 // One block per matrix; the matrix stays in global memory (L2), reflector in shared.
 template <typename T>
 __global__ void __launch_bounds__(512) qrcp_kernel(Ctx<T> c, const DSpars* __restrict__ items, T* ws, T* norms,
-                                                    int* jpvt_ws, const int* __restrict__ colcount, T* taus,
-                                                    int* rank_out, double tol, const int* __restrict__ only) {
+                                                    int* jpvt_ws, int* ipvt_ws, const int* __restrict__ colcount,
+                                                    T* taus, int* rank_out, double tol, const int* __restrict__ only) {
     extern __shared__ unsigned char smem_raw[];
     T* vsh = reinterpret_cast<T*>(smem_raw);  // cap(c) entries
     __shared__ T red[33];
@@ -705,744 +602,195 @@ __global__ void __launch_bounds__(512) qrcp_kernel(Ctx<T> c, const DSpars* __res
             __syncthreads();
         }
     }
+    // inverse pivot vector (column -> position)
+    __syncthreads();
+    int* ipvt = ipvt_ws + it.col_off;
+    for (int j = threadIdx.x; j < cols; j += blockDim.x) {
+        const int q = jpvt[j];
+        if (q >= 0 && q < cols) ipvt[q] = j;
+    }
     if (threadIdx.x == 0) rank_out[it.cluster] = rank;
-}
-
-// QRCP with the sparsification matrix resident in the shared memory of a thread-block
-// cluster (CS CTAs, CS = 1..16).  CTA r of the cluster owns the column slab
-// [r*cpc, min(cols, (r+1)*cpc)) of Asn, gathered straight from the edge blocks.  Per
-// pivot step: the cluster-wide largest partial norm and the first column inside the tie
-// window are reduced through distributed shared memory; the owner of column i swaps in
-// the pivot column (remote read/write of the other slab) and builds the reflector; every
-// CTA then reads the reflector from the owner's slab and updates its own columns and
-// norms.  Three cluster barriers per step.  Arithmetic and pivot rule are those of
-// qrcp_kernel; the result (R, reflectors, jpvt, tau, rank) is written to the same global
-// workspace for sparsify_scatter_kernel.  Matrices too large for the cluster's shared
-// memory set fallback[item] and are handled by asn_gather_kernel + qrcp_kernel.
-constexpr int QC_THREADS = 256;
-
-template <typename T>
-__global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, const DSpars* __restrict__ items,
-                                                                  const DAsn* __restrict__ pieces, T* ws,
-                                                                  int* jpvt_ws, T* taus, int* rank_out,
-                                                                  int* colcount, int* fallback, double tol,
-                                                                  int smem_bytes) {
-    namespace cgx = cooperative_groups;
-    cgx::cluster_group cl = cgx::this_cluster();
-    const int CS = (int)cl.num_blocks();
-    const int me = (int)cl.block_rank();
-    const int item = blockIdx.x / CS;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ T red[33];
-    __shared__ int ired[33];
-    __shared__ T pub_max;
-    __shared__ int pub_idx;
-    __shared__ T pub_beta, pub_tau, pub_r00;
-    __shared__ int pub_stop;
-    if (c.status->not_spd) return;
-    const DSpars it = items[item];
-    const int rows = c.csize[it.cluster];
-    int cols = 0;
-    for (int p = 0; p < it.count; p++) cols += c.csize[pieces[it.first + p].nbr];
-    const int mn = min(rows, cols);
-    const int cpc = (cols + CS - 1) / CS;
-    // shared layout: A slab (rows x cpc), v (rows), vn1, vn2 (cpc), jp (cpc)
-    const long long need = ((long long)rows * cpc + rows + 2LL * cpc) * sizeof(T) + (long long)cpc * sizeof(int);
-    const bool fits = need <= smem_bytes;
-    if (threadIdx.x == 0 && me == 0) {
-        fallback[item] = (mn > 0 && tol < 1.0 && !fits) ? 1 : 0;
-        colcount[item] = cols;
-    }
-    int* jpg = jpvt_ws + it.col_off;
-    if (mn == 0 || tol >= 1.0) {
-        // choose_rank gives 0 for an empty diagonal and for tol >= 1: no reflectors
-        if (me == 0) {
-            for (int j = threadIdx.x; j < cols; j += blockDim.x) jpg[j] = j;
-            if (threadIdx.x == 0) rank_out[it.cluster] = 0;
-        }
-        return;
-    }
-    if (!fits) return;
-    T* A = reinterpret_cast<T*>(smem_raw);
-    T* vsh = A + (size_t)rows * cpc;
-    T* vn1 = vsh + rows;
-    T* vn2 = vn1 + cpc;
-    int* jp = reinterpret_cast<int*>(vn2 + cpc);
-    const int c0 = me * cpc;
-    const int c1 = min(cols, c0 + cpc);
-    const int nloc = max(0, c1 - c0);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    // gather this slab of Asn = [A_sn | A_ns^T] from the edge blocks
-    {
-        int col = 0;
-        for (int p = 0; p < it.count && col < c1; p++) {
-            const DAsn pc = pieces[it.first + p];
-            const int n = c.csize[pc.nbr];
-            const int lo = max(col, c0), hi = min(col + n, c1);
-            if (lo < hi) {
-                const T* B = bptr(c, pc.block);
-                const int bld = c.blk[pc.block].ld;
-                const int width = hi - lo;
-                if (!pc.transposed) {
-                    for (int idx = threadIdx.x; idx < rows * width; idx += blockDim.x) {
-                        int i = idx % rows, jj = idx / rows;
-                        A[i + (size_t)(lo - c0 + jj) * rows] = B[i + (size_t)(lo - col + jj) * bld];
-                    }
-                } else {
-                    for (int idx = threadIdx.x; idx < rows * width; idx += blockDim.x) {
-                        int jj = idx % width, i = idx / width;
-                        A[i + (size_t)(lo - c0 + jj) * rows] = B[(lo - col + jj) + (size_t)i * bld];
-                    }
-                }
-            }
-            col += n;
-        }
-    }
-    __syncthreads();
-    for (int j = w; j < nloc; j += nw) {
-        const T* a = A + (size_t)j * rows;
-        T s = 0;
-        for (int r = lane; r < rows; r += 32) s += a[r] * a[r];
-        s = warp_sum(s);
-        if (lane == 0) {
-            vn1[j] = dsqrt(s);
-            vn2[j] = vn1[j];
-            jp[j] = c0 + j;
-        }
-    }
-    const T tol3z = dsqrt(sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-07));
-    int rank = mn;
-    T r00 = 0;
-    for (int i = 0; i < mn; i++) {
-        __syncthreads();
-        // (1) cluster-wide largest partial norm over columns >= i
-        T bv = 0;
-        for (int j = max(i - c0, 0) + threadIdx.x; j < nloc; j += blockDim.x) bv = fmax(bv, vn1[j]);
-        for (int o = 16; o > 0; o >>= 1) bv = fmax(bv, __shfl_xor_sync(0xffffffffu, bv, o));
-        if (lane == 0) red[w] = bv;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            T m = red[0];
-            for (int k = 1; k < nw; k++) m = fmax(m, red[k]);
-            pub_max = m;
-        }
-        cl.sync();
-        T gmax = 0;
-        for (int q = 0; q < CS; q++) gmax = fmax(gmax, *cl.map_shared_rank(&pub_max, q));
-        const T thresh = gmax * (T(1) - qrcp_tie<T>());
-        // (2) first column >= i inside the tie window
-        int bi = cols;
-        for (int j = max(i - c0, 0) + threadIdx.x; j < nloc; j += blockDim.x)
-            if (vn1[j] >= thresh) { bi = c0 + j; break; }
-        for (int o = 16; o > 0; o >>= 1) bi = min(bi, __shfl_xor_sync(0xffffffffu, bi, o));
-        if (lane == 0) ired[w] = bi;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int m = ired[0];
-            for (int k = 1; k < nw; k++) m = min(m, ired[k]);
-            pub_idx = m;
-        }
-        cl.sync();
-        int pvt = cols;
-        for (int q = 0; q < CS; q++) pvt = min(pvt, *cl.map_shared_rank(&pub_idx, q));
-        if (pvt >= cols) pvt = i;  // all norms NaN: keep the current column
-        const int own_i = i / cpc;
-        // (3) the owner of column i swaps in the pivot column and builds the reflector
-        if (me == own_i) {
-            const int li = i - c0;
-            T* ai = A + (size_t)li * rows;
-            if (pvt != i) {
-                const int own_p = pvt / cpc;
-                const int lp = pvt - own_p * cpc;
-                T* Ap = cl.map_shared_rank(A, own_p) + (size_t)lp * rows;
-                for (int r = threadIdx.x; r < rows; r += blockDim.x) {
-                    T t = ai[r];
-                    ai[r] = Ap[r];
-                    Ap[r] = t;
-                }
-                if (threadIdx.x == 0) {
-                    T* rvn1 = cl.map_shared_rank(vn1, own_p);
-                    T* rvn2 = cl.map_shared_rank(vn2, own_p);
-                    int* rjp = cl.map_shared_rank(jp, own_p);
-                    int t = jp[li];
-                    jp[li] = rjp[lp];
-                    rjp[lp] = t;
-                    rvn1[lp] = vn1[li];
-                    rvn2[lp] = vn2[li];
-                }
-                __syncthreads();
-            }
-            T part = 0;
-            for (int r = i + 1 + threadIdx.x; r < rows; r += blockDim.x) part += ai[r] * ai[r];
-            const T xnorm2 = block_sum(part, red);
-            if (threadIdx.x == 0) {
-                const T alpha = ai[i];
-                const T xnorm = dsqrt(xnorm2);
-                T beta, tu, sc;
-                if (xnorm == T(0)) {
-                    beta = alpha;
-                    tu = 0;
-                    sc = 0;
-                } else {
-                    beta = -copysign(hypot(alpha, xnorm), alpha);
-                    tu = (beta - alpha) / beta;
-                    sc = T(1) / (alpha - beta);
-                }
-                const T rii = fabs(beta);
-                T ref = (i == 0) ? rii : pub_r00;
-                int stop = 0;
-                if (tol != 0.0 && i >= 1 && !(rii / ref >= T(tol))) stop = 1;
-                pub_beta = beta;
-                pub_tau = tu;
-                pub_r00 = ref;
-                pub_stop = stop;
-                red[32] = sc;
-            }
-            __syncthreads();
-            if (!pub_stop) {
-                const T sc = red[32];
-                if (pub_tau != T(0))
-                    for (int r = i + 1 + threadIdx.x; r < rows; r += blockDim.x) ai[r] *= sc;
-                __syncthreads();
-                if (threadIdx.x == 0) {
-                    ai[i] = pub_beta;
-                    taus[it.tau_off + i] = pub_tau;
-                }
-            }
-        }
-        cl.sync();
-        const int stop = *cl.map_shared_rank(&pub_stop, own_i);
-        const T tu = *cl.map_shared_rank(&pub_tau, own_i);
-        if (me != own_i && threadIdx.x == 0) pub_r00 = *cl.map_shared_rank(&pub_r00, own_i);
-        if (stop) {
-            rank = i;
-            break;
-        }
-        // (4) reflector from the owner's slab, applied to this slab's columns > i
-        {
-            const T* vi = cl.map_shared_rank(A, own_i) + (size_t)(i - own_i * cpc) * rows;
-            for (int r = i + 1 + threadIdx.x; r < rows; r += blockDim.x) vsh[r] = vi[r];
-            if (threadIdx.x == 0) vsh[i] = T(1);
-        }
-        __syncthreads();
-        for (int j = max(i + 1 - c0, 0) + w; j < nloc; j += nw) {
-            T* aj = A + (size_t)j * rows;
-            if (tu != T(0)) {
-                T s = 0;
-                for (int r = i + lane; r < rows; r += 32) s += vsh[r] * aj[r];
-                s = warp_sum(s) * tu;
-                for (int r = i + lane; r < rows; r += 32) aj[r] -= s * vsh[r];
-            }
-            __syncwarp();
-            const T v1 = vn1[j];
-            if (v1 != T(0)) {
-                T temp = fabs(aj[i]) / v1;
-                temp = T(1) - temp * temp;
-                temp = temp > T(0) ? temp : T(0);
-                const T rr = v1 / vn2[j];
-                const T temp2 = temp * rr * rr;
-                if (temp2 <= tol3z) {
-                    T s = 0;
-                    for (int r = i + 1 + lane; r < rows; r += 32) s += aj[r] * aj[r];
-                    s = warp_sum(s);
-                    if (lane == 0) {
-                        if (i < rows - 1) {
-                            vn1[j] = dsqrt(s);
-                            vn2[j] = vn1[j];
-                        } else {
-                            vn1[j] = 0;
-                            vn2[j] = 0;
-                        }
-                    }
-                } else if (lane == 0) {
-                    vn1[j] = v1 * dsqrt(temp);
-                }
-            }
-            __syncwarp();
-        }
-    }
-    // no CTA leaves while another may still read its shared memory
-    cl.sync();
-    const int ld = c.cap[it.cluster];
-    T* W = ws + it.ws_off;
-    for (int idx = threadIdx.x; idx < rows * nloc; idx += blockDim.x) {
-        int i = idx % rows, j = idx / rows;
-        W[i + (size_t)(c0 + j) * ld] = A[i + (size_t)j * rows];
-    }
-    for (int j = threadIdx.x; j < nloc; j += blockDim.x) jpg[c0 + j] = jp[j];
-    if (me == 0 && threadIdx.x == 0) rank_out[it.cluster] = rank;
-}
-
-// QRCP, version without column movement.  The sparsification matrix stays in the shared
-// memory of a thread-block cluster (CS CTAs, column slabs); a column never moves: the
-// pivoting is tracked as a permutation (perm: position -> column, replicated in every
-// CTA; pos: column -> position for the slab's own columns).  Per pivot step i:
-//   1. every CTA reads the published (slab maximum m_q, first position f_q inside the tie
-//      window of m_q) of all slabs and derives the pivot; exact as long as no slab maximum
-//      lies inside the tie window below the global one (else one more barrier);
-//   2. every CTA reads the pivot column through distributed shared memory and builds the
-//      Householder reflector itself (identical arithmetic in every CTA);
-//   3. every CTA applies the reflector to its trailing columns (G threads per column) and
-//      downdates their norms (LAWN 176), then publishes its next (m, f) and arrives at the
-//      cluster barrier.
-// The owner writes the reflector into the pivot column one step later, once no CTA can
-// still be reading that column.  At the end the slabs are written to the global workspace
-// in LAPACK's column order (position p holds column perm[p]).
-template <typename T>
-__device__ __forceinline__ void qc_barrier(cooperative_groups::cluster_group& cl, int cs) {
-    if (cs > 1) cl.sync();
-    else __syncthreads();
-}
-
-template <typename T>
-__global__ void __launch_bounds__(QC_THREADS) qrcp3_kernel(Ctx<T> c, const DSpars* __restrict__ items,
-                                                           const DAsn* __restrict__ pieces, T* ws, int* jpvt_ws,
-                                                           T* taus, int* rank_out, int* colcount, int* fallback,
-                                                           double tol, int smem_bytes, unsigned long long* probe) {
-    namespace cgx = cooperative_groups;
-    cgx::cluster_group cl = cgx::this_cluster();
-    const int CS = (int)cl.num_blocks();
-    const int me = (int)cl.block_rank();
-    const int item = blockIdx.x / CS;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ T red[32];
-    __shared__ int ired[32];
-    __shared__ T pubm[2][16];
-    __shared__ int pubf[2][16];
-    __shared__ T s_alpha;
-    if (c.status->not_spd) return;
-    const DSpars it = items[item];
-    const int rows = c.csize[it.cluster];
-    int cols = 0;
-    for (int p = 0; p < it.count; p++) cols += c.csize[pieces[it.first + p].nbr];
-    const int mn = min(rows, cols);
-    const int cpc = (cols + CS - 1) / CS;
-    const int lda = rows | 1;
-    const long long need = ((long long)lda * cpc + rows + 2LL * cpc) * sizeof(T) + ((long long)cols + cpc) * sizeof(int);
-    const bool fits = need <= smem_bytes;
-    if (threadIdx.x == 0 && me == 0) {
-        fallback[item] = (mn > 0 && tol < 1.0 && !fits) ? 1 : 0;
-        colcount[item] = cols;
-    }
-    int* jpg = jpvt_ws + it.col_off;
-    if (mn == 0 || tol >= 1.0) {
-        if (me == 0) {
-            for (int j = threadIdx.x; j < cols; j += blockDim.x) jpg[j] = j;
-            if (threadIdx.x == 0) rank_out[it.cluster] = 0;
-        }
-        return;
-    }
-    if (!fits) return;
-    T* A = reinterpret_cast<T*>(smem_raw);
-    T* vsh = A + (size_t)lda * cpc;
-    T* vn1 = vsh + rows;
-    T* vn2 = vn1 + cpc;
-    int* perm = reinterpret_cast<int*>(vn2 + cpc);
-    int* pos = perm + cols;
-    const int c0 = me * cpc;
-    const int c1 = min(cols, c0 + cpc);
-    const int nloc = max(0, c1 - c0);
-    const int tid = threadIdx.x, nth = blockDim.x;
-    const int lane = tid & 31, w = tid >> 5, nw = nth >> 5;
-    // gather the slab of Asn = [A_sn | A_ns^T]
-    {
-        int col = 0;
-        for (int p = 0; p < it.count && col < c1; p++) {
-            const DAsn pc = pieces[it.first + p];
-            const int n = c.csize[pc.nbr];
-            const int lo = max(col, c0), hi = min(col + n, c1);
-            if (lo < hi) {
-                const T* B = bptr(c, pc.block);
-                const int bld = c.blk[pc.block].ld;
-                const int width = hi - lo;
-                if (!pc.transposed) {
-                    for (int idx = tid; idx < rows * width; idx += nth) {
-                        int i = idx % rows, jj = idx / rows;
-                        A[i + (size_t)(lo - c0 + jj) * lda] = B[i + (size_t)(lo - col + jj) * bld];
-                    }
-                } else {
-                    for (int idx = tid; idx < rows * width; idx += nth) {
-                        int jj = idx % width, i = idx / width;
-                        A[i + (size_t)(lo - c0 + jj) * lda] = B[(lo - col + jj) + (size_t)i * bld];
-                    }
-                }
-            }
-            col += n;
-        }
-    }
-    for (int p = tid; p < cols; p += nth) perm[p] = p;
-    for (int j = tid; j < nloc; j += nth) pos[j] = c0 + j;
-    __syncthreads();
-    for (int j = w; j < nloc; j += nw) {
-        const T* a = A + (size_t)j * lda;
-        T s = 0;
-        for (int r = lane; r < rows; r += 32) s += a[r] * a[r];
-        s = warp_sum(s);
-        if (lane == 0) {
-            vn1[j] = dsqrt(s);
-            vn2[j] = vn1[j];
-        }
-    }
-    // threads per column for the trailing update
-    int G = 1;
-    while (G < 8 && (nloc * G * 2 <= nth || rows >= 64 * G)) G *= 2;
-    const int gid = tid / G, gl = tid % G, ngroups = nth / G;
-    const T tie = T(1) - qrcp_tie<T>();
-    const T tol3z = dsqrt(sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-07));
-
-    // publish (slab max over columns at positions >= from, first position inside its tie window)
-    auto publish = [&](int par, int from) {
-        __syncthreads();
-        T m = 0;
-        for (int j = tid; j < nloc; j += nth)
-            if (pos[j] >= from) m = fmax(m, vn1[j]);
-        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (lane == 0) red[w] = m;
-        __syncthreads();
-        m = red[0];
-        for (int k = 1; k < nw; k++) m = fmax(m, red[k]);
-        int f = INT_MAX;
-        for (int j = tid; j < nloc; j += nth)
-            if (pos[j] >= from && vn1[j] >= m * tie) f = min(f, pos[j]);
-        for (int o = 16; o > 0; o >>= 1) f = min(f, __shfl_xor_sync(0xffffffffu, f, o));
-        if (lane == 0) ired[w] = f;
-        __syncthreads();
-        if (tid == 0) {
-            for (int k = 1; k < nw; k++) f = min(f, ired[k]);
-            f = min(f, ired[0]);
-            for (int q = 0; q < CS; q++) {
-                *cl.map_shared_rank(&pubm[par][me], q) = m;
-                *cl.map_shared_rank(&pubf[par][me], q) = f;
-            }
-        }
-    };
-
-    const bool probing = probe && item == 0 && me == 0 && tid == 0;
-    long long tmark = probing ? clock64() : 0;
-    auto mark = [&](int k) {
-        if (probing) {
-            long long t = clock64();
-            probe[k] += (unsigned long long)(t - tmark);
-            tmark = t;
-        }
-    };
-    publish(0, 0);
-    qc_barrier<T>(cl, CS);
-    mark(0);
-    int rank = mn;
-    T r00 = 0;
-    int pend = -1;        // local column awaiting its reflector
-    T pend_beta = 0;
-    int pend_i = 0;
-    for (int i = 0; i < mn; i++) {
-        const int par = i & 1;
-        T gmax = 0;
-        for (int q = 0; q < CS; q++) gmax = fmax(gmax, pubm[par][q]);
-        bool amb = false;
-        for (int q = 0; q < CS; q++) amb |= (pubm[par][q] < gmax && pubm[par][q] >= gmax * tie);
-        int pvt = INT_MAX;
-        if (!amb) {
-            for (int q = 0; q < CS; q++)
-                if (pubm[par][q] == gmax) pvt = min(pvt, pubf[par][q]);
-        } else {
-            // a slab maximum inside the tie window below the global one: search every slab
-            // with the global threshold
-            int f = INT_MAX;
-            for (int j = tid; j < nloc; j += nth)
-                if (pos[j] >= i && vn1[j] >= gmax * tie) f = min(f, pos[j]);
-            for (int o = 16; o > 0; o >>= 1) f = min(f, __shfl_xor_sync(0xffffffffu, f, o));
-            if (lane == 0) ired[w] = f;
-            __syncthreads();
-            if (tid == 0) {
-                for (int k = 0; k < nw; k++) f = min(f, ired[k]);
-                for (int q = 0; q < CS; q++) *cl.map_shared_rank(&pubf[par][me], q) = f;
-            }
-            qc_barrier<T>(cl, CS);
-            for (int q = 0; q < CS; q++) pvt = min(pvt, pubf[par][q]);
-        }
-        if (pvt < i || pvt >= cols) pvt = i;  // all norms NaN: keep the current position
-        mark(1);
-        const int phys = perm[pvt];
-        const int phys_i = perm[i];
-        const int own = phys / cpc, lj = phys - own * cpc;
-        // reflector of the previous step into its column (no CTA reads it any more)
-        if (pend >= 0) {
-            T* a = A + (size_t)pend * lda;
-            for (int r = pend_i + 1 + tid; r < rows; r += nth) a[r] = vsh[r];
-            if (tid == 0) a[pend_i] = pend_beta;
-            pend = -1;
-        }
-        __syncthreads();
-        mark(2);
-        // pivot column -> vsh (rows >= i)
-        const T* src = (own == me ? A : cl.map_shared_rank(A, own)) + (size_t)lj * lda;
-        T part = 0;
-        for (int r = i + tid; r < rows; r += nth) {
-            const T v = src[r];
-            if (r == i) {
-                s_alpha = v;
-                vsh[r] = T(1);
-            } else {
-                vsh[r] = v;
-                part += v * v;
-            }
-        }
-        part = warp_sum(part);
-        if (lane == 0) red[w] = part;
-        __syncthreads();
-        T xnorm2 = 0;
-        for (int k = 0; k < nw; k++) xnorm2 += red[k];
-        const T alpha = s_alpha;
-        const T xnorm = dsqrt(xnorm2);
-        T beta, tu, sc;
-        if (xnorm == T(0)) {
-            beta = alpha;
-            tu = 0;
-            sc = 0;
-        } else {
-            beta = -copysign(hypot(alpha, xnorm), alpha);
-            tu = (beta - alpha) / beta;
-            sc = T(1) / (alpha - beta);
-        }
-        const T rii = fabs(beta);
-        if (i == 0) r00 = rii;
-        if (tol != 0.0 && i >= 1 && !(rii / r00 >= T(tol))) {
-            rank = i;
-            break;
-        }
-        if (tu != T(0))
-            for (int r = i + 1 + tid; r < rows; r += nth) vsh[r] *= sc;
-        if (me == 0 && tid == 0) taus[it.tau_off + i] = tu;
-        __syncthreads();  // vsh final; every thread has read perm
-        mark(3);
-        if (tid == 0) {
-            perm[i] = phys;
-            perm[pvt] = phys_i;
-        }
-        // trailing update of this slab's columns and their norms; positions after the swap.
-        // The loop runs the same number of times in every thread so that the group
-        // shuffles always see all 32 lanes.  The first lane of each group also keeps the
-        // largest new norm of its columns for the next pivot search.
-        T mloc = 0;
-        for (int base = 0; base < nloc; base += ngroups) {
-            const int j = base + gid;
-            const int ph = c0 + j;
-            const bool active = j < nloc && ph != phys && pos[j] >= i;
-            T* aj = A + (size_t)(active ? j : 0) * lda;
-            T s = 0;
-            if (active && tu != T(0)) {
-                // four independent partial sums so the shared-memory loads overlap
-                T s0 = 0, s1 = 0, s2 = 0, s3 = 0;
-                int r = i + gl;
-                for (; r + 3 * G < rows; r += 4 * G) {
-                    s0 += vsh[r] * aj[r];
-                    s1 += vsh[r + G] * aj[r + G];
-                    s2 += vsh[r + 2 * G] * aj[r + 2 * G];
-                    s3 += vsh[r + 3 * G] * aj[r + 3 * G];
-                }
-                for (; r < rows; r += G) s0 += vsh[r] * aj[r];
-                s = (s0 + s1) + (s2 + s3);
-            }
-            for (int o = G >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (active && tu != T(0)) {
-                s *= tu;
-                int r = i + gl;
-                for (; r + 3 * G < rows; r += 4 * G) {
-                    const T a0 = aj[r], a1 = aj[r + G], a2 = aj[r + 2 * G], a3 = aj[r + 3 * G];
-                    aj[r] = a0 - s * vsh[r];
-                    aj[r + G] = a1 - s * vsh[r + G];
-                    aj[r + 2 * G] = a2 - s * vsh[r + 2 * G];
-                    aj[r + 3 * G] = a3 - s * vsh[r + 3 * G];
-                }
-                for (; r < rows; r += G) aj[r] -= s * vsh[r];
-            }
-            __syncwarp();
-            // norm downdating (LAWN 176), decided by the group's first lane
-            int recompute = 0;
-            T newv = 0;
-            if (active && gl == 0) {
-                const T v1 = vn1[j];
-                newv = v1;
-                if (v1 != T(0)) {
-                    T temp = fabs(aj[i]) / v1;
-                    temp = T(1) - temp * temp;
-                    temp = temp > T(0) ? temp : T(0);
-                    const T rr = v1 / vn2[j];
-                    if (temp * rr * rr <= tol3z) recompute = 1;
-                    else newv = v1 * dsqrt(temp);
-                }
-            }
-            recompute = __shfl_sync(0xffffffffu, recompute, (lane / G) * G);
-            T q2 = 0;
-            if (active && recompute) {
-                T q0 = 0, q1 = 0, q2b = 0, q3 = 0;
-                int r = i + 1 + gl;
-                for (; r + 3 * G < rows; r += 4 * G) {
-                    q0 += aj[r] * aj[r];
-                    q1 += aj[r + G] * aj[r + G];
-                    q2b += aj[r + 2 * G] * aj[r + 2 * G];
-                    q3 += aj[r + 3 * G] * aj[r + 3 * G];
-                }
-                for (; r < rows; r += G) q0 += aj[r] * aj[r];
-                q2 = (q0 + q1) + (q2b + q3);
-            }
-            for (int o = G >> 1; o > 0; o >>= 1) q2 += __shfl_xor_sync(0xffffffffu, q2, o);
-            if (active && gl == 0) {
-                if (recompute) {
-                    newv = (i < rows - 1) ? dsqrt(q2) : T(0);
-                    vn2[j] = newv;
-                }
-                vn1[j] = newv;
-                if (ph == phys_i) pos[j] = pvt;
-                mloc = fmax(mloc, newv);
-            }
-            if (j < nloc && gl == 0 && ph == phys) pos[j] = i;
-        }
-        mark(4);
-        if (own == me) {
-            pend = lj;
-            pend_beta = beta;
-            pend_i = i;
-        }
-        if (i + 1 < mn) {
-            // publish (slab maximum, first position inside its tie window) for step i+1;
-            // every thread rescans only the columns it updated itself
-            for (int o = 16; o > 0; o >>= 1) mloc = fmax(mloc, __shfl_xor_sync(0xffffffffu, mloc, o));
-            if (lane == 0) red[w] = mloc;
-            __syncthreads();
-            T m = red[0];
-            for (int k = 1; k < nw; k++) m = fmax(m, red[k]);
-            int f = INT_MAX;
-            if (gl == 0)
-                for (int j = gid; j < nloc; j += ngroups)
-                    if (pos[j] > i && vn1[j] >= m * tie) f = min(f, pos[j]);
-            for (int o = 16; o > 0; o >>= 1) f = min(f, __shfl_xor_sync(0xffffffffu, f, o));
-            if (lane == 0) ired[w] = f;
-            __syncthreads();
-            if (tid == 0) {
-                for (int k = 0; k < nw; k++) f = min(f, ired[k]);
-                for (int q = 0; q < CS; q++) {
-                    *cl.map_shared_rank(&pubm[par ^ 1][me], q) = m;
-                    *cl.map_shared_rank(&pubf[par ^ 1][me], q) = f;
-                }
-            }
-            mark(5);
-            qc_barrier<T>(cl, CS);
-            mark(6);
-        }
-        if (probing) probe[7] += 1;
-    }
-    if (pend >= 0) {
-        __syncthreads();
-        T* a = A + (size_t)pend * lda;
-        for (int r = pend_i + 1 + tid; r < rows; r += nth) a[r] = vsh[r];
-        if (tid == 0) a[pend_i] = pend_beta;
-    }
-    // no CTA leaves while another may still read its shared memory
-    qc_barrier<T>(cl, CS);
-    const int ld = c.cap[it.cluster];
-    T* W = ws + it.ws_off;
-    for (int j = w; j < nloc; j += nw) {
-        const int p = pos[j];
-        const T* a = A + (size_t)j * lda;
-        T* dst = W + (size_t)p * ld;
-        for (int r = lane; r < rows; r += 32) dst[r] = a[r];
-        if (lane == 0) jpg[p] = c0 + j;
-    }
-    if (me == 0 && tid == 0) rank_out[it.cluster] = rank;
 }
 
 // Blocked compact WY form of Q = H_0 ... H_{k-1}: reflectors in blocks of QB = 32,
 // Q = Q_0 Q_1 ..., Q_b = I - V_b T_b V_b^T with T_b the 32x32 upper triangular factor of
-// block b (LAPACK dlarft, forward, columnwise, per block).  One warp per block: lanes
-// compute Z_b = striu(V_b^T V_b) then the 32-step recurrence
-// T_b[j][i] = -tau_i sum_{l=j}^{i-1} T_b[j][l] Z_b[l][i].  T_b is stored in the diagonal
-// block b of the k x k T store (ld ldt); Z uses the same positions of the scratch zs.
+// block b (LAPACK dlarft, forward, columnwise, per block):
+//   T_b[i][i] = tau_i,  T_b[j][i] = -tau_i sum_{l=j}^{i-1} T_b[j][l] Z_b[l][i]  (j < i),
+// Z_b = V_b^T V_b (V_b unit lower trapezoidal).  Phase 1: one pass over the rows of up to
+// LB_GROUP blocks, staged LB_ROWS rows at a time in shared memory; thread (w, lane) sums
+// Z_b[w + 8q][lane], q < 4, for every block of the group.  Phase 2: warp b runs the
+// 32-step recurrence of block b with row j of T_b in lane j's registers and column i of
+// Z_b in lane i's registers.  T_b goes to the diagonal block b of the k x k T store (ld
+// ldt).  256 threads; sm holds larft_smem_elems() elements.
 constexpr int QB = 32;
+constexpr int LB_GROUP = 8;
+constexpr int LB_ROWS = 32;
+constexpr int LB_LD = LB_GROUP * QB + 1;
+__host__ __device__ constexpr int larft_smem_elems() {
+    return LB_ROWS * LB_LD > LB_GROUP * QB * (QB + 1) ? LB_ROWS * LB_LD : LB_GROUP * QB * (QB + 1);
+}
 
 template <typename T>
-__device__ void larft_blocks(const T* V, int ldv, int rows, int k, const T* tau, T* Tm, int ldt, T* zs) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+__device__ void larft_blocks(const T* V, int ldv, int rows, int k, const T* tau, T* Tm, int ldt, T* sm) {
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const int lane = tid & 31, w = tid >> 5;
     const int nb = (k + QB - 1) / QB;
-    for (int b = w; b < nb; b += nw) {
-        const int i0 = b * QB, bw = min(QB, k - i0);
-        T* Z = zs + (size_t)i0 + (size_t)i0 * ldt;
-        T* Tb = Tm + (size_t)i0 + (size_t)i0 * ldt;
-        // Z[j][i] = v_j^T v_i, j < i (overlap from row i0+i where v_i is 1)
-        for (int i = 1; i < bw; i++) {
-            const T* vi = V + (size_t)(i0 + i) * ldv;
-            for (int j = 0; j < i; j++) {
-                const T* vj = V + (size_t)(i0 + j) * ldv;
-                T s = 0;
-                for (int r = i0 + i + 1 + lane; r < rows; r += 32) s += vj[r] * vi[r];
-                s = warp_sum(s);
-                if (lane == 0) Z[j + (size_t)i * ldt] = vj[i0 + i] + s;
+    for (int g0 = 0; g0 < nb; g0 += LB_GROUP) {
+        const int gb = min(LB_GROUP, nb - g0);
+        const int c0 = g0 * QB, gw = gb * QB;
+        T acc[LB_GROUP][4];
+#pragma unroll
+        for (int b = 0; b < LB_GROUP; b++)
+#pragma unroll
+            for (int q = 0; q < 4; q++) acc[b][q] = T(0);
+        for (int r0 = c0; r0 < rows; r0 += LB_ROWS) {
+            __syncthreads();
+            for (int idx = tid; idx < LB_ROWS * gw; idx += nth) {
+                const int rr = idx % LB_ROWS, cc = idx / LB_ROWS;
+                const int r = r0 + rr, j = c0 + cc;
+                T v = T(0);
+                if (r < rows && j < k) v = r > j ? V[r + (size_t)j * ldv] : (r == j ? T(1) : T(0));
+                sm[rr * LB_LD + cc] = v;
+            }
+            __syncthreads();
+            const int nr = min(LB_ROWS, rows - r0);
+            for (int rr = 0; rr < nr; rr++) {
+                const T* tr = sm + rr * LB_LD;
+#pragma unroll
+                for (int b = 0; b < LB_GROUP; b++) {
+                    if (b < gb) {
+                        const T vi = tr[b * QB + lane];
+#pragma unroll
+                        for (int q = 0; q < 4; q++) acc[b][q] += tr[b * QB + w + 8 * q] * vi;
+                    }
+                }
             }
         }
-        __syncwarp();
-        for (int i = 0; i < bw; i++) {
-            if (lane < i) {
-                T s = 0;
-                for (int l = lane; l < i; l++) s += Tb[lane + (size_t)l * ldt] * Z[l + (size_t)i * ldt];
-                Tb[lane + (size_t)i * ldt] = -tau[i0 + i] * s;
+        __syncthreads();
+#pragma unroll
+        for (int b = 0; b < LB_GROUP; b++)
+            if (b < gb)
+#pragma unroll
+                for (int q = 0; q < 4; q++) sm[(b * QB + w + 8 * q) * (QB + 1) + lane] = acc[b][q];
+        __syncthreads();
+        if (w < gb) {
+            const int i0 = c0 + w * QB, bw = min(QB, k - i0);
+            T zc[QB], trow[QB];
+#pragma unroll
+            for (int l = 0; l < QB; l++) {
+                zc[l] = sm[(w * QB + l) * (QB + 1) + lane];
+                trow[l] = T(0);
             }
-            if (lane == i) Tb[i + (size_t)i * ldt] = tau[i0 + i];
-            __syncwarp();
+            const T ti = lane < bw ? tau[i0 + lane] : T(0);
+#pragma unroll
+            for (int i = 0; i < QB; i++) {
+                const T taui = __shfl_sync(0xffffffffu, ti, i);
+                T sum = T(0);
+#pragma unroll
+                for (int l = 0; l < i; l++) sum += trow[l] * __shfl_sync(0xffffffffu, zc[l], i);
+                if (lane < i) trow[i] = -taui * sum;
+                else if (lane == i) trow[i] = taui;
+            }
+            if (lane < bw)
+#pragma unroll
+                for (int l = 0; l < QB; l++)
+                    if (l < bw) Tm[(i0 + lane) + (size_t)(i0 + l) * ldt] = trow[l];
         }
     }
 }
 
-// Compressed edges AsnP = triu(R[:k,:]) P^T written back into the cluster's edge blocks,
-// reflectors saved for the Orthogonal op, cluster size set to the rank.
+// WY factors of a sparsified cluster's reflectors (for the Orthogonal op of the solve),
+// its tau saved, its size set to the rank.  One CTA per cluster of the wave.  The
+// reflectors are read in place from the QRCP workspace (below the diagonal of the
+// position-ordered Asn, ld = capacity).
 template <typename T>
-__global__ void sparsify_scatter_kernel(Ctx<T> c, const DSpars* __restrict__ items, const DAsn* __restrict__ pieces,
-                                        T* ws, int* jpvt_ws, int* ipvt_ws, const int* __restrict__ rank_in,
-                                        T* vstore, const T* taus_ws, T* taustore, const int* __restrict__ colcount,
-                                        T* tstore) {
+__global__ void __launch_bounds__(256) sparsify_wy_kernel(Ctx<T> c, const DSpars* __restrict__ items, const T* ws,
+                                                          const int* __restrict__ rank_in, const T* taus_ws,
+                                                          T* taustore, T* tstore) {
     if (c.status->not_spd) return;
     const DSpars it = items[blockIdx.x];
-    const int rows = c.csize[it.cluster];
+    const int rows = c.rows0[it.cluster];
     const int k = rank_in[it.cluster];
     if (k >= rows) return;
-    const int cols = colcount[blockIdx.x];
+    const int ld = c.cap[it.cluster];
+    for (int j = threadIdx.x; j < k; j += blockDim.x) taustore[it.tau_off + j] = taus_ws[it.tau_off + j];
+    extern __shared__ __align__(16) unsigned char lb_raw[];
+    larft_blocks(ws + it.ws_off, ld, rows, k, taus_ws + it.tau_off, tstore + it.v_off, ld, reinterpret_cast<T*>(lb_raw));
+    if (threadIdx.x == 0) c.csize[it.cluster] = k;
+}
+
+// Compressed edges AsnP = triu(R[:k,:]) P^T written back into the cluster's edge blocks
+// and the reflectors copied to their persistent store.  Grid (items, tiles): a CTA copies
+// one 32-column tile of the reflectors (capacity tiles first) or of one edge block (then
+// the capacity tiles of every piece).  Column c of Asn comes from position ipvt[c] of the
+// QRCP output.  The cluster's own size is read from the level snapshot: the WY kernel
+// of the same wave sets it to the rank.
+template <typename T>
+__global__ void __launch_bounds__(256) sparsify_scatter_kernel(Ctx<T> c, const DSpars* __restrict__ items,
+                                                               const DAsn* __restrict__ pieces, const T* ws,
+                                                               const int* __restrict__ ipvt_ws,
+                                                               const int* __restrict__ rank_in, T* vstore) {
+    __shared__ T tile[32][33];
+    __shared__ int qs[32];
+    if (c.status->not_spd) return;
+    const DSpars it = items[blockIdx.x];
+    const int rows = c.rows0[it.cluster];
+    const int k = rank_in[it.cluster];
+    if (k >= rows) return;
     const int ld = c.cap[it.cluster];
     const T* A = ws + it.ws_off;
-    const int* jpvt = jpvt_ws + it.col_off;
-    int* ipvt = ipvt_ws + it.col_off;
-    (void)0;
-    if (k > 0)
-        for (int j = threadIdx.x; j < cols; j += blockDim.x) {
-            const int q = jpvt[j];
-            if (q >= 0 && q < cols) ipvt[q] = j;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int t = blockIdx.y;
+    const int nvt = (ld + 31) / 32;
+    if (t < nvt) {
+        T* V = vstore + it.v_off;
+        for (int jj = w; jj < 32; jj += nw) {
+            const int j = 32 * t + jj;
+            if (j >= k) break;
+            for (int r = lane; r < rows; r += 32) V[r + (size_t)j * ld] = A[r + (size_t)j * ld];
         }
-    T* V = vstore + it.v_off;
-    for (int idx = threadIdx.x; idx < rows * k; idx += blockDim.x) {
-        int i = idx % rows, j = idx / rows;
-        V[i + (size_t)j * ld] = A[i + (size_t)j * ld];
+        return;
     }
-    for (int j = threadIdx.x; j < k; j += blockDim.x) taustore[it.tau_off + j] = taus_ws[it.tau_off + j];
-    __syncthreads();
-    int col = 0;
-    for (int p = 0; p < it.count; p++) {
-        const DAsn pc = pieces[it.first + p];
-        const int n = c.csize[pc.nbr];
-        T* B = bptr(c, pc.block);
-        const int bld = c.blk[pc.block].ld;
-        for (int idx = threadIdx.x; idx < k * n; idx += blockDim.x) {
-            int i, jj;
-            if (!pc.transposed) { i = idx % k; jj = idx / k; } else { jj = idx % n; i = idx / n; }
-            const int q = ipvt[col + jj];
-            const T v = (i <= q) ? A[i + (size_t)q * ld] : T(0);
-            if (!pc.transposed) B[i + (size_t)jj * bld] = v;
-            else B[jj + (size_t)i * bld] = v;
+    t -= nvt;
+    int col = 0, p = 0;
+    for (; p < it.count; p++) {
+        const int nbr = pieces[it.first + p].nbr;
+        const int nt = (c.cap[nbr] + 31) / 32;
+        if (t < nt) break;
+        t -= nt;
+        col += c.csize[nbr];
+    }
+    if (p >= it.count) return;
+    const DAsn pc = pieces[it.first + p];
+    const int n = c.csize[pc.nbr];
+    const int j0 = 32 * t;
+    if (j0 >= n) return;
+    const int jw = min(32, n - j0);
+    const int* ipvt = ipvt_ws + it.col_off + col + j0;
+    T* B = bptr(c, pc.block);
+    const int bld = c.blk[pc.block].ld;
+    if (!pc.transposed) {
+        for (int jj = w; jj < jw; jj += nw) {
+            const int q = ipvt[jj];
+            const T* src = A + (size_t)q * ld;
+            T* dst = B + (size_t)(j0 + jj) * bld;
+            for (int i = lane; i < k; i += 32) dst[i] = i <= q ? src[i] : T(0);
         }
-        col += n;
+    } else {
+        if (threadIdx.x < jw) qs[threadIdx.x] = ipvt[threadIdx.x];
+        __syncthreads();
+        for (int i0 = 0; i0 < k; i0 += 32) {
+            const int i = i0 + lane;
+            for (int jj = w; jj < jw; jj += nw) {
+                const int q = qs[jj];
+                tile[jj][lane] = (i < k && i <= q) ? A[i + (size_t)q * ld] : T(0);
+            }
+            __syncthreads();
+            for (int ii = w; ii < 32 && i0 + ii < k; ii += nw)
+                if (lane < jw) B[(j0 + lane) + (size_t)(i0 + ii) * bld] = tile[lane][ii];
+            __syncthreads();
+        }
     }
-    __syncthreads();
-    // WY triangular factor of the reflectors, for the solve; the QRCP workspace (R is no
-    // longer needed) holds the k x k scratch
-    larft_blocks(V, ld, rows, k, taus_ws + it.tau_off, tstore + it.v_off, ld, ws + it.ws_off);
-    if (threadIdx.x == 0) c.csize[it.cluster] = k;
 }
 
 // ------------------------------------------------------------------------------------
@@ -1937,6 +1285,7 @@ class DeviceFactor : public DeviceFactorBase {
     void upload(const Plan& P, const std::vector<int64_t>& amap) override {
         P_ = &P;
         nc_ = P.nclusters;
+        init_qrcp_limits();
         arena_ = alloc<T>(P.arena_len);
         pristine_ = alloc<T>(P.assembled_len);
         amap_n_ = (int64_t)amap.size();
@@ -2025,12 +1374,17 @@ class DeviceFactor : public DeviceFactorBase {
                 W.n = (int)items.size();
                 W.items = up(items);
                 W.maxcap = maxcap;
+                for (const SparsifyItem& it : wave) {
+                    int nt = (P.c_cap[it.cluster] + 31) / 32;
+                    for (int p = 0; p < it.count; p++) nt += (P.c_cap[P.asn_pieces[it.first + p].nbr] + 31) / 32;
+                    W.ytiles = std::max(W.ytiles, nt);
+                }
                 W.host = wave;
                 {
                     // capacity bound until the first factorization reports the actual sizes
-                    int64_t need = 0;
-                    for (const SparsifyItem& it : wave) need = std::max(need, qc_need(P.c_cap[it.cluster], it.cap_cols, 1));
-                    choose_cluster(W, need);
+                    std::vector<std::pair<int, int>> dims;
+                    for (const SparsifyItem& it : wave) dims.push_back({P.c_cap[it.cluster], it.cap_cols});
+                    choose_cluster(W, dims);
                 }
                 D.waves.push_back(W);
             }
@@ -2141,9 +1495,10 @@ class DeviceFactor : public DeviceFactorBase {
         SPAND_CUDA(cudaFuncSetAttribute(trtri_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(trsm3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(qrcp_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        SPAND_CUDA(cudaFuncSetAttribute(qrcp3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, QC_SMEM_MAX));
         fallback_ = alloc<int>(max_items);
         SPAND_CUDA(cudaFuncSetAttribute(trsv3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SPAND_CUDA(cudaFuncSetAttribute(sparsify_wy_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        larft_smem_elems() * (int)sizeof(T)));
         SPAND_CUDA(cudaFuncSetAttribute(ortho_wyb_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         caps_h_ = P.c_cap;
     }
@@ -2201,19 +1556,27 @@ class DeviceFactor : public DeviceFactorBase {
                     snapshot_kernel<<<(D.n_level + 255) / 256, 256, 0, s_>>>(csize_, rows0_, D.level_clusters,
                                                                              D.n_level);
                 });
-            for (WaveDev& W : D.waves) {
+            for (size_t wi = 0; wi < D.waves.size(); wi++) {
+                WaveDev& W = D.waves[wi];
+                cur_wave_ = (int)wi;
                 launch("qrcp", [&] { launch_qrcp_cluster(W, tol); });
+                cur_wave_ = -1;
                 // matrices larger than the cluster's shared memory: gather to global memory
                 // and factor there (blocks of other matrices exit at once)
                 launch("qrcp_fallback", [&] {
                     asn_gather_kernel<T><<<W.n, 256, 0, s_>>>(ctx_, W.items, pieces_, ws_, colcount_, fallback_);
-                    qrcp_kernel<T><<<W.n, 512, W.maxcap * sizeof(T), s_>>>(ctx_, W.items, ws_, norms_, jpvt_,
+                    qrcp_kernel<T><<<W.n, 512, W.maxcap * sizeof(T), s_>>>(ctx_, W.items, ws_, norms_, jpvt_, ipvt_,
                                                                             colcount_, tauws_, rank_, tol, fallback_);
                 }, 2);
-                launch("sparsify_scatter", [&] {
-                    sparsify_scatter_kernel<T><<<W.n, 256, 0, s_>>>(ctx_, W.items, pieces_, ws_, jpvt_, ipvt_, rank_,
-                                                                     vstore_, tauws_, taustore_, colcount_, tstore_);
+                launch("sparsify_wy", [&] {
+                    sparsify_wy_kernel<T><<<W.n, 256, larft_smem_elems() * sizeof(T), s_>>>(
+                        ctx_, W.items, ws_, rank_, tauws_, taustore_, tstore_);
                 });
+                if (W.ytiles)
+                    launch("sparsify_scatter", [&] {
+                        sparsify_scatter_kernel<T><<<dim3((unsigned)W.n, (unsigned)W.ytiles), 256, 0, s_>>>(
+                            ctx_, W.items, pieces_, ws_, ipvt_, rank_, vstore_);
+                    });
             }
             if (D.merged) {
                 launch("merge_sizes", [&] {
@@ -2259,7 +1622,7 @@ class DeviceFactor : public DeviceFactorBase {
             for (size_t w = 0; w < D.waves.size(); w++)
                 for (const SparsifyItem& it : D.waves[w].host) wave_of[it.cluster] = (int)w;
             for (size_t w = 0; w < D.waves.size(); w++) {
-                int64_t need = 0;
+                std::vector<std::pair<int, int>> dims;
                 for (const SparsifyItem& it : D.waves[w].host) {
                     int64_t cols = 0;
                     for (int p = 0; p < it.count; p++) {
@@ -2267,10 +1630,19 @@ class DeviceFactor : public DeviceFactorBase {
                         auto wn = wave_of.find(n);
                         cols += (wn != wave_of.end() && wn->second < (int)w) ? cs[n] : r0[n];
                     }
+                    // 10% slack for the sizes of later factorizations
                     int rows = r0[it.cluster];
-                    need = std::max(need, qc_need(rows + rows / 10 + 1, (int)(cols + cols / 10 + 1), 1));
+                    dims.push_back({rows + rows / 10 + 1, (int)(cols + cols / 10 + 1)});
                 }
-                choose_cluster(D.waves[w], need);
+                choose_cluster(D.waves[w], dims);
+                if (per_wave_) {
+                    int maxr = 0;
+                    for (const SparsifyItem& it : D.waves[w].host) maxr = std::max(maxr, r0[it.cluster]);
+                    const WaveDev& Wv = D.waves[w];
+                    fprintf(stderr, "qrcp wave L%d w%zu: items %d max rows %d cs %d smem %d active %d\n",
+                            (int)(&D - levels_.data()), w, Wv.n, maxr, Wv.cs, Wv.smem,
+                            active_clusters(Wv.n * Wv.cs, Wv.cs, Wv.smem));
+                }
             }
         }
         // POTRF / TRSM shared memory from the actual pivot sizes (10% slack; larger
@@ -2419,6 +1791,7 @@ class DeviceFactor : public DeviceFactorBase {
         int maxcap = 1;
         int cs = 1;          // CTAs per thread-block cluster of the shared-memory QRCP
         int smem = 0;        // dynamic shared memory per CTA
+        int ytiles = 0;      // scatter tiles per matrix (reflector + edge-block capacity tiles)
         std::vector<SparsifyItem> host;  // plan items, for tuning
     };
     struct LevelDev {
@@ -2474,7 +1847,8 @@ class DeviceFactor : public DeviceFactorBase {
     template <typename F>
     void launch(const char* cls, F&& f, int kernels = 1) {
         if (prof_.enabled() && per_level_ && cur_level_ >= 0) {
-            const std::string name = std::string(cls) + "@L" + std::to_string(cur_level_);
+            std::string name = std::string(cls) + "@L" + std::to_string(cur_level_);
+            if (per_wave_ && cur_wave_ >= 0) name += "w" + std::to_string(cur_wave_);
             prof_.begin(s_, name.c_str());
         } else {
             prof_.begin(s_, cls);
@@ -2524,25 +1898,82 @@ class DeviceFactor : public DeviceFactorBase {
         side0 = {up(it0), up(t0), (int)t0.size(), 0, trsm_smem(clusters, P)};
         side1 = {up(it1), up(t1), (int)t1.size(), 1, trsm_smem(clusters, P)};
     }
-    static constexpr int QC_SMEM_MAX = 200 * 1024;
-    static constexpr int QC_SMEM_SHARED = 96 * 1024;  // two CTAs per SM
-    // shared-memory bytes of one CTA holding a rows x ceil(cols/cs) slab
-    static int64_t qc_need(int rows, int cols, int cs) {
-        int64_t cpc = (cols + cs - 1) / cs;
-        return ((int64_t)(rows | 1) * cpc + rows + 2 * cpc) * (int64_t)sizeof(T) + (cols + cpc) * (int64_t)sizeof(int);
+    // ---- QRCP launch configuration -------------------------------------------------
+    int qc_smem_cap_ = 0;  // dynamic shared memory per CTA available to the QRCP kernel
+    int qc_max_cs_ = 8;    // largest cluster (16 where non-portable sizes are allowed)
+    int num_sms_ = 1;
+    void init_qrcp_limits() {
+        int dev = 0, optin = 0;
+        SPAND_CUDA(cudaGetDevice(&dev));
+        SPAND_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        SPAND_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev));
+        const QcKernel<T> fn = qrcp_smem_kernel_ptr<T>();
+        cudaFuncAttributes fa;
+        SPAND_CUDA(cudaFuncGetAttributes(&fa, fn));
+        qc_smem_cap_ = (int)(optin - (int)fa.sharedSizeBytes) & ~255;
+        SPAND_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, qc_smem_cap_));
+        qc_max_cs_ = 8;
+        if (cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+            if (active_clusters(16, 16, qc_smem_cap_) > 0) qc_max_cs_ = 16;
+        } else {
+            cudaGetLastError();
+        }
     }
-    // smallest cluster whose shared memory holds `need` bytes (need computed for cs = 1)
-    void choose_cluster(WaveDev& W, int64_t need1) {
-        for (int cs = 1; cs <= 8; cs *= 2) {
-            int64_t per = need1 / cs + need1 / 8 + 2048;
-            if (per <= QC_SMEM_SHARED || (cs == 8 && per <= QC_SMEM_MAX)) {
-                W.cs = cs;
-                W.smem = (int)std::max<int64_t>(per, 4096);
-                return;
+    // co-resident thread-block clusters of a QRCP configuration (-1: not launchable)
+    int active_clusters(int ctas, int cs, int smem) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)ctas);
+        cfg.blockDim = dim3(QC_THREADS);
+        cfg.dynamicSmemBytes = (size_t)smem;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)cs;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int n = -1;
+        if (cudaOccupancyMaxActiveClusters(&n, qrcp_smem_kernel_ptr<T>(), &cfg) != cudaSuccess) {
+            cudaGetLastError();
+            n = -1;
+        }
+        return n;
+    }
+    // Cluster size and shared memory of a wave's QRCP launch.  dims: (rows, cols) bound
+    // of every matrix of the wave.  Per candidate cluster size: the slab of the largest
+    // matrix sets the shared memory, the occupancy query the number of co-resident
+    // clusters; the estimate is rounds x (per-step latency + shared-memory passes over the
+    // largest slab, shared by the CTAs resident on one SM) and the smallest wins.
+    void choose_cluster(WaveDev& W, const std::vector<std::pair<int, int>>& dims) {
+        double best = 1e300;
+        int bcs = 0, bsm = 0;
+        for (int cs = 1; cs <= qc_max_cs_; cs *= 2) {
+            int64_t sm = 4096, work = 0;
+            for (const auto& d : dims) {
+                sm = std::max<int64_t>(sm, qc_need(d.first, d.second, cs, (int)sizeof(T)));
+                work = std::max(work, (int64_t)d.first * ((d.second + cs - 1) / cs));
+            }
+            sm = (sm + 255) & ~int64_t(255);
+            if (sm > qc_smem_cap_) continue;
+            const int active = active_clusters(W.n * cs, cs, (int)sm);
+            if (active <= 0) continue;
+            const int rounds = (W.n + active - 1) / active;
+            const double resident = (double)std::min(W.n, active) * cs;
+            const double share = std::max(1.0, std::ceil(resident / num_sms_));
+            const double est = rounds * (3000.0 + 500.0 * std::log2((double)cs) + 5.0 / 32.0 * (double)work * share);
+            if (est < best) {
+                best = est;
+                bcs = cs;
+                bsm = (int)sm;
             }
         }
-        W.cs = 8;
-        W.smem = QC_SMEM_MAX;
+        if (!bcs) {  // matrices above the cap take the global-memory path
+            W.cs = qc_max_cs_;
+            W.smem = qc_smem_cap_;
+            return;
+        }
+        W.cs = bcs;
+        W.smem = bsm;
     }
     void launch_qrcp_cluster(WaveDev& W, double tol) {
         cudaLaunchConfig_t cfg = {};
@@ -2562,8 +1993,8 @@ class DeviceFactor : public DeviceFactorBase {
             probe = probe_;
             probe_waves_ += 1;
         }
-        SPAND_CUDA(cudaLaunchKernelEx(&cfg, qrcp3_kernel<T>, ctx_, (const DSpars*)W.items,
-                                      (const DAsn*)pieces_, ws_, jpvt_, tauws_, rank_, colcount_, fallback_, tol,
+        SPAND_CUDA(cudaLaunchKernelEx(&cfg, qrcp_smem_kernel_ptr<T>(), ctx_, (const DSpars*)W.items,
+                                      (const DAsn*)pieces_, ws_, jpvt_, ipvt_, tauws_, rank_, colcount_, fallback_, tol,
                                       W.smem, probe));
     }
     void launch_potrf(int* pivots, int* clusters, int n, int smem, const TrtriDev& tri) {
@@ -2714,6 +2145,9 @@ class DeviceFactor : public DeviceFactorBase {
     int probe_waves_ = 0;
     // per-level kernel classes in the profile (SPAND_PROFILE_LEVELS=1)
     bool per_level_ = getenv("SPAND_PROFILE_LEVELS") != nullptr;
+    // per-wave QRCP classes and a line per wave after tuning (SPAND_PROFILE_LEVELS=2)
+    bool per_wave_ = per_level_ && atoi(getenv("SPAND_PROFILE_LEVELS")) >= 2;
+    int cur_wave_ = -1;
     DAsn* pieces_ = nullptr;
     DUpd* d_ups_ = nullptr;
     std::vector<LevelDev> levels_;

@@ -1,0 +1,27 @@
+// QRCP of the sparsification matrices (rank-revealing Householder QR with column
+// pivoting, resident in the shared memory of a thread-block cluster): what the device
+// driver needs to configure and launch it.  The kernel lives in qrcp.cu.
+#pragma once
+
+#include "kcommon.cuh"
+
+namespace spand {
+
+constexpr int QC_THREADS = 256;
+
+// Shared memory of one CTA holding a rows x ceil(cols/cs) column slab: the slab (ld =
+// rows | 1), the reflector, two partial-norm arrays, the replicated permutation and the
+// slab's column positions.
+__host__ __device__ inline long long qc_need(int rows, int cols, int cs, int elem) {
+    const long long cpc = (cols + cs - 1) / cs;
+    return ((long long)(rows | 1) * cpc + rows + 2 * cpc) * elem + ((long long)cols + cpc) * 4;
+}
+
+template <typename T>
+using QcKernel = void (*)(Ctx<T>, const DSpars*, const DAsn*, T*, int*, int*, T*, int*, int*, int*, double, int,
+                          unsigned long long*);
+
+template <typename T>
+QcKernel<T> qrcp_smem_kernel_ptr();
+
+}  // namespace spand
