@@ -72,11 +72,11 @@ int spand_tree_solve(spand_tree* t, double* x, int nrhs, int ld);
 /* Same on a device buffer; runs on the tree's stream and returns without synchronising. */
 int spand_tree_solve_device(spand_tree* t, double* x_dev, int nrhs, int ld);
 /* No counterpart in the reference.  spand_tree_solve_device that allocates nothing: the
- * per-cluster solve vectors live in a fixed 16 MiB device array inside the library instead
- * of memory the tree allocates on its first solve.  For callers that cannot allocate when
- * they solve -- code being captured into a CUDA graph (no cudaMalloc during capture), code
- * with a preallocated memory budget, a framework that owns the allocator.  Limit:
- * x_len * nrhs * sizeof(factor type) <= 16 MiB, where x_len is the sum of all cluster
+ * per-cluster solve vectors and their scratch copy live in a fixed 16 MiB device array
+ * inside the library instead of memory the tree allocates on its first solve.  For callers
+ * that cannot allocate when they solve -- code being captured into a CUDA graph (no
+ * cudaMalloc during capture), code with a preallocated memory budget, a framework that owns
+ * the allocator.  Limit: 2 * x_len * nrhs * sizeof(factor type) <= 16 MiB, where x_len is the sum of all cluster
  * capacities (about 3N for a 3D grid); larger requests return SPAND_ERR_ARG.  The first call
  * on a device looks up the array's device address; make it before any stream capture.
  * All calls share the array, so allocation-free solves that overlap on the GPU race. */

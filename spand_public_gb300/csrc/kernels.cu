@@ -715,7 +715,10 @@ __global__ void __launch_bounds__(256) sparsify_wy_kernel(Ctx<T> c, const DSpars
     const int ld = c.cap[it.cluster];
     for (int j = threadIdx.x; j < k; j += blockDim.x) taustore[it.tau_off + j] = taus_ws[it.tau_off + j];
     extern __shared__ __align__(16) unsigned char lb_raw[];
-    larft_blocks(ws + it.ws_off, ld, rows, k, taus_ws + it.tau_off, tstore + it.v_off, ld, reinterpret_cast<T*>(lb_raw));
+    T* sm = reinterpret_cast<T*>(lb_raw);
+    const T* V = ws + it.ws_off;
+    T* Tm = tstore + it.v_off;
+    larft_blocks(V, ld, rows, k, taus_ws + it.tau_off, Tm, ld, sm);
     if (threadIdx.x == 0) c.csize[it.cluster] = k;
 }
 
@@ -885,47 +888,99 @@ __global__ void perm_out_kernel(double* __restrict__ x, int ldx, XCtx<T> X, cons
     x[perm[p] + (size_t)r * ldx] = (double)X.xs[slot[p] + r * X.xld];
 }
 
-// ------------------------------------------------------------------------------------
-// ScalingLLT ops of the solve (operations.cpp:97-103) as triangular products with the
-// inverse factor: fwd y[c] = sum_{k<=c} Linv[c][k] x[k] (a warp per c), bwd
-// y[c] = sum_{k>=c} Linv[k][c] x[k] (a thread per c).  One barrier.
-// ------------------------------------------------------------------------------------
+// Triangular products of the solve (ScalingLLT, operations.cpp:97-103): forward
+// x_c <- L_c^{-1} x_c, backward x_c <- L_c^{-T} x_c.  L^{-1} is stored transposed in the
+// strictly upper triangle of the pivot block (row i of L^{-1} = column i of the block),
+// its diagonal as 1 / L_ii.  Work list: (cluster, row tile).  A cluster of at most
+// 2*TV_ROWS rows is one tile, computed in place by one CTA; a larger one is cut into
+// TV_ROWS-row tiles whose CTAs write their rows to the scratch copy of the solve vectors;
+// the last CTA of the cluster to finish (atomic counter, reset by that CTA) copies the
+// rows back.  Forward: warp per row, lanes over the columns; backward: lanes over the
+// rows, warps over the columns, partial sums added in a fixed order.  All right-hand
+// sides in one CTA.  Shared memory: the staged x range + 8 x 2*TV_ROWS partial sums.
+constexpr int TV_ROWS = 32;
+constexpr int TV_THREADS = 256;
+
 template <typename T>
-__global__ void __launch_bounds__(512) trsv3_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ clusters,
-                                                   const int* __restrict__ lblocks, int count, int trans) {
-    const int item = blockIdx.x % count;
-    const int r = blockIdx.x / count;
+__global__ void __launch_bounds__(TV_THREADS) trsv4_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ clusters,
+                                                          const int* __restrict__ lblocks,
+                                                          const int2* __restrict__ tiles, int trans, T* tmp,
+                                                          int* counters) {
+    const int2 tl = tiles[blockIdx.x];
+    const int item = tl.x, tile = tl.y;
     const int cl = clusters[item];
     const int n = c.rows0[cl];
-    if (n == 0) return;
+    const int nt = n <= 2 * TV_ROWS ? 1 : (n + TV_ROWS - 1) / TV_ROWS;
+    if (n == 0 || tile >= nt) return;
+    const int r0 = nt == 1 ? 0 : tile * TV_ROWS, r1 = nt == 1 ? n : min(n, r0 + TV_ROWS);
     const T* L = bptr(c, lblocks[item]);
     const int ld = c.blk[lblocks[item]].ld;
-    T* x = X.xs + X.xoff[cl] + r * X.xld;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* xs = reinterpret_cast<T*>(smem_raw);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) xs[i] = x[i];
-    __syncthreads();
-    if (!trans) {
-        for (int cc = w; cc < n; cc += nw) {
-            const T* lrow = L + (size_t)cc * ld;
-            T s = 0;
-            for (int k = lane; k < cc; k += 32) s += lrow[k] * xs[k];
-            s = warp_sum(s);
-            if (lane == 0) x[cc] = s + xs[cc] / L[cc + (size_t)cc * ld];
-        }
-    } else {
-        for (int cc = threadIdx.x; cc < n; cc += blockDim.x) {
-            T s0 = 0, s1 = 0;
-            int k = cc + 1;
-            for (; k + 1 < n; k += 2) {
-                s0 += L[cc + (size_t)k * ld] * xs[k];
-                s1 += L[cc + (size_t)(k + 1) * ld] * xs[k + 1];
+    constexpr int NW = TV_THREADS / 32;
+    T* part = reinterpret_cast<T*>(smem_raw);  // NW x 2*TV_ROWS
+    T* xs = part + NW * 2 * TV_ROWS;            // x[lo, hi)
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int lo = trans ? r0 : 0, hi = trans ? n : r1;
+    for (int rhs = 0; rhs < X.nrhs; rhs++) {
+        const T* x = X.xs + X.xoff[cl] + (size_t)rhs * X.xld;
+        T* y = (nt == 1 ? X.xs : tmp) + X.xoff[cl] + (size_t)rhs * X.xld;
+        __syncthreads();
+        for (int k = lo + threadIdx.x; k < hi; k += TV_THREADS) xs[k - lo] = x[k];
+        __syncthreads();
+        if (!trans) {
+            for (int row = r0 + w; row < r1; row += NW) {
+                const T* lrow = L + (size_t)row * ld;
+                T a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                int k = lane;
+                for (; k + 7 * 32 < row; k += 8 * 32) {
+#pragma unroll
+                    for (int u = 0; u < 8; u++) a[u] += lrow[k + 32 * u] * xs[k + 32 * u];
+                }
+                for (; k < row; k += 32) a[0] += lrow[k] * xs[k];
+                const T s = warp_sum(((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7])));
+                if (lane == 0) y[row] = s + xs[row] / L[row + (size_t)row * ld];
             }
-            for (; k < n; k++) s0 += L[cc + (size_t)k * ld] * xs[k];
-            x[cc] = (s0 + s1) + xs[cc] / L[cc + (size_t)cc * ld];
+        } else {
+            const int nr = r1 - r0;
+            for (int rb = 0; rb < nr; rb += 32) {
+                const int row = r0 + rb + lane;
+                const bool live = rb + lane < nr;
+                T a[4] = {0, 0, 0, 0};
+                int k = r0 + 1 + w;
+                for (; k + 3 * NW < n; k += 4 * NW) {
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int kk = k + u * NW;
+                        if (live && row < kk) a[u] += L[row + (size_t)kk * ld] * xs[kk - lo];
+                    }
+                }
+                for (; k < n; k += NW)
+                    if (live && row < k) a[0] += L[row + (size_t)k * ld] * xs[k - lo];
+                part[w * 2 * TV_ROWS + rb + lane] = (a[0] + a[1]) + (a[2] + a[3]);
+            }
+            __syncthreads();
+            for (int q = threadIdx.x; q < nr; q += TV_THREADS) {
+                T s = 0;
+                for (int ww = 0; ww < NW; ww++) s += part[ww * 2 * TV_ROWS + q];
+                const int row = r0 + q;
+                y[row] = s + xs[row - lo] / L[row + (size_t)row * ld];
+            }
         }
     }
+    if (nt == 1) return;
+    // the last tile of the cluster copies the rows of every tile back
+    __threadfence();
+    __syncthreads();
+    __shared__ int last;
+    if (threadIdx.x == 0) last = atomicAdd(&counters[cl], 1) == nt - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    for (int rhs = 0; rhs < X.nrhs; rhs++) {
+        const size_t off = X.xoff[cl] + (size_t)rhs * X.xld;
+        for (int k = threadIdx.x; k < n; k += TV_THREADS) X.xs[off + k] = __ldcg(tmp + off + k);
+    }
+    if (threadIdx.x == 0) counters[cl] = 0;
 }
 
 // Forward Gemm ops grouped by neighbour n (operations.cpp:55-93): x_n -= sum over the
@@ -1426,6 +1481,20 @@ class DeviceFactor : public DeviceFactorBase {
             D.x_smem_elim = xsmem_for(L.op_elim_llt, P);
             D.x_smem_scale = xsmem_for(L.op_scale_llt, P);
             {
+                auto tv = [&](const std::vector<int>& cl, int& count) {
+                    std::vector<int2> t;
+                    for (size_t k = 0; k < cl.size(); k++) {
+                        const int cap = P.c_cap[cl[k]];
+                        const int nt = cap <= 2 * TV_ROWS ? 1 : (cap + TV_ROWS - 1) / TV_ROWS;
+                        for (int q = 0; q < nt; q++) t.push_back(make_int2((int)k, q));
+                    }
+                    count = (int)t.size();
+                    return up(t);
+                };
+                D.elim_tv = tv(L.op_elim_llt, D.n_elim_tv);
+                D.scale_tv = tv(L.op_scale_llt, D.n_scale_tv);
+            }
+            {
                 // Gemm ops grouped: forward by neighbour in op order, backward by
                 // eliminated cluster in reverse op order.
                 std::map<int, std::vector<DGemmOp>> fwd, bwd;
@@ -1496,7 +1565,9 @@ class DeviceFactor : public DeviceFactorBase {
         SPAND_CUDA(cudaFuncSetAttribute(trsm3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(qrcp_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         fallback_ = alloc<int>(max_items);
-        SPAND_CUDA(cudaFuncSetAttribute(trsv3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SPAND_CUDA(cudaFuncSetAttribute(trsv4_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        tv_count_ = alloc<int>(nc_);
+        SPAND_CUDA(cudaMemsetAsync(tv_count_, 0, (size_t)std::max(nc_, 1) * sizeof(int), s_));
         SPAND_CUDA(cudaFuncSetAttribute(sparsify_wy_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         larft_smem_elems() * (int)sizeof(T)));
         SPAND_CUDA(cudaFuncSetAttribute(ortho_wyb_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
@@ -1679,18 +1750,18 @@ class DeviceFactor : public DeviceFactorBase {
 
     void solve_device_noalloc(double* x, int nrhs, int ld) override {
         if (!factored_) throw DeviceError{SPAND_ERR_STATE, "solve before factorize"};
-        const size_t need = (size_t)xld_ * (size_t)nrhs * sizeof(T);
+        const size_t need = 2 * (size_t)xld_ * (size_t)nrhs * sizeof(T);
         if (need > kNoAllocSolveScratchBytes)
             throw DeviceError{SPAND_ERR_ARG, "allocation-free solve needs " + std::to_string(need) +
-                                                 " bytes of solve vectors (" + std::to_string(xld_) + " x " +
-                                                 std::to_string(nrhs) + " x " + std::to_string(sizeof(T)) +
-                                                 "); its fixed scratch holds " +
+                                                 " bytes of solve vectors and their scratch copy (2 x " +
+                                                 std::to_string(xld_) + " x " + std::to_string(nrhs) + " x " +
+                                                 std::to_string(sizeof(T)) + "); its fixed scratch holds " +
                                                  std::to_string(kNoAllocSolveScratchBytes) + " bytes"};
         T* slots = static_cast<T*>(noalloc_solve_scratch());
         const bool was_on = prof_.enabled();  // the profiler creates CUDA events
         prof_.enable(false);
         try {
-            run_solve_slots(x, nrhs, ld, slots);
+            run_solve_slots(x, nrhs, ld, slots, slots + (size_t)xld_ * nrhs);
         } catch (...) {
             prof_.enable(was_on);
             throw;
@@ -1822,6 +1893,8 @@ class DeviceFactor : public DeviceFactorBase {
         int n_elim_llt = 0, n_scale_llt = 0;
         int *elim_llt = nullptr, *elim_llt_blk = nullptr, *scale_llt = nullptr, *scale_llt_blk = nullptr;
         int x_smem_elim = 0, x_smem_scale = 0, x_smem_ortho = 0;
+        int2 *elim_tv = nullptr, *scale_tv = nullptr;  // (item, row tile) of the triangular products
+        int n_elim_tv = 0, n_scale_tv = 0;
         int n_gf = 0, n_gb = 0;
         DGroup *gf = nullptr, *gb = nullptr;
         DTile *gf_tiles = nullptr, *gb_tiles = nullptr;
@@ -1861,7 +1934,8 @@ class DeviceFactor : public DeviceFactorBase {
         if (nrhs <= x_nrhs_) return;
         if (xs_) cudaFree(xs_);
         xs_ = nullptr;
-        SPAND_CUDA(cudaMalloc(&xs_, (size_t)xld_ * nrhs * sizeof(T)));
+        // solve vectors and their scratch copy (second half)
+        SPAND_CUDA(cudaMalloc(&xs_, 2 * (size_t)xld_ * nrhs * sizeof(T)));
         x_nrhs_ = nrhs;
     }
     int smem_for(const std::vector<int>& clusters, const Plan& P) {
@@ -1872,9 +1946,9 @@ class DeviceFactor : public DeviceFactorBase {
     int xsmem_for(const std::vector<int>& clusters, const Plan& P) {
         int mx = 1;
         for (int c0 : clusters) mx = std::max(mx, P.c_cap[c0]);
-        if ((int64_t)mx * (int64_t)sizeof(T) > 200 * 1024)
-            throw DeviceError{SPAND_ERR_UNSUPPORTED, "cluster too large for the solve kernels"};
-        return mx * (int)sizeof(T);
+        const int64_t b = ((int64_t)mx + (TV_THREADS / 32) * 2 * TV_ROWS) * (int64_t)sizeof(T);
+        if (b > 200 * 1024) throw DeviceError{SPAND_ERR_UNSUPPORTED, "cluster too large for the solve kernels"};
+        return (int)b;
     }
     void build_trsm(const std::vector<TrsmItem>& items, const std::vector<int>& pivots, const std::vector<int>& clusters,
                     const Plan& P, TrsmDev& side0, TrsmDev& side1) {
@@ -2043,9 +2117,10 @@ class DeviceFactor : public DeviceFactorBase {
         return trsm_smem_n(mx);
     }
 
-    void run_solve(double* x, int nrhs, int ld) { run_solve_slots(x, nrhs, ld, xs_); }
+    void run_solve(double* x, int nrhs, int ld) { run_solve_slots(x, nrhs, ld, xs_, xs_ + (size_t)xld_ * x_nrhs_); }
 
-    void run_solve_slots(double* x, int nrhs, int ld, T* slots) {
+    // slots: the solve vectors (xld x nrhs); tmp: their scratch copy, same layout
+    void run_solve_slots(double* x, int nrhs, int ld, T* slots, T* tmp) {
         const Plan& P = *P_;
         XCtx<T> X{slots, (long long)xld_, d_xoff_, nrhs};
         const int n = (int)perm_h_.size();
@@ -2056,20 +2131,20 @@ class DeviceFactor : public DeviceFactorBase {
         for (int l = 0; l < P.nlevels; l++) {
             LevelDev& D = levels_[l];
             cur_level_ = l;
-            if (D.n_elim_llt)
+            if (D.n_elim_tv)
                 launch("trsv", [&] {
-                    trsv3_kernel<T><<<D.n_elim_llt * nrhs, 512, D.x_smem_elim, s_>>>(ctx_, X, D.elim_llt,
-                                                                                    D.elim_llt_blk, D.n_elim_llt, 0);
+                    trsv4_kernel<T><<<D.n_elim_tv, TV_THREADS, D.x_smem_elim, s_>>>(ctx_, X, D.elim_llt, D.elim_llt_blk,
+                                                                                   D.elim_tv, 0, tmp, tv_count_);
                 });
             if (D.n_gf)
                 launch("gemm_fwd", [&] {
                     gemm_fwd2_kernel<T><<<D.n_gf_tiles * nrhs, 256, 0, s_>>>(ctx_, X, D.gf, D.gfo, D.gf_tiles,
                                                                              D.n_gf_tiles, 0);
                 });
-            if (D.n_scale_llt)
+            if (D.n_scale_tv)
                 launch("trsv", [&] {
-                    trsv3_kernel<T><<<D.n_scale_llt * nrhs, 512, D.x_smem_scale, s_>>>(ctx_, X, D.scale_llt,
-                                                                                      D.scale_llt_blk, D.n_scale_llt, 0);
+                    trsv4_kernel<T><<<D.n_scale_tv, TV_THREADS, D.x_smem_scale, s_>>>(
+                        ctx_, X, D.scale_llt, D.scale_llt_blk, D.scale_tv, 0, tmp, tv_count_);
                 });
             if (D.n_ortho)
                 launch("ortho", [&] {
@@ -2095,20 +2170,20 @@ class DeviceFactor : public DeviceFactorBase {
                     ortho_wyb_kernel<T><<<D.n_ortho * nrhs, 512, D.x_smem_ortho, s_>>>(ctx_, X, D.ortho, D.n_ortho,
                                                                                           vstore_, tstore_, 0);
                 });
-            if (D.n_scale_llt)
+            if (D.n_scale_tv)
                 launch("trsv", [&] {
-                    trsv3_kernel<T><<<D.n_scale_llt * nrhs, 512, D.x_smem_scale, s_>>>(ctx_, X, D.scale_llt,
-                                                                                      D.scale_llt_blk, D.n_scale_llt, 1);
+                    trsv4_kernel<T><<<D.n_scale_tv, TV_THREADS, D.x_smem_scale, s_>>>(
+                        ctx_, X, D.scale_llt, D.scale_llt_blk, D.scale_tv, 1, tmp, tv_count_);
                 });
             if (D.n_gb)
                 launch("gemm_bwd", [&] {
                     gemm_bwd2_kernel<T><<<D.n_gb_tiles * nrhs, 256, 0, s_>>>(ctx_, X, D.gb, D.gbo, D.gb_tiles,
                                                                              D.n_gb_tiles);
                 });
-            if (D.n_elim_llt)
+            if (D.n_elim_tv)
                 launch("trsv", [&] {
-                    trsv3_kernel<T><<<D.n_elim_llt * nrhs, 512, D.x_smem_elim, s_>>>(ctx_, X, D.elim_llt,
-                                                                                    D.elim_llt_blk, D.n_elim_llt, 1);
+                    trsv4_kernel<T><<<D.n_elim_tv, TV_THREADS, D.x_smem_elim, s_>>>(ctx_, X, D.elim_llt, D.elim_llt_blk,
+                                                                                   D.elim_tv, 1, tmp, tv_count_);
                 });
         }
         cur_level_ = -1;
@@ -2137,6 +2212,7 @@ class DeviceFactor : public DeviceFactorBase {
     T* tstore_ = nullptr;
     T *vstore_ = nullptr, *taustore_ = nullptr, *tauws_ = nullptr, *ws_ = nullptr, *norms_ = nullptr;
     int *jpvt_ = nullptr, *ipvt_ = nullptr, *colcount_ = nullptr, *fallback_ = nullptr;
+    int* tv_count_ = nullptr;  // finished row tiles per cluster (triangular products)
     bool tuned_ = false;
     int cur_level_ = -1;
     // in-kernel phase timing of the QRCP of one level (SPAND_QC_PROBE=<level>)
