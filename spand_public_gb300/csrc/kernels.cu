@@ -129,11 +129,11 @@ __device__ bool chol_blocked(T* A, int ld, int n, int* bad) {
 template <typename T>
 __global__ void __launch_bounds__(256) potrf3_kernel(Ctx<T> c, const int* __restrict__ pivots,
                                                      const int* __restrict__ clusters, int count, int smem_elems,
-                                                     int strip_max_n) {
+                                                     int strip_max_n, const int* __restrict__ only) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
     const int item = blockIdx.x;
-    if (item >= count) return;
+    if (item >= count || (only && !only[item])) return;
     __shared__ int failed;
     __shared__ int bad;
     if (threadIdx.x == 0) {
@@ -163,6 +163,183 @@ __global__ void __launch_bounds__(256) potrf3_kernel(Ctx<T> c, const int* __rest
     // pivots too large for the strip-wise inverse kernel get their inverse here
     if (!bad && n > strip_max_n) trtri_to_upper(G, gld, n);
     if (bad && threadIdx.x == 0) atomicCAS(&c.status->not_spd, 0, cl + 1);
+}
+
+// Cholesky factorization of pivot blocks too large for one CTA's shared memory, in the
+// shared memory of a thread-block cluster of CS CTAs (LLT pivots, src/tree.cpp:587-590).
+// The lower triangle is cut into 32-column panels; panel p (rows [32p, n)) lives in CTA
+// p mod CS.  Per panel: the owner factors the 32x32 diagonal block (one warp, as in
+// chol_blocked) and solves the rows below against it; one cluster barrier; every CTA
+// copies the panel's trailing rows through distributed shared memory and applies them to
+// its own later panels (4x4 register tiles).  A non-SPD diagonal stops every CTA after
+// the barrier.  Pivots whose panels exceed smem_bytes set fallback[item] (the
+// single-CTA kernel then factors them from global memory).
+constexpr int PC_THREADS = 256;
+
+// shared memory of CTA r: its panels of an n x n pivot plus one staged panel
+__host__ __device__ inline long long pc_need(int n, int cs, int r, int elem) {
+    long long e = 0;
+    const int np = (n + 31) / 32;
+    for (int p = r; p < np; p += cs) e += (long long)(n - 32 * p) * 32;
+    return (e + (long long)n * 32) * elem;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(PC_THREADS) potrf_cluster_kernel(Ctx<T> c, const int* __restrict__ pivots,
+                                                                   const int* __restrict__ clusters, int count,
+                                                                   int smem_bytes, int* fallback) {
+    namespace cgx = cooperative_groups;
+    cgx::cluster_group cl = cgx::this_cluster();
+    const int CS = (int)cl.num_blocks(), me = (int)cl.block_rank();
+    const int item = blockIdx.x / CS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sm = reinterpret_cast<T*>(smem_raw);
+    __shared__ int bad;
+    // all CTAs of a cluster hold the same pivot, so these exits are uniform over it
+    if (item >= count) return;
+    const int cid = clusters[item];
+    const int n = c.csize[cid];
+    const bool fits = pc_need(n, CS, 0, (int)sizeof(T)) <= smem_bytes;
+    if (me == 0 && threadIdx.x == 0) fallback[item] = (n > 0 && !fits) ? 1 : 0;
+    if (n == 0 || !fits) return;
+    T* G = bptr(c, pivots[item]);
+    const int gld = c.blk[pivots[item]].ld;
+    const int tid = threadIdx.x;
+    const int np = (n + 31) / 32;
+    // offset of panel p (owned by CTA r = p mod CS) in its owner's shared memory
+    auto poff = [&](int p) -> long long {
+        long long e = 0;
+        for (int q = p % CS; q < p; q += CS) e += (long long)(n - 32 * q) * 32;
+        return e;
+    };
+    long long own = 0;
+    for (int p = me; p < np; p += CS) {
+        T* P = sm + own;
+        const int r0 = 32 * p, ldp = n - r0, w = min(32, n - r0);
+        for (int idx = tid; idx < ldp * w; idx += PC_THREADS) {
+            const int t = idx % ldp, j = idx / ldp;
+            if (t >= j) P[t + (size_t)j * ldp] = G[(r0 + t) + (size_t)(r0 + j) * gld];
+        }
+        own += (long long)ldp * 32;
+    }
+    T* S = sm + own;  // staged trailing rows of the current panel
+    if (tid == 0) bad = 0;
+    __syncthreads();
+    bool failed = false;
+    for (int p = 0; p < np; p++) {
+        const int owner = p % CS;
+        const int r0 = 32 * p, ldp = n - r0, w = min(32, n - r0);
+        if (owner == me) {
+            T* P = sm + poff(p);
+            if (tid < 32) {
+                int fail = 0;
+                for (int j = 0; j < w; j++) {
+                    T* cj = P + (size_t)j * ldp;
+                    T d = 0;
+                    if (tid == j) {
+                        d = cj[j];
+                        if (!(d > T(0))) {
+                            fail = 1;
+                            d = T(1);
+                        } else {
+                            d = dsqrt(d);
+                        }
+                        cj[j] = d;
+                    }
+                    d = __shfl_sync(0xffffffffu, d, j);
+                    fail = __shfl_sync(0xffffffffu, fail, j);
+                    if (fail) break;
+                    if (tid > j && tid < w) cj[tid] /= d;
+                    __syncwarp();
+                    if (tid > j && tid < w) {
+                        const T lij = cj[tid];
+                        for (int kk = j + 1; kk <= tid; kk++) P[tid + (size_t)kk * ldp] -= lij * cj[kk];
+                    }
+                    __syncwarp();
+                }
+                if (tid == 0 && fail) bad = 1;
+            }
+            __syncthreads();
+            if (!bad)
+                for (int t = w + tid; t < ldp; t += PC_THREADS)
+                    for (int j = 0; j < w; j++) {
+                        T x = P[t + (size_t)j * ldp];
+                        for (int l = 0; l < j; l++) x -= P[t + (size_t)l * ldp] * P[j + (size_t)l * ldp];
+                        P[t + (size_t)j * ldp] = x / P[j + (size_t)j * ldp];
+                    }
+            __syncthreads();
+        }
+        cl.sync();
+        if (*cl.map_shared_rank(&bad, owner)) {
+            failed = true;
+            break;
+        }
+        const int rs = r0 + w;  // first trailing row
+        if (rs >= n) continue;
+        const int ls = n - rs;
+        const T* Pp = cl.map_shared_rank(sm, owner) + poff(p);
+        for (int idx = tid; idx < ls * w; idx += PC_THREADS) {
+            const int t = idx % ls, k = idx / ls;
+            S[t + (size_t)k * ls] = Pp[(rs - r0 + t) + (size_t)k * ldp];
+        }
+        __syncthreads();
+        const int rg = tid >> 3, cg = tid & 7;
+        for (int q = p + 1 + ((me - (p + 1)) % CS + CS) % CS; q < np; q += CS) {
+            T* Q = sm + poff(q);
+            const int q0 = 32 * q, ldq = n - q0, wq = min(32, n - q0);
+            for (int rb = 0; rb < ldq; rb += 128) {
+                T acc[4][4];
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int v = 0; v < 4; v++) acc[u][v] = T(0);
+                for (int k = 0; k < w; k++) {
+                    const T* sk = S + (size_t)k * ls;
+                    T a[4], b[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int i = q0 + rb + rg + 32 * u;
+                        a[u] = i < n ? sk[i - rs] : T(0);
+                    }
+#pragma unroll
+                    for (int v = 0; v < 4; v++) {
+                        const int jj = 4 * cg + v;
+                        b[v] = jj < wq ? sk[q0 + jj - rs] : T(0);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; u++)
+#pragma unroll
+                        for (int v = 0; v < 4; v++) acc[u][v] += a[u] * b[v];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int t = rb + rg + 32 * u;
+#pragma unroll
+                    for (int v = 0; v < 4; v++) {
+                        const int jj = 4 * cg + v;
+                        if (t < ldq && jj < wq && t >= jj) Q[t + (size_t)jj * ldq] -= acc[u][v];
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    // no CTA leaves while another may still read its panels
+    cl.sync();
+    if (failed) {
+        if (me == 0 && tid == 0) atomicCAS(&c.status->not_spd, 0, cid + 1);
+        return;
+    }
+    long long off = 0;
+    for (int p = me; p < np; p += CS) {
+        const T* P = sm + off;
+        const int r0 = 32 * p, ldp = n - r0, w = min(32, n - r0);
+        for (int idx = tid; idx < ldp * w; idx += PC_THREADS) {
+            const int t = idx % ldp, j = idx / ldp;
+            if (t >= j) G[(r0 + t) + (size_t)(r0 + j) * gld] = P[t + (size_t)j * ldp];
+        }
+        off += (long long)ldp * 32;
+    }
 }
 
 // ------------------------------------------------------------------------------------
@@ -1567,6 +1744,12 @@ class DeviceFactor : public DeviceFactorBase {
         fallback_ = alloc<int>(max_items);
         SPAND_CUDA(cudaFuncSetAttribute(trsv4_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         tv_count_ = alloc<int>(nc_);
+        {
+            int mx = 1;
+            for (const LevelPlan& L : P.levels)
+                mx = std::max(mx, (int)std::max(L.elim_clusters.size(), L.scale_clusters.size()));
+            pc_fallback_ = alloc<int>(mx);
+        }
         SPAND_CUDA(cudaMemsetAsync(tv_count_, 0, (size_t)std::max(nc_, 1) * sizeof(int), s_));
         SPAND_CUDA(cudaFuncSetAttribute(sparsify_wy_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         larft_smem_elems() * (int)sizeof(T)));
@@ -1608,7 +1791,8 @@ class DeviceFactor : public DeviceFactorBase {
             LevelDev& D = levels_[l];
             cur_level_ = l;
             if (D.n_elim) {
-                launch_potrf(D.elim_pivots, D.elim_clusters, D.n_elim, D.elim_smem, D.elim_tri);
+                launch_potrf(D.elim_pivots, D.elim_clusters, D.n_elim, D.elim_smem, D.elim_tri, D.elim_pc_cs,
+                             D.elim_pc_smem);
                 launch_trsm(D.elim_trsm0);
                 launch_trsm(D.elim_trsm1);
                 if (D.n_schur_tiles)
@@ -1618,7 +1802,8 @@ class DeviceFactor : public DeviceFactorBase {
                     });
             }
             if (D.scaled && D.n_scale) {
-                launch_potrf(D.scale_pivots, D.scale_clusters, D.n_scale, D.scale_smem, D.scale_tri);
+                launch_potrf(D.scale_pivots, D.scale_clusters, D.n_scale, D.scale_smem, D.scale_tri,
+                             D.scale_pc_cs, D.scale_pc_smem);
                 launch_trsm(D.scale_trsm0);
                 launch_trsm(D.scale_trsm1);
             }
@@ -1729,6 +1914,8 @@ class DeviceFactor : public DeviceFactorBase {
             int ne = nmax(L.elim_clusters), ns = nmax(L.scale_clusters);
             D.elim_smem = potrf_smem_n(ne);
             D.scale_smem = potrf_smem_n(ns);
+            choose_potrf_cluster(ne, D.elim_smem, D.n_elim, D.elim_pc_cs, D.elim_pc_smem);
+            choose_potrf_cluster(ns, D.scale_smem, D.n_scale, D.scale_pc_cs, D.scale_pc_smem);
             D.elim_tri.smem = trtri_smem_n(ne);
             D.scale_tri.smem = trtri_smem_n(ns);
             D.elim_trsm0.smem = D.elim_trsm1.smem = trsm_smem_n(ne);
@@ -1870,6 +2057,7 @@ class DeviceFactor : public DeviceFactorBase {
         int* elim_clusters = nullptr;
         int* elim_pivots = nullptr;
         int elim_smem = 0;
+        int elim_pc_cs = 0, elim_pc_smem = 0;   // cluster Cholesky (0: single-CTA kernel)
         TrsmDev elim_trsm0, elim_trsm1;
         TrtriDev elim_tri, scale_tri;
         DTarget* schur_targets = nullptr;
@@ -1880,6 +2068,7 @@ class DeviceFactor : public DeviceFactorBase {
         int* scale_clusters = nullptr;
         int* scale_pivots = nullptr;
         int scale_smem = 0;
+        int scale_pc_cs = 0, scale_pc_smem = 0;
         TrsmDev scale_trsm0, scale_trsm1;
         int n_level = 0;
         int* level_clusters = nullptr;
@@ -1986,6 +2175,11 @@ class DeviceFactor : public DeviceFactorBase {
         SPAND_CUDA(cudaFuncGetAttributes(&fa, fn));
         qc_smem_cap_ = (int)(optin - (int)fa.sharedSizeBytes) & ~255;
         SPAND_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, qc_smem_cap_));
+        SPAND_CUDA(cudaFuncSetAttribute(potrf_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        qc_smem_cap_));
+        if (cudaFuncSetAttribute(potrf_cluster_kernel<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+            cudaSuccess)
+            cudaGetLastError();
         qc_max_cs_ = 8;
         if (cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
             if (active_clusters(16, 16, qc_smem_cap_) > 0) qc_max_cs_ = 16;
@@ -2071,10 +2265,30 @@ class DeviceFactor : public DeviceFactorBase {
                                       (const DAsn*)pieces_, ws_, jpvt_, ipvt_, tauws_, rank_, colcount_, fallback_, tol,
                                       W.smem, probe));
     }
-    void launch_potrf(int* pivots, int* clusters, int n, int smem, const TrtriDev& tri) {
+    void launch_potrf(int* pivots, int* clusters, int n, int smem, const TrtriDev& tri, int pc_cs, int pc_smem) {
+        if (pc_cs > 0) {
+            launch("potrf", [&] {
+                cudaLaunchConfig_t cfg = {};
+                cfg.gridDim = dim3((unsigned)(n * pc_cs));
+                cfg.blockDim = dim3(PC_THREADS);
+                cfg.dynamicSmemBytes = (size_t)pc_smem;
+                cfg.stream = s_;
+                cudaLaunchAttribute attr[1];
+                attr[0].id = cudaLaunchAttributeClusterDimension;
+                attr[0].val.clusterDim.x = (unsigned)pc_cs;
+                attr[0].val.clusterDim.y = 1;
+                attr[0].val.clusterDim.z = 1;
+                cfg.attrs = attr;
+                cfg.numAttrs = 1;
+                SPAND_CUDA(cudaLaunchKernelEx(&cfg, potrf_cluster_kernel<T>, ctx_, (const int*)pivots,
+                                              (const int*)clusters, n, pc_smem, pc_fallback_));
+            });
+        }
+        // single-CTA kernel: every pivot, or (after the cluster kernel) those it could not hold
         launch("potrf", [&] {
             potrf3_kernel<T><<<n, 256, smem, s_>>>(ctx_, pivots, clusters, n, smem / (int)sizeof(T),
-                                                   tri.smem / (32 * (int)sizeof(T)));
+                                                   tri.smem / (32 * (int)sizeof(T)),
+                                                   pc_cs > 0 ? (const int*)pc_fallback_ : nullptr);
         });
         if (tri.ntiles)
             launch("trtri", [&] {
@@ -2087,6 +2301,38 @@ class DeviceFactor : public DeviceFactorBase {
         launch("trsm", [&] {
             trsm3_kernel<T><<<t.ntiles, 256, t.smem, s_>>>(ctx_, t.items, t.tiles, t.ntiles, t.smem / (int)sizeof(T));
         });
+    }
+    // Cluster Cholesky for pivots of up to nmax rows that one CTA's shared memory cannot
+    // hold: the smallest cluster whose CTAs hold their panels (cs = 0: keep the single-CTA
+    // kernel)
+    void choose_potrf_cluster(int nmax, int single_smem, int count, int& cs_out, int& smem_out) {
+        cs_out = 0;
+        smem_out = 0;
+        if (single_smem > 0 || count == 0) return;
+        for (int cs = 2; cs <= qc_max_cs_; cs *= 2) {
+            const long long need = (pc_need(nmax, cs, 0, (int)sizeof(T)) + 255) & ~255LL;
+            if (need > qc_smem_cap_) continue;
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3((unsigned)(count * cs));
+            cfg.blockDim = dim3(PC_THREADS);
+            cfg.dynamicSmemBytes = (size_t)need;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = (unsigned)cs;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            int active = 0;
+            if (cudaOccupancyMaxActiveClusters(&active, potrf_cluster_kernel<T>, &cfg) != cudaSuccess) {
+                cudaGetLastError();
+                continue;
+            }
+            if (active <= 0) continue;
+            cs_out = cs;
+            smem_out = (int)need;
+            return;
+        }
     }
     // shared memory of the POTRF kernel for pivots of size up to nmax: whole block, else one panel
     static int potrf_smem_n(int nmax) {
@@ -2213,6 +2459,7 @@ class DeviceFactor : public DeviceFactorBase {
     T *vstore_ = nullptr, *taustore_ = nullptr, *tauws_ = nullptr, *ws_ = nullptr, *norms_ = nullptr;
     int *jpvt_ = nullptr, *ipvt_ = nullptr, *colcount_ = nullptr, *fallback_ = nullptr;
     int* tv_count_ = nullptr;  // finished row tiles per cluster (triangular products)
+    int* pc_fallback_ = nullptr;  // pivots the cluster Cholesky could not hold
     bool tuned_ = false;
     int cur_level_ = -1;
     // in-kernel phase timing of the QRCP of one level (SPAND_QC_PROBE=<level>)

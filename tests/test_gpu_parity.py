@@ -15,7 +15,7 @@ TOL_BLOCK = 1e-12   # relative Frobenius error per factor block, FP64 path
 TOL_SOLVE = 1e-12   # relative error of M^{-1} b, FP64 path
 
 
-def _build(n, dim, nlevels, tol, skip=0, fp32=False, A=None):
+def _build(n, dim, nlevels, tol, skip=0, fp32=False, A=None, factorizations=1):
     import spand_public_gb300 as pkg
     from oracle.oracle import OracleTree
     from spand_public_gb300 import problems as P
@@ -31,7 +31,8 @@ def _build(n, dim, nlevels, tol, skip=0, fp32=False, A=None):
     t.set_fp32(fp32)
     pt = t.partition(A)
     t.assemble(A)
-    t.factorize()
+    for _ in range(factorizations):
+        t.factorize()
     o = OracleTree(nlevels)
     o.set_Xcoo(X)
     o.set_tol(tol)
@@ -56,9 +57,15 @@ CASES = [
 ]
 
 
-@pytest.mark.parametrize("n,dim,nlevels,tol,skip", CASES)
-def test_factor_parity_fp64(n, dim, nlevels, tol, skip):
-    A, t, o = _build(n, dim, nlevels, tol, skip)
+# (n, dim, levels, tol, skip, factorizations): the second factorization of a tree runs
+# with the launch configuration tuned from the first one's sizes (for 3D 32^3 the
+# largest pivots, 224-256 rows, take the thread-block-cluster Cholesky)
+CASES_F = [c + (1,) for c in CASES] + [(32, 3, 8, 1e-2, 0, 2)]
+
+
+@pytest.mark.parametrize("n,dim,nlevels,tol,skip,nf", CASES_F)
+def test_factor_parity_fp64(n, dim, nlevels, tol, skip, nf):
+    A, t, o = _build(n, dim, nlevels, tol, skip, factorizations=nf)
     assert np.array_equal(t.get_assembly_perm(), o.get_assembly_perm())
     # ranks
     rt, ro = t.ranks(), o.ranks()
@@ -112,12 +119,13 @@ def test_pcg_iterations_match(n, dim, nlevels, tol):
     assert np.linalg.norm(xt - xo) / np.linalg.norm(xo) < 1e-9
 
 
-@pytest.mark.parametrize("n,dim,nlevels,tol", [(64, 2, 7, 1e-2), (16, 3, 6, 1e-2), (24, 3, 7, 1e-3)])
-def test_mixed_precision_pcg(n, dim, nlevels, tol):
+@pytest.mark.parametrize("n,dim,nlevels,tol,nf", [(64, 2, 7, 1e-2, 1), (16, 3, 6, 1e-2, 1), (24, 3, 7, 1e-3, 1),
+                                                   (32, 3, 8, 1e-2, 2)])
+def test_mixed_precision_pcg(n, dim, nlevels, tol, nf):
     """FP32 factor + FP64 PCG reaches 1e-10 with <= 15% more iterations than FP64."""
     from spand_public_gb300 import problems as P
-    A, t64, o = _build(n, dim, nlevels, tol)
-    _, t32, _ = _build(n, dim, nlevels, tol, fp32=True)
+    A, t64, o = _build(n, dim, nlevels, tol, factorizations=nf)
+    _, t32, _ = _build(n, dim, nlevels, tol, fp32=True, factorizations=nf)
     b = P.rhs(A.shape[0], 1, seed=5)[:, 0]
     x64, it64, _ = t64.cg(b, iters=200, tol=1e-10)
     x32, it32, _ = t32.cg(b, iters=200, tol=1e-10)
