@@ -52,11 +52,11 @@ __device__ void trtri_to_upper(T* A, int ld, int n) {
 }
 
 // ------------------------------------------------------------------------------------
-// Cholesky of pivot blocks, blocked left-looking with 32-column panels (dpotrf 'L',
-// tree.cpp:582-593).  One block per pivot; the block is staged in shared memory when it
-// fits, else factored in place in global memory.  Per panel: (1) update by the factored
-// columns, (2) the 32x32 diagonal block by one warp with shuffles, (3) the rows below by
-// a triangular solve, one row per thread.  Three barriers per panel.
+// Cholesky of pivot blocks in place in global memory, blocked left-looking with 32-column
+// panels (dpotrf 'L', tree.cpp:582-593): the path of pivots too large for shared memory.
+// Per panel: (1) update by the factored columns, (2) the 32x32 diagonal block by one warp
+// with shuffles, (3) the rows below by a triangular solve, one row per thread.  Three
+// barriers per panel.  (Pivots that fit are factored and inverted by chol_inv_smem.)
 // ------------------------------------------------------------------------------------
 constexpr int PNB = 32;
 
@@ -126,6 +126,136 @@ __device__ bool chol_blocked(T* A, int ld, int n, int* bad) {
     return true;
 }
 
+// Cholesky and inverse of a pivot block held in shared memory (ld = n, lower triangle
+// in, L in the lower triangle and L^{-1} transposed in the strictly upper triangle out;
+// the diagonal of L^{-1}, 1 / L_ii, is not stored).  32-column panels: (1) update of the
+// panel by the factored columns (left-looking), (2) the 32x32 diagonal block by one warp
+// with shuffles, then its inverse D by forward substitution (lane = column, in
+// registers), (3) rows below: row x D^T, a warp per row.  Then L^{-1} block row by block row:
+// L^{-1}[I][J] = -D_I sum_{J <= K < I} L[I][K] L^{-1}[K][J], the sum written into the
+// block's upper-triangle slots first and multiplied by D_I per column.  256 threads.
+template <typename T>
+__device__ bool chol_inv_smem(T* A, int n, int* bad) {
+    __shared__ T Dpad[PNB * (PNB + 1)];  // inverse of the current diagonal block, padded rows
+    const int tid = threadIdx.x, lane = tid & 31, w8 = tid >> 5;
+    constexpr int NWARP = 8;
+    const int nb = (n + PNB - 1) / PNB;
+    for (int pb = 0; pb < nb; pb++) {
+        const int jb = pb * PNB, w = min(PNB, n - jb);
+        // (1) left-looking update of the panel
+        if (jb > 0) {
+            for (int jj = w8; jj < w; jj += NWARP) {
+                const int j = jb + jj;
+                for (int i = j + lane; i < n; i += 32) {
+                    T s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+                    int k = 0;
+                    for (; k + 3 < jb; k += 4) {
+                        s0 += A[i + k * n] * A[j + k * n];
+                        s1 += A[i + (k + 1) * n] * A[j + (k + 1) * n];
+                        s2 += A[i + (k + 2) * n] * A[j + (k + 2) * n];
+                        s3 += A[i + (k + 3) * n] * A[j + (k + 3) * n];
+                    }
+                    for (; k < jb; k++) s0 += A[i + k * n] * A[j + k * n];
+                    A[i + j * n] -= (s0 + s1) + (s2 + s3);
+                }
+            }
+            __syncthreads();
+        }
+        // (2) diagonal block and its inverse (upper-triangle slots of the block)
+        if (tid < 32) {
+            int fail = 0;
+            for (int j = 0; j < w; j++) {
+                T* cj = A + (jb + j) * n + jb;
+                T d = 0;
+                if (lane == j) {
+                    d = cj[j];
+                    if (!(d > T(0))) {
+                        fail = 1;
+                        d = T(1);
+                    } else {
+                        d = dsqrt(d);
+                    }
+                    cj[j] = d;
+                }
+                d = __shfl_sync(0xffffffffu, d, j);
+                fail = __shfl_sync(0xffffffffu, fail, j);
+                if (fail) break;
+                if (lane > j && lane < w) cj[lane] /= d;
+                __syncwarp();
+                if (lane > j && lane < w) {
+                    const T lij = cj[lane];
+                    for (int kk = j + 1; kk <= lane; kk++) A[(jb + lane) + (jb + kk) * n] -= lij * cj[kk];
+                }
+                __syncwarp();
+            }
+            if (lane == 0 && fail) *bad = 1;
+            if (!fail) {
+                // column c = lane of D = L_pp^{-1} in registers (forward substitution on e_c,
+                // L read by broadcast): D[r][c] = (delta_rc - sum_{l<r} L[r][l] D[l][c]) / L[r][r]
+                T d[PNB];
+#pragma unroll
+                for (int r = 0; r < PNB; r++) {
+                    d[r] = T(0);
+                    if (r < w) {
+                        T acc = r == lane ? T(1) : T(0);
+#pragma unroll
+                        for (int l = 0; l < r; l++) acc -= A[(jb + r) + (jb + l) * n] * d[l];
+                        d[r] = acc / A[(jb + r) + (jb + r) * n];
+                    }
+                }
+                // D transposed into the block's upper slots (A[(jb+c) + (jb+r)*n] = D[r][c],
+                // r > c) and row-major into Dpad for the rows below
+#pragma unroll
+                for (int r = 0; r < PNB; r++) {
+                    if (r < w && r > lane) A[(jb + lane) + (jb + r) * n] = d[r];
+                    Dpad[r * (PNB + 1) + lane] = d[r];
+                }
+            }
+        }
+        __syncthreads();
+        if (*bad) return false;
+        // (3) rows below: L[i][jb+j] = sum_{l <= j} A[i][jb+l] D[j][l]
+        for (int i = jb + w + w8; i < n; i += NWARP) {
+            T out = 0;
+            if (lane < w)
+                for (int l = 0; l <= lane; l++) out += A[i + (jb + l) * n] * Dpad[lane * (PNB + 1) + l];
+            __syncwarp();
+            if (lane < w) A[i + (jb + lane) * n] = out;
+        }
+        __syncthreads();
+    }
+    // off-diagonal blocks of L^{-1}, block row by block row
+    for (int ib = 1; ib < nb; ib++) {
+        const int i0 = ib * PNB, h = min(PNB, n - i0);
+        // E[i][j] = sum_{j <= m < i0} L[i][m] Linv[m][j] for rows i in the block, j < i0
+        for (int idx = tid; idx < h * i0; idx += blockDim.x) {
+            const int ii = idx % h, j = idx / h;
+            const int i = i0 + ii;
+            T sum = A[i + j * n] / A[j + j * n];  // m = j: Linv[j][j] = 1 / L[j][j]
+            for (int m = j + 1; m < i0; m++) sum += A[i + m * n] * A[j + m * n];
+            A[j + i * n] = sum;
+        }
+        __syncthreads();
+        // Linv[i][j] = -sum_{l <= i} D[i][l] E[l][j] (block rows, D = diagonal block inverse)
+        for (int j = tid; j < i0; j += blockDim.x) {
+            T e[PNB];
+#pragma unroll
+            for (int l = 0; l < PNB; l++) e[l] = l < h ? A[j + (i0 + l) * n] : T(0);
+#pragma unroll
+            for (int ii = PNB - 1; ii >= 0; ii--) {
+                if (ii < h) {
+                    T sum = e[ii] / A[(i0 + ii) + (i0 + ii) * n];
+#pragma unroll
+                    for (int l = 0; l < ii; l++) sum += A[(i0 + l) + (i0 + ii) * n] * e[l];
+                    A[j + (i0 + ii) * n] = -sum;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    return true;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) potrf3_kernel(Ctx<T> c, const int* __restrict__ pivots,
                                                      const int* __restrict__ clusters, int count, int smem_elems,
@@ -152,16 +282,17 @@ __global__ void __launch_bounds__(256) potrf3_kernel(Ctx<T> c, const int* __rest
         for (int j = ty; j < n; j += nty)
             for (int i = j + tx; i < n; i += 32) sm[i + j * n] = G[i + (size_t)j * gld];
         __syncthreads();
-        if (chol_blocked(sm, n, n, &bad)) {
+        // factor and inverse together; the whole block (L below, L^{-1} transposed above) back
+        if (chol_inv_smem(sm, n, &bad)) {
             for (int j = ty; j < n; j += nty)
-                for (int i = j + tx; i < n; i += 32) G[i + (size_t)j * gld] = sm[i + j * n];
+                for (int i = tx; i < n; i += 32) G[i + (size_t)j * gld] = sm[i + j * n];
         }
     } else {
         chol_blocked(G, gld, n, &bad);
+        __syncthreads();
+        // pivots the strip-wise inverse kernel does not take get their inverse here
+        if (!bad && n > strip_max_n) trtri_to_upper(G, gld, n);
     }
-    __syncthreads();
-    // pivots too large for the strip-wise inverse kernel get their inverse here
-    if (!bad && n > strip_max_n) trtri_to_upper(G, gld, n);
     if (bad && threadIdx.x == 0) atomicCAS(&c.status->not_spd, 0, cl + 1);
 }
 
@@ -352,7 +483,7 @@ __global__ void __launch_bounds__(PC_THREADS) potrf_cluster_kernel(Ctx<T> c, con
 template <typename T>
 __global__ void __launch_bounds__(256) trtri_kernel(Ctx<T> c, const int* __restrict__ pivots,
                                                     const int* __restrict__ clusters, const DTile* __restrict__ tiles,
-                                                    int ntiles, int smem_elems) {
+                                                    int ntiles, int smem_elems, long long skip_n2) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* Y = reinterpret_cast<T*>(smem_raw);  // Y[i + jj * n], rows i >= jb
     const int t = blockIdx.x;
@@ -361,7 +492,9 @@ __global__ void __launch_bounds__(256) trtri_kernel(Ctx<T> c, const int* __restr
     const int cl = clusters[item];
     const int n = c.csize[cl];
     const int jb = tiles[t].tile_i * 32;
-    if (jb >= n || (long long)n * 32 > smem_elems) return;  // large pivots: inverted by potrf3_kernel
+    // pivots inverted by potrf3_kernel: those it held in shared memory (n^2 <= skip_n2) and
+    // the large ones
+    if (jb >= n || (long long)n * n <= skip_n2 || (long long)n * 32 > smem_elems) return;
     const int w = min(32, n - jb);
     T* A = bptr(c, pivots[item]);
     const int ld = c.blk[pivots[item]].ld;
@@ -2210,11 +2343,13 @@ class DeviceFactor : public DeviceFactorBase {
     // Cluster size and shared memory of a wave's QRCP launch.  dims: (rows, cols) bound
     // of every matrix of the wave.  Per candidate cluster size: the slab of the largest
     // matrix sets the shared memory, the occupancy query the number of co-resident
-    // clusters; the estimate is rounds x (per-step latency + shared-memory passes over the
-    // largest slab, shared by the CTAs resident on one SM) and the smallest wins.
+    // clusters; the estimate is rounds x (per-step latency + passes over the largest slab)
+    // and the smallest wins.
     void choose_cluster(WaveDev& W, const std::vector<std::pair<int, int>>& dims) {
         double best = 1e300;
         int bcs = 0, bsm = 0;
+        // SPAND_QC_CS=<cs>: that cluster size wherever the matrices fit (measurement aid)
+        const int force = getenv("SPAND_QC_CS") ? atoi(getenv("SPAND_QC_CS")) : 0;
         for (int cs = 1; cs <= qc_max_cs_; cs *= 2) {
             int64_t sm = 4096, work = 0;
             for (const auto& d : dims) {
@@ -2226,9 +2361,10 @@ class DeviceFactor : public DeviceFactorBase {
             const int active = active_clusters(W.n * cs, cs, (int)sm);
             if (active <= 0) continue;
             const int rounds = (W.n + active - 1) / active;
-            const double resident = (double)std::min(W.n, active) * cs;
-            const double share = std::max(1.0, std::ceil(resident / num_sms_));
-            const double est = rounds * (3000.0 + 500.0 * std::log2((double)cs) + 5.0 / 32.0 * (double)work * share);
+            // per pivot step: barrier latency + the passes over the largest slab (the kernel
+            // is latency-bound: CTAs sharing an SM do not slow each other down much)
+            double est = rounds * (3000.0 + 500.0 * std::log2((double)cs) + 5.0 / 32.0 * (double)work);
+            if (force > 0) est = cs == force ? 0.0 : 1e200;
             if (est < best) {
                 best = est;
                 bcs = cs;
@@ -2284,16 +2420,20 @@ class DeviceFactor : public DeviceFactorBase {
                                               (const int*)clusters, n, pc_smem, pc_fallback_));
             });
         }
+        // The strip-wise inverse runs only where pivots may miss the single-CTA kernel's shared
+        // memory (which inverts what it holds); without it potrf3 inverts every pivot itself.
+        const bool strips = tri.ntiles > 0 && (smem == 0 || pc_cs > 0);
         // single-CTA kernel: every pivot, or (after the cluster kernel) those it could not hold
         launch("potrf", [&] {
             potrf3_kernel<T><<<n, 256, smem, s_>>>(ctx_, pivots, clusters, n, smem / (int)sizeof(T),
-                                                   tri.smem / (32 * (int)sizeof(T)),
+                                                   strips ? tri.smem / (32 * (int)sizeof(T)) : 0,
                                                    pc_cs > 0 ? (const int*)pc_fallback_ : nullptr);
         });
-        if (tri.ntiles)
+        if (strips)
             launch("trtri", [&] {
                 trtri_kernel<T><<<tri.ntiles, 256, tri.smem, s_>>>(ctx_, pivots, clusters, tri.tiles, tri.ntiles,
-                                                                   tri.smem / (int)sizeof(T));
+                                                                   tri.smem / (int)sizeof(T),
+                                                                   pc_cs > 0 ? 0LL : (long long)(smem / (int)sizeof(T)));
             });
     }
     void launch_trsm(const TrsmDev& t) {
