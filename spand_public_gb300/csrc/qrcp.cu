@@ -11,21 +11,37 @@
 
 namespace spand {
 
-// QRCP, version without column movement.  The sparsification matrix stays in the shared
-// memory of a thread-block cluster (CS CTAs, column slabs); a column never moves: the
-// pivoting is tracked as a permutation (perm: position -> column, replicated in every
-// CTA; pos: column -> position for the slab's own columns).  Per pivot step i:
-//   1. every CTA reads the published (slab maximum m_q, first position f_q inside the tie
-//      window of m_q) of all slabs and derives the pivot; exact as long as no slab maximum
-//      lies inside the tie window below the global one (else one more barrier);
-//   2. every CTA reads the pivot column through distributed shared memory and builds the
-//      Householder reflector itself (identical arithmetic in every CTA);
-//   3. every CTA applies the reflector to its trailing columns (G threads per column) and
-//      downdates their norms (LAWN 176), then publishes its next (m, f) and arrives at the
-//      cluster barrier.
-// The owner writes the reflector into the pivot column one step later, once no CTA can
-// still be reading that column.  At the end the slabs are written to the global workspace
-// in LAPACK's column order (position p holds column perm[p]).
+// QRCP without column movement.  The sparsification matrix stays in the shared memory of
+// a thread-block cluster (CS CTAs, column slabs); a column never moves: the pivoting is
+// tracked as a permutation (perm: position -> column, replicated in every CTA; pos:
+// column -> position for the slab's own columns).  G threads per column.  Per pivot step i:
+//   1. every warp reads the entries published by every warp of the cluster (largest
+//      partial norm m of its columns, first position inside the tie window of m) and
+//      derives the pivot with shuffles; exact as long as no warp maximum lies inside the
+//      tie window below the global one (else every warp searches with the global
+//      threshold, one more barrier);
+//   2. the owner writes the previous reflector into its column and every CTA reads the
+//      pivot column (distributed shared memory) with the same row -> thread map, so
+//      neither needs a barrier; one barrier for the column norm, then every thread forms
+//      the Householder scalars itself;
+//   3. every CTA applies H = I - tau v v^T, v = [1; sc * x] (the unscaled column x stays
+//      in shared memory, sc is folded into the update), downdates the norms (LAWN 176),
+//      and every warp publishes its next entry into every CTA; one cluster barrier.
+// At the end the slabs are written to the global workspace in LAPACK's column order
+// (position p holds column perm[p]).
+constexpr int QC_SLOTS = 16 * (QC_THREADS / 32);  // warps of the largest cluster
+
+template <typename T>
+__device__ __forceinline__ T warp_max(T v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__device__ __forceinline__ int warp_min(int v) {
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
 __device__ __forceinline__ void qc_barrier(cooperative_groups::cluster_group& cl, int cs) {
     if (cs > 1) cl.sync();
     else __syncthreads();
@@ -44,9 +60,9 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_smem_kernel(Ctx<T> c, const D
     const int item = blockIdx.x / CS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ T red[32];
-    __shared__ int ired[32];
-    __shared__ T pubm[2][16];
-    __shared__ int pubf[2][16];
+    __shared__ T pubm[2][QC_SLOTS];  // per warp of the cluster: largest partial norm
+    __shared__ int pubf[2][QC_SLOTS];  // first position inside its tie window
+    __shared__ int pubx[2][QC_SLOTS];  // exact search with the global threshold
     __shared__ T s_alpha;
     if (c.status->not_spd) return;
     const DSpars it = items[item];
@@ -132,30 +148,24 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_smem_kernel(Ctx<T> c, const D
     const T tie = T(1) - qrcp_tie<T>();
     const T tol3z = dsqrt(sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-07));
 
-    // publish (slab max over columns at positions >= from, first position inside its tie window)
-    auto publish = [&](int par, int from) {
-        __syncthreads();
-        T m = 0;
-        for (int j = tid; j < nloc; j += nth)
-            if (pos[j] >= from) m = fmax(m, vn1[j]);
-        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (lane == 0) red[w] = m;
-        __syncthreads();
-        m = red[0];
-        for (int k = 1; k < nw; k++) m = fmax(m, red[k]);
+    const int E = CS * nw;          // published entries: every warp of every CTA
+    const int slot = me * nw + w;   // this warp's entry
+    // A warp publishes into every CTA (largest partial norm m of its columns at positions
+    // >= from, first position inside the tie window of m).  mlane: the lane's maximum over
+    // its column group's columns (0 if it leads no group).
+    auto publish = [&](int par, int from, T mlane) {
+        const T m = warp_max(mlane);
+        const T thr = m * tie;
         int f = INT_MAX;
-        for (int j = tid; j < nloc; j += nth)
-            if (pos[j] >= from && vn1[j] >= m * tie) f = min(f, pos[j]);
-        for (int o = 16; o > 0; o >>= 1) f = min(f, __shfl_xor_sync(0xffffffffu, f, o));
-        if (lane == 0) ired[w] = f;
-        __syncthreads();
-        if (tid == 0) {
-            for (int k = 1; k < nw; k++) f = min(f, ired[k]);
-            f = min(f, ired[0]);
-            for (int q = 0; q < CS; q++) {
-                *cl.map_shared_rank(&pubm[par][me], q) = m;
-                *cl.map_shared_rank(&pubf[par][me], q) = f;
+        if (gl == 0)
+            for (int j = gid; j < nloc; j += ngroups) {
+                const int p = pos[j];
+                if (p >= from && vn1[j] >= thr && p < f) f = p;
             }
+        f = warp_min(f);
+        if (lane < CS) {
+            *cl.map_shared_rank(&pubm[par][slot], lane) = m;
+            *cl.map_shared_rank(&pubf[par][slot], lane) = f;
         }
     };
 
@@ -170,70 +180,79 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_smem_kernel(Ctx<T> c, const D
             tmark = t;
         }
     };
-    publish(0, 0);
+    __syncthreads();  // norms of every slab column written
+    {
+        T m = 0;
+        if (gl == 0)
+            for (int j = gid; j < nloc; j += ngroups) m = fmax(m, vn1[j]);
+        publish(0, 0, m);
+    }
     qc_barrier(cl, CS);
     mark(0);
     int rank = mn;
     T r00 = 0;
-    int pend = -1;        // local column awaiting its reflector
-    T pend_beta = 0;
+    int pend = -1;  // local column awaiting its reflector (scaled vsh rows > pend_i, beta at pend_i)
+    T pend_beta = 0, pend_sc = 0;
     int pend_i = 0;
     for (int i = 0; i < mn; i++) {
         const int par = i & 1;
+        // (1) pivot, in every warp from the published entries
         T gmax = 0;
-        for (int q = 0; q < CS; q++) gmax = fmax(gmax, pubm[par][q]);
-        bool amb = false;
-        for (int q = 0; q < CS; q++) amb |= (pubm[par][q] < gmax && pubm[par][q] >= gmax * tie);
+        for (int e = lane; e < E; e += 32) gmax = fmax(gmax, pubm[par][e]);
+        gmax = warp_max(gmax);
+        const T thr = gmax * tie;
         int pvt = INT_MAX;
-        if (!amb) {
-            for (int q = 0; q < CS; q++)
-                if (pubm[par][q] == gmax) pvt = min(pvt, pubf[par][q]);
-        } else {
-            // a slab maximum inside the tie window below the global one: search every slab
-            // with the global threshold
-            int f = INT_MAX;
-            for (int j = tid; j < nloc; j += nth)
-                if (pos[j] >= i && vn1[j] >= gmax * tie) f = min(f, pos[j]);
-            for (int o = 16; o > 0; o >>= 1) f = min(f, __shfl_xor_sync(0xffffffffu, f, o));
-            if (lane == 0) ired[w] = f;
-            __syncthreads();
-            if (tid == 0) {
-                for (int k = 0; k < nw; k++) f = min(f, ired[k]);
-                for (int q = 0; q < CS; q++) *cl.map_shared_rank(&pubf[par][me], q) = f;
+        bool amb = false;
+        for (int e = lane; e < E; e += 32) {
+            const T m = pubm[par][e];
+            if (m >= thr) {
+                if (m == gmax) pvt = min(pvt, pubf[par][e]);
+                else amb = true;
             }
+        }
+        pvt = warp_min(pvt);
+        if (__any_sync(0xffffffffu, amb)) {
+            // a warp maximum inside the tie window below the global one: every warp searches
+            // its columns with the global threshold (the same decision in every warp)
+            int f = INT_MAX;
+            if (gl == 0)
+                for (int j = gid; j < nloc; j += ngroups) {
+                    const int p = pos[j];
+                    if (p >= i && vn1[j] >= thr && p < f) f = p;
+                }
+            f = warp_min(f);
+            if (lane < CS) *cl.map_shared_rank(&pubx[par][slot], lane) = f;
             qc_barrier(cl, CS);
-            for (int q = 0; q < CS; q++) pvt = min(pvt, pubf[par][q]);
+            pvt = INT_MAX;
+            for (int e = lane; e < E; e += 32) pvt = min(pvt, pubx[par][e]);
+            pvt = warp_min(pvt);
         }
         if (pvt < i || pvt >= cols) pvt = i;  // all norms NaN: keep the current position
-        mark(1);
         const int phys = perm[pvt];
         const int phys_i = perm[i];
         const int own = phys / cpc, lj = phys - own * cpc;
-        // reflector of the previous step into its column (no CTA reads it any more)
-        if (pend >= 0) {
-            T* a = A + (size_t)pend * lda;
-            for (int r = pend_i + 1 + tid; r < rows; r += nth) a[r] = vsh[r];
-            if (tid == 0) a[pend_i] = pend_beta;
-            pend = -1;
-        }
-        __syncthreads();
-        mark(2);
-        // pivot column -> vsh (rows >= i)
+        mark(1);
+        // (2) the previous reflector into its column (owner) and the pivot column into vsh,
+        // both with the row -> thread map r = tid (mod nth): a thread reads its old vsh rows
+        // before it overwrites them
         const T* src = (own == me ? A : cl.map_shared_rank(A, own)) + (size_t)lj * lda;
+        T* apend = pend >= 0 ? A + (size_t)pend * lda : nullptr;
         T part = 0;
-        for (int r = i + tid; r < rows; r += nth) {
-            const T v = src[r];
-            if (r == i) {
-                s_alpha = v;
-                vsh[r] = T(1);
-            } else {
+        for (int r = tid; r < rows; r += nth) {
+            if (apend && r > pend_i) apend[r] = vsh[r] * pend_sc;
+            if (r >= i) {
+                const T v = src[r];
                 vsh[r] = v;
-                part += v * v;
+                if (r == i) s_alpha = v;
+                else part += v * v;
             }
         }
+        if (apend && tid == 0) apend[pend_i] = pend_beta;
+        pend = -1;
         part = warp_sum(part);
         if (lane == 0) red[w] = part;
-        __syncthreads();
+        __syncthreads();  // partial norms, alpha; every thread has read perm
+        mark(2);
         T xnorm2 = 0;
         for (int k = 0; k < nw; k++) xnorm2 += red[k];
         const T alpha = s_alpha;
@@ -254,19 +273,16 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_smem_kernel(Ctx<T> c, const D
             rank = i;
             break;
         }
-        if (tu != T(0))
-            for (int r = i + 1 + tid; r < rows; r += nth) vsh[r] *= sc;
         if (me == 0 && tid == 0) taus[it.tau_off + i] = tu;
-        __syncthreads();  // vsh final; every thread has read perm
-        mark(3);
         if (tid == 0) {
             perm[i] = phys;
             perm[pvt] = phys_i;
         }
-        // trailing update of this slab's columns and their norms; positions after the swap.
-        // The loop runs the same number of times in every thread so that the group
-        // shuffles always see all 32 lanes.  The first lane of each group also keeps the
-        // largest new norm of its columns for the next pivot search.
+        mark(3);
+        // (3) H = I - tu v v^T, v = [1; sc * vsh[i+1:]], on this slab's columns at positions
+        // >= i (positions after the swap), norms downdated (LAWN 176) by the group's first
+        // lane.  The loop runs the same number of times in every thread so that the group
+        // shuffles always see all 32 lanes.
         T mloc = 0;
         for (int base = 0; base < nloc; base += ngroups) {
             const int j = base + gid;
@@ -275,9 +291,8 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_smem_kernel(Ctx<T> c, const D
             T* aj = A + (size_t)(active ? j : 0) * lda;
             T s = 0;
             if (active && tu != T(0)) {
-                // four independent partial sums so the shared-memory loads overlap
                 T s0 = 0, s1 = 0, s2 = 0, s3 = 0;
-                int r = i + gl;
+                int r = i + 1 + gl;
                 for (; r + 3 * G < rows; r += 4 * G) {
                     s0 += vsh[r] * aj[r];
                     s1 += vsh[r + G] * aj[r + G];
@@ -288,20 +303,22 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_smem_kernel(Ctx<T> c, const D
                 s = (s0 + s1) + (s2 + s3);
             }
             for (int o = G >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            const T ai0 = __shfl_sync(0xffffffffu, (active && gl == 0) ? aj[i] : T(0), (lane / G) * G);
             if (active && tu != T(0)) {
-                s *= tu;
-                int r = i + gl;
+                const T coef = tu * (ai0 + sc * s);
+                const T cr = coef * sc;
+                if (gl == 0) aj[i] = ai0 - coef;
+                int r = i + 1 + gl;
                 for (; r + 3 * G < rows; r += 4 * G) {
                     const T a0 = aj[r], a1 = aj[r + G], a2 = aj[r + 2 * G], a3 = aj[r + 3 * G];
-                    aj[r] = a0 - s * vsh[r];
-                    aj[r + G] = a1 - s * vsh[r + G];
-                    aj[r + 2 * G] = a2 - s * vsh[r + 2 * G];
-                    aj[r + 3 * G] = a3 - s * vsh[r + 3 * G];
+                    aj[r] = a0 - cr * vsh[r];
+                    aj[r + G] = a1 - cr * vsh[r + G];
+                    aj[r + 2 * G] = a2 - cr * vsh[r + 2 * G];
+                    aj[r + 3 * G] = a3 - cr * vsh[r + 3 * G];
                 }
-                for (; r < rows; r += G) aj[r] -= s * vsh[r];
+                for (; r < rows; r += G) aj[r] -= cr * vsh[r];
             }
             __syncwarp();
-            // norm downdating (LAWN 176), decided by the group's first lane
             int recompute = 0;
             T newv = 0;
             if (active && gl == 0) {
@@ -345,31 +362,12 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_smem_kernel(Ctx<T> c, const D
         mark(4);
         if (own == me) {
             pend = lj;
-            pend_beta = beta;
             pend_i = i;
+            pend_beta = beta;
+            pend_sc = sc;
         }
         if (i + 1 < mn) {
-            // publish (slab maximum, first position inside its tie window) for step i+1;
-            // every thread rescans only the columns it updated itself
-            for (int o = 16; o > 0; o >>= 1) mloc = fmax(mloc, __shfl_xor_sync(0xffffffffu, mloc, o));
-            if (lane == 0) red[w] = mloc;
-            __syncthreads();
-            T m = red[0];
-            for (int k = 1; k < nw; k++) m = fmax(m, red[k]);
-            int f = INT_MAX;
-            if (gl == 0)
-                for (int j = gid; j < nloc; j += ngroups)
-                    if (pos[j] > i && vn1[j] >= m * tie) f = min(f, pos[j]);
-            for (int o = 16; o > 0; o >>= 1) f = min(f, __shfl_xor_sync(0xffffffffu, f, o));
-            if (lane == 0) ired[w] = f;
-            __syncthreads();
-            if (tid == 0) {
-                for (int k = 0; k < nw; k++) f = min(f, ired[k]);
-                for (int q = 0; q < CS; q++) {
-                    *cl.map_shared_rank(&pubm[par ^ 1][me], q) = m;
-                    *cl.map_shared_rank(&pubf[par ^ 1][me], q) = f;
-                }
-            }
+            publish(par ^ 1, i + 1, mloc);
             mark(5);
             qc_barrier(cl, CS);
             mark(6);
@@ -378,14 +376,14 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_smem_kernel(Ctx<T> c, const D
     }
     if (probing)
         for (int k = 0; k < 8; k++) probe[k] += pacc[k];
+    // no CTA reads another's shared memory after this barrier (nor leaves before it)
+    qc_barrier(cl, CS);
     if (pend >= 0) {
-        __syncthreads();
         T* a = A + (size_t)pend * lda;
-        for (int r = pend_i + 1 + tid; r < rows; r += nth) a[r] = vsh[r];
+        for (int r = pend_i + 1 + tid; r < rows; r += nth) a[r] = vsh[r] * pend_sc;
         if (tid == 0) a[pend_i] = pend_beta;
     }
-    // no CTA leaves while another may still read its shared memory
-    qc_barrier(cl, CS);
+    __syncthreads();
     const int ld = c.cap[it.cluster];
     T* W = ws + it.ws_off;
     for (int j = w; j < nloc; j += nw) {
