@@ -92,6 +92,18 @@ int spand_cg(spand_tree* t, const double* b, double* x, int iters, double tol, i
 /* Same with device vectors. */
 int spand_cg_device(spand_tree* t, const double* b_dev, double* x_dev, int iters, double tol, int* iters_out,
                     double* relres_out);
+/* No counterpart in the reference: cg on nrhs right-hand sides at once.  Each column is an
+ * independent CG with the reference's stopping rule (|r| < tol |b|); the columns advance in
+ * lockstep so that one multi-right-hand-side preconditioner application, one SpMV and three
+ * dots per iteration serve them all, and a converged column stops changing.  b, x: host
+ * n x nrhs with leading dimension ld (x holds the initial guess); iters_out[nrhs] and
+ * relres_out[nrhs] receive each column's iteration count and recurrence residual. */
+int spand_cg_multi(spand_tree* t, const double* b, double* x, int nrhs, int ld, int iters, double tol,
+                   int* iters_out, double* relres_out);
+/* Same on device buffers (n x nrhs, leading dimension n); runs on the tree's stream and
+ * returns after the last column converged (one host read per iteration for the test). */
+int spand_cg_multi_device(spand_tree* t, const double* b_dev, double* x_dev, int nrhs, int iters, double tol,
+                          int* iters_out, double* relres_out);
 
 /* Introspection (reference: get_N, get_assembly_perm, nnz, get_stop, print_log fields;
  * include/tree.h:150-165, src/tree.cpp:1645-1727) */
@@ -118,10 +130,12 @@ int spand_tree_launches(spand_tree* t, long long* n, int reset);
 int spand_tree_device_bytes(spand_tree* t, long long* bytes);
 
 /* No reference counterpart -- measurement hooks used by bench.py:
- * one factorize() + device CG on device vectors b_dev / x_dev (x_dev is zeroed first),
- * timed with CUDA events on the tree's stream.  out[4]: factor ms, CG ms, iterations,
- * |r|/|b| of the recurrence residual. */
-int spand_tree_bench_step(spand_tree* t, const double* b_dev, double* x_dev, int iters, double tol, double* out);
+ * one factorize() + device CG on device arrays b_dev / x_dev, n x nrhs with leading
+ * dimension n (x_dev is zeroed first; nrhs > 1: the columns' CGs in lockstep, as in
+ * spand_cg_multi_device), timed with CUDA events on the tree's stream.  out[4]: factor ms,
+ * CG ms, iterations and |r|/|b| of the recurrence residual (largest over the columns). */
+int spand_tree_bench_step(spand_tree* t, const double* b_dev, double* x_dev, int nrhs, int iters, double tol,
+                          double* out);
 /* Bytes uploaded by assemble() for the block values (the factorization's device input). */
 int spand_tree_assembled_bytes(spand_tree* t, long long* bytes);
 /* Per-kernel-class device time (CUDA events around every launch while enabled). */

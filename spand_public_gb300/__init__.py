@@ -55,6 +55,10 @@ _PROTOS = {
                            C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "spand_cg_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
                                   C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "spand_cg_multi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,
+                                 C.c_void_p, C.c_void_p]),
+    "spand_cg_multi_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double,
+                                        C.c_void_p, C.c_void_p]),
     "spand_tree_get_N": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "spand_tree_get_perm": (C.c_int, [C.c_void_p, C.c_void_p]),
     "spand_tree_nnz": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
@@ -69,7 +73,8 @@ _PROTOS = {
     "spand_tree_timings": (C.c_int, [C.c_void_p, C.c_void_p]),
     "spand_tree_launches": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.c_int]),
     "spand_tree_device_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
-    "spand_tree_bench_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p]),
+    "spand_tree_bench_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double,
+                                        C.c_void_p]),
     "spand_tree_assembled_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
     "spand_tree_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "spand_tree_profile_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
@@ -186,6 +191,8 @@ class Tree:
         _check(self.L.spand_tree_solve_device(self.h, C.c_void_p(ptr), int(nrhs), int(ld)))
 
     def cg(self, b, iters=100, tol=1e-12, x0=None, verb=False):
+        if np.ndim(b) == 2:
+            return self.cg_multi(b, iters, tol, x0)
         b = np.ascontiguousarray(b, dtype=np.float64)
         x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.float64)
         it = C.c_int()
@@ -193,6 +200,20 @@ class Tree:
         _check(self.L.spand_cg(self.h, _ptr(b), _ptr(x), int(iters), float(tol), int(bool(verb)), C.byref(it),
                                C.byref(rr)))
         return x, it.value, rr.value
+
+    def cg_multi(self, B, iters=100, tol=1e-12, X0=None):
+        """Independent CGs on the columns of B (n x k) in lockstep (one multi-right-hand-side
+        preconditioner application per iteration).  Returns X (n x k), the iteration count
+        and the recurrence residual |r|/|b| of every column."""
+        B = np.asfortranarray(B, dtype=np.float64)
+        n, k = B.shape
+        X = np.zeros((n, k), dtype=np.float64, order="F") if X0 is None else \
+            np.array(X0, dtype=np.float64, order="F", copy=True)
+        its = np.zeros(k, dtype=np.int32)
+        rr = np.zeros(k, dtype=np.float64)
+        _check(self.L.spand_cg_multi(self.h, _ptr(B), _ptr(X), int(k), int(n), int(iters), float(tol), _ptr(its),
+                                     _ptr(rr)))
+        return X, its, rr
 
     def cg_device(self, b_ptr: int, x_ptr: int, iters=100, tol=1e-12):
         it = C.c_int()
@@ -263,11 +284,12 @@ class Tree:
         _check(self.L.spand_tree_launches(self.h, C.byref(v), int(bool(reset))))
         return v.value
 
-    def bench_step(self, b_ptr: int, x_ptr: int, iters=200, tol=1e-10):
-        """factorize + device CG, timed with CUDA events on the tree's stream."""
+    def bench_step(self, b_ptr: int, x_ptr: int, iters=200, tol=1e-10, nrhs=1):
+        """factorize + device CG (nrhs columns of n doubles each), timed with CUDA events on
+        the tree's stream."""
         out = np.zeros(4)
-        _check(self.L.spand_tree_bench_step(self.h, C.c_void_p(b_ptr), C.c_void_p(x_ptr), int(iters), float(tol),
-                                            _ptr(out)))
+        _check(self.L.spand_tree_bench_step(self.h, C.c_void_p(b_ptr), C.c_void_p(x_ptr), int(nrhs), int(iters),
+                                            float(tol), _ptr(out)))
         return dict(factor_ms=out[0], pcg_ms=out[1], iterations=int(out[2]), relres=out[3])
 
     def assembled_bytes(self):

@@ -179,6 +179,30 @@ int spand_cg_device(spand_tree* t, const double* b, double* x, int iters, double
     });
 }
 
+int spand_cg_multi(spand_tree* t, const double* b, double* x, int nrhs, int ld, int iters, double tol,
+                   int* iters_out, double* relres_out) {
+    CHECK_T(t);
+    if (!b || !x || !iters_out || !relres_out) return fail(SPAND_ERR_ARG, "null argument");
+    if (nrhs < 0 || ld < 0) return fail(SPAND_ERR_ARG, "negative size");
+    return guard([&] {
+        if (!t->t->device()) throw std::logic_error("cg before factorize");
+        spaND::cg_multi(*t->t, b, x, nrhs, ld, iters, tol, iters_out, relres_out);
+    });
+}
+
+int spand_cg_multi_device(spand_tree* t, const double* b, double* x, int nrhs, int iters, double tol,
+                          int* iters_out, double* relres_out) {
+    CHECK_T(t);
+    if (!b || !x || !iters_out || !relres_out) return fail(SPAND_ERR_ARG, "null argument");
+    if (nrhs < 0) return fail(SPAND_ERR_ARG, "negative size");
+    return guard([&] {
+        if (!t->t->device()) throw std::logic_error("cg before factorize");
+        if (nrhs > 0)
+            spand::device_pcg_multi(*t->t->device(), t->t->device_csr(), b, x, nrhs, iters, tol, true, iters_out,
+                                    relres_out);
+    });
+}
+
 int spand_tree_get_N(spand_tree* t, int* n) { CHECK_T(t); *n = t->t->get_N(); return SPAND_OK; }
 int spand_tree_get_perm(spand_tree* t, int* perm) {
     CHECK_T(t);
@@ -247,10 +271,11 @@ int spand_tree_launches(spand_tree* t, long long* n, int reset) {
 }
 int spand_tree_device_bytes(spand_tree* t, long long* b) { CHECK_T(t); *b = (long long)t->t->device_bytes(); return SPAND_OK; }
 
-int spand_tree_bench_step(spand_tree* t, const double* b, double* x, int iters, double tol, double* out) {
+int spand_tree_bench_step(spand_tree* t, const double* b, double* x, int nrhs, int iters, double tol, double* out) {
     CHECK_T(t);
     if (!b || !x || !out) return fail(SPAND_ERR_ARG, "null argument");
-    return guard([&] { t->t->bench_step(b, x, iters, tol, out); });
+    if (nrhs < 1) return fail(SPAND_ERR_ARG, "nrhs < 1");
+    return guard([&] { t->t->bench_step(b, x, nrhs, iters, tol, out); });
 }
 int spand_tree_assembled_bytes(spand_tree* t, long long* b) {
     CHECK_T(t);

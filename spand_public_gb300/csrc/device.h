@@ -126,6 +126,12 @@ struct PcgResult {
 PcgResult device_pcg(DeviceFactorBase& M, const DeviceCsr& A, const double* b, double* x, int maxit, double tol,
                      bool use_graph);
 
+// k independent PCGs in lockstep sharing one multi-right-hand-side preconditioner
+// application per iteration; b, x: n x k (column j at offset j * n), device memory.
+// Per column: iterations and recurrence residual |r|/|b|.
+void device_pcg_multi(DeviceFactorBase& M, const DeviceCsr& A, const double* b, double* x, int k, int maxit,
+                      double tol, bool use_graph, int* iters_out, double* relres_out);
+
 void device_spmv(const DeviceCsr& A, const double* x, double* y, cudaStream_t s);
 
 // dst[map[k]] = src[k] for map[k] >= 0 (device arrays), on stream s

@@ -1514,6 +1514,71 @@ __global__ void sub_kernel(int n, const double* a, const double* b, double* y) {
     if (i < n) y[i] = a[i] - b[i];
 }
 
+// Several right-hand sides at once: column j of every n x k operand at offset j * n
+// (blockIdx.y = j), the same per-column arithmetic and reduction order as the kernels above.
+// Scalars of column j at sc[8 * j + slot] (slots as above, [4] b.b); active[j] == 0 freezes
+// a converged column.
+__global__ void spmv_multi_kernel(int n, const int* __restrict__ rp, const int* __restrict__ ci,
+                                  const double* __restrict__ v, const double* __restrict__ x, double* __restrict__ y) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= n) return;
+    const size_t off = (size_t)blockIdx.y * n;
+    double s = 0;
+    for (int k = rp[row]; k < rp[row + 1]; k++) s += v[k] * x[off + ci[k]];
+    y[off + row] = s;
+}
+
+__global__ void dot_multi_partial_kernel(int n, const double* __restrict__ a, const double* __restrict__ b,
+                                         double* partial) {
+    __shared__ double red[33];
+    const size_t off = (size_t)blockIdx.y * n;
+    double s = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        s += a[off + i] * b[off + i];
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) partial[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = s;
+}
+
+__global__ void dot_multi_final_kernel(const double* partial, int np, double* sc, int slot) {
+    __shared__ double red[33];
+    double s = 0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) s += partial[(size_t)blockIdx.x * np + i];
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) sc[8 * blockIdx.x + slot] = s;
+}
+
+__global__ void cg_multi_update_xr_kernel(int n, double* x, double* r, const double* p, const double* Ap,
+                                          const double* sc, const int* active) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    if (i >= n || !active[j]) return;
+    const size_t o = (size_t)j * n + i;
+    const double alpha = sc[8 * j] / sc[8 * j + 1];
+    x[o] += alpha * p[o];
+    r[o] -= alpha * Ap[o];
+}
+
+__global__ void cg_multi_update_p_kernel(int n, double* p, const double* z, const double* sc, const int* active) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    if (i >= n || !active[j]) return;
+    const size_t o = (size_t)j * n + i;
+    const double beta = sc[8 * j] / sc[8 * j + 3];
+    p[o] = z[o] + beta * p[o];
+}
+
+__global__ void copy_scalar_multi_kernel(double* sc, int k, int dst, int src) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < k) sc[8 * j + dst] = sc[8 * j + src];
+}
+
+__global__ void sub_multi_kernel(int n, const double* a, const double* b, double* y) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t o = (size_t)blockIdx.y * n + i;
+    y[o] = a[o] - b[o];
+}
+
 // ------------------------------------------------------------------------------------
 // Kernel profiler
 // ------------------------------------------------------------------------------------
@@ -2759,6 +2824,134 @@ PcgResult device_pcg(DeviceFactorBase& M, const DeviceCsr& A, const double* b, d
     res.iterations = i + 1;
     res.relres = std::sqrt(resNorm2 / rhsNorm2);
     return res;
+}
+
+
+// Work buffers of the multi-right-hand-side PCG (n x k operands), grown on demand.
+struct PcgMultiWork {
+    size_t cap = 0;  // elements per operand
+    int kcap = 0;
+    double *r = nullptr, *p = nullptr, *z = nullptr, *q = nullptr, *partial = nullptr, *sc = nullptr;
+    int* active = nullptr;
+    double* h_sc = nullptr;
+    int* h_active = nullptr;
+    ~PcgMultiWork() { release(); }
+    void release() {
+        cudaFree(r); cudaFree(p); cudaFree(z); cudaFree(q); cudaFree(partial); cudaFree(sc); cudaFree(active);
+        if (h_sc) cudaFreeHost(h_sc);
+        if (h_active) cudaFreeHost(h_active);
+        r = p = z = q = partial = sc = h_sc = nullptr;
+        active = h_active = nullptr;
+        cap = 0;
+        kcap = 0;
+    }
+    void ensure(int n, int k) {
+        const size_t need = (size_t)n * k;
+        if (need <= cap && k <= kcap) return;
+        release();
+        SPAND_CUDA(cudaMalloc(&r, need * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&p, need * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&z, need * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&q, need * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&partial, (size_t)RED_BLOCKS * k * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&sc, 8 * (size_t)k * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&active, (size_t)k * sizeof(int)));
+        SPAND_CUDA(cudaMallocHost(&h_sc, 8 * (size_t)k * sizeof(double)));
+        SPAND_CUDA(cudaMallocHost(&h_active, (size_t)k * sizeof(int)));
+        cap = need;
+        kcap = k;
+    }
+};
+
+static thread_local PcgMultiWork g_pcgm;
+
+// k independent preconditioned CGs (is.cpp:39-121 per column) advanced in lockstep: one
+// SpMV, one multi-right-hand-side preconditioner application and three dots per
+// iteration serve every column; a converged column is frozen (its x and r stop changing)
+// and keeps its own iteration count.  b, x: n x k, column j at offset j * n.
+void device_pcg_multi(DeviceFactorBase& M, const DeviceCsr& A, const double* b, double* x, int k, int maxit,
+                      double tol, bool use_graph, int* iters_out, double* relres_out) {
+    cudaStream_t s = M.stream();
+    KernelProfiler& prof = M.profiler();
+    const int n = A.n;
+    g_pcgm.ensure(n, k);
+    PcgMultiWork& w = g_pcgm;
+    auto L = [&](const char* cls, auto&& f, int nk = 1) {
+        prof.begin(s, cls);
+        f();
+        prof.end(s);
+        M.add_launches(nk);
+    };
+    const dim3 gb((unsigned)((n + 255) / 256), (unsigned)k);
+    auto dot = [&](const double* a, const double* bb, int slot) {
+        L("dot", [&] {
+            dot_multi_partial_kernel<<<dim3(RED_BLOCKS, (unsigned)k), RED_THREADS, 0, s>>>(n, a, bb, w.partial);
+            dot_multi_final_kernel<<<(unsigned)k, RED_THREADS, 0, s>>>(w.partial, RED_BLOCKS, w.sc, slot);
+        }, 2);
+    };
+    auto spmv = [&](const double* in, double* out) {
+        L("spmv", [&] { spmv_multi_kernel<<<gb, 256, 0, s>>>(n, A.rowptr, A.colind, A.val, in, out); });
+    };
+    spmv(x, w.q);
+    L("axpy", [&] { sub_multi_kernel<<<gb, 256, 0, s>>>(n, b, w.q, w.r); });
+    dot(b, b, 4);
+    dot(w.r, w.r, 2);
+    SPAND_CUDA(cudaMemcpyAsync(w.h_sc, w.sc, 8 * (size_t)k * sizeof(double), cudaMemcpyDeviceToHost, s));
+    SPAND_CUDA(cudaStreamSynchronize(s));
+    std::vector<double> thr(k), bb(k);
+    int live = 0;
+    for (int j = 0; j < k; j++) {
+        bb[j] = w.h_sc[8 * j + 4];
+        thr[j] = tol * tol * bb[j];
+        const double rr = w.h_sc[8 * j + 2];
+        iters_out[j] = 0;
+        relres_out[j] = bb[j] > 0 ? std::sqrt(rr / bb[j]) : 0.0;
+        w.h_active[j] = (bb[j] > 0 && !(rr < thr[j])) ? 1 : 0;
+        if (bb[j] == 0) SPAND_CUDA(cudaMemsetAsync(x + (size_t)j * n, 0, n * sizeof(double), s));
+        live += w.h_active[j];
+    }
+    if (!live) {
+        SPAND_CUDA(cudaStreamSynchronize(s));
+        return;
+    }
+    SPAND_CUDA(cudaMemcpyAsync(w.active, w.h_active, (size_t)k * sizeof(int), cudaMemcpyHostToDevice, s));
+    SPAND_CUDA(cudaMemcpyAsync(w.p, w.r, (size_t)n * k * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    M.solve_device(w.p, k, n);
+    dot(w.r, w.p, 0);
+    if (use_graph) M.capture_solve(w.z, k, n);
+    int i = 0;
+    while (i < maxit) {
+        spmv(w.p, w.q);
+        dot(w.p, w.q, 1);
+        L("axpy", [&] { cg_multi_update_xr_kernel<<<gb, 256, 0, s>>>(n, x, w.r, w.p, w.q, w.sc, w.active); });
+        dot(w.r, w.r, 2);
+        SPAND_CUDA(cudaMemcpyAsync(w.h_sc, w.sc, 8 * (size_t)k * sizeof(double), cudaMemcpyDeviceToHost, s));
+        SPAND_CUDA(cudaStreamSynchronize(s));
+        live = 0;
+        for (int j = 0; j < k; j++) {
+            if (!w.h_active[j]) continue;
+            const double rr = w.h_sc[8 * j + 2];
+            relres_out[j] = std::sqrt(rr / bb[j]);
+            if (rr < thr[j]) {
+                w.h_active[j] = 0;
+                iters_out[j] = i + 1;
+            } else {
+                live++;
+            }
+        }
+        if (!live) break;
+        SPAND_CUDA(cudaMemcpyAsync(w.active, w.h_active, (size_t)k * sizeof(int), cudaMemcpyHostToDevice, s));
+        SPAND_CUDA(cudaMemcpyAsync(w.z, w.r, (size_t)n * k * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        M.solve_device(w.z, k, n);
+        L("axpy", [&] { copy_scalar_multi_kernel<<<(unsigned)((k + 63) / 64), 64, 0, s>>>(w.sc, k, 3, 0); });
+        dot(w.r, w.z, 0);
+        L("axpy", [&] { cg_multi_update_p_kernel<<<gb, 256, 0, s>>>(n, w.p, w.z, w.sc, w.active); });
+        i++;
+    }
+    for (int j = 0; j < k; j++)
+        if (w.h_active[j]) iters_out[j] = i + 1;
+    SPAND_CUDA(cudaGetLastError());
+    SPAND_CUDA(cudaStreamSynchronize(s));
 }
 
 }  // namespace spand

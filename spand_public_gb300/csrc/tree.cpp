@@ -5,6 +5,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <numeric>
 
@@ -158,7 +159,7 @@ void Tree::factorize() {
     log_dirty_ = true;
 }
 
-void Tree::bench_step(const double* b_dev, double* x_dev, int iters, double tol, double out[4]) {
+void Tree::bench_step(const double* b_dev, double* x_dev, int nrhs, int iters, double tol, double out[4]) {
     if (!assembled_ok_) throw std::logic_error("bench_step() before assemble()");
     cudaEvent_t e[3];
     for (auto& ev : e) cuda_check(cudaEventCreate(&ev), "cudaEventCreate");
@@ -169,8 +170,16 @@ void Tree::bench_step(const double* b_dev, double* x_dev, int iters, double tol,
         factored_ = true;
         log_dirty_ = true;
         cuda_check(cudaEventRecord(e[1], stream_), "cudaEventRecord");
-        cuda_check(cudaMemsetAsync(x_dev, 0, get_N() * sizeof(double), stream_), "cudaMemsetAsync");
-        r = spand::device_pcg(*dev_, dA_, b_dev, x_dev, iters, tol, true);
+        cuda_check(cudaMemsetAsync(x_dev, 0, (size_t)get_N() * nrhs * sizeof(double), stream_), "cudaMemsetAsync");
+        if (nrhs == 1) {
+            r = spand::device_pcg(*dev_, dA_, b_dev, x_dev, iters, tol, true);
+        } else {
+            std::vector<int> its(nrhs);
+            std::vector<double> rel(nrhs);
+            spand::device_pcg_multi(*dev_, dA_, b_dev, x_dev, nrhs, iters, tol, true, its.data(), rel.data());
+            r.iterations = *std::max_element(its.begin(), its.end());
+            r.relres = *std::max_element(rel.begin(), rel.end());
+        }
         cuda_check(cudaEventRecord(e[2], stream_), "cudaEventRecord");
         cuda_check(cudaEventSynchronize(e[2]), "cudaEventSynchronize");
     } catch (spand::DeviceError& err) {
@@ -495,6 +504,28 @@ int cg(const Csc& A, const double* rhs, double* x, const Tree& precond, int iter
     if (verb) printf("# of iter:  %d\n", r.iterations);
     if (relres) *relres = r.relres;
     return r.iterations;
+}
+
+void cg_multi(const Tree& precond, const double* rhs, double* x, int nrhs, int ld, int iters, double tol,
+              int* iters_out, double* relres_out) {
+    const int n = precond.get_N();
+    if (nrhs <= 0) return;
+    if (ld < n) throw std::invalid_argument("leading dimension smaller than the matrix order");
+    const size_t tot = (size_t)n * nrhs;
+    double* db = precond.cg_buffer(0, (int)tot);
+    double* dx = precond.cg_buffer(1, (int)tot);
+    cudaStream_t s = precond.stream();
+    const size_t row = (size_t)n * sizeof(double), pitch = (size_t)ld * sizeof(double);
+    cuda_check(cudaMemcpy2DAsync(db, row, rhs, pitch, row, nrhs, cudaMemcpyHostToDevice, s), "H2D");
+    cuda_check(cudaMemcpy2DAsync(dx, row, x, pitch, row, nrhs, cudaMemcpyHostToDevice, s), "H2D");
+    try {
+        spand::device_pcg_multi(*precond.device(), precond.device_csr(), db, dx, nrhs, iters, tol, true, iters_out,
+                                relres_out);
+    } catch (spand::DeviceError& e) {
+        throw std::runtime_error(e.msg);
+    }
+    cuda_check(cudaMemcpy2DAsync(x, pitch, dx, row, row, nrhs, cudaMemcpyDeviceToHost, s), "D2H");
+    cuda_check(cudaStreamSynchronize(s), "sync");
 }
 
 }  // namespace spaND

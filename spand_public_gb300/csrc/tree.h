@@ -103,7 +103,8 @@ class Tree {
 
     // No reference counterpart: factorize + device PCG on device vectors, timed with
     // CUDA events on the tree's stream.  out: factor ms, PCG ms, iterations, |r|/|b|.
-    void bench_step(const double* b_dev, double* x_dev, int iters, double tol, double out[4]);
+    // nrhs right-hand sides: b_dev, x_dev n x nrhs (leading dimension n)
+    void bench_step(const double* b_dev, double* x_dev, int nrhs, int iters, double tol, double out[4]);
 
    private:
     void build_ops_and_log();
@@ -145,5 +146,11 @@ class Tree {
 // Preconditioned CG (is.cpp:39-121) on the device; b and x are host vectors.
 int cg(const Csc& A, const double* rhs, double* x, const Tree& precond, int iters, double tol, bool verb,
        double* relres = nullptr);
+
+// No counterpart in the reference: cg on nrhs right-hand sides at once (independent CGs
+// in lockstep, one multi-right-hand-side preconditioner application per iteration).
+// rhs, x: host n x nrhs, leading dimension ld; per column the iteration count and |r|/|b|.
+void cg_multi(const Tree& precond, const double* rhs, double* x, int nrhs, int ld, int iters, double tol,
+              int* iters_out, double* relres_out);
 
 }  // namespace spaND

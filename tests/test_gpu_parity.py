@@ -205,3 +205,28 @@ def test_reassemble_same_pattern():
     b = P.rhs(A2.shape[0], 1, seed=4)[:, 0]
     xt, xo = t.solve(b), o.solve(b)
     assert np.linalg.norm(xt - xo) / np.linalg.norm(xo) < TOL_SOLVE
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+def test_cg_multi_matches_single(fp32):
+    """Several right-hand sides at once: every column takes the iterations and reaches the
+    solution of its own single-right-hand-side CG (the columns share the preconditioner
+    applications only); a zero column stays zero after 0 iterations."""
+    from spand_public_gb300 import problems as P
+    A, t, o = _build(16, 3, 6, 1e-2, fp32=fp32)
+    B = P.rhs(A.shape[0], 5, seed=7)
+    B[:, 3] = 0.0
+    X, its, rr = t.cg(B, iters=200, tol=1e-10)
+    assert X.shape == B.shape and its.shape == (5,)
+    for j in range(5):
+        if j == 3:
+            assert its[j] == 0 and not np.any(X[:, j])
+            continue
+        xj, itj, rj = t.cg(B[:, j], iters=200, tol=1e-10)
+        assert its[j] == itj, (j, its[j], itj)
+        assert np.linalg.norm(X[:, j] - xj) <= 1e-12 * np.linalg.norm(xj)
+        assert abs(rr[j] - rj) <= 1e-12 + 1e-9 * rj
+        assert np.linalg.norm(A @ X[:, j] - B[:, j]) / np.linalg.norm(B[:, j]) < 1e-9
+        if not fp32:
+            _, ito = o.cg(B[:, j], 200, 1e-10)
+            assert its[j] == ito
