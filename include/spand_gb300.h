@@ -62,6 +62,12 @@ int spand_tree_partition(spand_tree* t, int n, const int* colptr, const int* row
 /* void assemble(SpMat&)                            -- include/tree.h:182, src/tree.cpp:505-575
  * Also builds the symbolic plan of the factorization and uploads the blocks. */
 int spand_tree_assemble(spand_tree* t, int n, const int* colptr, const int* rowval, const double* vals);
+/* No counterpart in the reference: assemble() again with new values on the pattern of the
+ * last spand_tree_assemble (vals: nnz doubles in that matrix's CSC order; device memory
+ * when on_device != 0).  The symbolic plan and the device work lists are reused: one copy
+ * of the values and two scatter kernels (blocks, CSR).  SPAND_ERR_STATE before the first
+ * assemble, SPAND_ERR_ARG when nnz differs. */
+int spand_tree_assemble_values(spand_tree* t, const double* vals, long long nnz, int on_device);
 
 /* void factorize()                                 -- include/tree.h:186, src/tree.cpp:1447-1551 */
 int spand_tree_factorize(spand_tree* t);

@@ -55,6 +55,7 @@ _PROTOS = {
                            C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "spand_cg_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
                                   C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "spand_tree_assemble_values": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_int]),
     "spand_cg_multi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,
                                  C.c_void_p, C.c_void_p]),
     "spand_cg_multi_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double,
@@ -200,6 +201,15 @@ class Tree:
         _check(self.L.spand_cg(self.h, _ptr(b), _ptr(x), int(iters), float(tol), int(bool(verb)), C.byref(it),
                                C.byref(rr)))
         return x, it.value, rr.value
+
+    def assemble_values(self, vals, on_device=False):
+        """New values on the pattern of the last assemble() (CSC order).  vals: numpy array,
+        or (on_device=True) the address of nnz doubles in device memory."""
+        if on_device:
+            _check(self.L.spand_tree_assemble_values(self.h, C.c_void_p(int(vals[0])), int(vals[1]), 1))
+        else:
+            v = np.ascontiguousarray(vals, dtype=np.float64)
+            _check(self.L.spand_tree_assemble_values(self.h, _ptr(v), int(v.size), 0))
 
     def cg_multi(self, B, iters=100, tol=1e-12, X0=None):
         """Independent CGs on the columns of B (n x k) in lockstep (one multi-right-hand-side

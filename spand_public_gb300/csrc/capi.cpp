@@ -179,6 +179,12 @@ int spand_cg_device(spand_tree* t, const double* b, double* x, int iters, double
     });
 }
 
+int spand_tree_assemble_values(spand_tree* t, const double* vals, long long nnz, int on_device) {
+    CHECK_T(t);
+    if (!vals && nnz > 0) return fail(SPAND_ERR_ARG, "null values");
+    return guard([&] { t->t->assemble_values(vals, (int64_t)nnz, on_device != 0); });
+}
+
 int spand_cg_multi(spand_tree* t, const double* b, double* x, int nrhs, int ld, int iters, double tol,
                    int* iters_out, double* relres_out) {
     CHECK_T(t);

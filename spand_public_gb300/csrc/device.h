@@ -80,7 +80,8 @@ class DeviceFactorBase {
     virtual void upload(const Plan& P, const std::vector<int64_t>& amap) = 0;
     // assemble the level-0 blocks from the values of A (host, CSC order of the pattern):
     // one copy to the device and a scatter through the assembly map
-    virtual void assemble_values(const double* vals, int64_t nnz) = 0;
+    // values of the assembled pattern (CSC order), host or device memory
+    virtual void assemble_values(const double* vals, int64_t nnz, bool on_device = false) = 0;
     // device copy of the last uploaded values of A (CSC order)
     virtual const double* device_values() const = 0;
     virtual void factorize(double tol) = 0;  // throws DeviceError

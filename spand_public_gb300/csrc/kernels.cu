@@ -1959,9 +1959,9 @@ class DeviceFactor : public DeviceFactorBase {
         caps_h_ = P.c_cap;
     }
 
-    void assemble_values(const double* vals, int64_t nnz) override {
+    void assemble_values(const double* vals, int64_t nnz, bool on_device) override {
         if (nnz != amap_n_) throw DeviceError{SPAND_ERR_ARG, "values do not match the assembled pattern"};
-        if (nnz > 0) SPAND_CUDA(cudaMemcpyAsync(d_vals_, vals, nnz * sizeof(double), cudaMemcpyHostToDevice, s_));
+        if (nnz > 0) SPAND_CUDA(cudaMemcpyAsync(d_vals_, vals, nnz * sizeof(double), (on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice), s_));
         if (P_->assembled_len) SPAND_CUDA(cudaMemsetAsync(pristine_, 0, P_->assembled_len * sizeof(T), s_));
         if (nnz > 0) {
             assemble_scatter_kernel<T><<<(unsigned)((nnz + 255) / 256), 256, 0, s_>>>(d_vals_, d_amap_, nnz, pristine_);

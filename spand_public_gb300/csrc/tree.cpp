@@ -141,6 +141,23 @@ void Tree::assemble(const Csc& A) {
     t_assemble = now_s() - t0;
 }
 
+void Tree::assemble_values(const double* vals, int64_t nnz, bool on_device) {
+    if (!assembled_ok_ || !dev_) throw std::logic_error("assemble_values() before assemble()");
+    if (nnz != (int64_t)A_.rowval.size()) throw std::invalid_argument("values do not match the assembled pattern");
+    double t0 = now_s();
+    if (!on_device) A_.val.assign(vals, vals + nnz);
+    try {
+        dev_->assemble_values(vals, nnz, on_device);
+    } catch (spand::DeviceError& e) {
+        throw std::runtime_error(e.msg);
+    }
+    spand::device_scatter(dev_->device_values(), d_cmap_, nnz, dA_.val, stream_);
+    cuda_check(cudaGetLastError(), "assembly scatter");
+    cuda_check(cudaStreamSynchronize(stream_), "sync");
+    factored_ = false;
+    t_assemble = now_s() - t0;
+}
+
 // tree.cpp:1447-1551
 void Tree::factorize() {
     if (!assembled_ok_) throw std::logic_error("factorize() before assemble()");

@@ -60,6 +60,10 @@ class Tree {
 
     std::vector<ClusterID> partition(const Csc& A);
     void assemble(const Csc& A);
+    // No counterpart in the reference: new values on the pattern of the last assemble()
+    // (CSC order, nnz entries), from host or device memory; the plan and device work lists
+    // are reused.  Device values leave the host copy of A (matrix()) unchanged.
+    void assemble_values(const double* vals, int64_t nnz, bool on_device);
     void factorize();
     // x <- M^{-1} x, host vector(s) in natural ordering (tree.cpp:1610-1635)
     void solve(double* x, int nrhs = 1, int ld = -1) const;

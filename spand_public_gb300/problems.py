@@ -89,6 +89,45 @@ def face_diffusion(n: int, dim: int, face_k: list[np.ndarray], shift: np.ndarray
     return _canonical(A)
 
 
+def face_diffusion_map(n: int, dim: int):
+    """The linear map from face conductivities to the CSC values of face_diffusion(n, dim, ·):
+    with w the axis-by-axis concatenation of the flattened (C order) face arrays,
+    values = zeros(nnz); values[pos[t]] += coef[t] * w[face[t]] for every t.  Returns
+    (pattern, pos, face, coef), pattern being the CSC matrix for unit conductivities."""
+    N = n ** dim
+    idx = np.arange(N).reshape((n,) * dim)
+    rows, cols, face, coef = [], [], [], []
+    base = 0
+    for ax in range(dim):
+        shape = [n] * dim
+        shape[ax] = n - 1
+        fid = base + np.arange(int(np.prod(shape))).reshape(shape)
+        a = np.take(idx, np.arange(n - 1), axis=ax).reshape(-1)
+        b = np.take(idx, np.arange(1, n), axis=ax).reshape(-1)
+        f = fid.reshape(-1)
+        for r, c, k in ((a, b, -1.0), (b, a, -1.0), (a, a, 1.0), (b, b, 1.0)):
+            rows.append(r)
+            cols.append(c)
+            face.append(f)
+            coef.append(np.full(f.size, k))
+        # Dirichlet boundary cells: the conductivity of their interior neighbour face
+        for layer, fl in ((0, 0), (n - 1, n - 2)):
+            cell = np.take(idx, [layer], axis=ax).reshape(-1)
+            rows.append(cell)
+            cols.append(cell)
+            face.append(np.take(fid, [fl], axis=ax).reshape(-1))
+            coef.append(np.ones(cell.size))
+        base += fid.size
+    rows, cols = np.concatenate(rows), np.concatenate(cols)
+    face, coef = np.concatenate(face), np.concatenate(coef)
+    pattern = _canonical(sp.coo_matrix((np.ones(rows.size), (rows, cols)), shape=(N, N)))
+    # CSC position of every (row, col): CSC order is (col, row) lexicographic
+    pcol = np.repeat(np.arange(N, dtype=np.int64), np.diff(pattern.indptr))
+    keys = pcol * N + pattern.indices.astype(np.int64)
+    pos = np.searchsorted(keys, cols.astype(np.int64) * N + rows)
+    return pattern, pos, face, coef
+
+
 def high_contrast_fv2d(n: int = 1024, tile: int = 8, seed: int = 0) -> sp.csc_matrix:
     """2D 5-point finite-volume diffusion, cell coefficients 10^U(−3,3) constant on
     tile×tile blocks, harmonic-mean face conductivities, Dirichlet."""
