@@ -31,11 +31,19 @@ sys.path.insert(0, ROOT)
 METRIC = "factor+PCG seconds to 1e-10 FP64 rel. residual (3D 7-pt Laplacian 64^3, eps=1e-2)"
 
 
+PROBLEMS = {
+    "lap3d": "3D 7-pt Laplacian {n}^3",
+    "fv2d": "2D 5-pt finite-volume diffusion {n}^2, coefficients 10^U(-3,3) on 8x8 tiles",
+    "aniso3d": "3D anisotropic diffusion {n}^3, face conductivities exp(0.5 z), axis scaling (1,1,0.01)",
+}
+
+
 def metric(args):
-    """The headline metric string; other grids, tolerances and right-hand-side counts say so."""
-    if (args.n, args.eps, args.nrhs) == (64, 1e-2, 1):
+    """The headline metric string; other problems, grids, tolerances and right-hand-side
+    counts say so."""
+    if (args.problem, args.n, args.eps, args.nrhs) == ("lap3d", 64, 1e-2, 1):
         return METRIC
-    return (f"factor+PCG seconds to {args.tol:g} FP64 rel. residual (3D 7-pt Laplacian {args.n}^3, "
+    return (f"factor+PCG seconds to {args.tol:g} FP64 rel. residual ({PROBLEMS[args.problem].format(n=args.n)}, "
             f"eps={args.eps:g}, {args.nrhs} RHS)")
 
 
@@ -45,6 +53,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--problem", default="lap3d", choices=sorted(PROBLEMS))
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--levels", type=int, default=12)
     ap.add_argument("--eps", type=float, default=1e-2)
@@ -59,16 +68,21 @@ def parse():
 def workload(args):
     from spand_public_gb300 import problems as P
 
-    A = P.neglapl(args.n, 3)
-    X = P.linspace_nd(args.n, 3)
+    if args.problem == "lap3d":
+        A, X = P.neglapl(args.n, 3), P.linspace_nd(args.n, 3)
+    elif args.problem == "fv2d":
+        A, X = P.high_contrast_fv2d(args.n, 8, seed=0), P.linspace_nd(args.n, 2)
+    else:
+        A, X = P.anisotropic3d(args.n, P.anisotropic_theta(args.n, seed=0)), P.linspace_nd(args.n, 3)
     B = np.asfortranarray(P.rhs(A.shape[0], args.nrhs, seed=0))  # n x nrhs, column j = RHS j
     return A, X, B
 
 
 def config(args, extra=None):
-    c = {"workload": f"3d 7-point -Laplacian {args.n}^3 (n={args.n ** 3}), {args.levels} ND levels, eps={args.eps:g}, "
-                     f"{args.nrhs} RHS N(0,1) seed 0, PCG to {args.tol:g}",
-         "grid": args.n, "levels": args.levels, "eps": args.eps, "nrhs": args.nrhs, "pcg_tol": args.tol,
+    dim = 2 if args.problem == "fv2d" else 3
+    c = {"workload": f"{PROBLEMS[args.problem].format(n=args.n)} (n={args.n ** dim}), {args.levels} ND levels, "
+                     f"eps={args.eps:g}, {args.nrhs} RHS N(0,1) seed 0, PCG to {args.tol:g}",
+         "problem": args.problem, "grid": args.n, "levels": args.levels, "eps": args.eps, "nrhs": args.nrhs, "pcg_tol": args.tol,
          "ordering": "geometric modified nested dissection",
          "l2": "working set larger than L2 (factor arena of several GB)"}
     if extra:
