@@ -702,225 +702,10 @@ __global__ void __launch_bounds__(256) schur_kernel(Ctx<T> c, const DTarget* __r
 // ------------------------------------------------------------------------------------
 // Sparsification (tree.cpp:1189-1224, 1292-1347, 980-1104)
 // ------------------------------------------------------------------------------------
-// Asn = [A_sn (in-edges) | A_ns^T (out-edges)], rows = size(c); ld = cap(c).
-template <typename T>
-__global__ void asn_gather_kernel(Ctx<T> c, const DSpars* __restrict__ items, const DAsn* __restrict__ pieces, T* ws,
-                                  int* colcount, const int* __restrict__ only) {
-    if (c.status->not_spd || (only && !only[blockIdx.x])) return;
-    const DSpars it = items[blockIdx.x];
-    const int rows = c.csize[it.cluster];
-    const int ld = c.cap[it.cluster];
-    T* W = ws + it.ws_off;
-    int col = 0;
-    for (int p = 0; p < it.count; p++) {
-        const DAsn pc = pieces[it.first + p];
-        const int n = c.csize[pc.nbr];
-        const T* B = bptr(c, pc.block);
-        const int bld = c.blk[pc.block].ld;
-        if (!pc.transposed) {
-            for (int idx = threadIdx.x; idx < rows * n; idx += blockDim.x) {
-                int i = idx % rows, j = idx / rows;
-                W[i + (size_t)(col + j) * ld] = B[i + (size_t)j * bld];
-            }
-        } else {
-            for (int idx = threadIdx.x; idx < rows * n; idx += blockDim.x) {
-                int j = idx % n, i = idx / n;
-                W[i + (size_t)(col + j) * ld] = B[j + (size_t)i * bld];
-            }
-        }
-        col += n;
-    }
-    if (threadIdx.x == 0) colcount[blockIdx.x] = col;
-}
+// The sparsification QRCP (Asn = [A_sn (in-edges) | A_ns^T (out-edges)], rows = size(c))
+// lives in qrcp.cu; its output (R, reflectors, pivot vector and inverse, tau, rank) lands
+// in the workspace ws at the matrix's offset, ld = cap(c), columns in position order.
 
-// Householder QR with column pivoting (LAPACK dgeqp3/dlaqp2 with LAWN 176 norm
-// downdating), stopped as soon as |R_ii| / |R_00| < tol (choose_rank, util.cpp:434-452).
-// One block per matrix; the matrix stays in global memory (L2), reflector in shared.
-template <typename T>
-__global__ void __launch_bounds__(512) qrcp_kernel(Ctx<T> c, const DSpars* __restrict__ items, T* ws, T* norms,
-                                                    int* jpvt_ws, int* ipvt_ws, const int* __restrict__ colcount,
-                                                    T* taus, int* rank_out, double tol, const int* __restrict__ only) {
-    extern __shared__ unsigned char smem_raw[];
-    T* vsh = reinterpret_cast<T*>(smem_raw);  // cap(c) entries
-    __shared__ T red[33];
-    __shared__ T s_val[16];
-    __shared__ int s_idx[16];
-    __shared__ int s_pvt;
-    __shared__ T s_beta, s_tau, s_scal;
-    __shared__ int s_stop;
-    if (c.status->not_spd || (only && !only[blockIdx.x])) return;
-    const DSpars it = items[blockIdx.x];
-    const int rows = c.csize[it.cluster];
-    const int cols = colcount[blockIdx.x];
-    const int ld = c.cap[it.cluster];
-    T* A = ws + it.ws_off;
-    T* vn1 = norms + 2 * it.col_off;
-    T* vn2 = vn1 + it.cap_cols;
-    int* jpvt = jpvt_ws + it.col_off;
-    T* tau = taus + it.tau_off;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int mn = min(rows, cols);
-    int rank;
-    if (tol >= 1.0) {
-        // choose_rank returns 0 without looking at R; keep the pivot vector defined
-        rank = 0;
-        for (int j = threadIdx.x; j < cols; j += blockDim.x) jpvt[j] = j;
-    } else {
-        // initial column norms, warp per column
-        for (int j = w; j < cols; j += nw) {
-            T s = 0;
-            const T* a = A + (size_t)j * ld;
-            for (int r = lane; r < rows; r += 32) s += a[r] * a[r];
-            s = warp_sum(s);
-            if (lane == 0) {
-                vn1[j] = dsqrt(s);
-                vn2[j] = vn1[j];
-                jpvt[j] = j;
-            }
-        }
-        const T tol3z = dsqrt(sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-07));
-        T r00 = 0;
-        rank = mn;
-        if (threadIdx.x == 0) s_stop = 0;
-        __syncthreads();
-        for (int i = 0; i < mn; i++) {
-            // pivot: first column of [i, cols) whose partial norm is within a relative
-            // qrcp_tie<T>() of the largest; exact-arithmetic ties (mirror-symmetric
-            // stencil columns) then do not depend on the summation order of the norms.
-            T bv = 0;
-            for (int j = i + threadIdx.x; j < cols; j += blockDim.x) bv = fmax(bv, vn1[j]);
-            for (int o = 16; o > 0; o >>= 1) bv = fmax(bv, __shfl_xor_sync(0xffffffffu, bv, o));
-            if (lane == 0) s_val[w] = bv;
-            __syncthreads();
-            T vmax = s_val[0];
-            for (int k = 1; k < nw; k++) vmax = fmax(vmax, s_val[k]);
-            const T thresh = vmax * (T(1) - qrcp_tie<T>());
-            int bi = cols;
-            for (int j = i + threadIdx.x; j < cols; j += blockDim.x)
-                if (vn1[j] >= thresh) { bi = j; break; }
-            for (int o = 16; o > 0; o >>= 1) bi = min(bi, __shfl_xor_sync(0xffffffffu, bi, o));
-            if (lane == 0) s_idx[w] = bi;
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                int id = s_idx[0];
-                for (int k = 1; k < nw; k++) id = min(id, s_idx[k]);
-                s_pvt = id < cols ? id : i;  // all norms NaN: keep the current column
-            }
-            __syncthreads();
-            const int pvt = s_pvt;
-            if (pvt != i) {
-                T* a = A + (size_t)i * ld;
-                T* b = A + (size_t)pvt * ld;
-                for (int r = threadIdx.x; r < rows; r += blockDim.x) {
-                    T tmp = a[r];
-                    a[r] = b[r];
-                    b[r] = tmp;
-                }
-                if (threadIdx.x == 0) {
-                    int tj = jpvt[i];
-                    jpvt[i] = jpvt[pvt];
-                    jpvt[pvt] = tj;
-                    vn1[pvt] = vn1[i];
-                    vn2[pvt] = vn2[i];
-                }
-            }
-            __syncthreads();
-            // reflector of column i (dlarfg)
-            T* ai = A + (size_t)i * ld;
-            T part = 0;
-            for (int r = i + 1 + threadIdx.x; r < rows; r += blockDim.x) part += ai[r] * ai[r];
-            T xnorm2 = block_sum(part, red);
-            if (threadIdx.x == 0) {
-                T alpha = ai[i];
-                T xnorm = dsqrt(xnorm2);
-                T beta, tu, sc;
-                if (xnorm == T(0)) {
-                    beta = alpha;
-                    tu = 0;
-                    sc = 0;
-                } else {
-                    beta = -copysign(hypot(alpha, xnorm), alpha);
-                    tu = (beta - alpha) / beta;
-                    sc = T(1) / (alpha - beta);
-                }
-                s_beta = beta;
-                s_tau = tu;
-                s_scal = sc;
-                T rii = fabs(beta);
-                if (i == 0) r00 = rii;
-                int stop = 0;
-                if (tol != 0.0 && i >= 1) {
-                    T ratio = rii / r00;
-                    if (!(ratio >= T(tol))) stop = 1;
-                }
-                s_stop = stop;
-                red[32] = r00;
-            }
-            __syncthreads();
-            r00 = red[32];
-            if (s_stop) {
-                rank = i;
-                break;
-            }
-            const T tu = s_tau, sc = s_scal;
-            if (tu != T(0))
-                for (int r = i + 1 + threadIdx.x; r < rows; r += blockDim.x) ai[r] *= sc;
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                ai[i] = s_beta;
-                tau[i] = tu;
-            }
-            for (int r = i + 1 + threadIdx.x; r < rows; r += blockDim.x) vsh[r] = ai[r];
-            if (threadIdx.x == 0) vsh[i] = T(1);
-            __syncthreads();
-            // apply H(i) to the trailing columns and downdate their norms, warp per column
-            for (int j = i + 1 + w; j < cols; j += nw) {
-                T* aj = A + (size_t)j * ld;
-                if (tu != T(0)) {
-                    T s = 0;
-                    for (int r = i + lane; r < rows; r += 32) s += vsh[r] * aj[r];
-                    s = warp_sum(s) * tu;
-                    for (int r = i + lane; r < rows; r += 32) aj[r] -= s * vsh[r];
-                }
-                __syncwarp();
-                T v1 = vn1[j];
-                if (v1 != T(0)) {
-                    T temp = fabs(aj[i]) / v1;
-                    temp = T(1) - temp * temp;
-                    temp = temp > T(0) ? temp : T(0);
-                    T rr = v1 / vn2[j];
-                    T temp2 = temp * rr * rr;
-                    if (temp2 <= tol3z) {
-                        T s = 0;
-                        for (int r = i + 1 + lane; r < rows; r += 32) s += aj[r] * aj[r];
-                        s = warp_sum(s);
-                        if (lane == 0) {
-                            if (i < rows - 1) {
-                                vn1[j] = dsqrt(s);
-                                vn2[j] = vn1[j];
-                            } else {
-                                vn1[j] = 0;
-                                vn2[j] = 0;
-                            }
-                        }
-                    } else if (lane == 0) {
-                        vn1[j] = v1 * dsqrt(temp);
-                    }
-                }
-                __syncwarp();
-            }
-            __syncthreads();
-        }
-    }
-    // inverse pivot vector (column -> position)
-    __syncthreads();
-    int* ipvt = ipvt_ws + it.col_off;
-    for (int j = threadIdx.x; j < cols; j += blockDim.x) {
-        const int q = jpvt[j];
-        if (q >= 0 && q < cols) ipvt[q] = j;
-    }
-    if (threadIdx.x == 0) rank_out[it.cluster] = rank;
-}
 
 // Blocked compact WY form of Q = H_0 ... H_{k-1}: reflectors in blocks of QB = 32,
 // Q = Q_0 Q_1 ..., Q_b = I - V_b T_b V_b^T with T_b the 32x32 upper triangular factor of
@@ -1740,6 +1525,7 @@ class DeviceFactor : public DeviceFactorBase {
         taustore_ = alloc<T>(std::max<int64_t>(P.tau_len, 1));
         tauws_ = alloc<T>(std::max<int64_t>(P.tau_len, 1));
         ws_ = alloc<T>(std::max<int64_t>(P.ws_len, 1));
+        ws2_ = alloc<T>(std::max<int64_t>(P.ws_len, 1));
         {
             std::vector<DUpd> u;
             for (const SchurUpdate& su : P.schur_updates) u.push_back({su.b1, su.t1, su.b2, su.t2, su.s});
@@ -1801,8 +1587,6 @@ class DeviceFactor : public DeviceFactorBase {
                     coloff += std::max(it.cap_cols, 1);
                     maxcap = std::max(maxcap, P.c_cap[it.cluster]);
                 }
-                if ((int64_t)maxcap * (int64_t)sizeof(T) > 200 * 1024)
-                    throw DeviceError{SPAND_ERR_UNSUPPORTED, "cluster too large for the QRCP kernel"};
                 max_cols = std::max(max_cols, coloff);
                 max_items = std::max(max_items, (int)items.size());
                 W.n = (int)items.size();
@@ -1819,6 +1603,18 @@ class DeviceFactor : public DeviceFactorBase {
                     std::vector<std::pair<int, int>> dims;
                     for (const SparsifyItem& it : wave) dims.push_back({P.c_cap[it.cluster], it.cap_cols});
                     choose_cluster(W, dims);
+                    // global-memory launch: a full cluster where some matrix at its capacity
+                    // could exceed the largest shared-memory configuration, else one CTA as
+                    // the safety net for sizes that grow beyond the tuned configuration
+                    bool big = false;
+                    for (const auto& d : dims)
+                        big |= qc_need(d.first, d.second, qc_max_cs_, (int)sizeof(T)) > qc_smem_cap_;
+                    W.gcs = (big || force_global_) ? qc_max_cs_ : 1;
+                    int64_t g = 4096;
+                    for (const auto& d : dims) g = std::max<int64_t>(g, qc_small_need(d.first, d.second, W.gcs, (int)sizeof(T)));
+                    if (g > qc_smem_cap_)
+                        throw DeviceError{SPAND_ERR_UNSUPPORTED, "sparsification matrix too large for the QRCP kernels"};
+                    W.gsmem = (int)((g + 255) & ~int64_t(255));
                 }
                 D.waves.push_back(W);
             }
@@ -1924,7 +1720,6 @@ class DeviceFactor : public DeviceFactorBase {
                 D.x_smem_ortho = mx * (int)sizeof(T);
             }
         }
-        norms_ = alloc<T>(2 * max_cols);
         jpvt_ = alloc<int>(max_cols);
         ipvt_ = alloc<int>(max_cols);
         colcount_ = alloc<int>(max_items);
@@ -1942,7 +1737,6 @@ class DeviceFactor : public DeviceFactorBase {
         SPAND_CUDA(cudaFuncSetAttribute(potrf3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(trtri_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(trsm3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        SPAND_CUDA(cudaFuncSetAttribute(qrcp_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         fallback_ = alloc<int>(max_items);
         SPAND_CUDA(cudaFuncSetAttribute(trsv4_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         tv_count_ = alloc<int>(nc_);
@@ -2020,13 +1814,9 @@ class DeviceFactor : public DeviceFactorBase {
                 cur_wave_ = (int)wi;
                 launch("qrcp", [&] { launch_qrcp_cluster(W, tol); });
                 cur_wave_ = -1;
-                // matrices larger than the cluster's shared memory: gather to global memory
-                // and factor there (blocks of other matrices exit at once)
-                launch("qrcp_fallback", [&] {
-                    asn_gather_kernel<T><<<W.n, 256, 0, s_>>>(ctx_, W.items, pieces_, ws_, colcount_, fallback_);
-                    qrcp_kernel<T><<<W.n, 512, W.maxcap * sizeof(T), s_>>>(ctx_, W.items, ws_, norms_, jpvt_, ipvt_,
-                                                                            colcount_, tauws_, rank_, tol, fallback_);
-                }, 2);
+                // matrices larger than the cluster's shared memory: the same algorithm with the
+                // slabs in global memory (clusters of other matrices exit at once)
+                launch("qrcp_global", [&] { launch_qrcp_global(W, tol); });
                 launch("sparsify_scatter", [&] {
                     sparsify_scatter_kernel<T><<<dim3((unsigned)W.n, (unsigned)W.ytiles), 256, 0, s_>>>(
                         ctx_, W.items, pieces_, ws_, ipvt_, rank_, vstore_);
@@ -2266,6 +2056,8 @@ class DeviceFactor : public DeviceFactorBase {
         int maxcap = 1;
         int cs = 1;          // CTAs per thread-block cluster of the shared-memory QRCP
         int smem = 0;        // dynamic shared memory per CTA
+        int gcs = 1;         // cluster of the global-memory QRCP (matrices the first does not hold)
+        int gsmem = 0;       // its dynamic shared memory per CTA
         int ytiles = 0;      // scatter tiles per matrix (reflector + edge-block capacity tiles)
         std::vector<SparsifyItem> host;  // plan items, for tuning
     };
@@ -2394,6 +2186,11 @@ class DeviceFactor : public DeviceFactorBase {
         SPAND_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, qc_smem_cap_));
         SPAND_CUDA(cudaFuncSetAttribute(potrf_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         qc_smem_cap_));
+        SPAND_CUDA(cudaFuncSetAttribute(qrcp_gslab_kernel_ptr<T>(), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        qc_smem_cap_));
+        if (cudaFuncSetAttribute(qrcp_gslab_kernel_ptr<T>(), cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+            cudaSuccess)
+            cudaGetLastError();
         if (cudaFuncSetAttribute(potrf_cluster_kernel<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
             cudaSuccess)
             cudaGetLastError();
@@ -2463,11 +2260,28 @@ class DeviceFactor : public DeviceFactorBase {
         W.cs = bcs;
         W.smem = bsm;
     }
+    void launch_qrcp_global(WaveDev& W, double tol) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)(W.n * W.gcs));
+        cfg.blockDim = dim3(QC_THREADS);
+        cfg.dynamicSmemBytes = (size_t)W.gsmem;
+        cfg.stream = s_;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)W.gcs;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        SPAND_CUDA(cudaLaunchKernelEx(&cfg, qrcp_gslab_kernel_ptr<T>(), ctx_, (const DSpars*)W.items,
+                                      (const DAsn*)pieces_, ws_, ws2_, jpvt_, ipvt_, tauws_, rank_, colcount_,
+                                      fallback_, tol, W.gsmem, (unsigned long long*)nullptr));
+    }
     void launch_qrcp_cluster(WaveDev& W, double tol) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3((unsigned)(W.n * W.cs));
         cfg.blockDim = dim3(QC_THREADS);
-        cfg.dynamicSmemBytes = (size_t)W.smem;
+        cfg.dynamicSmemBytes = force_global_ ? 0 : (size_t)W.smem;
         cfg.stream = s_;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -2482,8 +2296,8 @@ class DeviceFactor : public DeviceFactorBase {
             probe_waves_ += 1;
         }
         SPAND_CUDA(cudaLaunchKernelEx(&cfg, qrcp_smem_kernel_ptr<T>(), ctx_, (const DSpars*)W.items,
-                                      (const DAsn*)pieces_, ws_, jpvt_, ipvt_, tauws_, rank_, colcount_, fallback_, tol,
-                                      W.smem, probe));
+                                      (const DAsn*)pieces_, ws_, (T*)nullptr, jpvt_, ipvt_, tauws_, rank_, colcount_,
+                                      fallback_, tol, force_global_ ? 0 : W.smem, probe));
     }
     void launch_potrf(int* pivots, int* clusters, int n, int smem, const TrtriDev& tri, int pc_cs, int pc_smem) {
         if (pc_cs > 0) {
@@ -2680,7 +2494,8 @@ class DeviceFactor : public DeviceFactorBase {
     int *csize_ = nullptr, *rows0_ = nullptr, *rank_ = nullptr, *cpos_ = nullptr;
     DStatus* status_ = nullptr;
     T* tstore_ = nullptr;
-    T *vstore_ = nullptr, *taustore_ = nullptr, *tauws_ = nullptr, *ws_ = nullptr, *norms_ = nullptr;
+    T *vstore_ = nullptr, *taustore_ = nullptr, *tauws_ = nullptr, *ws_ = nullptr;
+    T* ws2_ = nullptr;  // column slabs of the global-memory QRCP
     int *jpvt_ = nullptr, *ipvt_ = nullptr, *colcount_ = nullptr, *fallback_ = nullptr;
     int* tv_count_ = nullptr;  // finished row tiles per cluster (triangular products)
     cudaStream_t s2_ = nullptr;  // side stream of the WY factors
@@ -2694,6 +2509,9 @@ class DeviceFactor : public DeviceFactorBase {
     int probe_waves_ = 0;
     // per-level kernel classes in the profile (SPAND_PROFILE_LEVELS=1)
     bool per_level_ = getenv("SPAND_PROFILE_LEVELS") != nullptr;
+    // every sparsification matrix through the global-memory QRCP on full clusters
+    // (SPAND_QC_GLOBAL=1; testing and measurement)
+    bool force_global_ = getenv("SPAND_QC_GLOBAL") != nullptr;
     // per-wave QRCP classes and a line per wave after tuning (SPAND_PROFILE_LEVELS=2)
     bool per_wave_ = per_level_ && atoi(getenv("SPAND_PROFILE_LEVELS")) >= 2;
     int cur_wave_ = -1;

@@ -47,12 +47,17 @@ __device__ __forceinline__ void qc_barrier(cooperative_groups::cluster_group& cl
     else __syncthreads();
 }
 
-template <typename T>
-__global__ void __launch_bounds__(QC_THREADS) qrcp_smem_kernel(Ctx<T> c, const DSpars* __restrict__ items,
-                                                               const DAsn* __restrict__ pieces, T* ws, int* jpvt_ws,
-                                                               int* ipvt_ws, T* taus, int* rank_out, int* colcount,
-                                                               int* fallback, double tol, int smem_bytes,
-                                                               unsigned long long* probe) {
+// GS = false: the column slabs live in the CTAs' shared memory; a matrix that does not fit
+// sets fallback[item].  GS = true: the same algorithm with the slabs in global memory (the
+// second workspace gslab, L2-resident), for exactly the matrices flagged by the
+// shared-memory launch; the CTAs read other slabs' columns with L2-only loads.
+template <typename T, bool GS>
+__global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, const DSpars* __restrict__ items,
+                                                                  const DAsn* __restrict__ pieces, T* ws, T* gslab,
+                                                                  int* jpvt_ws, int* ipvt_ws, T* taus,
+                                                                  int* rank_out, int* colcount, int* fallback,
+                                                                  double tol, int smem_bytes,
+                                                                  unsigned long long* probe) {
     namespace cgx = cooperative_groups;
     cgx::cluster_group cl = cgx::this_cluster();
     const int CS = (int)cl.num_blocks();
@@ -65,15 +70,17 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_smem_kernel(Ctx<T> c, const D
     __shared__ int pubx[2][QC_SLOTS];  // exact search with the global threshold
     __shared__ T s_alpha;
     if (c.status->not_spd) return;
+    if (GS && !fallback[item]) return;  // handled by the shared-memory launch
     const DSpars it = items[item];
     const int rows = c.csize[it.cluster];
     int cols = 0;
     for (int p = 0; p < it.count; p++) cols += c.csize[pieces[it.first + p].nbr];
     const int mn = min(rows, cols);
     const int cpc = (cols + CS - 1) / CS;
-    const int lda = rows | 1;
-    const bool fits = qc_need(rows, cols, CS, (int)sizeof(T)) <= smem_bytes;
-    if (threadIdx.x == 0 && me == 0) {
+    const int lda = GS ? c.cap[it.cluster] : (rows | 1);
+    const bool fits = GS ? qc_small_need(rows, cols, CS, (int)sizeof(T)) <= smem_bytes
+                         : qc_need(rows, cols, CS, (int)sizeof(T)) <= smem_bytes;
+    if (!GS && threadIdx.x == 0 && me == 0) {
         fallback[item] = (mn > 0 && tol < 1.0 && !fits) ? 1 : 0;
         colcount[item] = cols;
     }
@@ -91,13 +98,14 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_smem_kernel(Ctx<T> c, const D
         return;
     }
     if (!fits) return;
-    T* A = reinterpret_cast<T*>(smem_raw);
-    T* vsh = A + (size_t)lda * cpc;
+    const int c0 = me * cpc;
+    T* Aitem = gslab + it.ws_off;  // GS: the whole matrix, column j at Aitem + j * lda
+    T* A = GS ? Aitem + (size_t)c0 * lda : reinterpret_cast<T*>(smem_raw);
+    T* vsh = GS ? reinterpret_cast<T*>(smem_raw) : A + (size_t)lda * cpc;
     T* vn1 = vsh + rows;
     T* vn2 = vn1 + cpc;
     int* perm = reinterpret_cast<int*>(vn2 + cpc);
     int* pos = perm + cols;
-    const int c0 = me * cpc;
     const int c1 = min(cols, c0 + cpc);
     const int nloc = max(0, c1 - c0);
     const int tid = threadIdx.x, nth = blockDim.x;
@@ -235,13 +243,14 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_smem_kernel(Ctx<T> c, const D
         // (2) the previous reflector into its column (owner) and the pivot column into vsh,
         // both with the row -> thread map r = tid (mod nth): a thread reads its old vsh rows
         // before it overwrites them
-        const T* src = (own == me ? A : cl.map_shared_rank(A, own)) + (size_t)lj * lda;
+        const T* src = GS ? Aitem + (size_t)phys * lda
+                          : (own == me ? A : cl.map_shared_rank(A, own)) + (size_t)lj * lda;
         T* apend = pend >= 0 ? A + (size_t)pend * lda : nullptr;
         T part = 0;
         for (int r = tid; r < rows; r += nth) {
             if (apend && r > pend_i) apend[r] = vsh[r] * pend_sc;
             if (r >= i) {
-                const T v = src[r];
+                const T v = GS ? __ldcg(src + r) : src[r];
                 vsh[r] = v;
                 if (r == i) s_alpha = v;
                 else part += v * v;
@@ -401,10 +410,17 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_smem_kernel(Ctx<T> c, const D
 
 template <typename T>
 QcKernel<T> qrcp_smem_kernel_ptr() {
-    return qrcp_smem_kernel<T>;
+    return qrcp_cluster_kernel<T, false>;
+}
+
+template <typename T>
+QcKernel<T> qrcp_gslab_kernel_ptr() {
+    return qrcp_cluster_kernel<T, true>;
 }
 
 template QcKernel<float> qrcp_smem_kernel_ptr<float>();
 template QcKernel<double> qrcp_smem_kernel_ptr<double>();
+template QcKernel<float> qrcp_gslab_kernel_ptr<float>();
+template QcKernel<double> qrcp_gslab_kernel_ptr<double>();
 
 }  // namespace spand

@@ -17,11 +17,24 @@ __host__ __device__ inline long long qc_need(int rows, int cols, int cs, int ele
     return ((long long)(rows | 1) * cpc + rows + 2 * cpc) * elem + ((long long)cols + cpc) * 4;
 }
 
-template <typename T>
-using QcKernel = void (*)(Ctx<T>, const DSpars*, const DAsn*, T*, int*, int*, T*, int*, int*, int*, double, int,
-                          unsigned long long*);
+// Shared memory of one CTA of the global-slab variant: the reflector, the two norm
+// arrays, the replicated permutation and the slab's column positions.
+__host__ __device__ inline long long qc_small_need(int rows, int cols, int cs, int elem) {
+    const long long cpc = (cols + cs - 1) / cs;
+    return ((long long)rows + 2 * cpc) * elem + ((long long)cols + cpc) * 4;
+}
 
+// (ctx, items, pieces, ws, gslab, jpvt, ipvt, tau, rank, colcount, fallback, tol,
+//  dynamic shared bytes, probe)
+template <typename T>
+using QcKernel = void (*)(Ctx<T>, const DSpars*, const DAsn*, T*, T*, int*, int*, T*, int*, int*, int*, double,
+                          int, unsigned long long*);
+
+// column slabs in the cluster's shared memory
 template <typename T>
 QcKernel<T> qrcp_smem_kernel_ptr();
+// column slabs in global memory, for the matrices the shared-memory launch flagged
+template <typename T>
+QcKernel<T> qrcp_gslab_kernel_ptr();
 
 }  // namespace spand

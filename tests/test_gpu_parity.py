@@ -65,6 +65,19 @@ CASES_F = [c + (1,) for c in CASES] + [(32, 3, 8, 1e-2, 0, 2)]
 
 @pytest.mark.parametrize("n,dim,nlevels,tol,skip,nf", CASES_F)
 def test_factor_parity_fp64(n, dim, nlevels, tol, skip, nf):
+    _check_parity(n, dim, nlevels, tol, skip, nf)
+
+
+@pytest.mark.parametrize("n,dim,nlevels,tol", [(16, 3, 6, 1e-2), (64, 2, 7, 1e-2)])
+def test_factor_parity_fp64_global_qrcp(n, dim, nlevels, tol, monkeypatch):
+    """Every sparsification matrix through the QRCP variant whose column slabs live in
+    global memory (the path of matrices too large for a cluster's shared memory), on
+    full clusters."""
+    monkeypatch.setenv("SPAND_QC_GLOBAL", "1")
+    _check_parity(n, dim, nlevels, tol, 0, 2)
+
+
+def _check_parity(n, dim, nlevels, tol, skip, nf):
     A, t, o = _build(n, dim, nlevels, tol, skip, factorizations=nf)
     assert np.array_equal(t.get_assembly_perm(), o.get_assembly_perm())
     # ranks
