@@ -1244,6 +1244,267 @@ __global__ void merge_x_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ chil
 }
 
 // ------------------------------------------------------------------------------------
+// Solve sweeps for many right-hand sides (16 or more).  Right-hand sides in blocks of 32,
+// one per lane; factor tiles and x tiles staged in shared memory with coalesced loads, so
+// that every factor element is read once per 32 right-hand sides.  8 warps; warp w owns
+// the tile rows w + 8u.  Same operations, same order of ops, as the one-right-hand-side
+// kernels above; sums within an op run in chunks of MR_KC.
+// ------------------------------------------------------------------------------------
+constexpr int MR_RB = 32;      // right-hand sides per block (lanes)
+constexpr int MR_KC = 32;      // reduction chunk
+constexpr int MR_MAXROWS = 64; // rows of one tile (2 * TV_ROWS for single-tile clusters)
+constexpr int MR_U = MR_MAXROWS / 8;
+
+// acc[u] += sum_{k in [k0, k1)} F(r0 + w + 8u, k) * x[k][rb0 + lane] with F(i, k) at
+// A[i + k*ld] (row_fast) or A[k + i*ld]; pred: 0 all, 1 k < i only, 2 k > i only.
+// x column j of the block at xcol + j * xld.  Leaves the tiles free (ends with a barrier).
+template <typename T>
+__device__ __forceinline__ void mr_accum(T (&acc)[MR_U], const T* __restrict__ A, int ld, bool row_fast, int r0,
+                                         int nr, int k0, int k1, int pred, const T* __restrict__ xcol, long long xld,
+                                         int nrb, T (*xs)[MR_RB + 1], T (*fs)[MR_KC + 1]) {
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    for (int kb = k0; kb < k1; kb += MR_KC) {
+        const int kw = min(MR_KC, k1 - kb);
+        for (int idx = tid; idx < MR_KC * MR_RB; idx += blockDim.x) {
+            const int kk = idx % MR_KC, j = idx / MR_KC;
+            xs[kk][j] = (kk < kw && j < nrb) ? xcol[(kb + kk) + (size_t)j * xld] : T(0);
+        }
+        if (row_fast) {
+            for (int idx = tid; idx < MR_KC * nr; idx += blockDim.x) {
+                const int i = idx % nr, kk = idx / nr;
+                const int k = kb + kk, row = r0 + i;
+                const bool ok = kk < kw && (pred == 0 || (pred == 1 ? k < row : k > row));
+                fs[i][kk] = ok ? A[row + (size_t)k * ld] : T(0);
+            }
+        } else {
+            for (int idx = tid; idx < MR_KC * nr; idx += blockDim.x) {
+                const int kk = idx % MR_KC, i = idx / MR_KC;
+                const int k = kb + kk, row = r0 + i;
+                const bool ok = kk < kw && (pred == 0 || (pred == 1 ? k < row : k > row));
+                fs[i][kk] = ok ? A[k + (size_t)row * ld] : T(0);
+            }
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int kk = 0; kk < MR_KC; kk++) {
+            const T xv = xs[kk][lane];
+#pragma unroll
+            for (int u = 0; u < MR_U; u++)
+                if (w + 8 * u < nr) acc[u] += fs[w + 8 * u][kk] * xv;
+        }
+        __syncthreads();
+    }
+}
+
+// Triangular products (as trsv4_kernel) for many right-hand sides: one CTA per (cluster,
+// row tile), every right-hand-side block in turn; multi-tile clusters go through the
+// scratch copy and the last tile copies back.
+template <typename T>
+__global__ void __launch_bounds__(256) trsv_mrhs_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ clusters,
+                                                        const int* __restrict__ lblocks,
+                                                        const int2* __restrict__ tiles, int trans, T* tmp,
+                                                        int* counters) {
+    __shared__ T xs[MR_KC][MR_RB + 1];
+    __shared__ T fs[MR_MAXROWS][MR_KC + 1];
+    const int2 tl = tiles[blockIdx.x];
+    const int cl = clusters[tl.x];
+    const int n = c.rows0[cl];
+    const int nt = n <= 2 * TV_ROWS ? 1 : (n + TV_ROWS - 1) / TV_ROWS;
+    if (n == 0 || tl.y >= nt) return;
+    const int r0 = nt == 1 ? 0 : tl.y * TV_ROWS, r1 = nt == 1 ? n : min(n, r0 + TV_ROWS), nr = r1 - r0;
+    const T* L = bptr(c, lblocks[tl.x]);
+    const int ld = c.blk[lblocks[tl.x]].ld;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int rb0 = 0; rb0 < X.nrhs; rb0 += MR_RB) {
+        const int nrb = min(MR_RB, X.nrhs - rb0);
+        const T* xcol = X.xs + X.xoff[cl] + (size_t)rb0 * X.xld;
+        T acc[MR_U];
+#pragma unroll
+        for (int u = 0; u < MR_U; u++) acc[u] = T(0);
+        // forward: L^{-1}[i][k] (k < i) at L[k + i*ld]; backward: L^{-1}[k][i] (k > i) at L[i + k*ld]
+        if (!trans) mr_accum(acc, L, ld, false, r0, nr, 0, r1, 1, xcol, X.xld, nrb, xs, fs);
+        else mr_accum(acc, L, ld, true, r0, nr, r0 + 1, n, 2, xcol, X.xld, nrb, xs, fs);
+        T* ycol = (nt == 1 ? X.xs : tmp) + X.xoff[cl] + (size_t)rb0 * X.xld;
+        if (lane < nrb)
+#pragma unroll
+            for (int u = 0; u < MR_U; u++) {
+                const int row = r0 + w + 8 * u;
+                if (w + 8 * u < nr) {
+                    const size_t o = row + (size_t)lane * X.xld;
+                    ycol[o] = acc[u] + xcol[o] / L[row + (size_t)row * ld];
+                }
+            }
+        __syncthreads();
+    }
+    if (nt == 1) return;
+    __threadfence();
+    __syncthreads();
+    __shared__ int last;
+    if (threadIdx.x == 0) last = atomicAdd(&counters[cl], 1) == nt - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    for (int rhs = 0; rhs < X.nrhs; rhs++) {
+        const size_t off = X.xoff[cl] + (size_t)rhs * X.xld;
+        for (int k = threadIdx.x; k < n; k += blockDim.x) X.xs[off + k] = __ldcg(tmp + off + k);
+    }
+    if (threadIdx.x == 0) counters[cl] = 0;
+}
+
+// Gemm sweeps (as gemm_fwd2 / gemm_bwd2) for many right-hand sides: one CTA per (group,
+// 32 rows of the updated slot), ops of the group in order, all right-hand-side blocks.
+// fwd: x_n -= A_ns x_s (kind 1, A[i + j*ld]) or A_sn^T x_s (kind 2, A[j + i*ld]);
+// bwd: x_s -= A_ns^T x_n (kind 1, A[j + i*ld]) or A_sn x_n (kind 2, A[i + j*ld]).
+template <typename T>
+__global__ void __launch_bounds__(256) gemm_mrhs_kernel(Ctx<T> c, XCtx<T> X, const DGroup* __restrict__ groups,
+                                                        const DGemmOp* __restrict__ ops,
+                                                        const DTile* __restrict__ tiles, int fwd) {
+    __shared__ T xs[MR_KC][MR_RB + 1];
+    __shared__ T fs[MR_MAXROWS][MR_KC + 1];
+    const DTile tl = tiles[blockIdx.x];
+    const DGroup G = groups[tl.item];
+    const int key = G.key;
+    const int nk = fwd ? c.rows0[key] : c.csize[key];
+    const int i0 = tl.tile_i * 32;
+    if (i0 >= nk) return;
+    const int nr = min(32, nk - i0);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    T* ycol0 = X.xs + X.xoff[key];
+    for (int rb0 = 0; rb0 < X.nrhs; rb0 += MR_RB) {
+        const int nrb = min(MR_RB, X.nrhs - rb0);
+        T acc[MR_U];
+#pragma unroll
+        for (int u = 0; u < MR_U; u++) acc[u] = T(0);
+        for (int o = 0; o < G.count; o++) {
+            const DGemmOp op = ops[G.first + o];
+            const int other = fwd ? op.self : op.nbr;
+            const int nj = fwd ? c.csize[op.self] : c.rows0[op.nbr];
+            const T* xcol = X.xs + X.xoff[other] + (size_t)rb0 * X.xld;
+            const bool row_fast = fwd ? op.kind == 1 : op.kind == 2;
+            mr_accum(acc, bptr(c, op.block), c.blk[op.block].ld, row_fast, i0, nr, 0, nj, 0, xcol, X.xld, nrb, xs,
+                     fs);
+        }
+        if (lane < nrb)
+#pragma unroll
+            for (int u = 0; u < MR_U; u++)
+                if (w + 8 * u < nr) ycol0[(i0 + w + 8 * u) + (size_t)(rb0 + lane) * X.xld] -= acc[u];
+    }
+}
+
+// Orthogonal op (as ortho_wyb_kernel) for many right-hand sides: one CTA per cluster, x of
+// a right-hand-side block resident in shared memory (rows x 33), every 32-reflector block:
+// W = V_b^T X, Y = T_b^T W or T_b W, X -= V_b Y.
+template <typename T>
+__global__ void __launch_bounds__(256) ortho_mrhs_kernel(Ctx<T> c, XCtx<T> X, const DOrtho* __restrict__ items,
+                                                         const T* vstore, const T* tstore, int trans) {
+    __shared__ T vt[MR_KC][QB + 1];
+    __shared__ T Wm[QB][MR_RB + 1];
+    __shared__ T Ym[QB][MR_RB + 1];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T (*Xs)[MR_RB + 1] = reinterpret_cast<T (*)[MR_RB + 1]>(smem_raw);
+    const DOrtho it = items[blockIdx.x];
+    const int rows = c.rows0[it.cluster];
+    const int k = c.csize[it.cluster];
+    if (k >= rows || k == 0) return;
+    const int ld = c.cap[it.cluster];
+    const T* V = vstore + it.v_off;
+    const T* Tm = tstore + it.v_off;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int nb = (k + QB - 1) / QB;
+    for (int rb0 = 0; rb0 < X.nrhs; rb0 += MR_RB) {
+        const int nrb = min(MR_RB, X.nrhs - rb0);
+        T* xcol = X.xs + X.xoff[it.cluster] + (size_t)rb0 * X.xld;
+        __syncthreads();
+        for (int idx = tid; idx < rows * MR_RB; idx += blockDim.x) {
+            const int r = idx % rows, j = idx / rows;
+            Xs[r][j] = j < nrb ? xcol[r + (size_t)j * X.xld] : T(0);
+        }
+        for (int q = 0; q < nb; q++) {
+            const int b = trans ? q : nb - 1 - q;
+            const int i0 = b * QB, bw = min(QB, k - i0);
+            // W[i][l] = sum_{r >= i0+i} v_i[r] X[r][l]   (v_i[i0+i] = 1)
+            T acc[4] = {0, 0, 0, 0};
+            for (int rb = i0; rb < rows; rb += MR_KC) {
+                __syncthreads();
+                for (int idx = tid; idx < MR_KC * QB; idx += blockDim.x) {
+                    const int kk = idx % MR_KC, ii = idx / MR_KC;
+                    const int r = rb + kk, col = i0 + ii;
+                    T v = T(0);
+                    if (ii < bw && r < rows) v = r > col ? V[r + (size_t)col * ld] : (r == col ? T(1) : T(0));
+                    vt[kk][ii] = v;
+                }
+                __syncthreads();
+                const int kw = min(MR_KC, rows - rb);
+                for (int kk = 0; kk < kw; kk++) {
+                    const T xv = Xs[rb + kk][lane];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) acc[u] += vt[kk][w + 8 * u] * xv;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) Wm[w + 8 * u][lane] = acc[u];
+            __syncthreads();
+            // Y = T_b^T W (fwd) or T_b W (bwd)
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int i = w + 8 * u;
+                T y = T(0);
+                if (i < bw) {
+                    if (trans)
+                        for (int j = 0; j <= i; j++) y += Tm[(i0 + j) + (size_t)(i0 + i) * ld] * Wm[j][lane];
+                    else
+                        for (int j = i; j < bw; j++) y += Tm[(i0 + i) + (size_t)(i0 + j) * ld] * Wm[j][lane];
+                }
+                Ym[i][lane] = y;
+            }
+            __syncthreads();
+            // X[r][l] -= sum_i v_i[r] Y[i][l]
+            for (int rb = i0; rb < rows; rb += MR_KC) {
+                __syncthreads();
+                for (int idx = tid; idx < MR_KC * QB; idx += blockDim.x) {
+                    const int kk = idx % MR_KC, ii = idx / MR_KC;
+                    const int r = rb + kk, col = i0 + ii;
+                    T v = T(0);
+                    if (ii < bw && r < rows) v = r > col ? V[r + (size_t)col * ld] : (r == col ? T(1) : T(0));
+                    vt[kk][ii] = v;
+                }
+                __syncthreads();
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int kk = w + 8 * u;
+                    if (rb + kk < rows) {
+                        T s2 = T(0);
+                        for (int ii = 0; ii < QB; ii++) s2 += vt[kk][ii] * Ym[ii][lane];
+                        Xs[rb + kk][lane] -= s2;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        for (int idx = tid; idx < rows * MR_RB; idx += blockDim.x) {
+            const int r = idx % rows, j = idx / rows;
+            if (j < nrb) xcol[r + (size_t)j * X.xld] = Xs[r][j];
+        }
+    }
+}
+
+// Merge op for many right-hand sides: one CTA per child, every right-hand side.
+template <typename T>
+__global__ void merge_x_mrhs_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ children,
+                                    const int* __restrict__ parent_of, const int* __restrict__ cpos, int fwd) {
+    const int ch = children[blockIdx.x];
+    const int p = parent_of[blockIdx.x];
+    const int n = c.csize[ch];
+    for (int idx = threadIdx.x; idx < n * X.nrhs; idx += blockDim.x) {
+        const int i = idx % n, r = idx / n;
+        T* xc = X.xs + X.xoff[ch] + (size_t)r * X.xld;
+        T* xp = X.xs + X.xoff[p] + cpos[ch] + (size_t)r * X.xld;
+        if (fwd) xp[i] = xc[i];
+        else xc[i] = xp[i];
+    }
+}
+
+// ------------------------------------------------------------------------------------
 // FP64 Krylov kernels
 // ------------------------------------------------------------------------------------
 __global__ void spmv_kernel(int n, const int* __restrict__ rp, const int* __restrict__ ci, const double* __restrict__ v,
@@ -1706,6 +1967,9 @@ class DeviceFactor : public DeviceFactorBase {
                 D.n_gf_tiles = (int)tf.size();
                 D.gb_tiles = up(tb);
                 D.n_gb_tiles = (int)tb.size();
+                auto tf32 = tiles_1d(ef, 32);
+                D.gf_tiles32 = up(tf32);
+                D.n_gf_tiles32 = (int)tf32.size();
             }
             {
                 std::vector<DOrtho> ot;
@@ -1718,6 +1982,8 @@ class DeviceFactor : public DeviceFactorBase {
                 D.n_ortho = (int)ot.size();
                 D.ortho = up(ot);
                 D.x_smem_ortho = mx * (int)sizeof(T);
+                const int64_t mr = (int64_t)mx * (MR_RB + 1) * (int64_t)sizeof(T);
+                D.ortho_mrhs_smem = mr <= 200 * 1024 ? (int)mr : 0;
             }
         }
         jpvt_ = alloc<int>(max_cols);
@@ -1739,6 +2005,7 @@ class DeviceFactor : public DeviceFactorBase {
         SPAND_CUDA(cudaFuncSetAttribute(trsm3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         fallback_ = alloc<int>(max_items);
         SPAND_CUDA(cudaFuncSetAttribute(trsv4_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SPAND_CUDA(cudaFuncSetAttribute(ortho_mrhs_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         tv_count_ = alloc<int>(nc_);
         {
             int mx = 1;
@@ -2091,6 +2358,9 @@ class DeviceFactor : public DeviceFactorBase {
         int n_elim_llt = 0, n_scale_llt = 0;
         int *elim_llt = nullptr, *elim_llt_blk = nullptr, *scale_llt = nullptr, *scale_llt_blk = nullptr;
         int x_smem_elim = 0, x_smem_scale = 0, x_smem_ortho = 0;
+        DTile* gf_tiles32 = nullptr;  // forward Gemm groups in 32-row tiles (many right-hand sides)
+        int n_gf_tiles32 = 0;
+        int ortho_mrhs_smem = 0;      // x of 32 right-hand sides (rows x 33); 0: one at a time
         int2 *elim_tv = nullptr, *scale_tv = nullptr;  // (item, row tile) of the triangular products
         int n_elim_tv = 0, n_scale_tv = 0;
         int n_gf = 0, n_gb = 0;
@@ -2409,66 +2679,72 @@ class DeviceFactor : public DeviceFactorBase {
         XCtx<T> X{slots, (long long)xld_, d_xoff_, nrhs};
         const int n = (int)perm_h_.size();
         const long long tot = (long long)n * nrhs;
+        // 16 or more right-hand sides: the kernels that read each factor block once per 32
+        const bool mr = nrhs >= 16;
         launch("perm", [&] {
             perm_in_kernel<T><<<(unsigned)((tot + 255) / 256), 256, 0, s_>>>(x, ld, X, d_perm_, d_slot_, n);
         });
+        auto trsv = [&](const int* clusters, const int* blks, const int2* tv, int ntv, int smem, int trans) {
+            if (!ntv) return;
+            launch("trsv", [&] {
+                if (mr)
+                    trsv_mrhs_kernel<T><<<ntv, 256, 0, s_>>>(ctx_, X, clusters, blks, tv, trans, tmp, tv_count_);
+                else
+                    trsv4_kernel<T><<<ntv, TV_THREADS, smem, s_>>>(ctx_, X, clusters, blks, tv, trans, tmp, tv_count_);
+            });
+        };
+        auto ortho = [&](const LevelDev& D, int trans) {
+            if (!D.n_ortho) return;
+            launch("ortho", [&] {
+                if (mr && D.ortho_mrhs_smem)
+                    ortho_mrhs_kernel<T><<<D.n_ortho, 256, D.ortho_mrhs_smem, s_>>>(ctx_, X, D.ortho, vstore_, tstore_,
+                                                                                    trans);
+                else
+                    ortho_wyb_kernel<T><<<D.n_ortho * nrhs, 512, D.x_smem_ortho, s_>>>(ctx_, X, D.ortho, D.n_ortho,
+                                                                                      vstore_, tstore_, trans);
+            });
+        };
+        auto merge = [&](const LevelDev& D, int fwd) {
+            if (!(D.merged && D.n_children)) return;
+            launch("merge_x", [&] {
+                if (mr)
+                    merge_x_mrhs_kernel<T><<<D.n_children, 256, 0, s_>>>(ctx_, X, D.child_idx, D.child_parent, cpos_, fwd);
+                else
+                    merge_x_kernel<T><<<D.n_children * nrhs, 128, 0, s_>>>(ctx_, X, D.child_idx, D.child_parent,
+                                                                           D.n_children, cpos_, fwd);
+            });
+        };
         for (int l = 0; l < P.nlevels; l++) {
             LevelDev& D = levels_[l];
             cur_level_ = l;
-            if (D.n_elim_tv)
-                launch("trsv", [&] {
-                    trsv4_kernel<T><<<D.n_elim_tv, TV_THREADS, D.x_smem_elim, s_>>>(ctx_, X, D.elim_llt, D.elim_llt_blk,
-                                                                                   D.elim_tv, 0, tmp, tv_count_);
-                });
+            trsv(D.elim_llt, D.elim_llt_blk, D.elim_tv, D.n_elim_tv, D.x_smem_elim, 0);
             if (D.n_gf)
                 launch("gemm_fwd", [&] {
-                    gemm_fwd2_kernel<T><<<D.n_gf_tiles * nrhs, 256, 0, s_>>>(ctx_, X, D.gf, D.gfo, D.gf_tiles,
-                                                                             D.n_gf_tiles, 0);
+                    if (mr)
+                        gemm_mrhs_kernel<T><<<D.n_gf_tiles32, 256, 0, s_>>>(ctx_, X, D.gf, D.gfo, D.gf_tiles32, 1);
+                    else
+                        gemm_fwd2_kernel<T><<<D.n_gf_tiles * nrhs, 256, 0, s_>>>(ctx_, X, D.gf, D.gfo, D.gf_tiles,
+                                                                                 D.n_gf_tiles, 0);
                 });
-            if (D.n_scale_tv)
-                launch("trsv", [&] {
-                    trsv4_kernel<T><<<D.n_scale_tv, TV_THREADS, D.x_smem_scale, s_>>>(
-                        ctx_, X, D.scale_llt, D.scale_llt_blk, D.scale_tv, 0, tmp, tv_count_);
-                });
-            if (D.n_ortho)
-                launch("ortho", [&] {
-                    ortho_wyb_kernel<T><<<D.n_ortho * nrhs, 512, D.x_smem_ortho, s_>>>(ctx_, X, D.ortho, D.n_ortho,
-                                                                                          vstore_, tstore_, 1);
-                });
-            if (D.merged && D.n_children)
-                launch("merge_x", [&] {
-                    merge_x_kernel<T><<<D.n_children * nrhs, 128, 0, s_>>>(ctx_, X, D.child_idx, D.child_parent,
-                                                                           D.n_children, cpos_, 1);
-                });
+            trsv(D.scale_llt, D.scale_llt_blk, D.scale_tv, D.n_scale_tv, D.x_smem_scale, 0);
+            ortho(D, 1);
+            merge(D, 1);
         }
         for (int l = P.nlevels - 1; l >= 0; l--) {
             LevelDev& D = levels_[l];
             cur_level_ = l;
-            if (D.merged && D.n_children)
-                launch("merge_x", [&] {
-                    merge_x_kernel<T><<<D.n_children * nrhs, 128, 0, s_>>>(ctx_, X, D.child_idx, D.child_parent,
-                                                                           D.n_children, cpos_, 0);
-                });
-            if (D.n_ortho)
-                launch("ortho", [&] {
-                    ortho_wyb_kernel<T><<<D.n_ortho * nrhs, 512, D.x_smem_ortho, s_>>>(ctx_, X, D.ortho, D.n_ortho,
-                                                                                          vstore_, tstore_, 0);
-                });
-            if (D.n_scale_tv)
-                launch("trsv", [&] {
-                    trsv4_kernel<T><<<D.n_scale_tv, TV_THREADS, D.x_smem_scale, s_>>>(
-                        ctx_, X, D.scale_llt, D.scale_llt_blk, D.scale_tv, 1, tmp, tv_count_);
-                });
+            merge(D, 0);
+            ortho(D, 0);
+            trsv(D.scale_llt, D.scale_llt_blk, D.scale_tv, D.n_scale_tv, D.x_smem_scale, 1);
             if (D.n_gb)
                 launch("gemm_bwd", [&] {
-                    gemm_bwd2_kernel<T><<<D.n_gb_tiles * nrhs, 256, 0, s_>>>(ctx_, X, D.gb, D.gbo, D.gb_tiles,
-                                                                             D.n_gb_tiles);
+                    if (mr)
+                        gemm_mrhs_kernel<T><<<D.n_gb_tiles, 256, 0, s_>>>(ctx_, X, D.gb, D.gbo, D.gb_tiles, 0);
+                    else
+                        gemm_bwd2_kernel<T><<<D.n_gb_tiles * nrhs, 256, 0, s_>>>(ctx_, X, D.gb, D.gbo, D.gb_tiles,
+                                                                                 D.n_gb_tiles);
                 });
-            if (D.n_elim_tv)
-                launch("trsv", [&] {
-                    trsv4_kernel<T><<<D.n_elim_tv, TV_THREADS, D.x_smem_elim, s_>>>(ctx_, X, D.elim_llt, D.elim_llt_blk,
-                                                                                   D.elim_tv, 1, tmp, tv_count_);
-                });
+            trsv(D.elim_llt, D.elim_llt_blk, D.elim_tv, D.n_elim_tv, D.x_smem_elim, 1);
         }
         cur_level_ = -1;
         launch("perm", [&] {

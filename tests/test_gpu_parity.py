@@ -220,26 +220,49 @@ def test_reassemble_same_pattern():
     assert np.linalg.norm(xt - xo) / np.linalg.norm(xo) < TOL_SOLVE
 
 
-@pytest.mark.parametrize("fp32", [False, True])
-def test_cg_multi_matches_single(fp32):
+@pytest.mark.parametrize("fp32,k", [(False, 5), (True, 5), (False, 20), (True, 20)])
+def test_cg_multi_matches_single(fp32, k):
     """Several right-hand sides at once: every column takes the iterations and reaches the
     solution of its own single-right-hand-side CG (the columns share the preconditioner
-    applications only); a zero column stays zero after 0 iterations."""
+    applications only); a zero column stays zero after 0 iterations.  20 columns take the
+    many-right-hand-side solve kernels (one block of 32, 20 lanes live)."""
     from spand_public_gb300 import problems as P
     A, t, o = _build(16, 3, 6, 1e-2, fp32=fp32)
-    B = P.rhs(A.shape[0], 5, seed=7)
+    B = P.rhs(A.shape[0], k, seed=7)
     B[:, 3] = 0.0
     X, its, rr = t.cg(B, iters=200, tol=1e-10)
-    assert X.shape == B.shape and its.shape == (5,)
-    for j in range(5):
+    assert X.shape == B.shape and its.shape == (k,)
+    for j in range(k):
         if j == 3:
             assert its[j] == 0 and not np.any(X[:, j])
             continue
         xj, itj, rj = t.cg(B[:, j], iters=200, tol=1e-10)
-        assert its[j] == itj, (j, its[j], itj)
-        assert np.linalg.norm(X[:, j] - xj) <= 1e-12 * np.linalg.norm(xj)
-        assert abs(rr[j] - rj) <= 1e-12 + 1e-9 * rj
+        if k < 16:  # the same kernels: the same arithmetic as one column at a time
+            assert its[j] == itj, (j, its[j], itj)
+            assert np.linalg.norm(X[:, j] - xj) <= 1e-12 * np.linalg.norm(xj)
+            assert abs(rr[j] - rj) <= 1e-12 + 1e-9 * rj
+        else:  # chunked sums: rounding may move the stopping test by one iteration
+            assert abs(int(its[j]) - itj) <= 1, (j, its[j], itj)
+            assert np.linalg.norm(X[:, j] - xj) <= 1e-8 * np.linalg.norm(xj)
         assert np.linalg.norm(A @ X[:, j] - B[:, j]) / np.linalg.norm(B[:, j]) < 1e-9
-        if not fp32:
+        if not fp32 and k < 16:
             _, ito = o.cg(B[:, j], 200, 1e-10)
             assert its[j] == ito
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+def test_solve_many_rhs(fp32):
+    """The preconditioner on 40 right-hand sides at once (the many-right-hand-side kernels:
+    one full block of 32 and one of 8) against the columns solved one at a time and, for
+    the FP64 factor, against the oracle."""
+    from spand_public_gb300 import problems as P
+    A, t, o = _build(16, 3, 6, 1e-2, fp32=fp32)
+    B = P.rhs(A.shape[0], 40, seed=9)
+    X = t.solve(B)
+    tol = 1e-5 if fp32 else 1e-12
+    for j in range(0, 40, 7):
+        xj = t.solve(B[:, j])
+        assert np.linalg.norm(X[:, j] - xj) <= tol * np.linalg.norm(xj)
+    if not fp32:
+        Xo = o.solve(B)
+        assert np.linalg.norm(X - Xo) <= TOL_SOLVE * np.linalg.norm(Xo)
