@@ -111,6 +111,16 @@ int spand_cg_multi(spand_tree* t, const double* b, double* x, int nrhs, int ld, 
 int spand_cg_multi_device(spand_tree* t, const double* b_dev, double* x_dev, int nrhs, int iters, double tol,
                           int* iters_out, double* relres_out);
 
+/* No counterpart in the reference: many independent systems at once (e.g. a batch of
+ * small problems).  spand_batch_factorize queues every tree's factorization on its own
+ * stream before it waits for any; status_out[count] receives each tree's status (the call
+ * returns the first failure's status and message).  spand_batch_cg runs tree k's cg on
+ * host vectors b[k] -> x[k] (its own size, x[k] holds the initial guess) for all trees in
+ * lockstep, one host wait per iteration for the whole batch. */
+int spand_batch_factorize(spand_tree* const* trees, int count, int* status_out);
+int spand_batch_cg(spand_tree* const* trees, int count, const double* const* b, double* const* x, int iters,
+                   double tol, int* iters_out, double* relres_out);
+
 /* Introspection (reference: get_N, get_assembly_perm, nnz, get_stop, print_log fields;
  * include/tree.h:150-165, src/tree.cpp:1645-1727) */
 int spand_tree_get_N(spand_tree* t, int* n);

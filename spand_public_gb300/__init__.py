@@ -55,6 +55,9 @@ _PROTOS = {
                            C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "spand_cg_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
                                   C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "spand_batch_factorize": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "spand_batch_cg": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p,
+                                 C.c_void_p]),
     "spand_tree_assemble_values": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_int]),
     "spand_cg_multi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,
                                  C.c_void_p, C.c_void_p]),
@@ -341,3 +344,31 @@ class Tree:
         v = C.c_longlong()
         _check(self.L.spand_tree_device_bytes(self.h, C.byref(v)))
         return v.value
+
+
+def batch_factorize(trees):
+    """Factorize many trees at once (every tree's launches queued on its own stream before
+    the first wait).  Returns the status of every tree (0: factored)."""
+    L = lib()
+    hs = (C.c_void_p * len(trees))(*[t.h for t in trees])
+    st = np.zeros(len(trees), dtype=np.int32)
+    rc = L.spand_batch_factorize(hs, len(trees), _ptr(st))
+    if rc not in (0, 4):
+        _check(rc)
+    return st
+
+
+def batch_cg(trees, bs, iters=100, tol=1e-12):
+    """cg on many independent systems in lockstep: tree k solves with bs[k].  Returns
+    ([x_k], iterations, recurrence residuals)."""
+    L = lib()
+    k = len(trees)
+    bs = [np.ascontiguousarray(b, dtype=np.float64) for b in bs]
+    xs = [np.zeros_like(b) for b in bs]
+    hs = (C.c_void_p * k)(*[t.h for t in trees])
+    bp = (C.c_void_p * k)(*[b.ctypes.data for b in bs])
+    xp = (C.c_void_p * k)(*[x.ctypes.data for x in xs])
+    its = np.zeros(k, dtype=np.int32)
+    rr = np.zeros(k, dtype=np.float64)
+    _check(L.spand_batch_cg(hs, k, bp, xp, int(iters), float(tol), _ptr(its), _ptr(rr)))
+    return xs, its, rr

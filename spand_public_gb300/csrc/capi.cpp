@@ -185,6 +185,37 @@ int spand_tree_assemble_values(spand_tree* t, const double* vals, long long nnz,
     return guard([&] { t->t->assemble_values(vals, (int64_t)nnz, on_device != 0); });
 }
 
+int spand_batch_factorize(spand_tree* const* trees, int count, int* status_out) {
+    if (!trees || !status_out || count < 0) return fail(SPAND_ERR_ARG, "null argument");
+    std::vector<spaND::Tree*> ts(count);
+    for (int k = 0; k < count; k++) {
+        if (!trees[k]) return fail(SPAND_ERR_ARG, "null tree");
+        ts[k] = trees[k]->t;
+    }
+    return guard([&] {
+        std::vector<std::string> msg(count);
+        spaND::batch_factorize(ts.data(), count, status_out, msg.data());
+        std::string first;
+        for (int k = 0; k < count; k++) {
+            if (!status_out[k]) continue;
+            status_out[k] = msg[k].find("Non-SPD") != std::string::npos ? SPAND_ERR_NOT_SPD : SPAND_ERR_CUDA;
+            if (first.empty()) first = "tree " + std::to_string(k) + ": " + msg[k];
+        }
+        if (!first.empty()) throw std::runtime_error(first);
+    });
+}
+
+int spand_batch_cg(spand_tree* const* trees, int count, const double* const* b, double* const* x, int iters,
+                   double tol, int* iters_out, double* relres_out) {
+    if (!trees || !b || !x || !iters_out || !relres_out || count < 0) return fail(SPAND_ERR_ARG, "null argument");
+    std::vector<spaND::Tree*> ts(count);
+    for (int k = 0; k < count; k++) {
+        if (!trees[k] || !b[k] || !x[k]) return fail(SPAND_ERR_ARG, "null tree or vector");
+        ts[k] = trees[k]->t;
+    }
+    return guard([&] { spaND::batch_cg(ts.data(), count, b, x, iters, tol, iters_out, relres_out); });
+}
+
 int spand_cg_multi(spand_tree* t, const double* b, double* x, int nrhs, int ld, int iters, double tol,
                    int* iters_out, double* relres_out) {
     CHECK_T(t);

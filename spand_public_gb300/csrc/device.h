@@ -84,7 +84,14 @@ class DeviceFactorBase {
     virtual void assemble_values(const double* vals, int64_t nnz, bool on_device = false) = 0;
     // device copy of the last uploaded values of A (CSC order)
     virtual const double* device_values() const = 0;
-    virtual void factorize(double tol) = 0;  // throws DeviceError
+    // every launch of the factorization on this object's stream, the status read queued
+    // behind them; factorize_finish waits for it (throws DeviceError on a non-SPD pivot)
+    virtual void factorize_enqueue(double tol) = 0;
+    virtual void factorize_finish() = 0;
+    void factorize(double tol) {
+        factorize_enqueue(tol);
+        factorize_finish();
+    }
     // x: device pointer, natural ordering, n x nrhs (ld), FP64; in-place M^{-1} x
     virtual void solve_device(double* x, int nrhs, int ld) = 0;
     virtual void sizes(std::vector<int>& csize, std::vector<int>& rows0) = 0;
@@ -126,6 +133,31 @@ struct PcgResult {
 
 PcgResult device_pcg(DeviceFactorBase& M, const DeviceCsr& A, const double* b, double* x, int maxit, double tol,
                      bool use_graph);
+
+// Work vectors of one device CG (n doubles each, scalars on the device and pinned on the host)
+struct PcgWork {
+    int n = 0;
+    double *r = nullptr, *p = nullptr, *z = nullptr, *tmp = nullptr, *partial = nullptr, *sc = nullptr;
+    double* h_sc = nullptr;
+    ~PcgWork() { release(); }
+    void release();
+    void ensure(int n);
+};
+
+// One system of a batch: its preconditioner, matrix, work vectors, b and x (device,
+// FP64, natural ordering); res receives its iterations and |r|/|b|.
+struct PcgSystem {
+    DeviceFactorBase* M;
+    const DeviceCsr* A;
+    PcgWork* w;
+    const double* b;
+    double* x;
+    PcgResult res;
+};
+
+// device_pcg on `count` independent systems in lockstep (one host wait per iteration for
+// all of them); each system runs on its preconditioner's stream.
+void device_pcg_batch(PcgSystem* sys, int count, int maxit, double tol, bool use_graph);
 
 // k independent PCGs in lockstep sharing one multi-right-hand-side preconditioner
 // application per iteration; b, x: n x k (column j at offset j * n), device memory.

@@ -1749,6 +1749,7 @@ class DeviceFactor : public DeviceFactorBase {
         if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
         if (graph_) cudaGraphDestroy(graph_);
         if (xs_) cudaFree(xs_);
+        if (h_status_) cudaFreeHost(h_status_);
         if (ev_fork_) cudaEventDestroy(ev_fork_);
         if (ev_join_) cudaEventDestroy(ev_join_);
         if (s2_) cudaStreamDestroy(s2_);
@@ -2032,7 +2033,7 @@ class DeviceFactor : public DeviceFactorBase {
     }
     const double* device_values() const override { return d_vals_; }
 
-    void factorize(double tol) override {
+    void factorize_enqueue(double tol) override {
         const Plan& P = *P_;
         // inputs: the assembled blocks (device copy) and the initial cluster sizes
         if (probe_level_ >= 0) {
@@ -2123,6 +2124,12 @@ class DeviceFactor : public DeviceFactorBase {
             SPAND_CUDA(cudaStreamWaitEvent(s_, ev_join_, 0));
         }
         SPAND_CUDA(cudaGetLastError());
+        if (!h_status_) SPAND_CUDA(cudaMallocHost(&h_status_, sizeof(DStatus)));
+        SPAND_CUDA(cudaMemcpyAsync(h_status_, status_, sizeof(DStatus), cudaMemcpyDeviceToHost, s_));
+    }
+
+    void factorize_finish() override {
+        SPAND_CUDA(cudaStreamSynchronize(s_));
         if (probe_) {
             unsigned long long h[8];
             SPAND_CUDA(cudaMemcpyAsync(h, probe_, sizeof(h), cudaMemcpyDeviceToHost, s_));
@@ -2133,9 +2140,7 @@ class DeviceFactor : public DeviceFactorBase {
             for (int k = 0; k < 7; k++) fprintf(stderr, " %s %.0f", nm[k], h[7] ? (double)h[k] / h[7] : 0.0);
             fprintf(stderr, "\n");
         }
-        DStatus st;
-        SPAND_CUDA(cudaMemcpyAsync(&st, status_, sizeof(st), cudaMemcpyDeviceToHost, s_));
-        SPAND_CUDA(cudaStreamSynchronize(s_));
+        const DStatus st = *h_status_;
         if (st.not_spd)
             throw DeviceError{SPAND_ERR_NOT_SPD, "Error: Non-SPD Pivot (cluster " + std::to_string(st.not_spd - 1) + ")"};
         factored_ = true;
@@ -2775,6 +2780,7 @@ class DeviceFactor : public DeviceFactorBase {
     int *jpvt_ = nullptr, *ipvt_ = nullptr, *colcount_ = nullptr, *fallback_ = nullptr;
     int* tv_count_ = nullptr;  // finished row tiles per cluster (triangular products)
     cudaStream_t s2_ = nullptr;  // side stream of the WY factors
+    DStatus* h_status_ = nullptr;  // pinned copy of the status word, filled by factorize_enqueue
     cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
     int* pc_fallback_ = nullptr;  // pivots the cluster Cholesky could not hold
     bool tuned_ = false;
@@ -2823,30 +2829,25 @@ void device_scatter(const double* src, const int* map, int64_t n, double* dst, c
 }
 
 // Workspace of the device CG, kept across calls for one matrix size.
-struct PcgWork {
-    int n = 0;
-    double *r = nullptr, *p = nullptr, *z = nullptr, *tmp = nullptr, *partial = nullptr, *sc = nullptr;
-    double* h_sc = nullptr;
-    ~PcgWork() { release(); }
-    void release() {
-        cudaFree(r); cudaFree(p); cudaFree(z); cudaFree(tmp); cudaFree(partial); cudaFree(sc);
-        if (h_sc) cudaFreeHost(h_sc);
-        r = p = z = tmp = partial = sc = h_sc = nullptr;
-        n = 0;
-    }
-    void ensure(int nn) {
-        if (nn == n) return;
-        release();
-        SPAND_CUDA(cudaMalloc(&r, nn * sizeof(double)));
-        SPAND_CUDA(cudaMalloc(&p, nn * sizeof(double)));
-        SPAND_CUDA(cudaMalloc(&z, nn * sizeof(double)));
-        SPAND_CUDA(cudaMalloc(&tmp, nn * sizeof(double)));
-        SPAND_CUDA(cudaMalloc(&partial, RED_BLOCKS * sizeof(double)));
-        SPAND_CUDA(cudaMalloc(&sc, 8 * sizeof(double)));
-        SPAND_CUDA(cudaMallocHost(&h_sc, 8 * sizeof(double)));
-        n = nn;
-    }
-};
+void PcgWork::release() {
+    cudaFree(r); cudaFree(p); cudaFree(z); cudaFree(tmp); cudaFree(partial); cudaFree(sc);
+    if (h_sc) cudaFreeHost(h_sc);
+    r = p = z = tmp = partial = sc = h_sc = nullptr;
+    n = 0;
+}
+
+void PcgWork::ensure(int nn) {
+    if (nn == n) return;
+    release();
+    SPAND_CUDA(cudaMalloc(&r, nn * sizeof(double)));
+    SPAND_CUDA(cudaMalloc(&p, nn * sizeof(double)));
+    SPAND_CUDA(cudaMalloc(&z, nn * sizeof(double)));
+    SPAND_CUDA(cudaMalloc(&tmp, nn * sizeof(double)));
+    SPAND_CUDA(cudaMalloc(&partial, RED_BLOCKS * sizeof(double)));
+    SPAND_CUDA(cudaMalloc(&sc, 8 * sizeof(double)));
+    SPAND_CUDA(cudaMallocHost(&h_sc, 8 * sizeof(double)));
+    n = nn;
+}
 
 static thread_local PcgWork g_pcg;
 
@@ -2854,72 +2855,122 @@ static thread_local PcgWork g_pcg;
 // scalar read back per iteration for the stopping test.
 PcgResult device_pcg(DeviceFactorBase& M, const DeviceCsr& A, const double* b, double* x, int maxit, double tol,
                      bool use_graph) {
-    cudaStream_t s = M.stream();
-    KernelProfiler& prof = M.profiler();
-    const int n = A.n;
-    PcgResult res;
-    g_pcg.ensure(n);
-    double *r = g_pcg.r, *p = g_pcg.p, *z = g_pcg.z, *tmp = g_pcg.tmp, *partial = g_pcg.partial, *sc = g_pcg.sc;
-    double* h_sc = g_pcg.h_sc;
-    auto L = [&](const char* cls, auto&& f, int k = 1) {
-        prof.begin(s, cls);
-        f();
-        prof.end(s);
-        M.add_launches(k);
-    };
-    const unsigned gb = (unsigned)((n + 255) / 256);
-    auto dot = [&](const double* a, const double* bb, int slot) {
-        L("dot", [&] {
-            dot_partial_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, a, bb, partial);
-            dot_final_kernel<<<1, RED_THREADS, 0, s>>>(partial, RED_BLOCKS, sc + slot);
-        }, 2);
-    };
-    auto spmv = [&](const double* in, double* out) {
-        L("spmv", [&] { spmv_kernel<<<gb, 256, 0, s>>>(n, A.rowptr, A.colind, A.val, in, out); });
-    };
-    spmv(x, tmp);
-    L("axpy", [&] { sub_kernel<<<gb, 256, 0, s>>>(n, b, tmp, r); });
-    dot(b, b, 4);
-    dot(r, r, 2);
-    SPAND_CUDA(cudaMemcpyAsync(h_sc, sc, 8 * sizeof(double), cudaMemcpyDeviceToHost, s));
-    SPAND_CUDA(cudaStreamSynchronize(s));
-    const double rhsNorm2 = h_sc[4];
-    if (rhsNorm2 == 0) {
-        SPAND_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
-        SPAND_CUDA(cudaStreamSynchronize(s));
-        return res;
-    }
-    const double threshold = tol * tol * rhsNorm2;
-    double resNorm2 = h_sc[2];
-    res.relres = std::sqrt(resNorm2 / rhsNorm2);
-    if (resNorm2 < threshold) return res;
-    SPAND_CUDA(cudaMemcpyAsync(p, r, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    M.solve_device(p, 1, n);
-    dot(r, p, 0);
-    if (use_graph) M.capture_solve(z, 1, n);
-    int i = 0;
-    while (i < maxit) {
-        spmv(p, tmp);
-        dot(p, tmp, 1);
-        L("axpy", [&] { cg_update_xr_kernel<<<gb, 256, 0, s>>>(n, x, r, p, tmp, sc); });
-        dot(r, r, 2);
-        SPAND_CUDA(cudaMemcpyAsync(h_sc + 2, sc + 2, sizeof(double), cudaMemcpyDeviceToHost, s));
-        SPAND_CUDA(cudaStreamSynchronize(s));
-        resNorm2 = h_sc[2];
-        if (resNorm2 < threshold) break;
-        SPAND_CUDA(cudaMemcpyAsync(z, r, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-        M.solve_device(z, 1, n);
-        L("axpy", [&] { copy_scalar_kernel<<<1, 1, 0, s>>>(sc, 3, 0); });
-        dot(r, z, 0);
-        L("axpy", [&] { cg_update_p_kernel<<<gb, 256, 0, s>>>(n, p, z, sc); });
-        i++;
-    }
-    SPAND_CUDA(cudaGetLastError());
-    res.iterations = i + 1;
-    res.relres = std::sqrt(resNorm2 / rhsNorm2);
-    return res;
+    PcgSystem sys{&M, &A, &g_pcg, b, x};
+    device_pcg_batch(&sys, 1, maxit, tol, use_graph);
+    return sys.res;
 }
 
+// Independent systems advanced in lockstep: every phase of an iteration is queued on all
+// systems' streams before the one wait of the iteration (the stopping test of each).
+void device_pcg_batch(PcgSystem* sys, int count, int maxit, double tol, bool use_graph) {
+    struct St {
+        double thr = 0, bb = 0, rr = 0;
+        bool active = false;
+    };
+    std::vector<St> st(count);
+    auto L = [&](PcgSystem& q, const char* cls, auto&& f, int k = 1) {
+        KernelProfiler& prof = q.M->profiler();
+        prof.begin(q.M->stream(), cls);
+        f(q.M->stream(), q.A->n, (unsigned)((q.A->n + 255) / 256));
+        prof.end(q.M->stream());
+        q.M->add_launches(k);
+    };
+    auto dot = [&](PcgSystem& q, const double* a, const double* bb, int slot) {
+        L(q, "dot", [&](cudaStream_t s, int n, unsigned) {
+            dot_partial_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, a, bb, q.w->partial);
+            dot_final_kernel<<<1, RED_THREADS, 0, s>>>(q.w->partial, RED_BLOCKS, q.w->sc + slot);
+        }, 2);
+    };
+    auto spmv = [&](PcgSystem& q, const double* in, double* out) {
+        L(q, "spmv", [&](cudaStream_t s, int n, unsigned gb) {
+            spmv_kernel<<<gb, 256, 0, s>>>(n, q.A->rowptr, q.A->colind, q.A->val, in, out);
+        });
+    };
+    auto wait_all = [&]() {
+        for (int k = 0; k < count; k++)
+            if (st[k].active) SPAND_CUDA(cudaStreamSynchronize(sys[k].M->stream()));
+    };
+    for (int k = 0; k < count; k++) {
+        PcgSystem& q = sys[k];
+        q.w->ensure(q.A->n);
+        q.res = PcgResult{};
+        st[k].active = true;
+        spmv(q, q.x, q.w->tmp);
+        L(q, "axpy", [&](cudaStream_t s, int n, unsigned gb) { sub_kernel<<<gb, 256, 0, s>>>(n, q.b, q.w->tmp, q.w->r); });
+        dot(q, q.b, q.b, 4);
+        dot(q, q.w->r, q.w->r, 2);
+        SPAND_CUDA(cudaMemcpyAsync(q.w->h_sc, q.w->sc, 8 * sizeof(double), cudaMemcpyDeviceToHost, q.M->stream()));
+    }
+    wait_all();
+    for (int k = 0; k < count; k++) {
+        PcgSystem& q = sys[k];
+        st[k].bb = q.w->h_sc[4];
+        if (st[k].bb == 0) {
+            SPAND_CUDA(cudaMemsetAsync(q.x, 0, q.A->n * sizeof(double), q.M->stream()));
+            SPAND_CUDA(cudaStreamSynchronize(q.M->stream()));
+            st[k].active = false;
+            continue;
+        }
+        st[k].thr = tol * tol * st[k].bb;
+        st[k].rr = q.w->h_sc[2];
+        q.res.relres = std::sqrt(st[k].rr / st[k].bb);
+        if (st[k].rr < st[k].thr) {
+            st[k].active = false;
+            continue;
+        }
+        SPAND_CUDA(cudaMemcpyAsync(q.w->p, q.w->r, q.A->n * sizeof(double), cudaMemcpyDeviceToDevice, q.M->stream()));
+        q.M->solve_device(q.w->p, 1, q.A->n);
+        dot(q, q.w->r, q.w->p, 0);
+        if (use_graph) q.M->capture_solve(q.w->z, 1, q.A->n);
+    }
+    int i = 0;
+    int live = 0;
+    for (int k = 0; k < count; k++) live += st[k].active;
+    while (live && i < maxit) {
+        for (int k = 0; k < count; k++) {
+            if (!st[k].active) continue;
+            PcgSystem& q = sys[k];
+            spmv(q, q.w->p, q.w->tmp);
+            dot(q, q.w->p, q.w->tmp, 1);
+            L(q, "axpy", [&](cudaStream_t s, int n, unsigned gb) {
+                cg_update_xr_kernel<<<gb, 256, 0, s>>>(n, q.x, q.w->r, q.w->p, q.w->tmp, q.w->sc);
+            });
+            dot(q, q.w->r, q.w->r, 2);
+            SPAND_CUDA(cudaMemcpyAsync(q.w->h_sc + 2, q.w->sc + 2, sizeof(double), cudaMemcpyDeviceToHost,
+                                       q.M->stream()));
+        }
+        wait_all();
+        live = 0;
+        for (int k = 0; k < count; k++) {
+            if (!st[k].active) continue;
+            PcgSystem& q = sys[k];
+            st[k].rr = q.w->h_sc[2];
+            if (st[k].rr < st[k].thr) {
+                st[k].active = false;
+                q.res.iterations = i + 1;
+                q.res.relres = std::sqrt(st[k].rr / st[k].bb);
+                continue;
+            }
+            live++;
+            SPAND_CUDA(cudaMemcpyAsync(q.w->z, q.w->r, q.A->n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                       q.M->stream()));
+            q.M->solve_device(q.w->z, 1, q.A->n);
+            L(q, "axpy", [&](cudaStream_t s, int, unsigned) { copy_scalar_kernel<<<1, 1, 0, s>>>(q.w->sc, 3, 0); });
+            dot(q, q.w->r, q.w->z, 0);
+            L(q, "axpy", [&](cudaStream_t s, int n, unsigned gb) {
+                cg_update_p_kernel<<<gb, 256, 0, s>>>(n, q.w->p, q.w->z, q.w->sc);
+            });
+        }
+        i++;
+    }
+    for (int k = 0; k < count; k++) {
+        if (!st[k].active) continue;
+        PcgSystem& q = sys[k];
+        q.res.iterations = i + 1;
+        q.res.relres = std::sqrt(st[k].rr / st[k].bb);
+    }
+    for (int k = 0; k < count; k++) SPAND_CUDA(cudaGetLastError());
+}
 
 // Work buffers of the multi-right-hand-side PCG (n x k operands), grown on demand.
 struct PcgMultiWork {

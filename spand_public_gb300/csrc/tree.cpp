@@ -176,6 +176,34 @@ void Tree::factorize() {
     log_dirty_ = true;
 }
 
+void Tree::factorize_enqueue() {
+    if (!assembled_ok_) throw std::logic_error("factorize() before assemble()");
+    try {
+        dev_->factorize_enqueue(tol_);
+    } catch (spand::DeviceError& e) {
+        throw std::runtime_error(e.msg);
+    }
+}
+
+void Tree::factorize_finish() {
+    try {
+        dev_->factorize_finish();
+    } catch (spand::DeviceError& e) {
+        if (e.status == spand::SPAND_ERR_NOT_SPD) {
+            if (verb_) printf("Not SPD!\n");
+            throw std::runtime_error("Error: Non-SPD Pivot\n");
+        }
+        throw std::runtime_error(e.msg);
+    }
+    factored_ = true;
+    log_dirty_ = true;
+}
+
+spand::PcgWork& Tree::pcg_work() const {
+    if (!pcg_work_) pcg_work_.reset(new spand::PcgWork());
+    return *pcg_work_;
+}
+
 void Tree::bench_step(const double* b_dev, double* x_dev, int nrhs, int iters, double tol, double out[4]) {
     if (!assembled_ok_) throw std::logic_error("bench_step() before assemble()");
     cudaEvent_t e[3];
@@ -543,6 +571,59 @@ void cg_multi(const Tree& precond, const double* rhs, double* x, int nrhs, int l
     }
     cuda_check(cudaMemcpy2DAsync(x, pitch, dx, row, row, nrhs, cudaMemcpyDeviceToHost, s), "D2H");
     cuda_check(cudaStreamSynchronize(s), "sync");
+}
+
+void batch_factorize(Tree* const* trees, int count, int* status, std::string* messages) {
+    std::vector<bool> queued(count, false);
+    for (int k = 0; k < count; k++) {
+        status[k] = 0;
+        try {
+            trees[k]->factorize_enqueue();
+            queued[k] = true;
+        } catch (std::exception& e) {
+            status[k] = 1;
+            if (messages) messages[k] = e.what();
+        }
+    }
+    for (int k = 0; k < count; k++) {
+        if (!queued[k]) continue;
+        try {
+            trees[k]->factorize_finish();
+        } catch (std::exception& e) {
+            status[k] = 1;
+            if (messages) messages[k] = e.what();
+        }
+    }
+}
+
+void batch_cg(Tree* const* trees, int count, const double* const* rhs, double* const* x, int iters, double tol,
+              int* iters_out, double* relres_out) {
+    std::vector<spand::PcgSystem> sys(count);
+    std::vector<double*> db(count), dx(count);
+    for (int k = 0; k < count; k++) {
+        const Tree& t = *trees[k];
+        if (!t.device()) throw std::logic_error("cg before factorize");
+        const int n = t.get_N();
+        db[k] = t.cg_buffer(0, n);
+        dx[k] = t.cg_buffer(1, n);
+        cuda_check(cudaMemcpyAsync(db[k], rhs[k], n * sizeof(double), cudaMemcpyHostToDevice, t.stream()), "H2D");
+        cuda_check(cudaMemcpyAsync(dx[k], x[k], n * sizeof(double), cudaMemcpyHostToDevice, t.stream()), "H2D");
+        sys[k] = spand::PcgSystem{t.device(), &t.device_csr(), &t.pcg_work(), db[k], dx[k], spand::PcgResult{}};
+    }
+    try {
+        spand::device_pcg_batch(sys.data(), count, iters, tol, true);
+    } catch (spand::DeviceError& e) {
+        throw std::runtime_error(e.msg);
+    }
+    for (int k = 0; k < count; k++) {
+        const Tree& t = *trees[k];
+        cuda_check(cudaMemcpyAsync(x[k], dx[k], t.get_N() * sizeof(double), cudaMemcpyDeviceToHost, t.stream()), "D2H");
+    }
+    for (int k = 0; k < count; k++) {
+        cuda_check(cudaStreamSynchronize(trees[k]->stream()), "sync");
+        iters_out[k] = sys[k].res.iterations;
+        relres_out[k] = sys[k].res.relres;
+    }
 }
 
 }  // namespace spaND

@@ -65,6 +65,12 @@ class Tree {
     // are reused.  Device values leave the host copy of A (matrix()) unchanged.
     void assemble_values(const double* vals, int64_t nnz, bool on_device);
     void factorize();
+    // factorize() in two halves: every launch queued on the tree's stream, then the wait
+    // and the status check (what factorize() does in one call)
+    void factorize_enqueue();
+    void factorize_finish();
+    // work vectors of this tree's device CG
+    spand::PcgWork& pcg_work() const;
     // x <- M^{-1} x, host vector(s) in natural ordering (tree.cpp:1610-1635)
     void solve(double* x, int nrhs = 1, int ld = -1) const;
     // device vector(s)
@@ -90,7 +96,7 @@ class Tree {
     const Csc& matrix() const { return A_; }
     const spand::Plan& plan() const { return plan_; }
     cudaStream_t stream() const { return stream_; }
-    spand::DeviceCsr device_csr() const { return dA_; }
+    const spand::DeviceCsr& device_csr() const { return dA_; }
     size_t device_bytes() const;
     // device vectors of the CG driver (b, x), kept across calls
     double* cg_buffer(int which, int n) const;
@@ -139,6 +145,7 @@ class Tree {
     mutable size_t dx_len_ = 0;
     mutable double* cg_buf_[2] = {nullptr, nullptr};
     mutable size_t cg_len_ = 0;
+    mutable std::unique_ptr<spand::PcgWork> pcg_work_;
     int* d_cmap_ = nullptr;  // CSC entry -> CSR position
     bool partitioned_ = false, assembled_ok_ = false, factored_ = false;
     std::vector<LevelLog> log_;
@@ -155,6 +162,16 @@ int cg(const Csc& A, const double* rhs, double* x, const Tree& precond, int iter
 // in lockstep, one multi-right-hand-side preconditioner application per iteration).
 // rhs, x: host n x nrhs, leading dimension ld; per column the iteration count and |r|/|b|.
 void cg_multi(const Tree& precond, const double* rhs, double* x, int nrhs, int ld, int iters, double tol,
+              int* iters_out, double* relres_out);
+
+// No counterpart in the reference: factorize many trees at once (every tree's launches
+// queued on its own stream before the first wait); status[k]: 0 or the error of tree k.
+void batch_factorize(Tree* const* trees, int count, int* status, std::string* messages);
+
+// No counterpart in the reference: cg on many independent systems at once (tree k with
+// rhs[k] -> x[k], host vectors of the tree's size), advanced in lockstep with one host
+// wait per iteration for all systems.
+void batch_cg(Tree* const* trees, int count, const double* const* rhs, double* const* x, int iters, double tol,
               int* iters_out, double* relres_out);
 
 }  // namespace spaND
