@@ -35,6 +35,7 @@ PROBLEMS = {
     "lap3d": "3D 7-pt Laplacian {n}^3",
     "fv2d": "2D 5-pt finite-volume diffusion {n}^2, coefficients 10^U(-3,3) on 8x8 tiles",
     "aniso3d": "3D anisotropic diffusion {n}^3, face conductivities exp(0.5 z), axis scaling (1,1,0.01)",
+    "batch": "{systems} systems -Laplacian + cI on m^3 grids, m ~ U{{16..40}}, c ~ U(0,1)",
 }
 
 
@@ -43,6 +44,9 @@ def metric(args):
     counts say so."""
     if (args.problem, args.n, args.eps, args.nrhs) == ("lap3d", 64, 1e-2, 1):
         return METRIC
+    if args.problem == "batch":
+        return (f"seconds to factor and PCG-solve every system to {args.tol:g} FP64 rel. residual "
+                f"({PROBLEMS['batch'].format(systems=args.systems)}, eps={args.eps:g})")
     return (f"factor+PCG seconds to {args.tol:g} FP64 rel. residual ({PROBLEMS[args.problem].format(n=args.n)}, "
             f"eps={args.eps:g}, {args.nrhs} RHS)")
 
@@ -61,6 +65,7 @@ def parse():
     ap.add_argument("--maxit", type=int, default=200)
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--nrhs", type=int, default=1, help="right-hand sides solved together (independent CGs)")
+    ap.add_argument("--systems", type=int, default=256, help="independent systems of --problem batch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -375,6 +380,135 @@ def run_gb300(args, rank, world, local_rank):
     return 0
 
 
+def batch_workload(args):
+    """args.systems systems -Laplacian + cI on m^3 grids, m ~ U{16..40}, c ~ U(0,1), one
+    N(0,1) right-hand side each, ceil(log2(m^3/64)) levels; generator seeded with 0."""
+    from spand_public_gb300 import problems as P
+
+    rng = np.random.default_rng(0)
+    out = []
+    for _ in range(args.systems):
+        m = int(rng.integers(16, 41))
+        c = float(rng.uniform(0.0, 1.0))
+        levels = max(2, int(np.ceil(np.log2(m ** 3 / 64))))
+        out.append((m, P.reaction_diffusion3d(m, c), P.linspace_nd(m, 3), levels, rng.standard_normal(m ** 3)))
+    return out
+
+
+def run_batch(args, rank, world, local_rank):
+    import torch
+
+    import spand_public_gb300 as pkg
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    systems = batch_workload(args)
+
+    def trees(fp32):
+        out = []
+        for m, A, X, levels, _ in systems:
+            t = pkg.Tree(levels)
+            t.set_verb(False)
+            t.set_use_geo(True)
+            t.set_Xcoo(X)
+            t.set_tol(args.eps)
+            t.set_fp32(fp32)
+            t.partition(A)
+            t.assemble(A)
+            out.append(t)
+        return out
+
+    t_an = time.perf_counter()
+    T32 = trees(True)
+    t_an = time.perf_counter() - t_an
+    bd = [torch.from_numpy(b).to(dev) for *_, b in systems]
+    xd = [torch.zeros_like(b) for b in bd]
+
+    def step(ts):
+        for x in xd:
+            x.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = pkg.batch_factorize(ts)
+        t1 = time.perf_counter()
+        its, rr = pkg.batch_cg_device(ts, [b.data_ptr() for b in bd], [x.data_ptr() for x in xd], args.maxit,
+                                      args.tol)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        assert not np.any(st), st
+        return t1 - t0, t2 - t1, its, rr
+
+    for _ in range(args.warmup):
+        step(T32)
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    res = [step(T32) for _ in range(args.steps)]
+    clk = clocks.stop()
+    value = float(np.mean([f + g for f, g, _, _ in res]))
+    its = res[-1][2]
+    true_rel = max(float(np.linalg.norm(A @ x.cpu().numpy() - b) / np.linalg.norm(b))
+                   for (m, A, X, levels, b), x in zip(systems, xd))
+    fp64 = None
+    if args.fp64_steps > 0:
+        T64 = trees(False)
+        step(T64)
+        r64 = [step(T64) for _ in range(args.fp64_steps)]
+        fp64 = {"seconds": float(np.mean([f + g for f, g, _, _ in r64])), "pcg_iterations_max": int(r64[-1][2].max())}
+        for t in T64:
+            t.close()
+    # end to end through the C ABI with host buffers: values upload, batch factor, batch CG
+    e2e_t = []
+    for _ in range(max(args.steps, 1)):
+        t0 = time.perf_counter()
+        for (m, A, X, levels, b), t in zip(systems, T32):
+            t.assemble_values(A.data)
+        pkg.batch_factorize(T32)
+        xs, its_h, _ = pkg.batch_cg(T32, [b for *_, b in systems], args.maxit, args.tol)
+        e2e_t.append(time.perf_counter() - t0)
+    h2d = sum(A.data.nbytes + 2 * b.nbytes for _, A, _, _, b in systems)
+    d2h = sum(b.nbytes for *_, b in systems)
+    e2e = {"value": float(np.mean(e2e_t)), "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+           "pcg_iterations_max": int(its_h.max())}
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle.oracle import OracleTree
+
+        sample = systems[:8]
+        ts = 0.0
+        for m, A, X, levels, b in sample:
+            o = OracleTree(levels)
+            o.set_Xcoo(X)
+            o.set_tol(args.eps)
+            o.partition(A)
+            o.assemble(A)
+            t0 = time.perf_counter()
+            o.factorize()
+            o.cg(b, args.maxit, args.tol)
+            ts += time.perf_counter() - t0
+        frac = sum(s[0] ** 3 for s in sample) / sum(s[0] ** 3 for s in systems)
+        cpu = {"value": ts / frac, "unit": "s", "cores": 1, "kind": "port",
+               "sample": f"factor+CG of the first {len(sample)} systems by the oracle (one thread), scaled to all "
+                         f"{args.systems} by unknown count ({frac:.3f} of the dofs)"}
+    line = {"metric": metric(args), "value": value, "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": PROBLEMS["batch"].format(systems=args.systems) + f", eps={args.eps:g}, "
+                                   f"PCG to {args.tol:g} per system", "systems": args.systems,
+                       "dofs": int(sum(s[0] ** 3 for s in systems)), "eps": args.eps, "pcg_tol": args.tol,
+                       "factor_s": float(np.mean([f for f, _, _, _ in res])),
+                       "pcg_s": float(np.mean([g for _, g, _, _ in res])),
+                       "pcg_iterations_max": int(its.max()), "pcg_iterations_mean": float(its.mean()),
+                       "true_relres_max": true_rel, "analysis_s": t_an, "plain_fp64": fp64,
+                       "timing": "host wall clock between device-wide synchronisations (one stream per system)",
+                       "precision": "FP32 factor (SIMT), FP64 CG/SpMV/dots", "parallelism": "1 GPU"},
+            "e2e": e2e, "gpu_launches": None, "roofline": None, "cpu_baseline": cpu, "clocks": clk}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    for t in T32:
+        t.close()
+    return 0
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -382,6 +516,8 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.problem == "batch":
+        return run_batch(args, rank, world, local_rank)
     if world > 1:
         import torch
         import torch.distributed as dist

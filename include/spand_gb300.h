@@ -120,6 +120,10 @@ int spand_cg_multi_device(spand_tree* t, const double* b_dev, double* x_dev, int
 int spand_batch_factorize(spand_tree* const* trees, int count, int* status_out);
 int spand_batch_cg(spand_tree* const* trees, int count, const double* const* b, double* const* x, int iters,
                    double tol, int* iters_out, double* relres_out);
+/* Same on device vectors b_dev[k] -> x_dev[k] (FP64, the tree's size; x_dev[k] holds the
+ * initial guess); every system runs on its tree's stream and the call returns when all have converged or stopped. */
+int spand_batch_cg_device(spand_tree* const* trees, int count, const double* const* b_dev, double* const* x_dev,
+                          int iters, double tol, int* iters_out, double* relres_out);
 
 /* Introspection (reference: get_N, get_assembly_perm, nnz, get_stop, print_log fields;
  * include/tree.h:150-165, src/tree.cpp:1645-1727) */

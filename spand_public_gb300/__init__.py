@@ -58,6 +58,8 @@ _PROTOS = {
     "spand_batch_factorize": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "spand_batch_cg": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p,
                                  C.c_void_p]),
+    "spand_batch_cg_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
+                                        C.c_void_p, C.c_void_p]),
     "spand_tree_assemble_values": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_int]),
     "spand_cg_multi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,
                                  C.c_void_p, C.c_void_p]),
@@ -372,3 +374,16 @@ def batch_cg(trees, bs, iters=100, tol=1e-12):
     rr = np.zeros(k, dtype=np.float64)
     _check(L.spand_batch_cg(hs, k, bp, xp, int(iters), float(tol), _ptr(its), _ptr(rr)))
     return xs, its, rr
+
+
+def batch_cg_device(trees, b_ptrs, x_ptrs, iters=100, tol=1e-12):
+    """batch_cg on device vectors (addresses of FP64 arrays of each tree's size)."""
+    L = lib()
+    k = len(trees)
+    hs = (C.c_void_p * k)(*[t.h for t in trees])
+    bp = (C.c_void_p * k)(*[int(p) for p in b_ptrs])
+    xp = (C.c_void_p * k)(*[int(p) for p in x_ptrs])
+    its = np.zeros(k, dtype=np.int32)
+    rr = np.zeros(k, dtype=np.float64)
+    _check(L.spand_batch_cg_device(hs, k, bp, xp, int(iters), float(tol), _ptr(its), _ptr(rr)))
+    return its, rr

@@ -216,6 +216,17 @@ int spand_batch_cg(spand_tree* const* trees, int count, const double* const* b, 
     return guard([&] { spaND::batch_cg(ts.data(), count, b, x, iters, tol, iters_out, relres_out); });
 }
 
+int spand_batch_cg_device(spand_tree* const* trees, int count, const double* const* b, double* const* x, int iters,
+                          double tol, int* iters_out, double* relres_out) {
+    if (!trees || !b || !x || !iters_out || !relres_out || count < 0) return fail(SPAND_ERR_ARG, "null argument");
+    std::vector<spaND::Tree*> ts(count);
+    for (int k = 0; k < count; k++) {
+        if (!trees[k] || !b[k] || !x[k]) return fail(SPAND_ERR_ARG, "null tree or vector");
+        ts[k] = trees[k]->t;
+    }
+    return guard([&] { spaND::batch_cg_device(ts.data(), count, b, x, iters, tol, iters_out, relres_out); });
+}
+
 int spand_cg_multi(spand_tree* t, const double* b, double* x, int nrhs, int ld, int iters, double tol,
                    int* iters_out, double* relres_out) {
     CHECK_T(t);

@@ -626,4 +626,23 @@ void batch_cg(Tree* const* trees, int count, const double* const* rhs, double* c
     }
 }
 
+void batch_cg_device(Tree* const* trees, int count, const double* const* b_dev, double* const* x_dev, int iters,
+                     double tol, int* iters_out, double* relres_out) {
+    std::vector<spand::PcgSystem> sys(count);
+    for (int k = 0; k < count; k++) {
+        const Tree& t = *trees[k];
+        if (!t.device()) throw std::logic_error("cg before factorize");
+        sys[k] = spand::PcgSystem{t.device(), &t.device_csr(), &t.pcg_work(), b_dev[k], x_dev[k], spand::PcgResult{}};
+    }
+    try {
+        spand::device_pcg_batch(sys.data(), count, iters, tol, true);
+    } catch (spand::DeviceError& e) {
+        throw std::runtime_error(e.msg);
+    }
+    for (int k = 0; k < count; k++) {
+        iters_out[k] = sys[k].res.iterations;
+        relres_out[k] = sys[k].res.relres;
+    }
+}
+
 }  // namespace spaND

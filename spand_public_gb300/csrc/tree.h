@@ -173,5 +173,8 @@ void batch_factorize(Tree* const* trees, int count, int* status, std::string* me
 // wait per iteration for all systems.
 void batch_cg(Tree* const* trees, int count, const double* const* rhs, double* const* x, int iters, double tol,
               int* iters_out, double* relres_out);
+// batch_cg on device vectors (b_dev[k], x_dev[k]: the tree's size, x holds the initial guess)
+void batch_cg_device(Tree* const* trees, int count, const double* const* b_dev, double* const* x_dev, int iters,
+                     double tol, int* iters_out, double* relres_out);
 
 }  // namespace spaND

@@ -65,3 +65,21 @@ def test_batch_reports_a_failing_system():
     xs, its, _ = pkg.batch_cg([sysb[0][3], sysb[2][3]], [sysb[0][4], sysb[2][4]], iters=200, tol=1e-10)
     for (A2, _, _, _, b2), x in zip([sysb[0], sysb[2]], xs):
         assert np.linalg.norm(A2 @ x - b2) / np.linalg.norm(b2) < 1e-9
+
+
+def test_batch_cg_device_matches_host():
+    """batch_cg_device on torch device vectors: the iterations and solutions of batch_cg."""
+    torch = pytest.importorskip("torch")
+    import spand_public_gb300 as pkg
+    sysb = _systems(True, [9, 13, 10, 16])
+    trees = [s[3] for s in sysb]
+    assert not np.any(pkg.batch_factorize(trees))
+    xs, its, rr = pkg.batch_cg(trees, [s[4] for s in sysb], iters=200, tol=1e-10)
+    bd = [torch.from_numpy(s[4]).cuda() for s in sysb]
+    xd = [torch.zeros_like(b) for b in bd]  # x holds the initial guess
+    torch.cuda.synchronize()
+    itd, rrd = pkg.batch_cg_device(trees, [b.data_ptr() for b in bd], [x.data_ptr() for x in xd], 200, 1e-10)
+    assert np.array_equal(its, itd)
+    assert np.allclose(rr, rrd, rtol=1e-12, atol=0)
+    for x, xh in zip(xd, xs):
+        assert np.linalg.norm(x.cpu().numpy() - xh) <= 1e-13 * np.linalg.norm(xh)
