@@ -98,6 +98,13 @@ int spand_cg(spand_tree* t, const double* b, double* x, int iters, double tol, i
 /* Same with device vectors. */
 int spand_cg_device(spand_tree* t, const double* b_dev, double* x_dev, int iters, double tol, int* iters_out,
                     double* relres_out);
+/* No counterpart in the reference: the adjoint of x = A^{-1} b.  lambda_dev = A^{-T} g_dev
+ * (g = dL/dx; A SPD, so the PCG of spand_cg_device with the same factor), then
+ * grad_vals_dev[k] = -lambda[row_k] * x[col_k] for every stored entry k of the assembled
+ * pattern, in its CSC order (dL/dvalues; dL/db = lambda).  x_dev: the solution of the
+ * forward solve.  Device vectors; lambda_dev holds the initial guess. */
+int spand_adjoint_device(spand_tree* t, const double* g_dev, const double* x_dev, double* lambda_dev,
+                         double* grad_vals_dev, int iters, double tol, int* iters_out, double* relres_out);
 /* No counterpart in the reference: cg on nrhs right-hand sides at once.  Each column is an
  * independent CG with the reference's stopping rule (|r| < tol |b|); the columns advance in
  * lockstep so that one multi-right-hand-side preconditioner application, one SpMV and three

@@ -55,6 +55,8 @@ _PROTOS = {
                            C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "spand_cg_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
                                   C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "spand_adjoint_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                       C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "spand_batch_factorize": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "spand_batch_cg": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p,
                                  C.c_void_p]),
@@ -235,6 +237,15 @@ class Tree:
         rr = C.c_double()
         _check(self.L.spand_cg_device(self.h, C.c_void_p(b_ptr), C.c_void_p(x_ptr), int(iters), float(tol),
                                       C.byref(it), C.byref(rr)))
+        return it.value, rr.value
+
+    def adjoint_device(self, g_ptr: int, x_ptr: int, lam_ptr: int, grad_ptr: int, iters=100, tol=1e-12):
+        """lambda = A^{-T} g by PCG with this factor, grad[k] = -lambda[row_k] x[col_k] over
+        the stored entries (CSC order); device addresses.  Returns (iterations, |r|/|g|)."""
+        it = C.c_int()
+        rr = C.c_double()
+        _check(self.L.spand_adjoint_device(self.h, C.c_void_p(g_ptr), C.c_void_p(x_ptr), C.c_void_p(lam_ptr),
+                                           C.c_void_p(grad_ptr), int(iters), float(tol), C.byref(it), C.byref(rr)))
         return it.value, rr.value
 
     # introspection

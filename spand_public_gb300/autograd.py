@@ -8,7 +8,9 @@ with the same operator and preconditioner, and
     dL/db          = λ
     dL/dvalues[k]  = -λ[row_k] · x[col_k]     for every stored entry k of A
 
-(the −λxᵀ outer product restricted to the sparsity pattern).  Gradients with respect to
+(the −λxᵀ outer product restricted to the sparsity pattern).  Both come from one call,
+`Tree.adjoint_device` (C ABI `spand_adjoint_device`): the PCG for λ and the pattern
+scatter kernel.  Gradients with respect to
 parameters that A's values depend on (face conductivities, shifts) follow from torch
 autograd through the code that forms the values.
 
@@ -78,8 +80,13 @@ class SpandSolve(torch.autograd.Function):
         if getattr(tree, "_autograd_values", None) is not vals:
             _refactor(tree, vals)  # the tree was re-assembled since this forward
         gg = g.detach().to(device="cuda", dtype=torch.float64).contiguous()
-        lam = _pcg(tree, gg, ctx.iters, ctx.tol)
-        grad_vals = -(lam[pat.rows] * x[pat.cols])
+        lam = torch.zeros_like(gg)
+        grad_vals = torch.empty(pat.nnz, dtype=torch.float64, device=gg.device)
+        torch.cuda.synchronize()  # the tree runs on its own stream
+        it, rr = tree.adjoint_device(gg.data_ptr(), x.data_ptr(), lam.data_ptr(), grad_vals.data_ptr(), ctx.iters,
+                                     ctx.tol)
+        if not rr < ctx.tol:
+            raise RuntimeError(f"adjoint CG did not converge: |r|/|g| = {rr:.3e} after {it} iterations")
         return grad_vals.to(ctx.vdev), lam.to(ctx.bdev), None, None, None, None
 
 

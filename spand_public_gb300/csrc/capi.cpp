@@ -179,6 +179,17 @@ int spand_cg_device(spand_tree* t, const double* b, double* x, int iters, double
     });
 }
 
+int spand_adjoint_device(spand_tree* t, const double* g, const double* x, double* lambda, double* grad_vals,
+                         int iters, double tol, int* iters_out, double* relres_out) {
+    CHECK_T(t);
+    if (!g || !x || !lambda || !grad_vals) return fail(SPAND_ERR_ARG, "null vector");
+    return guard([&] {
+        spand::PcgResult r = t->t->adjoint_device(g, x, lambda, grad_vals, iters, tol);
+        if (iters_out) *iters_out = r.iterations;
+        if (relres_out) *relres_out = r.relres;
+    });
+}
+
 int spand_tree_assemble_values(spand_tree* t, const double* vals, long long nnz, int on_device) {
     CHECK_T(t);
     if (!vals && nnz > 0) return fail(SPAND_ERR_ARG, "null values");

@@ -170,4 +170,8 @@ void device_spmv(const DeviceCsr& A, const double* x, double* y, cudaStream_t s)
 // dst[map[k]] = src[k] for map[k] >= 0 (device arrays), on stream s
 void device_scatter(const double* src, const int* map, int64_t n, double* dst, cudaStream_t s);
 
+// out[k] = -lam[rows[k]] * x[cols[k]] for k < nnz (device arrays), on stream s
+void device_pattern_outer(const int* rows, const int* cols, int64_t nnz, const double* lam, const double* x,
+                          double* out, cudaStream_t s);
+
 }  // namespace spand

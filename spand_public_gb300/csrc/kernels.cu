@@ -945,6 +945,15 @@ __global__ void scatter_f64_kernel(const double* __restrict__ src, const int* __
     if (k < n && map[k] >= 0) dst[map[k]] = src[k];
 }
 
+// out[k] = -lam[rows[k]] * x[cols[k]]: the adjoint -lambda x^T restricted to the stored
+// entries of A (one entry per thread; the gathers of lam and x hit L2 for stencil patterns)
+__global__ void pattern_outer_kernel(long long nnz, const int* __restrict__ rows, const int* __restrict__ cols,
+                                     const double* __restrict__ lam, const double* __restrict__ x,
+                                     double* __restrict__ out) {
+    long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (k < nnz) out[k] = -lam[rows[k]] * x[cols[k]];
+}
+
 __global__ void snapshot_kernel(const int* csize, int* rows0, const int* __restrict__ clusters, int n) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n) rows0[clusters[k]] = csize[clusters[k]];
@@ -2826,6 +2835,11 @@ void device_spmv(const DeviceCsr& A, const double* x, double* y, cudaStream_t s)
 
 void device_scatter(const double* src, const int* map, int64_t n, double* dst, cudaStream_t s) {
     if (n > 0) scatter_f64_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, map, n, dst);
+}
+
+void device_pattern_outer(const int* rows, const int* cols, int64_t nnz, const double* lam, const double* x,
+                          double* out, cudaStream_t s) {
+    if (nnz > 0) pattern_outer_kernel<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, rows, cols, lam, x, out);
 }
 
 // Workspace of the device CG, kept across calls for one matrix size.

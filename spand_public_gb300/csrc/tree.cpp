@@ -40,6 +40,8 @@ Tree::~Tree() {
     for (auto& p : cg_buf_)
         if (p) cudaFree(p);
     if (d_cmap_) cudaFree(d_cmap_);
+    if (d_prow_) cudaFree(d_prow_);
+    if (d_pcol_) cudaFree(d_pcol_);
     if (dx_) cudaFree(dx_);
     if (dA_.rowptr) cudaFree(dA_.rowptr);
     if (dA_.colind) cudaFree(dA_.colind);
@@ -117,6 +119,9 @@ void Tree::assemble(const Csc& A) {
             }
         if (dA_.rowptr) { cudaFree(dA_.rowptr); cudaFree(dA_.colind); cudaFree(dA_.val); }
         if (d_cmap_) cudaFree(d_cmap_);
+        if (d_prow_) cudaFree(d_prow_);
+        if (d_pcol_) cudaFree(d_pcol_);
+        d_prow_ = d_pcol_ = nullptr;
         dA_.n = n;
         cuda_check(cudaMalloc(&dA_.rowptr, rp.size() * sizeof(int)), "cudaMalloc");
         cuda_check(cudaMalloc(&dA_.colind, std::max<size_t>(nnz, 1) * sizeof(int)), "cudaMalloc");
@@ -527,6 +532,32 @@ std::vector<Tree::Work> Tree::work_solve() const {
     const double n = get_N();
     add_work(w, "perm", 2 * n * (8 + 4 + 8 + sz), 0);
     return w;
+}
+
+spand::PcgResult Tree::adjoint_device(const double* g, const double* x, double* lambda, double* grad_vals,
+                                      int iters, double tol) const {
+    if (!dev_ || !factored_) throw std::logic_error("adjoint before factorize");
+    const size_t nnz = A_.rowval.size();
+    if (!d_prow_) {
+        std::vector<int> cols(nnz);
+        for (int j = 0; j < A_.n; j++)
+            for (int k = A_.colptr[j]; k < A_.colptr[j + 1]; k++) cols[k] = j;
+        cuda_check(cudaMalloc(&d_prow_, std::max<size_t>(nnz, 1) * sizeof(int)), "cudaMalloc");
+        cuda_check(cudaMalloc(&d_pcol_, std::max<size_t>(nnz, 1) * sizeof(int)), "cudaMalloc");
+        cuda_check(cudaMemcpy(d_prow_, A_.rowval.data(), nnz * sizeof(int), cudaMemcpyHostToDevice), "H2D");
+        cuda_check(cudaMemcpy(d_pcol_, cols.data(), nnz * sizeof(int), cudaMemcpyHostToDevice), "H2D");
+    }
+    spand::PcgResult r;
+    try {
+        r = spand::device_pcg(*dev_, dA_, g, lambda, iters, tol, true);
+    } catch (spand::DeviceError& e) {
+        throw std::runtime_error(e.msg);
+    }
+    spand::device_pattern_outer(d_prow_, d_pcol_, (int64_t)nnz, lambda, x, grad_vals, stream_);
+    dev_->add_launches(1);
+    cuda_check(cudaGetLastError(), "adjoint scatter");
+    cuda_check(cudaStreamSynchronize(stream_), "sync");
+    return r;
 }
 
 int cg(const Csc& A, const double* rhs, double* x, const Tree& precond, int iters, double tol, bool verb,

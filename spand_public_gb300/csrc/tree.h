@@ -116,6 +116,14 @@ class Tree {
     // nrhs right-hand sides: b_dev, x_dev n x nrhs (leading dimension n)
     void bench_step(const double* b_dev, double* x_dev, int nrhs, int iters, double tol, double out[4]);
 
+    // No reference counterpart: the adjoint of x = A^{-1} b for a loss L(x).  lambda =
+    // A^{-T} g (g = dL/dx) by the preconditioned Krylov solve with this factor (A SPD:
+    // A^{-T} = A^{-1}, PCG), then grad_vals[k] = -lambda[row_k] x[col_k] for every stored
+    // entry k of A in the CSC order of the assembled pattern (dL/dvalues); dL/db = lambda.
+    // Device vectors; lambda holds the initial guess.
+    spand::PcgResult adjoint_device(const double* g, const double* x, double* lambda, double* grad_vals, int iters,
+                                    double tol) const;
+
    private:
     void build_ops_and_log();
     void ensure_log() const {
@@ -147,6 +155,8 @@ class Tree {
     mutable size_t cg_len_ = 0;
     mutable std::unique_ptr<spand::PcgWork> pcg_work_;
     int* d_cmap_ = nullptr;  // CSC entry -> CSR position
+    mutable int* d_prow_ = nullptr;  // row / column of every CSC entry (adjoint scatter)
+    mutable int* d_pcol_ = nullptr;
     bool partitioned_ = false, assembled_ok_ = false, factored_ = false;
     std::vector<LevelLog> log_;
     std::vector<OpRecord> ops_;
