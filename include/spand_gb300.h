@@ -23,7 +23,8 @@ typedef enum {
     SPAND_ERR_ARG = 1,            /* invalid argument */
     SPAND_ERR_STATE = 2,          /* call out of order (e.g. solve before factorize) */
     SPAND_ERR_CUDA = 3,           /* CUDA runtime failure */
-    SPAND_ERR_NOT_SPD = 4,        /* non-SPD pivot: the reference throws "Error: Non-SPD Pivot" (src/tree.cpp:587-590) */
+    SPAND_ERR_NOT_SPD = 4,        /* failed pivot: the reference throws "Error: Non-SPD Pivot" (LLT, src/tree.cpp:587-590)
+                                     or "Error: Singular Pivot" (PLU, src/tree.cpp:624-628) */
     SPAND_ERR_UNSUPPORTED = 5,    /* configuration not implemented on the device path */
     SPAND_ERR_NO_CONVERGENCE = 6
 } spand_status;
@@ -98,6 +99,25 @@ int spand_cg(spand_tree* t, const double* b, double* x, int iters, double tol, i
 /* Same with device vectors. */
 int spand_cg_device(spand_tree* t, const double* b_dev, double* x_dev, int iters, double tol, int* iters_out,
                     double* relres_out);
+/* gmres(A, rhs, x, precond, iters, restart, tol, verb) (include/is.h:13, src/is.cpp:123-300):
+ * restarted GMRES with Householder Arnoldi, left preconditioned by the tree, on the device.
+ * b, x: host vectors (x holds the initial guess); iters_out: the iteration count the
+ * reference returns; relres_out: |w_k| / |M^{-1} r_0|, the quantity of its stopping test. */
+int spand_gmres(spand_tree* t, const double* b, double* x, int iters, int restart, double tol, int verb,
+                int* iters_out, double* relres_out);
+/* Same with device vectors. */
+int spand_gmres_device(spand_tree* t, const double* b_dev, double* x_dev, int iters, int restart, double tol,
+                       int* iters_out, double* relres_out);
+/* No counterpart in the reference: flexible (right-preconditioned) restarted GMRES.  Its
+ * recurrence residual is the true |b - A x| whatever precision the factor is stored in, so
+ * an FP32 factor (spand_tree_set_fp32) reaches an FP64 tolerance; stops when
+ * |b - A x| < tol |b|, relres_out = that ratio.  Host vectors, x holds the initial guess. */
+int spand_fgmres(spand_tree* t, const double* b, double* x, int iters, int restart, double tol, int verb,
+                 int* iters_out, double* relres_out);
+/* ir(A, rhs, x, precond, iters, tol, verb) (include/is.h:14, src/is.cpp:12-37): iterative
+ * refinement x += M^{-1}(b - A x) on the device; relres_out = |b - A x| / |b|. */
+int spand_ir(spand_tree* t, const double* b, double* x, int iters, double tol, int verb, int* iters_out,
+             double* relres_out);
 /* No counterpart in the reference: the adjoint of x = A^{-1} b.  lambda_dev = A^{-T} g_dev
  * (g = dL/dx; A SPD, so the PCG of spand_cg_device with the same factor), then
  * grad_vals_dev[k] = -lambda[row_k] * x[col_k] for every stored entry k of the assembled
@@ -145,11 +165,15 @@ int spand_tree_level_log(spand_tree* t, long long* out);
 int spand_tree_num_ranks(spand_tree* t, int* n);
 int spand_tree_get_ranks(spand_tree* t, int* out);
 /* Operation list in recording order: kind level self nbr ns nn rows cols (8 ints each);
- * kind: 0 ScalingLLT 1 GemmSymmOut 2 GemmSymmIn 3 Orthogonal 4 Merge 5 Split */
+ * kind: 0 ScalingLLT 1 GemmSymmOut 2 GemmSymmIn 3 Orthogonal 4 Merge 5 Split
+ *       6 GemmOut 7 GemmIn 8 ScalingPLUQ (GEN / PLU; its matrix: L_s strictly below the
+ *       diagonal, U_s on and above it) */
 int spand_tree_num_ops(spand_tree* t, int* n);
 int spand_tree_get_ops(spand_tree* t, int* out);
 int spand_tree_get_op_matrix(spand_tree* t, int idx, double* out);
 int spand_tree_get_op_tau(spand_tree* t, int idx, double* out);
+/* row permutation p (ns entries) of a ScalingPLUQ op: x_s <- x_s[p] before L_s^{-1} */
+int spand_tree_get_op_perm(spand_tree* t, int idx, int* out);
 /* seconds: partition, assemble, factorize */
 int spand_tree_timings(spand_tree* t, double* out);
 /* kernels launched by this tree since the last reset */

@@ -60,6 +60,8 @@ def lib():
             "orc_dense_potf": (I, [I, pd]), "orc_dense_geqp3": (None, [I, I, pd, pi, pd]),
             "orc_dense_getf": (I, [I, pd, pi]), "orc_choose_rank": (I, [pd, I, D]),
             "orc_spmv": (None, [P, pd, pd]),
+            "orc_gmres": (I, [P, pd, pd, I, I, D, pd]),
+            "orc_get_op_u": (C.c_longlong, [P, I, pd]), "orc_get_op_perm": (I, [P, I, pi]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -150,6 +152,16 @@ class OracleTree:
         it = self.L.orc_cg(self.h, _dp(b), _dp(x), int(iters), float(tol), _dp(rr))
         return x, it
 
+    def gmres(self, b, iters=100, restart=None, tol=1e-12, x0=None):
+        """Restarted GMRES (is.cpp:123-300); returns (x, iterations, preconditioned
+        residual estimate |w_k| / |M^{-1} r_0|)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.float64)
+        rr = np.zeros(1)
+        restart = iters if restart is None else restart
+        it = self.L.orc_gmres(self.h, _dp(b), _dp(x), int(iters), int(restart), float(tol), _dp(rr))
+        return x, it, float(rr[0])
+
     def ir(self, b, iters=100, tol=1e-12):
         b = np.ascontiguousarray(b, dtype=np.float64)
         x = np.zeros_like(b)
@@ -214,6 +226,16 @@ class OracleTree:
         buf = np.zeros(rows * cols)
         self.L.orc_get_op_matrix(self.h, idx, _dp(buf))
         return buf.reshape((cols, rows)).T
+
+    def op_u(self, idx, n):
+        buf = np.zeros(n * n)
+        self.L.orc_get_op_u(self.h, idx, _dp(buf))
+        return buf.reshape((n, n)).T
+
+    def op_perm(self, idx, n):
+        buf = np.zeros(max(n, 1), dtype=np.int32)
+        self.L.orc_get_op_perm(self.h, idx, _ip(buf))
+        return buf[:n]
 
     def op_tau(self, idx, k):
         buf = np.zeros(max(k, 1))

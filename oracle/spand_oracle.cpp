@@ -1381,6 +1381,158 @@ static int ir(const CSC& A, const double* rhs, double* x, Tree& M, int iters, do
     return i;
 }
 
+// ---------------------------------------------------------------------------------
+// Restarted GMRES with Householder Arnoldi, left preconditioned; is.cpp:123-300.  The
+// reference is Eigen's GMRES (unsupported/Eigen/src/IterativeSolvers/GMRES.h, Eigen
+// 3.3.x) with the preconditioner's solve in place of Eigen's preconditioner: the
+// Householder helpers below restate Eigen's published makeHouseholder /
+// applyHouseholderOnTheLeft and the real makeGivens / applyOnTheLeft of JacobiRotation.
+// ---------------------------------------------------------------------------------
+namespace gm {
+// x (length len) = beta e_0 after I - tau [1; ess][1; ess]^T; ess has len - 1 entries
+static void make_householder(const double* x, int len, double* ess, double& tau, double& beta) {
+    double tail = 0;
+    for (int i = 1; i < len; i++) tail += x[i] * x[i];
+    const double c0 = x[0];
+    if (tail <= std::numeric_limits<double>::min()) {
+        tau = 0;
+        beta = c0;
+        for (int i = 1; i < len; i++) ess[i - 1] = 0;
+        return;
+    }
+    beta = std::sqrt(c0 * c0 + tail);
+    if (c0 >= 0) beta = -beta;
+    for (int i = 1; i < len; i++) ess[i - 1] = x[i] / (c0 - beta);
+    tau = (beta - c0) / beta;
+}
+// y (length len) <- (I - tau [1; ess][1; ess]^T) y
+static void apply_householder(double* y, int len, const double* ess, double tau) {
+    if (len == 1) {
+        y[0] *= 1.0 - tau;
+        return;
+    }
+    if (tau == 0) return;
+    double t = y[0];
+    for (int i = 1; i < len; i++) t += ess[i - 1] * y[i];
+    y[0] -= tau * t;
+    for (int i = 1; i < len; i++) y[i] -= tau * ess[i - 1] * t;
+}
+struct Givens {
+    double c = 1, s = 0;
+};
+// G such that G^T applied to (p, q) gives (r, 0)
+static Givens make_givens(double p, double q) {
+    Givens g;
+    if (q == 0) {
+        g.c = p < 0 ? -1 : 1;
+        g.s = 0;
+    } else if (p == 0) {
+        g.c = 0;
+        g.s = q < 0 ? 1 : -1;
+    } else if (std::fabs(p) > std::fabs(q)) {
+        double t = q / p, u = std::sqrt(1 + t * t);
+        if (p < 0) u = -u;
+        g.c = 1 / u;
+        g.s = -t * g.c;
+    } else {
+        double t = p / q, u = std::sqrt(1 + t * t);
+        if (q < 0) u = -u;
+        g.s = -1 / u;
+        g.c = -t * g.s;
+    }
+    return g;
+}
+// rows (i, j) of v <- G^T (rows i, j): x' = c x - s y, y' = s x + c y
+static void apply_givens_t(double* v, int i, int j, const Givens& g) {
+    const double x = v[i], y = v[j];
+    v[i] = g.c * x - g.s * y;
+    v[j] = g.s * x + g.c * y;
+}
+}  // namespace gm
+
+static int gmres(const CSC& A, const double* rhs, double* x, Tree& M, int iters, int restart, double tol,
+                 double* relres_out) {
+    const int m = A.n;
+    if (std::sqrt(dot(m, rhs, rhs)) <= std::numeric_limits<double>::min()) {
+        std::fill(x, x + m, 0.0);
+        if (relres_out) *relres_out = 0;
+        return 1;
+    }
+    int it = 0;
+    std::vector<double> r0(m), t(m), v(m);
+    // H: reflector i in column i (its essential part at rows i+1..m-1); above the diagonal,
+    // the upper triangle of the rotated Hessenberg matrix
+    std::vector<double> H((size_t)m * (restart + 1), 0.0), w(restart + 1, 0.0), tau(restart + 1, 0.0);
+    std::vector<gm::Givens> G(restart);
+    auto col = [&](int i) { return H.data() + (size_t)i * m; };
+    // the stopping test divides by the norm of the FIRST preconditioned residual, also
+    // after a restart (r0Norm is computed once, is.cpp:161)
+    double r0norm = -1;
+    auto start = [&]() {  // preconditioned residual and the first reflector
+        spmv(A, x, t.data());
+        for (int i = 0; i < m; i++) r0[i] = rhs[i] - t[i];
+        M.solve(r0.data());
+        if (r0norm < 0) r0norm = std::sqrt(dot(m, r0.data(), r0.data()));
+        std::fill(H.begin(), H.end(), 0.0);
+        std::fill(w.begin(), w.end(), 0.0);
+        std::fill(tau.begin(), tau.end(), 0.0);
+        double beta;
+        gm::make_householder(r0.data(), m, col(0) + 1, tau[0], beta);
+        w[0] = beta;
+    };
+    start();
+    if (r0norm == 0) {
+        if (relres_out) *relres_out = 0;
+        return 1;
+    }
+    double err = 1.0;
+    for (int k = 1; k <= restart; ++k) {
+        ++it;
+        std::fill(v.begin(), v.end(), 0.0);
+        v[k - 1] = 1.0;
+        for (int i = k - 1; i >= 0; --i) gm::apply_householder(v.data() + i, m - i, col(i) + i + 1, tau[i]);
+        spmv(A, v.data(), t.data());
+        v = t;
+        M.solve(v.data());
+        for (int i = 0; i < k; ++i) gm::apply_householder(v.data() + i, m - i, col(i) + i + 1, tau[i]);
+        double tailsq = 0;
+        for (int i = k; i < m; i++) tailsq += v[i] * v[i];
+        if (tailsq != 0.0 && k < m) {
+            double beta;
+            gm::make_householder(v.data() + k, m - k, col(k) + k + 1, tau[k], beta);
+            gm::apply_householder(v.data() + k, m - k, col(k) + k + 1, tau[k]);
+        }
+        for (int i = 0; i + 1 < k; ++i) gm::apply_givens_t(v.data(), i, i + 1, G[i]);
+        if (k < m && v[k] != 0.0) {
+            G[k - 1] = gm::make_givens(v[k - 1], v[k]);
+            gm::apply_givens_t(v.data(), k - 1, k, G[k - 1]);
+            gm::apply_givens_t(w.data(), k - 1, k, G[k - 1]);
+        }
+        for (int i = 0; i < k; i++) col(k - 1)[i] = v[i];
+        err = std::fabs(w[k]) / r0norm;
+        const bool stop = (k == m || err < tol || it == iters);
+        if (stop || k == restart) {
+            // y = R^{-1} w[0:k] (R: upper triangle of H), then x += H_0 ... H_{k-1} [y; 0]
+            std::vector<double> y(w.begin(), w.begin() + k), xn(m, 0.0);
+            for (int i = k - 1; i >= 0; i--) {
+                double s = y[i];
+                for (int j = i + 1; j < k; j++) s -= col(j)[i] * y[j];
+                y[i] = s / col(i)[i];
+            }
+            for (int i = k - 1; i >= 0; --i) {
+                xn[i] += y[i];
+                gm::apply_householder(xn.data() + i, m - i, col(i) + i + 1, tau[i]);
+            }
+            for (int i = 0; i < m; i++) x[i] += xn[i];
+            if (stop) break;
+            k = 0;
+            start();
+        }
+    }
+    if (relres_out) *relres_out = err;
+    return it;
+}
+
 }  // namespace orc
 
 // =================================================================================
@@ -1489,6 +1641,10 @@ int orc_cg(void* p, const double* b, double* x, int iters, double tol, double* r
     auto h = (OrcHandle*)p;
     return cg(h->A, b, x, *h->t, iters, tol, relres);
 }
+int orc_gmres(void* p, const double* b, double* x, int iters, int restart, double tol, double* relres) {
+    auto h = (OrcHandle*)p;
+    return gmres(h->A, b, x, *h->t, iters, restart, tol, relres);
+}
 int orc_ir(void* p, const double* b, double* x, int iters, double tol) {
     auto h = (OrcHandle*)p;
     return ir(h->A, b, x, *h->t, iters, tol);
@@ -1544,6 +1700,22 @@ long long orc_get_op_matrix(void* p, int idx, double* out) {
     auto& v = (*it)->A->v;
     if (out) std::copy(v.begin(), v.end(), out);
     return (long long)v.size();
+}
+// U factor (n x n, column-major) and row permutation of a PLUQ op
+long long orc_get_op_u(void* p, int idx, double* out) {
+    auto it = ((OrcHandle*)p)->t->ops.begin();
+    std::advance(it, idx);
+    if (!(*it)->U) return 0;
+    auto& v = (*it)->U->v;
+    if (out) std::copy(v.begin(), v.end(), out);
+    return (long long)v.size();
+}
+int orc_get_op_perm(void* p, int idx, int* out) {
+    auto it = ((OrcHandle*)p)->t->ops.begin();
+    std::advance(it, idx);
+    auto& q = (*it)->p;
+    if (out) std::copy(q.begin(), q.end(), out);
+    return (int)q.size();
 }
 int orc_get_op_tau(void* p, int idx, double* out) {
     auto it = ((OrcHandle*)p)->t->ops.begin();

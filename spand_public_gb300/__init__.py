@@ -20,7 +20,8 @@ SVD, PLU, PLUQ, EVD, LLT, LDLT = range(6)
 SPD, SYM, GEN = range(3)
 MND, RB = range(2)
 
-OP_NAMES = {0: "ScalingLLT", 1: "GemmSymmOut", 2: "GemmSymmIn", 3: "Orthogonal", 4: "Merge", 5: "Split"}
+OP_NAMES = {0: "ScalingLLT", 1: "GemmSymmOut", 2: "GemmSymmIn", 3: "Orthogonal", 4: "Merge", 5: "Split",
+            6: "GemmOut", 7: "GemmIn", 8: "ScalingPLUQ"}
 
 _lib = None
 
@@ -53,6 +54,14 @@ _PROTOS = {
     "spand_tree_solve_device_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
     "spand_cg": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int,
                            C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "spand_gmres": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int,
+                              C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "spand_gmres_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double,
+                                     C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "spand_fgmres": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int,
+                               C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "spand_ir": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int,
+                           C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "spand_cg_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
                                   C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "spand_adjoint_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
@@ -78,6 +87,7 @@ _PROTOS = {
     "spand_tree_get_ops": (C.c_int, [C.c_void_p, C.c_void_p]),
     "spand_tree_get_op_matrix": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "spand_tree_get_op_tau": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "spand_tree_get_op_perm": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "spand_tree_timings": (C.c_int, [C.c_void_p, C.c_void_p]),
     "spand_tree_launches": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.c_int]),
     "spand_tree_device_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
@@ -209,6 +219,49 @@ class Tree:
                                C.byref(rr)))
         return x, it.value, rr.value
 
+    def gmres(self, b, iters=100, restart=None, tol=1e-12, x0=None, verb=False):
+        """Restarted GMRES (is.cpp:123-300) preconditioned by this tree, on the device
+        (restart defaults to iters, as the reference's driver passes it).  Returns
+        (x, iterations, |w_k| / |M^{-1} r_0|)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.float64)
+        restart = iters if restart is None else restart
+        it = C.c_int()
+        rr = C.c_double()
+        _check(self.L.spand_gmres(self.h, _ptr(b), _ptr(x), int(iters), int(restart), float(tol), int(bool(verb)),
+                                  C.byref(it), C.byref(rr)))
+        return x, it.value, rr.value
+
+    def gmres_device(self, b_ptr: int, x_ptr: int, iters=100, restart=None, tol=1e-12):
+        restart = iters if restart is None else restart
+        it = C.c_int()
+        rr = C.c_double()
+        _check(self.L.spand_gmres_device(self.h, C.c_void_p(b_ptr), C.c_void_p(x_ptr), int(iters), int(restart),
+                                         float(tol), C.byref(it), C.byref(rr)))
+        return it.value, rr.value
+
+    def fgmres(self, b, iters=100, restart=None, tol=1e-12, x0=None, verb=False):
+        """Flexible (right-preconditioned) GMRES: stops on the true |b - Ax| < tol |b| also
+        with an FP32 factor.  Returns (x, iterations, |b - Ax| / |b|)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.float64)
+        restart = iters if restart is None else restart
+        it = C.c_int()
+        rr = C.c_double()
+        _check(self.L.spand_fgmres(self.h, _ptr(b), _ptr(x), int(iters), int(restart), float(tol), int(bool(verb)),
+                                   C.byref(it), C.byref(rr)))
+        return x, it.value, rr.value
+
+    def ir(self, b, iters=100, tol=1e-12, x0=None, verb=False):
+        """Iterative refinement (is.cpp:12-37) on the device.  Returns (x, iterations, |b - Ax|/|b|)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.float64)
+        it = C.c_int()
+        rr = C.c_double()
+        _check(self.L.spand_ir(self.h, _ptr(b), _ptr(x), int(iters), float(tol), int(bool(verb)), C.byref(it),
+                               C.byref(rr)))
+        return x, it.value, rr.value
+
     def assemble_values(self, vals, on_device=False):
         """New values on the pattern of the last assemble() (CSC order).  vals: numpy array,
         or (on_device=True) the address of nnz doubles in device memory."""
@@ -294,6 +347,12 @@ class Tree:
         buf = np.zeros(max(rows * cols, 1))
         _check(self.L.spand_tree_get_op_matrix(self.h, int(idx), _ptr(buf)))
         return buf[: rows * cols].reshape((cols, rows)).T
+
+    def op_perm(self, idx, n):
+        """Row permutation of a ScalingPLUQ op (n entries)."""
+        buf = np.zeros(max(n, 1), dtype=np.int32)
+        _check(self.L.spand_tree_get_op_perm(self.h, int(idx), _ptr(buf)))
+        return buf[:n]
 
     def op_tau(self, idx, k):
         buf = np.zeros(max(k, 1))

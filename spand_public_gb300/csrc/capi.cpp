@@ -30,7 +30,8 @@ static int guard(F&& f) {
         return fail(SPAND_ERR_STATE, e.what());
     } catch (std::runtime_error& e) {
         std::string m = e.what();
-        if (m.find("Non-SPD") != std::string::npos) return fail(SPAND_ERR_NOT_SPD, m);
+        if (m.find("Non-SPD") != std::string::npos || m.find("Singular Pivot") != std::string::npos)
+            return fail(SPAND_ERR_NOT_SPD, m);
         if (m.find("cuda") != std::string::npos || m.find("CUDA") != std::string::npos) return fail(SPAND_ERR_CUDA, m);
         return fail(SPAND_ERR_UNSUPPORTED, m);
     } catch (spand::DeviceError& e) {
@@ -167,6 +168,57 @@ int spand_cg(spand_tree* t, const double* b, double* x, int iters, double tol, i
     });
 }
 
+int spand_gmres(spand_tree* t, const double* b, double* x, int iters, int restart, double tol, int verb,
+                int* iters_out, double* relres_out) {
+    CHECK_T(t);
+    if (!b || !x) return fail(SPAND_ERR_ARG, "null vector");
+    if (restart < 1) return fail(SPAND_ERR_ARG, "restart < 1");
+    return guard([&] {
+        double rr = 0;
+        int it = spaND::gmres(t->t->matrix(), b, x, *t->t, iters, restart, tol, verb != 0, &rr);
+        if (iters_out) *iters_out = it;
+        if (relres_out) *relres_out = rr;
+    });
+}
+
+int spand_gmres_device(spand_tree* t, const double* b, double* x, int iters, int restart, double tol,
+                       int* iters_out, double* relres_out) {
+    CHECK_T(t);
+    if (!b || !x) return fail(SPAND_ERR_ARG, "null vector");
+    if (restart < 1) return fail(SPAND_ERR_ARG, "restart < 1");
+    return guard([&] {
+        if (!t->t->device()) throw std::logic_error("gmres before factorize");
+        spand::PcgResult r = spand::device_gmres(*t->t->device(), t->t->device_csr(), b, x, iters, restart, tol);
+        if (iters_out) *iters_out = r.iterations;
+        if (relres_out) *relres_out = r.relres;
+    });
+}
+
+int spand_fgmres(spand_tree* t, const double* b, double* x, int iters, int restart, double tol, int verb,
+                 int* iters_out, double* relres_out) {
+    CHECK_T(t);
+    if (!b || !x) return fail(SPAND_ERR_ARG, "null vector");
+    if (restart < 1) return fail(SPAND_ERR_ARG, "restart < 1");
+    return guard([&] {
+        double rr = 0;
+        int it = spaND::fgmres(t->t->matrix(), b, x, *t->t, iters, restart, tol, verb != 0, &rr);
+        if (iters_out) *iters_out = it;
+        if (relres_out) *relres_out = rr;
+    });
+}
+
+int spand_ir(spand_tree* t, const double* b, double* x, int iters, double tol, int verb, int* iters_out,
+             double* relres_out) {
+    CHECK_T(t);
+    if (!b || !x) return fail(SPAND_ERR_ARG, "null vector");
+    return guard([&] {
+        double rr = 0;
+        int it = spaND::ir(t->t->matrix(), b, x, *t->t, iters, tol, verb != 0, &rr);
+        if (iters_out) *iters_out = it;
+        if (relres_out) *relres_out = rr;
+    });
+}
+
 int spand_cg_device(spand_tree* t, const double* b, double* x, int iters, double tol, int* iters_out,
                     double* relres_out) {
     CHECK_T(t);
@@ -209,7 +261,9 @@ int spand_batch_factorize(spand_tree* const* trees, int count, int* status_out) 
         std::string first;
         for (int k = 0; k < count; k++) {
             if (!status_out[k]) continue;
-            status_out[k] = msg[k].find("Non-SPD") != std::string::npos ? SPAND_ERR_NOT_SPD : SPAND_ERR_CUDA;
+            const bool piv = msg[k].find("Non-SPD") != std::string::npos ||
+                             msg[k].find("Singular Pivot") != std::string::npos;
+            status_out[k] = piv ? SPAND_ERR_NOT_SPD : SPAND_ERR_CUDA;
             if (first.empty()) first = "tree " + std::to_string(k) + ": " + msg[k];
         }
         if (!first.empty()) throw std::runtime_error(first);
@@ -307,6 +361,14 @@ int spand_tree_get_op_matrix(spand_tree* t, int idx, double* out) {
         std::vector<double> m;
         t->t->op_matrix(idx, m);
         std::memcpy(out, m.data(), m.size() * sizeof(double));
+    });
+}
+int spand_tree_get_op_perm(spand_tree* t, int idx, int* out) {
+    CHECK_T(t);
+    return guard([&] {
+        std::vector<int> m;
+        t->t->op_perm(idx, m);
+        std::memcpy(out, m.data(), m.size() * sizeof(int));
     });
 }
 int spand_tree_get_op_tau(spand_tree* t, int idx, double* out) {

@@ -97,6 +97,9 @@ class DeviceFactorBase {
     virtual void sizes(std::vector<int>& csize, std::vector<int>& rows0) = 0;
     virtual void block(int b, std::vector<double>& out) = 0;  // host copy (ld layout)
     virtual void ortho(int c, std::vector<double>& v, std::vector<double>& tau) = 0;
+    // PLU path: the row permutation of cluster c's pivot (capacity entries; the first
+    // csize[c] are meaningful)
+    virtual void lu_perm(int c, std::vector<int>& out) = 0;
     virtual int precision_bytes() const = 0;
     virtual cudaStream_t stream() const = 0;
     virtual size_t device_bytes() const = 0;
@@ -166,6 +169,20 @@ void device_pcg_multi(DeviceFactorBase& M, const DeviceCsr& A, const double* b, 
                       double tol, bool use_graph, int* iters_out, double* relres_out);
 
 void device_spmv(const DeviceCsr& A, const double* x, double* y, cudaStream_t s);
+
+// Restarted GMRES (is.cpp:123-300), left preconditioned by M, on the device; b, x device
+// vectors (x: initial guess).  relres: the reference's stopping quantity |w_k| / |M^{-1} r_0|.
+PcgResult device_gmres(DeviceFactorBase& M, const DeviceCsr& A, const double* b, double* x, int maxit, int restart,
+                       double tol);
+
+// Flexible (right-preconditioned) restarted GMRES, no reference counterpart: the
+// recurrence residual is the true |b - A x| whatever the factor's precision, so an FP32
+// factor reaches an FP64 tolerance; stops when |b - A x| < tol |b| (relres: that ratio).
+PcgResult device_fgmres(DeviceFactorBase& M, const DeviceCsr& A, const double* b, double* x, int maxit, int restart,
+                        double tol);
+
+// Iterative refinement (is.cpp:12-37) on the device; relres = |b - A x| / |b|.
+PcgResult device_ir(DeviceFactorBase& M, const DeviceCsr& A, const double* b, double* x, int maxit, double tol);
 
 // dst[map[k]] = src[k] for map[k] >= 0 (device arrays), on stream s
 void device_scatter(const double* src, const int* map, int64_t n, double* dst, cudaStream_t s);

@@ -360,8 +360,9 @@ struct SymTree {
 
 }  // namespace
 
-Plan build_plan(const Hierarchy& H, const Assembly& asmb, int skip, bool use_want_sparsify) {
+Plan build_plan(const Hierarchy& H, const Assembly& asmb, int skip, bool use_want_sparsify, bool lu) {
     Plan P;
+    P.lu = lu;
     const int nl = H.nlevels;
     const int nc = (int)H.start.size();
     P.nlevels = nl;
@@ -423,7 +424,7 @@ Plan build_plan(const Hierarchy& H, const Assembly& asmb, int skip, bool use_wan
             auto it = pending.find(tb);
             if (it == pending.end()) {
                 target_order.push_back(tb);
-                target_syrk.push_back(n1 == n2 ? 1 : 0);
+                target_syrk.push_back(n1 == n2 && !lu ? 1 : 0);
                 it = pending.emplace(tb, std::vector<SchurUpdate>()).first;
             }
             it->second.push_back({E1.block, t1 ? 1 : 0, E2.block, t2 ? 1 : 0, s});
@@ -433,24 +434,28 @@ Plan build_plan(const Hierarchy& H, const Assembly& asmb, int skip, bool use_wan
             int piv = T.edges[T.pivot(s)].block;
             L.elim_clusters.push_back(s);
             L.elim_pivots.push_back(piv);
+            L.elim_inv.push_back(lu ? T.new_block(s, s, BLK_STORED, cursor) : -1);
             auto ins = T.in_nbr(s);
             auto outs = T.out_nbr(s);
             for (int e : ins) L.elim_trsm.push_back({T.edges[e].block, s, 0});
             for (int e : outs) L.elim_trsm.push_back({T.edges[e].block, s, 1});
-            // schur_symmetric (tree.cpp:862-883)
-            for (int e1 : outs)
-                for (int e2 : outs)
-                    if (T.edges[e1].n2 >= T.edges[e2].n2) gemm_edges(e1, e2, false, true);
-            for (int e1 : ins)
-                for (int e2 : ins)
-                    if (T.edges[e1].n1 >= T.edges[e2].n1) gemm_edges(e1, e2, true, false);
+            if (!lu) {
+                // schur_symmetric (tree.cpp:862-883)
+                for (int e1 : outs)
+                    for (int e2 : outs)
+                        if (T.edges[e1].n2 >= T.edges[e2].n2) gemm_edges(e1, e2, false, true);
+                for (int e1 : ins)
+                    for (int e2 : ins)
+                        if (T.edges[e1].n1 >= T.edges[e2].n1) gemm_edges(e1, e2, true, false);
+            }
+            // the general path's Schur complement is this product alone (tree.cpp:943-947)
             for (int e1 : outs)
                 for (int e2 : ins) gemm_edges(e1, e2, false, false);
-            // record (tree.cpp:909-910, 885-892)
+            // record (tree.cpp:909-910, 885-892; PLU: 950-956)
             L.op_elim_llt.push_back(s);
             L.op_elim_llt_block.push_back(piv);
-            for (int e : T.out_nbr(s)) L.op_gemm.push_back({s, T.edges[e].n2, T.edges[e].block, 1});
-            for (int e : T.in_nbr(s)) L.op_gemm.push_back({s, T.edges[e].n1, T.edges[e].block, 2});
+            for (int e : T.out_nbr(s)) L.op_gemm.push_back({s, T.edges[e].n2, T.edges[e].block, lu ? 6 : 1});
+            for (int e : T.in_nbr(s)) L.op_gemm.push_back({s, T.edges[e].n1, T.edges[e].block, lu ? 7 : 2});
             T.set_eliminated(s);
         }
         L.fill_len = cursor - L.fill_off;
@@ -476,6 +481,7 @@ Plan build_plan(const Hierarchy& H, const Assembly& asmb, int skip, bool use_wan
                 int piv = T.edges[pe].block;
                 L.scale_clusters.push_back(c);
                 L.scale_pivots.push_back(piv);
+                L.scale_inv.push_back(lu ? T.new_block(c, c, BLK_STORED, cursor) : -1);
                 for (int e : T.in_nbr(c)) L.scale_trsm.push_back({T.edges[e].block, c, 0});
                 for (int e : T.out_nbr(c)) L.scale_trsm.push_back({T.edges[e].block, c, 1});
                 L.op_scale_llt.push_back(c);

@@ -76,13 +76,13 @@ struct SchurUpdate {
 
 struct SchurTarget {
     int target;     // target block
-    int syrk;       // n1 == n2 on the symmetric path: lower triangle only
+    int syrk;       // n1 == n2 on the symmetric path: lower triangle only (0 on the LU path)
     int first, count;  // slice of Plan::schur_updates, in reference order
 };
 
-// Triangular solve of a block by the Cholesky factor of a cluster's pivot:
-// side 0: B <- L^{-1} B (block rows belong to the cluster: in-edge)
-// side 1: B <- B L^{-T} (block columns belong to the cluster: out-edge)
+// Triangular solve of a block by the factor of a cluster's pivot:
+// side 0: B <- L^{-1} B (block rows belong to the cluster: in-edge); LU path: L^{-1} P^T B
+// side 1: B <- B L^{-T} (block columns belong to the cluster: out-edge); LU path: B U^{-1}
 struct TrsmItem {
     int block, cluster, side;
 };
@@ -112,13 +112,16 @@ struct MergeCopy {
 
 // Solve-time operations, grouped per level and phase (src/operations.cpp:31-208).
 struct GemmOpItem {
-    int self, nbr, block, kind;  // kind 1: GemmSymmOut (A: nbr x self), 2: GemmSymmIn (A: self x nbr)
+    // kind 1: GemmSymmOut (A: nbr x self), 2: GemmSymmIn (A: self x nbr); LU path:
+    // 6: GemmOut (A: nbr x self, forward only), 7: GemmIn (A: self x nbr, backward only)
+    int self, nbr, block, kind;
 };
 
 struct LevelPlan {
     // elimination (src/tree.cpp:1494-1506)
     std::vector<int> elim_clusters;
     std::vector<int> elim_pivots;
+    std::vector<int> elim_inv;  // LU path: block of the pivot's inverse factors (else -1)
     std::vector<TrsmItem> elim_trsm;
     int schur_first = 0, schur_count = 0;  // slice of Plan::schur_targets
     int64_t fill_off = 0, fill_len = 0;    // zero-initialised fill-in region
@@ -126,6 +129,7 @@ struct LevelPlan {
     bool scaled = false;
     std::vector<int> scale_clusters;
     std::vector<int> scale_pivots;
+    std::vector<int> scale_inv;
     std::vector<TrsmItem> scale_trsm;
     // sparsification (src/tree.cpp:1521-1532): waves of mutually non-adjacent clusters
     std::vector<std::vector<SparsifyItem>> waves;
@@ -137,7 +141,7 @@ struct LevelPlan {
     std::vector<MergeCopy> merge_copies;
     int64_t merge_off = 0, merge_len = 0;
     // solve operations recorded at this level
-    std::vector<int> op_elim_llt;         // eliminated clusters (ScalingLLT of the pivot block)
+    std::vector<int> op_elim_llt;         // eliminated clusters (ScalingLLT / ScalingPLUQ of the pivot block)
     std::vector<int> op_elim_llt_block;
     std::vector<GemmOpItem> op_gemm;      // in reference order
     std::vector<int> op_scale_llt;        // scaled clusters
@@ -148,6 +152,9 @@ struct LevelPlan {
 
 struct Plan {
     int nlevels = 0;
+    // LU path (SymmKind::GEN, ScalingKind::PLU): every stored block in both directions,
+    // partial-pivot LU of the pivots, Schur updates over (out-edge, in-edge) pairs
+    bool lu = false;
     int nclusters = 0;        // clusters of the hierarchy (siblings are implicit)
     std::vector<int> c_start, c_cap, c_level, c_order, c_hlevel, c_parent, c_sparsify;
     std::vector<std::vector<int>> c_children;
@@ -167,7 +174,8 @@ struct Plan {
     int64_t n_fill_blocks = 0, n_merge_blocks = 0;
 };
 
-// The symbolic replay of Tree::factorize (src/tree.cpp:1447-1551) for the LLT path.
+// The symbolic replay of Tree::factorize (src/tree.cpp:1447-1551) for the LLT path, or
+// for the PLU path (lu: general matrices, src/tree.cpp:614-742, 929-956).
 // leaves: per leaf cluster (start, size, level, order, sparsify); the hierarchy through
 // parent/children; assembled leaf blocks come from assemble().
 struct Hierarchy {
@@ -186,7 +194,7 @@ struct Assembly {
 };
 Assembly assembly_structure(const Hierarchy& H, const Csc& App, bool symmetric);
 
-Plan build_plan(const Hierarchy& H, const Assembly& asmb, int skip, bool use_want_sparsify);
+Plan build_plan(const Hierarchy& H, const Assembly& asmb, int skip, bool use_want_sparsify, bool lu = false);
 
 // For every entry k of A (natural ordering, CSC order): the element offset of A(r, c) in
 // the assembled level-0 blocks, or -1 when the entry is not stored (upper triangle of the

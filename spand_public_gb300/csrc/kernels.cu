@@ -619,6 +619,273 @@ __global__ void __launch_bounds__(256) trsm3_kernel(Ctx<T> c, const DTrsm* __res
 }
 
 // ------------------------------------------------------------------------------------
+// General (PLU) path.  Partial-pivot LU of a pivot block (tree.cpp:614-635; getf,
+// util.cpp:183-200, in the LAPACK dgetf2 order: the pivot is the first row of largest
+// magnitude, the rows are interchanged across the block, the column below is scaled by
+// the reciprocal of the pivot, then the rank-1 update), the split of split_LU
+// (util.cpp:212-227): L_s = L |D|^1/2, U_s = sign(D) |D|^1/2 D^-1 U, and the inverses of
+// both factors for the triangular products of the panels and of the solve:
+//   pivot block:   strict lower = L_s, upper with the diagonal = U_s
+//   inverse block: strict lower = L_s^{-1}, upper with the diagonal = U_s^{-1}
+//                  (diag L_s^{-1} = |diag U_s^{-1}|, not stored)
+//   perm[i]: the row of the pivot block that is row i of P^T A (swap2perm, util.cpp:76-88);
+//   swp[j]: the row interchanged with row j at step j (both at the cluster's offset poff)
+// One CTA per pivot.  The block is worked on in shared memory when n^2 + n elements fit,
+// else in the inverse block in global memory (n elements of shared memory).
+// ------------------------------------------------------------------------------------
+constexpr int LU_THREADS = 256;
+
+template <typename T>
+__device__ __forceinline__ void argmax_merge(T& v, int& i, T ov, int oi) {
+    if (ov > v || (ov == v && oi < i)) {
+        v = ov;
+        i = oi;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(LU_THREADS) getrf_kernel(Ctx<T> c, const int* __restrict__ pivots,
+                                                          const int* __restrict__ invs,
+                                                          const int* __restrict__ clusters, int count, int smem_elems,
+                                                          int* __restrict__ perm_store, int* __restrict__ swp_store,
+                                                          const long long* __restrict__ poff) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ T wv[LU_THREADS / 32];
+    __shared__ int wi[LU_THREADS / 32];
+    __shared__ int prow, bad;
+    const int item = blockIdx.x;
+    if (item >= count || c.status->not_spd) return;
+    const int cid = clusters[item];
+    const int n = c.csize[cid];
+    if (n == 0) return;
+    T* G = bptr(c, pivots[item]);
+    const int gld = c.blk[pivots[item]].ld;
+    T* Wg = bptr(c, invs[item]);
+    const int wld = c.blk[invs[item]].ld;
+    T* tmp = reinterpret_cast<T*>(smem_raw);
+    const bool in_smem = (long long)n * n + n <= smem_elems;
+    T* A = in_smem ? tmp + n : Wg;
+    const int lda = in_smem ? n : wld;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    int* swp = swp_store + poff[cid];
+    int* perm = perm_store + poff[cid];
+    for (int idx = tid; idx < n * n; idx += LU_THREADS) {
+        const int i = idx % n, j = idx / n;
+        A[i + (size_t)j * lda] = G[i + (size_t)j * gld];
+    }
+    if (tid == 0) bad = 0;
+    __syncthreads();
+    for (int j = 0; j < n; j++) {
+        T bv = T(-1);
+        int bi = n;
+        for (int i = j + tid; i < n; i += LU_THREADS) argmax_merge(bv, bi, (T)fabs(A[i + (size_t)j * lda]), i);
+        for (int o = 16; o > 0; o >>= 1) {
+            const T ov = __shfl_down_sync(0xffffffffu, bv, o);
+            const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+            argmax_merge(bv, bi, ov, oi);
+        }
+        if (lane == 0) {
+            wv[wid] = bv;
+            wi[wid] = bi;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            T v = wv[0];
+            int i = wi[0];
+            for (int w = 1; w < LU_THREADS / 32; w++) argmax_merge(v, i, wv[w], wi[w]);
+            prow = i;
+            swp[j] = i;
+            if (A[i + (size_t)j * lda] == T(0)) bad = 1;  // singular pivot (getf info > 0)
+        }
+        __syncthreads();
+        if (bad) break;
+        const int p = prow;
+        if (p != j)
+            for (int col = tid; col < n; col += LU_THREADS) {
+                const T a = A[j + (size_t)col * lda];
+                A[j + (size_t)col * lda] = A[p + (size_t)col * lda];
+                A[p + (size_t)col * lda] = a;
+            }
+        __syncthreads();
+        const T d = T(1) / A[j + (size_t)j * lda];
+        for (int i = j + 1 + tid; i < n; i += LU_THREADS) A[i + (size_t)j * lda] *= d;
+        __syncthreads();
+        const int m = n - j - 1;
+        for (int idx = tid; idx < m * m; idx += LU_THREADS) {
+            const int i = j + 1 + idx % m, col = j + 1 + idx / m;
+            A[i + (size_t)col * lda] -= A[i + (size_t)j * lda] * A[j + (size_t)col * lda];
+        }
+        __syncthreads();
+    }
+    if (bad) {
+        if (tid == 0) atomicCAS(&c.status->not_spd, 0, cid + 1);
+        return;
+    }
+    if (tid == 0) {
+        for (int i = 0; i < n; i++) perm[i] = i;
+        for (int i = 0; i < n; i++) {
+            const int s = swp[i], t = perm[s];
+            perm[s] = perm[i];
+            perm[i] = t;
+        }
+    }
+    // split_LU: off-diagonal entries from the unsplit diagonal, then the diagonal
+    for (int idx = tid; idx < n * n; idx += LU_THREADS) {
+        const int i = idx % n, j = idx / n;
+        if (i == j) continue;
+        T& a = A[i + (size_t)j * lda];
+        if (i > j) {
+            a = a * dsqrt((T)fabs(A[j + (size_t)j * lda]));
+        } else {
+            const T di = A[i + (size_t)i * lda];
+            const T sg = T((di > T(0)) - (di < T(0)));
+            a = sg * dsqrt((T)fabs(di)) * (a / di);
+        }
+    }
+    __syncthreads();
+    for (int j = tid; j < n; j += LU_THREADS) {
+        T& d = A[j + (size_t)j * lda];
+        const T sg = T((d > T(0)) - (d < T(0)));
+        d = sg * dsqrt((T)fabs(d));
+    }
+    __syncthreads();
+    for (int idx = tid; idx < n * n; idx += LU_THREADS) {
+        const int i = idx % n, j = idx / n;
+        G[i + (size_t)j * gld] = A[i + (size_t)j * lda];
+    }
+    __syncthreads();
+    // L_s^{-1} in the strict lower triangle, columns from the last: with L_s = [l x; 0 L22]
+    // partitioned at j, column j of the inverse below the diagonal is -L22^{-1} x / l
+    // (L_s(i,i) = |U_s(i,i)|, still on the diagonal)
+    for (int j = n - 1; j >= 0; j--) {
+        const int m = n - j - 1;
+        for (int i = tid; i < m; i += LU_THREADS) tmp[i] = A[(j + 1 + i) + (size_t)j * lda];
+        __syncthreads();
+        const T lj = T(1) / (T)fabs(A[j + (size_t)j * lda]);
+        for (int i = j + 1 + tid; i < n; i += LU_THREADS) {
+            T s = tmp[i - j - 1] / (T)fabs(A[i + (size_t)i * lda]);
+            for (int k = j + 1; k < i; k++) s += A[i + (size_t)k * lda] * tmp[k - j - 1];
+            A[i + (size_t)j * lda] = -lj * s;
+        }
+        __syncthreads();
+    }
+    // U_s^{-1} in the upper triangle, columns from the first (LAPACK dtrti2 order)
+    for (int j = 0; j < n; j++) {
+        for (int i = tid; i < j; i += LU_THREADS) tmp[i] = A[i + (size_t)j * lda];
+        if (tid == 0) A[j + (size_t)j * lda] = T(1) / A[j + (size_t)j * lda];
+        __syncthreads();
+        const T uj = A[j + (size_t)j * lda];
+        for (int i = tid; i < j; i += LU_THREADS) {
+            T s = 0;
+            for (int k = i; k < j; k++) s += A[i + (size_t)k * lda] * tmp[k];
+            A[i + (size_t)j * lda] = -uj * s;
+        }
+        __syncthreads();
+    }
+    if (in_smem)
+        for (int idx = tid; idx < n * n; idx += LU_THREADS) {
+            const int i = idx % n, j = idx / n;
+            Wg[i + (size_t)j * wld] = A[i + (size_t)j * lda];
+        }
+}
+
+// Panels of the PLU path (tree.cpp:668-689): in-edge blocks B <- L_s^{-1} P^T B (side 0),
+// out-edge blocks B <- B U_s^{-1} (side 1), as triangular products with the inverse block
+// (DTrsm::lblock).  Tiles of 32 independent indices as in trsm3_kernel; the rows of a
+// side-0 tile are gathered through perm while it is staged.  Blocks too large for the
+// shared-memory budget: one thread per index, in place (rows interchanged first).
+template <typename T>
+__global__ void __launch_bounds__(256) lu_trsm_kernel(Ctx<T> c, const DTrsm* __restrict__ items,
+                                                     const DTile* __restrict__ tiles, int ntiles, int smem_elems,
+                                                     const int* __restrict__ perm_store,
+                                                     const int* __restrict__ swp_store,
+                                                     const long long* __restrict__ poff) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* X = reinterpret_cast<T*>(smem_raw);
+    const int t = blockIdx.x;
+    if (t >= ntiles || c.status->not_spd) return;
+    const DTrsm it = items[tiles[t].item];
+    const int n = c.csize[it.cluster];
+    if (n == 0) return;
+    const T* W = bptr(c, it.lblock);
+    const int wld = c.blk[it.lblock].ld;
+    T* B = bptr(c, it.block);
+    const int bld = c.blk[it.block].ld;
+    const int m = it.side == 1 ? c.csize[c.blk[it.block].rowc] : c.csize[c.blk[it.block].colc];
+    const int r0 = tiles[t].tile_i * TRB;
+    if (r0 >= m) return;
+    const int tr = min(TRB, m - r0);
+    const long long sq = it.side == 1 ? 1 : bld, sk = it.side == 1 ? bld : 1;
+    T* Bt = B + (it.side == 1 ? (size_t)r0 : (size_t)r0 * bld);
+    const int* perm = perm_store + poff[it.cluster];
+    const int q = threadIdx.x % TRB, sub = threadIdx.x / TRB, lanes = blockDim.x / TRB;
+    if ((long long)tr * n <= smem_elems) {
+        for (int idx = threadIdx.x; idx < tr * n; idx += blockDim.x) {
+            int qq, k;
+            if (it.side == 1) {
+                qq = idx % tr;
+                k = idx / tr;
+            } else {
+                k = idx % n;
+                qq = idx / n;
+            }
+            const int kr = it.side == 1 ? k : perm[k];
+            X[qq + k * TRB] = Bt[qq * sq + (long long)kr * sk];
+        }
+        __syncthreads();
+        if (q < tr) {
+            const T* xr = X + q;
+            for (int cc = sub; cc < n; cc += lanes) {
+                T s0 = 0, s1 = 0;
+                if (it.side == 0) {
+                    int k = 0;
+                    for (; k + 1 < cc; k += 2) {
+                        s0 += W[cc + (size_t)k * wld] * xr[k * TRB];
+                        s1 += W[cc + (size_t)(k + 1) * wld] * xr[(k + 1) * TRB];
+                    }
+                    for (; k < cc; k++) s0 += W[cc + (size_t)k * wld] * xr[k * TRB];
+                    s0 += (T)fabs(W[cc + (size_t)cc * wld]) * xr[cc * TRB];
+                } else {
+                    const T* wc = W + (size_t)cc * wld;
+                    int k = 0;
+                    for (; k + 1 <= cc; k += 2) {
+                        s0 += xr[k * TRB] * wc[k];
+                        s1 += xr[(k + 1) * TRB] * wc[k + 1];
+                    }
+                    for (; k <= cc; k++) s0 += xr[k * TRB] * wc[k];
+                }
+                Bt[q * sq + (long long)cc * sk] = s0 + s1;
+            }
+        }
+    } else if (sub == 0 && q < tr) {
+        T* xr = Bt + q * sq;
+        if (it.side == 0) {
+            const int* swp = swp_store + poff[it.cluster];
+            for (int i = 0; i < n; i++) {
+                const int s = swp[i];
+                if (s != i) {
+                    const T a = xr[i * sk];
+                    xr[i * sk] = xr[s * sk];
+                    xr[s * sk] = a;
+                }
+            }
+            for (int cc = n - 1; cc >= 0; cc--) {
+                T s = (T)fabs(W[cc + (size_t)cc * wld]) * xr[cc * sk];
+                for (int k = 0; k < cc; k++) s += W[cc + (size_t)k * wld] * xr[k * sk];
+                xr[cc * sk] = s;
+            }
+        } else {
+            for (int cc = n - 1; cc >= 0; cc--) {
+                const T* wc = W + (size_t)cc * wld;
+                T s = 0;
+                for (int k = 0; k <= cc; k++) s += xr[k * sk] * wc[k];
+                xr[cc * sk] = s;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------
 // Schur complement updates grouped by target block, applied in the reference order
 // (tree.cpp:748-793, 858-883): C(n1 x n2) -= op1(B1) op2(B2).  32x32 output tile per
 // block, 256 threads, 2x2 outputs per thread, K staged through shared memory.
@@ -970,6 +1237,50 @@ struct XCtx {
     const long long* xoff;
     int nrhs;
 };
+
+// ScalingPLUQ of the solve (operations.cpp:112-127, q = identity for PLU): forward
+// x_s <- L_s^{-1} P^T x_s, backward x_s <- U_s^{-1} x_s, as products with the inverse
+// block (consecutive threads read consecutive rows of one of its columns).  One CTA per
+// (cluster, right-hand side); x_s is staged in shared memory.
+template <typename T>
+__global__ void __launch_bounds__(256) lu_apply_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ clusters,
+                                                      const int* __restrict__ invs, int count,
+                                                      const int* __restrict__ perm_store,
+                                                      const long long* __restrict__ poff, int fwd) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* xs = reinterpret_cast<T*>(smem_raw);
+    const int item = blockIdx.x, r = blockIdx.y;
+    if (item >= count) return;
+    const int cid = clusters[item];
+    const int n = c.rows0[cid];  // the size when the pivot was factored (before sparsification)
+    if (n == 0) return;
+    T* x = X.xs + X.xoff[cid] + (long long)r * X.xld;
+    const T* W = bptr(c, invs[item]);
+    const int wld = c.blk[invs[item]].ld;
+    const int* perm = perm_store + poff[cid];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) xs[i] = fwd ? x[perm[i]] : x[i];
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        T s0 = 0, s1 = 0;
+        if (fwd) {
+            int k = 0;
+            for (; k + 1 < i; k += 2) {
+                s0 += W[i + (size_t)k * wld] * xs[k];
+                s1 += W[i + (size_t)(k + 1) * wld] * xs[k + 1];
+            }
+            for (; k < i; k++) s0 += W[i + (size_t)k * wld] * xs[k];
+            s0 += (T)fabs(W[i + (size_t)i * wld]) * xs[i];
+        } else {
+            int k = i;
+            for (; k + 1 < n; k += 2) {
+                s0 += W[i + (size_t)k * wld] * xs[k];
+                s1 += W[i + (size_t)(k + 1) * wld] * xs[k + 1];
+            }
+            for (; k < n; k++) s0 += W[i + (size_t)k * wld] * xs[k];
+        }
+        x[i] = s0 + s1;
+    }
+}
 
 // b = P^T x (natural -> permuted leaf slots), FP64 in, T out
 template <typename T>
@@ -1564,6 +1875,12 @@ __global__ void cg_update_p_kernel(int n, double* p, const double* z, const doub
 
 __global__ void copy_scalar_kernel(double* sc, int dst, int src) { sc[dst] = sc[src]; }
 
+// y += a x
+__global__ void axpy_kernel(int n, double a, const double* __restrict__ x, double* __restrict__ y) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) y[i] += a * x[i];
+}
+
 __global__ void sub_kernel(int n, const double* a, const double* b, double* y) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i < n) y[i] = a[i] - b[i];
@@ -1772,6 +2089,7 @@ class DeviceFactor : public DeviceFactorBase {
     void upload(const Plan& P, const std::vector<int64_t>& amap) override {
         P_ = &P;
         nc_ = P.nclusters;
+        lu_ = P.lu;
         init_qrcp_limits();
         SPAND_CUDA(cudaStreamCreateWithFlags(&s2_, cudaStreamNonBlocking));
         SPAND_CUDA(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
@@ -1816,7 +2134,12 @@ class DeviceFactor : public DeviceFactorBase {
             D.elim_pivots = up(L.elim_pivots);
             D.elim_smem = smem_for(L.elim_clusters, P);
             D.elim_tri = build_trtri(L.elim_clusters, P);
-            build_trsm(L.elim_trsm, L.elim_pivots, L.elim_clusters, P, D.elim_trsm0, D.elim_trsm1);
+            // PLU: the panels are products with the inverse block
+            build_trsm(L.elim_trsm, lu_ ? L.elim_inv : L.elim_pivots, L.elim_clusters, P, D.elim_trsm0, D.elim_trsm1);
+            if (lu_) {
+                D.elim_inv = up(L.elim_inv);
+                D.elim_lu_smem = lu_smem_for(L.elim_clusters, P);
+            }
             {
                 std::vector<DTarget> tg;
                 std::vector<DTile> tiles;
@@ -1839,7 +2162,12 @@ class DeviceFactor : public DeviceFactorBase {
             D.scale_pivots = up(L.scale_pivots);
             D.scale_smem = smem_for(L.scale_clusters, P);
             D.scale_tri = build_trtri(L.scale_clusters, P);
-            build_trsm(L.scale_trsm, L.scale_pivots, L.scale_clusters, P, D.scale_trsm0, D.scale_trsm1);
+            build_trsm(L.scale_trsm, lu_ ? L.scale_inv : L.scale_pivots, L.scale_clusters, P, D.scale_trsm0,
+                       D.scale_trsm1);
+            if (lu_) {
+                D.scale_inv = up(L.scale_inv);
+                D.scale_lu_smem = lu_smem_for(L.scale_clusters, P);
+            }
             {
                 std::vector<int> all;
                 for (int cl = 0; cl < nc_; cl++)
@@ -1945,13 +2273,18 @@ class DeviceFactor : public DeviceFactorBase {
                 // eliminated cluster in reverse op order.
                 std::map<int, std::vector<DGemmOp>> fwd, bwd;
                 std::vector<int> fkeys, bkeys;
+                // PLU: GemmOut (6) acts in the forward sweep only, as GemmSymmOut does there;
+                // GemmIn (7) in the backward sweep only, as GemmSymmIn does there
+                // (operations.cpp:85-110)
                 for (const GemmOpItem& g : L.op_gemm) {
+                    if (g.kind == 7) continue;
                     if (!fwd.count(g.nbr)) fkeys.push_back(g.nbr);
-                    fwd[g.nbr].push_back({g.self, g.nbr, g.block, g.kind});
+                    fwd[g.nbr].push_back({g.self, g.nbr, g.block, g.kind == 6 ? 1 : g.kind});
                 }
                 for (auto it = L.op_gemm.rbegin(); it != L.op_gemm.rend(); ++it) {
+                    if (it->kind == 6) continue;
                     if (!bwd.count(it->self)) bkeys.push_back(it->self);
-                    bwd[it->self].push_back({it->self, it->nbr, it->block, it->kind});
+                    bwd[it->self].push_back({it->self, it->nbr, it->block, it->kind == 7 ? 2 : it->kind});
                 }
                 std::vector<DGroup> fg, bg;
                 std::vector<DGemmOp> fo, bo;
@@ -1998,6 +2331,10 @@ class DeviceFactor : public DeviceFactorBase {
         }
         jpvt_ = alloc<int>(max_cols);
         ipvt_ = alloc<int>(max_cols);
+        if (lu_) {
+            lu_perm_ = alloc<int>(std::max<int64_t>(P.x_len, 1));
+            lu_swp_ = alloc<int>(std::max<int64_t>(P.x_len, 1));
+        }
         colcount_ = alloc<int>(max_items);
         d_xoff_ = up(std::vector<long long>(P.c_xoff.begin(), P.c_xoff.end()));
         xld_ = P.x_len;
@@ -2013,6 +2350,11 @@ class DeviceFactor : public DeviceFactorBase {
         SPAND_CUDA(cudaFuncSetAttribute(potrf3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(trtri_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(trsm3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        if (lu_) {
+            SPAND_CUDA(cudaFuncSetAttribute(getrf_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+            SPAND_CUDA(cudaFuncSetAttribute(lu_trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+            SPAND_CUDA(cudaFuncSetAttribute(lu_apply_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        }
         fallback_ = alloc<int>(max_items);
         SPAND_CUDA(cudaFuncSetAttribute(trsv4_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(ortho_mrhs_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
@@ -2065,10 +2407,16 @@ class DeviceFactor : public DeviceFactorBase {
             LevelDev& D = levels_[l];
             cur_level_ = l;
             if (D.n_elim) {
-                launch_potrf(D.elim_pivots, D.elim_clusters, D.n_elim, D.elim_smem, D.elim_tri, D.elim_pc_cs,
-                             D.elim_pc_smem);
-                launch_trsm(D.elim_trsm0);
-                launch_trsm(D.elim_trsm1);
+                if (lu_) {
+                    launch_getrf(D.elim_pivots, D.elim_inv, D.elim_clusters, D.n_elim, D.elim_lu_smem);
+                    launch_lu_trsm(D.elim_trsm0);
+                    launch_lu_trsm(D.elim_trsm1);
+                } else {
+                    launch_potrf(D.elim_pivots, D.elim_clusters, D.n_elim, D.elim_smem, D.elim_tri, D.elim_pc_cs,
+                                 D.elim_pc_smem);
+                    launch_trsm(D.elim_trsm0);
+                    launch_trsm(D.elim_trsm1);
+                }
                 if (D.n_schur_tiles)
                     launch("schur", [&] {
                         schur_kernel<T><<<D.n_schur_tiles, 256, 0, s_>>>(ctx_, D.schur_targets, d_ups_, D.schur_tiles,
@@ -2076,10 +2424,16 @@ class DeviceFactor : public DeviceFactorBase {
                     });
             }
             if (D.scaled && D.n_scale) {
-                launch_potrf(D.scale_pivots, D.scale_clusters, D.n_scale, D.scale_smem, D.scale_tri,
-                             D.scale_pc_cs, D.scale_pc_smem);
-                launch_trsm(D.scale_trsm0);
-                launch_trsm(D.scale_trsm1);
+                if (lu_) {
+                    launch_getrf(D.scale_pivots, D.scale_inv, D.scale_clusters, D.n_scale, D.scale_lu_smem);
+                    launch_lu_trsm(D.scale_trsm0);
+                    launch_lu_trsm(D.scale_trsm1);
+                } else {
+                    launch_potrf(D.scale_pivots, D.scale_clusters, D.n_scale, D.scale_smem, D.scale_tri,
+                                 D.scale_pc_cs, D.scale_pc_smem);
+                    launch_trsm(D.scale_trsm0);
+                    launch_trsm(D.scale_trsm1);
+                }
             }
             if (D.n_level)
                 launch("snapshot", [&] {
@@ -2151,7 +2505,8 @@ class DeviceFactor : public DeviceFactorBase {
         }
         const DStatus st = *h_status_;
         if (st.not_spd)
-            throw DeviceError{SPAND_ERR_NOT_SPD, "Error: Non-SPD Pivot (cluster " + std::to_string(st.not_spd - 1) + ")"};
+            throw DeviceError{SPAND_ERR_NOT_SPD, std::string(lu_ ? "Error: Singular Pivot" : "Error: Non-SPD Pivot") +
+                                                     " (cluster " + std::to_string(st.not_spd - 1) + ")"};
         factored_ = true;
         if (!tuned_) tune_qrcp();
     }
@@ -2298,6 +2653,14 @@ class DeviceFactor : public DeviceFactorBase {
         out.assign(tmp.begin(), tmp.end());
     }
 
+    void lu_perm(int cl, std::vector<int>& out) override {
+        out.assign(P_->c_cap[cl], 0);
+        if (!lu_perm_ || out.empty()) return;
+        SPAND_CUDA(cudaMemcpyAsync(out.data(), lu_perm_ + P_->c_xoff[cl], out.size() * sizeof(int),
+                                   cudaMemcpyDeviceToHost, s_));
+        SPAND_CUDA(cudaStreamSynchronize(s_));
+    }
+
     void ortho(int cl, std::vector<double>& v, std::vector<double>& tau) override {
         for (const LevelPlan& L : P_->levels)
             for (const auto& wave : L.waves)
@@ -2370,6 +2733,8 @@ class DeviceFactor : public DeviceFactorBase {
         DTile* merge_tiles = nullptr;
         int n_merge_tiles = 0;
         int n_elim_llt = 0, n_scale_llt = 0;
+        int *elim_inv = nullptr, *scale_inv = nullptr;  // PLU: inverse blocks, parallel to the pivots
+        int elim_lu_smem = 0, scale_lu_smem = 0;
         int *elim_llt = nullptr, *elim_llt_blk = nullptr, *scale_llt = nullptr, *scale_llt_blk = nullptr;
         int x_smem_elim = 0, x_smem_scale = 0, x_smem_ortho = 0;
         DTile* gf_tiles32 = nullptr;  // forward Gemm groups in 32-row tiles (many right-hand sides)
@@ -2618,6 +2983,29 @@ class DeviceFactor : public DeviceFactorBase {
                                                                    pc_cs > 0 ? 0LL : (long long)(smem / (int)sizeof(T)));
             });
     }
+    void launch_getrf(int* pivots, int* invs, int* clusters, int n, int smem) {
+        launch("getrf", [&] {
+            getrf_kernel<T><<<n, LU_THREADS, smem, s_>>>(ctx_, pivots, invs, clusters, n, smem / (int)sizeof(T),
+                                                          lu_perm_, lu_swp_, d_xoff_);
+        });
+    }
+    void launch_lu_trsm(const TrsmDev& t) {
+        if (!t.ntiles) return;
+        launch("trsm", [&] {
+            lu_trsm_kernel<T><<<t.ntiles, 256, t.smem, s_>>>(ctx_, t.items, t.tiles, t.ntiles, t.smem / (int)sizeof(T),
+                                                             lu_perm_, lu_swp_, d_xoff_);
+        });
+    }
+    // shared memory of the PLU pivot kernel: the whole block and one column where it fits,
+    // else the column alone (the block is then worked on in global memory)
+    int lu_smem_for(const std::vector<int>& clusters, const Plan& P) {
+        int64_t mx = 1;
+        for (int c0 : clusters) mx = std::max<int64_t>(mx, P.c_cap[c0]);
+        const int64_t full = (mx * mx + mx) * (int64_t)sizeof(T);
+        if (full <= 200 * 1024) return (int)full;
+        if (mx * (int64_t)sizeof(T) > 200 * 1024) throw DeviceError{SPAND_ERR_UNSUPPORTED, "pivot too large"};
+        return (int)(mx * sizeof(T));
+    }
     void launch_trsm(const TrsmDev& t) {
         if (!t.ntiles) return;
         launch("trsm", [&] {
@@ -2700,6 +3088,15 @@ class DeviceFactor : public DeviceFactorBase {
         });
         auto trsv = [&](const int* clusters, const int* blks, const int2* tv, int ntv, int smem, int trans) {
             if (!ntv) return;
+            if (lu_) {
+                // PLU: blks are the inverse blocks; one CTA per (cluster, right-hand side)
+                const int count = cur_count_;
+                launch("trsv", [&] {
+                    lu_apply_kernel<T><<<dim3((unsigned)count, (unsigned)nrhs), 256, smem, s_>>>(
+                        ctx_, X, clusters, blks, count, lu_perm_, d_xoff_, trans ? 0 : 1);
+                });
+                return;
+            }
             launch("trsv", [&] {
                 if (mr)
                     trsv_mrhs_kernel<T><<<ntv, 256, 0, s_>>>(ctx_, X, clusters, blks, tv, trans, tmp, tv_count_);
@@ -2731,7 +3128,8 @@ class DeviceFactor : public DeviceFactorBase {
         for (int l = 0; l < P.nlevels; l++) {
             LevelDev& D = levels_[l];
             cur_level_ = l;
-            trsv(D.elim_llt, D.elim_llt_blk, D.elim_tv, D.n_elim_tv, D.x_smem_elim, 0);
+            cur_count_ = D.n_elim_llt;
+            trsv(D.elim_llt, lu_ ? D.elim_inv : D.elim_llt_blk, D.elim_tv, D.n_elim_tv, D.x_smem_elim, 0);
             if (D.n_gf)
                 launch("gemm_fwd", [&] {
                     if (mr)
@@ -2740,7 +3138,8 @@ class DeviceFactor : public DeviceFactorBase {
                         gemm_fwd2_kernel<T><<<D.n_gf_tiles * nrhs, 256, 0, s_>>>(ctx_, X, D.gf, D.gfo, D.gf_tiles,
                                                                                  D.n_gf_tiles, 0);
                 });
-            trsv(D.scale_llt, D.scale_llt_blk, D.scale_tv, D.n_scale_tv, D.x_smem_scale, 0);
+            cur_count_ = D.n_scale_llt;
+            trsv(D.scale_llt, lu_ ? D.scale_inv : D.scale_llt_blk, D.scale_tv, D.n_scale_tv, D.x_smem_scale, 0);
             ortho(D, 1);
             merge(D, 1);
         }
@@ -2749,7 +3148,8 @@ class DeviceFactor : public DeviceFactorBase {
             cur_level_ = l;
             merge(D, 0);
             ortho(D, 0);
-            trsv(D.scale_llt, D.scale_llt_blk, D.scale_tv, D.n_scale_tv, D.x_smem_scale, 1);
+            cur_count_ = D.n_scale_llt;
+            trsv(D.scale_llt, lu_ ? D.scale_inv : D.scale_llt_blk, D.scale_tv, D.n_scale_tv, D.x_smem_scale, 1);
             if (D.n_gb)
                 launch("gemm_bwd", [&] {
                     if (mr)
@@ -2758,7 +3158,8 @@ class DeviceFactor : public DeviceFactorBase {
                         gemm_bwd2_kernel<T><<<D.n_gb_tiles * nrhs, 256, 0, s_>>>(ctx_, X, D.gb, D.gbo, D.gb_tiles,
                                                                                  D.n_gb_tiles);
                 });
-            trsv(D.elim_llt, D.elim_llt_blk, D.elim_tv, D.n_elim_tv, D.x_smem_elim, 1);
+            cur_count_ = D.n_elim_llt;
+            trsv(D.elim_llt, lu_ ? D.elim_inv : D.elim_llt_blk, D.elim_tv, D.n_elim_tv, D.x_smem_elim, 1);
         }
         cur_level_ = -1;
         launch("perm", [&] {
@@ -2792,6 +3193,10 @@ class DeviceFactor : public DeviceFactorBase {
     DStatus* h_status_ = nullptr;  // pinned copy of the status word, filled by factorize_enqueue
     cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
     int* pc_fallback_ = nullptr;  // pivots the cluster Cholesky could not hold
+    bool lu_ = false;             // PLU path (general matrices)
+    int* lu_perm_ = nullptr;      // per cluster at its solve-slot offset: row permutation of its pivot
+    int* lu_swp_ = nullptr;       // and the row interchanges that make it
+    int cur_count_ = 0;           // clusters of the pivot op list being applied in the solve
     bool tuned_ = false;
     int cur_level_ = -1;
     // in-kernel phase timing of the QRCP of one level (SPAND_QC_PROBE=<level>)
@@ -3111,6 +3516,511 @@ void device_pcg_multi(DeviceFactorBase& M, const DeviceCsr& A, const double* b, 
         if (w.h_active[j]) iters_out[j] = i + 1;
     SPAND_CUDA(cudaGetLastError());
     SPAND_CUDA(cudaStreamSynchronize(s));
+}
+
+
+// ------------------------------------------------------------------------------------
+// GMRES (is.cpp:123-300): Eigen's restarted GMRES with Householder Arnoldi, left
+// preconditioned by M.  The reflectors H_i = I - tau_i u_i u_i^T (u_i: zero above row i,
+// one at row i) are the columns of Y (m x (restart+1), FP64, device); their product is
+// kept in compact WY form, H_0 H_1 ... H_{k-1} = I - Y_k T_k Y_k^T (T_k upper triangular,
+// host), so that each application of the k reflectors of an iteration becomes one
+// reduction Y^T v and one update v - Y z instead of k dependent rank-1 steps.  The
+// Hessenberg columns, Givens rotations and the small triangular solve stay on the host,
+// as small vectors.  Same arithmetic as the sequential reflectors up to rounding.
+// ------------------------------------------------------------------------------------
+constexpr int GM_BLOCKS = 304;
+
+// partial[b * k + i] = sum over block b's share of rows [r0, m) of Y[r + i ldy] v[r]
+__global__ void gm_dots_kernel(int r0, int m, int k, const double* __restrict__ Y, long long ldy,
+                               const double* __restrict__ v, double* __restrict__ partial) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const long long len = m - r0;
+    const long long span = (len + gridDim.x - 1) / gridDim.x;
+    const long long a = r0 + (long long)blockIdx.x * span;
+    const long long e = min((long long)m, a + span);
+    for (int i = warp; i < k; i += nw) {
+        const double* y = Y + (long long)i * ldy;
+        double s = 0;
+        for (long long r = a + lane; r < e; r += 32) s += y[r] * v[r];
+        s = warp_sum(s);
+        if (lane == 0) partial[(long long)blockIdx.x * k + i] = s;
+    }
+}
+
+__global__ void gm_dots_final_kernel(int nb, int k, const double* __restrict__ partial, double* __restrict__ out) {
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (i >= k) return;
+    double s = 0;
+    for (int b = lane; b < nb; b += 32) s += partial[(long long)b * k + i];
+    s = warp_sum(s);
+    if (lane == 0) out[i] = s;
+}
+
+// out[r] = base[r] - sum_{i<k} Y[r + i ldy] z[i]; zy = (z[0..k), y[0..k)).
+// mode 0: base = e_unit; 1: base = out; 2: base = out + (r < k ? y[r] : 0)
+__global__ void gm_update_kernel(int m, int k, const double* __restrict__ Y, long long ldy,
+                                 const double* __restrict__ zy, double* __restrict__ out, int mode, int unit) {
+    extern __shared__ double zs[];
+    for (int i = threadIdx.x; i < 2 * k; i += blockDim.x) zs[i] = zy[i];
+    __syncthreads();
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r >= m) return;
+    double s = 0;
+    for (int i = 0; i < k; i++) s += Y[r + i * ldy] * zs[i];
+    double base = mode == 0 ? (r == unit ? 1.0 : 0.0) : out[r];
+    if (mode == 2 && r < k) base += zs[k + r];
+    out[r] = base - s;
+}
+
+// column k of Y: zero above row k, one at row k, v[r] / d below (zero when d == 0)
+__global__ void gm_reflector_kernel(int m, int k, double* __restrict__ ycol, const double* __restrict__ v, double d) {
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r >= m) return;
+    ycol[r] = r < k ? 0.0 : (r == k ? 1.0 : (d != 0.0 ? v[r] / d : 0.0));
+}
+
+namespace {
+struct GmGivens {
+    double c = 1, s = 0;
+};
+// G with G^T (p, q) = (r, 0) (Eigen's real JacobiRotation::makeGivens)
+GmGivens gm_make_givens(double p, double q) {
+    GmGivens g;
+    if (q == 0) {
+        g.c = p < 0 ? -1 : 1;
+        g.s = 0;
+    } else if (p == 0) {
+        g.c = 0;
+        g.s = q < 0 ? 1 : -1;
+    } else if (std::fabs(p) > std::fabs(q)) {
+        double t = q / p, u = std::sqrt(1 + t * t);
+        if (p < 0) u = -u;
+        g.c = 1 / u;
+        g.s = -t * g.c;
+    } else {
+        double t = p / q, u = std::sqrt(1 + t * t);
+        if (q < 0) u = -u;
+        g.s = -1 / u;
+        g.c = -t * g.s;
+    }
+    return g;
+}
+void gm_rotate(double* v, int i, const GmGivens& g) {
+    const double x = v[i], y = v[i + 1];
+    v[i] = g.c * x - g.s * y;
+    v[i + 1] = g.s * x + g.c * y;
+}
+}  // namespace
+
+PcgResult device_gmres(DeviceFactorBase& M, const DeviceCsr& A, const double* b, double* x, int maxit, int restart,
+                       double tol) {
+    const int m = A.n;
+    const int R = std::max(1, std::min(restart, m));
+    if (2 * (int64_t)(R + 1) * (int64_t)sizeof(double) > 200 * 1024)
+        throw DeviceError{SPAND_ERR_UNSUPPORTED, "GMRES restart length above 12799"};
+    static std::once_flag attr_once;
+    std::call_once(attr_once, [] {
+        SPAND_CUDA(cudaFuncSetAttribute(gm_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    });
+    cudaStream_t s = M.stream();
+    PcgResult res;
+    const unsigned gb = (unsigned)((m + 255) / 256);
+    const int nb = GM_BLOCKS;
+    const long long ldy = m;
+    // device: two m-vectors, Y, partials, reduction output, z/y; host: pinned scalars
+    double *v = nullptr, *t = nullptr, *Y = nullptr, *partial = nullptr, *dout = nullptr, *dzy = nullptr, *hp = nullptr;
+    auto cleanup = [&] {
+        cudaFree(v); cudaFree(t); cudaFree(Y); cudaFree(partial); cudaFree(dout); cudaFree(dzy);
+        if (hp) cudaFreeHost(hp);
+    };
+    try {
+        SPAND_CUDA(cudaMalloc(&v, (size_t)m * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&t, (size_t)m * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&Y, (size_t)m * (R + 1) * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&partial, (size_t)nb * (R + 1) * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&dout, (size_t)(R + 2) * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&dzy, (size_t)2 * (R + 1) * sizeof(double)));
+        SPAND_CUDA(cudaMallocHost(&hp, (size_t)4 * (R + 2) * sizeof(double)));
+        double* hd = hp;                 // reduction results
+        double* hz = hp + (R + 2);       // z, y staged for upload
+        double* hv = hp + 3 * (R + 2);   // leading entries of v
+        auto launched = [&](int k) { M.add_launches(k); };
+        // k dot products Y[:, i] . w over rows [r0, m) -> hd[0..k)
+        auto dots = [&](int r0, int k, const double* Yp, long long ld, const double* w) {
+            if (k <= 0) return;
+            if (r0 >= m) {
+                for (int i = 0; i < k; i++) hd[i] = 0;
+                return;
+            }
+            gm_dots_kernel<<<nb, 256, 0, s>>>(r0, m, k, Yp, ld, w, partial);
+            gm_dots_final_kernel<<<(unsigned)((k + 7) / 8), 256, 0, s>>>(nb, k, partial, dout);
+            launched(2);
+            SPAND_CUDA(cudaMemcpyAsync(hd, dout, (size_t)k * sizeof(double), cudaMemcpyDeviceToHost, s));
+            SPAND_CUDA(cudaStreamSynchronize(s));
+        };
+        auto update = [&](int k, double* out, int mode, int unit) {
+            SPAND_CUDA(cudaMemcpyAsync(dzy, hz, (size_t)2 * std::max(k, 1) * sizeof(double), cudaMemcpyHostToDevice, s));
+            gm_update_kernel<<<gb, 256, (size_t)2 * std::max(k, 1) * sizeof(double), s>>>(m, k, Y, ldy, dzy, out, mode,
+                                                                                         unit);
+            launched(1);
+        };
+        dots(0, 1, b, 0, b);
+        if (std::sqrt(hd[0]) <= std::numeric_limits<double>::min()) {
+            SPAND_CUDA(cudaMemsetAsync(x, 0, (size_t)m * sizeof(double), s));
+            SPAND_CUDA(cudaStreamSynchronize(s));
+            cleanup();
+            res.iterations = 1;
+            return res;
+        }
+        std::vector<double> Ytop((size_t)(R + 1) * (R + 1), 0.0), T((size_t)(R + 1) * (R + 1), 0.0);
+        std::vector<double> Hr((size_t)(R + 1) * (R + 1), 0.0), w(R + 1, 0.0), tau(R + 1, 0.0), q(R + 1), z(R + 1);
+        std::vector<GmGivens> G(R);
+        auto ytop = [&](int i, int r) -> double& { return Ytop[(size_t)i * (R + 1) + r]; };  // Y[r, i], r <= R
+        auto Tm = [&](int i, int j) -> double& { return T[(size_t)j * (R + 1) + i]; };
+        auto Hc = [&](int i, int j) -> double& { return Hr[(size_t)j * (R + 1) + i]; };
+        // reflector k from v[k:] (c0 = v[k]); returns the new v[k]; fills Y column k, its top,
+        // tau[k] and column k of T
+        auto tail_of = [&](int k) {  // |v[k+1:]|^2
+            if (k + 1 >= m) return 0.0;
+            dots(k + 1, 1, v, 0, v);
+            return hd[0];
+        };
+        auto new_reflector = [&](int k, double c0, double tail) -> double {
+            double beta = c0, d = 0, tk = 0;
+            if (tail > std::numeric_limits<double>::min()) {
+                beta = std::sqrt(c0 * c0 + tail);
+                if (c0 >= 0) beta = -beta;
+                d = c0 - beta;
+                tk = (beta - c0) / beta;
+            }
+            gm_reflector_kernel<<<gb, 256, 0, s>>>(m, k, Y + (size_t)k * ldy, v, d);
+            launched(1);
+            const int top = std::min(R + 1, m);
+            SPAND_CUDA(cudaMemcpyAsync(&ytop(k, 0), Y + (size_t)k * ldy, (size_t)top * sizeof(double),
+                                       cudaMemcpyDeviceToHost, s));
+            SPAND_CUDA(cudaStreamSynchronize(s));
+            tau[k] = tk;
+            // T_{k+1} = [T_k, -tau_k T_k (Y_k^T u_k); 0, tau_k]
+            for (int i = 0; i <= k; i++) Tm(i, k) = 0;
+            Tm(k, k) = tk;
+            if (k > 0 && tk != 0) {
+                dots(0, k, Y, ldy, Y + (size_t)k * ldy);
+                for (int i = 0; i < k; i++) {
+                    double acc = 0;
+                    for (int j = i; j < k; j++) acc += Tm(i, j) * hd[j];
+                    Tm(i, k) = -tk * acc;
+                }
+            }
+            // v[k] after H_k: c0 - tau (c0 + ess . v_tail), ess . v_tail = tail / d
+            return tk == 0 ? c0 : c0 - tk * (c0 + tail / d);
+        };
+        double r0norm = -1;
+        auto start = [&] {
+            device_spmv(A, x, t, s);
+            sub_kernel<<<gb, 256, 0, s>>>(m, b, t, v);
+            launched(2);
+            M.solve_device(v, 1, m);
+            if (r0norm < 0) {
+                dots(0, 1, v, 0, v);
+                r0norm = std::sqrt(hd[0]);
+            }
+            SPAND_CUDA(cudaMemcpyAsync(hv, v, sizeof(double), cudaMemcpyDeviceToHost, s));
+            SPAND_CUDA(cudaStreamSynchronize(s));
+            std::fill(w.begin(), w.end(), 0.0);
+            std::fill(tau.begin(), tau.end(), 0.0);
+            std::fill(Hr.begin(), Hr.end(), 0.0);
+            w[0] = new_reflector(0, hv[0], tail_of(0));
+        };
+        start();
+        if (r0norm == 0) {
+            cleanup();
+            res.iterations = 1;
+            return res;
+        }
+        int it = 0;
+        double err = 1.0;
+        for (int k = 1; k <= R; ++k) {
+            ++it;
+            // v = H_0 ... H_{k-1} e_{k-1} = e_{k-1} - Y_k T_k Y_k[k-1, :]^T
+            for (int i = 0; i < k; i++) q[i] = ytop(i, k - 1);
+            for (int i = 0; i < k; i++) {
+                double acc = 0;
+                for (int j = i; j < k; j++) acc += Tm(i, j) * q[j];
+                hz[i] = acc;
+            }
+            update(k, v, 0, k - 1);
+            device_spmv(A, v, t, s);
+            launched(1);
+            std::swap(v, t);
+            M.solve_device(v, 1, m);
+            // v = H_{k-1} ... H_0 v = v - Y_k T_k^T (Y_k^T v)
+            dots(0, k, Y, ldy, v);
+            for (int i = 0; i < k; i++) {
+                double acc = 0;
+                for (int j = 0; j <= i; j++) acc += Tm(j, i) * hd[j];
+                hz[i] = acc;
+            }
+            update(k, v, 1, 0);
+            const int lead = std::min(k + 1, m);
+            SPAND_CUDA(cudaMemcpyAsync(hv, v, (size_t)lead * sizeof(double), cudaMemcpyDeviceToHost, s));
+            SPAND_CUDA(cudaStreamSynchronize(s));
+            if (k < m) {
+                const double tail = tail_of(k);
+                if (hv[k] * hv[k] + tail != 0.0) hv[k] = new_reflector(k, hv[k], tail);
+                else {
+                    tau[k] = 0;
+                    gm_reflector_kernel<<<gb, 256, 0, s>>>(m, k, Y + (size_t)k * ldy, v, 0.0);
+                    launched(1);
+                    for (int r = 0; r <= R; r++) ytop(k, r) = r == k ? 1.0 : 0.0;
+                    for (int i = 0; i <= k; i++) Tm(i, k) = 0;
+                }
+            }
+            for (int i = 0; i + 1 < k; ++i) gm_rotate(hv, i, G[i]);
+            if (k < m && hv[k] != 0) {
+                G[k - 1] = gm_make_givens(hv[k - 1], hv[k]);
+                gm_rotate(hv, k - 1, G[k - 1]);
+                gm_rotate(w.data(), k - 1, G[k - 1]);
+            }
+            for (int i = 0; i < k; i++) Hc(i, k - 1) = hv[i];
+            err = std::fabs(w[k]) / r0norm;
+            const bool stop = (k == m || err < tol || it == maxit);
+            if (stop || k == R) {
+                // y = R^{-1} w[0:k]; x += H_0 ... H_{k-1} [y; 0] = [y; 0] - Y T (Y[0:k, :]^T y)
+                std::vector<double> y(w.begin(), w.begin() + k);
+                for (int i = k - 1; i >= 0; i--) {
+                    double acc = y[i];
+                    for (int j = i + 1; j < k; j++) acc -= Hc(i, j) * y[j];
+                    y[i] = acc / Hc(i, i);
+                }
+                for (int i = 0; i < k; i++) {
+                    double acc = 0;
+                    for (int r = 0; r < k; r++) acc += ytop(i, r) * y[r];
+                    q[i] = acc;
+                }
+                for (int i = 0; i < k; i++) {
+                    double acc = 0;
+                    for (int j = i; j < k; j++) acc += Tm(i, j) * q[j];
+                    hz[i] = acc;
+                    hz[k + i] = y[i];
+                }
+                update(k, x, 2, 0);
+                if (stop) break;
+                k = 0;
+                start();
+            }
+        }
+        SPAND_CUDA(cudaGetLastError());
+        SPAND_CUDA(cudaStreamSynchronize(s));
+        res.iterations = it;
+        res.relres = err;
+    } catch (...) {
+        cleanup();
+        throw;
+    }
+    cleanup();
+    return res;
+}
+
+// v_out = v_in / h
+__global__ void gm_scale_kernel(int m, const double* __restrict__ in, double* __restrict__ out, double h) {
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r < m) out[r] = in[r] / h;
+}
+
+// Flexible GMRES (no reference counterpart): right preconditioned, z_j = M^{-1} v_j kept,
+// Arnoldi on A z_j with classical Gram-Schmidt applied twice, restarted from the true
+// residual.  The Arnoldi relation A Z_k = V_{k+1} H_k holds in FP64 whatever precision the
+// preconditioner computes in, so the recurrence residual is the true |b - A x| (up to FP64
+// rounding) and a reduced-precision factor still reaches an FP64 tolerance.  Stops when
+// |b - A x| < tol |b|; relres: that ratio.
+PcgResult device_fgmres(DeviceFactorBase& M, const DeviceCsr& A, const double* b, double* x, int maxit, int restart,
+                        double tol) {
+    const int m = A.n;
+    const int R = std::max(1, std::min(restart, m));
+    if (2 * (int64_t)(R + 1) * (int64_t)sizeof(double) > 200 * 1024)
+        throw DeviceError{SPAND_ERR_UNSUPPORTED, "FGMRES restart length above 12799"};
+    static std::once_flag attr_once;
+    std::call_once(attr_once, [] {
+        SPAND_CUDA(cudaFuncSetAttribute(gm_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    });
+    cudaStream_t s = M.stream();
+    PcgResult res;
+    const unsigned gb = (unsigned)((m + 255) / 256);
+    const int nb = GM_BLOCKS;
+    const long long ld = m;
+    double *V = nullptr, *Z = nullptr, *w = nullptr, *partial = nullptr, *dout = nullptr, *dzy = nullptr, *hp = nullptr;
+    auto cleanup = [&] {
+        cudaFree(V); cudaFree(Z); cudaFree(w); cudaFree(partial); cudaFree(dout); cudaFree(dzy);
+        if (hp) cudaFreeHost(hp);
+    };
+    try {
+        SPAND_CUDA(cudaMalloc(&V, (size_t)m * (R + 1) * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&Z, (size_t)m * R * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&w, (size_t)m * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&partial, (size_t)nb * (R + 1) * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&dout, (size_t)(R + 2) * sizeof(double)));
+        SPAND_CUDA(cudaMalloc(&dzy, (size_t)2 * (R + 1) * sizeof(double)));
+        SPAND_CUDA(cudaMallocHost(&hp, (size_t)3 * (R + 2) * sizeof(double)));
+        double* hd = hp;
+        double* hz = hp + (R + 2);
+        auto dots = [&](int k, const double* Yp, long long ldy, const double* v) {
+            gm_dots_kernel<<<nb, 256, 0, s>>>(0, m, k, Yp, ldy, v, partial);
+            gm_dots_final_kernel<<<(unsigned)((k + 7) / 8), 256, 0, s>>>(nb, k, partial, dout);
+            M.add_launches(2);
+            SPAND_CUDA(cudaMemcpyAsync(hd, dout, (size_t)k * sizeof(double), cudaMemcpyDeviceToHost, s));
+            SPAND_CUDA(cudaStreamSynchronize(s));
+        };
+        auto update = [&](int k, const double* Yp, double* out, int mode) {
+            SPAND_CUDA(cudaMemcpyAsync(dzy, hz, (size_t)2 * std::max(k, 1) * sizeof(double), cudaMemcpyHostToDevice, s));
+            gm_update_kernel<<<gb, 256, (size_t)2 * std::max(k, 1) * sizeof(double), s>>>(m, k, Yp, ld, dzy, out,
+                                                                                         mode, 0);
+            M.add_launches(1);
+        };
+        dots(1, b, 0, b);
+        const double bnorm = std::sqrt(hd[0]);
+        if (bnorm == 0) {
+            SPAND_CUDA(cudaMemsetAsync(x, 0, (size_t)m * sizeof(double), s));
+            SPAND_CUDA(cudaStreamSynchronize(s));
+            cleanup();
+            return res;
+        }
+        std::vector<double> H((size_t)(R + 1) * R, 0.0), g(R + 1), y(R);
+        std::vector<GmGivens> G(R);
+        auto Hc = [&](int i, int j) -> double& { return H[(size_t)j * (R + 1) + i]; };
+        int it = 0;
+        double err = 1.0;
+        while (true) {
+            // v_0 = r / |r|, r = b - A x (FP64)
+            device_spmv(A, x, w, s);
+            sub_kernel<<<gb, 256, 0, s>>>(m, b, w, w);
+            M.add_launches(2);
+            dots(1, w, 0, w);
+            const double beta = std::sqrt(hd[0]);
+            err = beta / bnorm;
+            if (err < tol || it >= maxit || beta == 0) break;
+            gm_scale_kernel<<<gb, 256, 0, s>>>(m, w, V, beta);
+            M.add_launches(1);
+            std::fill(g.begin(), g.end(), 0.0);
+            g[0] = beta;
+            int k = 0;
+            for (; k < R && it < maxit;) {
+                double* zk = Z + (size_t)k * ld;
+                SPAND_CUDA(cudaMemcpyAsync(zk, V + (size_t)k * ld, (size_t)m * sizeof(double), cudaMemcpyDeviceToDevice,
+                                           s));
+                M.solve_device(zk, 1, m);
+                device_spmv(A, zk, w, s);
+                M.add_launches(1);
+                // classical Gram-Schmidt, twice
+                for (int i = 0; i <= k; i++) Hc(i, k) = 0;
+                for (int pass = 0; pass < 2; pass++) {
+                    dots(k + 1, V, ld, w);
+                    for (int i = 0; i <= k; i++) {
+                        hz[i] = hd[i];
+                        Hc(i, k) += hd[i];
+                    }
+                    update(k + 1, V, w, 1);
+                }
+                dots(1, w, 0, w);
+                const double h = std::sqrt(hd[0]);
+                Hc(k + 1, k) = h;
+                if (h != 0) {
+                    gm_scale_kernel<<<gb, 256, 0, s>>>(m, w, V + (size_t)(k + 1) * ld, h);
+                    M.add_launches(1);
+                }
+                for (int i = 0; i < k; i++) {
+                    double col[2] = {Hc(i, k), Hc(i + 1, k)};
+                    gm_rotate(col, 0, G[i]);
+                    Hc(i, k) = col[0];
+                    Hc(i + 1, k) = col[1];
+                }
+                G[k] = gm_make_givens(Hc(k, k), Hc(k + 1, k));
+                {
+                    double col[2] = {Hc(k, k), Hc(k + 1, k)};
+                    gm_rotate(col, 0, G[k]);
+                    Hc(k, k) = col[0];
+                    Hc(k + 1, k) = 0;
+                }
+                gm_rotate(g.data(), k, G[k]);
+                ++it;
+                ++k;
+                err = std::fabs(g[k]) / bnorm;
+                if (err < tol || h == 0) break;
+            }
+            // x += Z_k y, y = R^{-1} g[0:k]
+            for (int i = k - 1; i >= 0; i--) {
+                double acc = g[i];
+                for (int j = i + 1; j < k; j++) acc -= Hc(i, j) * y[j];
+                y[i] = acc / Hc(i, i);
+            }
+            for (int i = 0; i < k; i++) hz[i] = -y[i];
+            update(k, Z, x, 1);
+            if (err < tol || it >= maxit) {
+                // the true residual decides; the loop head recomputes it
+                device_spmv(A, x, w, s);
+                sub_kernel<<<gb, 256, 0, s>>>(m, b, w, w);
+                M.add_launches(2);
+                dots(1, w, 0, w);
+                err = std::sqrt(hd[0]) / bnorm;
+                if (err < tol || it >= maxit) break;
+            }
+        }
+        SPAND_CUDA(cudaGetLastError());
+        SPAND_CUDA(cudaStreamSynchronize(s));
+        res.iterations = it;
+        res.relres = err;
+    } catch (...) {
+        cleanup();
+        throw;
+    }
+    cleanup();
+    return res;
+}
+
+// Iterative refinement (is.cpp:12-37): x += M^{-1} (b - A x) until |b - A x| < tol |b|.
+PcgResult device_ir(DeviceFactorBase& M, const DeviceCsr& A, const double* b, double* x, int maxit, double tol) {
+    const int n = A.n;
+    cudaStream_t s = M.stream();
+    PcgWork& w = g_pcg;
+    w.ensure(n);
+    const unsigned gb = (unsigned)((n + 255) / 256);
+    auto dot = [&](const double* a, const double* c) {
+        dot_partial_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, a, c, w.partial);
+        dot_final_kernel<<<1, RED_THREADS, 0, s>>>(w.partial, RED_BLOCKS, w.sc);
+        M.add_launches(2);
+        SPAND_CUDA(cudaMemcpyAsync(w.h_sc, w.sc, sizeof(double), cudaMemcpyDeviceToHost, s));
+        SPAND_CUDA(cudaStreamSynchronize(s));
+        return w.h_sc[0];
+    };
+    auto residual = [&] {
+        device_spmv(A, x, w.tmp, s);
+        sub_kernel<<<gb, 256, 0, s>>>(n, b, w.tmp, w.r);
+        M.add_launches(2);
+    };
+    PcgResult res;
+    residual();
+    const double bb = dot(b, b);
+    if (bb == 0) {
+        SPAND_CUDA(cudaMemsetAsync(x, 0, (size_t)n * sizeof(double), s));
+        SPAND_CUDA(cudaStreamSynchronize(s));
+        return res;
+    }
+    const double thr = tol * tol * bb;
+    double rr = dot(w.r, w.r);
+    int i = 1;
+    while (rr >= thr && i < maxit) {
+        M.solve_device(w.r, 1, n);
+        axpy_kernel<<<gb, 256, 0, s>>>(n, 1.0, w.r, x);
+        M.add_launches(1);
+        residual();
+        rr = dot(w.r, w.r);
+        if (rr < thr) break;
+        i++;
+    }
+    SPAND_CUDA(cudaGetLastError());
+    res.iterations = i;
+    res.relres = std::sqrt(rr / bb);
+    return res;
 }
 
 }  // namespace spand

@@ -83,8 +83,9 @@ std::vector<ClusterID> Tree::partition(const Csc& A) {
 // pattern only copy the new values and scatter them.
 void Tree::assemble(const Csc& A) {
     if (!partitioned_) throw std::logic_error("assemble() before partition()");
-    if (symm_ != SymmKind::SPD || scaling_ != ScalingKind::LLT)
-        throw std::invalid_argument("the device path implements the SPD / LLT configuration");
+    const bool lu = symm_ == SymmKind::GEN;
+    if (!((symm_ == SymmKind::SPD && scaling_ == ScalingKind::LLT) || (lu && scaling_ == ScalingKind::PLU)))
+        throw std::invalid_argument("the device path implements the SPD / LLT and GEN / PLU configurations");
     if (A.n != get_N()) throw std::invalid_argument("matrix size does not match the partition");
     if ((int64_t)A.val.size() != (int64_t)A.rowval.size()) throw std::invalid_argument("values do not match the pattern");
     double t0 = now_s();
@@ -92,8 +93,8 @@ void Tree::assemble(const Csc& A) {
     if (!same_pattern) {
         A_ = A;
         Csc App = spand::symm_perm(A, perm_);
-        asmb_ = spand::assembly_structure(H_, App, true);
-        plan_ = spand::build_plan(H_, asmb_, skip_, use_want_sparsify_);
+        asmb_ = spand::assembly_structure(H_, App, !lu);
+        plan_ = spand::build_plan(H_, asmb_, skip_, use_want_sparsify_, lu);
         std::vector<int64_t> amap = spand::assembly_map(plan_, H_, asmb_, A, perm_);
         if (!stream_) cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
         dev_ = spand::make_device_factor(fp32_, stream_, perm_);
@@ -163,6 +164,11 @@ void Tree::assemble_values(const double* vals, int64_t nnz, bool on_device) {
     t_assemble = now_s() - t0;
 }
 
+// The reference's message for a failed pivot: tree.cpp:587-590 (LLT), 624-628 (PLU)
+std::string Tree::pivot_error() const {
+    return symm_ == SymmKind::GEN ? "Error: Singular Pivot\n" : "Error: Non-SPD Pivot\n";
+}
+
 // tree.cpp:1447-1551
 void Tree::factorize() {
     if (!assembled_ok_) throw std::logic_error("factorize() before assemble()");
@@ -171,8 +177,8 @@ void Tree::factorize() {
         dev_->factorize(tol_);
     } catch (spand::DeviceError& e) {
         if (e.status == spand::SPAND_ERR_NOT_SPD) {
-            if (verb_) printf("Not SPD!\n");
-            throw std::runtime_error("Error: Non-SPD Pivot\n");
+            if (verb_) printf(symm_ == SymmKind::GEN ? "Singular Pivot!\n" : "Not SPD!\n");
+            throw std::runtime_error(pivot_error());
         }
         throw std::runtime_error(e.msg);
     }
@@ -195,8 +201,8 @@ void Tree::factorize_finish() {
         dev_->factorize_finish();
     } catch (spand::DeviceError& e) {
         if (e.status == spand::SPAND_ERR_NOT_SPD) {
-            if (verb_) printf("Not SPD!\n");
-            throw std::runtime_error("Error: Non-SPD Pivot\n");
+            if (verb_) printf(symm_ == SymmKind::GEN ? "Singular Pivot!\n" : "Not SPD!\n");
+            throw std::runtime_error(pivot_error());
         }
         throw std::runtime_error(e.msg);
     }
@@ -234,7 +240,7 @@ void Tree::bench_step(const double* b_dev, double* x_dev, int nrhs, int iters, d
         cuda_check(cudaEventSynchronize(e[2]), "cudaEventSynchronize");
     } catch (spand::DeviceError& err) {
         for (auto& ev : e) cudaEventDestroy(ev);
-        if (err.status == spand::SPAND_ERR_NOT_SPD) throw std::runtime_error("Error: Non-SPD Pivot\n");
+        if (err.status == spand::SPAND_ERR_NOT_SPD) throw std::runtime_error(pivot_error());
         throw std::runtime_error(err.msg);
     }
     float f = 0, p = 0;
@@ -297,11 +303,14 @@ void Tree::build_ops_and_log() {
     const spand::Plan& P = plan_;
     int next_order = P.nclusters;  // siblings are numbered after all clusters
     long long nnz = 0;
+    // pivot ops: ScalingLLT (0), or ScalingPLUQ (8) on the general path
+    const int kpiv = P.lu ? 8 : 0;
     auto push = [&](OpRecord r) {
-        switch (r.kind) {
+        switch (r.kind) {  // Operation::nnz (operations.h:32-163)
             case 0: nnz += (long long)r.ns * (r.ns + 1) / 2; break;
-            case 1: case 2: nnz += (long long)r.ns * r.nn; break;
+            case 1: case 2: case 6: case 7: nnz += (long long)r.ns * r.nn; break;
             case 3: nnz += (long long)r.ns * r.ns; break;
+            case 8: nnz += (long long)r.ns * r.ns + 2LL * r.ns; break;
             default: break;
         }
         ops_.push_back(r);
@@ -312,12 +321,12 @@ void Tree::build_ops_and_log() {
         size_t g = 0;
         for (size_t k = 0; k < L.op_elim_llt.size(); k++) {
             int s = L.op_elim_llt[k];
-            push({0, l, s, -1, rows0_[s], 0, rows0_[s], rows0_[s], L.op_elim_llt_block[k]});
+            push({kpiv, l, s, -1, rows0_[s], 0, rows0_[s], rows0_[s], L.op_elim_llt_block[k]});
             while (g < L.op_gemm.size() && L.op_gemm[g].self == s) {
                 const spand::GemmOpItem& it = L.op_gemm[g];
                 int ns = rows0_[s], nn = rows0_[it.nbr];
-                if (it.kind == 1) push({1, l, s, it.nbr, ns, nn, nn, ns, it.block});
-                else push({2, l, s, it.nbr, ns, nn, ns, nn, it.block});
+                if (it.kind == 1 || it.kind == 6) push({it.kind, l, s, it.nbr, ns, nn, nn, ns, it.block});
+                else push({it.kind, l, s, it.nbr, ns, nn, ns, nn, it.block});
                 g++;
             }
         }
@@ -327,7 +336,7 @@ void Tree::build_ops_and_log() {
         G.dofs_left_elim = left_elim;
         for (size_t k = 0; k < L.op_scale_llt.size(); k++) {
             int c = L.op_scale_llt[k];
-            push({0, l, c, -1, rows0_[c], 0, rows0_[c], rows0_[c], L.op_scale_llt_block[k]});
+            push({kpiv, l, c, -1, rows0_[c], 0, rows0_[c], rows0_[c], L.op_scale_llt_block[k]});
         }
         // wave index of every sparsified cluster of this level, for the Asn widths
         std::vector<int> wave_of;
@@ -357,7 +366,7 @@ void Tree::build_ops_and_log() {
                 push({3, l, c, -1, rows, 0, rows, k, c});
                 int sib = next_order++;
                 push({5, l, c, sib, k, rows - k, 0, 0, -1});
-                push({0, l, sib, -1, rows - k, 0, rows - k, rows - k, -1});
+                push({kpiv, l, sib, -1, rows - k, 0, rows - k, rows - k, -1});
             }
         }
         G.ignored = L.ignored;
@@ -398,7 +407,7 @@ std::vector<std::array<int, 4>> Tree::ranks() const {
 void Tree::op_matrix(int idx, std::vector<double>& out) const {
     const OpRecord& r = ops_.at(idx);
     out.clear();
-    if (r.kind == 0 || r.kind == 1 || r.kind == 2) {
+    if (r.kind == 0 || r.kind == 1 || r.kind == 2 || r.kind == 6 || r.kind == 7 || r.kind == 8) {
         if (r.block < 0) {  // sibling identity
             out.assign((size_t)r.rows * r.cols, 0.0);
             for (int i = 0; i < r.rows; i++) out[i + (size_t)i * r.rows] = 1.0;
@@ -418,6 +427,19 @@ void Tree::op_matrix(int idx, std::vector<double>& out) const {
         for (int j = 0; j < r.cols; j++)
             for (int i = 0; i < r.rows; i++) out[i + (size_t)j * r.rows] = v[i + (size_t)j * ld];
     }
+}
+
+void Tree::op_perm(int idx, std::vector<int>& out) const {
+    const OpRecord& r = ops_.at(idx);
+    out.clear();
+    if (r.kind != 8) return;
+    if (r.block < 0) {  // sibling: identity
+        out.resize(r.ns);
+        for (int i = 0; i < r.ns; i++) out[i] = i;
+        return;
+    }
+    dev_->lu_perm(r.self, out);
+    out.resize(r.ns);
 }
 
 void Tree::op_tau(int idx, std::vector<double>& out) const {
@@ -577,6 +599,62 @@ int cg(const Csc& A, const double* rhs, double* x, const Tree& precond, int iter
     }
     cuda_check(cudaMemcpyAsync(x, dx, n * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
     cuda_check(cudaStreamSynchronize(s), "sync");
+    if (verb) printf("# of iter:  %d\n", r.iterations);
+    if (relres) *relres = r.relres;
+    return r.iterations;
+}
+
+// GMRES and IR: host vectors through the tree's device buffers
+template <typename F>
+static spand::PcgResult krylov_host(const Tree& precond, const double* rhs, double* x, F&& run) {
+    const int n = precond.get_N();
+    double* db = precond.cg_buffer(0, n);
+    double* dx = precond.cg_buffer(1, n);
+    cudaStream_t s = precond.stream();
+    cuda_check(cudaMemcpyAsync(db, rhs, n * sizeof(double), cudaMemcpyHostToDevice, s), "H2D");
+    cuda_check(cudaMemcpyAsync(dx, x, n * sizeof(double), cudaMemcpyHostToDevice, s), "H2D");
+    spand::PcgResult r;
+    try {
+        r = run(db, dx);
+    } catch (spand::DeviceError& e) {
+        throw std::runtime_error(e.msg);
+    }
+    cuda_check(cudaMemcpyAsync(x, dx, n * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
+    cuda_check(cudaStreamSynchronize(s), "sync");
+    return r;
+}
+
+int gmres(const Csc& A, const double* rhs, double* x, const Tree& precond, int iters, int restart, double tol,
+          bool verb, double* relres) {
+    (void)A;
+    if (!precond.device()) throw std::logic_error("gmres before factorize");
+    spand::PcgResult r = krylov_host(precond, rhs, x, [&](const double* b, double* xx) {
+        return spand::device_gmres(*precond.device(), precond.device_csr(), b, xx, iters, restart, tol);
+    });
+    if (verb) printf("# of iter:  %d\n", r.iterations);
+    if (relres) *relres = r.relres;
+    return r.iterations;
+}
+
+int fgmres(const Csc& A, const double* rhs, double* x, const Tree& precond, int iters, int restart, double tol,
+           bool verb, double* relres) {
+    (void)A;
+    if (!precond.device()) throw std::logic_error("fgmres before factorize");
+    spand::PcgResult r = krylov_host(precond, rhs, x, [&](const double* b, double* xx) {
+        return spand::device_fgmres(*precond.device(), precond.device_csr(), b, xx, iters, restart, tol);
+    });
+    if (verb) printf("# of iter:  %d\n", r.iterations);
+    if (relres) *relres = r.relres;
+    return r.iterations;
+}
+
+int ir(const Csc& A, const double* rhs, double* x, const Tree& precond, int iters, double tol, bool verb,
+       double* relres) {
+    (void)A;
+    if (!precond.device()) throw std::logic_error("ir before factorize");
+    spand::PcgResult r = krylov_host(precond, rhs, x, [&](const double* b, double* xx) {
+        return spand::device_ir(*precond.device(), precond.device_csr(), b, xx, iters, tol);
+    });
     if (verb) printf("# of iter:  %d\n", r.iterations);
     if (relres) *relres = r.relres;
     return r.iterations;

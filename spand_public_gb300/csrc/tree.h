@@ -35,7 +35,9 @@ struct LevelLog {
 
 // One recorded operation of the factor, in the reference's op-list order
 // (operations.h:32-163): kind 0 ScalingLLT, 1 GemmSymmOut, 2 GemmSymmIn, 3 Orthogonal,
-// 4 Merge, 5 Split.
+// 4 Merge, 5 Split, 6 GemmOut, 7 GemmIn, 8 ScalingPLUQ (the last three on the GEN / PLU
+// path; the matrix of a ScalingPLUQ is its pivot block: L_s below the diagonal, U_s on and
+// above it).
 struct OpRecord {
     int kind, level, self, nbr, ns, nn, rows, cols;
     int block;  // device block (ScalingLLT / Gemm), or sparsified cluster (Orthogonal), or -1
@@ -89,6 +91,8 @@ class Tree {
     const std::vector<OpRecord>& ops() const { ensure_log(); return ops_; }
     void op_matrix(int idx, std::vector<double>& out) const;
     void op_tau(int idx, std::vector<double>& out) const;
+    // row permutation p of a ScalingPLUQ op (x_s <- x_s[p] before L_s^{-1})
+    void op_perm(int idx, std::vector<int>& out) const;
     double t_partition = 0, t_assemble = 0, t_factorize = 0;
     int64_t launches() const { return dev_ ? dev_->launches() : 0; }
     void reset_launches() { if (dev_) dev_->reset_launches(); }
@@ -126,6 +130,7 @@ class Tree {
 
    private:
     void build_ops_and_log();
+    std::string pivot_error() const;
     void ensure_log() const {
         if (log_dirty_) const_cast<Tree*>(this)->build_ops_and_log();
     }
@@ -166,6 +171,22 @@ class Tree {
 
 // Preconditioned CG (is.cpp:39-121) on the device; b and x are host vectors.
 int cg(const Csc& A, const double* rhs, double* x, const Tree& precond, int iters, double tol, bool verb,
+       double* relres = nullptr);
+
+// Restarted GMRES (is.cpp:123-300) with the tree as left preconditioner, on the device;
+// rhs, x host vectors (x: initial guess).  relres: |w_k| / |M^{-1} r_0|, the quantity the
+// reference's stopping test uses.
+int gmres(const Csc& A, const double* rhs, double* x, const Tree& precond, int iters, int restart, double tol,
+          bool verb, double* relres = nullptr);
+
+// No counterpart in the reference: flexible (right-preconditioned) restarted GMRES whose
+// recurrence residual is the true |b - A x|, for factors stored in FP32; stops when
+// |b - A x| < tol |b|.
+int fgmres(const Csc& A, const double* rhs, double* x, const Tree& precond, int iters, int restart, double tol,
+           bool verb, double* relres = nullptr);
+
+// Iterative refinement (is.cpp:12-37) on the device; relres = |b - A x| / |b|.
+int ir(const Csc& A, const double* rhs, double* x, const Tree& precond, int iters, double tol, bool verb,
        double* relres = nullptr);
 
 // No counterpart in the reference: cg on nrhs right-hand sides at once (independent CGs

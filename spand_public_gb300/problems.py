@@ -45,6 +45,15 @@ def neglapl(n: int, dim: int) -> sp.csc_matrix:
     return _canonical(A)
 
 
+def neglapl_unsym(n: int, dim: int, seed: int = 0, amp: float = 0.1) -> sp.csc_matrix:
+    """−Δ plus U(−amp, amp) on every stored entry: a nonsymmetric matrix with the Laplacian's
+    pattern, as the reference's tests build their GEN problems (tests/tests.cpp:98-109;
+    there with std::default_random_engine, here with numpy's generator from `seed`)."""
+    A = neglapl(n, dim).copy()
+    A.data += np.random.default_rng(seed).uniform(-amp, amp, A.nnz)
+    return A
+
+
 def face_diffusion(n: int, dim: int, face_k: list[np.ndarray], shift: np.ndarray | None = None) -> sp.csc_matrix:
     """Finite-volume diffusion with conductivity face_k[ax][face] on the faces between
     grid neighbours along axis ax (Dirichlet: a boundary face has the conductivity of its
