@@ -420,53 +420,68 @@ def run_batch(args, rank, world, local_rank):
 
     t_an = time.perf_counter()
     T32 = trees(True)
+    F32 = pkg.Forest(T32)
     t_an = time.perf_counter() - t_an
-    bd = [torch.from_numpy(b).to(dev) for *_, b in systems]
-    xd = [torch.zeros_like(b) for b in bd]
+    bs = [b for *_, b in systems]
+    bd = torch.from_numpy(F32.stack(bs)).to(dev)
+    xd = torch.zeros_like(bd)
 
-    def step(ts):
-        for x in xd:
-            x.zero_()
+    def step(f):
+        xd.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        st = pkg.batch_factorize(ts)
+        f.factorize()
         t1 = time.perf_counter()
-        its, rr = pkg.batch_cg_device(ts, [b.data_ptr() for b in bd], [x.data_ptr() for x in xd], args.maxit,
-                                      args.tol)
+        its, rr = f.cg_device(bd.data_ptr(), xd.data_ptr(), args.maxit, args.tol)
         torch.cuda.synchronize()
         t2 = time.perf_counter()
-        assert not np.any(st), st
         return t1 - t0, t2 - t1, its, rr
 
     for _ in range(args.warmup):
-        step(T32)
+        step(F32)
+    F32.launches(reset=True)
     clocks = ClockSampler(local_rank)
     clocks.start()
-    res = [step(T32) for _ in range(args.steps)]
+    res = [step(F32) for _ in range(args.steps)]
     clk = clocks.stop()
+    launches = F32.launches(reset=True) / max(args.steps, 1)
     value = float(np.mean([f + g for f, g, _, _ in res]))
     its = res[-1][2]
-    true_rel = max(float(np.linalg.norm(A @ x.cpu().numpy() - b) / np.linalg.norm(b))
-                   for (m, A, X, levels, b), x in zip(systems, xd))
+    xs = F32.split(xd.cpu().numpy())
+    true_rel = max(float(np.linalg.norm(A @ x - b) / np.linalg.norm(b)) for (m, A, X, levels, b), x in zip(systems, xs))
     fp64 = None
     if args.fp64_steps > 0:
         T64 = trees(False)
-        step(T64)
-        r64 = [step(T64) for _ in range(args.fp64_steps)]
-        fp64 = {"seconds": float(np.mean([f + g for f, g, _, _ in r64])), "pcg_iterations_max": int(r64[-1][2].max())}
+        F64 = pkg.Forest(T64)
         for t in T64:
             t.close()
-    # end to end through the C ABI with host buffers: values upload, batch factor, batch CG
+        step(F64)
+        r64 = [step(F64) for _ in range(args.fp64_steps)]
+        fp64 = {"seconds": float(np.mean([f + g for f, g, _, _ in r64])), "pcg_iterations_max": int(r64[-1][2].max())}
+        F64.close()
+    # the same systems as 256 trees on their own streams (batch_factorize + batch_cg_device)
+    bl = [torch.from_numpy(b).to(dev) for b in bs]
+    xl = [torch.zeros_like(b) for b in bl]
+    pkg.batch_factorize(T32)
+    pkg.batch_cg_device(T32, [b.data_ptr() for b in bl], [x.data_ptr() for x in xl], args.maxit, args.tol)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pkg.batch_factorize(T32)
+    pkg.batch_cg_device(T32, [b.data_ptr() for b in bl], [x.data_ptr() for x in xl], args.maxit, args.tol)
+    torch.cuda.synchronize()
+    streams_s = time.perf_counter() - t0
+    # end to end through the C ABI with host buffers: stacked values upload, factor, CG
+    vals = np.concatenate([A.data for _, A, _, _, _ in systems])
+    b_st = F32.stack(bs)
     e2e_t = []
     for _ in range(max(args.steps, 1)):
         t0 = time.perf_counter()
-        for (m, A, X, levels, b), t in zip(systems, T32):
-            t.assemble_values(A.data)
-        pkg.batch_factorize(T32)
-        xs, its_h, _ = pkg.batch_cg(T32, [b for *_, b in systems], args.maxit, args.tol)
+        F32.assemble_values(vals)
+        F32.factorize()
+        xs_h, its_h, _ = F32.cg(b_st, args.maxit, args.tol)
         e2e_t.append(time.perf_counter() - t0)
-    h2d = sum(A.data.nbytes + 2 * b.nbytes for _, A, _, _, b in systems)
-    d2h = sum(b.nbytes for *_, b in systems)
+    h2d = vals.nbytes + 2 * b_st.nbytes
+    d2h = b_st.nbytes
     e2e = {"value": float(np.mean(e2e_t)), "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
            "pcg_iterations_max": int(its_h.max())}
     cpu = None
@@ -499,11 +514,16 @@ def run_batch(args, rank, world, local_rank):
                        "pcg_s": float(np.mean([g for _, g, _, _ in res])),
                        "pcg_iterations_max": int(its.max()), "pcg_iterations_mean": float(its.mean()),
                        "true_relres_max": true_rel, "analysis_s": t_an, "plain_fp64": fp64,
-                       "timing": "host wall clock between device-wide synchronisations (one stream per system)",
+                       "design": "one Forest: every system's ordering and hierarchy side by side in one plan; each "
+                                 "launch carries all systems' work; segmented CG (per-system scalars)",
+                       "streams_s": streams_s,
+                       "streams": "the same step as 256 trees on 256 streams (batch_factorize + batch_cg_device)",
+                       "timing": "host wall clock between device-wide synchronisations",
                        "precision": "FP32 factor (SIMT), FP64 CG/SpMV/dots", "parallelism": "1 GPU"},
-            "e2e": e2e, "gpu_launches": None, "roofline": None, "cpu_baseline": cpu, "clocks": clk}
+            "e2e": e2e, "gpu_launches": int(round(launches)), "roofline": None, "cpu_baseline": cpu, "clocks": clk}
     if rank == 0:
         print(json.dumps(line), flush=True)
+    F32.close()
     for t in T32:
         t.close()
     return 0

@@ -30,6 +30,7 @@ typedef enum {
 } spand_status;
 
 typedef struct spand_tree spand_tree;
+typedef struct spand_forest spand_forest;
 
 /* Message of the last failing call on this thread ("" if none). */
 const char* spand_last_error(void);
@@ -151,6 +152,39 @@ int spand_batch_cg(spand_tree* const* trees, int count, const double* const* b, 
  * initial guess); every system runs on its tree's stream and the call returns when all have converged or stopped. */
 int spand_batch_cg_device(spand_tree* const* trees, int count, const double* const* b_dev, double* const* x_dev,
                           int iters, double tol, int* iters_out, double* relres_out);
+
+/* No counterpart in the reference: a forest factors many independent SPD systems as ONE
+ * block-diagonal matrix.  Each system keeps the ordering and cluster hierarchy of its
+ * (partitioned, assembled) tree; level l of the forest is level l of every system, so each
+ * launch of the factorization and of the solve carries the work of all systems, and one
+ * segmented CG (per-system scalars and stopping tests) serves all right-hand sides.  The
+ * trees share tolerance, skip, precision and sparsification setting; they are copied and
+ * may be destroyed afterwards.  Vectors are stacked: system k at rows [off[k], off[k+1])
+ * in its natural ordering; values stacked at [nnz_off[k], nnz_off[k+1]) in the CSC order
+ * of its tree's pattern. */
+int spand_forest_create(spand_forest** f, spand_tree* const* trees, int count);
+int spand_forest_destroy(spand_forest* f);
+/* off, nnz_off: count + 1 entries each (either may be NULL) */
+int spand_forest_offsets(spand_forest* f, long long* off, long long* nnz_off);
+int spand_forest_assemble_values(spand_forest* f, const double* vals, long long nnz, int on_device);
+/* SPAND_ERR_NOT_SPD when a pivot fails; *failed_system: that system (-1: none) */
+int spand_forest_factorize(spand_forest* f, int* failed_system);
+int spand_forest_solve_device(spand_forest* f, double* x_dev);
+/* cg (src/is.cpp:39-121) on every system: b, x stacked host vectors (x: initial guess);
+ * iters_out[count], relres_out[count] per system */
+int spand_forest_cg(spand_forest* f, const double* b, double* x, int iters, double tol, int* iters_out,
+                    double* relres_out);
+int spand_forest_cg_device(spand_forest* f, const double* b_dev, double* x_dev, int iters, double tol,
+                           int* iters_out, double* relres_out);
+/* 5 ints per sparsified cluster: system, level, cluster order in its tree, rows, rank */
+int spand_forest_num_ranks(spand_forest* f, int* n);
+int spand_forest_get_ranks(spand_forest* f, int* out);
+int spand_forest_launches(spand_forest* f, long long* n, int reset);
+/* per-kernel-class device time (CUDA events around every launch while on), as for trees */
+int spand_forest_set_profiling(spand_forest* f, int on);
+int spand_forest_profile_count(spand_forest* f, int* n);
+int spand_forest_profile_entry(spand_forest* f, int idx, char* name, long long* launches, double* ms);
+int spand_forest_profile_reset(spand_forest* f);
 
 /* Introspection (reference: get_N, get_assembly_perm, nnz, get_stop, print_log fields;
  * include/tree.h:150-165, src/tree.cpp:1645-1727) */

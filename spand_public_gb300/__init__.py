@@ -67,6 +67,24 @@ _PROTOS = {
     "spand_adjoint_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                        C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "spand_batch_factorize": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "spand_forest_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_void_p, C.c_int]),
+    "spand_forest_destroy": (C.c_int, [C.c_void_p]),
+    "spand_forest_offsets": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "spand_forest_assemble_values": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_int]),
+    "spand_forest_factorize": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "spand_forest_solve_device": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "spand_forest_cg": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p,
+                                  C.c_void_p]),
+    "spand_forest_cg_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p,
+                                         C.c_void_p]),
+    "spand_forest_num_ranks": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "spand_forest_get_ranks": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "spand_forest_launches": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.c_int]),
+    "spand_forest_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "spand_forest_profile_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "spand_forest_profile_entry": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.POINTER(C.c_longlong),
+                                             C.POINTER(C.c_double)]),
+    "spand_forest_profile_reset": (C.c_int, [C.c_void_p]),
     "spand_batch_cg": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p,
                                  C.c_void_p]),
     "spand_batch_cg_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
@@ -457,3 +475,106 @@ def batch_cg_device(trees, b_ptrs, x_ptrs, iters=100, tol=1e-12):
     rr = np.zeros(k, dtype=np.float64)
     _check(L.spand_batch_cg_device(hs, k, bp, xp, int(iters), float(tol), _ptr(its), _ptr(rr)))
     return its, rr
+
+
+class Forest:
+    """Many independent SPD systems factored and solved as one block-diagonal matrix
+    (C ABI ``spand_forest_*``).  ``trees``: partitioned and assembled Trees with one
+    tolerance, skip and precision; each keeps its own ordering and hierarchy.  Vectors are
+    stacked: system k at ``offsets[k]:offsets[k+1]``."""
+
+    def __init__(self, trees):
+        self.L = lib()
+        k = len(trees)
+        hs = (C.c_void_p * k)(*[t.h for t in trees])
+        h = C.c_void_p()
+        _check(self.L.spand_forest_create(C.byref(h), hs, k))
+        self.h = h
+        self.count = k
+        self.offsets = np.zeros(k + 1, dtype=np.int64)
+        self.value_offsets = np.zeros(k + 1, dtype=np.int64)
+        _check(self.L.spand_forest_offsets(self.h, _ptr(self.offsets), _ptr(self.value_offsets)))
+        self.N = int(self.offsets[-1])
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.spand_forest_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def assemble_values(self, vals, on_device=False):
+        """All systems' values, stacked (numpy array, or (address, nnz) of device memory)."""
+        if on_device:
+            _check(self.L.spand_forest_assemble_values(self.h, C.c_void_p(int(vals[0])), int(vals[1]), 1))
+        else:
+            v = np.ascontiguousarray(vals, dtype=np.float64)
+            _check(self.L.spand_forest_assemble_values(self.h, _ptr(v), int(v.size), 0))
+
+    def factorize(self):
+        """Raises SpandError when a pivot fails; ``failed_system`` names the system."""
+        f = C.c_int(-1)
+        rc = self.L.spand_forest_factorize(self.h, C.byref(f))
+        self.failed_system = f.value
+        _check(rc)
+
+    def solve_device(self, x_ptr: int):
+        _check(self.L.spand_forest_solve_device(self.h, C.c_void_p(int(x_ptr))))
+
+    def stack(self, bs):
+        return np.concatenate([np.ascontiguousarray(b, dtype=np.float64) for b in bs])
+
+    def split(self, x):
+        return [x[self.offsets[k]:self.offsets[k + 1]] for k in range(self.count)]
+
+    def cg(self, bs, iters=100, tol=1e-12):
+        """cg on every system (bs: list of right-hand sides, or one stacked vector).
+        Returns ([x_k], iterations, recurrence residuals)."""
+        b = self.stack(bs) if isinstance(bs, (list, tuple)) else np.ascontiguousarray(bs, dtype=np.float64)
+        x = np.zeros_like(b)
+        its = np.zeros(self.count, dtype=np.int32)
+        rr = np.zeros(self.count)
+        _check(self.L.spand_forest_cg(self.h, _ptr(b), _ptr(x), int(iters), float(tol), _ptr(its), _ptr(rr)))
+        return self.split(x), its, rr
+
+    def cg_device(self, b_ptr: int, x_ptr: int, iters=100, tol=1e-12):
+        """Stacked device vectors (x: initial guess).  Returns (iterations, residuals)."""
+        its = np.zeros(self.count, dtype=np.int32)
+        rr = np.zeros(self.count)
+        _check(self.L.spand_forest_cg_device(self.h, C.c_void_p(int(b_ptr)), C.c_void_p(int(x_ptr)), int(iters),
+                                             float(tol), _ptr(its), _ptr(rr)))
+        return its, rr
+
+    def ranks(self):
+        n = C.c_int()
+        _check(self.L.spand_forest_num_ranks(self.h, C.byref(n)))
+        out = np.zeros((n.value, 5), dtype=np.int32)
+        if n.value:
+            _check(self.L.spand_forest_get_ranks(self.h, _ptr(out)))
+        return out  # system, level, cluster order, rows, rank
+
+    def launches(self, reset=False):
+        n = C.c_longlong()
+        _check(self.L.spand_forest_launches(self.h, C.byref(n), int(bool(reset))))
+        return n.value
+
+    def set_profiling(self, on: bool):
+        _check(self.L.spand_forest_set_profiling(self.h, int(bool(on))))
+
+    def profile(self, reset=True):
+        n = C.c_int()
+        _check(self.L.spand_forest_profile_count(self.h, C.byref(n)))
+        out = {}
+        for i in range(n.value):
+            name = C.create_string_buffer(64)
+            la = C.c_longlong()
+            ms = C.c_double()
+            _check(self.L.spand_forest_profile_entry(self.h, i, name, C.byref(la), C.byref(ms)))
+            out[name.value.decode()] = dict(launches=la.value, ms=ms.value)
+        if reset:
+            _check(self.L.spand_forest_profile_reset(self.h))
+        return out

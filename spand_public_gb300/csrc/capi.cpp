@@ -4,11 +4,16 @@
 #include <string>
 
 #include "../../include/spand_gb300.h"
+#include "forest.h"
 #include "tree.h"
 
 struct spand_tree {
     spaND::Tree* t;
     int geo = 0;
+};
+
+struct spand_forest {
+    spaND::Forest* f;
 };
 
 static thread_local std::string g_err;
@@ -448,6 +453,125 @@ int spand_tree_work_entry(spand_tree* t, int which, int idx, char* name, double*
         *bytes = v[idx].bytes;
         *flops = v[idx].flops;
     });
+}
+
+#define CHECK_F(f) \
+    if (!(f) || !(f)->f) return fail(SPAND_ERR_ARG, "null forest")
+
+int spand_forest_create(spand_forest** out, spand_tree* const* trees, int count) {
+    if (!out || !trees || count <= 0) return fail(SPAND_ERR_ARG, "null argument");
+    std::vector<spaND::Tree*> ts(count);
+    for (int k = 0; k < count; k++) {
+        if (!trees[k] || !trees[k]->t) return fail(SPAND_ERR_ARG, "null tree");
+        ts[k] = trees[k]->t;
+    }
+    return guard([&] {
+        auto* h = new spand_forest();
+        try {
+            h->f = new spaND::Forest(ts.data(), count);
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+    });
+}
+
+int spand_forest_destroy(spand_forest* f) {
+    if (!f) return SPAND_OK;
+    delete f->f;
+    delete f;
+    return SPAND_OK;
+}
+
+int spand_forest_offsets(spand_forest* f, long long* off, long long* nnz_off) {
+    CHECK_F(f);
+    if (off) std::memcpy(off, f->f->offsets().data(), f->f->offsets().size() * sizeof(long long));
+    if (nnz_off)
+        std::memcpy(nnz_off, f->f->value_offsets().data(), f->f->value_offsets().size() * sizeof(long long));
+    return SPAND_OK;
+}
+
+int spand_forest_assemble_values(spand_forest* f, const double* vals, long long nnz, int on_device) {
+    CHECK_F(f);
+    if (!vals && nnz > 0) return fail(SPAND_ERR_ARG, "null values");
+    return guard([&] { f->f->assemble_values(vals, (int64_t)nnz, on_device != 0); });
+}
+
+int spand_forest_factorize(spand_forest* f, int* failed_system) {
+    CHECK_F(f);
+    const int rc = guard([&] { f->f->factorize(); });
+    if (failed_system) *failed_system = f->f->failed_system();
+    return rc;
+}
+
+int spand_forest_solve_device(spand_forest* f, double* x) {
+    CHECK_F(f);
+    if (!x) return fail(SPAND_ERR_ARG, "null vector");
+    return guard([&] { f->f->solve_device(x); });
+}
+
+int spand_forest_cg(spand_forest* f, const double* b, double* x, int iters, double tol, int* iters_out,
+                    double* relres_out) {
+    CHECK_F(f);
+    if (!b || !x || !iters_out || !relres_out) return fail(SPAND_ERR_ARG, "null argument");
+    return guard([&] { f->f->cg(b, x, iters, tol, iters_out, relres_out); });
+}
+
+int spand_forest_cg_device(spand_forest* f, const double* b, double* x, int iters, double tol, int* iters_out,
+                           double* relres_out) {
+    CHECK_F(f);
+    if (!b || !x || !iters_out || !relres_out) return fail(SPAND_ERR_ARG, "null argument");
+    return guard([&] { f->f->cg_device(b, x, iters, tol, iters_out, relres_out); });
+}
+
+int spand_forest_num_ranks(spand_forest* f, int* n) {
+    CHECK_F(f);
+    return guard([&] { *n = (int)f->f->ranks().size(); });
+}
+
+int spand_forest_get_ranks(spand_forest* f, int* out) {
+    CHECK_F(f);
+    return guard([&] {
+        auto r = f->f->ranks();
+        for (size_t i = 0; i < r.size(); i++)
+            for (int j = 0; j < 5; j++) out[5 * i + j] = r[i][j];
+    });
+}
+
+int spand_forest_set_profiling(spand_forest* f, int on) {
+    CHECK_F(f);
+    f->f->device()->profiler().enable(on != 0);
+    return SPAND_OK;
+}
+int spand_forest_profile_count(spand_forest* f, int* n) {
+    CHECK_F(f);
+    return guard([&] {
+        f->f->device()->profiler().collect();
+        *n = (int)f->f->device()->profiler().totals().size();
+    });
+}
+int spand_forest_profile_entry(spand_forest* f, int idx, char* name, long long* launches, double* ms) {
+    CHECK_F(f);
+    const auto& v = f->f->device()->profiler().totals();
+    if (idx < 0 || idx >= (int)v.size()) return fail(SPAND_ERR_ARG, "index out of range");
+    std::strncpy(name, v[idx].cls.c_str(), 63);
+    name[63] = 0;
+    *launches = v[idx].launches;
+    *ms = v[idx].ms;
+    return SPAND_OK;
+}
+int spand_forest_profile_reset(spand_forest* f) {
+    CHECK_F(f);
+    f->f->device()->profiler().clear();
+    return SPAND_OK;
+}
+
+int spand_forest_launches(spand_forest* f, long long* n, int reset) {
+    CHECK_F(f);
+    if (n) *n = (long long)f->f->launches();
+    if (reset) f->f->reset_launches();
+    return SPAND_OK;
 }
 
 }  // extern "C"

@@ -103,6 +103,8 @@ class DeviceFactorBase {
     virtual int precision_bytes() const = 0;
     virtual cudaStream_t stream() const = 0;
     virtual size_t device_bytes() const = 0;
+    // cluster of the pivot that failed in the last factorization (-1: none)
+    int failed_cluster() const { return failed_cluster_; }
     int64_t launches() const { return launches_; }
     void reset_launches() { launches_ = 0; }
     void add_launches(int64_t k) { launches_ += k; }
@@ -114,6 +116,7 @@ class DeviceFactorBase {
     virtual void solve_device_noalloc(double* x, int nrhs, int ld) = 0;
 
    protected:
+    int failed_cluster_ = -1;
     int64_t launches_ = 0;
     KernelProfiler prof_;
 };
@@ -169,6 +172,26 @@ void device_pcg_multi(DeviceFactorBase& M, const DeviceCsr& A, const double* b, 
                       double tol, bool use_graph, int* iters_out, double* relres_out);
 
 void device_spmv(const DeviceCsr& A, const double* x, double* y, cudaStream_t s);
+
+// Work of the segmented PCG: n-vectors and per-system scalars (device and pinned host)
+struct SegPcgWork {
+    int n = 0, k = 0;
+    double *r = nullptr, *p = nullptr, *z = nullptr, *Ap = nullptr, *sc = nullptr, *h_sc = nullptr;
+    int *active = nullptr, *h_active = nullptr;
+    ~SegPcgWork() { release(); }
+    void release();
+    void ensure(int n, int k);
+};
+
+// cg (is.cpp:39-121) on nseg independent systems stored as consecutive segments of one
+// vector (system s: rows [off[s], off[s+1]); seg[i]: the system of row i; device arrays;
+// off_host: the same offsets on the host) and preconditioned by M, one factor of their
+// block-diagonal matrix A.  Per
+// iteration one SpMV, one preconditioner application and per-system dots serve all
+// systems; a converged system stops changing.  Per system: iterations and |r|/|b|.
+void device_pcg_segmented(DeviceFactorBase& M, const DeviceCsr& A, const double* b, double* x, int nseg,
+                          const long long* off, const long long* off_host, const int* seg, SegPcgWork& w, int maxit,
+                          double tol, int* iters_out, double* relres_out);
 
 // Restarted GMRES (is.cpp:123-300), left preconditioned by M, on the device; b, x device
 // vectors (x: initial guess).  relres: the reference's stopping quantity |w_k| / |M^{-1} r_0|.

@@ -2504,6 +2504,7 @@ class DeviceFactor : public DeviceFactorBase {
             fprintf(stderr, "\n");
         }
         const DStatus st = *h_status_;
+        failed_cluster_ = st.not_spd - 1;
         if (st.not_spd)
             throw DeviceError{SPAND_ERR_NOT_SPD, std::string(lu_ ? "Error: Singular Pivot" : "Error: Non-SPD Pivot") +
                                                      " (cluster " + std::to_string(st.not_spd - 1) + ")"};
@@ -2538,9 +2539,9 @@ class DeviceFactor : public DeviceFactorBase {
                     int maxr = 0;
                     for (const SparsifyItem& it : D.waves[w].host) maxr = std::max(maxr, r0[it.cluster]);
                     const WaveDev& Wv = D.waves[w];
-                    fprintf(stderr, "qrcp wave L%d w%zu: items %d max rows %d cs %d smem %d active %d\n",
-                            (int)(&D - levels_.data()), w, Wv.n, maxr, Wv.cs, Wv.smem,
-                            active_clusters(Wv.n * Wv.cs, Wv.cs, Wv.smem));
+                    fprintf(stderr, "qrcp wave L%d w%zu: items %d max rows %d cs %d threads %d smem %d active %d\n",
+                            (int)(&D - levels_.data()), w, Wv.n, maxr, Wv.cs, Wv.threads, Wv.smem,
+                            active_clusters(Wv.n * Wv.cs, Wv.cs, Wv.smem, Wv.threads));
                 }
             }
         }
@@ -2699,6 +2700,7 @@ class DeviceFactor : public DeviceFactorBase {
         DSpars* items = nullptr;
         int maxcap = 1;
         int cs = 1;          // CTAs per thread-block cluster of the shared-memory QRCP
+        int threads = QC_THREADS;  // threads per CTA of that launch
         int smem = 0;        // dynamic shared memory per CTA
         int gcs = 1;         // cluster of the global-memory QRCP (matrices the first does not hold)
         int gsmem = 0;       // its dynamic shared memory per CTA
@@ -2851,10 +2853,10 @@ class DeviceFactor : public DeviceFactorBase {
         }
     }
     // co-resident thread-block clusters of a QRCP configuration (-1: not launchable)
-    int active_clusters(int ctas, int cs, int smem) {
+    int active_clusters(int ctas, int cs, int smem, int threads = QC_THREADS) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3((unsigned)ctas);
-        cfg.blockDim = dim3(QC_THREADS);
+        cfg.blockDim = dim3((unsigned)threads);
         cfg.dynamicSmemBytes = (size_t)smem;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -2870,16 +2872,20 @@ class DeviceFactor : public DeviceFactorBase {
         }
         return n;
     }
-    // Cluster size and shared memory of a wave's QRCP launch.  dims: (rows, cols) bound
-    // of every matrix of the wave.  Per candidate cluster size: the slab of the largest
-    // matrix sets the shared memory, the occupancy query the number of co-resident
-    // clusters; the estimate is rounds x (per-step latency + passes over the largest slab)
-    // and the smallest wins.
+    // Cluster size, threads per CTA and shared memory of a wave's QRCP launch.  dims:
+    // (rows, cols) bound of every matrix of the wave.  Per candidate (cluster size, threads):
+    // the slab of the largest matrix sets the shared memory, the occupancy query the number
+    // of co-resident clusters (the kernel's registers cap a 256-thread CTA at two per SM;
+    // 64-thread CTAs fit eight, which the many small matrices of the lower levels use); the
+    // estimate is rounds x (per-step latency + passes over the largest slab by the CTA's
+    // threads) and the smallest wins.
     void choose_cluster(WaveDev& W, const std::vector<std::pair<int, int>>& dims) {
         double best = 1e300;
-        int bcs = 0, bsm = 0;
-        // SPAND_QC_CS=<cs>: that cluster size wherever the matrices fit (measurement aid)
+        int bcs = 0, bsm = 0, bth = QC_THREADS;
+        // SPAND_QC_CS=<cs>, SPAND_QC_THREADS=<n>: that configuration wherever the matrices
+        // fit (measurement aids)
         const int force = getenv("SPAND_QC_CS") ? atoi(getenv("SPAND_QC_CS")) : 0;
+        const int force_th = getenv("SPAND_QC_THREADS") ? atoi(getenv("SPAND_QC_THREADS")) : 0;
         for (int cs = 1; cs <= qc_max_cs_; cs *= 2) {
             int64_t sm = 4096, work = 0;
             for (const auto& d : dims) {
@@ -2888,26 +2894,33 @@ class DeviceFactor : public DeviceFactorBase {
             }
             sm = (sm + 255) & ~int64_t(255);
             if (sm > qc_smem_cap_) continue;
-            const int active = active_clusters(W.n * cs, cs, (int)sm);
-            if (active <= 0) continue;
-            const int rounds = (W.n + active - 1) / active;
-            // per pivot step: barrier latency + the passes over the largest slab (the kernel
-            // is latency-bound: CTAs sharing an SM do not slow each other down much)
-            double est = rounds * (3000.0 + 500.0 * std::log2((double)cs) + 5.0 / 32.0 * (double)work);
-            if (force > 0) est = cs == force ? 0.0 : 1e200;
-            if (est < best) {
-                best = est;
-                bcs = cs;
-                bsm = (int)sm;
+            for (int th = 64; th <= QC_THREADS; th *= 2) {
+                const int active = active_clusters(W.n * cs, cs, (int)sm, th);
+                if (active <= 0) continue;
+                const int rounds = (W.n + active - 1) / active;
+                // per pivot step: barrier latency + the passes over the largest slab (the
+                // kernel is latency-bound: CTAs sharing an SM do not slow each other down much)
+                double est = rounds * (3000.0 + 500.0 * std::log2((double)cs) +
+                                       5.0 / 32.0 * (double)work * ((double)QC_THREADS / th));
+                if (force > 0 && cs != force) est = 1e200;
+                if (force_th > 0 && th != force_th) est = 1e200;
+                if (est < best) {
+                    best = est;
+                    bcs = cs;
+                    bsm = (int)sm;
+                    bth = th;
+                }
             }
         }
         if (!bcs) {  // matrices above the cap take the global-memory path
             W.cs = qc_max_cs_;
             W.smem = qc_smem_cap_;
+            W.threads = QC_THREADS;
             return;
         }
         W.cs = bcs;
         W.smem = bsm;
+        W.threads = bth;
     }
     void launch_qrcp_global(WaveDev& W, double tol) {
         cudaLaunchConfig_t cfg = {};
@@ -2929,7 +2942,7 @@ class DeviceFactor : public DeviceFactorBase {
     void launch_qrcp_cluster(WaveDev& W, double tol) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3((unsigned)(W.n * W.cs));
-        cfg.blockDim = dim3(QC_THREADS);
+        cfg.blockDim = dim3((unsigned)W.threads);
         cfg.dynamicSmemBytes = force_global_ ? 0 : (size_t)W.smem;
         cfg.stream = s_;
         cudaLaunchAttribute attr[1];
@@ -4021,6 +4034,168 @@ PcgResult device_ir(DeviceFactorBase& M, const DeviceCsr& A, const double* b, do
     res.iterations = i;
     res.relres = std::sqrt(rr / bb);
     return res;
+}
+
+
+// ------------------------------------------------------------------------------------
+// Segmented PCG: independent systems stored as consecutive segments of one vector
+// (system s = rows [off[s], off[s+1])) and preconditioned by one factor of their
+// block-diagonal matrix.  Each system follows cg (is.cpp:39-121) with its own scalars; one
+// SpMV, one preconditioner application and per-segment dots serve all systems per
+// iteration, and a converged system's x, r and p stop changing.
+// ------------------------------------------------------------------------------------
+__global__ void seg_dot_kernel(const long long* __restrict__ off, const double* __restrict__ a,
+                               const double* __restrict__ b, double* __restrict__ out) {
+    __shared__ double red[33];
+    const int s = blockIdx.x;
+    const long long lo = off[s], hi = off[s + 1];
+    double acc = 0;
+    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) acc += a[i] * b[i];
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) out[s] = acc;
+}
+
+// x += alpha_s p, r -= alpha_s Ap with alpha_s = rz[s] / pAp[s]
+__global__ void seg_update_xr_kernel(int n, const int* __restrict__ seg, double* __restrict__ x,
+                                     double* __restrict__ r, const double* __restrict__ p,
+                                     const double* __restrict__ Ap, const double* __restrict__ rz,
+                                     const double* __restrict__ pAp, const int* __restrict__ active) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int s = seg[i];
+    if (!active[s]) return;
+    const double alpha = rz[s] / pAp[s];
+    x[i] += alpha * p[i];
+    r[i] -= alpha * Ap[i];
+}
+
+// p = z + beta_s p with beta_s = rz[s] / rz_old[s]
+__global__ void seg_update_p_kernel(int n, const int* __restrict__ seg, double* __restrict__ p,
+                                    const double* __restrict__ z, const double* __restrict__ rz,
+                                    const double* __restrict__ rz_old, const int* __restrict__ active) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int s = seg[i];
+    if (!active[s]) return;
+    p[i] = z[i] + (rz[s] / rz_old[s]) * p[i];
+}
+
+void SegPcgWork::release() {
+    cudaFree(r); cudaFree(p); cudaFree(z); cudaFree(Ap); cudaFree(sc); cudaFree(active);
+    if (h_sc) cudaFreeHost(h_sc);
+    if (h_active) cudaFreeHost(h_active);
+    r = p = z = Ap = sc = h_sc = nullptr;
+    active = h_active = nullptr;
+    n = 0;
+    k = 0;
+}
+
+void SegPcgWork::ensure(int nn, int kk) {
+    if (nn == n && kk == k) return;
+    release();
+    SPAND_CUDA(cudaMalloc(&r, (size_t)nn * sizeof(double)));
+    SPAND_CUDA(cudaMalloc(&p, (size_t)nn * sizeof(double)));
+    SPAND_CUDA(cudaMalloc(&z, (size_t)nn * sizeof(double)));
+    SPAND_CUDA(cudaMalloc(&Ap, (size_t)nn * sizeof(double)));
+    SPAND_CUDA(cudaMalloc(&sc, (size_t)5 * kk * sizeof(double)));
+    SPAND_CUDA(cudaMalloc(&active, (size_t)kk * sizeof(int)));
+    SPAND_CUDA(cudaMallocHost(&h_sc, (size_t)5 * kk * sizeof(double)));
+    SPAND_CUDA(cudaMallocHost(&h_active, (size_t)kk * sizeof(int)));
+    n = nn;
+    k = kk;
+}
+
+void device_pcg_segmented(DeviceFactorBase& M, const DeviceCsr& A, const double* b, double* x, int nseg,
+                          const long long* off, const long long* off_host, const int* seg, SegPcgWork& w, int maxit,
+                          double tol, int* iters_out, double* relres_out) {
+    const int n = A.n, K = nseg;
+    cudaStream_t s = M.stream();
+    w.ensure(n, K);
+    const unsigned gb = (unsigned)((n + 255) / 256);
+    // scalars: rz, rz_old, pAp, rr, bb (K each)
+    double *rz = w.sc, *rz_old = w.sc + K, *pAp = w.sc + 2 * K, *rr = w.sc + 3 * K, *bb = w.sc + 4 * K;
+    auto L = [&](const char* cls, auto&& f, int k = 1) {
+        KernelProfiler& prof = M.profiler();
+        prof.begin(s, cls);
+        f();
+        prof.end(s);
+        M.add_launches(k);
+    };
+    auto dot = [&](const double* a, const double* c, double* out) {
+        L("dot", [&] { seg_dot_kernel<<<K, 512, 0, s>>>(off, a, c, out); });
+    };
+    auto read = [&](const double* src, int count) {
+        SPAND_CUDA(cudaMemcpyAsync(w.h_sc, src, (size_t)count * sizeof(double), cudaMemcpyDeviceToHost, s));
+        SPAND_CUDA(cudaStreamSynchronize(s));
+    };
+    std::vector<double> thr(K), bbh(K);
+    std::vector<char> done(K, 0);
+    device_spmv(A, x, w.Ap, s);
+    L("axpy", [&] { sub_kernel<<<gb, 256, 0, s>>>(n, b, w.Ap, w.r); }, 2);
+    dot(b, b, bb);
+    dot(w.r, w.r, rr);
+    read(rr, 2 * K);  // rr, bb
+    int live = 0;
+    for (int j = 0; j < K; j++) {
+        bbh[j] = w.h_sc[K + j];
+        const double r2 = w.h_sc[j];
+        iters_out[j] = 0;
+        relres_out[j] = 0;
+        w.h_active[j] = 0;
+        if (bbh[j] == 0) {  // zero right-hand side: x = 0 (is.cpp:55-60)
+            SPAND_CUDA(cudaMemsetAsync(x + off_host[j], 0, (size_t)(off_host[j + 1] - off_host[j]) * sizeof(double), s));
+            done[j] = 1;
+            continue;
+        }
+        thr[j] = tol * tol * bbh[j];
+        relres_out[j] = std::sqrt(r2 / bbh[j]);
+        if (r2 < thr[j]) {
+            done[j] = 1;
+            continue;
+        }
+        w.h_active[j] = 1;
+        live++;
+    }
+    if (!live) {
+        SPAND_CUDA(cudaStreamSynchronize(s));
+        return;
+    }
+    SPAND_CUDA(cudaMemcpyAsync(w.active, w.h_active, (size_t)K * sizeof(int), cudaMemcpyHostToDevice, s));
+    SPAND_CUDA(cudaMemcpyAsync(w.p, w.r, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    M.solve_device(w.p, 1, n);
+    dot(w.r, w.p, rz);
+    int i = 0;
+    while (i < maxit) {
+        device_spmv(A, w.p, w.Ap, s);
+        M.add_launches(1);
+        dot(w.p, w.Ap, pAp);
+        L("axpy", [&] { seg_update_xr_kernel<<<gb, 256, 0, s>>>(n, seg, x, w.r, w.p, w.Ap, rz, pAp, w.active); });
+        dot(w.r, w.r, rr);
+        read(rr, K);
+        live = 0;
+        for (int j = 0; j < K; j++) {
+            if (!w.h_active[j]) continue;
+            relres_out[j] = std::sqrt(w.h_sc[j] / bbh[j]);
+            if (w.h_sc[j] < thr[j]) {
+                w.h_active[j] = 0;
+                iters_out[j] = i + 1;
+            } else {
+                live++;
+            }
+        }
+        if (!live) break;
+        SPAND_CUDA(cudaMemcpyAsync(w.active, w.h_active, (size_t)K * sizeof(int), cudaMemcpyHostToDevice, s));
+        SPAND_CUDA(cudaMemcpyAsync(w.z, w.r, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        M.solve_device(w.z, 1, n);
+        SPAND_CUDA(cudaMemcpyAsync(rz_old, rz, (size_t)K * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        dot(w.r, w.z, rz);
+        L("axpy", [&] { seg_update_p_kernel<<<gb, 256, 0, s>>>(n, seg, w.p, w.z, rz, rz_old, w.active); });
+        i++;
+    }
+    for (int j = 0; j < K; j++)
+        if (w.h_active[j]) iters_out[j] = i + 1;
+    SPAND_CUDA(cudaGetLastError());
+    SPAND_CUDA(cudaStreamSynchronize(s));
 }
 
 }  // namespace spand

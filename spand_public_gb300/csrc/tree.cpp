@@ -19,6 +19,32 @@ static void cuda_check(cudaError_t e, const char* what) {
     if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+void upload_csr(const Csc& A, spand::DeviceCsr& dA, int** d_cmap) {
+    const int n = A.n;
+    const size_t nnz = A.rowval.size();
+    std::vector<int> rp(n + 1, 0), ci(nnz), cmap(nnz);
+    for (int j = 0; j < n; j++)
+        for (int k = A.colptr[j]; k < A.colptr[j + 1]; k++) rp[A.rowval[k] + 1]++;
+    for (int i = 0; i < n; i++) rp[i + 1] += rp[i];
+    std::vector<int> fill(rp.begin(), rp.end() - 1);
+    for (int j = 0; j < n; j++)
+        for (int k = A.colptr[j]; k < A.colptr[j + 1]; k++) {
+            const int r = A.rowval[k];
+            ci[fill[r]] = j;
+            cmap[k] = fill[r]++;
+        }
+    if (dA.rowptr) { cudaFree(dA.rowptr); cudaFree(dA.colind); cudaFree(dA.val); }
+    if (*d_cmap) cudaFree(*d_cmap);
+    dA.n = n;
+    cuda_check(cudaMalloc(&dA.rowptr, rp.size() * sizeof(int)), "cudaMalloc");
+    cuda_check(cudaMalloc(&dA.colind, std::max<size_t>(nnz, 1) * sizeof(int)), "cudaMalloc");
+    cuda_check(cudaMalloc(&dA.val, std::max<size_t>(nnz, 1) * sizeof(double)), "cudaMalloc");
+    cuda_check(cudaMalloc(d_cmap, std::max<size_t>(nnz, 1) * sizeof(int)), "cudaMalloc");
+    cuda_check(cudaMemcpy(dA.rowptr, rp.data(), rp.size() * sizeof(int), cudaMemcpyHostToDevice), "H2D");
+    cuda_check(cudaMemcpy(dA.colind, ci.data(), nnz * sizeof(int), cudaMemcpyHostToDevice), "H2D");
+    cuda_check(cudaMemcpy(*d_cmap, cmap.data(), nnz * sizeof(int), cudaMemcpyHostToDevice), "H2D");
+}
+
 Tree::Tree(int nlevels) : nlevels_(nlevels) {
     if (nlevels <= 0) throw std::invalid_argument("nlevels must be > 0");  // tree.cpp:87
 }
@@ -103,34 +129,10 @@ void Tree::assemble(const Csc& A) {
         } catch (spand::DeviceError& e) {
             throw std::runtime_error(e.msg);
         }
-        // CSR pattern of A for the device Krylov solvers (A structurally symmetric) and the
-        // position of every CSC entry in it
-        const int n = A.n;
-        const size_t nnz = A.rowval.size();
-        std::vector<int> rp(n + 1, 0), ci(nnz), cmap(nnz);
-        for (int j = 0; j < n; j++)
-            for (int k = A.colptr[j]; k < A.colptr[j + 1]; k++) rp[A.rowval[k] + 1]++;
-        for (int i = 0; i < n; i++) rp[i + 1] += rp[i];
-        std::vector<int> fill(rp.begin(), rp.end() - 1);
-        for (int j = 0; j < n; j++)
-            for (int k = A.colptr[j]; k < A.colptr[j + 1]; k++) {
-                const int r = A.rowval[k];
-                ci[fill[r]] = j;
-                cmap[k] = fill[r]++;
-            }
-        if (dA_.rowptr) { cudaFree(dA_.rowptr); cudaFree(dA_.colind); cudaFree(dA_.val); }
-        if (d_cmap_) cudaFree(d_cmap_);
         if (d_prow_) cudaFree(d_prow_);
         if (d_pcol_) cudaFree(d_pcol_);
         d_prow_ = d_pcol_ = nullptr;
-        dA_.n = n;
-        cuda_check(cudaMalloc(&dA_.rowptr, rp.size() * sizeof(int)), "cudaMalloc");
-        cuda_check(cudaMalloc(&dA_.colind, std::max<size_t>(nnz, 1) * sizeof(int)), "cudaMalloc");
-        cuda_check(cudaMalloc(&dA_.val, std::max<size_t>(nnz, 1) * sizeof(double)), "cudaMalloc");
-        cuda_check(cudaMalloc(&d_cmap_, std::max<size_t>(nnz, 1) * sizeof(int)), "cudaMalloc");
-        cuda_check(cudaMemcpy(dA_.rowptr, rp.data(), rp.size() * sizeof(int), cudaMemcpyHostToDevice), "H2D");
-        cuda_check(cudaMemcpy(dA_.colind, ci.data(), nnz * sizeof(int), cudaMemcpyHostToDevice), "H2D");
-        cuda_check(cudaMemcpy(d_cmap_, cmap.data(), nnz * sizeof(int), cudaMemcpyHostToDevice), "H2D");
+        upload_csr(A, dA_, &d_cmap_);
     } else {
         A_.val = A.val;
     }

@@ -99,6 +99,13 @@ class Tree {
     spand::DeviceFactorBase* device() const { return dev_.get(); }
     const Csc& matrix() const { return A_; }
     const spand::Plan& plan() const { return plan_; }
+    const spand::Hierarchy& hierarchy() const { return H_; }
+    double get_tol() const { return tol_; }
+    int get_skip() const { return skip_; }
+    bool get_fp32() const { return fp32_; }
+    bool get_use_sparsify() const { return use_want_sparsify_; }
+    SymmKind get_symm_kind() const { return symm_; }
+    bool assembled() const { return assembled_ok_; }
     cudaStream_t stream() const { return stream_; }
     const spand::DeviceCsr& device_csr() const { return dA_; }
     size_t device_bytes() const;
@@ -168,6 +175,10 @@ class Tree {
     std::vector<int> csize_, rows0_;
     bool log_dirty_ = false;
 };
+
+// CSR copy of A on the device (for the SpMV of the Krylov drivers; A structurally
+// symmetric) and the CSR position of every CSC entry (*d_cmap), replacing earlier arrays
+void upload_csr(const Csc& A, spand::DeviceCsr& dA, int** d_cmap);
 
 // Preconditioned CG (is.cpp:39-121) on the device; b and x are host vectors.
 int cg(const Csc& A, const double* rhs, double* x, const Tree& precond, int iters, double tol, bool verb,

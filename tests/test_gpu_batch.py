@@ -83,3 +83,79 @@ def test_batch_cg_device_matches_host():
     assert np.allclose(rr, rrd, rtol=1e-12, atol=0)
     for x, xh in zip(xd, xs):
         assert np.linalg.norm(x.cpu().numpy() - xh) <= 1e-13 * np.linalg.norm(xh)
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+def test_forest_matches_one_at_a_time(fp32):
+    """One plan for all systems (Forest): per-system ranks equal to each tree's, M^{-1}b
+    within 1e-12 (FP64) of each tree's solve, CG iteration counts equal and solutions
+    within 1e-10; systems of different depths (3..6 levels)."""
+    import spand_public_gb300 as pkg
+    sides = [8, 11, 14, 9, 12, 10, 16]
+    sysb = _systems(fp32, sides)
+    trees = [s[3] for s in sysb]
+    f = pkg.Forest(trees)
+    f.factorize()
+    for t in trees:
+        t.factorize()
+    fr = f.ranks()
+    for k, t in enumerate(trees):
+        mine = fr[fr[:, 0] == k][:, 1:]
+        assert np.array_equal(mine, t.ranks()), k
+    rng = np.random.default_rng(4)
+    bs = [rng.standard_normal(s[0].shape[0]) for s in sysb]
+    xs, its, rr = f.cg(bs, iters=200, tol=1e-10)
+    for k, (A, X, levels, t, _) in enumerate(sysb):
+        x1, it1, _ = t.cg(bs[k], iters=200, tol=1e-10)
+        assert its[k] == it1, (k, its[k], it1)
+        assert np.linalg.norm(A @ xs[k] - bs[k]) / np.linalg.norm(bs[k]) < 1e-9
+        assert np.linalg.norm(xs[k] - x1) <= 1e-10 * np.linalg.norm(x1)
+    if not fp32:
+        torch = pytest.importorskip("torch")
+        xd = torch.from_numpy(f.stack(bs)).cuda()
+        torch.cuda.synchronize()
+        f.solve_device(xd.data_ptr())
+        torch.cuda.synchronize()
+        for k, (b, x) in enumerate(zip(bs, f.split(xd.cpu().numpy()))):
+            ref = trees[k].solve(b)
+            assert np.linalg.norm(x - ref) <= 1e-12 * np.linalg.norm(ref), k
+    f.close()
+
+
+def test_forest_device_vectors_and_new_values():
+    """cg_device on stacked device vectors equals cg on host vectors; new stacked values
+    (each system scaled by its own factor) give the scaled systems' solutions."""
+    torch = pytest.importorskip("torch")
+    import spand_public_gb300 as pkg
+    sysb = _systems(True, [10, 13, 9])
+    f = pkg.Forest([s[3] for s in sysb])
+    f.factorize()
+    rng = np.random.default_rng(8)
+    bs = [rng.standard_normal(s[0].shape[0]) for s in sysb]
+    xs, its, _ = f.cg(bs, iters=200, tol=1e-10)
+    bd = torch.from_numpy(f.stack(bs)).cuda()
+    xd = torch.zeros_like(bd)
+    torch.cuda.synchronize()
+    itd, _ = f.cg_device(bd.data_ptr(), xd.data_ptr(), iters=200, tol=1e-10)
+    assert np.array_equal(its, itd)
+    assert np.array_equal(np.concatenate(xs), xd.cpu().numpy())
+    scale = [2.0, 0.5, 3.0]
+    vals = np.concatenate([s[0].tocsc().data * c for s, c in zip(sysb, scale)])
+    f.assemble_values(vals)
+    f.factorize()
+    xs2, _, _ = f.cg(bs, iters=200, tol=1e-10)
+    for (A, *_), x, b, c in zip(sysb, xs2, bs, scale):
+        assert np.linalg.norm(c * (A @ x) - b) / np.linalg.norm(b) < 1e-9
+    f.close()
+
+
+def test_forest_reports_the_failing_system():
+    import spand_public_gb300 as pkg
+    sysb = _systems(False, [8, 9, 10])
+    A, X, levels, t, b = sysb[2]
+    t.assemble(-A)
+    f = pkg.Forest([s[3] for s in sysb])
+    with pytest.raises(pkg.SpandError, match="Non-SPD Pivot"):
+        f.factorize()
+    assert f.failed_system == 2
+    f.close()

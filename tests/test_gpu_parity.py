@@ -77,6 +77,15 @@ def test_factor_parity_fp64_global_qrcp(n, dim, nlevels, tol, monkeypatch):
     _check_parity(n, dim, nlevels, tol, 0, 2)
 
 
+@pytest.mark.parametrize("threads", [64, 128])
+def test_factor_parity_fp64_narrow_qrcp(threads, monkeypatch):
+    """Every shared-memory QRCP launch with 64 or 128 threads per CTA (the configurations
+    the launch model picks for the many small matrices of the lower levels)."""
+    monkeypatch.setenv("SPAND_QC_THREADS", str(threads))
+    _check_parity(16, 3, 6, 1e-2, 0, 2)
+    _check_parity(64, 2, 7, 1e-2, 0, 1)
+
+
 def _check_parity(n, dim, nlevels, tol, skip, nf):
     A, t, o = _build(n, dim, nlevels, tol, skip, factorizations=nf)
     assert np.array_equal(t.get_assembly_perm(), o.get_assembly_perm())
