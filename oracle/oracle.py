@@ -62,6 +62,7 @@ def lib():
             "orc_spmv": (None, [P, pd, pd]),
             "orc_gmres": (I, [P, pd, pd, I, I, D, pd]),
             "orc_get_op_u": (C.c_longlong, [P, I, pd]), "orc_get_op_perm": (I, [P, I, pi]),
+            "orc_get_op_signs": (I, [P, I, pd]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -231,6 +232,11 @@ class OracleTree:
         buf = np.zeros(n * n)
         self.L.orc_get_op_u(self.h, idx, _dp(buf))
         return buf.reshape((n, n)).T
+
+    def op_signs(self, idx, n):
+        buf = np.zeros(max(n, 1))
+        self.L.orc_get_op_signs(self.h, idx, _dp(buf))
+        return buf[:n]
 
     def op_perm(self, idx, n):
         buf = np.zeros(max(n, 1), dtype=np.int32)

@@ -407,6 +407,79 @@ static int getf(Mat& A, std::vector<int>& perm) {
     return 0;
 }
 
+// Eigen's LDLT<MatrixXd, Lower> (Eigen/src/Cholesky/LDLT.h, ldlt_inplace<Lower>::unblocked,
+// Eigen 3.3): left-looking LDL^T with symmetric pivoting.  At step k the pivot is the first
+// entry of largest magnitude among the diagonal entries k..n-1 as they stand (for j > k not
+// yet updated by the earlier columns); the swap touches the lower triangle only.  On exit
+// the strict lower triangle holds the unit L, the diagonal holds D, transp[k] the row
+// swapped with k.  Returns false where Eigen reports failure: an all-zero diagonal at step
+// 0, or a nonzero pivot after a zero one.
+static bool ldlt_eigen(Mat& A, std::vector<int>& transp) {
+    const int n = A.r;
+    transp.assign(n, 0);
+    std::vector<double> temp(n);
+    bool ok = true, found_zero = false;
+    for (int k = 0; k < n; k++) {
+        int big = k;
+        double bv = std::fabs(A(k, k));
+        for (int j = k + 1; j < n; j++)
+            if (std::fabs(A(j, j)) > bv) { bv = std::fabs(A(j, j)); big = j; }
+        transp[k] = big;
+        if (big != k) {
+            for (int c = 0; c < k; c++) std::swap(A(k, c), A(big, c));
+            for (int r = big + 1; r < n; r++) std::swap(A(r, k), A(r, big));
+            std::swap(A(k, k), A(big, big));
+            for (int i = k + 1; i < big; i++) std::swap(A(i, k), A(big, i));
+        }
+        const int rs = n - k - 1;
+        if (k > 0) {
+            for (int j = 0; j < k; j++) temp[j] = A(j, j) * A(k, j);
+            double d = 0;
+            for (int j = 0; j < k; j++) d += A(k, j) * temp[j];
+            A(k, k) -= d;
+            for (int j = 0; j < k; j++)
+                for (int r = k + 1; r < n; r++) A(r, k) -= A(r, j) * temp[j];
+        }
+        const double akk = A(k, k);
+        const bool valid = std::fabs(akk) > 0.0;
+        if (k == 0 && !valid) {
+            for (int j = 0; j < n; j++) transp[j] = j;
+            return false;
+        }
+        if (rs > 0 && valid) {
+            for (int r = k + 1; r < n; r++) A(r, k) /= akk;
+        } else if (rs > 0) {
+            for (int r = k + 1; r < n; r++) ok = ok && A(r, k) == 0.0;
+        }
+        if (found_zero && valid) ok = false;
+        else if (!valid) found_zero = true;
+    }
+    return ok;
+}
+
+// util.cpp:167-184: L |D|^1/2 (lower, non-unit), sign(D), and the row permutation
+// (swap2perm of Eigen's transpositions); returns 1 when Eigen reports failure.
+static int ldlt(const Mat& Ass, Mat& L, std::vector<double>& s, std::vector<int>& perm) {
+    const int n = Ass.r;
+    if (n == 0) return 0;
+    Mat A = Ass;
+    std::vector<int> tr;
+    if (!ldlt_eigen(A, tr)) return 1;
+    L = Mat(n, n);
+    s.assign(n, 0.0);
+    for (int j = 0; j < n; j++) {
+        const double dj = A(j, j);
+        const double h = std::sqrt(std::fabs(dj));
+        s[j] = (dj > 0) - (dj < 0);
+        L(j, j) = h;
+        for (int i = j + 1; i < n; i++) L(i, j) = A(i, j) * h;
+    }
+    perm.resize(n);
+    for (int i = 0; i < n; i++) perm[i] = i;
+    for (int i = 0; i < n; i++) std::swap(perm[tr[i]], perm[i]);
+    return 0;
+}
+
 // A = L (D + U') -> L |D|^1/2 and |D|^1/2 sign(D) (I + D^-1 U'); util.cpp:212-227.
 static void split_LU(const Mat& A, Mat& L, Mat& U) {
     int n = A.r;
@@ -690,6 +763,7 @@ enum OpKind {
     OP_GEMM_OUT = 6,
     OP_GEMM_IN = 7,
     OP_SCALING_PLUQ = 8,
+    OP_SCALING_LDLT = 9,
 };
 
 struct Op {
@@ -700,7 +774,8 @@ struct Op {
     pMat A;                      // LLT, Gemm block, v (Orthogonal), L (PLUQ)
     pMat U;                      // PLUQ
     std::vector<double> h;       // Orthogonal
-    std::vector<int> p, q;       // PLUQ
+    std::vector<int> p, q;       // PLUQ, LDLT (p)
+    std::vector<double> s;       // LDLT: sign(D); Gemm ops of an LDLT pivot: the same signs
     int ilvl = 0;                // level at which the op was recorded
 
     long long nnz() const {
@@ -710,19 +785,39 @@ struct Op {
                 return (long long)ns * nn;
             case OP_ORTHOGONAL: return (long long)ns * ns;
             case OP_SCALING_PLUQ: return (long long)ns * ns + 2LL * ns;
+            case OP_SCALING_LDLT: return (long long)ns * (ns + 1) / 2 + 2LL * ns;
             default: return 0;
         }
+    }
+    // self's x scaled by the signs (Gemm ops recorded with a diagonal, operations.cpp:55-93)
+    std::vector<double> sx(const double* xs) const {
+        std::vector<double> t(xs, xs + ns);
+        for (int i = 0; i < ns; i++) t[i] *= s[i];
+        return t;
     }
     void fwd() {
         double* xs = self ? self->x.data() : nullptr;
         switch (kind) {
             case OP_SCALING_LLT: trsv_lower(*A, xs, ns, false); break;
             case OP_GEMM_SYMM_OUT: case OP_GEMM_OUT:
-                if (nn > 0 && ns > 0) gemv_sub(*A, false, xs, nbr->x.data());
+                if (nn > 0 && ns > 0) {
+                    if (s.empty()) gemv_sub(*A, false, xs, nbr->x.data());
+                    else gemv_sub(*A, false, sx(xs).data(), nbr->x.data());
+                }
                 break;
             case OP_GEMM_SYMM_IN:
-                if (nn > 0 && ns > 0) gemv_sub(*A, true, xs, nbr->x.data());
+                if (nn > 0 && ns > 0) {
+                    if (s.empty()) gemv_sub(*A, true, xs, nbr->x.data());
+                    else gemv_sub(*A, true, sx(xs).data(), nbr->x.data());
+                }
                 break;
+            case OP_SCALING_LDLT: {
+                std::vector<double> t(ns);
+                for (int i = 0; i < ns; i++) t[i] = xs[p[i]];
+                std::copy(t.begin(), t.end(), xs);
+                trsv_lower(*A, xs, ns, false);
+                break;
+            }
             case OP_GEMM_IN: break;
             case OP_ORTHOGONAL: ormqr_vec(*A, h, A->c, xs, true); break;
             case OP_MERGE: {
@@ -745,16 +840,40 @@ struct Op {
             }
         }
     }
+    // self -= s .* (op(A) nbr) (operations.cpp:65-73, 85-93)
+    void sub_scaled(bool trans, double* xs) const {
+        std::vector<double> t(ns, 0.0);
+        gemv_sub(*A, trans, nbr->x.data(), t.data());  // t = -op(A) nbr
+        for (int i = 0; i < ns; i++) xs[i] += s[i] * t[i];
+    }
+    void diag() {
+        if (kind != OP_SCALING_LDLT) return;
+        double* xs = self->x.data();
+        for (int i = 0; i < ns; i++) xs[i] /= s[i];  // operations.cpp:139-141
+    }
     void bwd() {
         double* xs = self ? self->x.data() : nullptr;
         switch (kind) {
             case OP_SCALING_LLT: trsv_lower(*A, xs, ns, true); break;
             case OP_GEMM_SYMM_OUT:
-                if (nn > 0 && ns > 0) gemv_sub(*A, true, nbr->x.data(), xs);
+                if (nn > 0 && ns > 0) {
+                    if (s.empty()) gemv_sub(*A, true, nbr->x.data(), xs);
+                    else sub_scaled(true, xs);
+                }
                 break;
             case OP_GEMM_SYMM_IN: case OP_GEMM_IN:
-                if (nn > 0 && ns > 0) gemv_sub(*A, false, nbr->x.data(), xs);
+                if (nn > 0 && ns > 0) {
+                    if (s.empty() || kind == OP_GEMM_IN) gemv_sub(*A, false, nbr->x.data(), xs);
+                    else sub_scaled(false, xs);
+                }
                 break;
+            case OP_SCALING_LDLT: {
+                trsv_lower(*A, xs, ns, true);
+                std::vector<double> t(ns);
+                for (int i = 0; i < ns; i++) t[p[i]] = xs[i];
+                std::copy(t.begin(), t.end(), xs);
+                break;
+            }
             case OP_GEMM_OUT: break;
             case OP_ORTHOGONAL: ormqr_vec(*A, h, A->c, xs, false); break;
             case OP_MERGE: {
@@ -1007,8 +1126,8 @@ struct Tree {
             log[ilvl].flops_trsm += (double)e->A->r * e->A->c * e->A->c;
         }
     }
-    // tree.cpp:748-793
-    void gemm_edges(Edge* e1, Edge* e2, bool t1, bool t2) {
+    // tree.cpp:748-793; with diag (LDLT): C -= op(A1) diag^-1 op(A2) on the whole block
+    void gemm_edges(Edge* e1, Edge* e2, bool t1, bool t2, const std::vector<double>* diag = nullptr) {
         Cluster* s = t1 ? e1->n2 : e1->n1;
         Cluster* n1 = t1 ? e1->n1 : e1->n2;
         Cluster* n2 = t2 ? e2->n2 : e2->n1;
@@ -1021,7 +1140,13 @@ struct Tree {
                 if (e->n2 == n1) { found = e.get(); break; }
         }
         Mat& C = *found->A;
-        if (n1 == n2 && symmetry()) {
+        if (diag) {
+            Mat B = *e2->A;  // op(B) has the s rows: rows of B, or columns when t2
+            for (int j = 0; j < B.c; j++)
+                for (int i = 0; i < B.r; i++) B(i, j) /= (*diag)[t2 ? j : i];
+            gemm_sub(*e1->A, t1, B, t2, C);
+            log[ilvl].flops_gemm += 2.0 * C.r * C.c * s->size;
+        } else if (n1 == n2 && symmetry()) {
             syrk_sub_lower(*e1->A, t1, C);
             log[ilvl].flops_gemm += (double)C.r * C.r * s->size;
         } else {
@@ -1029,17 +1154,45 @@ struct Tree {
             log[ilvl].flops_gemm += 2.0 * C.r * C.c * s->size;
         }
     }
-    void schur_symmetric(Cluster* self) {  // tree.cpp:862-883
+    void schur_symmetric(Cluster* self, const std::vector<double>* diag = nullptr) {  // tree.cpp:862-883
         auto outs = self->out_nbr();
         auto ins = self->in_nbr();
         for (auto e1 : outs)
             for (auto e2 : outs)
-                if (e1->n2->order >= e2->n2->order) gemm_edges(e1, e2, false, true);
+                if (e1->n2->order >= e2->n2->order) gemm_edges(e1, e2, false, true, diag);
         for (auto e1 : ins)
             for (auto e2 : ins)
-                if (e1->n1->order >= e2->n1->order) gemm_edges(e1, e2, true, false);
+                if (e1->n1->order >= e2->n1->order) gemm_edges(e1, e2, true, false, diag);
         for (auto e1 : outs)
-            for (auto e2 : ins) gemm_edges(e1, e2, false, false);
+            for (auto e2 : ins) gemm_edges(e1, e2, false, false, diag);
+    }
+    // tree.cpp:596-611
+    void ldlt_cluster(Cluster* self, Mat& L, std::vector<double>& s, std::vector<int>& p) {
+        const Mat& Ass = *self->pivot()->A;
+        if (ldlt(Ass, L, s, p) != 0) throw std::runtime_error("Error: Singular Pivot");
+        double n = Ass.r;
+        log[ilvl].flops_potf += n * n * n / 3.0;
+    }
+    // tree.cpp:691-715, 726-733: A_sn <- L^-1 P^T A_sn (in-edges), A_ns <- A_ns P L^-T (out-edges)
+    void panel_ldlt(Cluster* self, const Mat& L, const std::vector<int>& p) {
+        for (auto e : self->in_nbr()) {
+            Mat& Asn = *e->A;
+            Mat T(Asn.r, Asn.c);
+            for (int j = 0; j < Asn.c; j++)
+                for (int i = 0; i < Asn.r; i++) T(i, j) = Asn(p[i], j);
+            Asn = std::move(T);
+            trsm_left_lower(L, Asn);
+            log[ilvl].flops_trsm += (double)Asn.c * Asn.r * Asn.r;
+        }
+        for (auto e : self->out_nbr()) {
+            Mat& Ans = *e->A;
+            Mat T(Ans.r, Ans.c);
+            for (int j = 0; j < Ans.c; j++)
+                for (int i = 0; i < Ans.r; i++) T(i, j) = Ans(i, p[j]);
+            Ans = std::move(T);
+            trsm_right_lower_trans(L, Ans);
+            log[ilvl].flops_trsm += (double)Ans.r * Ans.c * Ans.c;
+        }
     }
     void push_op(pOp op) { op->ilvl = ilvl; ops.push_back(std::move(op)); }
     pOp make_op(OpKind k, Cluster* self, Cluster* nbr, pMat A) {
@@ -1061,6 +1214,27 @@ struct Tree {
             push_op(make_op(OP_SCALING_LLT, self, nullptr, std::move(self->pivot()->A)));
             for (auto e : self->out_nbr()) push_op(make_op(OP_GEMM_SYMM_OUT, self, e->n2, std::move(e->A)));
             for (auto e : self->in_nbr()) push_op(make_op(OP_GEMM_SYMM_IN, self, e->n1, std::move(e->A)));
+        } else if (scale_kind == S_LDLT) {  // tree.cpp:911-928
+            auto L = std::make_unique<Mat>();
+            std::vector<double> s;
+            std::vector<int> p;
+            ldlt_cluster(self, *L, s, p);
+            panel_ldlt(self, *L, p);
+            schur_symmetric(self, &s);
+            auto op = make_op(OP_SCALING_LDLT, self, nullptr, std::move(L));
+            op->s = s;
+            op->p = p;
+            push_op(std::move(op));
+            for (auto e : self->out_nbr()) {
+                auto g = make_op(OP_GEMM_SYMM_OUT, self, e->n2, std::move(e->A));
+                g->s = s;
+                push_op(std::move(g));
+            }
+            for (auto e : self->in_nbr()) {
+                auto g = make_op(OP_GEMM_SYMM_IN, self, e->n1, std::move(e->A));
+                g->s = s;
+                push_op(std::move(g));
+            }
         } else if (scale_kind == S_PLU || scale_kind == S_PLUQ) {
             pMat L, U;
             std::vector<int> p, q;
@@ -1086,6 +1260,20 @@ struct Tree {
             potf_cluster(self);
             panel_potf(self);
             push_op(make_op(OP_SCALING_LLT, self, nullptr, std::move(self->pivot()->A)));
+        } else if (scale_kind == S_LDLT) {  // tree.cpp:812-830: the new pivot is diag(sign D)
+            auto L = std::make_unique<Mat>();
+            std::vector<double> s;
+            std::vector<int> p;
+            ldlt_cluster(self, *L, s, p);
+            panel_ldlt(self, *L, p);
+            auto op = make_op(OP_SCALING_LDLT, self, nullptr, std::move(L));
+            op->s = s;
+            op->p = p;
+            push_op(std::move(op));
+            auto D = std::make_unique<Mat>(self->size, self->size);
+            for (int i = 0; i < self->size; i++) (*D)(i, i) = s[i];
+            self->pivot()->A = std::move(D);
+            return;
         } else {
             pMat L, U;
             std::vector<int> p, q;
@@ -1123,8 +1311,11 @@ struct Tree {
         log[ilvl].nbrs.add(cols);
         return Asn;
     }
-    // tree.cpp:980-1104 (pred == true branch, is_pivot_I == true)
-    Cluster* shrink_split(Cluster* original, int osize, Mat& AsnP) {
+    // tree.cpp:980-1104 (pred == true branch).  Pivot I (SPD, GEN), or (SYM) the signs of
+    // the scaling, transformed to Q^T piv Q and split: the sibling's pivot, an edge
+    // original -> sibling, and the original's new pivot (tree.cpp:1069-1097).
+    Cluster* shrink_split(Cluster* original, int osize, Mat& AsnP, const Mat& v, const std::vector<double>& h) {
+        const int n0 = original->size;
         int sib_size = original->size - osize;
         auto psib = std::make_unique<Cluster>(original->start + osize, sib_size, original->level, get_new_order(),
                                               original->sparsify);
@@ -1147,9 +1338,33 @@ struct Tree {
             e->A = std::move(M);
             col += cols;
         }
-        // pivot is identity: Aoo = I_osize, Ass = I_sib
-        sib->add_edge(std::make_unique<Edge>(Edge{sib, sib, std::make_unique<Mat>(Mat::eye(sib_size)), true}));
-        original->pivot()->A = std::make_unique<Mat>(Mat::eye(osize));
+        if (symm != SYM) {
+            // pivot is identity: Aoo = I_osize, Ass = I_sib
+            sib->add_edge(std::make_unique<Edge>(Edge{sib, sib, std::make_unique<Mat>(Mat::eye(sib_size)), true}));
+            original->pivot()->A = std::make_unique<Mat>(Mat::eye(osize));
+        } else {
+            Mat& piv = *original->pivot()->A;  // n0 x n0
+            const int k = (int)h.size();
+            std::vector<double> t(n0);
+            for (int r = 0; r < n0; r++) {  // piv <- piv Q (row by row: Q^T row^T)
+                for (int c = 0; c < n0; c++) t[c] = piv(r, c);
+                ormqr_vec(v, h, k, t.data(), true);
+                for (int c = 0; c < n0; c++) piv(r, c) = t[c];
+            }
+            for (int c = 0; c < n0; c++) ormqr_vec(v, h, k, &piv(0, c), true);  // piv <- Q^T piv
+            auto Aoo = std::make_unique<Mat>(osize, osize);
+            auto Ass = std::make_unique<Mat>(sib_size, sib_size);
+            auto Aso = std::make_unique<Mat>(sib_size, osize);
+            for (int j = 0; j < osize; j++)
+                for (int i = 0; i < osize; i++) (*Aoo)(i, j) = piv(i, j);
+            for (int j = 0; j < sib_size; j++)
+                for (int i = 0; i < sib_size; i++) (*Ass)(i, j) = piv(osize + i, osize + j);
+            for (int j = 0; j < osize; j++)
+                for (int i = 0; i < sib_size; i++) (*Aso)(i, j) = piv(osize + i, j);
+            sib->add_edge(std::make_unique<Edge>(Edge{sib, sib, std::move(Ass), true}));
+            original->add_edge(std::make_unique<Edge>(Edge{original, sib, std::move(Aso), true}));
+            original->pivot()->A = std::move(Aoo);
+        }
         others.push_back(std::move(psib));
         push_op(make_op(OP_SPLIT, original, sib, nullptr));
         return sib;
@@ -1175,12 +1390,13 @@ struct Tree {
             for (int i = 0; i < rows; i++) (*v)(i, j) = (*Asn)(i, j);
         auto op = make_op(OP_ORTHOGONAL, self, nullptr, std::move(v));
         op->h.assign(ht.begin(), ht.begin() + rank);
+        const Op* qop = op.get();
         push_op(std::move(op));
         // AsnP = triu(R[:rank,:]) P^T : column jpvt[j] of AsnP is column j of triu(R)
         Mat AsnP(rank, cols);
         for (int j = 0; j < cols; j++)
             for (int i = 0; i < rank && i <= j; i++) AsnP(i, jpvt[j]) = (*Asn)(i, j);
-        Cluster* sib = shrink_split(self, rank, AsnP);
+        Cluster* sib = shrink_split(self, rank, AsnP, *qop->A, qop->h);
         eliminate_cluster(sib);
     }
     void sparsify_cluster(Cluster* self) {  // tree.cpp:1417-1433
@@ -1284,6 +1500,7 @@ struct Tree {
             else std::fill(c->x.begin(), c->x.end(), 0.0);
         }
         for (auto& op : ops) op->fwd();
+        for (auto& op : ops) op->diag();  // tree.cpp:1621-1624 (LDLT only)
         for (auto it = ops.rbegin(); it != ops.rend(); ++it) (*it)->bwd();
         for (auto& c : bottom_original())
             if (c->children.empty()) std::copy(c->x.begin(), c->x.end(), b.begin() + c->start);
@@ -1709,6 +1926,14 @@ long long orc_get_op_u(void* p, int idx, double* out) {
     auto& v = (*it)->U->v;
     if (out) std::copy(v.begin(), v.end(), out);
     return (long long)v.size();
+}
+// sign(D) of a ScalingLDLT op (also carried by the Gemm ops of an LDLT pivot)
+int orc_get_op_signs(void* p, int idx, double* out) {
+    auto it = ((OrcHandle*)p)->t->ops.begin();
+    std::advance(it, idx);
+    auto& s = (*it)->s;
+    if (out) std::copy(s.begin(), s.end(), out);
+    return (int)s.size();
 }
 int orc_get_op_perm(void* p, int idx, int* out) {
     auto it = ((OrcHandle*)p)->t->ops.begin();

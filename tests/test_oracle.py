@@ -10,6 +10,7 @@ PartitionTest.Consistency exercises in the same loops.
 import numpy as np
 import pytest
 import scipy.linalg as sla
+import scipy.sparse as sp
 
 from oracle import oracle as O
 from spand_public_gb300 import problems as P
@@ -235,3 +236,87 @@ def test_cg_converges():
     x, it = t.cg(b, 100, 1e-12)
     assert it < 20
     assert np.linalg.norm(A @ x - b) / np.linalg.norm(b) < 1e-11
+
+
+@pytest.mark.parametrize("dim,n", [(2, 128), (3, 5), (3, 15)])
+def test_spd_vs_ldlt(dim, n):
+    """ApproxTest.SPD_vs_LDLT (tests/tests.cpp:614-683): SPD/LLT on A and SYM/LDLT on -A
+    (b -> -b) agree; errors and difference <= 1e-12 at tol 0, <= tol * 1e2 otherwise."""
+    A = P.neglapl(n, dim)
+    X = P.linspace_nd(n, dim)
+    N = A.shape[0]
+    lmin = 1 if N < 1000 else 8
+    levels = range(lmin, lmin + 5) if N < 5000 else (lmin, lmin + 2, lmin + 4)
+    for nlevels in levels:
+        for tol, skip in ((0.0, 100), (1e-4, 1), (1e-14, 0)):
+            b = np.random.default_rng(nlevels).uniform(-1, 1, N)
+            t = O.OracleTree(nlevels)
+            t.set_Xcoo(X)
+            t.set_tol(tol)
+            t.set_skip(skip)
+            t.partition(A)
+            t.assemble(A)
+            t.factorize()
+            xl = t.solve(b)
+            u = O.OracleTree(nlevels)
+            u.set_Xcoo(X)
+            u.set_tol(tol)
+            u.set_skip(skip)
+            u.set_symm_kind(O.OracleTree.SYM)
+            u.set_scaling_kind(O.OracleTree.LDLT)
+            u.partition(-A)
+            u.assemble(-A)
+            u.factorize()
+            xd = u.solve(-b)
+            bound = 1e-12 if tol == 0.0 else tol * 1e2
+            for x in (xl, xd):
+                assert np.linalg.norm(A @ x - b) / np.linalg.norm(b) <= bound
+            assert np.linalg.norm(xl - xd) / np.linalg.norm(xl) <= bound
+
+
+@pytest.mark.parametrize("dim,n,shift", [(2, 20, 0.5), (3, 10, 1.0)])
+def test_ldlt_indefinite(dim, n, shift):
+    """SYM/LDLT on the indefinite -Laplacian - shift*I (a few negative eigenvalues, the
+    smallest |eigenvalue| near 0.05): exact at tol 0 (<= 1e-10, ApproxTest.Exact); at tol
+    1e-6 the error is amplified by the conditioning (<= 1e-2) and GMRES converges fast."""
+    A = (P.neglapl(n, dim) - shift * sp.identity(n ** dim)).tocsc()
+    X = P.linspace_nd(n, dim)
+    b = np.random.default_rng(1).uniform(-1, 1, A.shape[0])
+    for nlevels in (3, 5):
+        for tol in (0.0, 1e-6):
+            u = O.OracleTree(nlevels)
+            u.set_Xcoo(X)
+            u.set_tol(tol)
+            u.set_symm_kind(O.OracleTree.SYM)
+            u.set_scaling_kind(O.OracleTree.LDLT)
+            u.partition(A)
+            u.assemble(A)
+            u.factorize()
+            x = u.solve(b)
+            err = np.linalg.norm(A @ x - b) / np.linalg.norm(b)
+            assert err <= (1e-10 if tol == 0.0 else 1e-2), (nlevels, tol, err)
+    x, it, rr = u.gmres(b, 50, 50, 1e-12)
+    assert rr < 1e-12 and it < 20
+    assert np.linalg.norm(A @ x - b) / np.linalg.norm(b) < 1e-10
+
+
+def test_plu_exact_and_gmres():
+    """GEN/PLU (ApproxTest.Exact with neglapl_unsym): exact at tol 0; restarted GMRES
+    converges with every restart length."""
+    A = P.neglapl_unsym(20, 2, seed=3)
+    X = P.linspace_nd(20, 2)
+    b = np.random.default_rng(2).uniform(-1, 1, A.shape[0])
+    for tol in (0.0, 1e-2):
+        u = O.OracleTree(5)
+        u.set_Xcoo(X)
+        u.set_tol(tol)
+        u.set_symm_kind(O.OracleTree.GEN)
+        u.set_scaling_kind(O.OracleTree.PLU)
+        u.partition(A)
+        u.assemble(A)
+        u.factorize()
+        if tol == 0.0:
+            assert np.linalg.norm(A @ u.solve(b) - b) / np.linalg.norm(b) <= 1e-10
+    for restart in (1, 3, 100):
+        x, it, rr = u.gmres(b, 200, restart, 1e-12)
+        assert rr < 1e-12 and np.linalg.norm(A @ x - b) / np.linalg.norm(b) < 1e-10
