@@ -201,13 +201,16 @@ int spand_tree_get_ranks(spand_tree* t, int* out);
 /* Operation list in recording order: kind level self nbr ns nn rows cols (8 ints each);
  * kind: 0 ScalingLLT 1 GemmSymmOut 2 GemmSymmIn 3 Orthogonal 4 Merge 5 Split
  *       6 GemmOut 7 GemmIn 8 ScalingPLUQ (GEN / PLU; its matrix: L_s strictly below the
- *       diagonal, U_s on and above it) */
+ *       diagonal, U_s on and above it) 9 ScalingLDLT (SYM / LDLT; L_s in the lower triangle) */
 int spand_tree_num_ops(spand_tree* t, int* n);
 int spand_tree_get_ops(spand_tree* t, int* out);
 int spand_tree_get_op_matrix(spand_tree* t, int idx, double* out);
 int spand_tree_get_op_tau(spand_tree* t, int idx, double* out);
-/* row permutation p (ns entries) of a ScalingPLUQ op: x_s <- x_s[p] before L_s^{-1} */
+/* row permutation p (ns entries) of a ScalingPLUQ / ScalingLDLT op: x_s <- x_s[p] before
+ * L_s^{-1} */
 int spand_tree_get_op_perm(spand_tree* t, int idx, int* out);
+/* sign(D) (ns entries) of a ScalingLDLT op (SYM / LDLT path) */
+int spand_tree_get_op_signs(spand_tree* t, int idx, double* out);
 /* seconds: partition, assemble, factorize */
 int spand_tree_timings(spand_tree* t, double* out);
 /* kernels launched by this tree since the last reset */

@@ -263,7 +263,9 @@ static void larfg(int n, double& alpha, double* x, double& tau) {
     if (n <= 1) { tau = 0.0; return; }
     double xnorm = nrm2(n - 1, x);
     if (xnorm == 0.0) { tau = 0.0; return; }
-    double beta = -std::copysign(std::hypot(alpha, xnorm), alpha);
+    // beta = -sign(alpha) |(alpha, x)|, with sign(-0) = +1: a zero leading entry is a zero
+    // whatever the sign bit that rounding left on it (LAPACK's SIGN would follow the bit)
+    double beta = alpha >= 0.0 ? -std::hypot(alpha, xnorm) : std::hypot(alpha, xnorm);
     const double safmin = std::numeric_limits<double>::min() / std::numeric_limits<double>::epsilon();
     int knt = 0;
     if (std::fabs(beta) < safmin) {
@@ -275,7 +277,7 @@ static void larfg(int n, double& alpha, double* x, double& tau) {
             alpha *= rsafmn;
         } while (std::fabs(beta) < safmin && knt < 20);
         xnorm = nrm2(n - 1, x);
-        beta = -std::copysign(std::hypot(alpha, xnorm), alpha);
+        beta = alpha >= 0.0 ? -std::hypot(alpha, xnorm) : std::hypot(alpha, xnorm);
     }
     tau = (beta - alpha) / beta;
     double scal = 1.0 / (alpha - beta);
@@ -414,16 +416,22 @@ static int getf(Mat& A, std::vector<int>& perm) {
 // the strict lower triangle holds the unit L, the diagonal holds D, transp[k] the row
 // swapped with k.  Returns false where Eigen reports failure: an all-zero diagonal at step
 // 0, or a nonzero pivot after a zero one.
+// Deviation, as for the QRCP pivots: the pivot is the FIRST entry within a relative
+// LDLT_TIE of the largest magnitude.  The sign pivots of the sparsified clusters are +-I
+// in exact arithmetic, so after Q^T D Q their diagonals tie up to rounding, and the
+// summation order alone would decide Eigen's strict maximum.
+static const double LDLT_TIE = 1e-7;
 static bool ldlt_eigen(Mat& A, std::vector<int>& transp) {
     const int n = A.r;
     transp.assign(n, 0);
     std::vector<double> temp(n);
     bool ok = true, found_zero = false;
     for (int k = 0; k < n; k++) {
+        double bv = 0;
+        for (int j = k; j < n; j++) bv = std::max(bv, std::fabs(A(j, j)));
         int big = k;
-        double bv = std::fabs(A(k, k));
-        for (int j = k + 1; j < n; j++)
-            if (std::fabs(A(j, j)) > bv) { bv = std::fabs(A(j, j)); big = j; }
+        for (int j = k; j < n; j++)
+            if (std::fabs(A(j, j)) >= bv * (1.0 - LDLT_TIE)) { big = j; break; }
         transp[k] = big;
         if (big != k) {
             for (int c = 0; c < k; c++) std::swap(A(k, c), A(big, c));
@@ -1343,15 +1351,20 @@ struct Tree {
             sib->add_edge(std::make_unique<Edge>(Edge{sib, sib, std::make_unique<Mat>(Mat::eye(sib_size)), true}));
             original->pivot()->A = std::make_unique<Mat>(Mat::eye(osize));
         } else {
-            Mat& piv = *original->pivot()->A;  // n0 x n0
+            Mat& piv = *original->pivot()->A;  // n0 x n0, the signs of the scaling
             const int k = (int)h.size();
+            // Deviation: when every sign is the same, Q^T D Q = D exactly and is kept as it
+            // is; the reference forms it in floating point, where its zero entries become
+            // rounding noise whose signs then steer later Householder reflectors.
+            bool uniform = true;
+            for (int i = 1; i < n0; i++) uniform = uniform && piv(i, i) == piv(0, 0);
             std::vector<double> t(n0);
-            for (int r = 0; r < n0; r++) {  // piv <- piv Q (row by row: Q^T row^T)
+            for (int r = 0; r < n0 && !uniform; r++) {  // piv <- piv Q (row by row: Q^T row^T)
                 for (int c = 0; c < n0; c++) t[c] = piv(r, c);
                 ormqr_vec(v, h, k, t.data(), true);
                 for (int c = 0; c < n0; c++) piv(r, c) = t[c];
             }
-            for (int c = 0; c < n0; c++) ormqr_vec(v, h, k, &piv(0, c), true);  // piv <- Q^T piv
+            for (int c = 0; c < n0 && !uniform; c++) ormqr_vec(v, h, k, &piv(0, c), true);  // piv <- Q^T piv
             auto Aoo = std::make_unique<Mat>(osize, osize);
             auto Ass = std::make_unique<Mat>(sib_size, sib_size);
             auto Aso = std::make_unique<Mat>(sib_size, osize);

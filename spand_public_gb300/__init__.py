@@ -21,7 +21,7 @@ SPD, SYM, GEN = range(3)
 MND, RB = range(2)
 
 OP_NAMES = {0: "ScalingLLT", 1: "GemmSymmOut", 2: "GemmSymmIn", 3: "Orthogonal", 4: "Merge", 5: "Split",
-            6: "GemmOut", 7: "GemmIn", 8: "ScalingPLUQ"}
+            6: "GemmOut", 7: "GemmIn", 8: "ScalingPLUQ", 9: "ScalingLDLT"}
 
 _lib = None
 
@@ -106,6 +106,7 @@ _PROTOS = {
     "spand_tree_get_op_matrix": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "spand_tree_get_op_tau": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "spand_tree_get_op_perm": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "spand_tree_get_op_signs": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "spand_tree_timings": (C.c_int, [C.c_void_p, C.c_void_p]),
     "spand_tree_launches": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.c_int]),
     "spand_tree_device_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
@@ -366,8 +367,14 @@ class Tree:
         _check(self.L.spand_tree_get_op_matrix(self.h, int(idx), _ptr(buf)))
         return buf[: rows * cols].reshape((cols, rows)).T
 
+    def op_signs(self, idx, n):
+        """sign(D) of a ScalingLDLT op (n entries)."""
+        buf = np.zeros(max(n, 1))
+        _check(self.L.spand_tree_get_op_signs(self.h, int(idx), _ptr(buf)))
+        return buf[:n]
+
     def op_perm(self, idx, n):
-        """Row permutation of a ScalingPLUQ op (n entries)."""
+        """Row permutation of a ScalingPLUQ / ScalingLDLT op (n entries)."""
         buf = np.zeros(max(n, 1), dtype=np.int32)
         _check(self.L.spand_tree_get_op_perm(self.h, int(idx), _ptr(buf)))
         return buf[:n]

@@ -368,6 +368,14 @@ int spand_tree_get_op_matrix(spand_tree* t, int idx, double* out) {
         std::memcpy(out, m.data(), m.size() * sizeof(double));
     });
 }
+int spand_tree_get_op_signs(spand_tree* t, int idx, double* out) {
+    CHECK_T(t);
+    return guard([&] {
+        std::vector<double> m;
+        t->t->op_signs(idx, m);
+        std::memcpy(out, m.data(), m.size() * sizeof(double));
+    });
+}
 int spand_tree_get_op_perm(spand_tree* t, int idx, int* out) {
     CHECK_T(t);
     return guard([&] {

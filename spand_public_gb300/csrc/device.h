@@ -100,6 +100,8 @@ class DeviceFactorBase {
     // PLU path: the row permutation of cluster c's pivot (capacity entries; the first
     // csize[c] are meaningful)
     virtual void lu_perm(int c, std::vector<int>& out) = 0;
+    // LDLT path: sign(D) of cluster c's pivot (capacity entries)
+    virtual void ldlt_signs(int c, std::vector<double>& out) = 0;
     virtual int precision_bytes() const = 0;
     virtual cudaStream_t stream() const = 0;
     virtual size_t device_bytes() const = 0;

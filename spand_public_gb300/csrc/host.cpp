@@ -360,9 +360,10 @@ struct SymTree {
 
 }  // namespace
 
-Plan build_plan(const Hierarchy& H, const Assembly& asmb, int skip, bool use_want_sparsify, bool lu) {
+Plan build_plan(const Hierarchy& H, const Assembly& asmb, int skip, bool use_want_sparsify, bool lu, bool ldlt) {
     Plan P;
     P.lu = lu;
+    P.ldlt = ldlt;
     const int nl = H.nlevels;
     const int nc = (int)H.start.size();
     P.nlevels = nl;
@@ -486,7 +487,9 @@ Plan build_plan(const Hierarchy& H, const Assembly& asmb, int skip, bool use_wan
                 for (int e : T.out_nbr(c)) L.scale_trsm.push_back({T.edges[e].block, c, 1});
                 L.op_scale_llt.push_back(c);
                 L.op_scale_llt_block.push_back(piv);
-                T.edges[pe].block = T.new_block(c, c, BLK_IDENTITY, cursor);
+                // the new pivot: I, or diag(sign D) on the LDLT path (tree.cpp:830)
+                T.edges[pe].block = T.new_block(c, c, ldlt ? BLK_STORED : BLK_IDENTITY, cursor);
+                L.scale_newpiv.push_back(ldlt ? T.edges[pe].block : -1);
             }
             // ---- sparsify (tree.cpp:1417-1433, 1292-1347), scheduled in waves ----
             std::vector<int> wave_of(nc, -1);
@@ -519,6 +522,24 @@ Plan build_plan(const Hierarchy& H, const Assembly& asmb, int skip, bool use_wan
                 P.v_len += (int64_t)P.c_cap[c] * P.c_cap[c];
                 it.tau_off = P.tau_len;
                 P.tau_len += P.c_cap[c];
+                if (ldlt) {
+                    // sibling: capacity of the cluster, its own solve slot, pivot and edge blocks
+                    const int sib = (int)P.c_cap.size();
+                    P.c_start.push_back(P.c_start[c]);
+                    P.c_cap.push_back(P.c_cap[c]);
+                    P.c_level.push_back(P.c_level[c]);
+                    P.c_order.push_back(sib);
+                    P.c_hlevel.push_back(ilvl);
+                    P.c_parent.push_back(-1);
+                    P.c_sparsify.push_back(0);
+                    P.c_children.push_back({});
+                    P.c_xoff.push_back(P.x_len);
+                    P.x_len += P.c_cap[c];
+                    it.piv = T.edges[T.pivot(c)].block;
+                    it.sib = sib;
+                    it.sib_piv = T.new_block(sib, sib, BLK_STORED, cursor);
+                    it.aso = T.new_block(sib, c, BLK_STORED, cursor);
+                }
                 wave_of[c] = w;
                 if ((int)L.waves.size() <= w) L.waves.resize(w + 1);
                 L.waves[w].push_back(it);
@@ -570,6 +591,8 @@ Plan build_plan(const Hierarchy& H, const Assembly& asmb, int skip, bool use_wan
         }
     }
     P.arena_len = cursor;
+    P.nclusters_h = nc;
+    P.nclusters = (int)P.c_cap.size();  // with the LDLT siblings
     return P;
 }
 

@@ -100,6 +100,10 @@ struct SparsifyItem {
     int cap_cols;       // capacity of Asn columns
     int64_t v_off;      // persistent reflector storage (cap x cap) for the Orthogonal op
     int64_t tau_off;    // persistent tau storage (cap)
+    // LDLT path (src/tree.cpp:1069-1097): the cluster's pivot block (sign(D) after its
+    // scaling, transformed to Q^T D Q and split), the sibling cluster made of the dropped
+    // rows, its pivot block and the block of the edge original -> sibling (-1 elsewhere)
+    int piv = -1, sib = -1, sib_piv = -1, aso = -1;
 };
 
 // Copy of a child block into a parent block during a merge (src/tree.cpp:1133-1184).
@@ -130,6 +134,7 @@ struct LevelPlan {
     std::vector<int> scale_clusters;
     std::vector<int> scale_pivots;
     std::vector<int> scale_inv;
+    std::vector<int> scale_newpiv;  // LDLT: block receiving diag(sign D) as the new pivot
     std::vector<TrsmItem> scale_trsm;
     // sparsification (src/tree.cpp:1521-1532): waves of mutually non-adjacent clusters
     std::vector<std::vector<SparsifyItem>> waves;
@@ -155,6 +160,11 @@ struct Plan {
     // LU path (SymmKind::GEN, ScalingKind::PLU): every stored block in both directions,
     // partial-pivot LU of the pivots, Schur updates over (out-edge, in-edge) pairs
     bool lu = false;
+    // LDLT path (SymmKind::SYM, ScalingKind::LDLT): the symmetric structure with pivoted
+    // LDL^T pivots, sign-weighted Schur updates, sign pivots after scaling and an explicit
+    // sibling per sparsified cluster (clusters nclusters_h .. nclusters-1)
+    bool ldlt = false;
+    int nclusters_h = 0;  // clusters of the hierarchy; the rest are LDLT siblings
     int nclusters = 0;        // clusters of the hierarchy (siblings are implicit)
     std::vector<int> c_start, c_cap, c_level, c_order, c_hlevel, c_parent, c_sparsify;
     std::vector<std::vector<int>> c_children;
@@ -194,7 +204,8 @@ struct Assembly {
 };
 Assembly assembly_structure(const Hierarchy& H, const Csc& App, bool symmetric);
 
-Plan build_plan(const Hierarchy& H, const Assembly& asmb, int skip, bool use_want_sparsify, bool lu = false);
+Plan build_plan(const Hierarchy& H, const Assembly& asmb, int skip, bool use_want_sparsify, bool lu = false,
+                bool ldlt = false);
 
 // For every entry k of A (natural ordering, CSC order): the element offset of A(r, c) in
 // the assembled level-0 blocks, or -1 when the entry is not stored (upper triangle of the

@@ -543,9 +543,14 @@ constexpr int TRB = 32;  // independent indices per TRSM tile
 // A tile of 32 independent indices is staged in shared memory; every thread computes
 // columns c of one q with four partial sums; no barrier after the staging.
 // ------------------------------------------------------------------------------------
+// LDLT path (perm_store != nullptr): the s index of B is gathered through the pivot's row
+// permutation while the tile is staged: side 0 L^{-1} P^T B, side 1 B P L^{-T}
+// (tree.cpp:691-715); such launches always stage (checked when the plan is uploaded).
 template <typename T>
 __global__ void __launch_bounds__(256) trsm3_kernel(Ctx<T> c, const DTrsm* __restrict__ items,
-                                                   const DTile* __restrict__ tiles, int ntiles, int smem_elems) {
+                                                   const DTile* __restrict__ tiles, int ntiles, int smem_elems,
+                                                   const int* __restrict__ perm_store = nullptr,
+                                                   const long long* __restrict__ poff = nullptr) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* X = reinterpret_cast<T*>(smem_raw);
     const int t = blockIdx.x;
@@ -565,13 +570,14 @@ __global__ void __launch_bounds__(256) trsm3_kernel(Ctx<T> c, const DTrsm* __res
     const long long sq = it.side == 1 ? 1 : bld, sk = it.side == 1 ? bld : 1;
     T* Bt = B + (it.side == 1 ? (size_t)r0 : (size_t)r0 * bld);
     const bool staged = (long long)tr * n <= smem_elems;
+    const int* perm = perm_store ? perm_store + poff[it.cluster] : nullptr;
     const T* src;
     long long xq, xk;
     if (staged) {
         for (int idx = threadIdx.x; idx < tr * n; idx += blockDim.x) {
             int q, k;
             if (it.side == 1) { q = idx % tr; k = idx / tr; } else { k = idx % n; q = idx / n; }
-            X[q + k * TRB] = Bt[q * sq + k * sk];
+            X[q + k * TRB] = Bt[q * sq + (long long)(perm ? perm[k] : k) * sk];
         }
         __syncthreads();
         src = X;
@@ -886,6 +892,280 @@ __global__ void __launch_bounds__(256) lu_trsm_kernel(Ctx<T> c, const DTrsm* __r
 }
 
 // ------------------------------------------------------------------------------------
+// LDLT path.  Eigen's pivoted LDL^T of a pivot block (util.cpp:167-184 over
+// Eigen/src/Cholesky/LDLT.h, ldlt_inplace<Lower>::unblocked): at step k the pivot is the
+// first diagonal entry of largest magnitude among k..n-1 as they stand (those after k not
+// yet updated), swapped symmetrically inside the lower triangle, then the left-looking
+// column update.  L_s = L |D|^1/2, s = sign(D), perm = swap2perm(transpositions); the
+// block is left in the Cholesky path's layout (L_s in the lower triangle, (L_s^{-1})^T in
+// the strict upper triangle), so the TRSM and solve kernels of that path apply.  newpiv
+// (scaling): receives diag(s), the cluster's new pivot (tree.cpp:830).  One CTA per pivot;
+// shared memory when n^2 + n elements fit, else in place in the pivot block.
+// ------------------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(LU_THREADS) ldlt_kernel(Ctx<T> c, const int* __restrict__ pivots,
+                                                         const int* __restrict__ clusters,
+                                                         const int* __restrict__ newpiv, int count, int smem_elems,
+                                                         int* __restrict__ perm_store, int* __restrict__ swp_store,
+                                                         T* __restrict__ sign_store,
+                                                         const long long* __restrict__ poff) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ T wv[LU_THREADS / 32];
+    __shared__ int wi[LU_THREADS / 32];
+    __shared__ T red[33];
+    __shared__ T s_gmax;
+    __shared__ int prow, bad, zero_seen;
+    const int item = blockIdx.x;
+    if (item >= count || c.status->not_spd) return;
+    const int cid = clusters[item];
+    const int n = c.csize[cid];
+    if (n == 0) return;
+    T* G = bptr(c, pivots[item]);
+    const int gld = c.blk[pivots[item]].ld;
+    T* tmp = reinterpret_cast<T*>(smem_raw);
+    const bool in_smem = (long long)n * n + n <= smem_elems;
+    T* A = in_smem ? tmp + n : G;
+    const int lda = in_smem ? n : gld;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    int* swp = swp_store + poff[cid];
+    int* perm = perm_store + poff[cid];
+    T* sg = sign_store + poff[cid];
+    if (in_smem)
+        for (int idx = tid; idx < n * n; idx += LU_THREADS) {
+            const int i = idx % n, j = idx / n;
+            if (i >= j) A[i + (size_t)j * lda] = G[i + (size_t)j * gld];
+        }
+    if (tid == 0) {
+        bad = 0;
+        zero_seen = 0;
+    }
+    __syncthreads();
+    for (int k = 0; k < n; k++) {
+        // pivot: the first diagonal entry of largest magnitude among k..n-1
+        T bv = T(-1);
+        int bi = n;
+        for (int j = k + tid; j < n; j += LU_THREADS) argmax_merge(bv, bi, (T)fabs(A[j + (size_t)j * lda]), j);
+        for (int o = 16; o > 0; o >>= 1) {
+            const T ov = __shfl_down_sync(0xffffffffu, bv, o);
+            const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+            argmax_merge(bv, bi, ov, oi);
+        }
+        if (lane == 0) {
+            wv[wid] = bv;
+            wi[wid] = bi;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            T v = wv[0];
+            int i = wi[0];
+            for (int w = 1; w < LU_THREADS / 32; w++) argmax_merge(v, i, wv[w], wi[w]);
+            s_gmax = v;
+        }
+        __syncthreads();
+        {
+            // the first entry within the tie window of the largest (the oracle's rule)
+            const T thr = s_gmax * (T(1) - qrcp_tie<T>());
+            int f = n;
+            for (int j = k + tid; j < n; j += LU_THREADS)
+                if ((T)fabs(A[j + (size_t)j * lda]) >= thr) {
+                    f = j;
+                    break;
+                }
+            for (int o = 16; o > 0; o >>= 1) f = min(f, __shfl_down_sync(0xffffffffu, f, o));
+            if (lane == 0) wi[wid] = f;
+            __syncthreads();
+            if (tid == 0) {
+                int i = wi[0];
+                for (int w = 1; w < LU_THREADS / 32; w++) i = min(i, wi[w]);
+                if (i >= n) i = k;
+                prow = i;
+                swp[k] = i;
+            }
+            __syncthreads();
+        }
+        const int big = prow;
+        if (big != k) {
+            // symmetric swap inside the lower triangle: row k / row big left of column k,
+            // columns k / big below row big, the two diagonals, and the entries between
+            for (int q = tid; q < n; q += LU_THREADS) {
+                if (q < k) {
+                    const T a = A[k + (size_t)q * lda];
+                    A[k + (size_t)q * lda] = A[big + (size_t)q * lda];
+                    A[big + (size_t)q * lda] = a;
+                } else if (q > big) {
+                    const T a = A[q + (size_t)k * lda];
+                    A[q + (size_t)k * lda] = A[q + (size_t)big * lda];
+                    A[q + (size_t)big * lda] = a;
+                } else if (q == k) {
+                    const T a = A[k + (size_t)k * lda];
+                    A[k + (size_t)k * lda] = A[big + (size_t)big * lda];
+                    A[big + (size_t)big * lda] = a;
+                } else if (q < big) {  // k < q < big
+                    const T a = A[q + (size_t)k * lda];
+                    A[q + (size_t)k * lda] = A[big + (size_t)q * lda];
+                    A[big + (size_t)q * lda] = a;
+                }
+            }
+            __syncthreads();
+        }
+        // left-looking update of column k: temp_j = D_j A(k,j), A(k,k) -= A(k,:) temp,
+        // A(k+1:,k) -= A(k+1:,0:k) temp
+        if (k > 0) {
+            for (int j = tid; j < k; j += LU_THREADS) tmp[j] = A[j + (size_t)j * lda] * A[k + (size_t)j * lda];
+            __syncthreads();
+            T part = 0;
+            for (int j = tid; j < k; j += LU_THREADS) part += A[k + (size_t)j * lda] * tmp[j];
+            part = block_sum(part, red);
+            for (int i = k + 1 + tid; i < n; i += LU_THREADS) {
+                T s = 0;
+                for (int j = 0; j < k; j++) s += A[i + (size_t)j * lda] * tmp[j];
+                A[i + (size_t)k * lda] -= s;
+            }
+            if (tid == 0) A[k + (size_t)k * lda] -= part;
+            __syncthreads();
+        }
+        const T akk = A[k + (size_t)k * lda];
+        const bool valid = fabs(akk) > T(0);
+        if (k == 0 && !valid) {
+            if (tid == 0) bad = 1;
+            break;
+        }
+        int nz = 0;
+        for (int i = k + 1 + tid; i < n; i += LU_THREADS) {
+            if (valid) A[i + (size_t)k * lda] /= akk;
+            else nz |= A[i + (size_t)k * lda] != T(0);
+        }
+        if (nz) bad = 1;
+        __syncthreads();
+        if (tid == 0) {
+            if (zero_seen && valid) bad = 1;
+            else if (!valid) zero_seen = 1;
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    if (bad) {
+        if (tid == 0) atomicCAS(&c.status->not_spd, 0, cid + 1);
+        return;
+    }
+    if (tid == 0) {
+        for (int i = 0; i < n; i++) perm[i] = i;
+        for (int i = 0; i < n; i++) {
+            const int s = swp[i], t = perm[s];
+            perm[s] = perm[i];
+            perm[i] = t;
+        }
+    }
+    // L_s = L |D|^1/2 below the diagonal from the unscaled diagonal, then the diagonal
+    for (int idx = tid; idx < n * n; idx += LU_THREADS) {
+        const int i = idx % n, j = idx / n;
+        if (i > j) A[i + (size_t)j * lda] *= dsqrt((T)fabs(A[j + (size_t)j * lda]));
+    }
+    __syncthreads();
+    for (int j = tid; j < n; j += LU_THREADS) {
+        T& d = A[j + (size_t)j * lda];
+        sg[j] = T((d > T(0)) - (d < T(0)));
+        d = dsqrt((T)fabs(d));
+    }
+    __syncthreads();
+    // (L_s^{-1})^T into the strict upper triangle, columns of L_s^{-1} from the last:
+    // column j below the diagonal = -L22^{-1} x / l_jj, L22^{-1} read back from the
+    // upper triangle (diagonal 1 / L_s(i,i))
+    for (int j = n - 1; j >= 0; j--) {
+        const T lj = T(1) / A[j + (size_t)j * lda];
+        for (int i = j + 1 + tid; i < n; i += LU_THREADS) {
+            T s = A[i + (size_t)j * lda] / A[i + (size_t)i * lda];
+            for (int k = j + 1; k < i; k++) s += A[k + (size_t)i * lda] * A[k + (size_t)j * lda];
+            A[j + (size_t)i * lda] = -lj * s;
+        }
+        __syncthreads();
+    }
+    if (in_smem)
+        for (int idx = tid; idx < n * n; idx += LU_THREADS) {
+            const int i = idx % n, j = idx / n;
+            G[i + (size_t)j * gld] = A[i + (size_t)j * lda];
+        }
+    if (newpiv) {
+        T* Np = bptr(c, newpiv[item]);
+        const int nld = c.blk[newpiv[item]].ld;
+        for (int j = tid; j < n; j += LU_THREADS) Np[j + (size_t)j * nld] = sg[j];
+    }
+}
+
+// LDLT sparsification with a sign pivot (tree.cpp:1069-1097): the pivot block of the
+// cluster (diag(s) from its scaling) becomes M = Q^T D Q (the rows first, piv Q, then the
+// columns, Q^T piv, as the reference's two ormqr calls), then splits: M[0:k, 0:k] stays
+// as the cluster's pivot, M[k:r, k:r] becomes the sibling's pivot, M[k:r, 0:k] the block
+// of the edge cluster -> sibling; the sibling's size is r - k.  Reflector j: 1 at row j,
+// V[j+1:r, j] below, tau from the QRCP.  One CTA per sparsified cluster.
+template <typename T>
+__global__ void __launch_bounds__(256) pivot_split_kernel(Ctx<T> c, const DSpars* __restrict__ items,
+                                                          const int* __restrict__ sib_of,
+                                                          const int* __restrict__ sib_piv_of,
+                                                          const int* __restrict__ aso_of,
+                                                          const int* __restrict__ piv_of, const T* vstore,
+                                                          const T* taus, const T* __restrict__ sign_store,
+                                                          const long long* __restrict__ soff) {
+    const DSpars it = items[blockIdx.x];
+    if (c.status->not_spd) return;
+    const int cl = it.cluster;
+    const int r = c.rows0[cl], k = c.csize[cl];
+    const int sib = sib_of[blockIdx.x];
+    if (k >= r) {
+        if (threadIdx.x == 0) c.csize[sib] = c.rows0[sib] = 0;
+        return;
+    }
+    T* M = bptr(c, piv_of[blockIdx.x]);
+    const int ld = c.blk[piv_of[blockIdx.x]].ld;
+    const int vld = c.cap[cl];
+    const T* V = vstore + it.v_off;
+    const T* tau = taus + it.tau_off;
+    // the oracle's deviation: signs all equal -> Q^T D Q = D exactly, kept as it is
+    const T* sg = sign_store + soff[cl];
+    int uni = 1;
+    for (int p = threadIdx.x; p < r; p += blockDim.x) uni &= sg[p] == sg[0];
+    const bool all_uniform = __syncthreads_and(uni);
+    // rows: M[p, :] <- M[p, :] H_0 H_1 ... H_{k-1}
+    for (int p = threadIdx.x; p < r && !all_uniform; p += blockDim.x)
+        for (int j = 0; j < k; j++) {
+            const T tj = tau[j];
+            if (tj == T(0)) continue;
+            T w = M[p + (size_t)j * ld];
+            for (int q = j + 1; q < r; q++) w += M[p + (size_t)q * ld] * V[q + (size_t)j * vld];
+            w *= tj;
+            M[p + (size_t)j * ld] -= w;
+            for (int q = j + 1; q < r; q++) M[p + (size_t)q * ld] -= w * V[q + (size_t)j * vld];
+        }
+    __syncthreads();
+    // columns: M[:, q] <- H_{k-1} ... H_0 M[:, q]
+    for (int q = threadIdx.x; q < r && !all_uniform; q += blockDim.x) {
+        T* m = M + (size_t)q * ld;
+        for (int j = 0; j < k; j++) {
+            const T tj = tau[j];
+            if (tj == T(0)) continue;
+            T w = m[j];
+            for (int i = j + 1; i < r; i++) w += V[i + (size_t)j * vld] * m[i];
+            w *= tj;
+            m[j] -= w;
+            for (int i = j + 1; i < r; i++) m[i] -= w * V[i + (size_t)j * vld];
+        }
+    }
+    __syncthreads();
+    T* S = bptr(c, sib_piv_of[blockIdx.x]);
+    const int sld = c.blk[sib_piv_of[blockIdx.x]].ld;
+    T* E = bptr(c, aso_of[blockIdx.x]);
+    const int eld = c.blk[aso_of[blockIdx.x]].ld;
+    const int m = r - k;
+    for (int idx = threadIdx.x; idx < m * r; idx += blockDim.x) {
+        const int i = idx % m, j = idx / m;  // row k + i, column j
+        const T v = M[(k + i) + (size_t)j * ld];
+        if (j < k) E[i + (size_t)j * eld] = v;
+        else S[i + (size_t)(j - k) * sld] = v;
+    }
+    if (threadIdx.x == 0) c.csize[sib] = c.rows0[sib] = m;
+}
+
+// ------------------------------------------------------------------------------------
 // Schur complement updates grouped by target block, applied in the reference order
 // (tree.cpp:748-793, 858-883): C(n1 x n2) -= op1(B1) op2(B2).  32x32 output tile per
 // block, 256 threads, 2x2 outputs per thread, K staged through shared memory.
@@ -893,10 +1173,13 @@ __global__ void __launch_bounds__(256) lu_trsm_kernel(Ctx<T> c, const DTrsm* __r
 constexpr int ST = 32;
 constexpr int SK = 16;
 
+// LDLT path (signs != nullptr): C -= op(B1) D^{-1} op(B2) with D = diag(sign) of the
+// eliminated cluster s (tree.cpp:784-789; the signs are +-1, so D^{-1} = D).
 template <typename T>
 __global__ void __launch_bounds__(256) schur_kernel(Ctx<T> c, const DTarget* __restrict__ targets,
                                                      const DUpd* __restrict__ ups, const DTile* __restrict__ tiles,
-                                                     int ntiles) {
+                                                     int ntiles, const T* __restrict__ signs = nullptr,
+                                                     const long long* __restrict__ soff = nullptr) {
     const int t = blockIdx.x;
     if (t >= ntiles || c.status->not_spd) return;
     const DTarget tg = targets[tiles[t].item];
@@ -932,7 +1215,10 @@ __global__ void __launch_bounds__(256) schur_kernel(Ctx<T> c, const DTarget* __r
                 if (up.t1) { kk = idx % SK; ii = idx / SK; } else { ii = idx % ST; kk = idx / ST; }
                 int i = i0 + ii, k = k0 + kk;
                 T v = T(0);
-                if (i < M && k < S) v = up.t1 ? B1[k + (size_t)i * ld1] : B1[i + (size_t)k * ld1];
+                if (i < M && k < S) {
+                    v = up.t1 ? B1[k + (size_t)i * ld1] : B1[i + (size_t)k * ld1];
+                    if (signs) v *= signs[soff[up.s] + k];
+                }
                 Xs[ii][kk] = v;
             }
             // Y tile: SK x ST, Y[k,j] = t2 ? B2[j + k ld2] : B2[k + j ld2]
@@ -1282,6 +1568,57 @@ __global__ void __launch_bounds__(256) lu_apply_kernel(Ctx<T> c, XCtx<T> X, cons
     }
 }
 
+// LDLT solve steps (operations.cpp:128-142, 44-53):
+// perm_x_kernel: x_s <- P^T x_s (fwd, before L_s^{-1}) or x_s <- P x_s (bwd, after L_s^{-T});
+// sign_x_kernel: the diag phase, x_s <- D^{-1} x_s = s .* x_s;
+// split_x_kernel: the Split op, x_sib <- x_c[k:r] (fwd) or x_c[k:r] <- x_sib (bwd).
+// One CTA per (cluster, right-hand side); sizes rows0 (the size when the op was recorded).
+template <typename T>
+__global__ void perm_x_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ clusters, int count,
+                              const int* __restrict__ perm_store, const long long* __restrict__ poff, int fwd) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* t = reinterpret_cast<T*>(smem_raw);
+    const int item = blockIdx.x, r = blockIdx.y;
+    if (item >= count) return;
+    const int cid = clusters[item];
+    const int n = c.rows0[cid];
+    T* x = X.xs + X.xoff[cid] + (long long)r * X.xld;
+    const int* perm = perm_store + poff[cid];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) t[i] = x[i];
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        if (fwd) x[i] = t[perm[i]];
+        else x[perm[i]] = t[i];
+    }
+}
+
+template <typename T>
+__global__ void sign_x_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ clusters, int count,
+                              const T* __restrict__ sign_store, const long long* __restrict__ poff) {
+    const int item = blockIdx.x, r = blockIdx.y;
+    if (item >= count) return;
+    const int cid = clusters[item];
+    const int n = c.rows0[cid];
+    T* x = X.xs + X.xoff[cid] + (long long)r * X.xld;
+    const T* s = sign_store + poff[cid];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] *= s[i];
+}
+
+template <typename T>
+__global__ void split_x_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ owners, const int* __restrict__ sibs,
+                               int count, int fwd) {
+    const int item = blockIdx.x, r = blockIdx.y;
+    if (item >= count) return;
+    const int cl = owners[item], sb = sibs[item];
+    const int k = c.csize[cl], m = c.csize[sb];
+    T* xc = X.xs + X.xoff[cl] + (long long)r * X.xld + k;
+    T* xsb = X.xs + X.xoff[sb] + (long long)r * X.xld;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        if (fwd) xsb[i] = xc[i];
+        else xc[i] = xsb[i];
+    }
+}
+
 // b = P^T x (natural -> permuted leaf slots), FP64 in, T out
 template <typename T>
 __global__ void perm_in_kernel(const double* __restrict__ x, int ldx, XCtx<T> X, const int* __restrict__ perm,
@@ -1402,15 +1739,20 @@ __global__ void __launch_bounds__(TV_THREADS) trsv4_kernel(Ctx<T> c, XCtx<T> X, 
 // reduced in a fixed order.
 constexpr int GF_ROWS = 64;
 
+// LDLT path: signs != nullptr weights x_self by the signs of self (A D x_s,
+// operations.cpp:55-83); sib_mode: the neighbour is a sparsified cluster whose size is now
+// csize (the op of a sibling, recorded after the split).
 template <typename T>
 __global__ void __launch_bounds__(256) gemm_fwd2_kernel(Ctx<T> c, XCtx<T> X, const DGroup* __restrict__ groups,
                                                         const DGemmOp* __restrict__ ops, const DTile* __restrict__ tiles,
-                                                        int ntiles, int rhs_stride) {
+                                                        int ntiles, int rhs_stride, const T* __restrict__ signs = nullptr,
+                                                        const long long* __restrict__ soff = nullptr,
+                                                        int sib_mode = 0) {
     const int t = blockIdx.x % ntiles;
     const int r = blockIdx.x / ntiles;
     const DGroup G = groups[tiles[t].item];
     const int nb = G.key;
-    const int nn = c.rows0[nb];
+    const int nn = sib_mode ? c.csize[nb] : c.rows0[nb];
     const int i0 = tiles[t].tile_i * GF_ROWS;
     if (i0 >= nn) return;
     (void)rhs_stride;
@@ -1425,9 +1767,17 @@ __global__ void __launch_bounds__(256) gemm_fwd2_kernel(Ctx<T> c, XCtx<T> X, con
         const T* xs = X.xs + X.xoff[op.self] + r * X.xld;
         const T* A = bptr(c, op.block);
         const int ld = c.blk[op.block].ld;
+        const T* sg = signs ? signs + soff[op.self] : nullptr;
         if (i < nn) {
             T s0 = 0, s1 = 0;
-            if (op.kind == 1) {
+            if (sg) {
+                if (op.kind == 1) {
+                    for (int j = sp; j < ns; j += 4) s0 += A[i + (size_t)j * ld] * (sg[j] * xs[j]);
+                } else {
+                    const T* a = A + (size_t)i * ld;
+                    for (int j = sp; j < ns; j += 4) s0 += a[j] * (sg[j] * xs[j]);
+                }
+            } else if (op.kind == 1) {
                 int j = sp;
                 for (; j + 4 < ns; j += 8) {
                     s0 += A[i + (size_t)j * ld] * xs[j];
@@ -1454,7 +1804,9 @@ constexpr int GB_ROWS = 32;
 template <typename T>
 __global__ void __launch_bounds__(256) gemm_bwd2_kernel(Ctx<T> c, XCtx<T> X, const DGroup* __restrict__ groups,
                                                         const DGemmOp* __restrict__ ops, const DTile* __restrict__ tiles,
-                                                        int ntiles) {
+                                                        int ntiles, const T* __restrict__ signs = nullptr,
+                                                        const long long* __restrict__ soff = nullptr,
+                                                        int sib_mode = 0) {
     const int t = blockIdx.x % ntiles;
     const int r = blockIdx.x / ntiles;
     const DGroup G = groups[tiles[t].item];
@@ -1470,7 +1822,7 @@ __global__ void __launch_bounds__(256) gemm_bwd2_kernel(Ctx<T> c, XCtx<T> X, con
         T acc = 0;
         for (int o = 0; o < G.count; o++) {
             const DGemmOp op = ops[G.first + o];
-            const int nn = c.rows0[op.nbr];
+            const int nn = sib_mode ? c.csize[op.nbr] : c.rows0[op.nbr];
             const T* xn = X.xs + X.xoff[op.nbr] + r * X.xld;
             const T* A = bptr(c, op.block);
             const int ld = c.blk[op.block].ld;
@@ -1483,7 +1835,7 @@ __global__ void __launch_bounds__(256) gemm_bwd2_kernel(Ctx<T> c, XCtx<T> X, con
             }
             acc += warp_sum(s);
         }
-        if (lane == 0) xs[i] -= acc;
+        if (lane == 0) xs[i] -= signs ? signs[soff[sc] + i] * acc : acc;  // LDLT: D (A^T x_n)
     }
 }
 
@@ -2090,6 +2442,7 @@ class DeviceFactor : public DeviceFactorBase {
         P_ = &P;
         nc_ = P.nclusters;
         lu_ = P.lu;
+        ldlt_ = P.ldlt;
         init_qrcp_limits();
         SPAND_CUDA(cudaStreamCreateWithFlags(&s2_, cudaStreamNonBlocking));
         SPAND_CUDA(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
@@ -2140,6 +2493,10 @@ class DeviceFactor : public DeviceFactorBase {
                 D.elim_inv = up(L.elim_inv);
                 D.elim_lu_smem = lu_smem_for(L.elim_clusters, P);
             }
+            if (ldlt_) {
+                D.elim_lu_smem = lu_smem_for(L.elim_clusters, P);
+                if (D.n_elim && !D.elim_trsm0.smem) throw DeviceError{SPAND_ERR_UNSUPPORTED, "pivot too large for the LDLT panels"};
+            }
             {
                 std::vector<DTarget> tg;
                 std::vector<DTile> tiles;
@@ -2167,6 +2524,12 @@ class DeviceFactor : public DeviceFactorBase {
             if (lu_) {
                 D.scale_inv = up(L.scale_inv);
                 D.scale_lu_smem = lu_smem_for(L.scale_clusters, P);
+            }
+            if (ldlt_) {
+                D.scale_newpiv = up(L.scale_newpiv);
+                D.scale_lu_smem = lu_smem_for(L.scale_clusters, P);
+                if (D.n_scale && !D.scale_trsm0.smem)
+                    throw DeviceError{SPAND_ERR_UNSUPPORTED, "pivot too large for the LDLT panels"};
             }
             {
                 std::vector<int> all;
@@ -2214,6 +2577,44 @@ class DeviceFactor : public DeviceFactorBase {
                     if (g > qc_smem_cap_)
                         throw DeviceError{SPAND_ERR_UNSUPPORTED, "sparsification matrix too large for the QRCP kernels"};
                     W.gsmem = (int)((g + 255) & ~int64_t(255));
+                }
+                if (ldlt_) {
+                    // the sign pivot's Q^T D Q split, the sibling's LDL^T, the edge's panel and
+                    // the Schur update of the cluster's pivot (tree.cpp:1069-1097, 1340-1341)
+                    std::vector<int> sib, sibp, aso, piv;
+                    std::vector<DTrsm> tr;
+                    std::vector<int> ext;
+                    std::vector<DTarget> tg;
+                    std::vector<DUpd> uu;
+                    std::vector<DTile> tiles;
+                    int mx = 1;
+                    for (const SparsifyItem& it : wave) {
+                        sib.push_back(it.sib);
+                        sibp.push_back(it.sib_piv);
+                        aso.push_back(it.aso);
+                        piv.push_back(it.piv);
+                        tr.push_back({it.aso, it.sib_piv, it.sib, 0});
+                        ext.push_back(P.c_cap[it.cluster]);
+                        const int t = (int)tg.size();
+                        tg.push_back({it.piv, 1, (int)uu.size(), 1});
+                        uu.push_back({it.aso, 1, it.aso, 0, it.sib});
+                        const int nt = (P.c_cap[it.cluster] + ST - 1) / ST;
+                        for (int a = 0; a < nt; a++)
+                            for (int b = 0; b <= a; b++) tiles.push_back({t, a, b});
+                        mx = std::max(mx, P.c_cap[it.cluster]);
+                    }
+                    W.sib = up(sib);
+                    W.sib_piv = up(sibp);
+                    W.aso = up(aso);
+                    W.piv = up(piv);
+                    auto tt = tiles_1d(ext, TRB);
+                    W.sib_trsm = {up(tr), up(tt), (int)tt.size(), 0, trsm_smem_n(mx)};
+                    if (!W.sib_trsm.smem) throw DeviceError{SPAND_ERR_UNSUPPORTED, "cluster too large for the LDLT panels"};
+                    W.sib_targets = up(tg);
+                    W.sib_ups = up(uu);
+                    W.sib_tiles = up(tiles);
+                    W.n_sib_tiles = (int)tiles.size();
+                    W.ldlt_smem = lu_smem_n(mx);
                 }
                 D.waves.push_back(W);
             }
@@ -2324,6 +2725,62 @@ class DeviceFactor : public DeviceFactorBase {
                     }
                 D.n_ortho = (int)ot.size();
                 D.ortho = up(ot);
+                if (ldlt_) {
+                    std::vector<int> sibs, owners, spiv;
+                    std::map<int, std::vector<DGemmOp>> fwd, bwd;
+                    std::vector<int> fk, bk;
+                    for (const auto& wave : L.waves)
+                        for (const SparsifyItem& it : wave) {
+                            sibs.push_back(it.sib);
+                            owners.push_back(it.cluster);
+                            spiv.push_back(it.sib_piv);
+                            // GemmSymmIn(sibling, cluster) with the sibling's signs
+                            fk.push_back(it.cluster);
+                            fwd[it.cluster].push_back({it.sib, it.cluster, it.aso, 2});
+                            bk.push_back(it.sib);
+                            bwd[it.sib].push_back({it.sib, it.cluster, it.aso, 2});
+                        }
+                    D.n_sib = (int)sibs.size();
+                    D.sib_clusters = up(sibs);
+                    D.sib_owner = up(owners);
+                    D.sib_piv = up(spiv);
+                    D.x_smem_sib = xsmem_for(sibs, P);
+                    {
+                        std::vector<int2> t;
+                        for (size_t k = 0; k < sibs.size(); k++) {
+                            const int cap = P.c_cap[sibs[k]];
+                            const int nt = cap <= 2 * TV_ROWS ? 1 : (cap + TV_ROWS - 1) / TV_ROWS;
+                            for (int q = 0; q < nt; q++) t.push_back(make_int2((int)k, q));
+                        }
+                        D.n_sib_tv = (int)t.size();
+                        D.sib_tv = up(t);
+                    }
+                    std::vector<DGroup> fg, bg;
+                    std::vector<DGemmOp> fo, bo;
+                    std::vector<int> ef, eb;
+                    for (int k : fk) {
+                        fg.push_back({k, (int)fo.size(), (int)fwd[k].size()});
+                        fo.insert(fo.end(), fwd[k].begin(), fwd[k].end());
+                        ef.push_back(P.c_cap[k]);
+                    }
+                    for (int k : bk) {
+                        bg.push_back({k, (int)bo.size(), (int)bwd[k].size()});
+                        bo.insert(bo.end(), bwd[k].begin(), bwd[k].end());
+                        eb.push_back(P.c_cap[k]);
+                    }
+                    D.sib_gf = up(fg);
+                    D.sib_gfo = up(fo);
+                    D.sib_gb = up(bg);
+                    D.sib_gbo = up(bo);
+                    auto tf = tiles_1d(ef, GF_ROWS), tb = tiles_1d(eb, GB_ROWS);
+                    D.sib_gf_tiles = up(tf);
+                    D.n_sib_gf_tiles = (int)tf.size();
+                    D.sib_gb_tiles = up(tb);
+                    D.n_sib_gb_tiles = (int)tb.size();
+                    for (int c0 : L.op_elim_llt) diag_h_.push_back(c0);
+                    for (int c0 : L.op_scale_llt) diag_h_.push_back(c0);
+                    for (int c0 : sibs) diag_h_.push_back(c0);
+                }
                 D.x_smem_ortho = mx * (int)sizeof(T);
                 const int64_t mr = (int64_t)mx * (MR_RB + 1) * (int64_t)sizeof(T);
                 D.ortho_mrhs_smem = mr <= 200 * 1024 ? (int)mr : 0;
@@ -2331,16 +2788,24 @@ class DeviceFactor : public DeviceFactorBase {
         }
         jpvt_ = alloc<int>(max_cols);
         ipvt_ = alloc<int>(max_cols);
-        if (lu_) {
+        if (lu_ || ldlt_) {
             lu_perm_ = alloc<int>(std::max<int64_t>(P.x_len, 1));
             lu_swp_ = alloc<int>(std::max<int64_t>(P.x_len, 1));
+        }
+        if (ldlt_) {
+            signs_ = alloc<T>(std::max<int64_t>(P.x_len, 1));
+            diag_ = up(diag_h_);
+            n_diag_ = (int)diag_h_.size();
+            int mx = 1;
+            for (int c0 : diag_h_) mx = std::max(mx, P.c_cap[c0]);
+            diag_smem_ = mx * (int)sizeof(T);
         }
         colcount_ = alloc<int>(max_items);
         d_xoff_ = up(std::vector<long long>(P.c_xoff.begin(), P.c_xoff.end()));
         xld_ = P.x_len;
         {
             std::vector<long long> slot(perm_h_.size());
-            for (int c0 = 0; c0 < nc_; c0++)
+            for (int c0 = 0; c0 < P.nclusters_h; c0++)
                 if (P.c_hlevel[c0] == 0)
                     for (int i = 0; i < P.c_cap[c0]; i++) slot[P.c_start[c0] + i] = P.c_xoff[c0] + i;
             d_slot_ = up(slot);
@@ -2350,6 +2815,10 @@ class DeviceFactor : public DeviceFactorBase {
         SPAND_CUDA(cudaFuncSetAttribute(potrf3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(trtri_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(trsm3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        if (ldlt_) {
+            SPAND_CUDA(cudaFuncSetAttribute(ldlt_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+            SPAND_CUDA(cudaFuncSetAttribute(perm_x_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        }
         if (lu_) {
             SPAND_CUDA(cudaFuncSetAttribute(getrf_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
             SPAND_CUDA(cudaFuncSetAttribute(lu_trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
@@ -2411,6 +2880,10 @@ class DeviceFactor : public DeviceFactorBase {
                     launch_getrf(D.elim_pivots, D.elim_inv, D.elim_clusters, D.n_elim, D.elim_lu_smem);
                     launch_lu_trsm(D.elim_trsm0);
                     launch_lu_trsm(D.elim_trsm1);
+                } else if (ldlt_) {
+                    launch_ldlt(D.elim_pivots, D.elim_clusters, nullptr, D.n_elim, D.elim_lu_smem);
+                    launch_trsm(D.elim_trsm0);
+                    launch_trsm(D.elim_trsm1);
                 } else {
                     launch_potrf(D.elim_pivots, D.elim_clusters, D.n_elim, D.elim_smem, D.elim_tri, D.elim_pc_cs,
                                  D.elim_pc_smem);
@@ -2420,7 +2893,7 @@ class DeviceFactor : public DeviceFactorBase {
                 if (D.n_schur_tiles)
                     launch("schur", [&] {
                         schur_kernel<T><<<D.n_schur_tiles, 256, 0, s_>>>(ctx_, D.schur_targets, d_ups_, D.schur_tiles,
-                                                                         D.n_schur_tiles);
+                                                                         D.n_schur_tiles, signs_, d_xoff_);
                     });
             }
             if (D.scaled && D.n_scale) {
@@ -2428,6 +2901,10 @@ class DeviceFactor : public DeviceFactorBase {
                     launch_getrf(D.scale_pivots, D.scale_inv, D.scale_clusters, D.n_scale, D.scale_lu_smem);
                     launch_lu_trsm(D.scale_trsm0);
                     launch_lu_trsm(D.scale_trsm1);
+                } else if (ldlt_) {
+                    launch_ldlt(D.scale_pivots, D.scale_clusters, D.scale_newpiv, D.n_scale, D.scale_lu_smem);
+                    launch_trsm(D.scale_trsm0);
+                    launch_trsm(D.scale_trsm1);
                 } else {
                     launch_potrf(D.scale_pivots, D.scale_clusters, D.n_scale, D.scale_smem, D.scale_tri,
                                  D.scale_pc_cs, D.scale_pc_smem);
@@ -2452,6 +2929,19 @@ class DeviceFactor : public DeviceFactorBase {
                     sparsify_scatter_kernel<T><<<dim3((unsigned)W.n, (unsigned)W.ytiles), 256, 0, s_>>>(
                         ctx_, W.items, pieces_, ws_, ipvt_, rank_, vstore_);
                 });
+                if (ldlt_) {
+                    launch("pivot_split", [&] {
+                        pivot_split_kernel<T><<<W.n, 256, 0, s_>>>(ctx_, W.items, W.sib, W.sib_piv, W.aso, W.piv,
+                                                                  vstore_, tauws_, signs_, d_xoff_);
+                    });
+                    launch_ldlt(W.sib_piv, W.sib, nullptr, W.n, W.ldlt_smem);
+                    launch_trsm(W.sib_trsm);
+                    if (W.n_sib_tiles)
+                        launch("schur", [&] {
+                            schur_kernel<T><<<W.n_sib_tiles, 256, 0, s_>>>(ctx_, W.sib_targets, W.sib_ups, W.sib_tiles,
+                                                                           W.n_sib_tiles, signs_, d_xoff_);
+                        });
+                }
                 // WY factors: on the side stream beside the next wave's QRCP (on the main
                 // stream when the profiler times every launch)
                 if (prof_.enabled()) {
@@ -2506,7 +2996,7 @@ class DeviceFactor : public DeviceFactorBase {
         const DStatus st = *h_status_;
         failed_cluster_ = st.not_spd - 1;
         if (st.not_spd)
-            throw DeviceError{SPAND_ERR_NOT_SPD, std::string(lu_ ? "Error: Singular Pivot" : "Error: Non-SPD Pivot") +
+            throw DeviceError{SPAND_ERR_NOT_SPD, std::string(lu_ || ldlt_ ? "Error: Singular Pivot" : "Error: Non-SPD Pivot") +
                                                      " (cluster " + std::to_string(st.not_spd - 1) + ")"};
         factored_ = true;
         if (!tuned_) tune_qrcp();
@@ -2562,8 +3052,10 @@ class DeviceFactor : public DeviceFactorBase {
             choose_potrf_cluster(ns, D.scale_smem, D.n_scale, D.scale_pc_cs, D.scale_pc_smem);
             D.elim_tri.smem = trtri_smem_n(ne);
             D.scale_tri.smem = trtri_smem_n(ns);
-            D.elim_trsm0.smem = D.elim_trsm1.smem = trsm_smem_n(ne);
-            D.scale_trsm0.smem = D.scale_trsm1.smem = trsm_smem_n(ns);
+            if (!ldlt_) {  // the LDLT panels always stage: keep their capacity-sized buffers
+                D.elim_trsm0.smem = D.elim_trsm1.smem = trsm_smem_n(ne);
+                D.scale_trsm0.smem = D.scale_trsm1.smem = trsm_smem_n(ns);
+            }
         }
         tuned_ = true;
     }
@@ -2654,6 +3146,16 @@ class DeviceFactor : public DeviceFactorBase {
         out.assign(tmp.begin(), tmp.end());
     }
 
+    void ldlt_signs(int cl, std::vector<double>& out) override {
+        std::vector<T> t(P_->c_cap[cl], T(0));
+        if (signs_ && !t.empty()) {
+            SPAND_CUDA(cudaMemcpyAsync(t.data(), signs_ + P_->c_xoff[cl], t.size() * sizeof(T), cudaMemcpyDeviceToHost,
+                                       s_));
+            SPAND_CUDA(cudaStreamSynchronize(s_));
+        }
+        out.assign(t.begin(), t.end());
+    }
+
     void lu_perm(int cl, std::vector<int>& out) override {
         out.assign(P_->c_cap[cl], 0);
         if (!lu_perm_ || out.empty()) return;
@@ -2705,6 +3207,14 @@ class DeviceFactor : public DeviceFactorBase {
         int gcs = 1;         // cluster of the global-memory QRCP (matrices the first does not hold)
         int gsmem = 0;       // its dynamic shared memory per CTA
         int ytiles = 0;      // scatter tiles per matrix (reflector + edge-block capacity tiles)
+        // LDLT: per item the sibling, its pivot, the edge block, the cluster's pivot; the
+        // sibling panels and the Schur update of the cluster's pivot
+        int *sib = nullptr, *sib_piv = nullptr, *aso = nullptr, *piv = nullptr;
+        TrsmDev sib_trsm;
+        DTarget* sib_targets = nullptr;
+        DUpd* sib_ups = nullptr;
+        DTile* sib_tiles = nullptr;
+        int n_sib_tiles = 0, ldlt_smem = 0;
         std::vector<SparsifyItem> host;  // plan items, for tuning
     };
     struct LevelDev {
@@ -2737,6 +3247,17 @@ class DeviceFactor : public DeviceFactorBase {
         int n_elim_llt = 0, n_scale_llt = 0;
         int *elim_inv = nullptr, *scale_inv = nullptr;  // PLU: inverse blocks, parallel to the pivots
         int elim_lu_smem = 0, scale_lu_smem = 0;
+        // LDLT: new sign pivots of the scaled clusters; siblings of the sparsified clusters
+        // (solve lists: their pivots, trsv tiles, GemmSymmIn groups forward by cluster and
+        // backward by sibling)
+        int* scale_newpiv = nullptr;
+        int n_sib = 0, n_sib_tv = 0, x_smem_sib = 0;
+        int *sib_clusters = nullptr, *sib_owner = nullptr, *sib_piv = nullptr;
+        int2* sib_tv = nullptr;
+        DGroup *sib_gf = nullptr, *sib_gb = nullptr;
+        DGemmOp *sib_gfo = nullptr, *sib_gbo = nullptr;
+        DTile *sib_gf_tiles = nullptr, *sib_gb_tiles = nullptr;
+        int n_sib_gf_tiles = 0, n_sib_gb_tiles = 0;
         int *elim_llt = nullptr, *elim_llt_blk = nullptr, *scale_llt = nullptr, *scale_llt_blk = nullptr;
         int x_smem_elim = 0, x_smem_scale = 0, x_smem_ortho = 0;
         DTile* gf_tiles32 = nullptr;  // forward Gemm groups in 32-row tiles (many right-hand sides)
@@ -3002,6 +3523,18 @@ class DeviceFactor : public DeviceFactorBase {
                                                           lu_perm_, lu_swp_, d_xoff_);
         });
     }
+    void launch_ldlt(int* pivots, int* clusters, int* newpiv, int n, int smem) {
+        if (!n) return;
+        launch("ldlt", [&] {
+            ldlt_kernel<T><<<n, LU_THREADS, smem, s_>>>(ctx_, pivots, clusters, newpiv, n, smem / (int)sizeof(T),
+                                                         lu_perm_, lu_swp_, signs_, d_xoff_);
+        });
+    }
+    static int lu_smem_n(int64_t mx) {
+        const int64_t full = (mx * mx + mx) * (int64_t)sizeof(T);
+        if (full <= 200 * 1024) return (int)full;
+        return (int)(mx * sizeof(T));
+    }
     void launch_lu_trsm(const TrsmDev& t) {
         if (!t.ntiles) return;
         launch("trsm", [&] {
@@ -3022,7 +3555,8 @@ class DeviceFactor : public DeviceFactorBase {
     void launch_trsm(const TrsmDev& t) {
         if (!t.ntiles) return;
         launch("trsm", [&] {
-            trsm3_kernel<T><<<t.ntiles, 256, t.smem, s_>>>(ctx_, t.items, t.tiles, t.ntiles, t.smem / (int)sizeof(T));
+            trsm3_kernel<T><<<t.ntiles, 256, t.smem, s_>>>(ctx_, t.items, t.tiles, t.ntiles, t.smem / (int)sizeof(T),
+                                                           ldlt_ ? lu_perm_ : nullptr, d_xoff_);
         });
     }
     // Cluster Cholesky for pivots of up to nmax rows that one CTA's shared memory cannot
@@ -3088,6 +3622,15 @@ class DeviceFactor : public DeviceFactorBase {
 
     void run_solve(double* x, int nrhs, int ld) { run_solve_slots(x, nrhs, ld, xs_, xs_ + (size_t)xld_ * x_nrhs_); }
 
+    // the Cholesky-layout triangular products on a list of LDLT pivots (siblings)
+    void trsv_ldlt(const int* clusters, const int* blks, const int2* tv, int ntv, int smem, int trans, XCtx<T> X,
+                   T* tmp) {
+        if (!ntv) return;
+        launch("trsv", [&] {
+            trsv4_kernel<T><<<ntv, TV_THREADS, smem, s_>>>(ctx_, X, clusters, blks, tv, trans, tmp, tv_count_);
+        });
+    }
+
     // slots: the solve vectors (xld x nrhs); tmp: their scratch copy, same layout
     void run_solve_slots(double* x, int nrhs, int ld, T* slots, T* tmp) {
         const Plan& P = *P_;
@@ -3095,7 +3638,44 @@ class DeviceFactor : public DeviceFactorBase {
         const int n = (int)perm_h_.size();
         const long long tot = (long long)n * nrhs;
         // 16 or more right-hand sides: the kernels that read each factor block once per 32
-        const bool mr = nrhs >= 16;
+        // (not on the LDLT path, whose sweeps carry signs and permutations)
+        const bool mr = nrhs >= 16 && !ldlt_;
+        const T* sg = ldlt_ ? signs_ : nullptr;
+        auto permx = [&](const int* clusters, int count, int fwd, int smem) {
+            if (!ldlt_ || !count) return;
+            launch("perm_x", [&] {
+                perm_x_kernel<T><<<dim3((unsigned)count, (unsigned)nrhs), 256, smem, s_>>>(ctx_, X, clusters, count,
+                                                                                         lu_perm_, d_xoff_, fwd);
+            });
+        };
+        auto siblings = [&](LevelDev& D, int fwd) {
+            if (!ldlt_ || !D.n_sib) return;
+            auto split = [&] {
+                launch("split_x", [&] {
+                    split_x_kernel<T><<<dim3((unsigned)D.n_sib, (unsigned)nrhs), 128, 0, s_>>>(
+                        ctx_, X, D.sib_owner, D.sib_clusters, D.n_sib, fwd);
+                });
+            };
+            if (fwd) {
+                split();
+                permx(D.sib_clusters, D.n_sib, 1, D.x_smem_sib);
+                trsv_ldlt(D.sib_clusters, D.sib_piv, D.sib_tv, D.n_sib_tv, D.x_smem_sib, 0, X, tmp);
+                if (D.n_sib_gf_tiles)
+                    launch("gemm_fwd", [&] {
+                        gemm_fwd2_kernel<T><<<D.n_sib_gf_tiles * nrhs, 256, 0, s_>>>(
+                            ctx_, X, D.sib_gf, D.sib_gfo, D.sib_gf_tiles, D.n_sib_gf_tiles, 0, signs_, d_xoff_, 1);
+                    });
+            } else {
+                if (D.n_sib_gb_tiles)
+                    launch("gemm_bwd", [&] {
+                        gemm_bwd2_kernel<T><<<D.n_sib_gb_tiles * nrhs, 256, 0, s_>>>(
+                            ctx_, X, D.sib_gb, D.sib_gbo, D.sib_gb_tiles, D.n_sib_gb_tiles, signs_, d_xoff_, 1);
+                    });
+                trsv_ldlt(D.sib_clusters, D.sib_piv, D.sib_tv, D.n_sib_tv, D.x_smem_sib, 1, X, tmp);
+                permx(D.sib_clusters, D.n_sib, 0, D.x_smem_sib);
+                split();
+            }
+        };
         launch("perm", [&] {
             perm_in_kernel<T><<<(unsigned)((tot + 255) / 256), 256, 0, s_>>>(x, ld, X, d_perm_, d_slot_, n);
         });
@@ -3142,6 +3722,7 @@ class DeviceFactor : public DeviceFactorBase {
             LevelDev& D = levels_[l];
             cur_level_ = l;
             cur_count_ = D.n_elim_llt;
+            permx(D.elim_llt, D.n_elim_llt, 1, D.x_smem_elim);
             trsv(D.elim_llt, lu_ ? D.elim_inv : D.elim_llt_blk, D.elim_tv, D.n_elim_tv, D.x_smem_elim, 0);
             if (D.n_gf)
                 launch("gemm_fwd", [&] {
@@ -3149,30 +3730,41 @@ class DeviceFactor : public DeviceFactorBase {
                         gemm_mrhs_kernel<T><<<D.n_gf_tiles32, 256, 0, s_>>>(ctx_, X, D.gf, D.gfo, D.gf_tiles32, 1);
                     else
                         gemm_fwd2_kernel<T><<<D.n_gf_tiles * nrhs, 256, 0, s_>>>(ctx_, X, D.gf, D.gfo, D.gf_tiles,
-                                                                                 D.n_gf_tiles, 0);
+                                                                                 D.n_gf_tiles, 0, sg, d_xoff_);
                 });
             cur_count_ = D.n_scale_llt;
+            permx(D.scale_llt, D.n_scale_llt, 1, D.x_smem_scale);
             trsv(D.scale_llt, lu_ ? D.scale_inv : D.scale_llt_blk, D.scale_tv, D.n_scale_tv, D.x_smem_scale, 0);
             ortho(D, 1);
+            siblings(D, 1);
             merge(D, 1);
         }
+        cur_level_ = -1;
+        if (ldlt_ && n_diag_)  // the diag phase (tree.cpp:1621-1624)
+            launch("sign_x", [&] {
+                sign_x_kernel<T><<<dim3((unsigned)n_diag_, (unsigned)nrhs), 128, 0, s_>>>(ctx_, X, diag_, n_diag_, signs_,
+                                                                                       d_xoff_);
+            });
         for (int l = P.nlevels - 1; l >= 0; l--) {
             LevelDev& D = levels_[l];
             cur_level_ = l;
             merge(D, 0);
+            siblings(D, 0);
             ortho(D, 0);
             cur_count_ = D.n_scale_llt;
             trsv(D.scale_llt, lu_ ? D.scale_inv : D.scale_llt_blk, D.scale_tv, D.n_scale_tv, D.x_smem_scale, 1);
+            permx(D.scale_llt, D.n_scale_llt, 0, D.x_smem_scale);
             if (D.n_gb)
                 launch("gemm_bwd", [&] {
                     if (mr)
                         gemm_mrhs_kernel<T><<<D.n_gb_tiles, 256, 0, s_>>>(ctx_, X, D.gb, D.gbo, D.gb_tiles, 0);
                     else
                         gemm_bwd2_kernel<T><<<D.n_gb_tiles * nrhs, 256, 0, s_>>>(ctx_, X, D.gb, D.gbo, D.gb_tiles,
-                                                                                 D.n_gb_tiles);
+                                                                                 D.n_gb_tiles, sg, d_xoff_);
                 });
             cur_count_ = D.n_elim_llt;
             trsv(D.elim_llt, lu_ ? D.elim_inv : D.elim_llt_blk, D.elim_tv, D.n_elim_tv, D.x_smem_elim, 1);
+            permx(D.elim_llt, D.n_elim_llt, 0, D.x_smem_elim);
         }
         cur_level_ = -1;
         launch("perm", [&] {
@@ -3210,6 +3802,11 @@ class DeviceFactor : public DeviceFactorBase {
     int* lu_perm_ = nullptr;      // per cluster at its solve-slot offset: row permutation of its pivot
     int* lu_swp_ = nullptr;       // and the row interchanges that make it
     int cur_count_ = 0;           // clusters of the pivot op list being applied in the solve
+    bool ldlt_ = false;           // LDLT path (symmetric indefinite)
+    T* signs_ = nullptr;          // LDLT: sign(D) of every factored pivot at the cluster's offset
+    std::vector<int> diag_h_;     // LDLT: clusters of every ScalingLDLT op (the diag phase)
+    int* diag_ = nullptr;
+    int n_diag_ = 0, diag_smem_ = 0;
     bool tuned_ = false;
     int cur_level_ = -1;
     // in-kernel phase timing of the QRCP of one level (SPAND_QC_PROBE=<level>)

@@ -272,7 +272,9 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, cons
             tu = 0;
             sc = 0;
         } else {
-            beta = -copysign(hypot(alpha, xnorm), alpha);
+            // -sign(alpha) |(alpha, x)| with sign(-0) = +1 (the oracle's rule: a zero leading
+            // entry counts as positive whatever sign bit rounding left on it)
+            beta = alpha >= T(0) ? -hypot(alpha, xnorm) : hypot(alpha, xnorm);
             tu = (beta - alpha) / beta;
             sc = T(1) / (alpha - beta);
         }

@@ -110,8 +110,10 @@ std::vector<ClusterID> Tree::partition(const Csc& A) {
 void Tree::assemble(const Csc& A) {
     if (!partitioned_) throw std::logic_error("assemble() before partition()");
     const bool lu = symm_ == SymmKind::GEN;
-    if (!((symm_ == SymmKind::SPD && scaling_ == ScalingKind::LLT) || (lu && scaling_ == ScalingKind::PLU)))
-        throw std::invalid_argument("the device path implements the SPD / LLT and GEN / PLU configurations");
+    const bool ldlt = symm_ == SymmKind::SYM;
+    if (!((symm_ == SymmKind::SPD && scaling_ == ScalingKind::LLT) || (lu && scaling_ == ScalingKind::PLU) ||
+          (ldlt && scaling_ == ScalingKind::LDLT)))
+        throw std::invalid_argument("the device path implements the SPD / LLT, SYM / LDLT and GEN / PLU configurations");
     if (A.n != get_N()) throw std::invalid_argument("matrix size does not match the partition");
     if ((int64_t)A.val.size() != (int64_t)A.rowval.size()) throw std::invalid_argument("values do not match the pattern");
     double t0 = now_s();
@@ -120,7 +122,7 @@ void Tree::assemble(const Csc& A) {
         A_ = A;
         Csc App = spand::symm_perm(A, perm_);
         asmb_ = spand::assembly_structure(H_, App, !lu);
-        plan_ = spand::build_plan(H_, asmb_, skip_, use_want_sparsify_, lu);
+        plan_ = spand::build_plan(H_, asmb_, skip_, use_want_sparsify_, lu, ldlt);
         std::vector<int64_t> amap = spand::assembly_map(plan_, H_, asmb_, A, perm_);
         if (!stream_) cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
         dev_ = spand::make_device_factor(fp32_, stream_, perm_);
@@ -303,16 +305,17 @@ void Tree::build_ops_and_log() {
         G = fresh;
     }
     const spand::Plan& P = plan_;
-    int next_order = P.nclusters;  // siblings are numbered after all clusters
+    int next_order = P.nclusters_h;  // siblings are numbered after all clusters
     long long nnz = 0;
-    // pivot ops: ScalingLLT (0), or ScalingPLUQ (8) on the general path
-    const int kpiv = P.lu ? 8 : 0;
+    // pivot ops: ScalingLLT (0), ScalingPLUQ (8) on the general path, ScalingLDLT (9)
+    const int kpiv = P.lu ? 8 : P.ldlt ? 9 : 0;
     auto push = [&](OpRecord r) {
         switch (r.kind) {  // Operation::nnz (operations.h:32-163)
             case 0: nnz += (long long)r.ns * (r.ns + 1) / 2; break;
             case 1: case 2: case 6: case 7: nnz += (long long)r.ns * r.nn; break;
             case 3: nnz += (long long)r.ns * r.ns; break;
             case 8: nnz += (long long)r.ns * r.ns + 2LL * r.ns; break;
+            case 9: nnz += (long long)r.ns * (r.ns + 1) / 2 + 2LL * r.ns; break;
             default: break;
         }
         ops_.push_back(r);
@@ -323,7 +326,7 @@ void Tree::build_ops_and_log() {
         size_t g = 0;
         for (size_t k = 0; k < L.op_elim_llt.size(); k++) {
             int s = L.op_elim_llt[k];
-            push({kpiv, l, s, -1, rows0_[s], 0, rows0_[s], rows0_[s], L.op_elim_llt_block[k]});
+            push({kpiv, l, s, -1, rows0_[s], 0, rows0_[s], rows0_[s], L.op_elim_llt_block[k], s});
             while (g < L.op_gemm.size() && L.op_gemm[g].self == s) {
                 const spand::GemmOpItem& it = L.op_gemm[g];
                 int ns = rows0_[s], nn = rows0_[it.nbr];
@@ -338,7 +341,7 @@ void Tree::build_ops_and_log() {
         G.dofs_left_elim = left_elim;
         for (size_t k = 0; k < L.op_scale_llt.size(); k++) {
             int c = L.op_scale_llt[k];
-            push({kpiv, l, c, -1, rows0_[c], 0, rows0_[c], rows0_[c], L.op_scale_llt_block[k]});
+            push({kpiv, l, c, -1, rows0_[c], 0, rows0_[c], rows0_[c], L.op_scale_llt_block[k], c});
         }
         // wave index of every sparsified cluster of this level, for the Asn widths
         std::vector<int> wave_of;
@@ -368,7 +371,13 @@ void Tree::build_ops_and_log() {
                 push({3, l, c, -1, rows, 0, rows, k, c});
                 int sib = next_order++;
                 push({5, l, c, sib, k, rows - k, 0, 0, -1});
-                push({kpiv, l, sib, -1, rows - k, 0, rows - k, rows - k, -1});
+                if (P.ldlt) {
+                    // the sibling's pivot and its edge to the cluster (tree.cpp:1340-1341)
+                    push({9, l, sib, -1, rows - k, 0, rows - k, rows - k, item->sib_piv, item->sib});
+                    push({2, l, sib, c, rows - k, k, rows - k, k, item->aso, item->sib});
+                } else {
+                    push({kpiv, l, sib, -1, rows - k, 0, rows - k, rows - k, -1});
+                }
             }
         }
         G.ignored = L.ignored;
@@ -409,7 +418,7 @@ std::vector<std::array<int, 4>> Tree::ranks() const {
 void Tree::op_matrix(int idx, std::vector<double>& out) const {
     const OpRecord& r = ops_.at(idx);
     out.clear();
-    if (r.kind == 0 || r.kind == 1 || r.kind == 2 || r.kind == 6 || r.kind == 7 || r.kind == 8) {
+    if (r.kind == 0 || r.kind == 1 || r.kind == 2 || (r.kind >= 6 && r.kind <= 9)) {
         if (r.block < 0) {  // sibling identity
             out.assign((size_t)r.rows * r.cols, 0.0);
             for (int i = 0; i < r.rows; i++) out[i + (size_t)i * r.rows] = 1.0;
@@ -434,13 +443,21 @@ void Tree::op_matrix(int idx, std::vector<double>& out) const {
 void Tree::op_perm(int idx, std::vector<int>& out) const {
     const OpRecord& r = ops_.at(idx);
     out.clear();
-    if (r.kind != 8) return;
+    if (r.kind != 8 && r.kind != 9) return;
     if (r.block < 0) {  // sibling: identity
         out.resize(r.ns);
         for (int i = 0; i < r.ns; i++) out[i] = i;
         return;
     }
-    dev_->lu_perm(r.self, out);
+    dev_->lu_perm(r.cl, out);
+    out.resize(r.ns);
+}
+
+void Tree::op_signs(int idx, std::vector<double>& out) const {
+    const OpRecord& r = ops_.at(idx);
+    out.clear();
+    if (r.kind != 9) return;
+    dev_->ldlt_signs(r.cl, out);
     out.resize(r.ns);
 }
 

@@ -37,10 +37,11 @@ struct LevelLog {
 // (operations.h:32-163): kind 0 ScalingLLT, 1 GemmSymmOut, 2 GemmSymmIn, 3 Orthogonal,
 // 4 Merge, 5 Split, 6 GemmOut, 7 GemmIn, 8 ScalingPLUQ (the last three on the GEN / PLU
 // path; the matrix of a ScalingPLUQ is its pivot block: L_s below the diagonal, U_s on and
-// above it).
+// above it), 9 ScalingLDLT (SYM / LDLT path; L_s in the lower triangle of its block).
 struct OpRecord {
     int kind, level, self, nbr, ns, nn, rows, cols;
-    int block;  // device block (ScalingLLT / Gemm), or sparsified cluster (Orthogonal), or -1
+    int block;    // device block (ScalingLLT / Gemm), or sparsified cluster (Orthogonal), or -1
+    int cl = -1;  // device cluster of self (pivot ops: where its permutation and signs live)
 };
 
 class Tree {
@@ -91,8 +92,10 @@ class Tree {
     const std::vector<OpRecord>& ops() const { ensure_log(); return ops_; }
     void op_matrix(int idx, std::vector<double>& out) const;
     void op_tau(int idx, std::vector<double>& out) const;
-    // row permutation p of a ScalingPLUQ op (x_s <- x_s[p] before L_s^{-1})
+    // row permutation p of a ScalingPLUQ / ScalingLDLT op (x_s <- x_s[p] before L_s^{-1})
     void op_perm(int idx, std::vector<int>& out) const;
+    // sign(D) of a ScalingLDLT op
+    void op_signs(int idx, std::vector<double>& out) const;
     double t_partition = 0, t_assemble = 0, t_factorize = 0;
     int64_t launches() const { return dev_ ? dev_->launches() : 0; }
     void reset_launches() { if (dev_) dev_->reset_launches(); }
