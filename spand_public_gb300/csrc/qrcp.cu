@@ -67,6 +67,7 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, cons
     __shared__ T red[32];
     __shared__ T pubm[2][QC_SLOTS];  // per warp of the cluster: largest partial norm
     __shared__ int pubf[2][QC_SLOTS];  // first position inside its tie window
+    __shared__ T pubn[2][QC_SLOTS];    // the partial norm at that position
     __shared__ int pubx[2][QC_SLOTS];  // exact search with the global threshold
     __shared__ T s_alpha;
     if (c.status->not_spd) return;
@@ -165,15 +166,28 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, cons
         const T m = warp_max(mlane);
         const T thr = m * tie;
         int f = INT_MAX;
+        T fn = 0;
         if (gl == 0)
             for (int j = gid; j < nloc; j += ngroups) {
                 const int p = pos[j];
-                if (p >= from && vn1[j] >= thr && p < f) f = p;
+                if (p >= from && vn1[j] >= thr && p < f) {
+                    f = p;
+                    fn = vn1[j];
+                }
             }
-        f = warp_min(f);
+        // first position with its norm (the norm rides along the minimum)
+        for (int o = 16; o > 0; o >>= 1) {
+            const int of = __shfl_xor_sync(0xffffffffu, f, o);
+            const T on = __shfl_xor_sync(0xffffffffu, fn, o);
+            if (of < f) {
+                f = of;
+                fn = on;
+            }
+        }
         if (lane < CS) {
             *cl.map_shared_rank(&pubm[par][slot], lane) = m;
             *cl.map_shared_rank(&pubf[par][slot], lane) = f;
+            *cl.map_shared_rank(&pubn[par][slot], lane) = fn;
         }
     };
 
@@ -211,10 +225,13 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, cons
         const T thr = gmax * tie;
         int pvt = INT_MAX;
         bool amb = false;
+        // a warp whose maximum reaches the global window published the first position of
+        // its own (wider or equal) window; where that column also reaches the global
+        // threshold it is the warp's first candidate, else the warp must search again
         for (int e = lane; e < E; e += 32) {
             const T m = pubm[par][e];
             if (m >= thr) {
-                if (m == gmax) pvt = min(pvt, pubf[par][e]);
+                if (pubn[par][e] >= thr) pvt = min(pvt, pubf[par][e]);
                 else amb = true;
             }
         }
