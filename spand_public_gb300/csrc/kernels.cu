@@ -1997,15 +1997,16 @@ __global__ void __launch_bounds__(256) trsv_mrhs_kernel(Ctx<T> c, XCtx<T> X, con
         if (!trans) mr_accum(acc, L, ld, false, r0, nr, 0, r1, 1, xcol, X.xld, nrb, xs, fs);
         else mr_accum(acc, L, ld, true, r0, nr, r0 + 1, n, 2, xcol, X.xld, nrb, xs, fs);
         T* ycol = (nt == 1 ? X.xs : tmp) + X.xoff[cl] + (size_t)rb0 * X.xld;
-        if (lane < nrb)
+        // through the (free) factor tile, so that consecutive threads write consecutive rows
 #pragma unroll
-            for (int u = 0; u < MR_U; u++) {
-                const int row = r0 + w + 8 * u;
-                if (w + 8 * u < nr) {
-                    const size_t o = row + (size_t)lane * X.xld;
-                    ycol[o] = acc[u] + xcol[o] / L[row + (size_t)row * ld];
-                }
-            }
+        for (int u = 0; u < MR_U; u++)
+            if (w + 8 * u < nr) fs[w + 8 * u][lane] = acc[u];
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < nr * nrb; idx += blockDim.x) {
+            const int i = idx % nr, j = idx / nr, row = r0 + i;
+            const size_t o = row + (size_t)j * X.xld;
+            ycol[o] = fs[i][j] + xcol[o] / L[row + (size_t)row * ld];
+        }
         __syncthreads();
     }
     if (nt == 1) return;
@@ -2056,10 +2057,16 @@ __global__ void __launch_bounds__(256) gemm_mrhs_kernel(Ctx<T> c, XCtx<T> X, con
             mr_accum(acc, bptr(c, op.block), c.blk[op.block].ld, row_fast, i0, nr, 0, nj, 0, xcol, X.xld, nrb, xs,
                      fs);
         }
-        if (lane < nrb)
+        // through the (free) factor tile, so that consecutive threads update consecutive rows
 #pragma unroll
-            for (int u = 0; u < MR_U; u++)
-                if (w + 8 * u < nr) ycol0[(i0 + w + 8 * u) + (size_t)(rb0 + lane) * X.xld] -= acc[u];
+        for (int u = 0; u < MR_U; u++)
+            if (w + 8 * u < nr) fs[w + 8 * u][lane] = acc[u];
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < nr * nrb; idx += blockDim.x) {
+            const int i = idx % nr, j = idx / nr;
+            ycol0[(i0 + i) + (size_t)(rb0 + j) * X.xld] -= fs[i][j];
+        }
+        __syncthreads();
     }
 }
 
