@@ -2024,6 +2024,73 @@ __global__ void __launch_bounds__(256) trsv_mrhs_kernel(Ctx<T> c, XCtx<T> X, con
     if (threadIdx.x == 0) counters[cl] = 0;
 }
 
+// Triangular products for many right-hand sides on clusters of at most MR_MAXROWS rows:
+// one WARP per (cluster, block of 32 right-hand sides), eight per CTA, no CTA barrier.
+// The warp stages its x tile (rows x 32) in shared memory with row-contiguous loads, each
+// lane forms its right-hand side's products with broadcast loads of L^{-1} (in place, rows
+// in the order that leaves every needed original entry unread-over), and the tile goes back
+// with row-contiguous stores.  The thousands of 10-60-row clusters of the lower levels
+// were CTA-latency-bound in trsv_mrhs_kernel.
+constexpr int MRS_WARPS = 8;
+
+template <typename T>
+__global__ void __launch_bounds__(32 * MRS_WARPS) trsv_mrhs_small_kernel(Ctx<T> c, XCtx<T> X,
+                                                                        const int* __restrict__ clusters,
+                                                                        const int* __restrict__ lblocks,
+                                                                        const int* __restrict__ idx, int count,
+                                                                        int trans) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    T (*xs)[MR_RB + 1] = reinterpret_cast<T (*)[MR_RB + 1]>(smem_raw) + (size_t)w * MR_MAXROWS;
+    const int nrbk = (X.nrhs + MR_RB - 1) / MR_RB;
+    const int pair = blockIdx.x * MRS_WARPS + w;
+    if (pair >= count * nrbk) return;
+    const int k = idx[pair / nrbk], rb0 = (pair % nrbk) * MR_RB;
+    const int cl = clusters[k];
+    const int n = c.rows0[cl];
+    if (n == 0) return;
+    const int nrb = min(MR_RB, X.nrhs - rb0);
+    const T* L = bptr(c, lblocks[k]);
+    const int ld = c.blk[lblocks[k]].ld;
+    T* xcol = X.xs + X.xoff[cl] + (size_t)rb0 * X.xld;
+    for (int j = 0; j < nrb; j++)
+        for (int i = lane; i < n; i += 32) xs[i][j] = xcol[i + (size_t)j * X.xld];
+    __syncwarp();
+    if (lane < nrb) {
+        if (!trans) {
+            // y_i = x_i / L_ii + sum_{k<i} L^{-1}[i][k] x_k, L^{-1}[i][k] at L[k + i ld]; rows from
+            // the last, so every x_k (k < i) is still the original
+            for (int i = n - 1; i >= 0; i--) {
+                const T* li = L + (size_t)i * ld;
+                T s0 = xs[i][lane] / li[i], s1 = 0;
+                int q = 0;
+                for (; q + 1 < i; q += 2) {
+                    s0 += li[q] * xs[q][lane];
+                    s1 += li[q + 1] * xs[q + 1][lane];
+                }
+                for (; q < i; q++) s0 += li[q] * xs[q][lane];
+                xs[i][lane] = s0 + s1;
+            }
+        } else {
+            // y_i = x_i / L_ii + sum_{k>i} L^{-1}[k][i] x_k, L^{-1}[k][i] at L[i + k ld]; rows from
+            // the first
+            for (int i = 0; i < n; i++) {
+                T s0 = xs[i][lane] / L[i + (size_t)i * ld], s1 = 0;
+                int q = i + 1;
+                for (; q + 1 < n; q += 2) {
+                    s0 += L[i + (size_t)q * ld] * xs[q][lane];
+                    s1 += L[i + (size_t)(q + 1) * ld] * xs[q + 1][lane];
+                }
+                for (; q < n; q++) s0 += L[i + (size_t)q * ld] * xs[q][lane];
+                xs[i][lane] = s0 + s1;
+            }
+        }
+    }
+    __syncwarp();
+    for (int j = 0; j < nrb; j++)
+        for (int i = lane; i < n; i += 32) xcol[i + (size_t)j * X.xld] = xs[i][j];
+}
+
 // Gemm sweeps (as gemm_fwd2 / gemm_bwd2) for many right-hand sides: one CTA per (group,
 // 32 rows of the updated slot), ops of the group in order, all right-hand-side blocks.
 // fwd: x_n -= A_ns x_s (kind 1, A[i + j*ld]) or A_sn^T x_s (kind 2, A[j + i*ld]);
@@ -2675,6 +2742,27 @@ class DeviceFactor : public DeviceFactorBase {
                 };
                 D.elim_tv = tv(L.op_elim_llt, D.n_elim_tv);
                 D.scale_tv = tv(L.op_scale_llt, D.n_scale_tv);
+                // many right-hand sides: clusters of at most MR_MAXROWS rows go to the warp
+                // kernel, the others keep the row tiles
+                auto split = [&](const std::vector<int>& cl, int*& small, int& nsmall, int2*& big, int& nbig) {
+                    std::vector<int> s;
+                    std::vector<int2> t;
+                    for (size_t k = 0; k < cl.size(); k++) {
+                        const int cap = P.c_cap[cl[k]];
+                        if (cap <= MR_MAXROWS) {
+                            s.push_back((int)k);
+                            continue;
+                        }
+                        const int nt = (cap + TV_ROWS - 1) / TV_ROWS;
+                        for (int q = 0; q < nt; q++) t.push_back(make_int2((int)k, q));
+                    }
+                    nsmall = (int)s.size();
+                    small = up(s);
+                    nbig = (int)t.size();
+                    big = up(t);
+                };
+                split(L.op_elim_llt, D.elim_small, D.n_elim_small, D.elim_big_tv, D.n_elim_big_tv);
+                split(L.op_scale_llt, D.scale_small, D.n_scale_small, D.scale_big_tv, D.n_scale_big_tv);
             }
             {
                 // Gemm ops grouped: forward by neighbour in op order, backward by
@@ -2834,6 +2922,8 @@ class DeviceFactor : public DeviceFactorBase {
         fallback_ = alloc<int>(max_items);
         SPAND_CUDA(cudaFuncSetAttribute(trsv4_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(ortho_mrhs_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SPAND_CUDA(cudaFuncSetAttribute(trsv_mrhs_small_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        MRS_WARPS * MR_MAXROWS * (MR_RB + 1) * (int)sizeof(T)));
         tv_count_ = alloc<int>(nc_);
         {
             int mx = 1;
@@ -3252,6 +3342,12 @@ class DeviceFactor : public DeviceFactorBase {
         DTile* merge_tiles = nullptr;
         int n_merge_tiles = 0;
         int n_elim_llt = 0, n_scale_llt = 0;
+        // many right-hand sides: small clusters (indices into the op lists) and the row tiles
+        // of the others
+        int *elim_small = nullptr, *scale_small = nullptr;
+        int n_elim_small = 0, n_scale_small = 0;
+        int2 *elim_big_tv = nullptr, *scale_big_tv = nullptr;
+        int n_elim_big_tv = 0, n_scale_big_tv = 0;
         int *elim_inv = nullptr, *scale_inv = nullptr;  // PLU: inverse blocks, parallel to the pivots
         int elim_lu_smem = 0, scale_lu_smem = 0;
         // LDLT: new sign pivots of the scaled clusters; siblings of the sparsified clusters
@@ -3686,8 +3782,30 @@ class DeviceFactor : public DeviceFactorBase {
         launch("perm", [&] {
             perm_in_kernel<T><<<(unsigned)((tot + 255) / 256), 256, 0, s_>>>(x, ld, X, d_perm_, d_slot_, n);
         });
+        auto trsv_mr = [&](const int* clusters, const int* blks, const int* small, int nsmall, const int2* big, int nbig,
+                           int trans) {
+            const int nrbk = (nrhs + MR_RB - 1) / MR_RB;
+            if (nsmall)
+                launch("trsv", [&] {
+                    const unsigned g = (unsigned)((nsmall * nrbk + MRS_WARPS - 1) / MRS_WARPS);
+                    trsv_mrhs_small_kernel<T><<<g, 32 * MRS_WARPS, MRS_WARPS * MR_MAXROWS * (MR_RB + 1) * sizeof(T), s_>>>(
+                        ctx_, X, clusters, blks, small, nsmall, trans);
+                });
+            if (nbig)
+                launch("trsv", [&] {
+                    trsv_mrhs_kernel<T><<<nbig, 256, 0, s_>>>(ctx_, X, clusters, blks, big, trans, tmp, tv_count_);
+                });
+        };
         auto trsv = [&](const int* clusters, const int* blks, const int2* tv, int ntv, int smem, int trans) {
             if (!ntv) return;
+            if (mr && !lu_) {
+                const LevelDev& D = levels_[cur_level_];
+                if (clusters == D.elim_llt)
+                    trsv_mr(clusters, blks, D.elim_small, D.n_elim_small, D.elim_big_tv, D.n_elim_big_tv, trans);
+                else
+                    trsv_mr(clusters, blks, D.scale_small, D.n_scale_small, D.scale_big_tv, D.n_scale_big_tv, trans);
+                return;
+            }
             if (lu_) {
                 // PLU: blks are the inverse blocks; one CTA per (cluster, right-hand side)
                 const int count = cur_count_;
