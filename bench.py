@@ -32,6 +32,7 @@ METRIC = "factor+PCG seconds to 1e-10 FP64 rel. residual (3D 7-pt Laplacian 64^3
 
 
 PROBLEMS = {
+    "lap2d": "2D 5-pt Laplacian {n}^2",
     "lap3d": "3D 7-pt Laplacian {n}^3",
     "fv2d": "2D 5-pt finite-volume diffusion {n}^2, coefficients 10^U(-3,3) on 8x8 tiles",
     "aniso3d": "3D anisotropic diffusion {n}^3, face conductivities exp(0.5 z), axis scaling (1,1,0.01)",
@@ -75,6 +76,8 @@ def workload(args):
 
     if args.problem == "lap3d":
         A, X = P.neglapl(args.n, 3), P.linspace_nd(args.n, 3)
+    elif args.problem == "lap2d":
+        A, X = P.neglapl(args.n, 2), P.linspace_nd(args.n, 2)
     elif args.problem == "fv2d":
         A, X = P.high_contrast_fv2d(args.n, 8, seed=0), P.linspace_nd(args.n, 2)
     else:
@@ -84,7 +87,7 @@ def workload(args):
 
 
 def config(args, extra=None):
-    dim = 2 if args.problem == "fv2d" else 3
+    dim = 2 if args.problem in ("fv2d", "lap2d") else 3
     c = {"workload": f"{PROBLEMS[args.problem].format(n=args.n)} (n={args.n ** dim}), {args.levels} ND levels, "
                      f"eps={args.eps:g}, {args.nrhs} RHS N(0,1) seed 0, PCG to {args.tol:g}",
          "problem": args.problem, "grid": args.n, "levels": args.levels, "eps": args.eps, "nrhs": args.nrhs, "pcg_tol": args.tol,
@@ -359,7 +362,7 @@ def run_gb300(args, rank, world, local_rank):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         f_c, g_c, it_c, rel_c = cpu_oracle_solve(A, X, b, args)
         cpu = {"value": f_c + k * g_c, "unit": "s", "cores": 1, "kind": "port",
-               "sample": f"one factorization + the CG of the first right-hand side of the same {args.n}^3 problem "
+               "sample": f"one factorization + the CG of the first right-hand side of the same {PROBLEMS[args.problem].format(n=args.n)} problem "
                          f"by the oracle (C++ restatement of the reference, one thread; CG time x {k} RHS): "
                          f"{it_c} CG iterations, true relres {rel_c:.2e}"}
 
