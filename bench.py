@@ -383,12 +383,26 @@ def run_gb300(args, rank, world, local_rank):
     return 0
 
 
-def batch_workload(args):
+def max_over_ranks(value, device=None):
+    """The largest of a per-rank number over the process group (the number itself without
+    one): the whole-job time of replicas or shards is the slowest rank's."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()):
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def batch_workload(args, rank=0):
     """args.systems systems -Laplacian + cI on m^3 grids, m ~ U{16..40}, c ~ U(0,1), one
-    N(0,1) right-hand side each, ceil(log2(m^3/64)) levels; generator seeded with 0."""
+    N(0,1) right-hand side each, ceil(log2(m^3/64)) levels; generator seeded with the rank
+    (rank r of N takes its own args.systems systems: weak scaling, no data exchange)."""
     from spand_public_gb300 import problems as P
 
-    rng = np.random.default_rng(0)
+    rng = np.random.default_rng(rank)
     out = []
     for _ in range(args.systems):
         m = int(rng.integers(16, 41))
@@ -405,7 +419,11 @@ def run_batch(args, rank, world, local_rank):
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    systems = batch_workload(args)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    systems = batch_workload(args, rank)
 
     def trees(fp32):
         out = []
@@ -442,13 +460,15 @@ def run_batch(args, rank, world, local_rank):
 
     for _ in range(args.warmup):
         step(F32)
+    if world > 1:
+        torch.distributed.barrier()
     F32.launches(reset=True)
     clocks = ClockSampler(local_rank)
     clocks.start()
     res = [step(F32) for _ in range(args.steps)]
     clk = clocks.stop()
     launches = F32.launches(reset=True) / max(args.steps, 1)
-    value = float(np.mean([f + g for f, g, _, _ in res]))
+    value = max_over_ranks(float(np.mean([f + g for f, g, _, _ in res])), dev)
     its = res[-1][2]
     xs = F32.split(xd.cpu().numpy())
     true_rel = max(float(np.linalg.norm(A @ x - b) / np.linalg.norm(b)) for (m, A, X, levels, b), x in zip(systems, xs))
@@ -488,7 +508,7 @@ def run_batch(args, rank, world, local_rank):
     e2e = {"value": float(np.mean(e2e_t)), "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
            "pcg_iterations_max": int(its_h.max())}
     cpu = None
-    if not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle.oracle import OracleTree
 
         sample = systems[:8]
@@ -524,11 +544,16 @@ def run_batch(args, rank, world, local_rank):
                        "timing": "host wall clock between device-wide synchronisations",
                        "precision": "FP32 factor (SIMT), FP64 CG/SpMV/dots", "parallelism": "1 GPU"},
             "e2e": e2e, "gpu_launches": int(round(launches)), "roofline": None, "cpu_baseline": cpu, "clocks": clk}
+    if world > 1:
+        line["config"]["systems_all_ranks"] = args.systems * world
+        line["config"]["sharding"] = "each rank factors and solves its own systems (seeded by rank); no collective"
     if rank == 0:
         print(json.dumps(line), flush=True)
     F32.close()
     for t in T32:
         t.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
     return 0
 
 
