@@ -3055,7 +3055,7 @@ class DeviceFactor : public DeviceFactorBase {
                     side_used = true;
                 }
             }
-            if (D.merged) {
+            if (D.merged && D.n_parents) {
                 launch("merge_sizes", [&] {
                     merge_sizes_kernel<<<(D.n_parents + 127) / 128, 128, 0, s_>>>(csize_, rows0_, cpos_, D.parents,
                                                                                     D.n_parents, D.child_ptr,
@@ -3400,6 +3400,11 @@ class DeviceFactor : public DeviceFactorBase {
             prof_.begin(s_, cls);
         }
         f();
+        if (check_launches_) {  // SPAND_CHECK_LAUNCHES=1: name the launch that failed
+            const cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess)
+                throw DeviceError{SPAND_ERR_CUDA, std::string(cls) + ": " + cudaGetErrorString(e)};
+        }
         prof_.end(s_);
         launches_ += kernels;
     }
@@ -3927,6 +3932,7 @@ class DeviceFactor : public DeviceFactorBase {
     int* lu_perm_ = nullptr;      // per cluster at its solve-slot offset: row permutation of its pivot
     int* lu_swp_ = nullptr;       // and the row interchanges that make it
     int cur_count_ = 0;           // clusters of the pivot op list being applied in the solve
+    bool check_launches_ = getenv("SPAND_CHECK_LAUNCHES") != nullptr;
     bool ldlt_ = false;           // LDLT path (symmetric indefinite)
     T* signs_ = nullptr;          // LDLT: sign(D) of every factored pivot at the cluster's offset
     std::vector<int> diag_h_;     // LDLT: clusters of every ScalingLDLT op (the diag phase)
