@@ -63,6 +63,7 @@ def lib():
             "orc_gmres": (I, [P, pd, pd, I, I, D, pd]),
             "orc_get_op_u": (C.c_longlong, [P, I, pd]), "orc_get_op_perm": (I, [P, I, pi]),
             "orc_get_op_signs": (I, [P, I, pd]),
+            "orc_set_preserve": (None, [P, I]), "orc_set_phi": (None, [P, pd, I, I]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -106,6 +107,12 @@ class OracleTree:
     def set_symm_kind(self, k): self.L.orc_set_symm_kind(self.h, int(k))
     def set_scaling_kind(self, k): self.L.orc_set_scaling_kind(self.h, int(k))
     def set_use_sparsify(self, u): self.L.orc_set_use_sparsify(self.h, int(bool(u)))
+    def set_preserve(self, on): self.L.orc_set_preserve(self.h, int(bool(on)))
+
+    def set_phi(self, phi):
+        """Vectors to preserve (tree.h:141): N x nphi, natural ordering (copied)."""
+        phi = np.asfortranarray(np.atleast_2d(np.asarray(phi, dtype=np.float64).T).T)
+        self.L.orc_set_phi(self.h, _dp(phi), phi.shape[0], phi.shape[1])
 
     def set_Xcoo(self, X):
         X = np.asfortranarray(X, dtype=np.float64)

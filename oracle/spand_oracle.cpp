@@ -376,6 +376,67 @@ static void ormqr_vec(const Mat& v, const std::vector<double>& h, int k, double*
     else for (int i = k - 1; i >= 0; i--) apply(i);
 }
 
+// Householder QR without pivoting (dgeqrf -> dgeqr2), reflectors below the diagonal,
+// tau of size min(m, n); util.cpp:424-432.
+static void geqrf(Mat& A, std::vector<double>& tau) {
+    const int m = A.r, n = A.c, k = std::min(m, n);
+    tau.assign(k, 0.0);
+    for (int i = 0; i < k; i++) {
+        double* ci = A.col(i);
+        if (i < m - 1) larfg(m - i, ci[i], ci + i + 1, tau[i]);
+        else larfg(1, ci[m - 1], ci + m - 1, tau[i]);
+        if (i < n - 1 && tau[i] != 0.0) {
+            const double aii = ci[i];
+            ci[i] = 1.0;
+            for (int j = i + 1; j < n; j++) {
+                double* cj = A.col(j);
+                double s = 0.0;
+                for (int r = i; r < m; r++) s += ci[r] * cj[r];
+                s *= tau[i];
+                for (int r = i; r < m; r++) cj[r] -= s * ci[r];
+            }
+            ci[i] = aii;
+        }
+    }
+}
+
+// The first k columns of Q = H_0 ... H_{k-1}, in place over the k reflectors of an m x k
+// matrix (dorgqr -> dorg2r order: reflectors applied last to first); util.cpp:372-380.
+static void orgqr(Mat& A, const std::vector<double>& tau) {
+    const int m = A.r, k = A.c;
+    for (int i = k - 1; i >= 0; i--) {
+        double* ci = A.col(i);
+        if (i < k - 1) {
+            ci[i] = 1.0;
+            if (tau[i] != 0.0)
+                for (int j = i + 1; j < k; j++) {
+                    double* cj = A.col(j);
+                    double s = 0.0;
+                    for (int r = i; r < m; r++) s += ci[r] * cj[r];
+                    s *= tau[i];
+                    for (int r = i; r < m; r++) cj[r] -= s * ci[r];
+                }
+        }
+        for (int r = i + 1; r < m; r++) ci[r] *= -tau[i];
+        ci[i] = 1.0 - tau[i];
+        for (int r = 0; r < i; r++) ci[r] = 0.0;
+    }
+}
+
+// B <- L^T B, L lower triangular (cblas_dtrmm Left Lower Trans NonUnit, rows ascending);
+// util.cpp:296-304.
+static void trmm_trans(const Mat& L, Mat& B) {
+    const int m = B.r;
+    for (int j = 0; j < B.c; j++) {
+        double* b = B.col(j);
+        for (int i = 0; i < m; i++) {
+            double t = b[i] * L(i, i);
+            for (int k = i + 1; k < m; k++) t += L(k, i) * b[k];
+            b[i] = t;
+        }
+    }
+}
+
 // Partial-pivot LU (dgetrf -> dgetf2); returns info; swap is 0-based; util.cpp:183-200.
 static int getf(Mat& A, std::vector<int>& perm) {
     int n = A.r;
@@ -704,6 +765,7 @@ struct Cluster {
     std::list<pEdge> edgesOut;   // pivot first
     std::list<Edge*> edgesIn;
     std::vector<double> x;       // x_ ; original_size() == x.size()
+    pMat phi;                    // preserved vectors restricted to the cluster (size x nphi)
     Cluster(int st, int sz, int lv, int ord, bool sp) : start(st), size(sz), level(lv), order(ord), sparsify(sp) {
         reset_size(sz);
     }
@@ -940,6 +1002,11 @@ struct Tree {
     int symm = SPD;
     int scale_kind = S_LLT;
     bool use_want_sparsify = true;
+    // preservation (tree.h:57, 140-141): the columns of phi (N x nphi, natural ordering,
+    // column-major) are kept in the range of every sparsification
+    bool preserve = false;
+    std::vector<double> phi;
+    int nphi = 0;
     const double* X = nullptr;
     int dim = 0;
     int max_order = 0;
@@ -1267,6 +1334,7 @@ struct Tree {
         if (scale_kind == S_LLT) {
             potf_cluster(self);
             panel_potf(self);
+            if (preserve) trmm_trans(*self->pivot()->A, *self->phi);  // tree.cpp:807-809
             push_op(make_op(OP_SCALING_LLT, self, nullptr, std::move(self->pivot()->A)));
         } else if (scale_kind == S_LDLT) {  // tree.cpp:812-830: the new pivot is diag(sign D)
             auto L = std::make_unique<Mat>();
@@ -1274,6 +1342,14 @@ struct Tree {
             std::vector<int> p;
             ldlt_cluster(self, *L, s, p);
             panel_ldlt(self, *L, p);
+            if (preserve) {  // tree.cpp:824-827: phi <- L^T P^T phi
+                Mat& F = *self->phi;
+                Mat T(F.r, F.c);
+                for (int j = 0; j < F.c; j++)
+                    for (int i = 0; i < F.r; i++) T(i, j) = F(p[i], j);
+                F = std::move(T);
+                trmm_trans(*L, F);
+            }
             auto op = make_op(OP_SCALING_LDLT, self, nullptr, std::move(L));
             op->s = s;
             op->p = p;
@@ -1322,27 +1398,55 @@ struct Tree {
     // tree.cpp:980-1104 (pred == true branch).  Pivot I (SPD, GEN), or (SYM) the signs of
     // the scaling, transformed to Q^T piv Q and split: the sibling's pivot, an edge
     // original -> sibling, and the original's new pivot (tree.cpp:1069-1097).
-    Cluster* shrink_split(Cluster* original, int osize, Mat& AsnP, const Mat& v, const std::vector<double>& h) {
+    // AsnP == nullptr: the preservation branch (pred == false, keep_sibling == false):
+    // phi and every edge block get Q^T (in-edges and phi from the left, out-edges from the
+    // right) and keep their first osize rows / columns; the sibling gets no edge.
+    Cluster* shrink_split(Cluster* original, int osize, Mat* AsnP, const Mat& v, const std::vector<double>& h) {
         const int n0 = original->size;
         int sib_size = original->size - osize;
         auto psib = std::make_unique<Cluster>(original->start + osize, sib_size, original->level, get_new_order(),
                                               original->sparsify);
         Cluster* sib = psib.get();
         original->size = osize;  // set_size keeps x
+        const int k = (int)h.size();
+        auto qt_rows = [&](Mat& B) {  // B (n0 x c) <- (Q^T B)[0:osize, :]
+            for (int j = 0; j < B.c; j++) ormqr_vec(v, h, k, B.col(j), true);
+            Mat T(osize, B.c);
+            for (int j = 0; j < B.c; j++)
+                for (int i = 0; i < osize; i++) T(i, j) = B(i, j);
+            B = std::move(T);
+        };
+        if (preserve) qt_rows(*original->phi);  // tree.cpp:993-1002
         int col = 0;
         for (auto e : original->in_nbr()) {
             int cols = e->n1->size;
+            if (!AsnP) {
+                qt_rows(*e->A);
+                continue;
+            }
             auto M = std::make_unique<Mat>(osize, cols);
             for (int j = 0; j < cols; j++)
-                for (int i = 0; i < osize; i++) (*M)(i, j) = AsnP(i, col + j);
+                for (int i = 0; i < osize; i++) (*M)(i, j) = (*AsnP)(i, col + j);
             e->A = std::move(M);
             col += cols;
         }
         for (auto e : original->out_nbr()) {
             int cols = e->n2->size;
+            if (!AsnP) {  // A Q, row by row as Q^T A^T
+                Mat& B = *e->A;
+                Mat Bt(B.c, B.r);
+                for (int j = 0; j < B.c; j++)
+                    for (int i = 0; i < B.r; i++) Bt(j, i) = B(i, j);
+                qt_rows(Bt);
+                Mat M(B.r, osize);
+                for (int j = 0; j < osize; j++)
+                    for (int i = 0; i < B.r; i++) M(i, j) = Bt(j, i);
+                B = std::move(M);
+                continue;
+            }
             auto M = std::make_unique<Mat>(cols, osize);
             for (int j = 0; j < cols; j++)
-                for (int i = 0; i < osize; i++) (*M)(j, i) = AsnP(i, col + j);
+                for (int i = 0; i < osize; i++) (*M)(j, i) = (*AsnP)(i, col + j);
             e->A = std::move(M);
             col += cols;
         }
@@ -1409,13 +1513,124 @@ struct Tree {
         Mat AsnP(rank, cols);
         for (int j = 0; j < cols; j++)
             for (int i = 0; i < rank && i <= j; i++) AsnP(i, jpvt[j]) = (*Asn)(i, j);
-        Cluster* sib = shrink_split(self, rank, AsnP, *qop->A, qop->h);
+        Cluster* sib = shrink_split(self, rank, &AsnP, *qop->A, qop->h);
         eliminate_cluster(sib);
+    }
+    // tree.cpp:1226-1254: [A_sn phi_n (in-edges) | A_ns^T phi_n (out-edges, pivot first)]
+    pMat assemble_Asphi(Cluster* self) {
+        const int rows = self->size;
+        auto ins = self->in_nbr();
+        auto outs = self->out_all();
+        auto M = std::make_unique<Mat>(rows, nphi * (int)(ins.size() + outs.size()));
+        int c = 0;
+        for (auto e : ins) {  // A (rows x n) phi_n (n x nphi)
+            const Mat& A = *e->A;
+            const Mat& F = *e->n1->phi;
+            for (int q = 0; q < nphi; q++, c++)
+                for (int i = 0; i < rows; i++) {
+                    double s = 0.0;
+                    for (int kk = 0; kk < A.c; kk++) s += A(i, kk) * F(kk, q);
+                    (*M)(i, c) = s;
+                }
+        }
+        for (auto e : outs) {  // A^T (A: n x rows) phi_n
+            const Mat& A = *e->A;
+            const Mat& F = *e->n2->phi;
+            for (int q = 0; q < nphi; q++, c++)
+                for (int i = 0; i < rows; i++) {
+                    double s = 0.0;
+                    for (int kk = 0; kk < A.r; kk++) s += A(kk, i) * F(kk, q);
+                    (*M)(i, c) = s;
+                }
+        }
+        return M;
+    }
+    void record_q_and_split(Cluster* self, pMat v, std::vector<double> h) {
+        const int rank = (int)h.size();
+        auto op = make_op(OP_ORTHOGONAL, self, nullptr, std::move(v));
+        op->h = std::move(h);
+        const Op* qop = op.get();
+        push_op(std::move(op));
+        Cluster* sib = shrink_split(self, rank, nullptr, *qop->A, qop->h);
+        eliminate_cluster(sib);
+    }
+    // tree.cpp:1257-1287: Q from the QR of [A_sn phi, phi]; rank = its column count
+    void sparsify_preserve_only(Cluster* self) {
+        auto A = assemble_Asphi(self);
+        const int rows = A->r, cols = A->c;
+        if (cols >= rows) {
+            rank_log.push_back({ilvl, self->order, rows, rows});
+            return;
+        }
+        std::vector<double> h;
+        geqrf(*A, h);
+        rank_log.push_back({ilvl, self->order, rows, cols});
+        record_q_and_split(self, std::move(A), std::move(h));
+    }
+    // tree.cpp:1350-1409: Q1 spans [A_sn phi, phi]; the QRCP of (I - Q1 Q1^T) Asn truncated
+    // at tol gives Q2; Q from the QR of [Q1 Q2]
+    void sparsify_preserve_adaptive(Cluster* self) {
+        const int rows = self->size;
+        auto Q1 = assemble_Asphi(self);
+        const int rank1 = std::min(rows, Q1->c);
+        std::vector<double> h1;
+        geqrf(*Q1, h1);
+        Q1->c = rank1;
+        Q1->v.resize((size_t)rows * rank1);
+        orgqr(*Q1, h1);
+        auto Asn = assemble_Asn(self);
+        const int cols2 = Asn->c;
+        {  // Asn -= Q1 (Q1^T Asn)
+            std::vector<double> w(rank1);
+            for (int j = 0; j < cols2; j++) {
+                double* a = Asn->col(j);
+                for (int q = 0; q < rank1; q++) {
+                    double s = 0.0;
+                    for (int i = 0; i < rows; i++) s += Q1->col(q)[i] * a[i];
+                    w[q] = s;
+                }
+                for (int i = 0; i < rows; i++) {
+                    double s = 0.0;
+                    for (int q = 0; q < rank1; q++) s += Q1->col(q)[i] * w[q];
+                    a[i] -= s;
+                }
+            }
+        }
+        std::vector<int> jpvt;
+        std::vector<double> h2;
+        geqp3(*Asn, jpvt, h2);
+        std::vector<double> diag(std::min(rows, cols2));
+        for (size_t i = 0; i < diag.size(); i++) diag[i] = (*Asn)((int)i, (int)i);
+        const int rank2 = choose_rank(diag, tol);
+        const int rank = rank1 + rank2;
+        if (rank >= rows) {
+            rank_log.push_back({ilvl, self->order, rows, rows});
+            return;
+        }
+        Mat Q2(rows, rank2);
+        for (int j = 0; j < rank2; j++)
+            for (int i = 0; i < rows; i++) Q2(i, j) = (*Asn)(i, j);
+        h2.resize(rank2);
+        orgqr(Q2, h2);
+        auto V = std::make_unique<Mat>(rows, rank);
+        for (int j = 0; j < rank1; j++)
+            for (int i = 0; i < rows; i++) (*V)(i, j) = (*Q1)(i, j);
+        for (int j = 0; j < rank2; j++)
+            for (int i = 0; i < rows; i++) (*V)(i, rank1 + j) = Q2(i, j);
+        std::vector<double> h;
+        geqrf(*V, h);
+        rank_log.push_back({ilvl, self->order, rows, rank});
+        record_q_and_split(self, std::move(V), std::move(h));
     }
     void sparsify_cluster(Cluster* self) {  // tree.cpp:1417-1433
         if (!use_want_sparsify || self->sparsify) {
             log[ilvl].rank_before.add(self->size);
-            sparsify_adaptive_only(self);
+            if (preserve) {
+                if (tol <= 1.0) sparsify_preserve_adaptive(self);
+                else sparsify_preserve_only(self);
+            } else {
+                sparsify_adaptive_only(self);
+            }
             log[ilvl].rank_after.add(self->size);
         } else {
             log[ilvl].ignored++;
@@ -1428,6 +1643,15 @@ struct Tree {
         int size = 0;
         for (auto sold : snew->children) { posparent[sold] = size; size += sold->size; }
         snew->reset_size(size);
+        if (preserve) {  // tree.cpp:1115-1128
+            snew->phi = std::make_unique<Mat>(size, nphi);
+            int row = 0;
+            for (auto sold : snew->children) {
+                for (int j = 0; j < nphi; j++)
+                    for (int i = 0; i < sold->size; i++) (*snew->phi)(row + i, j) = (*sold->phi)(i, j);
+                row += sold->size;
+            }
+        }
         push_op(make_op(OP_MERGE, snew, nullptr, nullptr));
     }
     // tree.cpp:1133-1184
@@ -1472,6 +1696,16 @@ struct Tree {
     // tree.cpp:1447-1551
     void factorize() {
         double t0 = now_s();
+        if (preserve) {  // tree.cpp:1477-1485: phi_ = P^T phi split over the leaf clusters
+            if (!symmetry()) throw std::runtime_error("oracle: preservation needs a symmetric matrix");
+            const int n = N();
+            if ((int)phi.size() != n * nphi || nphi <= 0) throw std::runtime_error("oracle: phi not set");
+            for (auto& c : bottom_original()) {
+                c->phi = std::make_unique<Mat>(c->size, nphi);
+                for (int j = 0; j < nphi; j++)
+                    for (int i = 0; i < c->size; i++) (*c->phi)(i, j) = phi[(size_t)perm[c->start + i] + (size_t)j * n];
+            }
+        }
         for (ilvl = 0; ilvl < nlevels; ilvl++) {
             double ta = now_s();
             {
@@ -1802,6 +2036,13 @@ void orc_set_skip(void* p, int skip) { ((OrcHandle*)p)->t->skip = skip; }
 void orc_set_symm_kind(void* p, int k) { ((OrcHandle*)p)->t->symm = k; }
 void orc_set_scaling_kind(void* p, int k) { ((OrcHandle*)p)->t->scale_kind = k; }
 void orc_set_use_sparsify(void* p, int u) { ((OrcHandle*)p)->t->use_want_sparsify = u != 0; }
+void orc_set_preserve(void* p, int on) { ((OrcHandle*)p)->t->preserve = on != 0; }
+// phi: n x nphi, column-major, natural ordering (copied)
+void orc_set_phi(void* p, const double* phi, int n, int nphi) {
+    auto t = ((OrcHandle*)p)->t.get();
+    t->phi.assign(phi, phi + (size_t)n * nphi);
+    t->nphi = nphi;
+}
 void orc_set_Xcoo(void* p, const double* X, int dim, int n) {
     auto h = (OrcHandle*)p;
     h->X.assign(X, X + (size_t)dim * n);

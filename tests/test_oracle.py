@@ -320,3 +320,52 @@ def test_plu_exact_and_gmres():
     for restart in (1, 3, 100):
         x, it, rr = u.gmres(b, 200, restart, 1e-12)
         assert rr < 1e-12 and np.linalg.norm(A @ x - b) / np.linalg.norm(b) < 1e-10
+
+
+def _preserved(t, A, phi):
+    """max over the columns of phi of |A x - A phi| / |A phi| and |x - phi| / |phi|, x = M^{-1} A phi."""
+    e = 0.0
+    for c in range(phi.shape[1]):
+        b = A @ phi[:, c]
+        x = t.solve(b)
+        e = max(e, np.linalg.norm(A @ x - b) / np.linalg.norm(b),
+                np.linalg.norm(x - phi[:, c]) / np.linalg.norm(phi[:, c]))
+    return e
+
+
+@pytest.mark.parametrize("dim,n", [(2, 5), (2, 10), (2, 20), (3, 5), (3, 10)])
+def test_preservation(dim, n):
+    """ApproxTest.Preservation (tests/tests.cpp:686-797): with preservation on, the
+    preconditioner reproduces phi (the ones vector, and 5 random vectors) to 1e-12 for A
+    (SPD / LLT) and -A (SYM / LDLT); a random b is solved to tol * 1e2 (1e-12 at tol 0).
+    Tolerance 10 takes the preserve-only branch (tree.cpp:1257-1287), the others the
+    preserve + RRQR branch (tree.cpp:1350-1409).  Levels and skips are a subset of the
+    reference's loops (it runs nlevels..nlevels+4 and skip 0..2)."""
+    A_spd = P.neglapl(n, dim)
+    X = P.linspace_nd(n, dim)
+    N = A_spd.shape[0]
+    lmin = 1 if N < 1000 else 8
+    for nlevels in (lmin, lmin + 2, lmin + 4):
+        for tol in (10.0, 1e-2, 1e-4, 0.0):
+            for skip in (0, 2):
+                for symm in (0, 1):
+                    A = A_spd if symm == 0 else -A_spd
+                    for phi in (np.ones((N, 1)),
+                                np.random.default_rng(nlevels + skip + 2019).uniform(-1, 1, (N, 5))):
+                        t = O.OracleTree(nlevels)
+                        t.set_Xcoo(X)
+                        if symm:
+                            t.set_symm_kind(O.OracleTree.SYM)
+                            t.set_scaling_kind(O.OracleTree.LDLT)
+                        t.partition(A)
+                        t.assemble(A)
+                        t.set_tol(tol)
+                        t.set_skip(skip)
+                        t.set_preserve(True)
+                        t.set_phi(phi)
+                        t.factorize()
+                        assert _preserved(t, A, phi) < 1e-12, (nlevels, tol, skip, symm)
+                        b = np.random.default_rng(nlevels + skip + 2019).uniform(-1, 1, N)
+                        x = t.solve(b)
+                        err = np.linalg.norm(A @ x - b) / np.linalg.norm(b)
+                        assert err < (1e-12 if tol == 0.0 else tol * 1e2), (nlevels, tol, skip, symm, err)
