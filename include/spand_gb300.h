@@ -53,6 +53,12 @@ int spand_tree_set_symm_kind(spand_tree* t, int kind);              /* set_symm_
 /* PartKind {MND=0, RB=1} (include/spaND.h:20)                                           */
 int spand_tree_set_part_kind(spand_tree* t, int kind);              /* set_part_kind     */
 int spand_tree_set_use_sparsify(spand_tree* t, int use);            /* set_use_sparsify  */
+/* set_preserve / set_phi                           -- include/tree.h:140-141
+ * Keep the columns of phi (n x nphi, column-major, natural ordering; copied) in the range
+ * of every sparsification: the preconditioner then reproduces them exactly.  SPD and SYM
+ * kinds only (factorize returns SPAND_ERR_ARG otherwise, or when phi has not N rows).    */
+int spand_tree_set_preserve(spand_tree* t, int preserve);
+int spand_tree_set_phi(spand_tree* t, const double* phi, int n, int nphi);
 /* No reference counterpart: factor storage and arithmetic in FP32 (1) or FP64 (0).      */
 int spand_tree_set_fp32(spand_tree* t, int fp32);
 

@@ -376,13 +376,22 @@ static void ormqr_vec(const Mat& v, const std::vector<double>& h, int k, double*
     else for (int i = k - 1; i >= 0; i--) apply(i);
 }
 
+// Relative size below which the part of a column left by the previous reflectors counts
+// as zero in geqrf (see there).
+static const double QR_DEAD = 1e-10;
+
 // Householder QR without pivoting (dgeqrf -> dgeqr2), reflectors below the diagonal,
-// tau of size min(m, n); util.cpp:424-432.
+// tau of size min(m, n); util.cpp:424-432.  Deviation: a column whose remaining part
+// A(i:m, i) is below QR_DEAD of its norm (a column that depends on the previous ones, as
+// the mirror-image columns of [A_sn phi, phi] on symmetric grids do) gets tau = 0 and is
+// left as it is -- dgeqrf would build its reflector from rounding noise, which no two
+// summation orders reproduce; the reflectors of the other columns are unchanged.
 static void geqrf(Mat& A, std::vector<double>& tau) {
     const int m = A.r, n = A.c, k = std::min(m, n);
     tau.assign(k, 0.0);
     for (int i = 0; i < k; i++) {
         double* ci = A.col(i);
+        if (nrm2(m - i, ci + i) <= QR_DEAD * nrm2(m, ci)) continue;
         if (i < m - 1) larfg(m - i, ci[i], ci + i + 1, tau[i]);
         else larfg(1, ci[m - 1], ci + m - 1, tau[i]);
         if (i < n - 1 && tau[i] != 0.0) {

@@ -46,6 +46,8 @@ _PROTOS = {
     "spand_tree_set_part_kind": (C.c_int, [C.c_void_p, C.c_int]),
     "spand_tree_set_use_sparsify": (C.c_int, [C.c_void_p, C.c_int]),
     "spand_tree_set_fp32": (C.c_int, [C.c_void_p, C.c_int]),
+    "spand_tree_set_preserve": (C.c_int, [C.c_void_p, C.c_int]),
+    "spand_tree_set_phi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
     "spand_tree_partition": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "spand_tree_assemble": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "spand_tree_factorize": (C.c_int, [C.c_void_p]),
@@ -196,6 +198,15 @@ class Tree:
     def set_part_kind(self, k): _check(self.L.spand_tree_set_part_kind(self.h, int(k)))
     def set_use_sparsify(self, u): _check(self.L.spand_tree_set_use_sparsify(self.h, int(bool(u))))
     def set_fp32(self, f): _check(self.L.spand_tree_set_fp32(self.h, int(bool(f))))
+    def set_preserve(self, p): _check(self.L.spand_tree_set_preserve(self.h, int(bool(p))))
+
+    def set_phi(self, phi):
+        """Vectors to preserve (include/tree.h:141): N x nphi (or N), natural ordering; copied."""
+        phi = np.asarray(phi, dtype=np.float64)
+        if phi.ndim == 1:
+            phi = phi[:, None]
+        phi = np.asfortranarray(phi)
+        _check(self.L.spand_tree_set_phi(self.h, phi.ctypes.data, phi.shape[0], phi.shape[1]))
 
     def set_Xcoo(self, X):
         X = np.asfortranarray(X, dtype=np.float64)

@@ -118,6 +118,11 @@ int spand_tree_set_part_kind(spand_tree* t, int k) {
 }
 int spand_tree_set_use_sparsify(spand_tree* t, int u) { CHECK_T(t); t->t->set_use_sparsify(u != 0); return SPAND_OK; }
 int spand_tree_set_fp32(spand_tree* t, int f) { CHECK_T(t); t->t->set_fp32(f != 0); return SPAND_OK; }
+int spand_tree_set_preserve(spand_tree* t, int p) { CHECK_T(t); t->t->set_preserve(p != 0); return SPAND_OK; }
+int spand_tree_set_phi(spand_tree* t, const double* phi, int n, int nphi) {
+    CHECK_T(t);
+    return guard([&] { t->t->set_phi(phi, n, nphi); });
+}
 
 int spand_tree_partition(spand_tree* t, int n, const int* colptr, const int* rowval, int* sepids) {
     CHECK_T(t);

@@ -21,6 +21,7 @@
 
 #include "device.h"
 #include "kcommon.cuh"
+#include "preserve.cuh"
 #include "qrcp.cuh"
 
 namespace spand {
@@ -2968,6 +2969,11 @@ class DeviceFactor : public DeviceFactorBase {
             SPAND_CUDA(cudaMemsetAsync(status_, 0, sizeof(DStatus), s_));
             SPAND_CUDA(cudaMemsetAsync(rank_, 0x7f, nc_ * sizeof(int), s_));
         }, 0);
+        pres_adaptive_ = nphi_ > 0 && tol <= 1.0;
+        if (nphi_)
+            launch("preserve_init", [&] {
+                preserve_init<T>(phictx(), d_phinat_, phi_n_, d_perm_, d_phidst_, d_phild_, s_);
+            });
         bool side_used = false;
         for (int l = 0; l < P.nlevels; l++) {
             LevelDev& D = levels_[l];
@@ -3008,6 +3014,11 @@ class DeviceFactor : public DeviceFactorBase {
                     launch_trsm(D.scale_trsm0);
                     launch_trsm(D.scale_trsm1);
                 }
+                if (nphi_)
+                    launch("preserve_scale", [&] {
+                        preserve_scale<T>(ctx_, phictx(), phitmp_, D.scale_clusters, D.scale_pivots, D.n_scale,
+                                          ldlt_ ? lu_perm_ : nullptr, d_xoff_, s_);
+                    });
             }
             if (D.n_level)
                 launch("snapshot", [&] {
@@ -3016,16 +3027,35 @@ class DeviceFactor : public DeviceFactorBase {
                 });
             for (size_t wi = 0; wi < D.waves.size(); wi++) {
                 WaveDev& W = D.waves[wi];
-                cur_wave_ = (int)wi;
-                launch("qrcp", [&] { launch_qrcp_cluster(W, tol); });
-                cur_wave_ = -1;
-                // matrices larger than the cluster's shared memory: the same algorithm with the
-                // slabs in global memory (clusters of other matrices exit at once)
-                launch("qrcp_global", [&] { launch_qrcp_global(W, tol); });
-                launch("sparsify_scatter", [&] {
-                    sparsify_scatter_kernel<T><<<dim3((unsigned)W.n, (unsigned)W.ytiles), 256, 0, s_>>>(
-                        ctx_, W.items, pieces_, ws_, ipvt_, rank_, vstore_);
-                });
+                if (nphi_) {
+                    // preservation (tree.cpp:1257-1409): Q from [A_sn phi, phi] (and the QRCP
+                    // of what it leaves of Asn), applied to phi and to every edge block
+                    launch("preserve_basis", [&] {
+                        preserve_basis<T>(ctx_, phictx(), W.items, W.n, pieces_, ldlt_ ? signs_ : nullptr, d_xoff_,
+                                          vstore_, tauws_, rank1_, rank_, pres_adaptive_, s_);
+                    });
+                    if (pres_adaptive_) {
+                        launch("qrcp", [&] { launch_qrcp_cluster(W, tol); });
+                        launch("qrcp_global", [&] { launch_qrcp_global(W, tol); });
+                        launch("preserve_combine", [&] {
+                            preserve_combine<T>(ctx_, W.items, W.n, ws_, vstore_, tauws_, rank1_, rank_, s_);
+                        });
+                    }
+                    launch("preserve_apply", [&] {
+                        preserve_apply<T>(ctx_, phictx(), W.items, W.n, W.ptiles, pieces_, vstore_, tauws_, rank_, s_);
+                    });
+                } else {
+                    cur_wave_ = (int)wi;
+                    launch("qrcp", [&] { launch_qrcp_cluster(W, tol); });
+                    cur_wave_ = -1;
+                    // matrices larger than the cluster's shared memory: the same algorithm with
+                    // the slabs in global memory (clusters of other matrices exit at once)
+                    launch("qrcp_global", [&] { launch_qrcp_global(W, tol); });
+                    launch("sparsify_scatter", [&] {
+                        sparsify_scatter_kernel<T><<<dim3((unsigned)W.n, (unsigned)W.ytiles), 256, 0, s_>>>(
+                            ctx_, W.items, pieces_, ws_, ipvt_, rank_, vstore_);
+                    });
+                }
                 if (ldlt_) {
                     launch("pivot_split", [&] {
                         pivot_split_kernel<T><<<W.n, 256, 0, s_>>>(ctx_, W.items, W.sib, W.sib_piv, W.aso, W.piv,
@@ -3065,6 +3095,11 @@ class DeviceFactor : public DeviceFactorBase {
                     launch("merge_copy", [&] {
                         merge_copy_kernel<T><<<D.n_merge_tiles, 256, 0, s_>>>(ctx_, D.merge_items, D.merge_tiles,
                                                                               D.n_merge_tiles, cpos_);
+                    });
+                if (nphi_)
+                    launch("preserve_merge", [&] {
+                        preserve_merge<T>(ctx_, phictx(), D.parents, D.n_parents, D.child_ptr, D.child_idx, cpos_,
+                                          s_);
                     });
             }
         }
@@ -3166,6 +3201,57 @@ class DeviceFactor : public DeviceFactorBase {
         }
         ensure_x(nrhs);
         run_solve(x, nrhs, ld);
+    }
+
+    void set_phi(const double* phi, int n, int nphi) override {
+        if (nphi <= 0) {
+            nphi_ = 0;
+            return;
+        }
+        const Plan& P = *P_;
+        if (n != (int)perm_h_.size()) throw DeviceError{SPAND_ERR_ARG, "phi does not match the matrix size"};
+        long long capsum = 0;
+        for (int c0 = 0; c0 < P.nclusters_h; c0++) capsum += P.c_cap[c0];
+        if (nphi > phi_alloc_) {
+            phis_ = alloc<T>(capsum * nphi);
+            phitmp_ = alloc<T>(capsum * nphi);
+            d_phinat_ = alloc<double>((int64_t)n * nphi);
+            phi_alloc_ = nphi;
+        }
+        if (!rank1_) rank1_ = alloc<int>(nc_);
+        if (nphi != nphi_ || !d_phioff_) {
+            std::vector<long long> off(nc_, 0), dst(std::max(n, 1), 0);
+            std::vector<int> ld(std::max(n, 1), 1);
+            long long o = 0;
+            for (int c0 = 0; c0 < P.nclusters_h; c0++) {
+                off[c0] = o;
+                o += (long long)P.c_cap[c0] * nphi;
+            }
+            for (int c0 = 0; c0 < P.nclusters_h; c0++)
+                if (P.c_hlevel[c0] == 0)
+                    for (int i = 0; i < P.c_cap[c0]; i++) {
+                        dst[P.c_start[c0] + i] = off[c0] + i;
+                        ld[P.c_start[c0] + i] = P.c_cap[c0];
+                    }
+            d_phioff_ = up(off);
+            d_phidst_ = up(dst);
+            d_phild_ = up(ld);
+            for (auto& D : levels_)
+                for (auto& W : D.waves) {
+                    W.ptiles = 1;
+                    for (const SparsifyItem& it : W.host) {
+                        long long cs = 0;
+                        for (int p = 0; p < it.count; p++) cs += P.c_cap[P.asn_pieces[it.first + p].nbr];
+                        W.ptiles = std::max(W.ptiles, preserve_apply_tiles(cs, nphi));
+                    }
+                }
+        }
+        nphi_ = nphi;
+        phi_n_ = n;
+        if (n > 0)
+            SPAND_CUDA(cudaMemcpyAsync(d_phinat_, phi, (size_t)n * nphi * sizeof(double), cudaMemcpyHostToDevice, s_));
+        SPAND_CUDA(cudaStreamSynchronize(s_));
+        factored_ = false;
     }
 
     void solve_device_noalloc(double* x, int nrhs, int ld) override {
@@ -3304,6 +3390,7 @@ class DeviceFactor : public DeviceFactorBase {
         int gcs = 1;         // cluster of the global-memory QRCP (matrices the first does not hold)
         int gsmem = 0;       // its dynamic shared memory per CTA
         int ytiles = 0;      // scatter tiles per matrix (reflector + edge-block capacity tiles)
+        int ptiles = 0;      // preservation: Q^T-application CTAs per matrix
         // LDLT: per item the sibling, its pivot, the edge block, the cluster's pivot; the
         // sibling panels and the Schur update of the cluster's pivot
         int *sib = nullptr, *sib_piv = nullptr, *aso = nullptr, *piv = nullptr;
@@ -3551,6 +3638,11 @@ class DeviceFactor : public DeviceFactorBase {
         W.smem = bsm;
         W.threads = bth;
     }
+    QcProj<T> qc_proj() const {
+        if (nphi_ && pres_adaptive_) return QcProj<T>{vstore_, rank1_};
+        return QcProj<T>{nullptr, nullptr};
+    }
+    PhiCtx<T> phictx() const { return PhiCtx<T>{phis_, d_phioff_, nphi_}; }
     void launch_qrcp_global(WaveDev& W, double tol) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3((unsigned)(W.n * W.gcs));
@@ -3566,7 +3658,7 @@ class DeviceFactor : public DeviceFactorBase {
         cfg.numAttrs = 1;
         SPAND_CUDA(cudaLaunchKernelEx(&cfg, qrcp_gslab_kernel_ptr<T>(), ctx_, (const DSpars*)W.items,
                                       (const DAsn*)pieces_, ws_, ws2_, jpvt_, ipvt_, tauws_, rank_, colcount_,
-                                      fallback_, tol, W.gsmem, (unsigned long long*)nullptr));
+                                      fallback_, tol, W.gsmem, (unsigned long long*)nullptr, qc_proj()));
     }
     void launch_qrcp_cluster(WaveDev& W, double tol) {
         cudaLaunchConfig_t cfg = {};
@@ -3588,7 +3680,7 @@ class DeviceFactor : public DeviceFactorBase {
         }
         SPAND_CUDA(cudaLaunchKernelEx(&cfg, qrcp_smem_kernel_ptr<T>(), ctx_, (const DSpars*)W.items,
                                       (const DAsn*)pieces_, ws_, (T*)nullptr, jpvt_, ipvt_, tauws_, rank_, colcount_,
-                                      fallback_, tol, force_global_ ? 0 : W.smem, probe));
+                                      fallback_, tol, force_global_ ? 0 : W.smem, probe, qc_proj()));
     }
     void launch_potrf(int* pivots, int* clusters, int n, int smem, const TrtriDev& tri, int pc_cs, int pc_smem) {
         if (pc_cs > 0) {
@@ -3933,6 +4025,15 @@ class DeviceFactor : public DeviceFactorBase {
     int* lu_swp_ = nullptr;       // and the row interchanges that make it
     int cur_count_ = 0;           // clusters of the pivot op list being applied in the solve
     bool check_launches_ = getenv("SPAND_CHECK_LAUNCHES") != nullptr;
+    // preservation: phi restricted to every hierarchy cluster (capacity x nphi at
+    // phioff), its scratch, the natural-order phi, the leaf scatter map, rank1 per cluster
+    int nphi_ = 0;
+    T *phis_ = nullptr, *phitmp_ = nullptr;
+    double* d_phinat_ = nullptr;
+    long long *d_phioff_ = nullptr, *d_phidst_ = nullptr;
+    int *d_phild_ = nullptr, *rank1_ = nullptr;
+    int phi_n_ = 0, phi_alloc_ = 0;
+    bool pres_adaptive_ = false;  // preserve + RRQR (tol <= 1) in the running factorization
     bool ldlt_ = false;           // LDLT path (symmetric indefinite)
     T* signs_ = nullptr;          // LDLT: sign(D) of every factored pivot at the cluster's offset
     std::vector<int> diag_h_;     // LDLT: clusters of every ScalingLDLT op (the diag phase)

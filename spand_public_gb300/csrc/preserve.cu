@@ -1,0 +1,396 @@
+// Preservation kernels (preserve.cuh).  Every matrix here is small and dense and lives in
+// global memory (L2-resident); one CTA works on one cluster, its warps on columns.
+#include "preserve.cuh"
+
+namespace spand {
+
+constexpr int PV_THREADS = 256;
+constexpr int PA_VPW = 2;  // vectors per warp in preserve_apply
+
+// Relative size below which the part of a column left by the previous reflectors counts
+// as zero (the oracle's rule, QR_DEAD there; FP32: its rounding level).
+template <typename T>
+__device__ __forceinline__ T qr_dead() {
+    return sizeof(T) == 8 ? T(1e-10) : T(1e-4);
+}
+
+// Householder QR without pivoting of an m x n matrix in place (LAPACK dgeqr2), n <= m:
+// reflector i is [1; A(i+1:m, i)], tau[i]; R on and above the diagonal.  beta =
+// -sign(alpha) |(alpha, x)| with sign(-0) = +1, as in the QRCP kernel and the oracle.  A
+// column whose remaining part A(i:m, i) is below qr_dead() of its norm depends on the
+// previous ones: tau = 0 and the column is left as it is (the oracle's rule; dgeqr2 would
+// build that reflector from rounding noise).
+template <typename T>
+__device__ void cta_geqrf(T* A, int lda, int m, int n, T* tau, T* red) {
+    const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, w = tid >> 5, nw = nth >> 5;
+    const int k = min(m, n);
+    for (int i = 0; i < k; i++) {
+        T* ci = A + (size_t)i * lda;
+        T part = 0, head = 0;
+        for (int r = i + 1 + tid; r < m; r += nth) part += ci[r] * ci[r];
+        for (int r = tid; r < i; r += nth) head += ci[r] * ci[r];
+        const T x2 = block_sum(part, red);
+        const T h2 = block_sum(head, red);
+        const T xnorm = dsqrt(x2);
+        const T alpha = ci[i];
+        const bool dead = dsqrt(alpha * alpha + x2) <= qr_dead<T>() * dsqrt(h2 + alpha * alpha + x2);
+        T beta = alpha, tu = 0, sc = 0;
+        if (xnorm != T(0) && !dead) {
+            beta = alpha >= T(0) ? -hypot(alpha, xnorm) : hypot(alpha, xnorm);
+            tu = (beta - alpha) / beta;
+            sc = T(1) / (alpha - beta);
+        }
+        // H = I - tu v v^T, v = [1; sc * x] with x = A(i+1:m, i) still unscaled
+        if (tu != T(0))
+            for (int j = i + 1 + w; j < n; j += nw) {
+                T* cj = A + (size_t)j * lda;
+                T s = 0;
+                for (int r = i + 1 + lane; r < m; r += 32) s += ci[r] * cj[r];
+                s = warp_sum(s);
+                const T cji = cj[i];
+                __syncwarp();
+                const T wv = tu * (cji + sc * s);
+                const T cr = wv * sc;
+                if (lane == 0) cj[i] = cji - wv;
+                for (int r = i + 1 + lane; r < m; r += 32) cj[r] -= cr * ci[r];
+            }
+        __syncthreads();  // every warp has read the unscaled column
+        if (tid == 0) {
+            tau[i] = tu;
+            ci[i] = beta;
+        }
+        if (tu != T(0))
+            for (int r = i + 1 + tid; r < m; r += nth) ci[r] *= sc;
+        __syncthreads();
+    }
+}
+
+// The first k columns of Q = H_0 ... H_{k-1} in place over the reflectors of an m x k
+// matrix (LAPACK dorg2r: reflectors applied last to first, column i finished at step i).
+template <typename T>
+__device__ void cta_orgqr(T* A, int lda, int m, int k, const T* tau) {
+    const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, w = tid >> 5, nw = nth >> 5;
+    for (int i = k - 1; i >= 0; i--) {
+        T* ci = A + (size_t)i * lda;
+        const T ti = tau[i];
+        if (i < k - 1 && ti != T(0))
+            for (int j = i + 1 + w; j < k; j += nw) {
+                T* cj = A + (size_t)j * lda;
+                T s = 0;
+                for (int r = i + 1 + lane; r < m; r += 32) s += ci[r] * cj[r];
+                s = warp_sum(s);
+                const T cji = cj[i];
+                __syncwarp();
+                const T wv = ti * (cji + s);
+                if (lane == 0) cj[i] = cji - wv;
+                for (int r = i + 1 + lane; r < m; r += 32) cj[r] -= wv * ci[r];
+            }
+        __syncthreads();
+        for (int r = i + 1 + tid; r < m; r += nth) ci[r] *= -ti;
+        for (int r = tid; r < i; r += nth) ci[r] = T(0);
+        if (tid == 0) ci[i] = T(1) - ti;
+        __syncthreads();
+    }
+}
+
+template <typename T>
+__global__ void phi_init_kernel(PhiCtx<T> P, const double* __restrict__ phinat, int n,
+                                const int* __restrict__ perm, const long long* __restrict__ dst,
+                                const int* __restrict__ ld) {
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= (long long)n * P.nphi) return;
+    const int q = (int)(idx % n), j = (int)(idx / n);
+    P.phis[dst[q] + (long long)j * ld[q]] = (T)phinat[perm[q] + (long long)j * n];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(PV_THREADS) phi_scale_kernel(Ctx<T> c, PhiCtx<T> P, T* tmp,
+                                                               const int* __restrict__ clusters,
+                                                               const int* __restrict__ pivots,
+                                                               const int* __restrict__ perm_store,
+                                                               const long long* __restrict__ poff) {
+    if (c.status->not_spd) return;
+    const int cl = clusters[blockIdx.x];
+    const int n = c.csize[cl], ld = c.cap[cl], nphi = P.nphi;
+    const T* L = bptr(c, pivots[blockIdx.x]);
+    const int lld = c.blk[pivots[blockIdx.x]].ld;
+    T* F = P.phis + P.off[cl];
+    T* X = tmp + P.off[cl];
+    const int* perm = perm_store ? perm_store + poff[cl] : nullptr;
+    for (int idx = threadIdx.x; idx < n * nphi; idx += blockDim.x) {
+        const int i = idx % n, j = idx / n;
+        X[i + (size_t)j * ld] = F[(perm ? perm[i] : i) + (size_t)j * ld];
+    }
+    __syncthreads();
+    // F(i, j) = sum_{k >= i} L(k, i) X(k, j), k ascending (the reference's dtrmm order)
+    for (int idx = threadIdx.x; idx < n * nphi; idx += blockDim.x) {
+        const int i = idx % n, j = idx / n;
+        const T* li = L + (size_t)i * lld;
+        const T* xj = X + (size_t)j * ld;
+        T t = xj[i] * li[i];
+        for (int k = i + 1; k < n; k++) t += li[k] * xj[k];
+        F[i + (size_t)j * ld] = t;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(PV_THREADS) phi_merge_kernel(Ctx<T> c, PhiCtx<T> P,
+                                                               const int* __restrict__ parents,
+                                                               const int* __restrict__ child_ptr,
+                                                               const int* __restrict__ child_idx,
+                                                               const int* __restrict__ cpos) {
+    if (c.status->not_spd) return;
+    const int par = parents[blockIdx.x];
+    T* Fp = P.phis + P.off[par];
+    const int ldp = c.cap[par];
+    for (int k = child_ptr[blockIdx.x]; k < child_ptr[blockIdx.x + 1]; k++) {
+        const int ch = child_idx[k];
+        const int m = c.csize[ch], r0 = cpos[ch], ldc = c.cap[ch];
+        const T* Fc = P.phis + P.off[ch];
+        for (int idx = threadIdx.x; idx < m * P.nphi; idx += blockDim.x) {
+            const int i = idx % m, j = idx / m;
+            Fp[r0 + i + (size_t)j * ldp] = Fc[i + (size_t)j * ldc];
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(PV_THREADS) preserve_basis_kernel(Ctx<T> c, PhiCtx<T> P,
+                                                                    const DSpars* __restrict__ items,
+                                                                    const DAsn* __restrict__ pieces,
+                                                                    const T* __restrict__ signs,
+                                                                    const long long* __restrict__ soff, T* vstore,
+                                                                    T* tauws, int* rank1_out, int* rank_out,
+                                                                    int adaptive) {
+    __shared__ T red[33];
+    if (c.status->not_spd) return;
+    const DSpars it = items[blockIdx.x];
+    const int cl = it.cluster;
+    const int rows = c.csize[cl], nphi = P.nphi;
+    const int cols = nphi * (it.count + 1);
+    if (cols >= rows) {  // [A_sn phi, phi] spans everything: nothing to compress
+        if (threadIdx.x == 0) {
+            rank_out[cl] = rows;
+            if (adaptive) rank1_out[cl] = rows;
+        }
+        return;
+    }
+    const int ld = c.cap[cl];
+    const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, w = tid >> 5, nw = nth >> 5;
+    T* V = vstore + it.v_off;
+    const T* Fs = P.phis + P.off[cl];
+    // column groups: in-edges (untransposed pieces, listed first), the pivot, out-edges
+    int nin = 0;
+    while (nin < it.count && !pieces[it.first + nin].transposed) nin++;
+    for (int g = 0; g <= it.count; g++) {
+        T* D = V + (size_t)g * nphi * ld;
+        if (g == nin) {  // pivot: I (LLT) or diag(sign D) (LDLT)
+            const T* sg = signs ? signs + soff[cl] : nullptr;
+            for (int idx = tid; idx < rows * nphi; idx += nth) {
+                const int i = idx % rows, q = idx / rows;
+                const T f = Fs[i + (size_t)q * ld];
+                D[i + (size_t)q * ld] = sg ? sg[i] * f : f;
+            }
+            continue;
+        }
+        const DAsn pc = pieces[it.first + (g < nin ? g : g - 1)];
+        const int n = c.csize[pc.nbr], ldn = c.cap[pc.nbr];
+        const T* B = bptr(c, pc.block);
+        const int bld = c.blk[pc.block].ld;
+        const T* Fn = P.phis + P.off[pc.nbr];
+        if (!pc.transposed) {  // A_sn (rows x n) phi_n
+            for (int idx = tid; idx < rows * nphi; idx += nth) {
+                const int i = idx % rows, q = idx / rows;
+                const T* f = Fn + (size_t)q * ldn;
+                T s = 0;
+                for (int k = 0; k < n; k++) s += B[i + (size_t)k * bld] * f[k];
+                D[i + (size_t)q * ld] = s;
+            }
+        } else {  // A_ns^T phi_n, A_ns: n x rows
+            for (int pr = w; pr < rows * nphi; pr += nw) {
+                const int i = pr % rows, q = pr / rows;
+                const T* b = B + (size_t)i * bld;
+                const T* f = Fn + (size_t)q * ldn;
+                T s = 0;
+                for (int k = lane; k < n; k += 32) s += b[k] * f[k];
+                s = warp_sum(s);
+                if (lane == 0) D[i + (size_t)q * ld] = s;
+            }
+        }
+    }
+    __syncthreads();
+    T* tau = tauws + it.tau_off;
+    cta_geqrf(V, ld, rows, cols, tau, red);
+    if (adaptive) {
+        cta_orgqr(V, ld, rows, cols, tau);
+        if (tid == 0) rank1_out[cl] = cols;
+    } else if (tid == 0) {
+        rank_out[cl] = cols;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(PV_THREADS) preserve_combine_kernel(Ctx<T> c, const DSpars* __restrict__ items,
+                                                                      const T* ws, T* vstore, T* tauws,
+                                                                      const int* __restrict__ rank1_in,
+                                                                      int* rank) {
+    __shared__ T red[33];
+    __shared__ int s_r2;
+    if (c.status->not_spd) return;
+    const DSpars it = items[blockIdx.x];
+    const int cl = it.cluster;
+    const int rows = c.csize[cl];
+    const int r1 = rank1_in[cl];
+    if (threadIdx.x == 0) s_r2 = rank[cl];
+    __syncthreads();
+    const int r2 = s_r2;
+    if (r1 >= rows || r1 + r2 >= rows) {
+        if (threadIdx.x == 0) rank[cl] = rows;
+        return;
+    }
+    const int k = r1 + r2, ld = c.cap[cl];
+    T* V = vstore + it.v_off;
+    const T* W = ws + it.ws_off;  // the QRCP's output, LAPACK column order, ld = cap
+    T* tau = tauws + it.tau_off;
+    for (int idx = threadIdx.x; idx < rows * r2; idx += blockDim.x) {
+        const int i = idx % rows, j = idx / rows;
+        V[i + (size_t)(r1 + j) * ld] = W[i + (size_t)j * ld];
+    }
+    __syncthreads();
+    cta_orgqr(V + (size_t)r1 * ld, ld, rows, r2, tau);  // Q2 (its taus are the QRCP's)
+    cta_geqrf(V, ld, rows, k, tau, red);                // QR of [Q1 Q2]
+    if (threadIdx.x == 0) rank[cl] = k;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(PV_THREADS) preserve_apply_kernel(Ctx<T> c, PhiCtx<T> P,
+                                                                    const DSpars* __restrict__ items,
+                                                                    const DAsn* __restrict__ pieces,
+                                                                    const T* __restrict__ vstore,
+                                                                    const T* __restrict__ tauws,
+                                                                    const int* __restrict__ rank) {
+    if (c.status->not_spd) return;
+    const DSpars it = items[blockIdx.x];
+    const int cl = it.cluster;
+    const int rows = c.rows0[cl];
+    const int k = rank[cl];
+    if (k >= rows) return;
+    if (blockIdx.y == 0 && threadIdx.x == 0) c.csize[cl] = k;
+    const int ld = c.cap[cl];
+    const T* V = vstore + it.v_off;
+    const T* tau = tauws + it.tau_off;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int sub = 0; sub < PA_VPW; sub++) {
+        int v = ((int)blockIdx.y * nw + w) * PA_VPW + sub;
+        // vector v: by capacity over the pieces (a column of an in-edge block, a row of an
+        // out-edge block), then the nphi columns of the cluster's phi
+        int p = 0;
+        for (; p < it.count; p++) {
+            const int cap_n = c.cap[pieces[it.first + p].nbr];
+            if (v < cap_n) break;
+            v -= cap_n;
+        }
+        T* x;
+        long long st;
+        if (p < it.count) {
+            const DAsn pc = pieces[it.first + p];
+            if (v >= c.csize[pc.nbr]) continue;
+            T* B = bptr(c, pc.block);
+            const int bld = c.blk[pc.block].ld;
+            if (!pc.transposed) {
+                x = B + (size_t)v * bld;
+                st = 1;
+            } else {
+                x = B + v;
+                st = bld;
+            }
+        } else {
+            if (v >= P.nphi) continue;
+            x = P.phis + P.off[cl] + (size_t)v * ld;
+            st = 1;
+        }
+        // x <- Q^T x = H_{k-1} ... H_0 x
+        for (int j = 0; j < k; j++) {
+            const T tj = tau[j];
+            if (tj == T(0)) continue;
+            const T* vj = V + (size_t)j * ld;
+            T s = 0;
+            for (int r = j + 1 + lane; r < rows; r += 32) s += vj[r] * x[r * st];
+            s = warp_sum(s);
+            const T xj = x[j * st];
+            __syncwarp();
+            const T wv = tj * (xj + s);
+            if (lane == 0) x[j * st] = xj - wv;
+            for (int r = j + 1 + lane; r < rows; r += 32) x[r * st] -= wv * vj[r];
+            __syncwarp();
+        }
+    }
+}
+
+int preserve_apply_tiles(long long capsum, int nphi) {
+    const long long per = (long long)(PV_THREADS / 32) * PA_VPW;
+    return (int)std::max<long long>(1, (capsum + nphi + per - 1) / per);
+}
+
+template <typename T>
+void preserve_init(PhiCtx<T> P, const double* phinat, int n, const int* perm, const long long* dst, const int* ld,
+                   cudaStream_t s) {
+    const long long tot = (long long)n * P.nphi;
+    if (tot == 0) return;
+    phi_init_kernel<T><<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(P, phinat, n, perm, dst, ld);
+}
+
+template <typename T>
+void preserve_scale(Ctx<T> c, PhiCtx<T> P, T* tmp, const int* clusters, const int* pivots, int count,
+                    const int* perm_store, const long long* poff, cudaStream_t s) {
+    if (count == 0) return;
+    phi_scale_kernel<T><<<count, PV_THREADS, 0, s>>>(c, P, tmp, clusters, pivots, perm_store, poff);
+}
+
+template <typename T>
+void preserve_merge(Ctx<T> c, PhiCtx<T> P, const int* parents, int np, const int* child_ptr, const int* child_idx,
+                    const int* cpos, cudaStream_t s) {
+    if (np == 0) return;
+    phi_merge_kernel<T><<<np, PV_THREADS, 0, s>>>(c, P, parents, child_ptr, child_idx, cpos);
+}
+
+template <typename T>
+void preserve_basis(Ctx<T> c, PhiCtx<T> P, const DSpars* items, int n, const DAsn* pieces, const T* signs,
+                    const long long* soff, T* vstore, T* tauws, int* rank1, int* rank, bool adaptive, cudaStream_t s) {
+    if (n == 0) return;
+    preserve_basis_kernel<T><<<n, PV_THREADS, 0, s>>>(c, P, items, pieces, signs, soff, vstore, tauws, rank1, rank,
+                                                      adaptive ? 1 : 0);
+}
+
+template <typename T>
+void preserve_combine(Ctx<T> c, const DSpars* items, int n, const T* ws, T* vstore, T* tauws, const int* rank1,
+                      int* rank, cudaStream_t s) {
+    if (n == 0) return;
+    preserve_combine_kernel<T><<<n, PV_THREADS, 0, s>>>(c, items, ws, vstore, tauws, rank1, rank);
+}
+
+template <typename T>
+void preserve_apply(Ctx<T> c, PhiCtx<T> P, const DSpars* items, int n, int ytiles, const DAsn* pieces,
+                    const T* vstore, const T* tauws, const int* rank, cudaStream_t s) {
+    if (n == 0) return;
+    preserve_apply_kernel<T><<<dim3((unsigned)n, (unsigned)ytiles), PV_THREADS, 0, s>>>(c, P, items, pieces, vstore,
+                                                                                       tauws, rank);
+}
+
+#define SPAND_PRESERVE_INST(T)                                                                                     \
+    template void preserve_init<T>(PhiCtx<T>, const double*, int, const int*, const long long*, const int*,         \
+                                   cudaStream_t);                                                                  \
+    template void preserve_scale<T>(Ctx<T>, PhiCtx<T>, T*, const int*, const int*, int, const int*,                 \
+                                    const long long*, cudaStream_t);                                                \
+    template void preserve_merge<T>(Ctx<T>, PhiCtx<T>, const int*, int, const int*, const int*, const int*,         \
+                                    cudaStream_t);                                                                 \
+    template void preserve_basis<T>(Ctx<T>, PhiCtx<T>, const DSpars*, int, const DAsn*, const T*,                   \
+                                    const long long*, T*, T*, int*, int*, bool, cudaStream_t);                     \
+    template void preserve_combine<T>(Ctx<T>, const DSpars*, int, const T*, T*, T*, const int*, int*, cudaStream_t); \
+    template void preserve_apply<T>(Ctx<T>, PhiCtx<T>, const DSpars*, int, int, const DAsn*, const T*, const T*,    \
+                                    const int*, cudaStream_t);
+
+SPAND_PRESERVE_INST(float)
+SPAND_PRESERVE_INST(double)
+
+}  // namespace spand

@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, cons
                                                                   int* jpvt_ws, int* ipvt_ws, T* taus,
                                                                   int* rank_out, int* colcount, int* fallback,
                                                                   double tol, int smem_bytes,
-                                                                  unsigned long long* probe) {
+                                                                  unsigned long long* probe, QcProj<T> proj) {
     namespace cgx = cooperative_groups;
     cgx::cluster_group cl = cgx::this_cluster();
     const int CS = (int)cl.num_blocks();
@@ -81,13 +81,15 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, cons
     const int lda = GS ? c.cap[it.cluster] : (rows | 1);
     const bool fits = GS ? qc_small_need(rows, cols, CS, (int)sizeof(T)) <= smem_bytes
                          : qc_need(rows, cols, CS, (int)sizeof(T)) <= smem_bytes;
+    const int r1 = proj.q ? proj.rank1[it.cluster] : 0;
+    const bool spanned = proj.q && r1 >= rows;
     if (!GS && threadIdx.x == 0 && me == 0) {
-        fallback[item] = (mn > 0 && tol < 1.0 && !fits) ? 1 : 0;
+        fallback[item] = (mn > 0 && tol < 1.0 && !fits && !spanned) ? 1 : 0;
         colcount[item] = cols;
     }
     int* jpg = jpvt_ws + it.col_off;
     int* ipg = ipvt_ws + it.col_off;
-    if (mn == 0 || tol >= 1.0) {
+    if (mn == 0 || tol >= 1.0 || spanned) {
         // choose_rank gives 0 for an empty diagonal and for tol >= 1: no reflectors
         if (me == 0) {
             for (int j = threadIdx.x; j < cols; j += blockDim.x) {
@@ -140,6 +142,22 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, cons
     for (int p = tid; p < cols; p += nth) perm[p] = p;
     for (int j = tid; j < nloc; j += nth) pos[j] = c0 + j;
     __syncthreads();
+    if (r1 > 0) {
+        // a <- (I - Q1 Q1^T) a, one basis vector at a time, by the warp that owns column a
+        const T* Q1 = proj.q + it.v_off;
+        const int ldq = c.cap[it.cluster];
+        for (int j = w; j < nloc; j += nw) {
+            T* a = A + (size_t)j * lda;
+            for (int k = 0; k < r1; k++) {
+                const T* q = Q1 + (size_t)k * ldq;
+                T s = 0;
+                for (int r = lane; r < rows; r += 32) s += q[r] * a[r];
+                s = warp_sum(s);
+                for (int r = lane; r < rows; r += 32) a[r] -= s * q[r];
+            }
+        }
+        __syncwarp();
+    }
     for (int j = w; j < nloc; j += nw) {
         const T* a = A + (size_t)j * lda;
         T s = 0;

@@ -24,11 +24,21 @@ __host__ __device__ inline long long qc_small_need(int rows, int cols, int cs, i
     return ((long long)rows + 2 * cpc) * elem + ((long long)cols + cpc) * 4;
 }
 
+// Preservation (src/tree.cpp:1371-1373): before the QRCP, Asn <- (I - Q1 Q1^T) Asn with
+// Q1 the orthonormal basis at the item's v_off in q (ld = the cluster's capacity) and
+// rank1[cluster] its column count; rank1 >= rows: nothing to factor (rank 0).  q ==
+// nullptr: plain QRCP.
+template <typename T>
+struct QcProj {
+    const T* q;
+    const int* rank1;
+};
+
 // (ctx, items, pieces, ws, gslab, jpvt, ipvt, tau, rank, colcount, fallback, tol,
-//  dynamic shared bytes, probe)
+//  dynamic shared bytes, probe, projection)
 template <typename T>
 using QcKernel = void (*)(Ctx<T>, const DSpars*, const DAsn*, T*, T*, int*, int*, T*, int*, int*, int*, double,
-                          int, unsigned long long*);
+                          int, unsigned long long*, QcProj<T>);
 
 // column slabs in the cluster's shared memory
 template <typename T>

@@ -173,9 +173,32 @@ std::string Tree::pivot_error() const {
     return symm_ == SymmKind::GEN ? "Error: Singular Pivot\n" : "Error: Non-SPD Pivot\n";
 }
 
+void Tree::set_phi(const double* phi, int n, int nphi) {
+    if (n < 0 || nphi < 0 || (n * (long long)nphi > 0 && !phi)) throw std::invalid_argument("bad phi");
+    phi_.assign(phi, phi + (size_t)n * nphi);
+    phi_n_ = n;
+    nphi_ = nphi;
+}
+
+// tree.cpp:1457-1459, 1477-1485: preservation needs a symmetric kind and phi of N rows
+void Tree::prepare_factorize() {
+    if (!assembled_ok_) throw std::logic_error("factorize() before assemble()");
+    try {
+        if (!preserve_) {
+            dev_->set_phi(nullptr, 0, 0);
+            return;
+        }
+        if (symm_ == SymmKind::GEN) throw std::invalid_argument("preservation needs a symmetric matrix (SPD or SYM)");
+        if (nphi_ <= 0 || phi_n_ != get_N()) throw std::invalid_argument("preservation needs phi with N rows");
+        dev_->set_phi(phi_.data(), phi_n_, nphi_);
+    } catch (spand::DeviceError& e) {
+        throw std::runtime_error(e.msg);
+    }
+}
+
 // tree.cpp:1447-1551
 void Tree::factorize() {
-    if (!assembled_ok_) throw std::logic_error("factorize() before assemble()");
+    prepare_factorize();
     double t0 = now_s();
     try {
         dev_->factorize(tol_);
@@ -192,7 +215,7 @@ void Tree::factorize() {
 }
 
 void Tree::factorize_enqueue() {
-    if (!assembled_ok_) throw std::logic_error("factorize() before assemble()");
+    prepare_factorize();
     try {
         dev_->factorize_enqueue(tol_);
     } catch (spand::DeviceError& e) {
@@ -220,7 +243,7 @@ spand::PcgWork& Tree::pcg_work() const {
 }
 
 void Tree::bench_step(const double* b_dev, double* x_dev, int nrhs, int iters, double tol, double out[4]) {
-    if (!assembled_ok_) throw std::logic_error("bench_step() before assemble()");
+    prepare_factorize();
     cudaEvent_t e[3];
     for (auto& ev : e) cuda_check(cudaEventCreate(&ev), "cudaEventCreate");
     spand::PcgResult r;
@@ -365,8 +388,10 @@ void Tree::build_ops_and_log() {
                 bool before = wn != wmap.end() && wn->second < wmap[c];
                 cols += before ? csize_[n] : rows0_[n];
             }
-            G.nbrs_sum += cols;
-            G.nbrs_count += 1;
+            if (!(preserve_ && tol_ > 1.0)) {  // preserve-only assembles no Asn (tree.cpp:1257-1287)
+                G.nbrs_sum += cols;
+                G.nbrs_count += 1;
+            }
             if (k < rows) {
                 push({3, l, c, -1, rows, 0, rows, k, c});
                 int sib = next_order++;

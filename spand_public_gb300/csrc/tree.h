@@ -58,6 +58,12 @@ class Tree {
     void set_symm_kind(SymmKind k) { symm_ = k; }
     void set_part_kind(PartKind k) { part_kind_ = k; }
     void set_use_sparsify(bool u) { use_want_sparsify_ = u; }
+    // tree.h:140-141: keep the columns of phi in the range of every sparsification
+    // (symmetric kinds only).  phi: n x nphi, column-major, natural ordering; copied (the
+    // reference borrows the pointer and reads it in factorize()).
+    void set_preserve(bool p) { preserve_ = p; }
+    void set_phi(const double* phi, int n, int nphi);
+    bool get_preserve() const { return preserve_; }
     // No reference counterpart: storage/arithmetic type of the factor (false: FP64).
     void set_fp32(bool f) { fp32_ = f; }
 
@@ -141,12 +147,16 @@ class Tree {
    private:
     void build_ops_and_log();
     std::string pivot_error() const;
+    void prepare_factorize();  // hands phi to the device (or turns preservation off)
     void ensure_log() const {
         if (log_dirty_) const_cast<Tree*>(this)->build_ops_and_log();
     }
 
     int nlevels_;
     bool verb_ = true, geo_ = false, use_want_sparsify_ = true, fp32_ = false;
+    bool preserve_ = false;
+    std::vector<double> phi_;
+    int phi_n_ = 0, nphi_ = 0;
     double tol_ = 10.0;  // tree.cpp:94
     int skip_ = 0;
     ScalingKind scaling_ = ScalingKind::LLT;
