@@ -3041,8 +3041,13 @@ class DeviceFactor : public DeviceFactorBase {
                             preserve_combine<T>(ctx_, W.items, W.n, ws_, vstore_, tauws_, rank1_, rank_, s_);
                         });
                     }
+                    // the WY factors first: the Q^T application uses them
+                    launch("sparsify_wy", [&] {
+                        sparsify_wy_kernel<T><<<W.n, 256, larft_smem_elems() * sizeof(T), s_>>>(
+                            ctx_, W.items, vstore_, rank_, tauws_, taustore_, tstore_);
+                    });
                     launch("preserve_apply", [&] {
-                        preserve_apply<T>(ctx_, phictx(), W.items, W.n, W.ptiles, pieces_, vstore_, tauws_, rank_, s_);
+                        preserve_apply<T>(ctx_, phictx(), W.items, W.n, W.ptiles, pieces_, vstore_, tstore_, rank_, s_);
                     });
                 } else {
                     cur_wave_ = (int)wi;
@@ -3070,8 +3075,9 @@ class DeviceFactor : public DeviceFactorBase {
                         });
                 }
                 // WY factors: on the side stream beside the next wave's QRCP (on the main
-                // stream when the profiler times every launch)
-                if (prof_.enabled()) {
+                // stream when the profiler times every launch); preservation made them above
+                if (nphi_) {
+                } else if (prof_.enabled()) {
                     launch("sparsify_wy", [&] {
                         sparsify_wy_kernel<T><<<W.n, 256, larft_smem_elems() * sizeof(T), s_>>>(
                             ctx_, W.items, vstore_, rank_, tauws_, taustore_, tstore_);
@@ -3240,9 +3246,9 @@ class DeviceFactor : public DeviceFactorBase {
                 for (auto& W : D.waves) {
                     W.ptiles = 1;
                     for (const SparsifyItem& it : W.host) {
-                        long long cs = 0;
-                        for (int p = 0; p < it.count; p++) cs += P.c_cap[P.asn_pieces[it.first + p].nbr];
-                        W.ptiles = std::max(W.ptiles, preserve_apply_tiles(cs, nphi));
+                        std::vector<int> caps;
+                        for (int p = 0; p < it.count; p++) caps.push_back(P.c_cap[P.asn_pieces[it.first + p].nbr]);
+                        W.ptiles = std::max(W.ptiles, preserve_apply_tiles(caps.data(), it.count, nphi));
                     }
                 }
         }

@@ -5,7 +5,6 @@
 namespace spand {
 
 constexpr int PV_THREADS = 256;
-constexpr int PA_VPW = 2;  // vectors per warp in preserve_apply
 
 // Relative size below which the part of a column left by the previous reflectors counts
 // as zero (the oracle's rule, QR_DEAD there; FP32: its rounding level).
@@ -262,13 +261,26 @@ __global__ void __launch_bounds__(PV_THREADS) preserve_combine_kernel(Ctx<T> c, 
     if (threadIdx.x == 0) rank[cl] = k;
 }
 
+// Q^T on a tile of up to 32 vectors (a 32-column tile of an in-edge block, a 32-row tile
+// of an out-edge block, or phi's columns), in the blocked compact WY form the solve uses
+// (blocks of QB = 32 reflectors, T_b upper triangular at the item's v_off in tstore, ld =
+// cap): per block b, W = V_b^T X, Y = T_b^T W, X -= V_b Y, blocks in increasing order
+// (Q^T = Q_{nb-1}^T ... Q_0^T).  X stays in global memory and passes through shared memory
+// PW_KC rows at a time; element (r, l) of the tile is base[r * sr + l * sv].
+constexpr int PW_KC = 32;
+constexpr int PW_QB = 32;
+
 template <typename T>
 __global__ void __launch_bounds__(PV_THREADS) preserve_apply_kernel(Ctx<T> c, PhiCtx<T> P,
                                                                     const DSpars* __restrict__ items,
                                                                     const DAsn* __restrict__ pieces,
                                                                     const T* __restrict__ vstore,
-                                                                    const T* __restrict__ tauws,
+                                                                    const T* __restrict__ tstore,
                                                                     const int* __restrict__ rank) {
+    __shared__ T vt[PW_KC][PW_QB + 1];
+    __shared__ T xs[PW_KC][PW_QB + 1];
+    __shared__ T Wm[PW_QB][PW_QB + 1];
+    __shared__ T Ym[PW_QB][PW_QB + 1];
     if (c.status->not_spd) return;
     const DSpars it = items[blockIdx.x];
     const int cl = it.cluster;
@@ -277,59 +289,110 @@ __global__ void __launch_bounds__(PV_THREADS) preserve_apply_kernel(Ctx<T> c, Ph
     if (k >= rows) return;
     if (blockIdx.y == 0 && threadIdx.x == 0) c.csize[cl] = k;
     const int ld = c.cap[cl];
-    const T* V = vstore + it.v_off;
-    const T* tau = tauws + it.tau_off;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int sub = 0; sub < PA_VPW; sub++) {
-        int v = ((int)blockIdx.y * nw + w) * PA_VPW + sub;
-        // vector v: by capacity over the pieces (a column of an in-edge block, a row of an
-        // out-edge block), then the nphi columns of the cluster's phi
-        int p = 0;
-        for (; p < it.count; p++) {
-            const int cap_n = c.cap[pieces[it.first + p].nbr];
-            if (v < cap_n) break;
-            v -= cap_n;
-        }
-        T* x;
-        long long st;
-        if (p < it.count) {
-            const DAsn pc = pieces[it.first + p];
-            if (v >= c.csize[pc.nbr]) continue;
-            T* B = bptr(c, pc.block);
-            const int bld = c.blk[pc.block].ld;
-            if (!pc.transposed) {
-                x = B + (size_t)v * bld;
-                st = 1;
-            } else {
-                x = B + v;
-                st = bld;
-            }
+    // the tile: 32-vector capacity tiles of the pieces, then those of phi
+    int t = blockIdx.y, p = 0;
+    for (; p < it.count; p++) {
+        const int nt = (c.cap[pieces[it.first + p].nbr] + PW_QB - 1) / PW_QB;
+        if (t < nt) break;
+        t -= nt;
+    }
+    const int j0 = PW_QB * t;
+    T* base;
+    long long sr, sv;
+    int nv;
+    if (p < it.count) {
+        const DAsn pc = pieces[it.first + p];
+        const int n = c.csize[pc.nbr];
+        if (j0 >= n) return;
+        nv = min(PW_QB, n - j0);
+        T* B = bptr(c, pc.block);
+        const long long bld = c.blk[pc.block].ld;
+        if (!pc.transposed) {
+            base = B + (size_t)j0 * bld;
+            sr = 1;
+            sv = bld;
         } else {
-            if (v >= P.nphi) continue;
-            x = P.phis + P.off[cl] + (size_t)v * ld;
-            st = 1;
+            base = B + j0;
+            sr = bld;
+            sv = 1;
         }
-        // x <- Q^T x = H_{k-1} ... H_0 x
-        for (int j = 0; j < k; j++) {
-            const T tj = tau[j];
-            if (tj == T(0)) continue;
-            const T* vj = V + (size_t)j * ld;
-            T s = 0;
-            for (int r = j + 1 + lane; r < rows; r += 32) s += vj[r] * x[r * st];
-            s = warp_sum(s);
-            const T xj = x[j * st];
-            __syncwarp();
-            const T wv = tj * (xj + s);
-            if (lane == 0) x[j * st] = xj - wv;
-            for (int r = j + 1 + lane; r < rows; r += 32) x[r * st] -= wv * vj[r];
-            __syncwarp();
+    } else {
+        if (j0 >= P.nphi) return;
+        nv = min(PW_QB, P.nphi - j0);
+        base = P.phis + P.off[cl] + (size_t)j0 * ld;
+        sr = 1;
+        sv = ld;
+    }
+    const T* V = vstore + it.v_off;
+    const T* Tm = tstore + it.v_off;
+    const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, w = tid >> 5;
+    const bool rfast = sr == 1;  // consecutive threads on consecutive rows (coalesced)
+    auto stage = [&](int rb, int i0, int bw) {
+        for (int idx = tid; idx < PW_KC * PW_QB; idx += nth) {
+            const int kk = idx % PW_KC, ii = idx / PW_KC;
+            const int r = rb + kk, col = i0 + ii;
+            T v = T(0);
+            if (ii < bw && r < rows) v = r > col ? V[r + (size_t)col * ld] : (r == col ? T(1) : T(0));
+            vt[kk][ii] = v;
+            const int rr = rfast ? kk : idx / PW_QB, l = rfast ? ii : idx % PW_QB;
+            const int r2 = rb + rr;
+            xs[rr][l] = (l < nv && r2 < rows) ? base[r2 * sr + l * sv] : T(0);
+        }
+    };
+    const int nb = (k + PW_QB - 1) / PW_QB;
+    for (int b = 0; b < nb; b++) {
+        const int i0 = b * PW_QB, bw = min(PW_QB, k - i0);
+        // W[i][l] = sum_{r >= i0 + i} v_i[r] X[r][l]   (v_i[i0 + i] = 1)
+        T acc[4] = {T(0), T(0), T(0), T(0)};
+        for (int rb = i0; rb < rows; rb += PW_KC) {
+            __syncthreads();
+            stage(rb, i0, bw);
+            __syncthreads();
+            const int kw = min(PW_KC, rows - rb);
+            for (int kk = 0; kk < kw; kk++) {
+                const T xv = xs[kk][lane];
+#pragma unroll
+                for (int u = 0; u < 4; u++) acc[u] += vt[kk][w + 8 * u] * xv;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) Wm[w + 8 * u][lane] = acc[u];
+        __syncthreads();
+        // Y = T_b^T W
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int i = w + 8 * u;
+            T y = T(0);
+            if (i < bw)
+                for (int j = 0; j <= i; j++) y += Tm[(i0 + j) + (size_t)(i0 + i) * ld] * Wm[j][lane];
+            Ym[i][lane] = y;
+        }
+        // X[r][l] -= sum_i v_i[r] Y[i][l], chunk by chunk
+        for (int rb = i0; rb < rows; rb += PW_KC) {
+            __syncthreads();
+            stage(rb, i0, bw);
+            __syncthreads();
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int kk = w + 8 * u;
+                T s2 = T(0);
+                for (int ii = 0; ii < bw; ii++) s2 += vt[kk][ii] * Ym[ii][lane];
+                xs[kk][lane] -= s2;
+            }
+            __syncthreads();
+            for (int idx = tid; idx < PW_KC * PW_QB; idx += nth) {
+                const int rr = rfast ? idx % PW_KC : idx / PW_QB, l = rfast ? idx / PW_KC : idx % PW_QB;
+                const int r2 = rb + rr;
+                if (l < nv && r2 < rows) base[r2 * sr + l * sv] = xs[rr][l];
+            }
         }
     }
 }
 
-int preserve_apply_tiles(long long capsum, int nphi) {
-    const long long per = (long long)(PV_THREADS / 32) * PA_VPW;
-    return (int)std::max<long long>(1, (capsum + nphi + per - 1) / per);
+int preserve_apply_tiles(const int* caps, int count, int nphi) {
+    int t = (nphi + PW_QB - 1) / PW_QB;
+    for (int p = 0; p < count; p++) t += (caps[p] + PW_QB - 1) / PW_QB;
+    return std::max(1, t);
 }
 
 template <typename T>
@@ -371,10 +434,10 @@ void preserve_combine(Ctx<T> c, const DSpars* items, int n, const T* ws, T* vsto
 
 template <typename T>
 void preserve_apply(Ctx<T> c, PhiCtx<T> P, const DSpars* items, int n, int ytiles, const DAsn* pieces,
-                    const T* vstore, const T* tauws, const int* rank, cudaStream_t s) {
+                    const T* vstore, const T* tstore, const int* rank, cudaStream_t s) {
     if (n == 0) return;
     preserve_apply_kernel<T><<<dim3((unsigned)n, (unsigned)ytiles), PV_THREADS, 0, s>>>(c, P, items, pieces, vstore,
-                                                                                       tauws, rank);
+                                                                                       tstore, rank);
 }
 
 #define SPAND_PRESERVE_INST(T)                                                                                     \

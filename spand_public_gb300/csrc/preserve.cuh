@@ -53,12 +53,14 @@ void preserve_combine(Ctx<T> c, const DSpars* items, int n, const T* ws, T* vsto
 
 // tree.cpp:993-1064 with pred == false: Q^T on phi and on every edge block of the cluster
 // (in-edges from the left, out-edges from the right), the first rank rows / columns kept;
-// the cluster's size becomes rank.  ytiles: CTAs per item (preserve_apply_tiles).
+// the cluster's size becomes rank.  Q in the blocked WY form of the solve: reflectors in
+// vstore, the T factors (sparsify_wy_kernel) in tstore.  ytiles: CTAs per item
+// (preserve_apply_tiles).
 template <typename T>
 void preserve_apply(Ctx<T> c, PhiCtx<T> P, const DSpars* items, int n, int ytiles, const DAsn* pieces,
-                    const T* vstore, const T* tauws, const int* rank, cudaStream_t s);
+                    const T* vstore, const T* tstore, const int* rank, cudaStream_t s);
 
-// CTAs per item of preserve_apply for a cluster whose pieces' capacities sum to capsum
-int preserve_apply_tiles(long long capsum, int nphi);
+// CTAs per item of preserve_apply: 32-vector tiles of the pieces' capacities and of phi
+int preserve_apply_tiles(const int* caps, int count, int nphi);
 
 }  // namespace spand
