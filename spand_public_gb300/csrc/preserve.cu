@@ -18,7 +18,10 @@ __device__ __forceinline__ T qr_dead() {
 // -sign(alpha) |(alpha, x)| with sign(-0) = +1, as in the QRCP kernel and the oracle.  A
 // column whose remaining part A(i:m, i) is below qr_dead() of its norm depends on the
 // previous ones: tau = 0 and the column is left as it is (the oracle's rule; dgeqr2 would
-// build that reflector from rounding noise).
+// build that reflector from rounding noise).  Two barriers per column: after the norms
+// (both sums in one pass, per-warp partials in red[0:8] and red[16:24]) and after the
+// update of the trailing columns; the scaling of column i needs none, since no later
+// step reads it.
 template <typename T>
 __device__ void cta_geqrf(T* A, int lda, int m, int n, T* tau, T* red) {
     const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, w = tid >> 5, nw = nth >> 5;
@@ -28,8 +31,18 @@ __device__ void cta_geqrf(T* A, int lda, int m, int n, T* tau, T* red) {
         T part = 0, head = 0;
         for (int r = i + 1 + tid; r < m; r += nth) part += ci[r] * ci[r];
         for (int r = tid; r < i; r += nth) head += ci[r] * ci[r];
-        const T x2 = block_sum(part, red);
-        const T h2 = block_sum(head, red);
+        part = warp_sum(part);
+        head = warp_sum(head);
+        if (lane == 0) {
+            red[w] = part;
+            red[16 + w] = head;
+        }
+        __syncthreads();  // partial norms; the previous step's updates of column i
+        T x2 = 0, h2 = 0;
+        for (int q = 0; q < nw; q++) {
+            x2 += red[q];
+            h2 += red[16 + q];
+        }
         const T xnorm = dsqrt(x2);
         const T alpha = ci[i];
         const bool dead = dsqrt(alpha * alpha + x2) <= qr_dead<T>() * dsqrt(h2 + alpha * alpha + x2);
@@ -53,15 +66,15 @@ __device__ void cta_geqrf(T* A, int lda, int m, int n, T* tau, T* red) {
                 if (lane == 0) cj[i] = cji - wv;
                 for (int r = i + 1 + lane; r < m; r += 32) cj[r] -= cr * ci[r];
             }
-        __syncthreads();  // every warp has read the unscaled column
+        __syncthreads();  // every warp has read the unscaled column and red[]
         if (tid == 0) {
             tau[i] = tu;
             ci[i] = beta;
         }
         if (tu != T(0))
             for (int r = i + 1 + tid; r < m; r += nth) ci[r] *= sc;
-        __syncthreads();
     }
+    __syncthreads();
 }
 
 // The first k columns of Q = H_0 ... H_{k-1} in place over the reflectors of an m x k
