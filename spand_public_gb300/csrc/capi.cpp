@@ -140,7 +140,9 @@ int spand_tree_partition(spand_tree* t, int n, const int* colptr, const int* row
 int spand_tree_assemble(spand_tree* t, int n, const int* colptr, const int* rowval, const double* vals) {
     CHECK_T(t);
     if (!vals) return fail(SPAND_ERR_ARG, "null values");
-    return guard([&] { t->t->assemble(make_csc(n, colptr, rowval, vals)); });
+    return guard([&] {
+        if (!t->t->assemble_same_pattern(n, colptr, rowval, vals)) t->t->assemble(make_csc(n, colptr, rowval, vals));
+    });
 }
 
 int spand_tree_factorize(spand_tree* t) {

@@ -151,6 +151,26 @@ void Tree::assemble(const Csc& A) {
     t_assemble = now_s() - t0;
 }
 
+bool Tree::assemble_same_pattern(int n, const int* colptr, const int* rowval, const double* vals) {
+    if (!assembled_ok_ || !dev_ || n != A_.n || !colptr || !vals) return false;
+    if (std::memcmp(colptr, A_.colptr.data(), ((size_t)n + 1) * sizeof(int)) != 0) return false;
+    const size_t nnz = A_.rowval.size();
+    if (nnz && (!rowval || std::memcmp(rowval, A_.rowval.data(), nnz * sizeof(int)) != 0)) return false;
+    double t0 = now_s();
+    std::memcpy(A_.val.data(), vals, nnz * sizeof(double));
+    try {
+        dev_->assemble_values(vals, (int64_t)nnz);
+    } catch (spand::DeviceError& e) {
+        throw std::runtime_error(e.msg);
+    }
+    spand::device_scatter(dev_->device_values(), d_cmap_, (int64_t)nnz, dA_.val, stream_);
+    cuda_check(cudaGetLastError(), "assembly scatter");
+    cuda_check(cudaStreamSynchronize(stream_), "sync");
+    factored_ = false;
+    t_assemble = now_s() - t0;
+    return true;
+}
+
 void Tree::assemble_values(const double* vals, int64_t nnz, bool on_device) {
     if (!assembled_ok_ || !dev_) throw std::logic_error("assemble_values() before assemble()");
     if (nnz != (int64_t)A_.rowval.size()) throw std::invalid_argument("values do not match the assembled pattern");

@@ -73,6 +73,10 @@ class Tree {
     // (CSC order, nnz entries), from host or device memory; the plan and device work lists
     // are reused.  Device values leave the host copy of A (matrix()) unchanged.
     void assemble_values(const double* vals, int64_t nnz, bool on_device);
+    // assemble() for the pattern of the last assemble() given as raw CSC arrays: new values
+    // without building, validating or comparing a second copy of the matrix; returns false
+    // (and does nothing) when the pattern differs or nothing was assembled yet
+    bool assemble_same_pattern(int n, const int* colptr, const int* rowval, const double* vals);
     void factorize();
     // factorize() in two halves: every launch queued on the tree's stream, then the wait
     // and the status check (what factorize() does in one call)
