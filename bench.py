@@ -324,6 +324,10 @@ def run_gb300(args, rank, world, local_rank):
                 "frac": round(achieved / hbm, 4), "peak_source": peak_kind,
                 "traffic": traffic, "bytes_per_launch": dom_by / max(dom_launches, 1),
                 "avg_launch_ms": dom_avg_ms, "share_of_step": round(prof[dom]["ms"] / max(total_prof, 1e-9), 3)}
+    if dom == "qrcp":
+        # what bounds it in practice (ncu summary in profiles/qrcp_cluster_3d32.md)
+        roofline["note"] = ("latency-bound per pivot step (dependent shared-memory passes and one "
+                            "cluster barrier per column); DRAM and FMA pipes both near idle")
 
     # plain FP64 path, same workload
     fp64 = None
