@@ -229,6 +229,49 @@ def test_reassemble_same_pattern():
     assert np.linalg.norm(xt - xo) / np.linalg.norm(xo) < TOL_SOLVE
 
 
+def test_reassemble_new_pattern():
+    """assemble() with a different pattern after a first assemble() rebuilds the plan
+    (the same-pattern shortcut of the C ABI must not take it): the result equals a fresh
+    tree's, bit for bit, and going back to the first pattern does too."""
+    import scipy.sparse as sp
+    import spand_public_gb300 as pkg
+    from spand_public_gb300 import problems as P
+
+    n, dim, nl, tol = 12, 3, 5, 1e-2
+    A1 = P.neglapl(n, dim)
+    N = A1.shape[0]
+    # second pattern: A1 without the couplings (i, i+1) for i = 0 mod 3 (fewer edges keep the
+    # separators of A1's partition; the diagonal still dominates)
+    C = A1.tocoo()
+    keep = ~((np.abs(C.row - C.col) == 1) & (np.minimum(C.row, C.col) % 3 == 0))
+    A2 = sp.csc_matrix((C.data[keep], (C.row[keep], C.col[keep])), shape=(N, N))
+    A2.sort_indices()
+    assert A2.nnz < A1.nnz
+    X = P.linspace_nd(n, dim)
+
+    def fresh(A):
+        u = pkg.Tree(nl)
+        u.set_verb(False)
+        u.set_use_geo(True)
+        u.set_Xcoo(X)
+        u.set_tol(tol)
+        u.partition(A1)
+        u.assemble(A)
+        u.factorize()
+        return u
+
+    t = fresh(A1)
+    b = P.rhs(N, 1, seed=5)[:, 0]
+    for A in (A2, A1):
+        t.assemble(A)
+        t.factorize()
+        ref = fresh(A)
+        assert np.array_equal(t.ranks(), ref.ranks())
+        assert np.array_equal(t.solve(b), ref.solve(b))
+        x, it, _ = t.cg(b, iters=100, tol=1e-10)
+        assert np.linalg.norm(A @ x - b) / np.linalg.norm(b) < 1e-9
+
+
 @pytest.mark.parametrize("fp32,k", [(False, 5), (True, 5), (False, 20), (True, 20)])
 def test_cg_multi_matches_single(fp32, k):
     """Several right-hand sides at once: every column takes the iterations and reaches the
