@@ -186,11 +186,31 @@ def make_tree(A, X, args, fp32: bool):
     return t
 
 
+_ORACLE_MODE = None
+
+
+def oracle_mode():
+    """Dense kernels of the timed oracle: the CBLAS / LAPACKE of scipy's bundled OpenBLAS
+    where it can be loaded (dgemm, dsyrk, dtrsm, dpotrf, dgeqp3 -- the calls the reference
+    makes, util.cpp:122-394), on one thread like the reference's build (sequential MKL,
+    tests/Makefile:29); else the oracle's restated kernels.  Returns a description."""
+    global _ORACLE_MODE
+    if _ORACLE_MODE is None:
+        from oracle import oracle as O
+
+        path = O.use_lapack(1)
+        _ORACLE_MODE = (f"dense kernels through {os.path.basename(path)} (CBLAS/LAPACKE as the reference calls "
+                        "them), one thread like the reference's sequential-BLAS build") if path else \
+            "dense kernels restated in plain C++ (no CBLAS/LAPACKE library found), one thread"
+    return _ORACLE_MODE
+
+
 def cpu_oracle_solve(A, X, B, args):
     """The oracle (C++ restatement of the reference, one thread): factorize + CG of the first
     right-hand side.  Returns (factor s, CG s, iterations, true relative residual)."""
     from oracle.oracle import OracleTree
 
+    oracle_mode()
     o = OracleTree(args.levels)
     o.set_Xcoo(X)
     o.set_tol(args.eps)
@@ -235,8 +255,7 @@ def run_reference(args, rank, world):
             "cpu_baseline": {"value": v, "unit": "s", "cores": 1, "kind": "port",
                              "sample": f"{steps_run} factorization(s) + CG of the first RHS of the {args.n}^3 problem"
                                        f" (CG time x {args.nrhs} RHS); the reference cannot be built here (no "
-                                       "Eigen/METIS/LAPACKE), so its C++ restatement runs, single-threaded like the "
-                                       "reference"},
+                                       "Eigen/METIS/LAPACKE), so its C++ restatement runs: " + oracle_mode()},
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -367,7 +386,7 @@ def run_gb300(args, rank, world, local_rank):
         f_c, g_c, it_c, rel_c = cpu_oracle_solve(A, X, b, args)
         cpu = {"value": f_c + k * g_c, "unit": "s", "cores": 1, "kind": "port",
                "sample": f"one factorization + the CG of the first right-hand side of the same {PROBLEMS[args.problem].format(n=args.n)} problem "
-                         f"by the oracle (C++ restatement of the reference, one thread; CG time x {k} RHS): "
+                         f"by the oracle (C++ restatement of the reference; CG time x {k} RHS; {oracle_mode()}): "
                          f"{it_c} CG iterations, true relres {rel_c:.2e}"}
 
     if rank == 0:
@@ -515,6 +534,7 @@ def run_batch(args, rank, world, local_rank):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle.oracle import OracleTree
 
+        oracle_mode()
         sample = systems[:8]
         ts = 0.0
         for m, A, X, levels, b in sample:
@@ -529,8 +549,8 @@ def run_batch(args, rank, world, local_rank):
             ts += time.perf_counter() - t0
         frac = sum(s[0] ** 3 for s in sample) / sum(s[0] ** 3 for s in systems)
         cpu = {"value": ts / frac, "unit": "s", "cores": 1, "kind": "port",
-               "sample": f"factor+CG of the first {len(sample)} systems by the oracle (one thread), scaled to all "
-                         f"{args.systems} by unknown count ({frac:.3f} of the dofs)"}
+               "sample": f"factor+CG of the first {len(sample)} systems by the oracle ({oracle_mode()}), scaled to "
+                         f"all {args.systems} by unknown count ({frac:.3f} of the dofs)"}
     line = {"metric": metric(args), "value": value, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",

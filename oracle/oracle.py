@@ -26,7 +26,7 @@ def build(force: bool = False) -> str:
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
         os.makedirs(os.path.dirname(LIB), exist_ok=True)
         tmp = LIB + ".tmp"
-        subprocess.check_call(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-o", tmp, SRC])
+        subprocess.check_call(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-o", tmp, SRC, "-ldl"])
         os.replace(tmp, LIB)
     return LIB
 
@@ -64,6 +64,7 @@ def lib():
             "orc_get_op_u": (C.c_longlong, [P, I, pd]), "orc_get_op_perm": (I, [P, I, pi]),
             "orc_get_op_signs": (I, [P, I, pd]),
             "orc_set_preserve": (None, [P, I]), "orc_set_phi": (None, [P, pd, I, I]),
+            "orc_use_lapack": (I, [C.c_char_p, C.c_char_p, I]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -71,6 +72,29 @@ def lib():
             f.argtypes = args
         _lib = L
     return _lib
+
+
+def use_lapack(threads=0):
+    """Route the oracle's dense kernels through the CBLAS / LAPACKE of scipy's bundled
+    OpenBLAS, as the reference calls them (timing only: LAPACK's dgeqp3 pivots without the
+    oracle's tie rule).  threads > 0 sets OpenBLAS's thread count.  Returns the library path,
+    or None when no such library is found (the restated kernels stay in use)."""
+    import glob
+    try:
+        import scipy
+    except ImportError:
+        return None
+    base = os.path.dirname(scipy.__file__)
+    for path in sorted(glob.glob(os.path.join(base, "..", "scipy.libs", "libscipy_openblas*.so*")) +
+                       glob.glob(os.path.join(base, ".libs", "libscipy_openblas*.so*"))):
+        if lib().orc_use_lapack(path.encode(), b"scipy_", int(threads)) == 0:
+            return os.path.realpath(path)
+    return None
+
+
+def use_restated():
+    """Back to the restated kernels (the default)."""
+    lib().orc_use_lapack(None, None, 0)
 
 
 def _ip(a):

@@ -26,6 +26,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <dlfcn.h>
 #include <functional>
 #include <limits>
 #include <list>
@@ -86,9 +87,33 @@ static double nrm2(int n, const double* x) {
     return scale * std::sqrt(ssq);
 }
 
+// ---------------------------------------------------------------------------------
+// Optional BLAS / LAPACK (timing only).  The reference calls cblas / LAPACKE for its dense
+// kernels (util.cpp:122-394).  For the timed CPU baseline the oracle can do the same through
+// a CBLAS / LAPACKE library loaded at run time (orc_use_lapack); the parity checks keep the
+// restated kernels below, whose QRCP pivots follow the deterministic tie rule.
+// ---------------------------------------------------------------------------------
+namespace lapk {
+using gemm_t = void (*)(int, int, int, int, int, int, double, const double*, int, const double*, int, double,
+                        double*, int);
+using syrk_t = void (*)(int, int, int, int, int, double, const double*, int, double, double*, int);
+using trsm_t = void (*)(int, int, int, int, int, int, int, double, const double*, int, double*, int);
+using potrf_t = int (*)(int, char, int, double*, int);
+using geqp3_t = int (*)(int, int, int, double*, int, int*, double*);
+using threads_t = void (*)(int);
+static gemm_t gemm = nullptr;
+static syrk_t syrk = nullptr;
+static trsm_t trsm = nullptr;
+static potrf_t potrf = nullptr;
+static geqp3_t geqp3 = nullptr;
+// CBLAS / LAPACKE enumerators (public cblas.h / lapacke.h)
+enum { ColMajor = 102, NoTrans = 111, Trans = 112, Upper = 121, Lower = 122, NonUnit = 131, Left = 141, Right = 142 };
+}  // namespace lapk
+
 // Lower Cholesky, A = L L^T in place (dpotrf 'L'); util.cpp:158-165.  Returns LAPACK info.
 static int potf(Mat& A) {
     int n = A.r;
+    if (lapk::potrf) return n ? lapk::potrf(lapk::ColMajor, 'L', n, A.v.data(), n) : 0;
     for (int j = 0; j < n; j++) {
         double ajj = A(j, j);
         if (!(ajj > 0.0) || std::isnan(ajj)) return j + 1;
@@ -109,6 +134,12 @@ static int potf(Mat& A) {
 // B <- L^{-1} B, L lower non-unit (dtrsm Left Lower NoTrans); util.cpp:266-274.
 static void trsm_left_lower(const Mat& L, Mat& B) {
     int m = B.r, n = B.c;
+    if (lapk::trsm) {
+        if (m && n)
+            lapk::trsm(lapk::ColMajor, lapk::Left, lapk::Lower, lapk::NoTrans, lapk::NonUnit, m, n, 1.0, L.v.data(), L.r,
+                       B.v.data(), m);
+        return;
+    }
     for (int j = 0; j < n; j++) {
         double* b = B.col(j);
         for (int k = 0; k < m; k++) {
@@ -124,6 +155,12 @@ static void trsm_left_lower(const Mat& L, Mat& B) {
 // B <- B L^{-T}, L lower non-unit (dtrsm Right Lower Trans); util.cpp:256-264.
 static void trsm_right_lower_trans(const Mat& L, Mat& B) {
     int m = B.r, n = B.c;
+    if (lapk::trsm) {
+        if (m && n)
+            lapk::trsm(lapk::ColMajor, lapk::Right, lapk::Lower, lapk::Trans, lapk::NonUnit, m, n, 1.0, L.v.data(), L.r,
+                       B.v.data(), m);
+        return;
+    }
     for (int j = 0; j < n; j++) {
         double* bj = B.col(j);
         double d = 1.0 / L(j, j);
@@ -140,6 +177,12 @@ static void trsm_right_lower_trans(const Mat& L, Mat& B) {
 // B <- B U^{-1}, U upper non-unit (dtrsm Right Upper NoTrans).
 static void trsm_right_upper(const Mat& U, Mat& B) {
     int m = B.r, n = B.c;
+    if (lapk::trsm) {
+        if (m && n)
+            lapk::trsm(lapk::ColMajor, lapk::Right, lapk::Upper, lapk::NoTrans, lapk::NonUnit, m, n, 1.0, U.v.data(), U.r,
+                       B.v.data(), m);
+        return;
+    }
     for (int j = 0; j < n; j++) {
         double* bj = B.col(j);
         for (int k = 0; k < j; k++) {
@@ -158,6 +201,11 @@ static void gemm_sub(const Mat& A, bool tA, const Mat& B, bool tB, Mat& C) {
     int m = C.r, n = C.c;
     int k = tA ? A.r : A.c;
     if (m == 0 || n == 0 || k == 0) return;
+    if (lapk::gemm) {
+        lapk::gemm(lapk::ColMajor, tA ? lapk::Trans : lapk::NoTrans, tB ? lapk::Trans : lapk::NoTrans, m, n, k, -1.0,
+                   A.v.data(), A.r, B.v.data(), B.r, 1.0, C.v.data(), m);
+        return;
+    }
     for (int j = 0; j < n; j++) {
         double* cj = C.col(j);
         if (!tA) {
@@ -188,6 +236,11 @@ static void syrk_sub_lower(const Mat& A, bool tA, Mat& C) {
     int n = C.r;
     int k = tA ? A.r : A.c;
     if (n == 0 || k == 0) return;
+    if (lapk::syrk) {
+        lapk::syrk(lapk::ColMajor, lapk::Lower, tA ? lapk::Trans : lapk::NoTrans, n, k, -1.0, A.v.data(), A.r, 1.0,
+                   C.v.data(), n);
+        return;
+    }
     for (int j = 0; j < n; j++) {
         double* cj = C.col(j);
         if (!tA) {
@@ -296,6 +349,12 @@ static void geqp3(Mat& A, std::vector<int>& jpvt, std::vector<double>& tau) {
     jpvt.resize(n);
     tau.assign(std::min(m, n), 0.0);
     if (m == 0 || n == 0) return;
+    if (lapk::geqp3) {  // LAPACK's own pivot choice (no tie rule): timing only
+        std::fill(jpvt.begin(), jpvt.end(), 0);
+        lapk::geqp3(lapk::ColMajor, m, n, A.v.data(), m, jpvt.data(), tau.data());
+        for (int& j : jpvt) j -= 1;
+        return;
+    }
     for (int j = 0; j < n; j++) jpvt[j] = j;
     std::vector<double> vn1(n), vn2(n), work(n);
     for (int j = 0; j < n; j++) { vn1[j] = nrm2(m, A.col(j)); vn2[j] = vn1[j]; }
@@ -2045,6 +2104,40 @@ void orc_set_skip(void* p, int skip) { ((OrcHandle*)p)->t->skip = skip; }
 void orc_set_symm_kind(void* p, int k) { ((OrcHandle*)p)->t->symm = k; }
 void orc_set_scaling_kind(void* p, int k) { ((OrcHandle*)p)->t->scale_kind = k; }
 void orc_set_use_sparsify(void* p, int u) { ((OrcHandle*)p)->t->use_want_sparsify = u != 0; }
+// Load CBLAS / LAPACKE entry points from a shared library (names with the given prefix,
+// e.g. "scipy_" for scipy's bundled OpenBLAS) and route the dense kernels through them;
+// threads > 0 sets the library's thread count when it exports <prefix>openblas_set_num_threads.
+// path == nullptr: back to the restated kernels.  Returns 0, or -1 when a symbol is missing.
+int orc_use_lapack(const char* path, const char* prefix, int threads) {
+    if (!path) {
+        lapk::gemm = nullptr;
+        lapk::syrk = nullptr;
+        lapk::trsm = nullptr;
+        lapk::potrf = nullptr;
+        lapk::geqp3 = nullptr;
+        return 0;
+    }
+    void* h = dlopen(path, RTLD_NOW | RTLD_LOCAL);
+    if (!h) return -1;
+    const std::string pre = prefix ? prefix : "";
+    auto sym = [&](const char* name) { return dlsym(h, (pre + name).c_str()); };
+    auto g = (lapk::gemm_t)sym("cblas_dgemm");
+    auto s = (lapk::syrk_t)sym("cblas_dsyrk");
+    auto t = (lapk::trsm_t)sym("cblas_dtrsm");
+    auto p = (lapk::potrf_t)sym("LAPACKE_dpotrf");
+    auto q = (lapk::geqp3_t)sym("LAPACKE_dgeqp3");
+    if (!g || !s || !t || !p || !q) return -1;
+    if (threads > 0) {
+        auto nt = (lapk::threads_t)sym("openblas_set_num_threads");
+        if (nt) nt(threads);
+    }
+    lapk::gemm = g;
+    lapk::syrk = s;
+    lapk::trsm = t;
+    lapk::potrf = p;
+    lapk::geqp3 = q;
+    return 0;
+}
 void orc_set_preserve(void* p, int on) { ((OrcHandle*)p)->t->preserve = on != 0; }
 // phi: n x nphi, column-major, natural ordering (copied)
 void orc_set_phi(void* p, const double* phi, int n, int nphi) {
