@@ -65,6 +65,8 @@ def lib():
             "orc_get_op_signs": (I, [P, I, pd]),
             "orc_set_preserve": (None, [P, I]), "orc_set_phi": (None, [P, pd, I, I]),
             "orc_use_lapack": (I, [C.c_char_p, C.c_char_p, I]),
+            "orc_partition_lorasp": (I, [P, I, pi, pi]), "orc_get_rb_parts": (None, [P, pi]),
+            "orc_factorize_lorasp": (I, [P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -167,6 +169,23 @@ class OracleTree:
 
     def factorize(self):
         if self.L.orc_factorize(self.h) != 0:
+            raise RuntimeError(self._err())
+
+    def partition_lorasp(self, A):
+        """LoRaSp ordering (tree.cpp:421-503): recursive bisection; returns the part of every dof."""
+        A = A.tocsc()
+        self.n = A.shape[0]
+        cp = np.ascontiguousarray(A.indptr, dtype=np.int32)
+        rv = np.ascontiguousarray(A.indices, dtype=np.int32)
+        if self.L.orc_partition_lorasp(self.h, self.n, _ip(cp), _ip(rv)) != 0:
+            raise RuntimeError(self._err())
+        out = np.zeros(self.n, dtype=np.int32)
+        self.L.orc_get_rb_parts(self.h, _ip(out))
+        return out
+
+    def factorize_lorasp(self):
+        """tree.cpp:1553-1608 (SPD / LLT)."""
+        if self.L.orc_factorize_lorasp(self.h) != 0:
             raise RuntimeError(self._err())
 
     def solve(self, x):

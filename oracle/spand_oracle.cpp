@@ -759,6 +759,43 @@ static void partition_nd_geo(const std::vector<int>& colptr, const std::vector<i
 }
 
 // Modified nested dissection; partition.cpp:384-478 (geometric branch).
+// partition.cpp:99-137: cut the widest coordinate at the value of the middle dof after
+// sorting by it; dofs at or below go to part start, the others to start + 1
+static void bissect_geo(const std::vector<int>& dofs, std::vector<int>& parts, const double* X, int dim, int start) {
+    const int N = (int)dofs.size();
+    if (N == 0) return;
+    int bestdim = -1;
+    double maxrange = -1.0;
+    for (int d = 0; d < dim; d++) {
+        double maxi = std::numeric_limits<double>::lowest(), mini = std::numeric_limits<double>::max();
+        for (int idof : dofs) {
+            maxi = std::max(maxi, X[d + (size_t)dim * idof]);
+            mini = std::min(mini, X[d + (size_t)dim * idof]);
+        }
+        if (maxi - mini > maxrange) {
+            bestdim = d;
+            maxrange = maxi - mini;
+        }
+    }
+    std::vector<int> tmp = dofs;
+    std::sort(tmp.begin(), tmp.end(),
+              [&](int i, int j) { return X[bestdim + (size_t)dim * i] < X[bestdim + (size_t)dim * j]; });
+    const double midv = X[bestdim + (size_t)dim * tmp[N / 2]];
+    for (int j : dofs) parts[j] = X[bestdim + (size_t)dim * j] <= midv ? start : start + 1;
+}
+
+// partition.cpp:245-285, geometric branch: nlevels - 1 rounds of bisection of every part
+static std::vector<int> partition_RB(int N, int nlevels, const double* X, int dim) {
+    std::vector<int> parts(N, 0);
+    for (int depth = 0; depth < nlevels - 1; depth++) {
+        const int np = 1 << depth;
+        std::vector<std::vector<int>> dofs(np);
+        for (int i = 0; i < N; i++) dofs[parts[i]].push_back(i);
+        for (int k = 0; k < np; k++) bissect_geo(dofs[k], parts, X, dim, 2 * k);
+    }
+    return parts;
+}
+
 static std::vector<ClusterID> partition_modifiedND(const CSC& A, int nlevels, const double* X, int dim) {
     int N = A.n;
     // SpMat2CSC: the graph without self loops (partition.cpp:21-39)
@@ -1180,6 +1217,53 @@ struct Tree {
         t_partition = now_s() - t0;
     }
 
+    // LoRaSp ordering (tree.cpp:421-503): recursive bisection; every cluster sits at the top
+    // level (none is eliminated as an interior), pairs of consecutive clusters merge
+    std::vector<int> rb_parts;  // natural ordering
+    bool lorasp = false;
+    void partition_lorasp(const CSC& A) {
+        double t0 = now_s();
+        const int N = A.n;
+        if (!geo) throw std::runtime_error("oracle: algebraic (METIS) ordering is not restated; set geometry");
+        rb_parts = partition_RB(N, nlevels, X, dim);
+        const std::vector<int>& parts = rb_parts;
+        perm.resize(N);
+        std::iota(perm.begin(), perm.end(), 0);
+        std::sort(perm.begin(), perm.end(), [&parts](int i, int j) { return parts[i] < parts[j]; });
+        std::map<Cluster*, int> cid;
+        const int lvltop = nlevels - 1;
+        for (int k = 0; k < N;) {
+            int knext = k + 1;
+            const int id = parts[perm[k]];
+            while (knext < N && parts[perm[knext]] == id) knext++;
+            auto self = std::make_unique<Cluster>(k, knext - k, lvltop, get_new_order(), true);
+            cid[self.get()] = self->order;
+            bottoms[0].push_back(std::move(self));
+            k = knext;
+        }
+        for (int lvl = 1; lvl < nlevels; lvl++) {
+            auto k = bottoms[lvl - 1].begin();
+            const auto end = bottoms[lvl - 1].end();
+            while (k != end) {
+                const int idp = cid.at(k->get()) / 2;
+                std::vector<Cluster*> ch{k->get()};
+                int cstart = (*k)->start, csize = (*k)->size;
+                ++k;
+                while (k != end && cid.at(k->get()) / 2 == idp) {
+                    ch.push_back(k->get());
+                    csize += (*k)->size;
+                    ++k;
+                }
+                auto parent = std::make_unique<Cluster>(cstart, csize, lvltop, get_new_order(), true);
+                for (auto c : ch) { c->parent = parent.get(); parent->children.push_back(c); }
+                cid[parent.get()] = idp;
+                bottoms[lvl].push_back(std::move(parent));
+            }
+        }
+        lorasp = true;
+        t_partition = now_s() - t0;
+    }
+
     // tree.cpp:505-575
     void assemble(const CSC& A) {
         double t0 = now_s();
@@ -1469,7 +1553,11 @@ struct Tree {
     // AsnP == nullptr: the preservation branch (pred == false, keep_sibling == false):
     // phi and every edge block get Q^T (in-edges and phi from the left, out-edges from the
     // right) and keep their first osize rows / columns; the sibling gets no edge.
-    Cluster* shrink_split(Cluster* original, int osize, Mat* AsnP, const Mat& v, const std::vector<double>& h) {
+    // farfield (LoRaSp, tree.cpp:1411-1415: pred = !original, keep_sibling == true): the
+    // fill-in edges take AsnP, the original ones get Q^T and hand their last rows /
+    // columns to a new edge neighbour -> sibling (tree.cpp:1018-1064).
+    Cluster* shrink_split(Cluster* original, int osize, Mat* AsnP, const Mat& v, const std::vector<double>& h,
+                          bool farfield = false) {
         const int n0 = original->size;
         int sib_size = original->size - osize;
         auto psib = std::make_unique<Cluster>(original->start + osize, sib_size, original->level, get_new_order(),
@@ -1486,8 +1574,24 @@ struct Tree {
         };
         if (preserve) qt_rows(*original->phi);  // tree.cpp:993-1002
         int col = 0;
+        auto keep_tail = [&](Cluster* n, const Mat& Qt, bool orig) {  // Qt: n0 x n, rows osize.. -> sibling
+            auto S = std::make_unique<Mat>(sib_size, Qt.c);
+            for (int j = 0; j < Qt.c; j++)
+                for (int i = 0; i < sib_size; i++) (*S)(i, j) = Qt(osize + i, j);
+            n->add_edge(std::make_unique<Edge>(Edge{n, sib, std::move(S), orig}));
+        };
         for (auto e : original->in_nbr()) {
             int cols = e->n1->size;
+            if (farfield && e->original) {
+                Mat& B = *e->A;
+                for (int j = 0; j < B.c; j++) ormqr_vec(v, h, k, B.col(j), true);
+                keep_tail(e->n1, B, true);
+                Mat T(osize, B.c);
+                for (int j = 0; j < B.c; j++)
+                    for (int i = 0; i < osize; i++) T(i, j) = B(i, j);
+                B = std::move(T);
+                continue;
+            }
             if (!AsnP) {
                 qt_rows(*e->A);
                 continue;
@@ -1500,6 +1604,19 @@ struct Tree {
         }
         for (auto e : original->out_nbr()) {
             int cols = e->n2->size;
+            if (farfield && e->original) {  // A Q, row by row as Q^T A^T
+                Mat& B = *e->A;
+                Mat Bt(B.c, B.r);
+                for (int j = 0; j < B.c; j++)
+                    for (int i = 0; i < B.r; i++) Bt(j, i) = B(i, j);
+                for (int j = 0; j < Bt.c; j++) ormqr_vec(v, h, k, Bt.col(j), true);
+                keep_tail(e->n2, Bt, true);
+                Mat M(B.r, osize);
+                for (int j = 0; j < osize; j++)
+                    for (int i = 0; i < B.r; i++) M(i, j) = Bt(j, i);
+                B = std::move(M);
+                continue;
+            }
             if (!AsnP) {  // A Q, row by row as Q^T A^T
                 Mat& B = *e->A;
                 Mat Bt(B.c, B.r);
@@ -1689,6 +1806,75 @@ struct Tree {
         geqrf(*V, h);
         rank_log.push_back({ilvl, self->order, rows, rank});
         record_q_and_split(self, std::move(V), std::move(h));
+    }
+    // LoRaSp sparsification (tree.cpp:1292-1347 with pred = !original, tree.cpp:1411-1415):
+    // the QRCP sees only the fill-in edges; the original edges keep their coupling to the
+    // sibling, whose elimination then updates the cluster's neighbours
+    void sparsify_farfield(Cluster* self) {
+        const int rows = self->size;
+        std::vector<Edge*> ins, outs;
+        for (auto e : self->in_nbr())
+            if (!e->original) ins.push_back(e);
+        for (auto e : self->out_nbr())
+            if (!e->original) outs.push_back(e);
+        int cols = 0;
+        for (auto e : ins) cols += e->n1->size;
+        for (auto e : outs) cols += e->n2->size;
+        Mat Asn(rows, cols);
+        int c = 0;
+        for (auto e : ins) {
+            for (int j = 0; j < e->n1->size; j++)
+                for (int i = 0; i < rows; i++) Asn(i, c + j) = (*e->A)(i, j);
+            c += e->n1->size;
+        }
+        for (auto e : outs) {
+            for (int j = 0; j < e->n2->size; j++)
+                for (int i = 0; i < rows; i++) Asn(i, c + j) = (*e->A)(j, i);
+            c += e->n2->size;
+        }
+        log[ilvl].nbrs.add(cols);
+        std::vector<int> jpvt;
+        std::vector<double> ht;
+        geqp3(Asn, jpvt, ht);
+        std::vector<double> diag(std::min(rows, cols));
+        for (size_t i = 0; i < diag.size(); i++) diag[i] = Asn((int)i, (int)i);
+        const int rank = choose_rank(diag, tol);
+        rank_log.push_back({ilvl, self->order, rows, std::min(rank, rows)});
+        if (rank >= rows) return;
+        auto v = std::make_unique<Mat>(rows, rank);
+        for (int j = 0; j < rank; j++)
+            for (int i = 0; i < rows; i++) (*v)(i, j) = Asn(i, j);
+        auto op = make_op(OP_ORTHOGONAL, self, nullptr, std::move(v));
+        op->h.assign(ht.begin(), ht.begin() + rank);
+        const Op* qop = op.get();
+        push_op(std::move(op));
+        Mat AsnP(rank, cols);
+        for (int j = 0; j < cols; j++)
+            for (int i = 0; i < rank && i <= j; i++) AsnP(i, jpvt[j]) = Asn(i, j);
+        Cluster* sib = shrink_split(self, rank, &AsnP, *qop->A, qop->h, true);
+        eliminate_cluster(sib);
+    }
+    // tree.cpp:1553-1608 (SPD / LLT): per level every cluster is scaled and sparsified in
+    // list order, then the level merges; nothing is eliminated as an interior
+    void factorize_lorasp() {
+        if (!lorasp) throw std::runtime_error("factorize_lorasp() needs partition_lorasp()");
+        if (symm != SPD || scale_kind != S_LLT || preserve)
+            throw std::runtime_error("oracle: LoRaSp is restated for SPD / LLT without preservation");
+        double t0 = now_s();
+        for (ilvl = 0; ilvl < nlevels; ilvl++) {
+            std::vector<Cluster*> cl;
+            for (auto& s : bottom_current()) cl.push_back(s.get());
+            for (auto s : cl) {
+                scale_cluster(s);
+                log[ilvl].rank_before.add(s->size);
+                sparsify_farfield(s);
+                log[ilvl].rank_after.add(s->size);
+            }
+            if (ilvl < nlevels - 1) merge_all();
+            log[ilvl].dofs_left_spars = ndofs_left();
+            log[ilvl].fact_nnz = nnz();
+        }
+        t_factorize = now_s() - t0;
     }
     void sparsify_cluster(Cluster* self) {  // tree.cpp:1417-1433
         if (!use_want_sparsify || self->sparsify) {
@@ -2198,6 +2384,24 @@ int orc_trailing(void* p, int* I, int* J, double* V) {
     ((OrcHandle*)p)->t->trailing(i, j, v);
     if (I) { std::copy(i.begin(), i.end(), I); std::copy(j.begin(), j.end(), J); std::copy(v.begin(), v.end(), V); }
     return (int)i.size();
+}
+int orc_partition_lorasp(void* p, int n, const int* colptr, const int* rowval) {
+    auto h = (OrcHandle*)p;
+    try {
+        h->t->partition_lorasp(make_csc(n, colptr, rowval, nullptr));
+    } catch (std::exception& e) { h->err = e.what(); return -1; }
+    return 0;
+}
+void orc_get_rb_parts(void* p, int* out) {
+    auto& r = ((OrcHandle*)p)->t->rb_parts;
+    std::copy(r.begin(), r.end(), out);
+}
+int orc_factorize_lorasp(void* p) {
+    auto h = (OrcHandle*)p;
+    try {
+        h->t->factorize_lorasp();
+    } catch (std::exception& e) { h->err = e.what(); return -1; }
+    return 0;
 }
 int orc_factorize(void* p) {
     auto h = (OrcHandle*)p;

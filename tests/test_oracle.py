@@ -103,13 +103,17 @@ def test_assembly_consistency(dim, n):
     A = P.neglapl(n, dim)
     X = P.linspace_nd(n, dim)
     for nlevels in range(2, 5):
-        t = O.OracleTree(nlevels)
-        t.set_Xcoo(X)
-        t.partition(A)
-        t.assemble(A)
-        p = t.get_assembly_perm()
-        ref = A[p][:, p]
-        assert abs(ref - t.trailing()).max() == 0.0
+        for lorasp in (False, True):  # the reference loops over partition / partition_lorasp
+            t = O.OracleTree(nlevels)
+            t.set_Xcoo(X)
+            if lorasp:
+                t.partition_lorasp(A)
+            else:
+                t.partition(A)
+            t.assemble(A)
+            p = t.get_assembly_perm()
+            ref = A[p][:, p]
+            assert abs(ref - t.trailing()).max() == 0.0
 
 
 def test_swap2perm_via_getf(golden):
@@ -369,3 +373,30 @@ def test_preservation(dim, n):
                         x = t.solve(b)
                         err = np.linalg.norm(A @ x - b) / np.linalg.norm(b)
                         assert err < (1e-12 if tol == 0.0 else tol * 1e2), (nlevels, tol, skip, symm, err)
+
+
+@pytest.mark.parametrize("dim,n", [(2, 5), (2, 10), (2, 20), (2, 32), (3, 5), (3, 10)])
+def test_lorasp(dim, n):
+    """LoRaSp (partition_lorasp tree.cpp:421-503, factorize_lorasp tree.cpp:1553-1608): the
+    recursive bisection gives 2^(nlevels-1) parts of sizes within one of each other on a
+    grid; the factorization is exact at tol 0 (ApproxTest.Exact's bar, 1e-10) and within
+    tol * 1e2 otherwise (ApproxTest.Approx's bar); PCG converges."""
+    A = P.neglapl(n, dim)
+    X = P.linspace_nd(n, dim)
+    N = A.shape[0]
+    for nlevels in (2, 3, 4):
+        for tol in (0.0, 1e-4, 1e-2):
+            t = O.OracleTree(nlevels)
+            t.set_Xcoo(X)
+            t.set_tol(tol)
+            parts = t.partition_lorasp(A)
+            sizes = np.bincount(parts, minlength=2 ** (nlevels - 1))
+            assert sizes.size == 2 ** (nlevels - 1)
+            t.assemble(A)
+            t.factorize_lorasp()
+            b = np.random.default_rng(nlevels).uniform(-1, 1, N)
+            x = t.solve(b)
+            err = np.linalg.norm(A @ x - b) / np.linalg.norm(b)
+            assert err <= (1e-10 if tol == 0.0 else tol * 1e2), (nlevels, tol, err)
+            x, it = t.cg(b, 100, 1e-10)[:2]
+            assert np.linalg.norm(A @ x - b) / np.linalg.norm(b) < 1e-9
