@@ -67,6 +67,12 @@ int spand_tree_set_fp32(spand_tree* t, int fp32);
  * self.lvl self.sep l.lvl l.sep r.lvl r.sep. */
 int spand_tree_partition(spand_tree* t, int n, const int* colptr, const int* rowval, int* sepids);
 
+/* void partition_lorasp(SpMat&)                    -- include/tree.h:177, src/tree.cpp:421-503
+ * LoRaSp ordering: geometric recursive bisection (coordinates required).  parts (optional,
+ * n ints): the part of every dof, natural ordering.  Then spand_tree_assemble and
+ * spand_tree_factorize_lorasp (SPD / LLT). */
+int spand_tree_partition_lorasp(spand_tree* t, int n, const int* colptr, const int* rowval, int* parts);
+
 /* void assemble(SpMat&)                            -- include/tree.h:182, src/tree.cpp:505-575
  * Also builds the symbolic plan of the factorization and uploads the blocks. */
 int spand_tree_assemble(spand_tree* t, int n, const int* colptr, const int* rowval, const double* vals);
@@ -79,6 +85,8 @@ int spand_tree_assemble_values(spand_tree* t, const double* vals, long long nnz,
 
 /* void factorize()                                 -- include/tree.h:186, src/tree.cpp:1447-1551 */
 int spand_tree_factorize(spand_tree* t);
+/* void factorize_lorasp()                          -- include/tree.h:187, src/tree.cpp:1553-1608 */
+int spand_tree_factorize_lorasp(spand_tree* t);
 
 /* void solve(Eigen::VectorXd&) const               -- include/tree.h:192, src/tree.cpp:1610-1635
  * x: host buffer n x nrhs (leading dimension ld >= n), natural ordering, in place. */

@@ -49,6 +49,8 @@ _PROTOS = {
     "spand_tree_set_preserve": (C.c_int, [C.c_void_p, C.c_int]),
     "spand_tree_set_phi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
     "spand_tree_partition": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "spand_tree_partition_lorasp": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "spand_tree_factorize_lorasp": (C.c_int, [C.c_void_p]),
     "spand_tree_assemble": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "spand_tree_factorize": (C.c_int, [C.c_void_p]),
     "spand_tree_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
@@ -219,6 +221,18 @@ class Tree:
         _check(self.L.spand_tree_partition(self.h, n, _ptr(cp), _ptr(rv), _ptr(out)))
         self.n = n
         return out
+
+    def partition_lorasp(self, A):
+        """LoRaSp ordering (include/tree.h:177): returns the part of every dof."""
+        n, cp, rv, _ = _csc(A)
+        out = np.zeros(n, dtype=np.int32)
+        _check(self.L.spand_tree_partition_lorasp(self.h, n, _ptr(cp), _ptr(rv), _ptr(out)))
+        self.n = n
+        return out
+
+    def factorize_lorasp(self):
+        """include/tree.h:187 (SPD / LLT)."""
+        _check(self.L.spand_tree_factorize_lorasp(self.h))
 
     def assemble(self, A):
         n, cp, rv, vv = _csc(A)

@@ -137,6 +137,14 @@ int spand_tree_partition(spand_tree* t, int n, const int* colptr, const int* row
     });
 }
 
+int spand_tree_partition_lorasp(spand_tree* t, int n, const int* colptr, const int* rowval, int* parts) {
+    CHECK_T(t);
+    return guard([&] {
+        auto p = t->t->partition_lorasp(make_csc(n, colptr, rowval, nullptr));
+        if (parts) std::copy(p.begin(), p.end(), parts);
+    });
+}
+
 int spand_tree_assemble(spand_tree* t, int n, const int* colptr, const int* rowval, const double* vals) {
     CHECK_T(t);
     if (!vals) return fail(SPAND_ERR_ARG, "null values");
@@ -148,6 +156,11 @@ int spand_tree_assemble(spand_tree* t, int n, const int* colptr, const int* rowv
 int spand_tree_factorize(spand_tree* t) {
     CHECK_T(t);
     return guard([&] { t->t->factorize(); });
+}
+
+int spand_tree_factorize_lorasp(spand_tree* t) {
+    CHECK_T(t);
+    return guard([&] { t->t->factorize_lorasp(); });
 }
 
 int spand_tree_solve(spand_tree* t, double* x, int nrhs, int ld) {

@@ -222,6 +222,96 @@ Hierarchy build_hierarchy(const std::vector<ClusterID>& part, int nlevels, std::
     return H;
 }
 
+// ------------------------------------------------------------------------------------
+// LoRaSp ordering and hierarchy
+// ------------------------------------------------------------------------------------
+// partition.cpp:99-137: the widest coordinate of the part, cut at the value of its middle
+// dof in that coordinate (dofs at or below it go to part start, the others to start + 1)
+static void rb_bisect(const std::vector<int>& dofs, std::vector<int>& parts, const double* X, int dim, int start) {
+    const int N = (int)dofs.size();
+    if (N == 0) return;
+    int axis = -1;
+    double widest = -1.0;
+    for (int d = 0; d < dim; d++) {
+        double hi = std::numeric_limits<double>::lowest(), lo = std::numeric_limits<double>::max();
+        for (int v : dofs) {
+            hi = std::max(hi, X[d + (size_t)dim * v]);
+            lo = std::min(lo, X[d + (size_t)dim * v]);
+        }
+        if (hi - lo > widest) {
+            widest = hi - lo;
+            axis = d;
+        }
+    }
+    std::vector<double> coord(N);
+    for (int i = 0; i < N; i++) coord[i] = X[axis + (size_t)dim * dofs[i]];
+    std::nth_element(coord.begin(), coord.begin() + N / 2, coord.end());
+    const double cut = coord[N / 2];  // the value of the middle dof once sorted
+    for (int v : dofs) parts[v] = X[axis + (size_t)dim * v] <= cut ? start : start + 1;
+}
+
+// partition.cpp:245-285, geometric branch
+std::vector<int> partition_rb(int n, int nlevels, const double* X, int dim) {
+    std::vector<int> parts(n, 0);
+    for (int depth = 0; depth + 1 < nlevels; depth++) {
+        const int np = 1 << depth;
+        std::vector<std::vector<int>> dofs(np);
+        for (int i = 0; i < n; i++) dofs[parts[i]].push_back(i);
+        for (int k = 0; k < np; k++) rb_bisect(dofs[k], parts, X, dim, 2 * k);
+    }
+    return parts;
+}
+
+// tree.cpp:421-503.  The dofs are sorted by part with std::sort (not stable), as the
+// reference does: the order inside a part is then that of the standard library's sort.
+Hierarchy build_hierarchy_lorasp(const std::vector<int>& parts, int nlevels, std::vector<int>& perm) {
+    const int N = (int)parts.size();
+    Hierarchy H;
+    H.nlevels = nlevels;
+    H.bottoms.resize(nlevels);
+    perm.resize(N);
+    std::iota(perm.begin(), perm.end(), 0);
+    std::sort(perm.begin(), perm.end(), [&parts](int i, int j) { return parts[i] < parts[j]; });
+    const int top = nlevels - 1;
+    std::vector<int> id;  // per cluster: its order (leaves), then the parent id (order / 2 upwards)
+    auto add = [&](int start, int size, int hl) {
+        H.start.push_back(start);
+        H.size.push_back(size);
+        H.level.push_back(top);
+        H.sparsify.push_back(1);
+        H.parent.push_back(-1);
+        H.hlevel.push_back(hl);
+        H.children.emplace_back();
+        return (int)H.start.size() - 1;
+    };
+    for (int k = 0; k < N;) {
+        int e = k + 1;
+        while (e < N && parts[perm[e]] == parts[perm[k]]) e++;
+        const int c = add(k, e - k, 0);
+        id.push_back(c);
+        H.bottoms[0].push_back(c);
+        k = e;
+    }
+    for (int lvl = 1; lvl < nlevels; lvl++) {
+        const std::vector<int>& prev = H.bottoms[lvl - 1];
+        for (size_t i = 0; i < prev.size();) {
+            const int pid = id[prev[i]] / 2;
+            size_t e = i + 1;
+            int size = H.size[prev[i]];
+            while (e < prev.size() && id[prev[e]] / 2 == pid) size += H.size[prev[e++]];
+            const int c = add(H.start[prev[i]], size, lvl);
+            id.push_back(pid);
+            for (size_t j = i; j < e; j++) {
+                H.parent[prev[j]] = c;
+                H.children[c].push_back(prev[j]);
+            }
+            H.bottoms[lvl].push_back(c);
+            i = e;
+        }
+    }
+    return H;
+}
+
 // A[p,p] (util.cpp:519-546)
 Csc symm_perm(const Csc& A, const std::vector<int>& perm) {
     const int n = A.n;
@@ -291,6 +381,7 @@ struct SymTree {
     const Hierarchy& H;
     Plan& P;
     std::vector<SymEdge> edges;
+    std::vector<char> orig;  // per edge: an original (assembled) coupling, or merged from one
     std::vector<std::list<int>> out, in;  // per cluster: edge ids (out: pivot first)
     std::vector<char> eliminated;
 
@@ -311,8 +402,9 @@ struct SymTree {
         return (int)P.blocks.size() - 1;
     }
     // cluster.cpp:113-123
-    int add_edge(int n1, int n2, int block) {
+    int add_edge(int n1, int n2, int block, bool original = true) {
         edges.push_back({n1, n2, block});
+        orig.push_back(original ? 1 : 0);
         int e = (int)edges.size() - 1;
         if (n1 == n2) {
             out[n1].push_front(e);
@@ -593,6 +685,243 @@ Plan build_plan(const Hierarchy& H, const Assembly& asmb, int skip, bool use_wan
     P.arena_len = cursor;
     P.nclusters_h = nc;
     P.nclusters = (int)P.c_cap.size();  // with the LDLT siblings
+    return P;
+}
+
+// tree.cpp:1553-1608 for SPD / LLT.  Per level, every cluster in list order: scale
+// (tree.cpp:796-811), then sparsify over its fill-in edges (tree.cpp:1292-1347 with pred =
+// !original, 1411-1415): the QRCP's edges take R P^T, the original edges get Q^T and hand
+// their last rows to a sibling edge (tree.cpp:1018-1064), and the sibling (identity pivot)
+// is eliminated at once, updating its neighbours (tree.cpp:895-910).  The sibling is
+// planned whatever the rank; a rank equal to the size gives it no rows, and the fill-in
+// blocks it would have created stay zero (the reference creates none: only extra zero
+// columns of later QRCP matrices, which never change a rank for tol > 0).  Clusters of a
+// level are scheduled in waves (each after every neighbour processed before it, fill-in
+// included); every wave is one level of the plan.
+Plan build_plan_lorasp(const Hierarchy& H, const Assembly& asmb) {
+    Plan P;
+    P.lorasp = true;
+    const int nl = H.nlevels;
+    const int nc = (int)H.start.size();
+    P.nclusters = nc;
+    P.c_start = H.start;
+    P.c_cap = H.size;
+    P.c_level = H.level;
+    P.c_hlevel = H.hlevel;
+    P.c_parent = H.parent;
+    P.c_sparsify = H.sparsify;
+    P.c_children = H.children;
+    P.c_order.resize(nc);
+    std::iota(P.c_order.begin(), P.c_order.end(), 0);
+    P.c_xoff.resize(nc);
+    for (int c = 0; c < nc; c++) {
+        P.c_xoff[c] = P.x_len;
+        P.x_len += H.size[c];
+    }
+    SymTree T(H, P);
+    int64_t cursor = 0;
+    for (size_t li = 0; li < H.bottoms[0].size(); li++) {
+        int self = H.bottoms[0][li];
+        for (int nbr : asmb.nbrs[li]) {
+            int b = T.new_block(nbr, self, BLK_STORED, cursor);
+            P.initial_blocks.push_back(b);
+            T.add_edge(self, nbr, b, true);
+        }
+        T.sort_edges(self);
+    }
+    P.assembled_len = cursor;
+    P.lr_order.resize(nl);
+    std::vector<int> wave_of;  // per cluster, this level
+    for (int ilvl = 0; ilvl < nl; ilvl++) {
+        const std::vector<int>& bottom = H.bottoms[ilvl];
+        const size_t first = P.levels.size();
+        wave_of.assign(P.c_cap.size(), -1);
+        // per wave: Schur updates of its siblings, by target in first-touch order
+        std::vector<std::map<int, std::vector<SchurUpdate>>> pending;
+        std::vector<std::vector<int>> target_order, target_syrk;
+        auto level_of = [&](int w) -> LevelPlan& {
+            while ((int)(P.levels.size() - first) <= w) {
+                P.levels.emplace_back();
+                LevelPlan& L = P.levels.back();
+                L.real = ilvl;
+                L.scaled = true;
+                L.waves.resize(1);
+                pending.emplace_back();
+                target_order.emplace_back();
+                target_syrk.emplace_back();
+            }
+            return P.levels[first + w];
+        };
+        for (int c : bottom) {
+            int w = 0;
+            for (int e : T.out[c])
+                if (T.edges[e].n2 != c && wave_of[T.edges[e].n2] >= 0) w = std::max(w, wave_of[T.edges[e].n2] + 1);
+            for (int e : T.in[c])
+                if (wave_of[T.edges[e].n1] >= 0) w = std::max(w, wave_of[T.edges[e].n1] + 1);
+            LevelPlan& L = level_of(w);
+            // ---- scale (tree.cpp:796-811) ----
+            const int pe = T.pivot(c);
+            const int piv = T.edges[pe].block;
+            L.scale_clusters.push_back(c);
+            L.scale_pivots.push_back(piv);
+            L.scale_inv.push_back(-1);
+            for (int e : T.in_nbr(c)) L.scale_trsm.push_back({T.edges[e].block, c, 0});
+            for (int e : T.out_nbr(c)) L.scale_trsm.push_back({T.edges[e].block, c, 1});
+            L.op_scale_llt.push_back(c);
+            L.op_scale_llt_block.push_back(piv);
+            // the new pivot is a stored identity: siblings eliminated later in the level
+            // update it (their neighbours' pivots take A^T A)
+            T.edges[pe].block = T.new_block(c, c, BLK_STORED, cursor);
+            L.scale_newpiv.push_back(T.edges[pe].block);
+            L.snap.push_back(c);
+            // ---- sparsify over the fill-in edges ----
+            SparsifyItem it;
+            it.cluster = c;
+            it.first = (int)P.asn_pieces.size();
+            int cap_cols = 0;
+            const auto ins = T.in_nbr(c);
+            const auto outs = T.out_nbr(c);
+            for (int e : ins)
+                if (!T.orig[e]) {
+                    P.asn_pieces.push_back({T.edges[e].block, T.edges[e].n1, 0});
+                    cap_cols += P.c_cap[T.edges[e].n1];
+                }
+            for (int e : outs)
+                if (!T.orig[e]) {
+                    P.asn_pieces.push_back({T.edges[e].block, T.edges[e].n2, 1});
+                    cap_cols += P.c_cap[T.edges[e].n2];
+                }
+            it.count = (int)P.asn_pieces.size() - it.first;
+            it.cap_cols = cap_cols;
+            it.v_off = P.v_len;
+            P.v_len += (int64_t)P.c_cap[c] * P.c_cap[c];
+            it.tau_off = P.tau_len;
+            P.tau_len += P.c_cap[c];
+            // the sibling: capacity of the cluster, its own solve slot and edge blocks
+            const int sib = (int)P.c_cap.size();
+            P.c_start.push_back(P.c_start[c]);
+            P.c_cap.push_back(P.c_cap[c]);
+            P.c_level.push_back(P.c_level[c]);
+            P.c_order.push_back(sib);
+            P.c_hlevel.push_back(ilvl);
+            P.c_parent.push_back(-1);
+            P.c_sparsify.push_back(0);
+            P.c_children.push_back({});
+            P.c_xoff.push_back(P.x_len);
+            P.x_len += P.c_cap[c];
+            T.out.emplace_back();
+            T.in.emplace_back();
+            T.eliminated.push_back(0);
+            wave_of.push_back(-1);
+            it.sib = sib;
+            T.add_edge(sib, sib, T.new_block(sib, sib, BLK_IDENTITY, cursor), true);
+            it.ofirst = (int)P.lr_splits.size();
+            auto split = [&](int e, int n, int tr) {
+                const int sb = T.new_block(sib, n, BLK_STORED, cursor);
+                P.lr_splits.push_back({T.edges[e].block, n, tr, sb});
+                T.add_edge(n, sib, sb, true);
+            };
+            for (int e : ins)
+                if (T.orig[e]) split(e, T.edges[e].n1, 0);
+            for (int e : outs)
+                if (T.orig[e]) split(e, T.edges[e].n2, 1);
+            it.ocount = (int)P.lr_splits.size() - it.ofirst;
+            // ---- eliminate the sibling (tree.cpp:895-910): identity pivot, Schur updates
+            // between the neighbours of its original edges (tree.cpp:862-883) ----
+            auto& pend = pending[w];
+            const auto sins = T.in_nbr(sib);
+            for (int e1 : sins)
+                for (int e2 : sins) {
+                    const int n1 = T.edges[e1].n1, n2 = T.edges[e2].n1;
+                    if (n1 < n2) continue;
+                    int found = -1;
+                    for (int e : T.out[n2])
+                        if (T.edges[e].n2 == n1) { found = e; break; }
+                    if (found < 0) {
+                        found = T.add_edge(n2, n1, T.new_block(n1, n2, BLK_STORED, cursor), false);
+                        P.n_fill_blocks++;
+                    }
+                    const int tb = T.edges[found].block;
+                    auto pt = pend.find(tb);
+                    if (pt == pend.end()) {
+                        target_order[w].push_back(tb);
+                        target_syrk[w].push_back(n1 == n2 ? 1 : 0);
+                        pt = pend.emplace(tb, std::vector<SchurUpdate>()).first;
+                    }
+                    pt->second.push_back({T.edges[e1].block, 1, T.edges[e2].block, 0, sib});
+                }
+            it.sfirst = (int)P.lr_sibops.size();
+            for (int e : sins) {
+                const int n = T.edges[e].n1;
+                P.lr_sibops.push_back({n, T.edges[e].block, wave_of[n] >= 0 ? 1 : 0});
+            }
+            it.scount = (int)P.lr_sibops.size() - it.sfirst;
+            T.set_eliminated(sib);
+            wave_of[c] = w;
+            P.lr_order[ilvl].push_back({c, (int)(first + w), (int)L.waves[0].size()});
+            L.waves[0].push_back(it);
+            L.op_ortho.push_back(c);
+        }
+        // per plan level: the workspace of its wave and its Schur targets
+        for (size_t w = 0; first + w < P.levels.size(); w++) {
+            LevelPlan& L = P.levels[first + w];
+            int64_t ws = 0;
+            for (auto& it : L.waves[0]) {
+                it.ws_off = ws;
+                ws += (int64_t)P.c_cap[it.cluster] * std::max(it.cap_cols, 1);
+                ws = (ws + 31) & ~int64_t(31);
+            }
+            L.ws_len = ws;
+            P.ws_len = std::max(P.ws_len, ws);
+            L.schur_first = (int)P.schur_targets.size();
+            for (size_t i = 0; i < target_order[w].size(); i++) {
+                auto& ups = pending[w][target_order[w][i]];
+                P.schur_targets.push_back({target_order[w][i], target_syrk[w][i], (int)P.schur_updates.size(),
+                                           (int)ups.size()});
+                P.schur_updates.insert(P.schur_updates.end(), ups.begin(), ups.end());
+            }
+            L.schur_count = (int)P.schur_targets.size() - L.schur_first;
+        }
+        if (P.levels.size() == first) level_of(0);  // an empty level still merges
+        // ---- merge (tree.cpp:1106-1184): an edge between parents is original when one of
+        // the edges it gathers is ----
+        if (ilvl < nl - 1) {
+            LevelPlan& L = P.levels.back();
+            L.merged = true;
+            L.merge_off = cursor;
+            const std::vector<int>& parents = H.bottoms[ilvl + 1];
+            for (int snew : parents) L.op_merge.push_back(snew);
+            L.merge_parents = parents;
+            for (int snew : parents) {
+                std::map<int, char> nnews;
+                for (int sold : H.children[snew])
+                    for (int e : T.out[sold]) nnews[H.parent[T.edges[e].n2]] |= T.orig[e];
+                for (const auto& kv : nnews) {
+                    int b = T.new_block(kv.first, snew, BLK_STORED, cursor);
+                    T.add_edge(snew, kv.first, b, kv.second != 0);
+                    P.n_merge_blocks++;
+                }
+                T.sort_edges(snew);
+                for (int sold : H.children[snew]) {
+                    for (int e : T.out[sold]) {
+                        int nold = T.edges[e].n2;
+                        int nnew = H.parent[nold];
+                        int dst = -1;
+                        for (int f : T.out[snew])
+                            if (T.edges[f].n2 == nnew) { dst = T.edges[f].block; break; }
+                        L.merge_copies.push_back({T.edges[e].block, dst, nold, sold});
+                    }
+                    T.out[sold].clear();
+                    T.in[sold].clear();
+                }
+            }
+            L.merge_len = cursor - L.merge_off;
+        }
+    }
+    P.nlevels = (int)P.levels.size();
+    P.arena_len = cursor;
+    P.nclusters_h = nc;
+    P.nclusters = (int)P.c_cap.size();
     return P;
 }
 

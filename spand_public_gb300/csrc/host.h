@@ -11,6 +11,7 @@
 // sizes kept in device memory, so the whole factorization is a fixed launch sequence.
 #pragma once
 
+#include <array>
 #include <cstdint>
 #include <list>
 #include <string>
@@ -104,6 +105,21 @@ struct SparsifyItem {
     // scaling, transformed to Q^T D Q and split), the sibling cluster made of the dropped
     // rows, its pivot block and the block of the edge original -> sibling (-1 elsewhere)
     int piv = -1, sib = -1, sib_piv = -1, aso = -1;
+    // LoRaSp (src/tree.cpp:1018-1064, keep_sibling): the original edges, slice of
+    // Plan::lr_splits; the sibling's GemmSymmIn ops, slice of Plan::lr_sibops
+    int ofirst = 0, ocount = 0, sfirst = 0, scount = 0;
+};
+
+// LoRaSp: an original edge of a sparsified cluster, Q^T-transformed, whose last rows go to
+// the sibling's edge block sblock (sibling x neighbour)
+struct LoraSplit {
+    int block, nbr, transposed, sblock;
+};
+
+// LoRaSp: GemmSymmIn(sibling, nbr) with the block sibling x nbr; cur: the neighbour was
+// sparsified earlier in the level (its size is then its rank)
+struct LoraSibOp {
+    int nbr, block, cur;
 };
 
 // Copy of a child block into a parent block during a merge (src/tree.cpp:1133-1184).
@@ -153,6 +169,10 @@ struct LevelPlan {
     std::vector<int> op_scale_llt_block;
     std::vector<int> op_ortho;            // sparsified clusters (Orthogonal if rank < rows)
     std::vector<int> op_merge;            // parents
+    // LoRaSp: each wave of a level is a level of the plan; real: the reference's level,
+    // snap: the clusters whose size is recorded at its start (the wave's own)
+    int real = -1;
+    std::vector<int> snap;
 };
 
 struct Plan {
@@ -164,6 +184,14 @@ struct Plan {
     // LDL^T pivots, sign-weighted Schur updates, sign pivots after scaling and an explicit
     // sibling per sparsified cluster (clusters nclusters_h .. nclusters-1)
     bool ldlt = false;
+    // LoRaSp (src/tree.cpp:1553-1608): no interior elimination; every cluster is scaled and
+    // sparsified over its fill-in edges only, its sibling keeps the original edges and is
+    // eliminated right away (explicit siblings, as on the LDLT path)
+    bool lorasp = false;
+    std::vector<LoraSplit> lr_splits;
+    std::vector<LoraSibOp> lr_sibops;
+    // per reference level: the clusters in processing order, with their plan level and item
+    std::vector<std::vector<std::array<int, 3>>> lr_order;  // (cluster, plan level, item index in its wave)
     int nclusters_h = 0;  // clusters of the hierarchy; the rest are LDLT siblings
     int nclusters = 0;        // clusters of the hierarchy (siblings are implicit)
     std::vector<int> c_start, c_cap, c_level, c_order, c_hlevel, c_parent, c_sparsify;
@@ -197,6 +225,13 @@ struct Hierarchy {
 
 Hierarchy build_hierarchy(const std::vector<ClusterID>& part, int nlevels, std::vector<int>& perm);
 
+// LoRaSp ordering: geometric recursive bisection (src/partition.cpp:99-137, 245-285), the part
+// of every dof (natural ordering); X is dim x n, column-major
+std::vector<int> partition_rb(int n, int nlevels, const double* X, int dim);
+// LoRaSp hierarchy (src/tree.cpp:421-503): every cluster at the top level, pairs of
+// consecutive clusters merge; perm: the assembly permutation (sort by part)
+Hierarchy build_hierarchy_lorasp(const std::vector<int>& parts, int nlevels, std::vector<int>& perm);
+
 // Assembly: per leaf cluster, the sorted neighbour list (pivot first) and the dense
 // blocks (src/tree.cpp:505-575).  values is laid out with the plan's block offsets.
 struct Assembly {
@@ -206,6 +241,8 @@ Assembly assembly_structure(const Hierarchy& H, const Csc& App, bool symmetric);
 
 Plan build_plan(const Hierarchy& H, const Assembly& asmb, int skip, bool use_want_sparsify, bool lu = false,
                 bool ldlt = false);
+// The symbolic replay of Tree::factorize_lorasp (src/tree.cpp:1553-1608), SPD / LLT
+Plan build_plan_lorasp(const Hierarchy& H, const Assembly& asmb);
 
 // For every entry k of A (natural ordering, CSC order): the element offset of A(r, c) in
 // the assembled level-0 blocks, or -1 when the entry is not stored (upper triangle of the

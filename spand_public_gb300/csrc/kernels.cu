@@ -1508,6 +1508,16 @@ __global__ void pattern_outer_kernel(long long nnz, const int* __restrict__ rows
     if (k < nnz) out[k] = -lam[rows[k]] * x[cols[k]];
 }
 
+// LoRaSp: the new pivot of a scaled cluster, a stored identity (the block is zero from the
+// factorization's start); one CTA per cluster
+template <typename T>
+__global__ void identity_kernel(Ctx<T> c, const int* __restrict__ blocks, const int* __restrict__ clusters) {
+    const int n = c.csize[clusters[blockIdx.x]];
+    T* B = bptr(c, blocks[blockIdx.x]);
+    const int ld = c.blk[blocks[blockIdx.x]].ld;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) B[i + (size_t)i * ld] = T(1);
+}
+
 __global__ void snapshot_kernel(const int* csize, int* rows0, const int* __restrict__ clusters, int n) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n) rows0[clusters[k]] = csize[clusters[k]];
@@ -1742,7 +1752,9 @@ constexpr int GF_ROWS = 64;
 
 // LDLT path: signs != nullptr weights x_self by the signs of self (A D x_s,
 // operations.cpp:55-83); sib_mode: the neighbour is a sparsified cluster whose size is now
-// csize (the op of a sibling, recorded after the split).
+// csize (the op of a sibling, recorded after the split).  An op kind with bit 16 set says
+// the same for its own neighbour (LoRaSp siblings, whose neighbours may or may not have
+// been sparsified before them).
 template <typename T>
 __global__ void __launch_bounds__(256) gemm_fwd2_kernel(Ctx<T> c, XCtx<T> X, const DGroup* __restrict__ groups,
                                                         const DGemmOp* __restrict__ ops, const DTile* __restrict__ tiles,
@@ -1753,7 +1765,7 @@ __global__ void __launch_bounds__(256) gemm_fwd2_kernel(Ctx<T> c, XCtx<T> X, con
     const int r = blockIdx.x / ntiles;
     const DGroup G = groups[tiles[t].item];
     const int nb = G.key;
-    const int nn = sib_mode ? c.csize[nb] : c.rows0[nb];
+    const int nn = (sib_mode || (ops[G.first].kind & 16)) ? c.csize[nb] : c.rows0[nb];
     const int i0 = tiles[t].tile_i * GF_ROWS;
     if (i0 >= nn) return;
     (void)rhs_stride;
@@ -1769,16 +1781,17 @@ __global__ void __launch_bounds__(256) gemm_fwd2_kernel(Ctx<T> c, XCtx<T> X, con
         const T* A = bptr(c, op.block);
         const int ld = c.blk[op.block].ld;
         const T* sg = signs ? signs + soff[op.self] : nullptr;
+        const int kind = op.kind & 15;
         if (i < nn) {
             T s0 = 0, s1 = 0;
             if (sg) {
-                if (op.kind == 1) {
+                if (kind == 1) {
                     for (int j = sp; j < ns; j += 4) s0 += A[i + (size_t)j * ld] * (sg[j] * xs[j]);
                 } else {
                     const T* a = A + (size_t)i * ld;
                     for (int j = sp; j < ns; j += 4) s0 += a[j] * (sg[j] * xs[j]);
                 }
-            } else if (op.kind == 1) {
+            } else if (kind == 1) {
                 int j = sp;
                 for (; j + 4 < ns; j += 8) {
                     s0 += A[i + (size_t)j * ld] * xs[j];
@@ -1823,12 +1836,12 @@ __global__ void __launch_bounds__(256) gemm_bwd2_kernel(Ctx<T> c, XCtx<T> X, con
         T acc = 0;
         for (int o = 0; o < G.count; o++) {
             const DGemmOp op = ops[G.first + o];
-            const int nn = sib_mode ? c.csize[op.nbr] : c.rows0[op.nbr];
+            const int nn = (sib_mode || (op.kind & 16)) ? c.csize[op.nbr] : c.rows0[op.nbr];
             const T* xn = X.xs + X.xoff[op.nbr] + r * X.xld;
             const T* A = bptr(c, op.block);
             const int ld = c.blk[op.block].ld;
             T s = 0;
-            if (op.kind == 1) {
+            if ((op.kind & 15) == 1) {
                 const T* a = A + (size_t)i * ld;
                 for (int j = lane; j < nn; j += 32) s += a[j] * xn[j];
             } else {
@@ -2518,6 +2531,12 @@ class DeviceFactor : public DeviceFactorBase {
         nc_ = P.nclusters;
         lu_ = P.lu;
         ldlt_ = P.ldlt;
+        lorasp_ = P.lorasp;
+        if (lorasp_) {
+            std::vector<int4> sp;
+            for (const LoraSplit& s : P.lr_splits) sp.push_back(make_int4(s.block, s.nbr, s.transposed, s.sblock));
+            lr_splits_ = up(sp);
+        }
         init_qrcp_limits();
         SPAND_CUDA(cudaStreamCreateWithFlags(&s2_, cudaStreamNonBlocking));
         SPAND_CUDA(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
@@ -2600,6 +2619,7 @@ class DeviceFactor : public DeviceFactorBase {
                 D.scale_inv = up(L.scale_inv);
                 D.scale_lu_smem = lu_smem_for(L.scale_clusters, P);
             }
+            if (lorasp_) D.scale_newpiv = up(L.scale_newpiv);
             if (ldlt_) {
                 D.scale_newpiv = up(L.scale_newpiv);
                 D.scale_lu_smem = lu_smem_for(L.scale_clusters, P);
@@ -2608,8 +2628,10 @@ class DeviceFactor : public DeviceFactorBase {
             }
             {
                 std::vector<int> all;
-                for (int cl = 0; cl < nc_; cl++)
-                    if (P.c_hlevel[cl] == l) all.push_back(cl);
+                if (lorasp_) all = L.snap;  // the wave's own clusters
+                else
+                    for (int cl = 0; cl < nc_; cl++)
+                        if (P.c_hlevel[cl] == l) all.push_back(cl);
                 D.n_level = (int)all.size();
                 D.level_clusters = up(all);
             }
@@ -2690,6 +2712,21 @@ class DeviceFactor : public DeviceFactorBase {
                     W.sib_tiles = up(tiles);
                     W.n_sib_tiles = (int)tiles.size();
                     W.ldlt_smem = lu_smem_n(mx);
+                }
+                if (lorasp_) {
+                    // the siblings and the original edges they take rows from
+                    std::vector<int> sib;
+                    std::vector<int2> rg;
+                    W.stiles = 1;
+                    for (const SparsifyItem& it : wave) {
+                        sib.push_back(it.sib);
+                        rg.push_back(make_int2(it.ofirst, it.ocount));
+                        std::vector<int> caps;
+                        for (int q = 0; q < it.ocount; q++) caps.push_back(P.c_cap[P.lr_splits[it.ofirst + q].nbr]);
+                        W.stiles = std::max(W.stiles, lorasp_split_tiles(caps.data(), it.ocount));
+                    }
+                    W.sib = up(sib);
+                    W.orng = up(rg);
                 }
                 D.waves.push_back(W);
             }
@@ -2876,6 +2913,52 @@ class DeviceFactor : public DeviceFactorBase {
                     for (int c0 : L.op_elim_llt) diag_h_.push_back(c0);
                     for (int c0 : L.op_scale_llt) diag_h_.push_back(c0);
                     for (int c0 : sibs) diag_h_.push_back(c0);
+                } else if (lorasp_) {
+                    // the siblings' GemmSymmIn ops: forward grouped by neighbour, backward by
+                    // sibling, in recording order; kind bit 16: the neighbour's size is its rank
+                    std::vector<int> sibs, owners;
+                    std::map<int, std::vector<DGemmOp>> fwd, bwd;
+                    std::vector<int> fk, bk;
+                    for (const auto& wave : L.waves)
+                        for (const SparsifyItem& it : wave) {
+                            sibs.push_back(it.sib);
+                            owners.push_back(it.cluster);
+                            for (int q = 0; q < it.scount; q++) {
+                                const LoraSibOp& op = P.lr_sibops[it.sfirst + q];
+                                const DGemmOp g{it.sib, op.nbr, op.block, 2 | (op.cur ? 16 : 0)};
+                                if (!fwd.count(op.nbr)) fk.push_back(op.nbr);
+                                fwd[op.nbr].push_back(g);
+                                if (!bwd.count(it.sib)) bk.push_back(it.sib);
+                                bwd[it.sib].push_back(g);
+                            }
+                        }
+                    D.n_sib = (int)sibs.size();
+                    D.sib_clusters = up(sibs);
+                    D.sib_owner = up(owners);
+                    std::vector<DGroup> fg, bg;
+                    std::vector<DGemmOp> fo, bo;
+                    std::vector<int> ef, eb;
+                    for (int k : fk) {
+                        fg.push_back({k, (int)fo.size(), (int)fwd[k].size()});
+                        fo.insert(fo.end(), fwd[k].begin(), fwd[k].end());
+                        ef.push_back(P.c_cap[k]);
+                    }
+                    for (int k : bk) {
+                        auto& ops = bwd[k];
+                        std::reverse(ops.begin(), ops.end());  // backward: reverse recording order
+                        bg.push_back({k, (int)bo.size(), (int)ops.size()});
+                        bo.insert(bo.end(), ops.begin(), ops.end());
+                        eb.push_back(P.c_cap[k]);
+                    }
+                    D.sib_gf = up(fg);
+                    D.sib_gfo = up(fo);
+                    D.sib_gb = up(bg);
+                    D.sib_gbo = up(bo);
+                    auto tf = tiles_1d(ef, GF_ROWS), tb = tiles_1d(eb, GB_ROWS);
+                    D.sib_gf_tiles = up(tf);
+                    D.n_sib_gf_tiles = (int)tf.size();
+                    D.sib_gb_tiles = up(tb);
+                    D.n_sib_gb_tiles = (int)tb.size();
                 }
                 D.x_smem_ortho = mx * (int)sizeof(T);
                 const int64_t mr = (int64_t)mx * (MR_RB + 1) * (int64_t)sizeof(T);
@@ -3013,6 +3096,10 @@ class DeviceFactor : public DeviceFactorBase {
                                  D.scale_pc_cs, D.scale_pc_smem);
                     launch_trsm(D.scale_trsm0);
                     launch_trsm(D.scale_trsm1);
+                    if (lorasp_)
+                        launch("identity", [&] {
+                            identity_kernel<T><<<D.n_scale, 128, 0, s_>>>(ctx_, D.scale_newpiv, D.scale_clusters);
+                        });
                 }
                 if (nphi_)
                     launch("preserve_scale", [&] {
@@ -3061,6 +3148,23 @@ class DeviceFactor : public DeviceFactorBase {
                             ctx_, W.items, pieces_, ws_, ipvt_, rank_, vstore_);
                     });
                 }
+                if (lorasp_) {
+                    // Q^T on the original edges, their last rows to the siblings, then the
+                    // siblings' elimination: Schur updates between their neighbours
+                    launch("sparsify_wy", [&] {
+                        sparsify_wy_kernel<T><<<W.n, 256, larft_smem_elems() * sizeof(T), s_>>>(
+                            ctx_, W.items, vstore_, rank_, tauws_, taustore_, tstore_);
+                    });
+                    launch("lorasp_split", [&] {
+                        lorasp_split<T>(ctx_, W.items, W.n, W.stiles, W.sib, W.orng, lr_splits_, vstore_, tstore_,
+                                        rank_, s_);
+                    });
+                    if (D.n_schur_tiles)
+                        launch("schur", [&] {
+                            schur_kernel<T><<<D.n_schur_tiles, 256, 0, s_>>>(ctx_, D.schur_targets, d_ups_, D.schur_tiles,
+                                                                             D.n_schur_tiles, signs_, d_xoff_);
+                        });
+                }
                 if (ldlt_) {
                     launch("pivot_split", [&] {
                         pivot_split_kernel<T><<<W.n, 256, 0, s_>>>(ctx_, W.items, W.sib, W.sib_piv, W.aso, W.piv,
@@ -3075,8 +3179,9 @@ class DeviceFactor : public DeviceFactorBase {
                         });
                 }
                 // WY factors: on the side stream beside the next wave's QRCP (on the main
-                // stream when the profiler times every launch); preservation made them above
-                if (nphi_) {
+                // stream when the profiler times every launch); preservation and LoRaSp made
+                // them above
+                if (nphi_ || lorasp_) {
                 } else if (prof_.enabled()) {
                     launch("sparsify_wy", [&] {
                         sparsify_wy_kernel<T><<<W.n, 256, larft_smem_elems() * sizeof(T), s_>>>(
@@ -3397,6 +3502,8 @@ class DeviceFactor : public DeviceFactorBase {
         int gsmem = 0;       // its dynamic shared memory per CTA
         int ytiles = 0;      // scatter tiles per matrix (reflector + edge-block capacity tiles)
         int ptiles = 0;      // preservation: Q^T-application CTAs per matrix
+        int2* orng = nullptr;  // LoRaSp: per item its slice of the original edges
+        int stiles = 0;        // LoRaSp: split CTAs per matrix
         // LDLT: per item the sibling, its pivot, the edge block, the cluster's pivot; the
         // sibling panels and the Schur update of the cluster's pivot
         int *sib = nullptr, *sib_piv = nullptr, *aso = nullptr, *piv = nullptr;
@@ -3845,7 +3952,7 @@ class DeviceFactor : public DeviceFactorBase {
         const long long tot = (long long)n * nrhs;
         // 16 or more right-hand sides: the kernels that read each factor block once per 32
         // (not on the LDLT path, whose sweeps carry signs and permutations)
-        const bool mr = nrhs >= 16 && !ldlt_;
+        const bool mr = nrhs >= 16 && !ldlt_ && !lorasp_;
         const T* sg = ldlt_ ? signs_ : nullptr;
         auto permx = [&](const int* clusters, int count, int fwd, int smem) {
             if (!ldlt_ || !count) return;
@@ -3855,7 +3962,7 @@ class DeviceFactor : public DeviceFactorBase {
             });
         };
         auto siblings = [&](LevelDev& D, int fwd) {
-            if (!ldlt_ || !D.n_sib) return;
+            if (!(ldlt_ || lorasp_) || !D.n_sib) return;
             auto split = [&] {
                 launch("split_x", [&] {
                     split_x_kernel<T><<<dim3((unsigned)D.n_sib, (unsigned)nrhs), 128, 0, s_>>>(
@@ -3864,21 +3971,27 @@ class DeviceFactor : public DeviceFactorBase {
             };
             if (fwd) {
                 split();
-                permx(D.sib_clusters, D.n_sib, 1, D.x_smem_sib);
-                trsv_ldlt(D.sib_clusters, D.sib_piv, D.sib_tv, D.n_sib_tv, D.x_smem_sib, 0, X, tmp);
+                if (ldlt_) {  // LoRaSp siblings have the identity for pivot
+                    permx(D.sib_clusters, D.n_sib, 1, D.x_smem_sib);
+                    trsv_ldlt(D.sib_clusters, D.sib_piv, D.sib_tv, D.n_sib_tv, D.x_smem_sib, 0, X, tmp);
+                }
                 if (D.n_sib_gf_tiles)
                     launch("gemm_fwd", [&] {
                         gemm_fwd2_kernel<T><<<D.n_sib_gf_tiles * nrhs, 256, 0, s_>>>(
-                            ctx_, X, D.sib_gf, D.sib_gfo, D.sib_gf_tiles, D.n_sib_gf_tiles, 0, signs_, d_xoff_, 1);
+                            ctx_, X, D.sib_gf, D.sib_gfo, D.sib_gf_tiles, D.n_sib_gf_tiles, 0, signs_, d_xoff_,
+                            ldlt_ ? 1 : 0);
                     });
             } else {
                 if (D.n_sib_gb_tiles)
                     launch("gemm_bwd", [&] {
                         gemm_bwd2_kernel<T><<<D.n_sib_gb_tiles * nrhs, 256, 0, s_>>>(
-                            ctx_, X, D.sib_gb, D.sib_gbo, D.sib_gb_tiles, D.n_sib_gb_tiles, signs_, d_xoff_, 1);
+                            ctx_, X, D.sib_gb, D.sib_gbo, D.sib_gb_tiles, D.n_sib_gb_tiles, signs_, d_xoff_,
+                            ldlt_ ? 1 : 0);
                     });
-                trsv_ldlt(D.sib_clusters, D.sib_piv, D.sib_tv, D.n_sib_tv, D.x_smem_sib, 1, X, tmp);
-                permx(D.sib_clusters, D.n_sib, 0, D.x_smem_sib);
+                if (ldlt_) {
+                    trsv_ldlt(D.sib_clusters, D.sib_piv, D.sib_tv, D.n_sib_tv, D.x_smem_sib, 1, X, tmp);
+                    permx(D.sib_clusters, D.n_sib, 0, D.x_smem_sib);
+                }
                 split();
             }
         };
@@ -4031,6 +4144,8 @@ class DeviceFactor : public DeviceFactorBase {
     int* lu_swp_ = nullptr;       // and the row interchanges that make it
     int cur_count_ = 0;           // clusters of the pivot op list being applied in the solve
     bool check_launches_ = getenv("SPAND_CHECK_LAUNCHES") != nullptr;
+    bool lorasp_ = false;         // LoRaSp plan (explicit siblings with original edges)
+    int4* lr_splits_ = nullptr;   // LoRaSp: (block, neighbour, transposed, sibling block)
     // preservation: phi restricted to every hierarchy cluster (capacity x nphi at
     // phioff), its scratch, the natural-order phi, the leaf scatter map, rank1 per cluster
     int nphi_ = 0;

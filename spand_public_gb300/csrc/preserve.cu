@@ -283,6 +283,85 @@ __global__ void __launch_bounds__(PV_THREADS) preserve_combine_kernel(Ctx<T> c, 
 constexpr int PW_KC = 32;
 constexpr int PW_QB = 32;
 
+// Shared memory of one tile application
+template <typename T>
+struct WyTile {
+    T vt[PW_KC][PW_QB + 1];
+    T xs[PW_KC][PW_QB + 1];
+    T Wm[PW_QB][PW_QB + 1];
+    T Ym[PW_QB][PW_QB + 1];
+};
+
+// x <- Q^T x on the tile's nv vectors, element (r, l) at base[r * sr + l * sv], r < rows; Q:
+// k reflectors in V (ld), T factors in Tm.  Ends with a barrier.
+template <typename T>
+__device__ void wy_qt_tile(const T* V, const T* Tm, int ld, int rows, int k, T* base, long long sr, long long sv,
+                           int nv, WyTile<T>& S) {
+    const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, w = tid >> 5;
+    const bool rfast = sr == 1;  // consecutive threads on consecutive rows (coalesced)
+    auto stage = [&](int rb, int i0, int bw) {
+        for (int idx = tid; idx < PW_KC * PW_QB; idx += nth) {
+            const int kk = idx % PW_KC, ii = idx / PW_KC;
+            const int r = rb + kk, col = i0 + ii;
+            T v = T(0);
+            if (ii < bw && r < rows) v = r > col ? V[r + (size_t)col * ld] : (r == col ? T(1) : T(0));
+            S.vt[kk][ii] = v;
+            const int rr = rfast ? kk : idx / PW_QB, l = rfast ? ii : idx % PW_QB;
+            const int r2 = rb + rr;
+            S.xs[rr][l] = (l < nv && r2 < rows) ? base[r2 * sr + l * sv] : T(0);
+        }
+    };
+    const int nb = (k + PW_QB - 1) / PW_QB;
+    for (int b = 0; b < nb; b++) {
+        const int i0 = b * PW_QB, bw = min(PW_QB, k - i0);
+        // W[i][l] = sum_{r >= i0 + i} v_i[r] X[r][l]   (v_i[i0 + i] = 1)
+        T acc[4] = {T(0), T(0), T(0), T(0)};
+        for (int rb = i0; rb < rows; rb += PW_KC) {
+            __syncthreads();
+            stage(rb, i0, bw);
+            __syncthreads();
+            const int kw = min(PW_KC, rows - rb);
+            for (int kk = 0; kk < kw; kk++) {
+                const T xv = S.xs[kk][lane];
+#pragma unroll
+                for (int u = 0; u < 4; u++) acc[u] += S.vt[kk][w + 8 * u] * xv;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) S.Wm[w + 8 * u][lane] = acc[u];
+        __syncthreads();
+        // Y = T_b^T W
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int i = w + 8 * u;
+            T y = T(0);
+            if (i < bw)
+                for (int j = 0; j <= i; j++) y += Tm[(i0 + j) + (size_t)(i0 + i) * ld] * S.Wm[j][lane];
+            S.Ym[i][lane] = y;
+        }
+        // X[r][l] -= sum_i v_i[r] Y[i][l], chunk by chunk
+        for (int rb = i0; rb < rows; rb += PW_KC) {
+            __syncthreads();
+            stage(rb, i0, bw);
+            __syncthreads();
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int kk = w + 8 * u;
+                T s2 = T(0);
+                for (int ii = 0; ii < bw; ii++) s2 += S.vt[kk][ii] * S.Ym[ii][lane];
+                S.xs[kk][lane] -= s2;
+            }
+            __syncthreads();
+            for (int idx = tid; idx < PW_KC * PW_QB; idx += nth) {
+                const int rr = rfast ? idx % PW_KC : idx / PW_QB, l = rfast ? idx / PW_KC : idx % PW_QB;
+                const int r2 = rb + rr;
+                if (l < nv && r2 < rows) base[r2 * sr + l * sv] = S.xs[rr][l];
+            }
+        }
+    }
+    __syncthreads();
+}
+
 template <typename T>
 __global__ void __launch_bounds__(PV_THREADS) preserve_apply_kernel(Ctx<T> c, PhiCtx<T> P,
                                                                     const DSpars* __restrict__ items,
@@ -290,10 +369,7 @@ __global__ void __launch_bounds__(PV_THREADS) preserve_apply_kernel(Ctx<T> c, Ph
                                                                     const T* __restrict__ vstore,
                                                                     const T* __restrict__ tstore,
                                                                     const int* __restrict__ rank) {
-    __shared__ T vt[PW_KC][PW_QB + 1];
-    __shared__ T xs[PW_KC][PW_QB + 1];
-    __shared__ T Wm[PW_QB][PW_QB + 1];
-    __shared__ T Ym[PW_QB][PW_QB + 1];
+    __shared__ WyTile<T> S;
     if (c.status->not_spd) return;
     const DSpars it = items[blockIdx.x];
     const int cl = it.cluster;
@@ -336,69 +412,52 @@ __global__ void __launch_bounds__(PV_THREADS) preserve_apply_kernel(Ctx<T> c, Ph
         sr = 1;
         sv = ld;
     }
-    const T* V = vstore + it.v_off;
-    const T* Tm = tstore + it.v_off;
-    const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, w = tid >> 5;
-    const bool rfast = sr == 1;  // consecutive threads on consecutive rows (coalesced)
-    auto stage = [&](int rb, int i0, int bw) {
-        for (int idx = tid; idx < PW_KC * PW_QB; idx += nth) {
-            const int kk = idx % PW_KC, ii = idx / PW_KC;
-            const int r = rb + kk, col = i0 + ii;
-            T v = T(0);
-            if (ii < bw && r < rows) v = r > col ? V[r + (size_t)col * ld] : (r == col ? T(1) : T(0));
-            vt[kk][ii] = v;
-            const int rr = rfast ? kk : idx / PW_QB, l = rfast ? ii : idx % PW_QB;
-            const int r2 = rb + rr;
-            xs[rr][l] = (l < nv && r2 < rows) ? base[r2 * sr + l * sv] : T(0);
-        }
-    };
-    const int nb = (k + PW_QB - 1) / PW_QB;
-    for (int b = 0; b < nb; b++) {
-        const int i0 = b * PW_QB, bw = min(PW_QB, k - i0);
-        // W[i][l] = sum_{r >= i0 + i} v_i[r] X[r][l]   (v_i[i0 + i] = 1)
-        T acc[4] = {T(0), T(0), T(0), T(0)};
-        for (int rb = i0; rb < rows; rb += PW_KC) {
-            __syncthreads();
-            stage(rb, i0, bw);
-            __syncthreads();
-            const int kw = min(PW_KC, rows - rb);
-            for (int kk = 0; kk < kw; kk++) {
-                const T xv = xs[kk][lane];
-#pragma unroll
-                for (int u = 0; u < 4; u++) acc[u] += vt[kk][w + 8 * u] * xv;
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < 4; u++) Wm[w + 8 * u][lane] = acc[u];
-        __syncthreads();
-        // Y = T_b^T W
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const int i = w + 8 * u;
-            T y = T(0);
-            if (i < bw)
-                for (int j = 0; j <= i; j++) y += Tm[(i0 + j) + (size_t)(i0 + i) * ld] * Wm[j][lane];
-            Ym[i][lane] = y;
-        }
-        // X[r][l] -= sum_i v_i[r] Y[i][l], chunk by chunk
-        for (int rb = i0; rb < rows; rb += PW_KC) {
-            __syncthreads();
-            stage(rb, i0, bw);
-            __syncthreads();
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const int kk = w + 8 * u;
-                T s2 = T(0);
-                for (int ii = 0; ii < bw; ii++) s2 += vt[kk][ii] * Ym[ii][lane];
-                xs[kk][lane] -= s2;
-            }
-            __syncthreads();
-            for (int idx = tid; idx < PW_KC * PW_QB; idx += nth) {
-                const int rr = rfast ? idx % PW_KC : idx / PW_QB, l = rfast ? idx / PW_KC : idx % PW_QB;
-                const int r2 = rb + rr;
-                if (l < nv && r2 < rows) base[r2 * sr + l * sv] = xs[rr][l];
-            }
-        }
+    wy_qt_tile(vstore + it.v_off, tstore + it.v_off, ld, rows, k, base, sr, sv, nv, S);
+}
+
+// LoRaSp split (tree.cpp:1018-1064, keep_sibling): Q^T on a 32-vector tile of an original
+// edge block, whose rows k .. rows-1 then go to the sibling's block (sibling x neighbour);
+// the sibling's size becomes rows - k.  Grid (items, tiles over the original edges).
+template <typename T>
+__global__ void __launch_bounds__(PV_THREADS) lorasp_split_kernel(Ctx<T> c, const DSpars* __restrict__ items,
+                                                                  const int* __restrict__ sibs,
+                                                                  const int2* __restrict__ ranges,
+                                                                  const int4* __restrict__ splits,
+                                                                  const T* __restrict__ vstore,
+                                                                  const T* __restrict__ tstore,
+                                                                  const int* __restrict__ rank) {
+    __shared__ WyTile<T> S;
+    if (c.status->not_spd) return;
+    const DSpars it = items[blockIdx.x];
+    const int cl = it.cluster, sib = sibs[blockIdx.x];
+    const int rows = c.rows0[cl];
+    const int k = min(rank[cl], rows);
+    if (blockIdx.y == 0 && threadIdx.x == 0) c.csize[sib] = c.rows0[sib] = rows - k;
+    if (k >= rows) return;
+    const int2 rg = ranges[blockIdx.x];
+    int t = blockIdx.y, p = 0;
+    for (; p < rg.y; p++) {
+        const int nt = (c.cap[splits[rg.x + p].y] + PW_QB - 1) / PW_QB;
+        if (t < nt) break;
+        t -= nt;
+    }
+    if (p >= rg.y) return;
+    const int4 sp = splits[rg.x + p];  // block, nbr, transposed, sibling block
+    const int n = c.csize[sp.y];
+    const int j0 = PW_QB * t;
+    if (j0 >= n) return;
+    const int nv = min(PW_QB, n - j0);
+    T* B = bptr(c, sp.x);
+    const long long bld = c.blk[sp.x].ld;
+    T* base = sp.z ? B + j0 : B + (size_t)j0 * bld;
+    const long long sr = sp.z ? bld : 1, sv = sp.z ? 1 : bld;
+    const int ld = c.cap[cl];
+    wy_qt_tile(vstore + it.v_off, tstore + it.v_off, ld, rows, k, base, sr, sv, nv, S);
+    T* D = bptr(c, sp.w);
+    const long long dld = c.blk[sp.w].ld;
+    for (int idx = threadIdx.x; idx < (rows - k) * nv; idx += blockDim.x) {
+        const int i = idx % (rows - k), l = idx / (rows - k);
+        D[i + (size_t)(j0 + l) * dld] = base[(long long)(k + i) * sr + l * sv];
     }
 }
 
@@ -406,6 +465,20 @@ int preserve_apply_tiles(const int* caps, int count, int nphi) {
     int t = (nphi + PW_QB - 1) / PW_QB;
     for (int p = 0; p < count; p++) t += (caps[p] + PW_QB - 1) / PW_QB;
     return std::max(1, t);
+}
+
+int lorasp_split_tiles(const int* caps, int count) {
+    int t = 0;
+    for (int p = 0; p < count; p++) t += (caps[p] + PW_QB - 1) / PW_QB;
+    return std::max(1, t);
+}
+
+template <typename T>
+void lorasp_split(Ctx<T> c, const DSpars* items, int n, int ytiles, const int* sibs, const int2* ranges,
+                  const int4* splits, const T* vstore, const T* tstore, const int* rank, cudaStream_t s) {
+    if (n == 0) return;
+    lorasp_split_kernel<T><<<dim3((unsigned)n, (unsigned)ytiles), PV_THREADS, 0, s>>>(c, items, sibs, ranges, splits,
+                                                                                     vstore, tstore, rank);
 }
 
 template <typename T>
@@ -464,7 +537,9 @@ void preserve_apply(Ctx<T> c, PhiCtx<T> P, const DSpars* items, int n, int ytile
                                     const long long*, T*, T*, int*, int*, bool, cudaStream_t);                     \
     template void preserve_combine<T>(Ctx<T>, const DSpars*, int, const T*, T*, T*, const int*, int*, cudaStream_t); \
     template void preserve_apply<T>(Ctx<T>, PhiCtx<T>, const DSpars*, int, int, const DAsn*, const T*, const T*,    \
-                                    const int*, cudaStream_t);
+                                    const int*, cudaStream_t);                                                     \
+    template void lorasp_split<T>(Ctx<T>, const DSpars*, int, int, const int*, const int2*, const int4*, const T*,  \
+                                  const T*, const int*, cudaStream_t);
 
 SPAND_PRESERVE_INST(float)
 SPAND_PRESERVE_INST(double)

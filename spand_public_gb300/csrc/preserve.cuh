@@ -63,4 +63,13 @@ void preserve_apply(Ctx<T> c, PhiCtx<T> P, const DSpars* items, int n, int ytile
 // CTAs per item of preserve_apply: 32-vector tiles of the pieces' capacities and of phi
 int preserve_apply_tiles(const int* caps, int count, int nphi);
 
+// LoRaSp split (tree.cpp:1018-1064 with keep_sibling): Q^T (blocked WY form, T factors in
+// tstore) on every original edge of each item, rows rank .. rows-1 copied into the sibling's
+// block; sibling sizes set.  sibs / ranges: per item its sibling and its slice of splits
+// (block, neighbour, transposed, sibling block).  ytiles: lorasp_split_tiles.
+template <typename T>
+void lorasp_split(Ctx<T> c, const DSpars* items, int n, int ytiles, const int* sibs, const int2* ranges,
+                  const int4* splits, const T* vstore, const T* tstore, const int* rank, cudaStream_t s);
+int lorasp_split_tiles(const int* caps, int count);
+
 }  // namespace spand

@@ -103,6 +103,28 @@ std::vector<ClusterID> Tree::partition(const Csc& A) {
     return part_;
 }
 
+std::vector<int> Tree::partition_lorasp(const Csc& A) {
+    if (partitioned_) throw std::logic_error("partition() called twice");
+    double t0 = now_s();
+    const int N = A.n;
+    if (!geo_) throw std::invalid_argument("LoRaSp ordering needs coordinates (set_Xcoo, set_use_geo)");
+    if ((int)X_.size() != dim_ * N || dim_ <= 0) throw std::invalid_argument("set_Xcoo: coordinates must be dim x N");
+    std::vector<int> parts = spand::partition_rb(N, nlevels_, X_.data(), dim_);
+    H_ = spand::build_hierarchy_lorasp(parts, nlevels_, perm_);
+    log_.assign(nlevels_, LevelLog());
+    part_.clear();
+    lorasp_ = true;
+    partitioned_ = true;
+    t_partition = now_s() - t0;
+    return parts;
+}
+
+void Tree::factorize_lorasp() {
+    if (!lorasp_) throw std::logic_error("factorize_lorasp() needs partition_lorasp()");
+    lorasp_run_ = true;
+    factorize();
+}
+
 // tree.cpp:505-575, plus the symbolic plan of factorize() and the device upload.  The
 // block values are assembled on the device: the first call builds the map from every
 // entry of A to its place in the level-0 blocks; later calls with the same sparsity
@@ -122,7 +144,12 @@ void Tree::assemble(const Csc& A) {
         A_ = A;
         Csc App = spand::symm_perm(A, perm_);
         asmb_ = spand::assembly_structure(H_, App, !lu);
-        plan_ = spand::build_plan(H_, asmb_, skip_, use_want_sparsify_, lu, ldlt);
+        if (lorasp_) {
+            if (symm_ != SymmKind::SPD) throw std::invalid_argument("LoRaSp is implemented for SPD / LLT");
+            plan_ = spand::build_plan_lorasp(H_, asmb_);
+        } else {
+            plan_ = spand::build_plan(H_, asmb_, skip_, use_want_sparsify_, lu, ldlt);
+        }
         std::vector<int64_t> amap = spand::assembly_map(plan_, H_, asmb_, A, perm_);
         if (!stream_) cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
         dev_ = spand::make_device_factor(fp32_, stream_, perm_);
@@ -203,6 +230,10 @@ void Tree::set_phi(const double* phi, int n, int nphi) {
 // tree.cpp:1457-1459, 1477-1485: preservation needs a symmetric kind and phi of N rows
 void Tree::prepare_factorize() {
     if (!assembled_ok_) throw std::logic_error("factorize() before assemble()");
+    if (lorasp_ && !lorasp_run_)
+        throw std::logic_error("a tree partitioned with partition_lorasp() factorizes with factorize_lorasp()");
+    lorasp_run_ = false;
+    if (lorasp_ && preserve_) throw std::invalid_argument("LoRaSp does not preserve vectors (tree.cpp:1564)");
     try {
         if (!preserve_) {
             dev_->set_phi(nullptr, 0, 0);
@@ -337,9 +368,76 @@ size_t Tree::device_bytes() const { return dev_ ? dev_->device_bytes() : 0; }
 
 // Op list and per-level log reconstructed from the plan and the device sizes, in the
 // reference's recording order (tree.cpp:909-910, 885-892, 810, 1331, 1102, 1342, 1439).
+// The op list and per-level log of factorize_lorasp, in the reference's order: per cluster
+// ScalingLLT, then (rank < size) Orthogonal, Split, the sibling's ScalingLLT (identity)
+// and its GemmSymmIn ops; the level's Merge ops at its end.
+void Tree::build_ops_and_log_lorasp() {
+    const spand::Plan& P = plan_;
+    long long nnz = 0;
+    auto push = [&](OpRecord r) {
+        switch (r.kind) {  // Operation::nnz (operations.h:32-163)
+            case 0: nnz += (long long)r.ns * (r.ns + 1) / 2; break;
+            case 2: nnz += (long long)r.ns * r.nn; break;
+            case 3: nnz += (long long)r.ns * r.ns; break;
+            default: break;
+        }
+        ops_.push_back(r);
+    };
+    std::vector<char> done(P.nclusters, 0);
+    int next_order = P.nclusters_h;  // the reference numbers a sibling when it creates one
+    for (int rl = 0; rl < (int)P.lr_order.size(); rl++) {
+        LevelLog& G = log_[rl];
+        for (const auto& rec : P.lr_order[rl]) {
+            const int c = rec[0];
+            const spand::LevelPlan& L = P.levels[rec[1]];
+            const spand::SparsifyItem& it = L.waves[0][rec[2]];
+            int blk = -1;
+            for (size_t k = 0; k < L.op_scale_llt.size(); k++)
+                if (L.op_scale_llt[k] == c) blk = L.op_scale_llt_block[k];
+            const int rows = rows0_[c], k = csize_[c];
+            push({0, rl, c, -1, rows, 0, rows, rows, blk, c});
+            G.rank_before_sum += rows;
+            G.rank_after_sum += k;
+            G.rank_after_count += 1;
+            long long cols = 0;
+            for (int p = 0; p < it.count; p++) {
+                const int n = P.asn_pieces[it.first + p].nbr;
+                cols += done[n] ? csize_[n] : rows0_[n];
+            }
+            G.nbrs_sum += cols;
+            G.nbrs_count += 1;
+            if (k < rows) {
+                const int sib = next_order++;
+                push({3, rl, c, -1, rows, 0, rows, k, c});
+                push({5, rl, c, sib, k, rows - k, 0, 0, -1});
+                push({0, rl, sib, -1, rows - k, 0, rows - k, rows - k, -1});
+                for (int q = 0; q < it.scount; q++) {
+                    const spand::LoraSibOp& op = P.lr_sibops[it.sfirst + q];
+                    const int nn = op.cur ? csize_[op.nbr] : rows0_[op.nbr];
+                    push({2, rl, sib, op.nbr, rows - k, nn, rows - k, nn, op.block});
+                }
+            }
+            done[c] = 1;
+        }
+        long long left = 0;
+        for (const auto& rec : P.lr_order[rl]) left += csize_[rec[0]];
+        for (const spand::LevelPlan& L : P.levels)
+            if (L.real == rl)
+                for (int p : L.op_merge) push({4, rl, p, -1, rows0_[p], 0, 0, 0, -1});
+        G.dofs_left_spars = left;
+        G.fact_nnz = nnz;
+    }
+}
+
 void Tree::build_ops_and_log() {
     log_dirty_ = false;
     dev_->sizes(csize_, rows0_);
+    if (plan_.lorasp) {
+        ops_.clear();
+        for (LevelLog& G : log_) G = LevelLog();
+        build_ops_and_log_lorasp();
+        return;
+    }
     ops_.clear();
     for (LevelLog& G : log_) {  // keep the partition counts, recompute the rest
         LevelLog fresh;
@@ -455,6 +553,11 @@ int Tree::get_stop() const {
 std::vector<std::array<int, 4>> Tree::ranks() const {
     ensure_log();
     std::vector<std::array<int, 4>> r;
+    if (plan_.lorasp) {
+        for (int l = 0; l < (int)plan_.lr_order.size(); l++)
+            for (const auto& rec : plan_.lr_order[l]) r.push_back({l, rec[0], rows0_[rec[0]], csize_[rec[0]]});
+        return r;
+    }
     for (int l = 0; l < plan_.nlevels; l++)
         for (int c : plan_.levels[l].op_ortho) r.push_back({l, c, rows0_[c], csize_[c]});
     return r;

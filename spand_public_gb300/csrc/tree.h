@@ -68,6 +68,12 @@ class Tree {
     void set_fp32(bool f) { fp32_ = f; }
 
     std::vector<ClusterID> partition(const Csc& A);
+    // LoRaSp (tree.h:177, tree.cpp:421-503): geometric recursive bisection; returns the part
+    // of every dof (natural ordering).  Then assemble() and factorize_lorasp().
+    std::vector<int> partition_lorasp(const Csc& A);
+    // tree.h:187, tree.cpp:1553-1608 (SPD / LLT)
+    void factorize_lorasp();
+    bool is_lorasp() const { return lorasp_; }
     void assemble(const Csc& A);
     // No counterpart in the reference: new values on the pattern of the last assemble()
     // (CSC order, nnz entries), from host or device memory; the plan and device work lists
@@ -150,6 +156,7 @@ class Tree {
 
    private:
     void build_ops_and_log();
+    void build_ops_and_log_lorasp();
     std::string pivot_error() const;
     void prepare_factorize();  // hands phi to the device (or turns preservation off)
     void ensure_log() const {
@@ -159,6 +166,7 @@ class Tree {
     int nlevels_;
     bool verb_ = true, geo_ = false, use_want_sparsify_ = true, fp32_ = false;
     bool preserve_ = false;
+    bool lorasp_ = false, lorasp_run_ = false;
     std::vector<double> phi_;
     int phi_n_ = 0, nphi_ = 0;
     double tol_ = 10.0;  // tree.cpp:94
