@@ -50,6 +50,25 @@ def test_partition_matches_oracle(n, dim, nlevels):
     assert np.array_equal(o.get_assembly_perm(), t.get_assembly_perm())
 
 
+@pytest.mark.parametrize("n,dim", [(5, 2), (20, 2), (64, 2), (10, 3), (17, 3)])
+def test_partition_lorasp_matches_oracle(n, dim):
+    """LoRaSp ordering (partition_lorasp, tree.cpp:421-503): the recursive-bisection parts and
+    the assembly permutation equal the oracle's."""
+    A = P.neglapl(n, dim)
+    X = P.linspace_nd(n, dim)
+    for nlevels in (2, 3, 5, 7):
+        t = pkg.Tree(nlevels)
+        t.set_verb(False)
+        t.set_use_geo(True)
+        t.set_Xcoo(X)
+        pt = t.partition_lorasp(A)
+        o = OracleTree(nlevels)
+        o.set_Xcoo(X)
+        po = o.partition_lorasp(A)
+        assert np.array_equal(pt, po)
+        assert np.array_equal(t.get_assembly_perm(), o.get_assembly_perm())
+
+
 def test_partition_square_golden(golden):
     g = golden["partition_square"]
     t = pkg.Tree(3)
