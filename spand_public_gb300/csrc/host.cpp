@@ -388,14 +388,18 @@ struct SymTree {
     SymTree(const Hierarchy& h, Plan& p) : H(h), P(p), out(h.start.size()), in(h.start.size()), eliminated(h.start.size(), 0) {}
 
     int new_block(int rowc, int colc, int flag, int64_t& cursor) {
+        return new_block(rowc, colc, flag, cursor, P.c_cap[rowc], P.c_cap[colc]);
+    }
+    // with explicit row / column capacities (the sizes the block can reach from now on)
+    int new_block(int rowc, int colc, int flag, int64_t& cursor, int rcap, int ccap) {
         PlanBlock b;
         b.rowc = rowc;
         b.colc = colc;
         b.flag = flag;
-        b.ld = P.c_cap[rowc];
+        b.ld = std::max(rcap, 1);
         if (flag == BLK_STORED) {
             b.off = cursor;
-            cursor += (int64_t)P.c_cap[rowc] * P.c_cap[colc];
+            cursor += (int64_t)b.ld * std::max(ccap, 0);
             cursor = (cursor + 31) & ~int64_t(31);  // 256-byte aligned blocks in FP64
         }
         P.blocks.push_back(b);
@@ -697,7 +701,11 @@ Plan build_plan(const Hierarchy& H, const Assembly& asmb, int skip, bool use_wan
 // blocks it would have created stay zero (the reference creates none: only extra zero
 // columns of later QRCP matrices, which never change a rank for tol > 0).  Clusters of a
 // level are scheduled in waves (each after every neighbour processed before it, fill-in
-// included); every wave is one level of the plan.
+// included); every wave is one level of the plan.  Capacities: a cluster's size after its
+// sparsification is at most min(its size, the size of its fill-in columns), so a parent's
+// capacity is the sum of its children's bounds after their sparsification, and every block
+// is allocated with the capacities its clusters have when it is created (they only shrink
+// afterwards within the level).
 Plan build_plan_lorasp(const Hierarchy& H, const Assembly& asmb) {
     Plan P;
     P.lorasp = true;
@@ -713,11 +721,13 @@ Plan build_plan_lorasp(const Hierarchy& H, const Assembly& asmb) {
     P.c_children = H.children;
     P.c_order.resize(nc);
     std::iota(P.c_order.begin(), P.c_order.end(), 0);
-    P.c_xoff.resize(nc);
-    for (int c = 0; c < nc; c++) {
+    // solve slots: the leaves now, every parent at its merge (its capacity is known then)
+    P.c_xoff.assign(nc, 0);
+    for (int c : H.bottoms[0]) {
         P.c_xoff[c] = P.x_len;
         P.x_len += H.size[c];
     }
+    std::vector<int> capnow(P.c_cap);  // current capacity bound of every cluster
     SymTree T(H, P);
     int64_t cursor = 0;
     for (size_t li = 0; li < H.bottoms[0].size(); li++) {
@@ -771,7 +781,7 @@ Plan build_plan_lorasp(const Hierarchy& H, const Assembly& asmb) {
             L.op_scale_llt_block.push_back(piv);
             // the new pivot is a stored identity: siblings eliminated later in the level
             // update it (their neighbours' pivots take A^T A)
-            T.edges[pe].block = T.new_block(c, c, BLK_STORED, cursor);
+            T.edges[pe].block = T.new_block(c, c, BLK_STORED, cursor, capnow[c], capnow[c]);
             L.scale_newpiv.push_back(T.edges[pe].block);
             L.snap.push_back(c);
             // ---- sparsify over the fill-in edges ----
@@ -784,12 +794,12 @@ Plan build_plan_lorasp(const Hierarchy& H, const Assembly& asmb) {
             for (int e : ins)
                 if (!T.orig[e]) {
                     P.asn_pieces.push_back({T.edges[e].block, T.edges[e].n1, 0});
-                    cap_cols += P.c_cap[T.edges[e].n1];
+                    cap_cols += capnow[T.edges[e].n1];
                 }
             for (int e : outs)
                 if (!T.orig[e]) {
                     P.asn_pieces.push_back({T.edges[e].block, T.edges[e].n2, 1});
-                    cap_cols += P.c_cap[T.edges[e].n2];
+                    cap_cols += capnow[T.edges[e].n2];
                 }
             it.count = (int)P.asn_pieces.size() - it.first;
             it.cap_cols = cap_cols;
@@ -813,11 +823,12 @@ Plan build_plan_lorasp(const Hierarchy& H, const Assembly& asmb) {
             T.in.emplace_back();
             T.eliminated.push_back(0);
             wave_of.push_back(-1);
+            capnow.push_back(capnow[c]);
             it.sib = sib;
             T.add_edge(sib, sib, T.new_block(sib, sib, BLK_IDENTITY, cursor), true);
             it.ofirst = (int)P.lr_splits.size();
             auto split = [&](int e, int n, int tr) {
-                const int sb = T.new_block(sib, n, BLK_STORED, cursor);
+                const int sb = T.new_block(sib, n, BLK_STORED, cursor, capnow[sib], capnow[n]);
                 P.lr_splits.push_back({T.edges[e].block, n, tr, sb});
                 T.add_edge(n, sib, sb, true);
             };
@@ -838,7 +849,8 @@ Plan build_plan_lorasp(const Hierarchy& H, const Assembly& asmb) {
                     for (int e : T.out[n2])
                         if (T.edges[e].n2 == n1) { found = e; break; }
                     if (found < 0) {
-                        found = T.add_edge(n2, n1, T.new_block(n1, n2, BLK_STORED, cursor), false);
+                        found = T.add_edge(n2, n1, T.new_block(n1, n2, BLK_STORED, cursor, capnow[n1], capnow[n2]),
+                                           false);
                         P.n_fill_blocks++;
                     }
                     const int tb = T.edges[found].block;
@@ -857,6 +869,7 @@ Plan build_plan_lorasp(const Hierarchy& H, const Assembly& asmb) {
             }
             it.scount = (int)P.lr_sibops.size() - it.sfirst;
             T.set_eliminated(sib);
+            capnow[c] = std::min(capnow[c], cap_cols);  // rank <= min(rows, fill-in columns)
             wave_of[c] = w;
             P.lr_order[ilvl].push_back({c, (int)(first + w), (int)L.waves[0].size()});
             L.waves[0].push_back(it);
@@ -892,6 +905,13 @@ Plan build_plan_lorasp(const Hierarchy& H, const Assembly& asmb) {
             const std::vector<int>& parents = H.bottoms[ilvl + 1];
             for (int snew : parents) L.op_merge.push_back(snew);
             L.merge_parents = parents;
+            for (int snew : parents) {  // capacity: the children's bounds after this level
+                int cap = 0;
+                for (int sold : H.children[snew]) cap += capnow[sold];
+                P.c_cap[snew] = capnow[snew] = cap;
+                P.c_xoff[snew] = P.x_len;
+                P.x_len += cap;
+            }
             for (int snew : parents) {
                 std::map<int, char> nnews;
                 for (int sold : H.children[snew])

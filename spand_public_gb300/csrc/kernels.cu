@@ -2651,6 +2651,7 @@ class DeviceFactor : public DeviceFactorBase {
                 W.n = (int)items.size();
                 W.items = up(items);
                 W.maxcap = maxcap;
+                W.ytiles = 1;  // capacities can be 0 (LoRaSp bounds): never an empty grid
                 for (const SparsifyItem& it : wave) {
                     int nt = (P.c_cap[it.cluster] + 31) / 32;
                     for (int p = 0; p < it.count; p++) nt += (P.c_cap[P.asn_pieces[it.first + p].nbr] + 31) / 32;
@@ -4065,7 +4066,7 @@ class DeviceFactor : public DeviceFactorBase {
             cur_count_ = D.n_elim_llt;
             permx(D.elim_llt, D.n_elim_llt, 1, D.x_smem_elim);
             trsv(D.elim_llt, lu_ ? D.elim_inv : D.elim_llt_blk, D.elim_tv, D.n_elim_tv, D.x_smem_elim, 0);
-            if (D.n_gf)
+            if (D.n_gf && D.n_gf_tiles)
                 launch("gemm_fwd", [&] {
                     if (mr)
                         gemm_mrhs_kernel<T><<<D.n_gf_tiles32, 256, 0, s_>>>(ctx_, X, D.gf, D.gfo, D.gf_tiles32, 1);
@@ -4095,7 +4096,7 @@ class DeviceFactor : public DeviceFactorBase {
             cur_count_ = D.n_scale_llt;
             trsv(D.scale_llt, lu_ ? D.scale_inv : D.scale_llt_blk, D.scale_tv, D.n_scale_tv, D.x_smem_scale, 1);
             permx(D.scale_llt, D.n_scale_llt, 0, D.x_smem_scale);
-            if (D.n_gb)
+            if (D.n_gb && D.n_gb_tiles)
                 launch("gemm_bwd", [&] {
                     if (mr)
                         gemm_mrhs_kernel<T><<<D.n_gb_tiles, 256, 0, s_>>>(ctx_, X, D.gb, D.gbo, D.gb_tiles, 0);
