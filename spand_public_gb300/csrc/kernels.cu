@@ -2070,34 +2070,45 @@ __global__ void __launch_bounds__(32 * MRS_WARPS) trsv_mrhs_small_kernel(Ctx<T> 
     for (int j = 0; j < nrb; j++)
         for (int i = lane; i < n; i += 32) xs[i][j] = xcol[i + (size_t)j * X.xld];
     __syncwarp();
-    if (lane < nrb) {
-        if (!trans) {
-            // y_i = x_i / L_ii + sum_{k<i} L^{-1}[i][k] x_k, L^{-1}[i][k] at L[k + i ld]; rows from
-            // the last, so every x_k (k < i) is still the original
-            for (int i = n - 1; i >= 0; i--) {
-                const T* li = L + (size_t)i * ld;
-                T s0 = xs[i][lane] / li[i], s1 = 0;
-                int q = 0;
-                for (; q + 1 < i; q += 2) {
-                    s0 += li[q] * xs[q][lane];
-                    s1 += li[q + 1] * xs[q + 1][lane];
+    // The factor entries of a row come in 32-element chunks, one per lane (coalesced when the
+    // row is contiguous), and reach every lane by shuffle; every lane runs the loops (lanes
+    // past the last right-hand side work on padding and are not written back).
+    if (!trans) {
+        // y_i = x_i / L_ii + sum_{k<i} L^{-1}[i][k] x_k, L^{-1}[i][k] at L[k + i ld]; rows from
+        // the last, so every x_k (k < i) is still the original
+        for (int i = n - 1; i >= 0; i--) {
+            const T* li = L + (size_t)i * ld;
+            T s0 = xs[i][lane] / li[i], s1 = 0;
+            for (int q0 = 0; q0 < i; q0 += 32) {
+                const T lv = q0 + lane < i ? li[q0 + lane] : T(0);
+                const int cnt = min(32, i - q0);
+                int u = 0;
+                for (; u + 1 < cnt; u += 2) {
+                    s0 += __shfl_sync(0xffffffffu, lv, u) * xs[q0 + u][lane];
+                    s1 += __shfl_sync(0xffffffffu, lv, u + 1) * xs[q0 + u + 1][lane];
                 }
-                for (; q < i; q++) s0 += li[q] * xs[q][lane];
-                xs[i][lane] = s0 + s1;
+                if (u < cnt) s0 += __shfl_sync(0xffffffffu, lv, u) * xs[q0 + u][lane];
             }
-        } else {
-            // y_i = x_i / L_ii + sum_{k>i} L^{-1}[k][i] x_k, L^{-1}[k][i] at L[i + k ld]; rows from
-            // the first
-            for (int i = 0; i < n; i++) {
-                T s0 = xs[i][lane] / L[i + (size_t)i * ld], s1 = 0;
-                int q = i + 1;
-                for (; q + 1 < n; q += 2) {
-                    s0 += L[i + (size_t)q * ld] * xs[q][lane];
-                    s1 += L[i + (size_t)(q + 1) * ld] * xs[q + 1][lane];
+            __syncwarp();
+            xs[i][lane] = s0 + s1;
+        }
+    } else {
+        // y_i = x_i / L_ii + sum_{k>i} L^{-1}[k][i] x_k, L^{-1}[k][i] at L[i + k ld]; rows from
+        // the first
+        for (int i = 0; i < n; i++) {
+            T s0 = xs[i][lane] / L[i + (size_t)i * ld], s1 = 0;
+            for (int q0 = i + 1; q0 < n; q0 += 32) {
+                const T lv = q0 + lane < n ? L[i + (size_t)(q0 + lane) * ld] : T(0);
+                const int cnt = min(32, n - q0);
+                int u = 0;
+                for (; u + 1 < cnt; u += 2) {
+                    s0 += __shfl_sync(0xffffffffu, lv, u) * xs[q0 + u][lane];
+                    s1 += __shfl_sync(0xffffffffu, lv, u + 1) * xs[q0 + u + 1][lane];
                 }
-                for (; q < n; q++) s0 += L[i + (size_t)q * ld] * xs[q][lane];
-                xs[i][lane] = s0 + s1;
+                if (u < cnt) s0 += __shfl_sync(0xffffffffu, lv, u) * xs[q0 + u][lane];
             }
+            __syncwarp();
+            xs[i][lane] = s0 + s1;
         }
     }
     __syncwarp();
