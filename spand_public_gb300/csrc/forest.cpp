@@ -19,6 +19,7 @@ Forest::Forest(Tree* const* trees, int count) {
         if (!t || !t->assembled()) throw std::logic_error("forest of trees that are not assembled");
         if (t->get_symm_kind() != SymmKind::SPD) throw std::invalid_argument("a forest holds SPD / LLT systems");
         if (t->get_preserve()) throw std::invalid_argument("a forest does not preserve vectors");
+        if (t->is_lorasp()) throw std::invalid_argument("a forest holds spaND trees (partition(), not partition_lorasp())");
         if (t->get_tol() != t0.get_tol() || t->get_skip() != t0.get_skip() || t->get_fp32() != t0.get_fp32() ||
             t->get_use_sparsify() != t0.get_use_sparsify())
             throw std::invalid_argument("the trees of a forest share tolerance, skip, precision and sparsification");
