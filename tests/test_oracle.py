@@ -400,3 +400,34 @@ def test_lorasp(dim, n):
             assert err <= (1e-10 if tol == 0.0 else tol * 1e2), (nlevels, tol, err)
             x, it = t.cg(b, 100, 1e-10)[:2]
             assert np.linalg.norm(A @ x - b) / np.linalg.norm(b) < 1e-9
+
+
+def test_lapack_mode_baseline():
+    """The timed CPU baseline (bench.py) runs the oracle with the reference's BLAS / LAPACK
+    calls (scipy's OpenBLAS: dgemm, dsyrk, dtrsm, dpotrf, and LAPACK's own dgeqp3 without the
+    tie rule).  It must compute the same preconditioner up to pivot ties: CG to 1e-10 with
+    at most one iteration more or less than the restated oracle, every cluster's rank within
+    one of the restated oracle's (equal on this case)."""
+    A = P.neglapl(16, 3)
+    X = P.linspace_nd(16, 3)
+    b = np.random.default_rng(0).uniform(-1, 1, A.shape[0])
+    res = {}
+    try:
+        for mode in ("restated", "lapack"):
+            if mode == "lapack" and O.use_lapack(1) is None:
+                pytest.skip("no CBLAS / LAPACKE library found next to scipy")
+            t = O.OracleTree(6)
+            t.set_Xcoo(X)
+            t.set_tol(1e-2)
+            t.partition(A)
+            t.assemble(A)
+            t.factorize()
+            x, it = t.cg(b, 100, 1e-10)[:2]
+            assert np.linalg.norm(A @ x - b) / np.linalg.norm(b) < 1e-9
+            res[mode] = (it, t.ranks())
+    finally:
+        O.use_restated()
+    assert abs(res["restated"][0] - res["lapack"][0]) <= 1
+    ra, rb = res["restated"][1], res["lapack"][1]
+    assert np.array_equal(ra[:, :3], rb[:, :3])
+    assert np.abs(ra[:, 3] - rb[:, 3]).max() <= 1
