@@ -375,29 +375,30 @@ def test_preservation(dim, n):
                         assert err < (1e-12 if tol == 0.0 else tol * 1e2), (nlevels, tol, skip, symm, err)
 
 
-@pytest.mark.parametrize("dim,n", [(2, 5), (2, 10), (2, 20), (2, 32), (3, 5), (3, 10)])
+@pytest.mark.parametrize("dim,n", [(2, 5), (2, 10), (2, 20), (2, 64), (3, 5), (3, 15)])
 def test_lorasp(dim, n):
-    """LoRaSp (partition_lorasp tree.cpp:421-503, factorize_lorasp tree.cpp:1553-1608): the
-    recursive bisection gives 2^(nlevels-1) parts of sizes within one of each other on a
-    grid; the factorization is exact at tol 0 (ApproxTest.Exact's bar, 1e-10) and within
-    tol * 1e2 otherwise (ApproxTest.Approx's bar); PCG converges."""
+    """ApproxTest.ApproxLoRaSp (tests/tests.cpp:858-912), SPD / LLT configuration:
+    partition_lorasp + factorize_lorasp for nlevels, ..., nlevels + 4 and tol in
+    {0, 1e-10, 1e-6, 1e-4}; |Ax - b| / |b| <= 5e-12 at tol 0, <= tol * 2e2 otherwise (the
+    reference's b is a seeded uniform vector, restated here with numpy's generator).  Also:
+    2^(nlevels-1) parts, and PCG converges."""
     A = P.neglapl(n, dim)
     X = P.linspace_nd(n, dim)
     N = A.shape[0]
-    for nlevels in (2, 3, 4):
-        for tol in (0.0, 1e-4, 1e-2):
+    lmin = 1 if N < 1000 else 8
+    for nlevels in range(lmin, lmin + 5):
+        for tol in (0.0, 1e-10, 1e-6, 1e-4):
             t = O.OracleTree(nlevels)
             t.set_Xcoo(X)
             t.set_tol(tol)
             parts = t.partition_lorasp(A)
-            sizes = np.bincount(parts, minlength=2 ** (nlevels - 1))
-            assert sizes.size == 2 ** (nlevels - 1)
+            assert np.bincount(parts, minlength=2 ** (nlevels - 1)).size == 2 ** (nlevels - 1)
             t.assemble(A)
             t.factorize_lorasp()
-            b = np.random.default_rng(nlevels).uniform(-1, 1, N)
+            b = np.random.default_rng(nlevels + 2019).uniform(-1, 1, N)
             x = t.solve(b)
             err = np.linalg.norm(A @ x - b) / np.linalg.norm(b)
-            assert err <= (1e-10 if tol == 0.0 else tol * 1e2), (nlevels, tol, err)
+            assert err <= (5e-12 if tol == 0.0 else tol * 2e2), (nlevels, tol, err)
             x, it = t.cg(b, 100, 1e-10)[:2]
             assert np.linalg.norm(A @ x - b) / np.linalg.norm(b) < 1e-9
 
