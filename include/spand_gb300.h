@@ -53,7 +53,7 @@ int spand_tree_set_symm_kind(spand_tree* t, int kind);              /* set_symm_
 /* PartKind {MND=0, RB=1} (include/spaND.h:20)                                           */
 int spand_tree_set_part_kind(spand_tree* t, int kind);              /* set_part_kind     */
 int spand_tree_set_use_sparsify(spand_tree* t, int use);            /* set_use_sparsify  */
-/* set_preserve / set_phi                           -- include/tree.h:140-141
+/* set_preserve / set_phi                           -- include/tree.h:136-137
  * Keep the columns of phi (n x nphi, column-major, natural ordering; copied) in the range
  * of every sparsification: the preconditioner then reproduces them exactly.  SPD and SYM
  * kinds only (factorize returns SPAND_ERR_ARG otherwise, or when phi has not N rows).    */

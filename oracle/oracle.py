@@ -136,7 +136,7 @@ class OracleTree:
     def set_preserve(self, on): self.L.orc_set_preserve(self.h, int(bool(on)))
 
     def set_phi(self, phi):
-        """Vectors to preserve (tree.h:141): N x nphi, natural ordering (copied)."""
+        """Vectors to preserve (tree.h:136): N x nphi, natural ordering (copied)."""
         phi = np.asfortranarray(np.atleast_2d(np.asarray(phi, dtype=np.float64).T).T)
         self.L.orc_set_phi(self.h, _dp(phi), phi.shape[0], phi.shape[1])
 

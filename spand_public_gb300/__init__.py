@@ -203,7 +203,7 @@ class Tree:
     def set_preserve(self, p): _check(self.L.spand_tree_set_preserve(self.h, int(bool(p))))
 
     def set_phi(self, phi):
-        """Vectors to preserve (include/tree.h:141): N x nphi (or N), natural ordering; copied."""
+        """Vectors to preserve (include/tree.h:136): N x nphi (or N), natural ordering; copied."""
         phi = np.asarray(phi, dtype=np.float64)
         if phi.ndim == 1:
             phi = phi[:, None]

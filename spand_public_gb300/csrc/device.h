@@ -116,7 +116,7 @@ class DeviceFactorBase {
     // solve_device with the per-cluster solve vectors in a fixed device array instead of
     // memory allocated by this object (no allocation of any kind on this path)
     virtual void solve_device_noalloc(double* x, int nrhs, int ld) = 0;
-    // preservation (tree.h:140-141): the columns of phi (n x nphi, column-major, natural
+    // preservation (tree.h:136-137): the columns of phi (n x nphi, column-major, natural
     // ordering, host memory; copied) are kept by every sparsification of the following
     // factorizations; nphi = 0 turns it off
     virtual void set_phi(const double* phi, int n, int nphi) = 0;

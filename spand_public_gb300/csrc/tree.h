@@ -58,7 +58,7 @@ class Tree {
     void set_symm_kind(SymmKind k) { symm_ = k; }
     void set_part_kind(PartKind k) { part_kind_ = k; }
     void set_use_sparsify(bool u) { use_want_sparsify_ = u; }
-    // tree.h:140-141: keep the columns of phi in the range of every sparsification
+    // tree.h:136-137: keep the columns of phi in the range of every sparsification
     // (symmetric kinds only).  phi: n x nphi, column-major, natural ordering; copied (the
     // reference borrows the pointer and reads it in factorize()).
     void set_preserve(bool p) { preserve_ = p; }
