@@ -95,13 +95,18 @@ int spand_tree_solve(spand_tree* t, double* x, int nrhs, int ld);
 int spand_tree_solve_device(spand_tree* t, double* x_dev, int nrhs, int ld);
 /* No counterpart in the reference.  spand_tree_solve_device that allocates nothing: the
  * per-cluster solve vectors and their scratch copy live in a fixed 16 MiB device array
- * inside the library instead of memory the tree allocates on its first solve.  For callers
- * that cannot allocate when they solve -- code being captured into a CUDA graph (no
- * cudaMalloc during capture), code with a preallocated memory budget, a framework that owns
- * the allocator.  Limit: 2 * x_len * nrhs * sizeof(factor type) <= 16 MiB, where x_len is the sum of all cluster
- * capacities (about 3N for a 3D grid); larger requests return SPAND_ERR_ARG.  The first call
- * on a device looks up the array's device address; make it before any stream capture.
- * All calls share the array, so allocation-free solves that overlap on the GPU race. */
+ * inside the library (a file-scope static __device__ array, held by every GPU that loads
+ * the library until the process exits) instead of memory the tree allocates on its first
+ * solve.  For callers that cannot call cudaMalloc when they solve: code that must stay
+ * within a device-memory budget fixed in advance, and frameworks whose own allocator owns
+ * the GPU's memory and must not be bypassed.  Limit: 2 * x_len * nrhs * sizeof(factor
+ * type) <= 16 MiB, where x_len is the sum of all cluster capacities (about 3N for a 3D
+ * grid; one right-hand side of a 64^3 problem fits in either precision); a larger request
+ * returns SPAND_ERR_ARG before anything is touched, and its message states x_len.  The
+ * first call on a device looks up the array's device address (cudaGetSymbolAddress, with
+ * the tree's device current); make that first call before any stream capture.  Runs on the
+ * tree's stream and returns without synchronising.  All calls share the array, which keeps
+ * the last call's contents: allocation-free solves that overlap on the GPU race. */
 int spand_tree_solve_device_noalloc(spand_tree* t, double* x_dev, int nrhs, int ld);
 
 /* int cg(const SpMat&, const VectorXd& rhs, VectorXd& x, const Tree&, int iters, double tol, bool verb)

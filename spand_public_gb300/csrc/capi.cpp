@@ -447,6 +447,7 @@ int spand_tree_profile_count(spand_tree* t, int* n) {
     CHECK_T(t);
     if (!t->t->device()) return fail(SPAND_ERR_STATE, "profiling before assemble");
     return guard([&] {
+        spand::DeviceScope scope(t->t->device_id());
         t->t->device()->profiler().collect();
         *n = (int)t->t->device()->profiler().totals().size();
     });
@@ -575,6 +576,7 @@ int spand_forest_set_profiling(spand_forest* f, int on) {
 int spand_forest_profile_count(spand_forest* f, int* n) {
     CHECK_F(f);
     return guard([&] {
+        spand::DeviceScope scope(f->f->device_id());
         f->f->device()->profiler().collect();
         *n = (int)f->f->device()->profiler().totals().size();
     });

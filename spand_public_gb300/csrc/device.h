@@ -34,6 +34,43 @@ struct DeviceError {
     std::string msg;
 };
 
+// Makes `dev` the current CUDA device for the scope's lifetime and gives the caller its
+// own device back afterwards (dev < 0: the current device is left alone).  A tree records
+// the device it was assembled on; every call that touches its memory or stream runs under
+// one of these, so a caller that switched devices in between still reaches the tree's.
+class DeviceScope {
+   public:
+    explicit DeviceScope(int dev) {
+        if (dev < 0) return;
+        if (cudaGetDevice(&prev_) != cudaSuccess) throw DeviceError{SPAND_ERR_CUDA, "cudaGetDevice failed"};
+        if (prev_ == dev) {
+            prev_ = -1;
+            return;
+        }
+        const cudaError_t e = cudaSetDevice(dev);
+        if (e != cudaSuccess) {
+            prev_ = -1;
+            throw DeviceError{SPAND_ERR_CUDA, std::string("cudaSetDevice(tree device): ") + cudaGetErrorString(e)};
+        }
+    }
+    ~DeviceScope() {
+        if (prev_ >= 0) cudaSetDevice(prev_);
+    }
+    DeviceScope(const DeviceScope&) = delete;
+    DeviceScope& operator=(const DeviceScope&) = delete;
+
+   private:
+    int prev_ = -1;
+};
+
+// The current CUDA device (throws DeviceError on failure).
+inline int current_device() {
+    int d = 0;
+    const cudaError_t e = cudaGetDevice(&d);
+    if (e != cudaSuccess) throw DeviceError{SPAND_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e)};
+    return d;
+}
+
 // Per-launch counters: how many kernels ran, for the bench's gpu_launches claim.
 struct LaunchCounter {
     int64_t launches = 0;

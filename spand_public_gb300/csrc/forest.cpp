@@ -72,6 +72,8 @@ Forest::Forest(Tree* const* trees, int count) {
     asmb_ = spand::assembly_structure(H_, App, true);
     plan_ = spand::build_plan(H_, asmb_, t0.get_skip(), t0.get_use_sparsify(), false);
     std::vector<int64_t> amap = spand::assembly_map(plan_, H_, asmb_, A_, perm_);
+    // the forest lives on the device current at its creation
+    device_ = spand::current_device();
     check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
     dev_ = spand::make_device_factor(t0.get_fp32(), stream_, perm_);
     try {
@@ -91,6 +93,7 @@ Forest::Forest(Tree* const* trees, int count) {
 }
 
 Forest::~Forest() {
+    spand::DeviceScope scope(device_);
     dev_.reset();
     work_.release();
     for (auto& p : buf_)
@@ -105,6 +108,7 @@ Forest::~Forest() {
 }
 
 void Forest::assemble_values(const double* vals, int64_t nnz, bool on_device) {
+    spand::DeviceScope scope(device_);
     if (nnz != (int64_t)A_.rowval.size()) throw std::invalid_argument("values do not match the stacked patterns");
     try {
         dev_->assemble_values(vals, nnz, on_device);
@@ -118,6 +122,7 @@ void Forest::assemble_values(const double* vals, int64_t nnz, bool on_device) {
 }
 
 void Forest::factorize_enqueue() {
+    spand::DeviceScope scope(device_);
     try {
         dev_->factorize_enqueue(tol_);
     } catch (spand::DeviceError& e) {
@@ -126,6 +131,7 @@ void Forest::factorize_enqueue() {
 }
 
 void Forest::factorize_finish() {
+    spand::DeviceScope scope(device_);
     failed_system_ = -1;
     try {
         dev_->factorize_finish();
@@ -146,6 +152,7 @@ void Forest::factorize() {
 }
 
 void Forest::solve_device(double* x) const {
+    spand::DeviceScope scope(device_);
     if (!factored_) throw std::logic_error("solve before factorize");
     try {
         dev_->solve_device(x, 1, N());
@@ -155,6 +162,7 @@ void Forest::solve_device(double* x) const {
 }
 
 void Forest::cg_device(const double* b, double* x, int iters, double tol, int* iters_out, double* relres_out) {
+    spand::DeviceScope scope(device_);
     if (!factored_) throw std::logic_error("cg before factorize");
     try {
         spand::device_pcg_segmented(*dev_, dA_, b, x, count(), d_off_, off_.data(), d_seg_, work_, iters, tol,
@@ -165,6 +173,7 @@ void Forest::cg_device(const double* b, double* x, int iters, double tol, int* i
 }
 
 void Forest::cg(const double* b, double* x, int iters, double tol, int* iters_out, double* relres_out) {
+    spand::DeviceScope scope(device_);
     const size_t n = (size_t)N();
     for (auto& p : buf_)
         if (!p) check(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(double)), "cudaMalloc");
@@ -176,6 +185,7 @@ void Forest::cg(const double* b, double* x, int iters, double tol, int* iters_ou
 }
 
 std::vector<std::array<int, 5>> Forest::ranks() const {
+    spand::DeviceScope scope(device_);
     std::vector<int> cs, r0;
     dev_->sizes(cs, r0);
     std::vector<std::array<int, 5>> out;

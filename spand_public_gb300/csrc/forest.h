@@ -50,6 +50,7 @@ class Forest {
 
     spand::DeviceFactorBase* device() const { return dev_.get(); }
     cudaStream_t stream() const { return stream_; }
+    int device_id() const { return device_; }
     int64_t launches() const { return dev_ ? dev_->launches() : 0; }
     void reset_launches() { if (dev_) dev_->reset_launches(); }
     const spand::Plan& plan() const { return plan_; }
@@ -66,6 +67,7 @@ class Forest {
     std::vector<int> perm_;
     std::unique_ptr<spand::DeviceFactorBase> dev_;
     cudaStream_t stream_ = nullptr;
+    int device_ = -1;
     spand::DeviceCsr dA_;
     int* d_cmap_ = nullptr;
     long long* d_off_ = nullptr;

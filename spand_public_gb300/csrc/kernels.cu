@@ -2475,15 +2475,15 @@ constexpr int kMaxDevices = 64;
 static void* g_noalloc_scratch_addr[kMaxDevices];
 static std::once_flag g_noalloc_scratch_once[kMaxDevices];
 
-// Device address of the scratch array on the current device.  In host code the array's
-// name is only a host-side stand-in, so the address is looked up with
-// cudaGetSymbolAddress, once per device, with that device current (the first
-// allocation-free solve on a device does this; make that first call before any stream
-// capture).
-static void* noalloc_solve_scratch() {
-    int dev = 0;
-    SPAND_CUDA(cudaGetDevice(&dev));
+// Device address of the scratch array on device `dev`.  In host code the array's name is
+// only a host-side stand-in, so the address is looked up with cudaGetSymbolAddress, once
+// per device, with that device current (the first allocation-free solve on a device does
+// this; make that first call before any stream capture).  The caller has made `dev` (the
+// tree's device) current; a different current device is refused rather than resolved.
+static void* noalloc_solve_scratch(int dev) {
     if (dev < 0 || dev >= kMaxDevices) throw DeviceError{SPAND_ERR_UNSUPPORTED, "device index out of range"};
+    if (current_device() != dev)
+        throw DeviceError{SPAND_ERR_STATE, "allocation-free solve: the tree's device is not the current device"};
     std::call_once(g_noalloc_scratch_once[dev], [dev] {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_solve_scratch);
@@ -2521,8 +2521,11 @@ static std::vector<DTile> tiles_1d(const std::vector<int>& extents, int tile) {
 template <typename T>
 class DeviceFactor : public DeviceFactorBase {
    public:
-    DeviceFactor(cudaStream_t s, const std::vector<int>& perm) : s_(s), perm_h_(perm) {}
+    // the current device is the tree's: every later call runs with it current
+    DeviceFactor(cudaStream_t s, const std::vector<int>& perm) : s_(s), perm_h_(perm), dev_(current_device()) {}
     ~DeviceFactor() override {
+        drop_factor_graph();
+        for (cudaEvent_t e : tune_ev_) cudaEventDestroy(e);
         if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
         if (graph_) cudaGraphDestroy(graph_);
         if (xs_) cudaFree(xs_);
@@ -3046,14 +3049,60 @@ class DeviceFactor : public DeviceFactorBase {
     }
     const double* device_values() const override { return d_vals_; }
 
+    // factorize() as one CUDA graph: captured on the first factorization after the launch
+    // configuration was tuned, replayed by every later one.  Every size lives in device
+    // memory and the inputs are restored from the HBM-resident assembled blocks, so one
+    // graph serves every re-factorization of the plan; it is captured again when the
+    // tolerance (a kernel argument) or the preservation buffers change.  Profiled runs and
+    // SPAND_CHECK_LAUNCHES run the launches one by one.
     void factorize_enqueue(double tol) override {
+        last_tol_ = tol;
+        if (measure_next_) {
+            // the factorization after tuning times the candidate QRCP launches per wave
+            measure_next_ = false;
+            measuring_ = true;
+            enqueue_factor(tol);
+            return;
+        }
+        const bool graphable = use_fgraph_ && tuned_ && !prof_.enabled() && !check_launches_;
+        if (!graphable) {
+            enqueue_factor(tol);
+            return;
+        }
+        if (!fgraph_exec_ || fgraph_tol_ != tol || fgraph_nphi_ != nphi_) {
+            drop_factor_graph();
+            const int64_t before = launches_;
+            SPAND_CUDA(cudaStreamBeginCapture(s_, cudaStreamCaptureModeThreadLocal));
+            try {
+                enqueue_factor(tol);
+            } catch (...) {
+                cudaGraph_t g = nullptr;
+                cudaStreamEndCapture(s_, &g);
+                if (g) cudaGraphDestroy(g);
+                launches_ = before;
+                throw;
+            }
+            SPAND_CUDA(cudaStreamEndCapture(s_, &fgraph_));
+            SPAND_CUDA(cudaGraphInstantiate(&fgraph_exec_, fgraph_, 0));
+            fgraph_kernels_ = launches_ - before;
+            launches_ = before;
+            fgraph_tol_ = tol;
+            fgraph_nphi_ = nphi_;
+        }
+        SPAND_CUDA(cudaGraphLaunch(fgraph_exec_, s_));
+        launches_ += fgraph_kernels_;
+    }
+    void drop_factor_graph() {
+        if (fgraph_exec_) cudaGraphExecDestroy(fgraph_exec_);
+        if (fgraph_) cudaGraphDestroy(fgraph_);
+        fgraph_exec_ = nullptr;
+        fgraph_ = nullptr;
+    }
+    int64_t factor_graph_kernels() const { return fgraph_exec_ ? fgraph_kernels_ : -1; }
+
+    void enqueue_factor(double tol) {
         const Plan& P = *P_;
         // inputs: the assembled blocks (device copy) and the initial cluster sizes
-        if (probe_level_ >= 0) {
-            if (!probe_) probe_ = alloc<unsigned long long>(8);
-            SPAND_CUDA(cudaMemsetAsync(probe_, 0, 8 * sizeof(unsigned long long), s_));
-            probe_waves_ = 0;
-        }
         launch("restore", [&] {
             if (P.assembled_len)
                 SPAND_CUDA(cudaMemcpyAsync(arena_, pristine_, P.assembled_len * sizeof(T), cudaMemcpyDeviceToDevice, s_));
@@ -3238,22 +3287,20 @@ class DeviceFactor : public DeviceFactorBase {
 
     void factorize_finish() override {
         SPAND_CUDA(cudaStreamSynchronize(s_));
-        if (probe_) {
-            unsigned long long h[8];
-            SPAND_CUDA(cudaMemcpyAsync(h, probe_, sizeof(h), cudaMemcpyDeviceToHost, s_));
-            SPAND_CUDA(cudaStreamSynchronize(s_));
-            fprintf(stderr, "qrcp probe level %d (%d waves, first cluster of each): steps %llu | cycles/step:", probe_level_,
-                    probe_waves_, h[7]);
-            const char* nm[7] = {"init", "pivot", "pend", "load+householder", "apply", "publish", "barrier"};
-            for (int k = 0; k < 7; k++) fprintf(stderr, " %s %.0f", nm[k], h[7] ? (double)h[k] / h[7] : 0.0);
-            fprintf(stderr, "\n");
-        }
         const DStatus st = *h_status_;
         failed_cluster_ = st.not_spd - 1;
         if (st.not_spd)
             throw DeviceError{SPAND_ERR_NOT_SPD, std::string(lu_ || ldlt_ ? "Error: Singular Pivot" : "Error: Non-SPD Pivot") +
                                                      " (cluster " + std::to_string(st.not_spd - 1) + ")"};
         factored_ = true;
+        if (measuring_) {
+            measuring_ = false;
+            std::vector<QcConf> chosen;
+            for (LevelDev& D : levels_)
+                for (WaveDev& W : D.waves) chosen.push_back(QcConf{W.rpl, W.cs, W.threads, W.smem, 0.0});
+            std::lock_guard<std::mutex> lk(qc_tune_mutex());
+            qc_tune_cache()[tune_key_] = chosen;
+        }
         if (!tuned_) tune_qrcp();
     }
 
@@ -3262,6 +3309,11 @@ class DeviceFactor : public DeviceFactorBase {
     void tune_qrcp() {
         std::vector<int> cs, r0;
         sizes(cs, r0);
+        {
+            char buf[96];
+            snprintf(buf, sizeof(buf), "T%d|sm%d|tol%a|", (int)sizeof(T), num_sms_, last_tol_);
+            tune_key_ = buf;
+        }
         for (LevelDev& D : levels_) {
             std::map<int, int> wave_of;
             for (size_t w = 0; w < D.waves.size(); w++)
@@ -3279,14 +3331,18 @@ class DeviceFactor : public DeviceFactorBase {
                     int rows = r0[it.cluster];
                     dims.push_back({rows + rows / 10 + 1, (int)(cols + cols / 10 + 1)});
                 }
-                choose_cluster(D.waves[w], dims);
+                choose_cluster(D.waves[w], dims, measure_on_);
+                tune_key_ += std::to_string(D.waves[w].n) + ":";
+                for (const auto& d : dims) tune_key_ += std::to_string(d.first) + "x" + std::to_string(d.second) + ",";
+                tune_key_ += ";";
                 if (per_wave_) {
                     int maxr = 0;
                     for (const SparsifyItem& it : D.waves[w].host) maxr = std::max(maxr, r0[it.cluster]);
                     const WaveDev& Wv = D.waves[w];
-                    fprintf(stderr, "qrcp wave L%d w%zu: items %d max rows %d cs %d threads %d smem %d active %d\n",
-                            (int)(&D - levels_.data()), w, Wv.n, maxr, Wv.cs, Wv.threads, Wv.smem,
-                            active_clusters(Wv.n * Wv.cs, Wv.cs, Wv.smem, Wv.threads));
+                    fprintf(stderr, "qrcp wave L%d w%zu: items %d max rows %d rpl %d cs %d threads %d smem %d active %d\n",
+                            (int)(&D - levels_.data()), w, Wv.n, maxr, Wv.rpl, Wv.cs, Wv.threads, Wv.smem,
+                            active_clusters(Wv.n * Wv.cs, Wv.cs, Wv.smem, Wv.threads,
+                                            Wv.rpl ? qrcp_blocked_kernel_ptr<T>(Wv.rpl) : nullptr));
                 }
             }
         }
@@ -3313,6 +3369,21 @@ class DeviceFactor : public DeviceFactorBase {
             }
         }
         tuned_ = true;
+        // configurations measured before for the same plan, sizes, tolerance and GPU: no
+        // measuring factorization
+        measure_next_ = false;
+        if (measure_on_) {
+            std::lock_guard<std::mutex> lk(qc_tune_mutex());
+            auto hit = qc_tune_cache().find(tune_key_);
+            if (hit != qc_tune_cache().end() && hit->second.size() == n_waves()) {
+                size_t k = 0;
+                for (LevelDev& D : levels_)
+                    for (WaveDev& W : D.waves) apply_conf(W, hit->second[k++]);
+            } else {
+                for (LevelDev& D : levels_)
+                    for (WaveDev& W : D.waves) measure_next_ |= W.cands.size() > 1;
+            }
+        }
     }
 
     void solve_device(double* x, int nrhs, int ld) override {
@@ -3335,6 +3406,7 @@ class DeviceFactor : public DeviceFactorBase {
         if (n != (int)perm_h_.size()) throw DeviceError{SPAND_ERR_ARG, "phi does not match the matrix size"};
         long long capsum = 0;
         for (int c0 = 0; c0 < P.nclusters_h; c0++) capsum += P.c_cap[c0];
+        if (nphi > phi_alloc_ || !rank1_ || nphi != nphi_ || !d_phioff_) drop_factor_graph();  // buffers change
         if (nphi > phi_alloc_) {
             phis_ = alloc<T>(capsum * nphi);
             phitmp_ = alloc<T>(capsum * nphi);
@@ -3386,7 +3458,7 @@ class DeviceFactor : public DeviceFactorBase {
                                                  std::to_string(xld_) + " x " + std::to_string(nrhs) + " x " +
                                                  std::to_string(sizeof(T)) + "); its fixed scratch holds " +
                                                  std::to_string(kNoAllocSolveScratchBytes) + " bytes"};
-        T* slots = static_cast<T*>(noalloc_solve_scratch());
+        T* slots = static_cast<T*>(noalloc_solve_scratch(dev_));
         const bool was_on = prof_.enabled();  // the profiler creates CUDA events
         prof_.enable(false);
         try {
@@ -3503,10 +3575,17 @@ class DeviceFactor : public DeviceFactorBase {
         int ntiles = 0;
         int smem = 0;
     };
+    // one launch configuration of a wave's shared-memory QRCP (rpl 0: the unblocked kernel)
+    struct QcConf {
+        int rpl = 0, cs = 1, threads = QC_THREADS, smem = 0;
+        double est = 0.0;  // the launch model's estimate (arbitrary units)
+    };
     struct WaveDev {
         int n = 0;
         DSpars* items = nullptr;
         int maxcap = 1;
+        std::vector<QcConf> cands;  // launch configurations the measuring factorization times
+        int rpl = 0;         // > 0: the blocked QRCP for up to 32 * rpl rows; 0: the unblocked kernel
         int cs = 1;          // CTAs per thread-block cluster of the shared-memory QRCP
         int threads = QC_THREADS;  // threads per CTA of that launch
         int smem = 0;        // dynamic shared memory per CTA
@@ -3665,6 +3744,7 @@ class DeviceFactor : public DeviceFactorBase {
     // ---- QRCP launch configuration -------------------------------------------------
     int qc_smem_cap_ = 0;  // dynamic shared memory per CTA available to the QRCP kernel
     int qc_max_cs_ = 8;    // largest cluster (16 where non-portable sizes are allowed)
+    int qb_smem_cap_ = 0;  // the same for the blocked QRCP kernels
     int num_sms_ = 1;
     void init_qrcp_limits() {
         int dev = 0, optin = 0;
@@ -3692,9 +3772,30 @@ class DeviceFactor : public DeviceFactorBase {
         } else {
             cudaGetLastError();
         }
+        // the blocked QRCP: every row-count instantiation gets the largest dynamic shared
+        // memory its static arrays leave (the smallest of them is the cap) and, like the
+        // unblocked kernel, non-portable cluster sizes
+        qb_smem_cap_ = qc_smem_cap_;
+        for (int rpl : {1, 2, 4, 8, 12}) {
+            const QcKernel<T> b = qrcp_blocked_kernel_ptr<T>(rpl);
+            SPAND_CUDA(cudaFuncGetAttributes(&fa, b));
+            qb_smem_cap_ = std::min(qb_smem_cap_, (int)(optin - (int)fa.sharedSizeBytes) & ~255);
+        }
+        for (int rpl : {1, 2, 4, 8, 12}) {
+            const QcKernel<T> b = qrcp_blocked_kernel_ptr<T>(rpl);
+            SPAND_CUDA(cudaFuncSetAttribute(b, cudaFuncAttributeMaxDynamicSharedMemorySize, qb_smem_cap_));
+            if (qc_max_cs_ > 8 && cudaFuncSetAttribute(b, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+                cudaGetLastError();
+        }
+    }
+    // rows-per-lane instantiation of the blocked QRCP for matrices of up to `rows` rows (0: none)
+    static int qb_rpl(int rows) {
+        for (int r : {1, 2, 4, 8, 12})
+            if (rows <= 32 * r) return r;
+        return 0;
     }
     // co-resident thread-block clusters of a QRCP configuration (-1: not launchable)
-    int active_clusters(int ctas, int cs, int smem, int threads = QC_THREADS) {
+    int active_clusters(int ctas, int cs, int smem, int threads = QC_THREADS, QcKernel<T> fn = nullptr) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3((unsigned)ctas);
         cfg.blockDim = dim3((unsigned)threads);
@@ -3707,7 +3808,7 @@ class DeviceFactor : public DeviceFactorBase {
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         int n = -1;
-        if (cudaOccupancyMaxActiveClusters(&n, qrcp_smem_kernel_ptr<T>(), &cfg) != cudaSuccess) {
+        if (cudaOccupancyMaxActiveClusters(&n, fn ? fn : qrcp_smem_kernel_ptr<T>(), &cfg) != cudaSuccess) {
             cudaGetLastError();
             n = -1;
         }
@@ -3720,9 +3821,10 @@ class DeviceFactor : public DeviceFactorBase {
     // 64-thread CTAs fit eight, which the many small matrices of the lower levels use); the
     // estimate is rounds x (per-step latency + passes over the largest slab by the CTA's
     // threads) and the smallest wins.
-    void choose_cluster(WaveDev& W, const std::vector<std::pair<int, int>>& dims) {
+    void choose_cluster(WaveDev& W, const std::vector<std::pair<int, int>>& dims, bool collect = false) {
         double best = 1e300;
         int bcs = 0, bsm = 0, bth = QC_THREADS;
+        std::vector<QcConf> all;  // every launchable configuration with its estimate
         // SPAND_QC_CS=<cs>, SPAND_QC_THREADS=<n>: that configuration wherever the matrices
         // fit (measurement aids)
         const int force = getenv("SPAND_QC_CS") ? atoi(getenv("SPAND_QC_CS")) : 0;
@@ -3745,6 +3847,7 @@ class DeviceFactor : public DeviceFactorBase {
                                        5.0 / 32.0 * (double)work * ((double)QC_THREADS / th));
                 if (force > 0 && cs != force) est = 1e200;
                 if (force_th > 0 && th != force_th) est = 1e200;
+                if (est < 1e200) all.push_back(QcConf{0, cs, th, (int)sm, est});
                 if (est < best) {
                     best = est;
                     bcs = cs;
@@ -3753,16 +3856,73 @@ class DeviceFactor : public DeviceFactorBase {
                 }
             }
         }
+        // the blocked kernel (plain QRCP only): one read of the slab per pivot step and a
+        // panel update every QB_NB steps instead of four loads and a store per element;
+        // SPAND_QC_BLOCKED=0 / 1 never / always takes it where the matrices fit
+        int brpl = 0;
+        const char* fb = getenv("SPAND_QC_BLOCKED");
+        const int force_b = fb ? atoi(fb) : -1;
+        int maxrows = 0;
+        for (const auto& d : dims) maxrows = std::max(maxrows, d.first);
+        const int rpl = qb_rpl(maxrows);
+        if (rpl > 0 && !(nphi_ && pres_adaptive_) && force_b != 0) {
+            const QcKernel<T> fn = qrcp_blocked_kernel_ptr<T>(rpl);
+            if (force_b == 1) best = 1e300;
+            for (int cs = 1; cs <= qc_max_cs_; cs *= 2) {
+                int64_t sm = 4096, work = 0;
+                for (const auto& d : dims) {
+                    sm = std::max<int64_t>(sm, qb_need(d.first, d.second, cs, (int)sizeof(T)));
+                    work = std::max(work, (int64_t)d.first * ((d.second + cs - 1) / cs));
+                }
+                sm = (sm + 255) & ~int64_t(255);
+                if (sm > qb_smem_cap_) continue;
+                for (int th = 64; th <= QC_THREADS; th *= 2) {
+                    const int active = active_clusters(W.n * cs, cs, (int)sm, th, fn);
+                    if (active <= 0) continue;
+                    const int rounds = (W.n + active - 1) / active;
+                    double est = rounds * (4500.0 + 500.0 * std::log2((double)cs) +
+                                           1.5 / 32.0 * (double)work * ((double)QC_THREADS / th));
+                    if (force > 0 && cs != force) est = 1e200;
+                    if (force_th > 0 && th != force_th) est = 1e200;
+                    if (est < 1e200) all.push_back(QcConf{rpl, cs, th, (int)sm, est});
+                    if (est < best) {
+                        best = est;
+                        bcs = cs;
+                        bsm = (int)sm;
+                        bth = th;
+                        brpl = rpl;
+                    }
+                }
+            }
+        }
         if (!bcs) {  // matrices above the cap take the global-memory path
+            W.rpl = 0;
             W.cs = qc_max_cs_;
             W.smem = qc_smem_cap_;
             W.threads = QC_THREADS;
             return;
         }
+        W.rpl = brpl;
         W.cs = bcs;
         W.smem = bsm;
         W.threads = bth;
+        W.cands.clear();
+        if (collect && force_b < 0 && force <= 0 && force_th <= 0) {
+            // the measuring factorization times the model's best configurations of each
+            // kernel (QC_TUNE_PER_KIND each, the model's pick first)
+            std::stable_sort(all.begin(), all.end(), [](const QcConf& a, const QcConf& b) { return a.est < b.est; });
+            W.cands.push_back(QcConf{brpl, bcs, bth, bsm, best});
+            int taken[2] = {0, 0};
+            for (const QcConf& q : all) {
+                const int kind = q.rpl > 0;
+                if (taken[kind] >= QC_TUNE_PER_KIND) continue;
+                taken[kind]++;
+                if (q.rpl == brpl && q.cs == bcs && q.threads == bth) continue;
+                W.cands.push_back(q);
+            }
+        }
     }
+    static constexpr int QC_TUNE_PER_KIND = 3;
     QcProj<T> qc_proj() const {
         if (nphi_ && pres_adaptive_) return QcProj<T>{vstore_, rank1_};
         return QcProj<T>{nullptr, nullptr};
@@ -3783,9 +3943,63 @@ class DeviceFactor : public DeviceFactorBase {
         cfg.numAttrs = 1;
         SPAND_CUDA(cudaLaunchKernelEx(&cfg, qrcp_gslab_kernel_ptr<T>(), ctx_, (const DSpars*)W.items,
                                       (const DAsn*)pieces_, ws_, ws2_, jpvt_, ipvt_, tauws_, rank_, colcount_,
-                                      fallback_, tol, W.gsmem, (unsigned long long*)nullptr, qc_proj()));
+                                      fallback_, tol, W.gsmem, qc_proj()));
     }
+    void apply_conf(WaveDev& W, const QcConf& q) {
+        W.rpl = q.rpl;
+        W.cs = q.cs;
+        W.threads = q.threads;
+        W.smem = q.smem;
+        W.cands.clear();
+    }
+    size_t n_waves() const {
+        size_t n = 0;
+        for (const LevelDev& D : levels_) n += D.waves.size();
+        return n;
+    }
+    // Measured choice: every candidate of the wave on the same inputs (the kernel only
+    // reads the edge blocks and sizes and rewrites its own outputs), timed with events on
+    // the stream, then the fastest once more so that its outputs are the ones that stay.
     void launch_qrcp_cluster(WaveDev& W, double tol) {
+        if (!measuring_ || W.cands.size() < 2) {
+            launch_qrcp_once(W, tol);
+            return;
+        }
+        const size_t K = W.cands.size();
+        while (tune_ev_.size() < 2 * K) {
+            cudaEvent_t e;
+            SPAND_CUDA(cudaEventCreate(&e));
+            tune_ev_.push_back(e);
+        }
+        for (size_t k = 0; k < K; k++) {
+            apply_conf_keep(W, W.cands[k]);
+            SPAND_CUDA(cudaEventRecord(tune_ev_[2 * k], s_));
+            launch_qrcp_once(W, tol);
+            SPAND_CUDA(cudaEventRecord(tune_ev_[2 * k + 1], s_));
+        }
+        SPAND_CUDA(cudaEventSynchronize(tune_ev_[2 * K - 1]));
+        size_t bk = 0;
+        float bms = 1e30f;
+        for (size_t k = 0; k < K; k++) {
+            float ms = 0;
+            SPAND_CUDA(cudaEventElapsedTime(&ms, tune_ev_[2 * k], tune_ev_[2 * k + 1]));
+            if (ms < bms) {
+                bms = ms;
+                bk = k;
+            }
+        }
+        const QcConf q = W.cands[bk];
+        apply_conf(W, q);
+        launch_qrcp_once(W, tol);
+        launches_ += (int64_t)K;
+    }
+    void apply_conf_keep(WaveDev& W, const QcConf& q) {
+        W.rpl = q.rpl;
+        W.cs = q.cs;
+        W.threads = q.threads;
+        W.smem = q.smem;
+    }
+    void launch_qrcp_once(WaveDev& W, double tol) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3((unsigned)(W.n * W.cs));
         cfg.blockDim = dim3((unsigned)W.threads);
@@ -3798,14 +4012,10 @@ class DeviceFactor : public DeviceFactorBase {
         attr[0].val.clusterDim.z = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        unsigned long long* probe = nullptr;
-        if (probe_level_ == cur_level_ && probe_) {
-            probe = probe_;
-            probe_waves_ += 1;
-        }
-        SPAND_CUDA(cudaLaunchKernelEx(&cfg, qrcp_smem_kernel_ptr<T>(), ctx_, (const DSpars*)W.items,
-                                      (const DAsn*)pieces_, ws_, (T*)nullptr, jpvt_, ipvt_, tauws_, rank_, colcount_,
-                                      fallback_, tol, force_global_ ? 0 : W.smem, probe, qc_proj()));
+        const QcKernel<T> fn = W.rpl > 0 && !force_global_ ? qrcp_blocked_kernel_ptr<T>(W.rpl) : qrcp_smem_kernel_ptr<T>();
+        SPAND_CUDA(cudaLaunchKernelEx(&cfg, fn, ctx_, (const DSpars*)W.items, (const DAsn*)pieces_, ws_, (T*)nullptr,
+                                      jpvt_, ipvt_, tauws_, rank_, colcount_, fallback_, tol,
+                                      force_global_ ? 0 : W.smem, qc_proj()));
     }
     void launch_potrf(int* pivots, int* clusters, int n, int smem, const TrtriDev& tri, int pc_cs, int pc_smem) {
         if (pc_cs > 0) {
@@ -4128,6 +4338,7 @@ class DeviceFactor : public DeviceFactorBase {
 
     cudaStream_t s_;
     std::vector<int> perm_h_;
+    int dev_;  // the CUDA device of the stream and of every allocation
     std::vector<int> caps_h_;
     const Plan* P_ = nullptr;
     int nc_ = 0;
@@ -4173,11 +4384,31 @@ class DeviceFactor : public DeviceFactorBase {
     int* diag_ = nullptr;
     int n_diag_ = 0, diag_smem_ = 0;
     bool tuned_ = false;
+    // measured QRCP tuning: the factorization after tune_qrcp() times every wave's
+    // candidates (SPAND_QC_TUNE=0: the launch model's choice only); the winners are kept per
+    // plan fingerprint for the process (trees of the same plan skip the measurement)
+    bool measure_on_ = !(getenv("SPAND_QC_TUNE") && atoi(getenv("SPAND_QC_TUNE")) == 0);
+    bool measure_next_ = false, measuring_ = false;
+    double last_tol_ = 0.0;
+    std::string tune_key_;
+    std::vector<cudaEvent_t> tune_ev_;
+    static std::mutex& qc_tune_mutex() {
+        static std::mutex m;
+        return m;
+    }
+    static std::map<std::string, std::vector<QcConf>>& qc_tune_cache() {
+        static std::map<std::string, std::vector<QcConf>> c;
+        return c;
+    }
+    // the factorization's CUDA graph (SPAND_FACTOR_GRAPH=0: launches one by one)
+    bool use_fgraph_ = !(getenv("SPAND_FACTOR_GRAPH") && atoi(getenv("SPAND_FACTOR_GRAPH")) == 0);
+    cudaGraph_t fgraph_ = nullptr;
+    cudaGraphExec_t fgraph_exec_ = nullptr;
+    int64_t fgraph_kernels_ = 0;
+    double fgraph_tol_ = -1.0;
+    int fgraph_nphi_ = -1;
     int cur_level_ = -1;
     // in-kernel phase timing of the QRCP of one level (SPAND_QC_PROBE=<level>)
-    int probe_level_ = getenv("SPAND_QC_PROBE") ? atoi(getenv("SPAND_QC_PROBE")) : -2;
-    unsigned long long* probe_ = nullptr;
-    int probe_waves_ = 0;
     // per-level kernel classes in the profile (SPAND_PROFILE_LEVELS=1)
     bool per_level_ = getenv("SPAND_PROFILE_LEVELS") != nullptr;
     // every sparsification matrix through the global-memory QRCP on full clusters

@@ -56,8 +56,7 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, cons
                                                                   const DAsn* __restrict__ pieces, T* ws, T* gslab,
                                                                   int* jpvt_ws, int* ipvt_ws, T* taus,
                                                                   int* rank_out, int* colcount, int* fallback,
-                                                                  double tol, int smem_bytes,
-                                                                  unsigned long long* probe, QcProj<T> proj) {
+                                                                  double tol, int smem_bytes, QcProj<T> proj) {
     namespace cgx = cooperative_groups;
     cgx::cluster_group cl = cgx::this_cluster();
     const int CS = (int)cl.num_blocks();
@@ -114,31 +113,7 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, cons
     const int tid = threadIdx.x, nth = blockDim.x;
     const int lane = tid & 31, w = tid >> 5, nw = nth >> 5;
     // gather the slab of Asn = [A_sn | A_ns^T]
-    {
-        int col = 0;
-        for (int p = 0; p < it.count && col < c1; p++) {
-            const DAsn pc = pieces[it.first + p];
-            const int n = c.csize[pc.nbr];
-            const int lo = max(col, c0), hi = min(col + n, c1);
-            if (lo < hi) {
-                const T* B = bptr(c, pc.block);
-                const int bld = c.blk[pc.block].ld;
-                const int width = hi - lo;
-                if (!pc.transposed) {
-                    for (int idx = tid; idx < rows * width; idx += nth) {
-                        int i = idx % rows, jj = idx / rows;
-                        A[i + (size_t)(lo - c0 + jj) * lda] = B[i + (size_t)(lo - col + jj) * bld];
-                    }
-                } else {
-                    for (int idx = tid; idx < rows * width; idx += nth) {
-                        int jj = idx % width, i = idx / width;
-                        A[i + (size_t)(lo - c0 + jj) * lda] = B[(lo - col + jj) + (size_t)i * bld];
-                    }
-                }
-            }
-            col += n;
-        }
-    }
+    qc_gather_slab(c, it, pieces, rows, c0, c1, A, lda);
     for (int p = tid; p < cols; p += nth) perm[p] = p;
     for (int j = tid; j < nloc; j += nth) pos[j] = c0 + j;
     __syncthreads();
@@ -209,17 +184,6 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, cons
         }
     };
 
-    // phase probe: cycles accumulated in registers, added to probe[] once at the end
-    const bool probing = probe && item == 0 && me == 0 && tid == 0;
-    long long tmark = probing ? clock64() : 0;
-    unsigned long long pacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    auto mark = [&](int k) {
-        if (probing) {
-            long long t = clock64();
-            pacc[k] += (unsigned long long)(t - tmark);
-            tmark = t;
-        }
-    };
     __syncthreads();  // norms of every slab column written
     {
         T m = 0;
@@ -228,7 +192,6 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, cons
         publish(0, 0, m);
     }
     qc_barrier(cl, CS);
-    mark(0);
     int rank = mn;
     T r00 = 0;
     int pend = -1;  // local column awaiting its reflector (scaled vsh rows > pend_i, beta at pend_i)
@@ -274,7 +237,6 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, cons
         const int phys = perm[pvt];
         const int phys_i = perm[i];
         const int own = phys / cpc, lj = phys - own * cpc;
-        mark(1);
         // (2) the previous reflector into its column (owner) and the pivot column into vsh,
         // both with the row -> thread map r = tid (mod nth): a thread reads its old vsh rows
         // before it overwrites them
@@ -296,7 +258,6 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, cons
         part = warp_sum(part);
         if (lane == 0) red[w] = part;
         __syncthreads();  // partial norms, alpha; every thread has read perm
-        mark(2);
         T xnorm2 = 0;
         for (int k = 0; k < nw; k++) xnorm2 += red[k];
         const T alpha = s_alpha;
@@ -324,7 +285,6 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, cons
             perm[i] = phys;
             perm[pvt] = phys_i;
         }
-        mark(3);
         // (3) H = I - tu v v^T, v = [1; sc * vsh[i+1:]], on this slab's columns at positions
         // >= i (positions after the swap), norms downdated (LAWN 176) by the group's first
         // lane.  The loop runs the same number of times in every thread so that the group
@@ -405,7 +365,6 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, cons
             }
             if (j < nloc && gl == 0 && ph == phys) pos[j] = i;
         }
-        mark(4);
         if (own == me) {
             pend = lj;
             pend_i = i;
@@ -414,14 +373,9 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, cons
         }
         if (i + 1 < mn) {
             publish(par ^ 1, i + 1, mloc);
-            mark(5);
             qc_barrier(cl, CS);
-            mark(6);
         }
-        if (probing) pacc[7] += 1;
     }
-    if (probing)
-        for (int k = 0; k < 8; k++) probe[k] += pacc[k];
     // no CTA reads another's shared memory after this barrier (nor leaves before it)
     qc_barrier(cl, CS);
     if (pend >= 0) {

@@ -50,6 +50,7 @@ Tree::Tree(int nlevels) : nlevels_(nlevels) {
 }
 
 double* Tree::cg_buffer(int which, int n) const {
+    spand::DeviceScope scope(device_);
     if (cg_len_ < (size_t)n) {
         for (auto& p : cg_buf_)
             if (p) cudaFree(p);
@@ -62,6 +63,7 @@ double* Tree::cg_buffer(int which, int n) const {
 }
 
 Tree::~Tree() {
+    spand::DeviceScope scope(device_);
     dev_.reset();
     for (auto& p : cg_buf_)
         if (p) cudaFree(p);
@@ -131,6 +133,7 @@ void Tree::factorize_lorasp() {
 // pattern only copy the new values and scatter them.
 void Tree::assemble(const Csc& A) {
     if (!partitioned_) throw std::logic_error("assemble() before partition()");
+    spand::DeviceScope scope(device_);
     const bool lu = symm_ == SymmKind::GEN;
     const bool ldlt = symm_ == SymmKind::SYM;
     if (!((symm_ == SymmKind::SPD && scaling_ == ScalingKind::LLT) || (lu && scaling_ == ScalingKind::PLU) ||
@@ -151,7 +154,11 @@ void Tree::assemble(const Csc& A) {
             plan_ = spand::build_plan(H_, asmb_, skip_, use_want_sparsify_, lu, ldlt);
         }
         std::vector<int64_t> amap = spand::assembly_map(plan_, H_, asmb_, A, perm_);
-        if (!stream_) cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+        if (!stream_) {
+            // the tree lives on the device current at its first assembly
+            device_ = spand::current_device();
+            cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+        }
         dev_ = spand::make_device_factor(fp32_, stream_, perm_);
         try {
             dev_->upload(plan_, amap);
@@ -179,6 +186,7 @@ void Tree::assemble(const Csc& A) {
 }
 
 bool Tree::assemble_same_pattern(int n, const int* colptr, const int* rowval, const double* vals) {
+    spand::DeviceScope scope(device_);
     if (!assembled_ok_ || !dev_ || n != A_.n || !colptr || !vals) return false;
     if (std::memcmp(colptr, A_.colptr.data(), ((size_t)n + 1) * sizeof(int)) != 0) return false;
     const size_t nnz = A_.rowval.size();
@@ -199,6 +207,7 @@ bool Tree::assemble_same_pattern(int n, const int* colptr, const int* rowval, co
 }
 
 void Tree::assemble_values(const double* vals, int64_t nnz, bool on_device) {
+    spand::DeviceScope scope(device_);
     if (!assembled_ok_ || !dev_) throw std::logic_error("assemble_values() before assemble()");
     if (nnz != (int64_t)A_.rowval.size()) throw std::invalid_argument("values do not match the assembled pattern");
     double t0 = now_s();
@@ -249,6 +258,7 @@ void Tree::prepare_factorize() {
 
 // tree.cpp:1447-1551
 void Tree::factorize() {
+    spand::DeviceScope scope(device_);
     prepare_factorize();
     double t0 = now_s();
     try {
@@ -266,6 +276,7 @@ void Tree::factorize() {
 }
 
 void Tree::factorize_enqueue() {
+    spand::DeviceScope scope(device_);
     prepare_factorize();
     try {
         dev_->factorize_enqueue(tol_);
@@ -275,6 +286,7 @@ void Tree::factorize_enqueue() {
 }
 
 void Tree::factorize_finish() {
+    spand::DeviceScope scope(device_);
     try {
         dev_->factorize_finish();
     } catch (spand::DeviceError& e) {
@@ -294,6 +306,7 @@ spand::PcgWork& Tree::pcg_work() const {
 }
 
 void Tree::bench_step(const double* b_dev, double* x_dev, int nrhs, int iters, double tol, double out[4]) {
+    spand::DeviceScope scope(device_);
     prepare_factorize();
     cudaEvent_t e[3];
     for (auto& ev : e) cuda_check(cudaEventCreate(&ev), "cudaEventCreate");
@@ -332,6 +345,7 @@ void Tree::bench_step(const double* b_dev, double* x_dev, int nrhs, int iters, d
 }
 
 void Tree::solve_device(double* x, int nrhs, int ld) const {
+    spand::DeviceScope scope(device_);
     if (!factored_) throw std::logic_error("solve() before factorize()");
     try {
         dev_->solve_device(x, nrhs, ld);
@@ -341,16 +355,19 @@ void Tree::solve_device(double* x, int nrhs, int ld) const {
 }
 
 void Tree::solve_device_noalloc(double* x, int nrhs, int ld) const {
+    spand::DeviceScope scope(device_);
     if (!factored_) throw std::logic_error("solve() before factorize()");
     try {
         dev_->solve_device_noalloc(x, nrhs, ld);
     } catch (spand::DeviceError& e) {
         if (e.status == spand::SPAND_ERR_ARG) throw std::invalid_argument(e.msg);
+        if (e.status == spand::SPAND_ERR_STATE) throw std::logic_error(e.msg);
         throw std::runtime_error(e.msg);
     }
 }
 
 void Tree::solve(double* x, int nrhs, int ld) const {
+    spand::DeviceScope scope(device_);
     if (ld < 0) ld = get_N();
     const size_t len = (size_t)ld * nrhs;
     if (dx_len_ < len) {
@@ -372,6 +389,7 @@ size_t Tree::device_bytes() const { return dev_ ? dev_->device_bytes() : 0; }
 // ScalingLLT, then (rank < size) Orthogonal, Split, the sibling's ScalingLLT (identity)
 // and its GemmSymmIn ops; the level's Merge ops at its end.
 void Tree::build_ops_and_log_lorasp() {
+    spand::DeviceScope scope(device_);
     const spand::Plan& P = plan_;
     long long nnz = 0;
     auto push = [&](OpRecord r) {
@@ -430,6 +448,7 @@ void Tree::build_ops_and_log_lorasp() {
 }
 
 void Tree::build_ops_and_log() {
+    spand::DeviceScope scope(device_);
     log_dirty_ = false;
     dev_->sizes(csize_, rows0_);
     if (plan_.lorasp) {
@@ -550,6 +569,24 @@ int Tree::get_stop() const {
     return stop;
 }
 
+void Tree::print_log() const {
+    ensure_log();
+    auto mean = [](long long sum, long long count) { return count > 0 ? (double)sum / (double)count : 0.0; };
+    printf("spaND factorization log: %d levels, N = %d, tol = %.1e, skip = %d, %s factor\n", nlevels_, get_N(), tol_,
+           skip_, fp32_ ? "FP32" : "FP64");
+    printf("%5s | %9s %9s %9s %9s | %10s | %9s %9s %9s | %9s %9s %9s %9s\n", "lvl", "nd", "left nd", "left el",
+           "left sp", "fact nnz", "rank bfr", "rank aft", "nbrs", "sum bfr", "sum aft", "sparsif", "ignored");
+    for (int l = 0; l < (int)log_.size(); l++) {
+        const LevelLog& g = log_[l];
+        printf("%5d | %9lld %9lld %9lld %9lld | %10.3e | %9.1f %9.1f %9.1f | %9lld %9lld %9lld %9lld\n", l, g.dofs_nd,
+               g.dofs_left_nd, g.dofs_left_elim, g.dofs_left_spars, (double)g.fact_nnz,
+               mean(g.rank_before_sum, g.rank_after_count), mean(g.rank_after_sum, g.rank_after_count),
+               mean(g.nbrs_sum, g.nbrs_count), g.rank_before_sum, g.rank_after_sum, g.rank_after_count, g.ignored);
+    }
+    printf("stop = %d, factor nnz = %lld, partition %.3e s, assemble %.3e s, factorize %.3e s\n", get_stop(), nnz(),
+           t_partition, t_assemble, t_factorize);
+}
+
 std::vector<std::array<int, 4>> Tree::ranks() const {
     ensure_log();
     std::vector<std::array<int, 4>> r;
@@ -564,6 +601,7 @@ std::vector<std::array<int, 4>> Tree::ranks() const {
 }
 
 void Tree::op_matrix(int idx, std::vector<double>& out) const {
+    spand::DeviceScope scope(device_);
     const OpRecord& r = ops_.at(idx);
     out.clear();
     if (r.kind == 0 || r.kind == 1 || r.kind == 2 || (r.kind >= 6 && r.kind <= 9)) {
@@ -589,6 +627,7 @@ void Tree::op_matrix(int idx, std::vector<double>& out) const {
 }
 
 void Tree::op_perm(int idx, std::vector<int>& out) const {
+    spand::DeviceScope scope(device_);
     const OpRecord& r = ops_.at(idx);
     out.clear();
     if (r.kind != 8 && r.kind != 9) return;
@@ -602,6 +641,7 @@ void Tree::op_perm(int idx, std::vector<int>& out) const {
 }
 
 void Tree::op_signs(int idx, std::vector<double>& out) const {
+    spand::DeviceScope scope(device_);
     const OpRecord& r = ops_.at(idx);
     out.clear();
     if (r.kind != 9) return;
@@ -610,6 +650,7 @@ void Tree::op_signs(int idx, std::vector<double>& out) const {
 }
 
 void Tree::op_tau(int idx, std::vector<double>& out) const {
+    spand::DeviceScope scope(device_);
     const OpRecord& r = ops_.at(idx);
     out.clear();
     if (r.kind != 3) return;
@@ -725,6 +766,7 @@ std::vector<Tree::Work> Tree::work_solve() const {
 
 spand::PcgResult Tree::adjoint_device(const double* g, const double* x, double* lambda, double* grad_vals,
                                       int iters, double tol) const {
+    spand::DeviceScope scope(device_);
     if (!dev_ || !factored_) throw std::logic_error("adjoint before factorize");
     const size_t nnz = A_.rowval.size();
     if (!d_prow_) {
@@ -751,6 +793,7 @@ spand::PcgResult Tree::adjoint_device(const double* g, const double* x, double* 
 
 int cg(const Csc& A, const double* rhs, double* x, const Tree& precond, int iters, double tol, bool verb,
        double* relres) {
+    spand::DeviceScope scope(precond.device_id());
     (void)A;  // the tree holds the device copy of the assembled matrix
     const int n = precond.get_N();
     double* db = precond.cg_buffer(0, n);
@@ -774,6 +817,7 @@ int cg(const Csc& A, const double* rhs, double* x, const Tree& precond, int iter
 // GMRES and IR: host vectors through the tree's device buffers
 template <typename F>
 static spand::PcgResult krylov_host(const Tree& precond, const double* rhs, double* x, F&& run) {
+    spand::DeviceScope scope(precond.device_id());
     const int n = precond.get_N();
     double* db = precond.cg_buffer(0, n);
     double* dx = precond.cg_buffer(1, n);
@@ -829,6 +873,7 @@ int ir(const Csc& A, const double* rhs, double* x, const Tree& precond, int iter
 
 void cg_multi(const Tree& precond, const double* rhs, double* x, int nrhs, int ld, int iters, double tol,
               int* iters_out, double* relres_out) {
+    spand::DeviceScope scope(precond.device_id());
     const int n = precond.get_N();
     if (nrhs <= 0) return;
     if (ld < n) throw std::invalid_argument("leading dimension smaller than the matrix order");
@@ -872,8 +917,17 @@ void batch_factorize(Tree* const* trees, int count, int* status, std::string* me
     }
 }
 
+// The trees of one batched CG share one device (their lockstep loop runs on it).
+static int batch_device(Tree* const* trees, int count) {
+    const int dev = count > 0 ? trees[0]->device_id() : -1;
+    for (int k = 1; k < count; k++)
+        if (trees[k]->device_id() != dev) throw std::invalid_argument("the trees of a batch live on different devices");
+    return dev;
+}
+
 void batch_cg(Tree* const* trees, int count, const double* const* rhs, double* const* x, int iters, double tol,
               int* iters_out, double* relres_out) {
+    spand::DeviceScope scope(batch_device(trees, count));
     std::vector<spand::PcgSystem> sys(count);
     std::vector<double*> db(count), dx(count);
     for (int k = 0; k < count; k++) {
@@ -904,6 +958,7 @@ void batch_cg(Tree* const* trees, int count, const double* const* rhs, double* c
 
 void batch_cg_device(Tree* const* trees, int count, const double* const* b_dev, double* const* x_dev, int iters,
                      double tol, int* iters_out, double* relres_out) {
+    spand::DeviceScope scope(batch_device(trees, count));
     std::vector<spand::PcgSystem> sys(count);
     for (int k = 0; k < count; k++) {
         const Tree& t = *trees[k];

@@ -103,6 +103,11 @@ class Tree {
     int get_stop() const;
     int get_nlevels() const { return nlevels_; }
     const std::vector<LevelLog>& log() const { ensure_log(); return log_; }
+    // print_log() (include/tree.h:197, src/tree.cpp:1645-1727): per level the dof counts of
+    // the ordering, elimination and sparsification, the factor's stored entries, the
+    // ranks before and after sparsification and the neighbour counts, then the phase
+    // times of the last partition / assemble / factorize; printed to stdout.
+    void print_log() const;
     // (level, cluster order, rows, rank) for every sparsified cluster, reference order
     std::vector<std::array<int, 4>> ranks() const;
     const std::vector<OpRecord>& ops() const { ensure_log(); return ops_; }
@@ -126,6 +131,9 @@ class Tree {
     SymmKind get_symm_kind() const { return symm_; }
     bool assembled() const { return assembled_ok_; }
     cudaStream_t stream() const { return stream_; }
+    // CUDA device the tree was assembled on (-1 before the first assemble()); every call
+    // that touches the tree's memory makes it current and then restores the caller's
+    int device_id() const { return device_; }
     const spand::DeviceCsr& device_csr() const { return dA_; }
     size_t device_bytes() const;
     // device vectors of the CG driver (b, x), kept across calls
@@ -185,6 +193,7 @@ class Tree {
 
     std::unique_ptr<spand::DeviceFactorBase> dev_;
     cudaStream_t stream_ = nullptr;
+    int device_ = -1;
     spand::DeviceCsr dA_;
     mutable double* dx_ = nullptr;
     mutable size_t dx_len_ = 0;

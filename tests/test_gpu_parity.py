@@ -86,6 +86,26 @@ def test_factor_parity_fp64_narrow_qrcp(threads, monkeypatch):
     _check_parity(64, 2, 7, 1e-2, 0, 1)
 
 
+@pytest.mark.parametrize("mode", ["0", "1"])
+def test_factor_parity_fp64_qrcp_kind(mode, monkeypatch):
+    """Every shared-memory QRCP launch through the unblocked kernel (0) or through the
+    blocked panel kernel (1, wherever the matrices fit it): the same bars, so the panel
+    scheme reproduces the unblocked pivots, ranks and factors."""
+    monkeypatch.setenv("SPAND_QC_BLOCKED", mode)
+    for case in [(16, 3, 6, 1e-2, 0, 2), (64, 2, 7, 1e-2, 0, 1), (20, 2, 4, 1e-14, 0, 1), (16, 3, 6, 0.0, 0, 1),
+                 (32, 3, 8, 1e-2, 0, 2), (24, 3, 7, 1e-3, 0, 2)]:
+        _check_parity(*case)
+
+
+@pytest.mark.parametrize("threads", [64, 128])
+def test_factor_parity_fp64_blocked_narrow(threads, monkeypatch):
+    """The blocked QRCP with 64- and 128-thread CTAs (fewer warps than slab columns)."""
+    monkeypatch.setenv("SPAND_QC_BLOCKED", "1")
+    monkeypatch.setenv("SPAND_QC_THREADS", str(threads))
+    _check_parity(16, 3, 6, 1e-2, 0, 2)
+    _check_parity(64, 2, 7, 1e-2, 0, 1)
+
+
 def _check_parity(n, dim, nlevels, tol, skip, nf):
     A, t, o = _build(n, dim, nlevels, tol, skip, factorizations=nf)
     assert np.array_equal(t.get_assembly_perm(), o.get_assembly_perm())
@@ -318,3 +338,37 @@ def test_solve_many_rhs(fp32):
     if not fp32:
         Xo = o.solve(B)
         assert np.linalg.norm(X - Xo) <= TOL_SOLVE * np.linalg.norm(Xo)
+
+
+def test_factor_graph_replay(monkeypatch):
+    """factorize() replayed from its CUDA graph (captured on the second factorization,
+    replayed from the third on) gives bit-identical factors to the launch-by-launch path,
+    and a new tolerance captures a new graph that matches the oracle at that tolerance."""
+    from spand_public_gb300 import problems as P
+    A = P.neglapl(16, 3)
+    b = P.rhs(A.shape[0], 2, seed=9)
+    monkeypatch.setenv("SPAND_FACTOR_GRAPH", "0")
+    _, t0, _ = _build(16, 3, 6, 1e-2, factorizations=3)
+    x0 = t0.solve(b)
+    monkeypatch.delenv("SPAND_FACTOR_GRAPH")
+    _, t1, o = _build(16, 3, 6, 1e-2, factorizations=3)
+    assert np.array_equal(t1.ranks(), o.ranks())
+    assert np.array_equal(t1.solve(b), x0)
+    t1.launches(reset=True)
+    t1.factorize()
+    assert t1.launches(reset=True) > 0  # the replay still counts its kernels
+    assert np.array_equal(t1.solve(b), x0)
+    # new tolerance: new graph, oracle parity at that tolerance
+    from oracle.oracle import OracleTree
+    t1.set_tol(1e-3)
+    t1.factorize()
+    t1.factorize()
+    o3 = OracleTree(6)
+    o3.set_Xcoo(P.linspace_nd(16, 3))
+    o3.set_tol(1e-3)
+    o3.partition(A)
+    o3.assemble(A)
+    o3.factorize()
+    assert np.array_equal(t1.ranks(), o3.ranks())
+    xt, xo = t1.solve(b), o3.solve(b)
+    assert np.linalg.norm(xt - xo) / np.linalg.norm(xo) < TOL_SOLVE
