@@ -570,7 +570,8 @@ __global__ void __launch_bounds__(256) trsm3_kernel(Ctx<T> c, const DTrsm* __res
     // element (q, k) of B: side 1 B[(r0+q) + k*bld], side 0 B[k + (r0+q)*bld]
     const long long sq = it.side == 1 ? 1 : bld, sk = it.side == 1 ? bld : 1;
     T* Bt = B + (it.side == 1 ? (size_t)r0 : (size_t)r0 * bld);
-    const bool staged = (long long)tr * n <= smem_elems;
+    // the staged tile is laid out with stride TRB whatever its height tr
+    const bool staged = (long long)TRB * n <= smem_elems;
     const int* perm = perm_store ? perm_store + poff[it.cluster] : nullptr;
     const T* src;
     long long xq, xk;
@@ -826,7 +827,7 @@ __global__ void __launch_bounds__(256) lu_trsm_kernel(Ctx<T> c, const DTrsm* __r
     T* Bt = B + (it.side == 1 ? (size_t)r0 : (size_t)r0 * bld);
     const int* perm = perm_store + poff[it.cluster];
     const int q = threadIdx.x % TRB, sub = threadIdx.x / TRB, lanes = blockDim.x / TRB;
-    if ((long long)tr * n <= smem_elems) {
+    if ((long long)TRB * n <= smem_elems) {  // the tile's stride is TRB whatever its height tr
         for (int idx = threadIdx.x; idx < tr * n; idx += blockDim.x) {
             int qq, k;
             if (it.side == 1) {
@@ -3057,6 +3058,13 @@ class DeviceFactor : public DeviceFactorBase {
     // SPAND_CHECK_LAUNCHES run the launches one by one.
     void factorize_enqueue(double tol) override {
         last_tol_ = tol;
+        if (tuned_ && tol != tuned_tol_) {
+            // another tolerance changes every rank: this factorization runs launch by launch
+            // on the current configuration (whose kernels take larger matrices on their
+            // fallback paths) and the launches are tuned again from its sizes
+            tuned_ = false;
+            measure_next_ = false;
+        }
         if (measure_next_) {
             // the factorization after tuning times the candidate QRCP launches per wave
             measure_next_ = false;
@@ -3200,7 +3208,6 @@ class DeviceFactor : public DeviceFactorBase {
                 } else {
                     cur_wave_ = (int)wi;
                     launch("qrcp", [&] { launch_qrcp_cluster(W, tol); });
-                    cur_wave_ = -1;
                     // matrices larger than the cluster's shared memory: the same algorithm with
                     // the slabs in global memory (clusters of other matrices exit at once)
                     launch("qrcp_global", [&] { launch_qrcp_global(W, tol); });
@@ -3239,11 +3246,12 @@ class DeviceFactor : public DeviceFactorBase {
                                                                            W.n_sib_tiles, signs_, d_xoff_);
                         });
                 }
+                cur_wave_ = -1;
                 // WY factors: on the side stream beside the next wave's QRCP (on the main
                 // stream when the profiler times every launch); preservation and LoRaSp made
                 // them above
                 if (nphi_ || lorasp_) {
-                } else if (prof_.enabled()) {
+                } else if (prof_.enabled() || check_launches_) {
                     launch("sparsify_wy", [&] {
                         sparsify_wy_kernel<T><<<W.n, 256, larft_smem_elems() * sizeof(T), s_>>>(
                             ctx_, W.items, vstore_, rank_, tauws_, taustore_, tstore_);
@@ -3314,6 +3322,7 @@ class DeviceFactor : public DeviceFactorBase {
             snprintf(buf, sizeof(buf), "T%d|sm%d|tol%a|", (int)sizeof(T), num_sms_, last_tol_);
             tune_key_ = buf;
         }
+        tuned_tol_ = last_tol_;
         for (LevelDev& D : levels_) {
             std::map<int, int> wave_of;
             for (size_t w = 0; w < D.waves.size(); w++)
@@ -3361,8 +3370,10 @@ class DeviceFactor : public DeviceFactorBase {
             D.scale_smem = potrf_smem_n(ns);
             choose_potrf_cluster(ne, D.elim_smem, D.n_elim, D.elim_pc_cs, D.elim_pc_smem);
             choose_potrf_cluster(ns, D.scale_smem, D.n_scale, D.scale_pc_cs, D.scale_pc_smem);
-            D.elim_tri.smem = trtri_smem_n(ne);
-            D.scale_tri.smem = trtri_smem_n(ns);
+            // the strip inverse must take every pivot the cluster Cholesky holds: its shared
+            // memory, rounded up to 256 bytes, admits pivots up to one row above nmax
+            D.elim_tri.smem = trtri_smem_n(ne + 2);
+            D.scale_tri.smem = trtri_smem_n(ns + 2);
             if (!ldlt_) {  // the LDLT panels always stage: keep their capacity-sized buffers
                 D.elim_trsm0.smem = D.elim_trsm1.smem = trsm_smem_n(ne);
                 D.scale_trsm0.smem = D.scale_trsm1.smem = trsm_smem_n(ns);
@@ -3691,10 +3702,15 @@ class DeviceFactor : public DeviceFactorBase {
             prof_.begin(s_, cls);
         }
         f();
-        if (check_launches_) {  // SPAND_CHECK_LAUNCHES=1: name the launch that failed
-            const cudaError_t e = cudaGetLastError();
+        if (check_launches_) {
+            // SPAND_CHECK_LAUNCHES=1: name the launch that failed (with a wait after every
+            // launch, so that a fault in the kernel itself is attributed to it too)
+            cudaError_t e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s_);
             if (e != cudaSuccess)
-                throw DeviceError{SPAND_ERR_CUDA, std::string(cls) + ": " + cudaGetErrorString(e)};
+                throw DeviceError{SPAND_ERR_CUDA, std::string(cls) + " (level " + std::to_string(cur_level_) +
+                                                      ", wave " + std::to_string(cur_wave_) + "): " +
+                                                      cudaGetErrorString(e)};
         }
         prof_.end(s_);
         launches_ += kernels;
@@ -4389,7 +4405,7 @@ class DeviceFactor : public DeviceFactorBase {
     // plan fingerprint for the process (trees of the same plan skip the measurement)
     bool measure_on_ = !(getenv("SPAND_QC_TUNE") && atoi(getenv("SPAND_QC_TUNE")) == 0);
     bool measure_next_ = false, measuring_ = false;
-    double last_tol_ = 0.0;
+    double last_tol_ = 0.0, tuned_tol_ = 0.0;
     std::string tune_key_;
     std::vector<cudaEvent_t> tune_ev_;
     static std::mutex& qc_tune_mutex() {
