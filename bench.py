@@ -186,31 +186,34 @@ def make_tree(A, X, args, fp32: bool):
     return t
 
 
-_ORACLE_MODE = None
-
-
-def oracle_mode():
+def oracle_mode(threads: int = 1):
     """Dense kernels of the timed oracle: the CBLAS / LAPACKE of scipy's bundled OpenBLAS
     where it can be loaded (dgemm, dsyrk, dtrsm, dpotrf, dgeqp3 -- the calls the reference
-    makes, util.cpp:122-394), on one thread like the reference's build (sequential MKL,
-    tests/Makefile:29); else the oracle's restated kernels.  Returns a description."""
-    global _ORACLE_MODE
-    if _ORACLE_MODE is None:
-        from oracle import oracle as O
+    makes, util.cpp:122-394), on `threads` OpenBLAS threads (1: like the reference's build,
+    sequential MKL, tests/Makefile:29); else the oracle's restated kernels on one thread.
+    Returns a description."""
+    from oracle import oracle as O
 
-        path = O.use_lapack(1)
-        _ORACLE_MODE = (f"dense kernels through {os.path.basename(path)} (CBLAS/LAPACKE as the reference calls "
-                        "them), one thread like the reference's sequential-BLAS build") if path else \
-            "dense kernels restated in plain C++ (no CBLAS/LAPACKE library found), one thread"
-    return _ORACLE_MODE
+    path = O.use_lapack(int(threads))
+    if path:
+        return (f"dense kernels through {os.path.basename(path)} (CBLAS/LAPACKE as the reference calls them), "
+                f"{threads} OpenBLAS thread(s)")
+    return "dense kernels restated in plain C++ (no CBLAS/LAPACKE library found), one thread"
 
 
-def cpu_oracle_solve(A, X, B, args):
-    """The oracle (C++ restatement of the reference, one thread): factorize + CG of the first
-    right-hand side.  Returns (factor s, CG s, iterations, true relative residual)."""
+def host_info():
+    import platform
+
+    return {"nproc": os.cpu_count(), "machine": platform.machine(), "processor": platform.processor() or None}
+
+
+def cpu_oracle_solve(A, X, B, args, threads: int = 1):
+    """The oracle (C++ restatement of the reference; its dense kernels on `threads` OpenBLAS
+    threads): factorize + CG of the first right-hand side.  Returns (factor s, CG s,
+    iterations, true relative residual)."""
     from oracle.oracle import OracleTree
 
-    oracle_mode()
+    oracle_mode(threads)
     o = OracleTree(args.levels)
     o.set_Xcoo(X)
     o.set_tol(args.eps)
@@ -226,37 +229,56 @@ def cpu_oracle_solve(A, X, B, args):
     return t1 - t0, t2 - t1, it, rel
 
 
+def cpu_thread_choice(A, X, B, args):
+    """One factor + CG on one OpenBLAS thread and one on every host core; the faster of the
+    two is the CPU configuration to report.  Returns (threads, {threads: (factor s, CG s,
+    iterations, relres)})."""
+    n = max(1, os.cpu_count() or 1)
+    runs = {1: cpu_oracle_solve(A, X, B, args, 1)}
+    if n > 1:
+        runs[n] = cpu_oracle_solve(A, X, B, args, n)
+    k = args.nrhs
+    best = min(runs, key=lambda t: runs[t][0] + k * runs[t][1])
+    return best, runs
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
     A, X, b = workload(args)
-    # each step is one full factor + CG of the 64^3 problem (~10-20 s on one core);
-    # the run is capped at about three minutes
-    steps_run, times, its, rels = 0, [], [], []
+    # one step is one full factor + CG of the 64^3 problem (~10 s on one core); the first
+    # two steps time one OpenBLAS thread and every host core, the rest use the faster; the
+    # run is capped at about three minutes
+    k = args.nrhs
     budget = 180.0
     t_start = time.perf_counter()
-    warm = min(args.warmup, 0)
-    for _ in range(warm):
-        cpu_oracle_solve(A, X, b, args)
-    while steps_run < args.steps:
-        f, g, it, rel = cpu_oracle_solve(A, X, b, args)
-        s = f + args.nrhs * g  # one factorization + a CG per right-hand side
-        times.append(s)
+    threads, probe = cpu_thread_choice(A, X, b, args)
+    its = [probe[threads][2]]
+    rels = [probe[threads][3]]
+    best_times = [probe[threads][0] + k * probe[threads][1]]
+    while len(best_times) + len(probe) - 1 < args.steps:
+        if time.perf_counter() - t_start + best_times[-1] > budget:
+            break
+        f, g, it, rel = cpu_oracle_solve(A, X, b, args, threads)
+        best_times.append(f + k * g)
         its.append(it)
         rels.append(rel)
-        steps_run += 1
-        if time.perf_counter() - t_start + s > budget:
-            break
-    v = float(np.mean(times))
-    line = {"impl": "reference", "metric": metric(args), "value": v, "unit": "s", "n_gpus": world, "steps": steps_run,
-            "warmup": warm, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+    v = float(np.mean(best_times))
+    by_threads = {t: round(probe[t][0] + k * probe[t][1], 3) for t in probe}
+    line = {"impl": "reference", "metric": metric(args), "value": v, "unit": "s", "n_gpus": world,
+            "steps": len(best_times), "warmup": 0, "ms_per_step": v * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config(args, {"pcg_iterations": its[-1], "true_relres": rels[-1]}),
-            "cpu_baseline": {"value": v, "unit": "s", "cores": 1, "kind": "port",
-                             "sample": f"{steps_run} factorization(s) + CG of the first RHS of the {args.n}^3 problem"
-                                       f" (CG time x {args.nrhs} RHS); the reference cannot be built here (no "
-                                       "Eigen/METIS/LAPACKE), so its C++ restatement runs: " + oracle_mode()},
+            "cpu_baseline": {"value": v, "unit": "s", "cores": threads, "kind": "port", "host": host_info(),
+                             "seconds_by_openblas_threads": by_threads,
+                             "sample": f"{len(best_times)} factorization(s) + CG of the first RHS of the {args.n}^3 "
+                                       f"problem (CG time x {k} RHS) with the faster of 1 and {os.cpu_count()} "
+                                       "OpenBLAS threads; the reference cannot be built here (no "
+                                       "Eigen/METIS/LAPACKE), so its C++ restatement runs: " + oracle_mode(threads)},
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    from oracle import oracle as O
+
+    O.use_restated()
     print(json.dumps(line), flush=True)
     return 0
 
@@ -285,6 +307,16 @@ def run_gb300(args, rank, world, local_rank):
 
     def step(tree):
         return tree.bench_step(b_dev.data_ptr(), x_dev.data_ptr(), args.maxit, args.tol, nrhs=k)
+    # a fresh tree's first factorization (launches sized from capacity bounds: what a
+    # one-shot caller pays) and its second (times the candidate QRCP launches of every
+    # wave); every later one replays the tuned factorization graph
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    t32.factorize()
+    cold_ms = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    t32.factorize()
+    tuning_ms = (time.perf_counter() - t0) * 1e3
     for _ in range(args.warmup):
         step(t32)
     if dist:
@@ -352,7 +384,10 @@ def run_gb300(args, rank, world, local_rank):
     fp64 = None
     if args.fp64_steps > 0:
         t64 = make_tree(A, X, args, fp32=False)
-        step(t64)
+        # the same warm state as the FP32 tree: cold, launch-measuring and graph-capturing
+        # factorizations before the timed ones
+        for _ in range(3):
+            step(t64)
         s64 = [step(t64) for _ in range(args.fp64_steps)]
         fp64 = {"seconds": float(np.mean([(s["factor_ms"] + s["pcg_ms"]) / 1e3 for s in s64])),
                 "factor_ms": float(np.mean([s["factor_ms"] for s in s64])),
@@ -383,15 +418,22 @@ def run_gb300(args, rank, world, local_rank):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        f_c, g_c, it_c, rel_c = cpu_oracle_solve(A, X, b, args)
-        cpu = {"value": f_c + k * g_c, "unit": "s", "cores": 1, "kind": "port",
+        threads, runs = cpu_thread_choice(A, X, b, args)
+        f_c, g_c, it_c, rel_c = runs[threads]
+        cpu = {"value": f_c + k * g_c, "unit": "s", "cores": threads, "kind": "port", "host": host_info(),
+               "seconds_by_openblas_threads": {t: round(r[0] + k * r[1], 3) for t, r in runs.items()},
                "sample": f"one factorization + the CG of the first right-hand side of the same {PROBLEMS[args.problem].format(n=args.n)} problem "
-                         f"by the oracle (C++ restatement of the reference; CG time x {k} RHS; {oracle_mode()}): "
+                         f"by the oracle (C++ restatement of the reference; CG time x {k} RHS; the faster of 1 and "
+                         f"{os.cpu_count()} OpenBLAS threads: {oracle_mode(threads)}): "
                          f"{it_c} CG iterations, true relres {rel_c:.2e}"}
+        from oracle import oracle as O
+
+        O.use_restated()
 
     if rank == 0:
         extra = {"pcg_iterations": iters, "true_relres": true_rel, "factor_ms": factor_ms, "pcg_ms": pcg_ms,
-                 "analysis_s": t_analysis, "precision": "FP32 factor (SIMT), FP64 CG/SpMV/dots",
+                 "analysis_s": t_analysis, "cold_factor_ms": cold_ms, "tuning_factor_ms": tuning_ms,
+                 "precision": "FP32 factor (SIMT), FP64 CG/SpMV/dots",
                  "plain_fp64": fp64,
                  "speedup_vs_plain_fp64": (fp64["seconds"] / value) if fp64 else None,
                  "kernels": kernels, "profiled_step_ms": prof_step["factor_ms"] + prof_step["pcg_ms"],

@@ -12,7 +12,8 @@
   ranks and CG iterations equal to the oracle's per system, and the forest (all systems
   in one plan) equal to the systems factored one at a time.
 * High-contrast finite-volume diffusion reduced to 256^2 (coefficients 10^U(-3,3) on 8x8
-  tiles), 12 levels, eps = 1e-3: full block parity and CG iterations.
+  tiles), 12 levels, eps = 1e-3: ranks, op list, log and CG iterations identical; blocks
+  and M^{-1}b within max(1e-12, 100 x the oracle's own one-ulp sensitivity).
 """
 import numpy as np
 import pytest
@@ -49,33 +50,65 @@ def _pair(A, X, nlevels, tol, fp32=False):
     return t, o
 
 
-def _blocks_worst(t, o):
+def _blocks(tree, ops, k):
+    kind, rows, cols = ops[k, 0], ops[k, 6], ops[k, 7]
+    m = tree.op_matrix(k, rows, cols)
+    if kind == 0:
+        return [np.tril(m)]
+    if kind == 3:
+        return [np.tril(m, -1), tree.op_tau(k, cols)]
+    return [m]
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def _blocks_worst(t, o, o2=None):
+    """Largest relative error of a device factor block against the oracle's; with o2 (the
+    oracle on the matrix moved by one unit in the last place) every block must instead stay
+    within max(1e-12, 100 x the oracle's own change), and the error scaled to that bar (as
+    if the bar were 1e-12) is returned."""
     opt, opo = t.ops(), o.ops()
     assert opt.shape == opo.shape
     assert np.array_equal(opt[:, :8], opo[:, :8])
-    worst = 0.0
+    worst, tight = 0.0, 0
     for k in range(opt.shape[0]):
         kind, rows, cols = opt[k, 0], opt[k, 6], opt[k, 7]
         if kind not in (0, 1, 2, 3) or rows * cols == 0:
             continue
-        mt = t.op_matrix(k, rows, cols)
-        mo = o.op_matrix(k, rows, cols)
-        if kind == 0:
-            mt, mo = np.tril(mt), np.tril(mo)
-        if kind == 3:
-            mt, mo = np.tril(mt, -1), np.tril(mo, -1)
-            ht, ho = t.op_tau(k, cols), o.op_tau(k, cols)
-            worst = max(worst, np.linalg.norm(ht - ho) / max(np.linalg.norm(ho), 1e-300))
-        worst = max(worst, np.linalg.norm(mt - mo) / max(np.linalg.norm(mo), 1e-300))
+        if o2 is None:
+            for a, b in zip(_blocks(t, opt, k), _blocks(o, opo, k)):
+                worst = max(worst, _rel(a, b))
+        else:
+            for a, b, c in zip(_blocks(t, opt, k), _blocks(o, opo, k), _blocks(o2, opo, k)):
+                bar = max(TOL_BLOCK, 100.0 * _rel(c, b))
+                worst = max(worst, _rel(a, b) / bar * TOL_BLOCK)
+                tight += bar == TOL_BLOCK
+    if o2 is not None:
+        assert tight > 0
     return worst
 
 
-def _full_parity(A, t, o, cg_tol, seed=0):
+def _ulp_moved(A, seed=1):
+    """A with every stored value moved by one unit in the last place (symmetrically)."""
+    import scipy.sparse as sp
+
+    rng = np.random.default_rng(seed)
+    L = sp.tril(A, -1).tocoo()
+    d = A.diagonal()
+    ld = L.data + np.spacing(np.abs(L.data)) * rng.choice([-1.0, 1.0], L.data.shape)
+    dd = d + np.spacing(np.abs(d)) * rng.choice([-1.0, 1.0], d.shape)
+    L2 = sp.coo_matrix((ld, (L.row, L.col)), shape=A.shape)
+    return (L2 + L2.T + sp.diags(dd)).tocsc()
+
+
+def _full_parity(A, t, o, cg_tol, seed=0, o2=None):
     from spand_public_gb300 import problems as P
 
     assert np.array_equal(t.get_assembly_perm(), o.get_assembly_perm())
     assert np.array_equal(t.ranks(), o.ranks()), "per-cluster ranks differ"
-    worst = _blocks_worst(t, o)
+    worst = _blocks_worst(t, o, o2)
     assert worst < TOL_BLOCK, worst
     for a, b in zip(t.level_log(), o.level_log()):
         for key in ("dofs_nd", "dofs_left_nd", "dofs_left_elim", "dofs_left_spars", "rank_before_sum",
@@ -83,7 +116,8 @@ def _full_parity(A, t, o, cg_tol, seed=0):
             assert a[key] == b[key], (key, a[key], b[key])
     b = P.rhs(A.shape[0], 2, seed=3)
     xt, xo = t.solve(b), o.solve(b)
-    assert np.linalg.norm(xt - xo) / np.linalg.norm(xo) < TOL_SOLVE
+    bar = TOL_SOLVE if o2 is None else max(TOL_SOLVE, 100.0 * _rel(o2.solve(b), xo))
+    assert _rel(xt, xo) < bar
     b1 = P.rhs(A.shape[0], 1, seed=seed)[:, 0]
     xs, it, _ = t.cg(b1, iters=200, tol=cg_tol)
     _, ito = o.cg(b1, iters=200, tol=cg_tol)
@@ -134,9 +168,21 @@ def test_many_systems_sample_to_side_40():
 
 
 def test_high_contrast_fv_256():
+    """Coefficients spanning six orders of magnitude make some factor blocks sensitive to
+    rounding beyond 1e-12 in the reference's own algorithm: the bar per block is
+    max(1e-12, 100 x the oracle's change when every value of A moves by one unit in the
+    last place) -- 1e-12 for the well-conditioned blocks, which are most of them."""
+    from oracle.oracle import OracleTree
     from spand_public_gb300 import problems as P
 
     n = 256
     A, X = P.high_contrast_fv2d(n, 8, seed=0), P.linspace_nd(n, 2)
     t, o = _pair(A, X, 12, 1e-3)
-    _full_parity(A, t, o, 1e-10, seed=1)
+    o2 = OracleTree(12)
+    o2.set_Xcoo(X)
+    o2.set_tol(1e-3)
+    o2.partition(A)
+    o2.assemble(_ulp_moved(A))
+    o2.factorize()
+    assert np.array_equal(o2.ranks(), o.ranks())
+    _full_parity(A, t, o, 1e-10, seed=1, o2=o2)
