@@ -300,8 +300,10 @@ __global__ void __launch_bounds__(256) potrf3_kernel(Ctx<T> c, const int* __rest
 // Cholesky factorization of pivot blocks too large for one CTA's shared memory, in the
 // shared memory of a thread-block cluster of CS CTAs (LLT pivots, src/tree.cpp:587-590).
 // The lower triangle is cut into 32-column panels; panel p (rows [32p, n)) lives in CTA
-// p mod CS.  Per panel: the owner factors the 32x32 diagonal block (one warp, as in
-// chol_blocked) and solves the rows below against it; one cluster barrier; every CTA
+// p mod CS.  Per panel: the owner factors the 32x32 diagonal block in one warp's registers
+// (a row per lane, columns broadcast by shuffles), inverts it (a column of the inverse per
+// lane) and forms the rows below as products with that inverse, four rows per warp at a
+// time (no sequential substitution over the columns); one cluster barrier; every CTA
 // copies the panel's trailing rows through distributed shared memory and applies them to
 // its own later panels (4x4 register tiles).  A non-SPD diagonal stops every CTA after
 // the barrier.  Pivots whose panels exceed smem_bytes set fallback[item] (the
@@ -327,6 +329,7 @@ __global__ void __launch_bounds__(PC_THREADS) potrf_cluster_kernel(Ctx<T> c, con
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
     __shared__ int bad;
+    __shared__ T Dpc[32 * 33];  // inverse of the current diagonal block, row-major, padded
     // all CTAs of a cluster hold the same pivot, so these exits are uniform over it
     if (item >= count) return;
     const int cid = clusters[item];
@@ -364,41 +367,76 @@ __global__ void __launch_bounds__(PC_THREADS) potrf_cluster_kernel(Ctx<T> c, con
         if (owner == me) {
             T* P = sm + poff(p);
             if (tid < 32) {
+                // the diagonal block in registers, lane i holding row i (a[k] = A[i][k], k <= i):
+                // right-looking Cholesky with the columns broadcast by shuffles, then
+                // D = L^{-1} by forward substitution, lane = column (L read back from P)
+                T a[32];
+#pragma unroll
+                for (int k = 0; k < 32; k++) a[k] = (k <= tid && tid < w) ? P[tid + (size_t)k * ldp] : T(0);
                 int fail = 0;
-                for (int j = 0; j < w; j++) {
-                    T* cj = P + (size_t)j * ldp;
-                    T d = 0;
-                    if (tid == j) {
-                        d = cj[j];
+#pragma unroll
+                for (int j = 0; j < 32; j++) {
+                    if (j < w) {
+                        T d = __shfl_sync(0xffffffffu, a[j], j);
                         if (!(d > T(0))) {
                             fail = 1;
                             d = T(1);
                         } else {
                             d = dsqrt(d);
                         }
-                        cj[j] = d;
+                        if (tid == j) a[j] = d;
+                        else if (tid > j) a[j] /= d;
+                        const T lij = a[j];
+#pragma unroll
+                        for (int k = j + 1; k < 32; k++) {
+                            const T lkj = __shfl_sync(0xffffffffu, a[j], k);
+                            if (tid > j && k <= tid) a[k] -= lij * lkj;
+                        }
                     }
-                    d = __shfl_sync(0xffffffffu, d, j);
-                    fail = __shfl_sync(0xffffffffu, fail, j);
-                    if (fail) break;
-                    if (tid > j && tid < w) cj[tid] /= d;
-                    __syncwarp();
-                    if (tid > j && tid < w) {
-                        const T lij = cj[tid];
-                        for (int kk = j + 1; kk <= tid; kk++) P[tid + (size_t)kk * ldp] -= lij * cj[kk];
-                    }
-                    __syncwarp();
                 }
+                if (tid < w)
+#pragma unroll
+                    for (int k = 0; k < 32; k++)
+                        if (k <= tid) P[tid + (size_t)k * ldp] = a[k];
+                __syncwarp();
+                // column c = tid of D: D[r][c] = (delta_rc - sum_{c <= l < r} L[r][l] D[l][c]) / L[r][r]
+                T dcol[32];
+#pragma unroll
+                for (int r = 0; r < 32; r++) {
+                    dcol[r] = T(0);
+                    if (r < w && r >= tid) {
+                        T acc0 = r == tid ? T(1) : T(0), acc1 = T(0);
+#pragma unroll
+                        for (int l = 0; l < r; l += 2) {
+                            if (l >= tid) acc0 -= P[r + (size_t)l * ldp] * dcol[l];
+                            if (l + 1 < r && l + 1 >= tid) acc1 -= P[r + (size_t)(l + 1) * ldp] * dcol[l + 1];
+                        }
+                        dcol[r] = (acc0 + acc1) / P[r + (size_t)r * ldp];
+                    }
+                }
+#pragma unroll
+                for (int r = 0; r < 32; r++) Dpc[r * 33 + tid] = dcol[r];  // Dpc[r][c] = D[r][c]
                 if (tid == 0 && fail) bad = 1;
             }
             __syncthreads();
-            if (!bad)
-                for (int t = w + tid; t < ldp; t += PC_THREADS)
-                    for (int j = 0; j < w; j++) {
-                        T x = P[t + (size_t)j * ldp];
-                        for (int l = 0; l < j; l++) x -= P[t + (size_t)l * ldp] * P[j + (size_t)l * ldp];
-                        P[t + (size_t)j * ldp] = x / P[j + (size_t)j * ldp];
+            // rows below: L[t][j] = sum_{l <= j} A[t][l] D[j][l], a warp per four rows, lane = j
+            if (!bad) {
+                const int lane = tid & 31, wid = tid >> 5;
+                for (int t0 = w + 4 * wid; t0 < ldp; t0 += 4 * (PC_THREADS / 32)) {
+                    T acc[4] = {T(0), T(0), T(0), T(0)};
+                    for (int l = 0; l < w; l++) {
+                        const T dl = l <= lane ? Dpc[lane * 33 + l] : T(0);
+#pragma unroll
+                        for (int u = 0; u < 4; u++)
+                            if (t0 + u < ldp) acc[u] += P[(t0 + u) + (size_t)l * ldp] * dl;
                     }
+                    __syncwarp();
+                    if (lane < w)
+#pragma unroll
+                        for (int u = 0; u < 4; u++)
+                            if (t0 + u < ldp) P[(t0 + u) + (size_t)lane * ldp] = acc[u];
+                }
+            }
             __syncthreads();
         }
         cl.sync();
@@ -500,33 +538,71 @@ __global__ void __launch_bounds__(256) trtri_kernel(Ctx<T> c, const int* __restr
     T* A = bptr(c, pivots[item]);
     const int ld = c.blk[pivots[item]].ld;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = blockDim.x >> 5;
+    // staging of the row block's L tile L[ib:ib+32, jb:ib] (ld 33) where it fits after Y
+    T* Lt = Y + (size_t)n * 32;
+    const bool stage = (long long)n * 65 <= smem_elems;
+    constexpr int TRI_COLS = 4;  // 32 columns over the 8 warps of a 256-thread CTA
     for (int ib = jb; ib < n; ib += 32) {
         const int h = min(32, n - ib);
-        // R = E - L[ib:ib+h, jb:ib] Y[jb:ib, :]
-        for (int jj = ty; jj < w; jj += nty) {
-            if (tx < h) {
-                const int i = ib + tx;
-                T s0 = 0, s1 = 0;
-                int k = jb;
-                for (; k + 1 < ib; k += 2) {
-                    s0 += A[i + (size_t)k * ld] * Y[k + jj * n];
-                    s1 += A[i + (size_t)(k + 1) * ld] * Y[(k + 1) + jj * n];
+        const int kw = ib - jb;
+        // R = E - L[ib:ib+h, jb:ib] Y[jb:ib, :]: thread (row tx, column group ty) reads each
+        // L[i][k] once for its TRI_COLS columns jj = ty + nty u; the tile is first copied to
+        // shared memory by the whole CTA (coalesced, many loads in flight)
+        if (stage && kw > 0) {
+            for (int idx = threadIdx.x; idx < 32 * kw; idx += blockDim.x) {
+                const int r = idx & 31, k = idx >> 5;
+                Lt[r + 33 * k] = r < h ? A[(ib + r) + (size_t)(jb + k) * ld] : T(0);
+            }
+            __syncthreads();
+        }
+        if (tx < h) {
+            const int i = ib + tx;
+            T acc[TRI_COLS];
+#pragma unroll
+            for (int u = 0; u < TRI_COLS; u++) acc[u] = T(0);
+            for (int k = jb; k < ib; k++) {
+                const T a0 = stage ? Lt[tx + 33 * (k - jb)] : A[i + (size_t)k * ld];
+#pragma unroll
+                for (int u = 0; u < TRI_COLS; u++) {
+                    const int jj = ty + nty * u;
+                    if (jj < w) acc[u] += a0 * Y[k + jj * n];
                 }
-                for (; k < ib; k++) s0 += A[i + (size_t)k * ld] * Y[k + jj * n];
-                Y[i + jj * n] = T(i == jb + jj ? 1 : 0) - (s0 + s1);
+            }
+#pragma unroll
+            for (int u = 0; u < TRI_COLS; u++) {
+                const int jj = ty + nty * u;
+                if (jj < w) Y[i + jj * n] = T(i == jb + jj ? 1 : 0) - acc[u];
             }
         }
         __syncthreads();
-        // Y[ib:ib+h, jj] = L_ii^{-1} R[:, jj]: a warp per column, lanes are rows
+        // Y[ib:ib+h, jj] = L_ii^{-1} R[:, jj]: lanes are rows; row ib+tx of the diagonal block
+        // in registers; the warp's TRI_COLS columns are substituted together
+        T lrow[32];
+#pragma unroll
+        for (int r = 0; r < 32; r++)
+            lrow[r] = (tx < h && r < tx) ? A[(ib + tx) + (size_t)(ib + r) * ld] : T(0);
         const T dii = tx < h ? A[(ib + tx) + (size_t)(ib + tx) * ld] : T(1);
-        for (int jj = ty; jj < w; jj += nty) {
-            T acc = tx < h ? Y[(ib + tx) + jj * n] : T(0);
-            for (int r = 0; r < h; r++) {
-                const T yr = __shfl_sync(0xffffffffu, acc / dii, r);
-                if (tx == r) acc = yr;
-                else if (tx > r && tx < h) acc -= A[(ib + tx) + (size_t)(ib + r) * ld] * yr;
+        T acc[TRI_COLS];
+#pragma unroll
+        for (int u = 0; u < TRI_COLS; u++) {
+            const int jj = ty + nty * u;
+            acc[u] = (tx < h && jj < w) ? Y[(ib + tx) + jj * n] : T(0);
+        }
+#pragma unroll
+        for (int r = 0; r < 32; r++) {
+            if (r < h) {
+#pragma unroll
+                for (int u = 0; u < TRI_COLS; u++) {
+                    const T yr = __shfl_sync(0xffffffffu, acc[u] / dii, r);
+                    if (tx == r) acc[u] = yr;
+                    else acc[u] -= lrow[r] * yr;
+                }
             }
-            if (tx < h) Y[(ib + tx) + jj * n] = acc;
+        }
+#pragma unroll
+        for (int u = 0; u < TRI_COLS; u++) {
+            const int jj = ty + nty * u;
+            if (tx < h && jj < w) Y[(ib + tx) + jj * n] = acc[u];
         }
         __syncthreads();
     }
@@ -3351,7 +3427,7 @@ class DeviceFactor : public DeviceFactorBase {
                     fprintf(stderr, "qrcp wave L%d w%zu: items %d max rows %d rpl %d cs %d threads %d smem %d active %d\n",
                             (int)(&D - levels_.data()), w, Wv.n, maxr, Wv.rpl, Wv.cs, Wv.threads, Wv.smem,
                             active_clusters(Wv.n * Wv.cs, Wv.cs, Wv.smem, Wv.threads,
-                                            Wv.rpl ? qrcp_blocked_kernel_ptr<T>(Wv.rpl) : nullptr));
+                                            Wv.rpl ? qrcp_blocked_kernel_ptr<T>(Wv.rpl) : qrcp_smem_kernel_ptr<T>(Wv.threads)));
                 }
             }
         }
@@ -3759,8 +3835,10 @@ class DeviceFactor : public DeviceFactorBase {
     }
     // ---- QRCP launch configuration -------------------------------------------------
     int qc_smem_cap_ = 0;  // dynamic shared memory per CTA available to the QRCP kernel
+    int pc_smem_cap_ = 0;  // the same for the cluster Cholesky
     int qc_max_cs_ = 8;    // largest cluster (16 where non-portable sizes are allowed)
     int qb_smem_cap_ = 0;  // the same for the blocked QRCP kernels
+    int qcw_smem_cap_ = 0;  // and for the wide (512-thread) unblocked QRCP
     int num_sms_ = 1;
     void init_qrcp_limits() {
         int dev = 0, optin = 0;
@@ -3772,8 +3850,13 @@ class DeviceFactor : public DeviceFactorBase {
         SPAND_CUDA(cudaFuncGetAttributes(&fa, fn));
         qc_smem_cap_ = (int)(optin - (int)fa.sharedSizeBytes) & ~255;
         SPAND_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, qc_smem_cap_));
+        {
+            cudaFuncAttributes pa;
+            SPAND_CUDA(cudaFuncGetAttributes(&pa, potrf_cluster_kernel<T>));
+            pc_smem_cap_ = (int)(optin - (int)pa.sharedSizeBytes) & ~255;
+        }
         SPAND_CUDA(cudaFuncSetAttribute(potrf_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        qc_smem_cap_));
+                                        pc_smem_cap_));
         SPAND_CUDA(cudaFuncSetAttribute(qrcp_gslab_kernel_ptr<T>(), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         qc_smem_cap_));
         if (cudaFuncSetAttribute(qrcp_gslab_kernel_ptr<T>(), cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
@@ -3787,6 +3870,15 @@ class DeviceFactor : public DeviceFactorBase {
             if (active_clusters(16, 16, qc_smem_cap_) > 0) qc_max_cs_ = 16;
         } else {
             cudaGetLastError();
+        }
+        // the wide unblocked QRCP (512 threads): its own cap (larger static arrays)
+        {
+            const QcKernel<T> wfn = qrcp_smem_kernel_ptr<T>(QC_WIDE_THREADS);
+            SPAND_CUDA(cudaFuncGetAttributes(&fa, wfn));
+            qcw_smem_cap_ = (int)(optin - (int)fa.sharedSizeBytes) & ~255;
+            SPAND_CUDA(cudaFuncSetAttribute(wfn, cudaFuncAttributeMaxDynamicSharedMemorySize, qcw_smem_cap_));
+            if (qc_max_cs_ > 8 && cudaFuncSetAttribute(wfn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+                cudaGetLastError();
         }
         // the blocked QRCP: every row-count instantiation gets the largest dynamic shared
         // memory its static arrays leave (the smallest of them is the cap) and, like the
@@ -3853,8 +3945,9 @@ class DeviceFactor : public DeviceFactorBase {
             }
             sm = (sm + 255) & ~int64_t(255);
             if (sm > qc_smem_cap_) continue;
-            for (int th = 64; th <= QC_THREADS; th *= 2) {
-                const int active = active_clusters(W.n * cs, cs, (int)sm, th);
+            for (int th = 64; th <= QC_WIDE_THREADS; th *= 2) {
+                if (th > QC_THREADS && sm > qcw_smem_cap_) continue;
+                const int active = active_clusters(W.n * cs, cs, (int)sm, th, qrcp_smem_kernel_ptr<T>(th));
                 if (active <= 0) continue;
                 const int rounds = (W.n + active - 1) / active;
                 // per pivot step: barrier latency + the passes over the largest slab (the
@@ -3873,11 +3966,13 @@ class DeviceFactor : public DeviceFactorBase {
             }
         }
         // the blocked kernel (plain QRCP only): one read of the slab per pivot step and a
-        // panel update every QB_NB steps instead of four loads and a store per element;
-        // SPAND_QC_BLOCKED=0 / 1 never / always takes it where the matrices fit
+        // panel update every QB_NB steps instead of four loads and a store per element.
+        // Measured on GB300 it is slower than the unblocked kernel at every wave (the step
+        // is bound by latency, not by shared-memory bandwidth), so it is taken only with
+        // SPAND_QC_BLOCKED=1 (wherever the matrices fit it)
         int brpl = 0;
         const char* fb = getenv("SPAND_QC_BLOCKED");
-        const int force_b = fb ? atoi(fb) : -1;
+        const int force_b = fb ? atoi(fb) : 0;
         int maxrows = 0;
         for (const auto& d : dims) maxrows = std::max(maxrows, d.first);
         const int rpl = qb_rpl(maxrows);
@@ -3923,7 +4018,7 @@ class DeviceFactor : public DeviceFactorBase {
         W.smem = bsm;
         W.threads = bth;
         W.cands.clear();
-        if (collect && force_b < 0 && force <= 0 && force_th <= 0) {
+        if (collect && force_b == 0 && force <= 0 && force_th <= 0) {
             // the measuring factorization times the model's best configurations of each
             // kernel (QC_TUNE_PER_KIND each, the model's pick first)
             std::stable_sort(all.begin(), all.end(), [](const QcConf& a, const QcConf& b) { return a.est < b.est; });
@@ -3938,7 +4033,7 @@ class DeviceFactor : public DeviceFactorBase {
             }
         }
     }
-    static constexpr int QC_TUNE_PER_KIND = 3;
+    static constexpr int QC_TUNE_PER_KIND = 4;
     QcProj<T> qc_proj() const {
         if (nphi_ && pres_adaptive_) return QcProj<T>{vstore_, rank1_};
         return QcProj<T>{nullptr, nullptr};
@@ -4028,14 +4123,15 @@ class DeviceFactor : public DeviceFactorBase {
         attr[0].val.clusterDim.z = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        const QcKernel<T> fn = W.rpl > 0 && !force_global_ ? qrcp_blocked_kernel_ptr<T>(W.rpl) : qrcp_smem_kernel_ptr<T>();
+        const QcKernel<T> fn =
+            W.rpl > 0 && !force_global_ ? qrcp_blocked_kernel_ptr<T>(W.rpl) : qrcp_smem_kernel_ptr<T>(W.threads);
         SPAND_CUDA(cudaLaunchKernelEx(&cfg, fn, ctx_, (const DSpars*)W.items, (const DAsn*)pieces_, ws_, (T*)nullptr,
                                       jpvt_, ipvt_, tauws_, rank_, colcount_, fallback_, tol,
                                       force_global_ ? 0 : W.smem, qc_proj()));
     }
     void launch_potrf(int* pivots, int* clusters, int n, int smem, const TrtriDev& tri, int pc_cs, int pc_smem) {
         if (pc_cs > 0) {
-            launch("potrf", [&] {
+            launch("potrf_cluster", [&] {
                 cudaLaunchConfig_t cfg = {};
                 cfg.gridDim = dim3((unsigned)(n * pc_cs));
                 cfg.blockDim = dim3(PC_THREADS);
@@ -4111,15 +4207,18 @@ class DeviceFactor : public DeviceFactorBase {
         });
     }
     // Cluster Cholesky for pivots of up to nmax rows that one CTA's shared memory cannot
-    // hold: the smallest cluster whose CTAs hold their panels (cs = 0: keep the single-CTA
-    // kernel)
+    // hold (cs = 0: keep the single-CTA kernel).  The panels' trailing updates are spread
+    // over the cluster, so a larger cluster shortens each panel step: among the clusters
+    // whose CTAs hold their panels, the largest with at least one panel per CTA whose
+    // CTAs all fit on the GPU at once (else the smallest that fits).
     void choose_potrf_cluster(int nmax, int single_smem, int count, int& cs_out, int& smem_out) {
         cs_out = 0;
         smem_out = 0;
         if (single_smem > 0 || count == 0) return;
+        const int np = (nmax + 31) / 32;
         for (int cs = 2; cs <= qc_max_cs_; cs *= 2) {
             const long long need = (pc_need(nmax, cs, 0, (int)sizeof(T)) + 255) & ~255LL;
-            if (need > qc_smem_cap_) continue;
+            if (need > pc_smem_cap_) continue;
             cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3((unsigned)(count * cs));
             cfg.blockDim = dim3(PC_THREADS);
@@ -4137,9 +4236,12 @@ class DeviceFactor : public DeviceFactorBase {
                 continue;
             }
             if (active <= 0) continue;
-            cs_out = cs;
-            smem_out = (int)need;
-            return;
+            const bool first = cs_out == 0;
+            if (first || (active >= count && cs <= np)) {
+                cs_out = cs;
+                smem_out = (int)need;
+            }
+            if (!first && (active < count || cs > np)) break;
         }
     }
     // shared memory of the POTRF kernel for pivots of size up to nmax: whole block, else one panel
@@ -4147,9 +4249,11 @@ class DeviceFactor : public DeviceFactorBase {
         int64_t full = (int64_t)nmax * nmax * sizeof(T);
         return full <= 200 * 1024 ? (int)std::max<int64_t>(full, 16) : 0;
     }
+    // the strip (32 columns) and, where it fits, the staged row-block tile (33 columns)
     static int trtri_smem_n(int nmax) {
-        int64_t b = (int64_t)32 * nmax * sizeof(T);
-        return (int)std::min<int64_t>(std::max<int64_t>(b, 16), 200 * 1024);
+        const int64_t b = (int64_t)65 * nmax * sizeof(T);
+        if (b <= 200 * 1024) return (int)std::max<int64_t>(b, 16);
+        return (int)std::min<int64_t>((int64_t)32 * nmax * sizeof(T), 200 * 1024);
     }
     TrtriDev build_trtri(const std::vector<int>& clusters, const Plan& P) {
         std::vector<int> ext;

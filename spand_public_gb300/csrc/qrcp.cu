@@ -29,7 +29,6 @@ namespace spand {
 //      and every warp publishes its next entry into every CTA; one cluster barrier.
 // At the end the slabs are written to the global workspace in LAPACK's column order
 // (position p holds column perm[p]).
-constexpr int QC_SLOTS = 16 * (QC_THREADS / 32);  // warps of the largest cluster
 
 template <typename T>
 __device__ __forceinline__ T warp_max(T v) {
@@ -51,8 +50,10 @@ __device__ __forceinline__ void qc_barrier(cooperative_groups::cluster_group& cl
 // sets fallback[item].  GS = true: the same algorithm with the slabs in global memory (the
 // second workspace gslab, L2-resident), for exactly the matrices flagged by the
 // shared-memory launch; the CTAs read other slabs' columns with L2-only loads.
-template <typename T, bool GS>
-__global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, const DSpars* __restrict__ items,
+// NT: the largest CTA this instantiation is launched with (QC_THREADS, or QC_WIDE_THREADS
+// for the waves whose shared memory admits one CTA per SM: twice the warps on each slab)
+template <typename T, bool GS, int NT>
+__global__ void __launch_bounds__(NT) qrcp_cluster_kernel(Ctx<T> c, const DSpars* __restrict__ items,
                                                                   const DAsn* __restrict__ pieces, T* ws, T* gslab,
                                                                   int* jpvt_ws, int* ipvt_ws, T* taus,
                                                                   int* rank_out, int* colcount, int* fallback,
@@ -63,6 +64,7 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, cons
     const int me = (int)cl.block_rank();
     const int item = blockIdx.x / CS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int QC_SLOTS = 16 * (NT / 32);  // warps of the largest cluster
     __shared__ T red[32];
     __shared__ T pubm[2][QC_SLOTS];  // per warp of the cluster: largest partial norm
     __shared__ int pubf[2][QC_SLOTS];  // first position inside its tie window
@@ -400,17 +402,18 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_cluster_kernel(Ctx<T> c, cons
 }
 
 template <typename T>
-QcKernel<T> qrcp_smem_kernel_ptr() {
-    return qrcp_cluster_kernel<T, false>;
+QcKernel<T> qrcp_smem_kernel_ptr(int threads) {
+    if (threads > QC_THREADS) return qrcp_cluster_kernel<T, false, QC_WIDE_THREADS>;
+    return qrcp_cluster_kernel<T, false, QC_THREADS>;
 }
 
 template <typename T>
 QcKernel<T> qrcp_gslab_kernel_ptr() {
-    return qrcp_cluster_kernel<T, true>;
+    return qrcp_cluster_kernel<T, true, QC_THREADS>;
 }
 
-template QcKernel<float> qrcp_smem_kernel_ptr<float>();
-template QcKernel<double> qrcp_smem_kernel_ptr<double>();
+template QcKernel<float> qrcp_smem_kernel_ptr<float>(int);
+template QcKernel<double> qrcp_smem_kernel_ptr<double>(int);
 template QcKernel<float> qrcp_gslab_kernel_ptr<float>();
 template QcKernel<double> qrcp_gslab_kernel_ptr<double>();
 

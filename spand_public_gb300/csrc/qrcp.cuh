@@ -8,6 +8,8 @@
 namespace spand {
 
 constexpr int QC_THREADS = 256;
+// the wide instantiation of the shared-memory QRCP (one CTA per SM, 16 warps per slab)
+constexpr int QC_WIDE_THREADS = 512;
 
 // Shared memory of one CTA holding a rows x ceil(cols/cs) column slab: the slab (ld =
 // rows | 1), the reflector, two partial-norm arrays, the replicated permutation and the
@@ -86,9 +88,10 @@ template <typename T>
 using QcKernel = void (*)(Ctx<T>, const DSpars*, const DAsn*, T*, T*, int*, int*, T*, int*, int*, int*, double,
                           int, QcProj<T>);
 
-// column slabs in the cluster's shared memory
+// column slabs in the cluster's shared memory, for CTAs of `threads` threads (at most
+// QC_THREADS, or at most QC_WIDE_THREADS)
 template <typename T>
-QcKernel<T> qrcp_smem_kernel_ptr();
+QcKernel<T> qrcp_smem_kernel_ptr(int threads = QC_THREADS);
 // column slabs in global memory, for the matrices the shared-memory launch flagged
 template <typename T>
 QcKernel<T> qrcp_gslab_kernel_ptr();

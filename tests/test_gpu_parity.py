@@ -77,10 +77,11 @@ def test_factor_parity_fp64_global_qrcp(n, dim, nlevels, tol, monkeypatch):
     _check_parity(n, dim, nlevels, tol, 0, 2)
 
 
-@pytest.mark.parametrize("threads", [64, 128])
+@pytest.mark.parametrize("threads", [64, 128, 512])
 def test_factor_parity_fp64_narrow_qrcp(threads, monkeypatch):
     """Every shared-memory QRCP launch with 64 or 128 threads per CTA (the configurations
-    the launch model picks for the many small matrices of the lower levels)."""
+    the launch model picks for the many small matrices of the lower levels), or with the
+    wide 512-thread instantiation (for waves held at one CTA per SM)."""
     monkeypatch.setenv("SPAND_QC_THREADS", str(threads))
     _check_parity(16, 3, 6, 1e-2, 0, 2)
     _check_parity(64, 2, 7, 1e-2, 0, 1)
