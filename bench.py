@@ -416,6 +416,39 @@ def run_gb300(args, rank, world, local_rank):
            "pcg_iterations": it_h,
            "true_relres": max(float(np.linalg.norm(A @ xh[:, j] - b[:, j]) / np.linalg.norm(b[:, j])) for j in range(k))}
 
+    # the differentiable solve (anisotropic workload): loss 0.5 |x - x*|^2 through
+    # spand_public_gb300.autograd.solve, forward (re-assembly of the values on the device,
+    # factorization, PCG) and backward (the adjoint PCG with the same factor and the
+    # -lambda x^T scatter onto the pattern), timed with CUDA events
+    adjoint = None
+    if args.problem == "aniso3d" and k == 1:
+        from spand_public_gb300.autograd import Pattern, solve
+
+        pat = Pattern(A)
+        vals = torch.as_tensor(A.data, device=dev).requires_grad_(True)
+        bb = torch.as_tensor(b[:, 0], device=dev).requires_grad_(True)
+        xstar = torch.as_tensor(np.random.default_rng(1).standard_normal(N), device=dev)
+
+        def fwd_bwd():
+            vals.grad = None
+            bb.grad = None
+            xx = solve(vals, bb, t32, pat, iters=args.maxit, tol=args.tol)
+            (0.5 * torch.sum((xx - xstar) ** 2)).backward()
+
+        for _ in range(2):
+            fwd_bwd()
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record()
+        nadj = max(1, min(args.steps, 5))
+        for _ in range(nadj):
+            fwd_bwd()
+        ev[1].record()
+        torch.cuda.synchronize()
+        adjoint = {"forward_backward_ms": ev[0].elapsed_time(ev[1]) / nadj, "steps": nadj,
+                   "what": "values -> factor + PCG (forward) -> loss 0.5|x - x*|^2 -> adjoint PCG + pattern "
+                           "scatter (backward), FP32 factor, FP64 PCG to the metric's tolerance"}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads, runs = cpu_thread_choice(A, X, b, args)
@@ -434,7 +467,7 @@ def run_gb300(args, rank, world, local_rank):
         extra = {"pcg_iterations": iters, "true_relres": true_rel, "factor_ms": factor_ms, "pcg_ms": pcg_ms,
                  "analysis_s": t_analysis, "cold_factor_ms": cold_ms, "tuning_factor_ms": tuning_ms,
                  "precision": "FP32 factor (SIMT), FP64 CG/SpMV/dots",
-                 "plain_fp64": fp64,
+                 "plain_fp64": fp64, "adjoint": adjoint,
                  "speedup_vs_plain_fp64": (fp64["seconds"] / value) if fp64 else None,
                  "kernels": kernels, "profiled_step_ms": prof_step["factor_ms"] + prof_step["pcg_ms"],
                  "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"}

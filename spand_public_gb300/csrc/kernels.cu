@@ -1847,9 +1847,14 @@ __global__ void __launch_bounds__(256) gemm_fwd2_kernel(Ctx<T> c, XCtx<T> X, con
     if (i0 >= nn) return;
     (void)rhs_stride;
     __shared__ T part[4][GF_ROWS];
+    __shared__ T racc[GF_ROWS];  // the GemmSymmIn products, a warp per row
     T* xn = X.xs + X.xoff[nb] + r * X.xld;
     const int li = threadIdx.x % GF_ROWS, sp = threadIdx.x / GF_ROWS;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    constexpr int RPW = GF_ROWS / 8;  // rows per warp in the GemmSymmIn products
     const int i = i0 + li;
+    if (threadIdx.x < GF_ROWS) racc[threadIdx.x] = T(0);
+    __syncthreads();
     T acc = 0;
     for (int o = 0; o < G.count; o++) {
         const DGemmOp op = ops[G.first + o];
@@ -1859,37 +1864,54 @@ __global__ void __launch_bounds__(256) gemm_fwd2_kernel(Ctx<T> c, XCtx<T> X, con
         const int ld = c.blk[op.block].ld;
         const T* sg = signs ? signs + soff[op.self] : nullptr;
         const int kind = op.kind & 15;
-        if (i < nn) {
-            T s0 = 0, s1 = 0;
-            if (sg) {
-                if (kind == 1) {
-                    for (int j = sp; j < ns; j += 4) s0 += A[i + (size_t)j * ld] * (sg[j] * xs[j]);
-                } else {
-                    const T* a = A + (size_t)i * ld;
-                    for (int j = sp; j < ns; j += 4) s0 += a[j] * (sg[j] * xs[j]);
-                }
-            } else if (kind == 1) {
+        if (kind == 1) {
+            // A_ns x_s: a thread per row (consecutive rows read consecutive entries)
+            if (i < nn) {
+                T s0 = 0, s1 = 0, s2 = 0, s3 = 0;
                 int j = sp;
-                for (; j + 4 < ns; j += 8) {
-                    s0 += A[i + (size_t)j * ld] * xs[j];
-                    s1 += A[i + (size_t)(j + 4) * ld] * xs[j + 4];
+                if (sg) {
+                    for (; j < ns; j += 4) s0 += A[i + (size_t)j * ld] * (sg[j] * xs[j]);
+                } else {
+                    for (; j + 12 < ns; j += 16) {
+                        s0 += A[i + (size_t)j * ld] * xs[j];
+                        s1 += A[i + (size_t)(j + 4) * ld] * xs[j + 4];
+                        s2 += A[i + (size_t)(j + 8) * ld] * xs[j + 8];
+                        s3 += A[i + (size_t)(j + 12) * ld] * xs[j + 12];
+                    }
+                    for (; j < ns; j += 4) s0 += A[i + (size_t)j * ld] * xs[j];
                 }
-                for (; j < ns; j += 4) s0 += A[i + (size_t)j * ld] * xs[j];
-            } else {
-                const T* a = A + (size_t)i * ld;
-                for (int j = sp; j < ns; j += 4) s0 += a[j] * xs[j];
+                acc += (s0 + s1) + (s2 + s3);
             }
-            acc += s0 + s1;
+        } else {
+            // A_sn^T x_s: row i is column i of A_sn; a warp per RPW rows, lanes over j
+            // (consecutive lanes read consecutive entries), the rows' sums in parallel
+            T sr[RPW];
+#pragma unroll
+            for (int u = 0; u < RPW; u++) sr[u] = T(0);
+            for (int j = lane; j < ns; j += 32) {
+                const T xj = sg ? sg[j] * xs[j] : xs[j];
+#pragma unroll
+                for (int u = 0; u < RPW; u++) {
+                    const int ii = i0 + wid * RPW + u;
+                    if (ii < nn) sr[u] += A[j + (size_t)ii * ld] * xj;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < RPW; u++) {
+                const T v = warp_sum(sr[u]);
+                if (lane == 0) racc[wid * RPW + u] += v;
+            }
         }
     }
     part[sp][li] = acc;
     __syncthreads();
-    if (sp == 0 && i < nn) xn[i] -= (part[0][li] + part[1][li]) + (part[2][li] + part[3][li]);
+    if (sp == 0 && i < nn) xn[i] -= ((part[0][li] + part[1][li]) + (part[2][li] + part[3][li])) + racc[li];
 }
 
 // Backward Gemm ops grouped by eliminated cluster s: x_s -= sum of A_ns^T x_n
 // (GemmSymmOut) or A_sn x_n (GemmSymmIn), ops in reverse recording order.  One block per
-// (s, 32 entries of x_s), a warp per entry.
+// (s, 32 entries of x_s): a warp per entry where the entry's terms are contiguous
+// (A_ns^T), a thread per entry with eight column slices where they are strided (A_sn).
 constexpr int GB_ROWS = 32;
 
 template <typename T>
@@ -1906,36 +1928,76 @@ __global__ void __launch_bounds__(256) gemm_bwd2_kernel(Ctx<T> c, XCtx<T> X, con
     const int i0 = tiles[t].tile_i * GB_ROWS;
     if (i0 >= ns) return;
     T* xs = X.xs + X.xoff[sc] + r * X.xld;
+    __shared__ T wacc[GB_ROWS];      // the A_ns^T terms, a warp per entry
+    __shared__ T part[8][GB_ROWS];   // the A_sn terms, eight column slices
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int ii = w; ii < GB_ROWS; ii += nw) {
-        const int i = i0 + ii;
-        if (i >= ns) break;
-        T acc = 0;
-        for (int o = 0; o < G.count; o++) {
-            const DGemmOp op = ops[G.first + o];
-            const int nn = (sib_mode || (op.kind & 16)) ? c.csize[op.nbr] : c.rows0[op.nbr];
-            const T* xn = X.xs + X.xoff[op.nbr] + r * X.xld;
-            const T* A = bptr(c, op.block);
-            const int ld = c.blk[op.block].ld;
-            T s = 0;
-            if ((op.kind & 15) == 1) {
-                const T* a = A + (size_t)i * ld;
-                for (int j = lane; j < nn; j += 32) s += a[j] * xn[j];
-            } else {
-                for (int j = lane; j < nn; j += 32) s += A[i + (size_t)j * ld] * xn[j];
+    const int li = threadIdx.x % GB_ROWS, sp = threadIdx.x / GB_ROWS;  // 8 slices of 256 threads
+    T pacc = 0;
+    T wsum[GB_ROWS / 8];
+#pragma unroll
+    for (int u = 0; u < GB_ROWS / 8; u++) wsum[u] = T(0);
+    for (int o = 0; o < G.count; o++) {
+        const DGemmOp op = ops[G.first + o];
+        const int nn = (sib_mode || (op.kind & 16)) ? c.csize[op.nbr] : c.rows0[op.nbr];
+        const T* xn = X.xs + X.xoff[op.nbr] + r * X.xld;
+        const T* A = bptr(c, op.block);
+        const int ld = c.blk[op.block].ld;
+        if ((op.kind & 15) == 1) {
+            // A_ns^T x_n: entry i is column i of A_ns
+#pragma unroll
+            for (int u = 0; u < GB_ROWS / 8; u++) {
+                const int ii = w + nw * u;
+                const int i = i0 + ii;
+                if (ii < GB_ROWS && i < ns) {
+                    const T* a = A + (size_t)i * ld;
+                    T s = 0;
+                    for (int j = lane; j < nn; j += 32) s += a[j] * xn[j];
+                    wsum[u] += s;
+                }
             }
-            acc += warp_sum(s);
+        } else {
+            // A_sn x_n: a thread per entry, column slices j = sp (mod 8)
+            const int i = i0 + li;
+            if (i < ns) {
+                T s0 = 0, s1 = 0;
+                int j = sp;
+                for (; j + 8 < nn; j += 16) {
+                    s0 += A[i + (size_t)j * ld] * xn[j];
+                    s1 += A[i + (size_t)(j + 8) * ld] * xn[j + 8];
+                }
+                for (; j < nn; j += 8) s0 += A[i + (size_t)j * ld] * xn[j];
+                pacc += s0 + s1;
+            }
         }
-        if (lane == 0) xs[i] -= signs ? signs[soff[sc] + i] * acc : acc;  // LDLT: D (A^T x_n)
+    }
+#pragma unroll
+    for (int u = 0; u < GB_ROWS / 8; u++) {
+        const T v = warp_sum(wsum[u]);
+        const int ii = w + nw * u;
+        if (lane == 0 && ii < GB_ROWS) wacc[ii] = v;
+    }
+    part[sp][li] = pacc;
+    __syncthreads();
+    if (threadIdx.x < GB_ROWS) {
+        const int i = i0 + threadIdx.x;
+        if (i < ns) {
+            T acc = wacc[threadIdx.x];
+            for (int q = 0; q < 8; q++) acc += part[q][threadIdx.x];
+            xs[i] -= signs ? signs[soff[sc] + i] * acc : acc;  // LDLT: D (A^T x_n)
+        }
     }
 }
 
 // Orthogonal op of the solve with the blocked WY form: fwd x <- Q^T x applies
 // Q_b^T = I - V_b T_b^T V_b^T for b = 0, 1, ...; bwd x <- Q x applies Q_b for b = nb-1 ... 0
-// (operations.cpp:153-158).  Three barriers per block of 32 reflectors.
+// (operations.cpp:153-158).  Three barriers per block of 32 reflectors.  Where the shared
+// memory holds them (staged), each block's reflectors (rows >= the block's first) and its
+// T factor are first copied there by the whole CTA with coalesced loads, all in flight at
+// once, so that the three phases read shared memory instead of chains of L2 loads.
 template <typename T>
 __global__ void __launch_bounds__(512) ortho_wyb_kernel(Ctx<T> c, XCtx<T> X, const DOrtho* __restrict__ items,
-                                                        int count, const T* vstore, const T* tstore, int trans) {
+                                                        int count, const T* vstore, const T* tstore, int trans,
+                                                        int smem_elems) {
     const int item = blockIdx.x % count;
     const int r = blockIdx.x / count;
     const DOrtho it = items[item];
@@ -1948,6 +2010,9 @@ __global__ void __launch_bounds__(512) ortho_wyb_kernel(Ctx<T> c, XCtx<T> X, con
     T* x = X.xs + X.xoff[it.cluster] + r * X.xld;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* xs = reinterpret_cast<T*>(smem_raw);  // rows
+    T* tb = xs + rows;                        // T_b, 32 x 33
+    T* vb = tb + QB * (QB + 1);               // V_b rows [i0, rows), column i at vb + i * (rows - i0)
+    const bool staged = (long long)rows + QB * (QB + 1) + (long long)QB * rows <= smem_elems;
     __shared__ T wv[QB], yv[QB];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int i = threadIdx.x; i < rows; i += blockDim.x) xs[i] = x[i];
@@ -1956,11 +2021,28 @@ __global__ void __launch_bounds__(512) ortho_wyb_kernel(Ctx<T> c, XCtx<T> X, con
     for (int q = 0; q < nb; q++) {
         const int b = trans ? q : nb - 1 - q;
         const int i0 = b * QB, bw = min(QB, k - i0);
+        const int h = rows - i0;
+        if (staged) {
+            for (int idx = threadIdx.x; idx < h * bw; idx += blockDim.x) {
+                const int rr = idx % h, i = idx / h;
+                vb[idx] = V[(i0 + rr) + (size_t)(i0 + i) * ld];
+            }
+            for (int idx = threadIdx.x; idx < bw * bw; idx += blockDim.x) {
+                const int jj = idx % bw, i = idx / bw;
+                tb[jj + i * (QB + 1)] = Tm[(i0 + jj) + (size_t)(i0 + i) * ld];
+            }
+            __syncthreads();
+        }
         // w = V_b^T x
         for (int i = w; i < bw; i += nw) {
-            const T* vi = V + (size_t)(i0 + i) * ld;
             T s = 0;
-            for (int rr = i0 + i + 1 + lane; rr < rows; rr += 32) s += vi[rr] * xs[rr];
+            if (staged) {
+                const T* vi = vb + (size_t)i * h;
+                for (int rr = i + 1 + lane; rr < h; rr += 32) s += vi[rr] * xs[i0 + rr];
+            } else {
+                const T* vi = V + (size_t)(i0 + i) * ld;
+                for (int rr = i0 + i + 1 + lane; rr < rows; rr += 32) s += vi[rr] * xs[rr];
+            }
             s = warp_sum(s);
             if (lane == 0) wv[i] = xs[i0 + i] + s;
         }
@@ -1970,9 +2052,11 @@ __global__ void __launch_bounds__(512) ortho_wyb_kernel(Ctx<T> c, XCtx<T> X, con
             const int i = threadIdx.x;
             T s = 0;
             if (trans) {
-                for (int j = 0; j <= i; j++) s += Tm[(i0 + j) + (size_t)(i0 + i) * ld] * wv[j];
+                for (int j = 0; j <= i; j++)
+                    s += (staged ? tb[j + i * (QB + 1)] : Tm[(i0 + j) + (size_t)(i0 + i) * ld]) * wv[j];
             } else {
-                for (int j = i; j < bw; j++) s += Tm[(i0 + i) + (size_t)(i0 + j) * ld] * wv[j];
+                for (int j = i; j < bw; j++)
+                    s += (staged ? tb[i + j * (QB + 1)] : Tm[(i0 + i) + (size_t)(i0 + j) * ld]) * wv[j];
             }
             yv[i] = s;
         }
@@ -1981,7 +2065,8 @@ __global__ void __launch_bounds__(512) ortho_wyb_kernel(Ctx<T> c, XCtx<T> X, con
         for (int rr = i0 + threadIdx.x; rr < rows; rr += blockDim.x) {
             const int imax = min(rr - i0, bw - 1);
             T s = 0;
-            for (int i = 0; i <= imax; i++) s += (i0 + i == rr ? T(1) : V[rr + (size_t)(i0 + i) * ld]) * yv[i];
+            for (int i = 0; i <= imax; i++)
+                s += (i0 + i == rr ? T(1) : (staged ? vb[(rr - i0) + (size_t)i * h] : V[rr + (size_t)(i0 + i) * ld])) * yv[i];
             xs[rr] -= s;
         }
         __syncthreads();
@@ -2653,6 +2738,7 @@ class DeviceFactor : public DeviceFactorBase {
         tauws_ = alloc<T>(std::max<int64_t>(P.tau_len, 1));
         ws_ = alloc<T>(std::max<int64_t>(P.ws_len, 1));
         ws2_ = alloc<T>(std::max<int64_t>(P.ws_len, 1));
+        ws_len_ = std::max<int64_t>(P.ws_len, 1);
         {
             std::vector<DUpd> u;
             for (const SchurUpdate& su : P.schur_updates) u.push_back({su.b1, su.t1, su.b2, su.t2, su.s});
@@ -2727,46 +2813,9 @@ class DeviceFactor : public DeviceFactorBase {
                 D.level_clusters = up(all);
             }
             for (const auto& wave : L.waves) {
-                WaveDev W;
-                std::vector<DSpars> items;
-                int64_t coloff = 0;
-                int maxcap = 1;
-                for (const SparsifyItem& it : wave) {
-                    items.push_back({it.cluster, it.first, it.count, it.cap_cols, (long long)it.ws_off,
-                                     (long long)coloff, (long long)it.v_off, (long long)it.tau_off});
-                    coloff += std::max(it.cap_cols, 1);
-                    maxcap = std::max(maxcap, P.c_cap[it.cluster]);
-                }
-                max_cols = std::max(max_cols, coloff);
-                max_items = std::max(max_items, (int)items.size());
-                W.n = (int)items.size();
-                W.items = up(items);
-                W.maxcap = maxcap;
-                W.ytiles = 1;  // capacities can be 0 (LoRaSp bounds): never an empty grid
-                for (const SparsifyItem& it : wave) {
-                    int nt = (P.c_cap[it.cluster] + 31) / 32;
-                    for (int p = 0; p < it.count; p++) nt += (P.c_cap[P.asn_pieces[it.first + p].nbr] + 31) / 32;
-                    W.ytiles = std::max(W.ytiles, nt);
-                }
-                W.host = wave;
-                {
-                    // capacity bound until the first factorization reports the actual sizes
-                    std::vector<std::pair<int, int>> dims;
-                    for (const SparsifyItem& it : wave) dims.push_back({P.c_cap[it.cluster], it.cap_cols});
-                    choose_cluster(W, dims);
-                    // global-memory launch: a full cluster where some matrix at its capacity
-                    // could exceed the largest shared-memory configuration, else one CTA as
-                    // the safety net for sizes that grow beyond the tuned configuration
-                    bool big = false;
-                    for (const auto& d : dims)
-                        big |= qc_need(d.first, d.second, qc_max_cs_, (int)sizeof(T)) > qc_smem_cap_;
-                    W.gcs = (big || force_global_) ? qc_max_cs_ : 1;
-                    int64_t g = 4096;
-                    for (const auto& d : dims) g = std::max<int64_t>(g, qc_small_need(d.first, d.second, W.gcs, (int)sizeof(T)));
-                    if (g > qc_smem_cap_)
-                        throw DeviceError{SPAND_ERR_UNSUPPORTED, "sparsification matrix too large for the QRCP kernels"};
-                    W.gsmem = (int)((g + 255) & ~int64_t(255));
-                }
+                WaveDev W = make_wave(wave);
+                max_cols = std::max(max_cols, W.cols);
+                max_items = std::max(max_items, W.n);
                 if (ldlt_) {
                     // the sign pivot's Q^T D Q split, the sibling's LDL^T, the edge's panel and
                     // the Schur update of the cluster's pivot (tree.cpp:1069-1097, 1340-1341)
@@ -3052,13 +3101,18 @@ class DeviceFactor : public DeviceFactorBase {
                     D.sib_gb_tiles = up(tb);
                     D.n_sib_gb_tiles = (int)tb.size();
                 }
-                D.x_smem_ortho = mx * (int)sizeof(T);
+                // the x range, and where they fit the staged T_b and V_b tiles
+                {
+                    const int64_t full = ((int64_t)mx + QB * (QB + 1) + (int64_t)QB * mx) * (int64_t)sizeof(T);
+                    D.x_smem_ortho = full <= 200 * 1024 ? (int)full : mx * (int)sizeof(T);
+                }
                 const int64_t mr = (int64_t)mx * (MR_RB + 1) * (int64_t)sizeof(T);
                 D.ortho_mrhs_smem = mr <= 200 * 1024 ? (int)mr : 0;
             }
         }
         jpvt_ = alloc<int>(max_cols);
         ipvt_ = alloc<int>(max_cols);
+        cols_len_ = max_cols;
         if (lu_ || ldlt_) {
             lu_perm_ = alloc<int>(std::max<int64_t>(P.x_len, 1));
             lu_swp_ = alloc<int>(std::max<int64_t>(P.x_len, 1));
@@ -3096,6 +3150,7 @@ class DeviceFactor : public DeviceFactorBase {
             SPAND_CUDA(cudaFuncSetAttribute(lu_apply_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         }
         fallback_ = alloc<int>(max_items);
+        items_len_ = max_items;
         SPAND_CUDA(cudaFuncSetAttribute(trsv4_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(ortho_mrhs_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(trsv_mrhs_small_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -3381,7 +3436,7 @@ class DeviceFactor : public DeviceFactorBase {
             measuring_ = false;
             std::vector<QcConf> chosen;
             for (LevelDev& D : levels_)
-                for (WaveDev& W : D.waves) chosen.push_back(QcConf{W.rpl, W.cs, W.threads, W.smem, 0.0});
+                for (WaveDev& W : D.waves) chosen.push_back(QcConf{W.rpl, W.cs, W.threads, W.smem, W.vec_rows, 0.0});
             std::lock_guard<std::mutex> lk(qc_tune_mutex());
             qc_tune_cache()[tune_key_] = chosen;
         }
@@ -3393,6 +3448,7 @@ class DeviceFactor : public DeviceFactorBase {
     void tune_qrcp() {
         std::vector<int> cs, r0;
         sizes(cs, r0);
+        if (relayer_on_ && !ldlt_ && !lorasp_ && !nphi_ && !phi_alloc_) relayer_waves(cs, r0);
         {
             char buf[96];
             snprintf(buf, sizeof(buf), "T%d|sm%d|tol%a|", (int)sizeof(T), num_sms_, last_tol_);
@@ -3665,6 +3721,7 @@ class DeviceFactor : public DeviceFactorBase {
     // one launch configuration of a wave's shared-memory QRCP (rpl 0: the unblocked kernel)
     struct QcConf {
         int rpl = 0, cs = 1, threads = QC_THREADS, smem = 0;
+        int vec_rows = INT_MAX;  // slabs of at least this many rows: vectorised trailing update
         double est = 0.0;  // the launch model's estimate (arbitrary units)
     };
     struct WaveDev {
@@ -3672,7 +3729,9 @@ class DeviceFactor : public DeviceFactorBase {
         DSpars* items = nullptr;
         int maxcap = 1;
         std::vector<QcConf> cands;  // launch configurations the measuring factorization times
+        int64_t cols = 0;           // Asn columns of all its matrices (pivot workspace)
         int rpl = 0;         // > 0: the blocked QRCP for up to 32 * rpl rows; 0: the unblocked kernel
+        int vec_rows = INT_MAX;  // unblocked kernel: slabs of at least this many rows are vectorised
         int cs = 1;          // CTAs per thread-block cluster of the shared-memory QRCP
         int threads = QC_THREADS;  // threads per CTA of that launch
         int smem = 0;        // dynamic shared memory per CTA
@@ -3754,6 +3813,165 @@ class DeviceFactor : public DeviceFactorBase {
         int n_ortho = 0;
         DOrtho* ortho = nullptr;
     };
+
+    // The device record of a sparsification wave (the matrices' work list, scatter tiles, the
+    // launch from capacity bounds and the global-memory fallback's launch); the wave's items
+    // carry their workspace offsets.  Workspaces grow here when a wave needs more.
+    WaveDev make_wave(const std::vector<SparsifyItem>& wave) {
+        const Plan& P = *P_;
+        WaveDev W;
+        std::vector<DSpars> items;
+        int64_t coloff = 0, ws = 0;
+        int maxcap = 1;
+        for (const SparsifyItem& it : wave) {
+            items.push_back({it.cluster, it.first, it.count, it.cap_cols, (long long)it.ws_off, (long long)coloff,
+                             (long long)it.v_off, (long long)it.tau_off});
+            coloff += std::max(it.cap_cols, 1);
+            maxcap = std::max(maxcap, P.c_cap[it.cluster]);
+            ws = std::max<int64_t>(ws, it.ws_off + (int64_t)P.c_cap[it.cluster] * std::max(it.cap_cols, 1));
+        }
+        W.cols = coloff;
+        W.n = (int)items.size();
+        W.items = up(items);
+        W.maxcap = maxcap;
+        W.ytiles = 1;  // capacities can be 0 (LoRaSp bounds): never an empty grid
+        for (const SparsifyItem& it : wave) {
+            int nt = (P.c_cap[it.cluster] + 31) / 32;
+            for (int p = 0; p < it.count; p++) nt += (P.c_cap[P.asn_pieces[it.first + p].nbr] + 31) / 32;
+            W.ytiles = std::max(W.ytiles, nt);
+        }
+        W.host = wave;
+        // capacity bound until the first factorization reports the actual sizes
+        std::vector<std::pair<int, int>> dims;
+        for (const SparsifyItem& it : wave) dims.push_back({P.c_cap[it.cluster], it.cap_cols});
+        choose_cluster(W, dims);
+        // global-memory launch: a full cluster where some matrix at its capacity could exceed
+        // the largest shared-memory configuration, else one CTA as the safety net for sizes
+        // that grow beyond the tuned configuration
+        bool big = false;
+        for (const auto& d : dims) big |= qc_need(d.first, d.second, qc_max_cs_, (int)sizeof(T)) > qc_smem_cap_;
+        W.gcs = (big || force_global_) ? qc_max_cs_ : 1;
+        int64_t g = 4096;
+        for (const auto& d : dims) g = std::max<int64_t>(g, qc_small_need(d.first, d.second, W.gcs, (int)sizeof(T)));
+        if (g > qc_smem_cap_) throw DeviceError{SPAND_ERR_UNSUPPORTED, "sparsification matrix too large for the QRCP kernels"};
+        W.gsmem = (int)((g + 255) & ~int64_t(255));
+        // workspaces of a re-layered wave (the plan sized them for its own waves)
+        if (ws_ && ws > ws_len_) {
+            ws_ = alloc<T>(ws);
+            ws2_ = alloc<T>(ws);
+            ws_len_ = ws;
+        }
+        if (jpvt_ && coloff > cols_len_) {
+            jpvt_ = alloc<int>(coloff);
+            ipvt_ = alloc<int>(coloff);
+            cols_len_ = coloff;
+        }
+        if (fallback_ && W.n > items_len_) {
+            fallback_ = alloc<int>(W.n);
+            colcount_ = alloc<int>(W.n);
+            items_len_ = W.n;
+        }
+        return W;
+    }
+
+    // Re-layer a level's sparsification into waves that fill the GPU (plain path, levels of
+    // small matrices: clusters of at most 4 CTAs).  A matrix depends only on its neighbours
+    // sparsified before it (they rewrote the edge blocks it gathers); the plan's waves put
+    // each matrix one wave after its latest such neighbour, however many matrices a wave
+    // then holds, so a wave of N matrices on A co-resident clusters ends with a partly
+    // filled round while later matrices that do not depend on its last ones wait.  With the
+    // actual sizes known, list scheduling builds waves of at most A matrices (A: co-resident clusters of the level's launch configuration), each
+    // matrix placed after all its dependencies, the ready matrices with the longest chains of
+    // dependents first; inside a wave the largest matrices start first.  Any order that keeps
+    // every dependency gives the same gathers and the same results bit for bit.
+    void relayer_waves(const std::vector<int>& cs, const std::vector<int>& r0) {
+        const Plan& P = *P_;
+        for (LevelDev& D : levels_) {
+            std::vector<SparsifyItem> items;
+            std::vector<int> owave;
+            for (size_t w = 0; w < D.waves.size(); w++)
+                for (const SparsifyItem& it : D.waves[w].host) {
+                    items.push_back(it);
+                    owave.push_back((int)w);
+                }
+            const int n = (int)items.size();
+            if (n < 2) continue;
+            std::map<int, int> idx_of;
+            for (int i = 0; i < n; i++) idx_of[items[i].cluster] = i;
+            std::vector<std::vector<int>> deps(n), users(n);
+            std::vector<std::pair<int, int>> dims(n);
+            std::vector<double> work(n);
+            for (int i = 0; i < n; i++) {
+                const SparsifyItem& it = items[i];
+                int64_t cols = 0;
+                for (int p = 0; p < it.count; p++) {
+                    const int nb = P.asn_pieces[it.first + p].nbr;
+                    auto f = idx_of.find(nb);
+                    const bool before = f != idx_of.end() && owave[f->second] < owave[i];
+                    cols += before ? cs[nb] : r0[nb];
+                    if (before) {
+                        deps[i].push_back(f->second);
+                        users[f->second].push_back(i);
+                    }
+                }
+                const int rows = r0[it.cluster];
+                dims[i] = {rows + rows / 10 + 1, (int)(cols + cols / 10 + 1)};
+                work[i] = (double)rows * (double)cols;
+            }
+            // co-resident clusters of the launch the level's matrices would take together
+            WaveDev probe;
+            probe.n = n;
+            choose_cluster(probe, dims);
+            const QcKernel<T> fn =
+                probe.rpl > 0 ? qrcp_blocked_kernel_ptr<T>(probe.rpl) : qrcp_smem_kernel_ptr<T>(probe.threads);
+            // Levels whose matrices need clusters of 8 or 16 CTAs keep their waves: with so few
+            // co-resident clusters the new waves are one round each and lose the overlap of
+            // uneven matrices inside a larger launch (measured slower at 64^3, levels 4-7).
+            if (probe.cs > 4) continue;
+            const int A = std::max(1, active_clusters(probe.n * probe.cs, probe.cs, probe.smem, probe.threads, fn));
+            // longest chain of dependents (items are in a dependency order: waves ascending)
+            std::vector<int> height(n, 1);
+            for (int i = n - 1; i >= 0; i--)
+                for (int u : users[i]) height[i] = std::max(height[i], height[u] + 1);
+            std::vector<int> layer(n, -1), left(n);
+            for (int i = 0; i < n; i++) left[i] = (int)deps[i].size();
+            std::vector<int> ready;
+            for (int i = 0; i < n; i++)
+                if (!left[i]) ready.push_back(i);
+            std::vector<std::vector<int>> layers;
+            int placed = 0;
+            while (placed < n) {
+                std::stable_sort(ready.begin(), ready.end(), [&](int a, int b) {
+                    return height[a] != height[b] ? height[a] > height[b] : work[a] > work[b];
+                });
+                const int take = std::min<int>(A, (int)ready.size());
+                std::vector<int> cur(ready.begin(), ready.begin() + take);
+                ready.erase(ready.begin(), ready.begin() + take);
+                for (int i : cur) layer[i] = (int)layers.size();
+                for (int i : cur)
+                    for (int u : users[i])
+                        if (--left[u] == 0) ready.push_back(u);
+                placed += take;
+                std::stable_sort(cur.begin(), cur.end(), [&](int a, int b) { return work[a] > work[b]; });
+                layers.push_back(cur);
+            }
+            std::vector<WaveDev> waves;
+            for (const auto& lay : layers) {
+                std::vector<SparsifyItem> wave;
+                int64_t ws = 0;
+                for (int i : lay) {
+                    SparsifyItem it = items[i];
+                    it.ws_off = ws;
+                    ws += (int64_t)P.c_cap[it.cluster] * std::max(it.cap_cols, 1);
+                    ws = (ws + 31) & ~int64_t(31);
+                    wave.push_back(it);
+                }
+                waves.push_back(make_wave(wave));
+            }
+            D.waves.swap(waves);
+        }
+    }
+
 
     template <typename V>
     V* alloc(int64_t n) {
@@ -3931,8 +4149,12 @@ class DeviceFactor : public DeviceFactorBase {
     // threads) and the smallest wins.
     void choose_cluster(WaveDev& W, const std::vector<std::pair<int, int>>& dims, bool collect = false) {
         double best = 1e300;
-        int bcs = 0, bsm = 0, bth = QC_THREADS;
+        int bcs = 0, bsm = 0, bth = QC_THREADS, bvec = INT_MAX;
         std::vector<QcConf> all;  // every launchable configuration with its estimate
+        int maxrows_ = 0;
+        for (const auto& d : dims) maxrows_ = std::max(maxrows_, d.first);
+        // SPAND_QC_VEC=0 / 1: never / always (where the slabs are tall enough) the vectorised update
+        const int force_vec = getenv("SPAND_QC_VEC") ? atoi(getenv("SPAND_QC_VEC")) : -1;
         // SPAND_QC_CS=<cs>, SPAND_QC_THREADS=<n>: that configuration wherever the matrices
         // fit (measurement aids)
         const int force = getenv("SPAND_QC_CS") ? atoi(getenv("SPAND_QC_CS")) : 0;
@@ -3956,12 +4178,20 @@ class DeviceFactor : public DeviceFactorBase {
                                        5.0 / 32.0 * (double)work * ((double)QC_THREADS / th));
                 if (force > 0 && cs != force) est = 1e200;
                 if (force_th > 0 && th != force_th) est = 1e200;
-                if (est < 1e200) all.push_back(QcConf{0, cs, th, (int)sm, est});
-                if (est < best) {
-                    best = est;
+                // the same launch with the vectorised update for slabs of QC_VEC_FROM rows or
+                // more (faster on the 200-400-row matrices of the top levels, slower below)
+                const bool vec_ok = maxrows_ >= QC_VEC_FROM && force_vec != 0;
+                const double est_vec = (vec_ok && est < 1e200) ? est * (maxrows_ >= 2 * QC_VEC_FROM ? 0.9 : 1.1) : 1e200;
+                const bool take_vec = force_vec == 1 ? vec_ok : (vec_ok && est_vec < est);
+                if (est < 1e200) all.push_back(QcConf{0, cs, th, (int)sm, INT_MAX, est});
+                if (est_vec < 1e200) all.push_back(QcConf{0, cs, th, (int)sm, QC_VEC_FROM, est_vec});
+                const double e = take_vec ? est_vec : est;
+                if (e < best) {
+                    best = e;
                     bcs = cs;
                     bsm = (int)sm;
                     bth = th;
+                    bvec = take_vec ? QC_VEC_FROM : INT_MAX;
                 }
             }
         }
@@ -3995,45 +4225,50 @@ class DeviceFactor : public DeviceFactorBase {
                                            1.5 / 32.0 * (double)work * ((double)QC_THREADS / th));
                     if (force > 0 && cs != force) est = 1e200;
                     if (force_th > 0 && th != force_th) est = 1e200;
-                    if (est < 1e200) all.push_back(QcConf{rpl, cs, th, (int)sm, est});
+                    if (est < 1e200) all.push_back(QcConf{rpl, cs, th, (int)sm, INT_MAX, est});
                     if (est < best) {
                         best = est;
                         bcs = cs;
                         bsm = (int)sm;
                         bth = th;
                         brpl = rpl;
+                        bvec = INT_MAX;
                     }
                 }
             }
         }
         if (!bcs) {  // matrices above the cap take the global-memory path
             W.rpl = 0;
+            W.vec_rows = INT_MAX;
             W.cs = qc_max_cs_;
             W.smem = qc_smem_cap_;
             W.threads = QC_THREADS;
             return;
         }
         W.rpl = brpl;
+        W.vec_rows = bvec;
         W.cs = bcs;
         W.smem = bsm;
         W.threads = bth;
         W.cands.clear();
-        if (collect && force_b == 0 && force <= 0 && force_th <= 0) {
+        if (collect && force_b == 0 && force <= 0 && force_th <= 0 && force_vec < 0) {
             // the measuring factorization times the model's best configurations of each
-            // kernel (QC_TUNE_PER_KIND each, the model's pick first)
+            // kernel variant (QC_TUNE_PER_KIND each: scalar, blocked, vectorised update; the
+            // model's pick first)
             std::stable_sort(all.begin(), all.end(), [](const QcConf& a, const QcConf& b) { return a.est < b.est; });
-            W.cands.push_back(QcConf{brpl, bcs, bth, bsm, best});
-            int taken[2] = {0, 0};
+            W.cands.push_back(QcConf{brpl, bcs, bth, bsm, bvec, best});
+            int taken[3] = {0, 0, 0};
             for (const QcConf& q : all) {
-                const int kind = q.rpl > 0;
+                const int kind = q.rpl > 0 ? 1 : (q.vec_rows < INT_MAX ? 2 : 0);
                 if (taken[kind] >= QC_TUNE_PER_KIND) continue;
                 taken[kind]++;
-                if (q.rpl == brpl && q.cs == bcs && q.threads == bth) continue;
+                if (q.rpl == brpl && q.cs == bcs && q.threads == bth && q.vec_rows == bvec) continue;
                 W.cands.push_back(q);
             }
         }
     }
-    static constexpr int QC_TUNE_PER_KIND = 4;
+    static constexpr int QC_VEC_FROM = 128;  // the vectorised update's candidates: slabs of >= 128 rows
+    static constexpr int QC_TUNE_PER_KIND = 3;
     QcProj<T> qc_proj() const {
         if (nphi_ && pres_adaptive_) return QcProj<T>{vstore_, rank1_};
         return QcProj<T>{nullptr, nullptr};
@@ -4054,9 +4289,10 @@ class DeviceFactor : public DeviceFactorBase {
         cfg.numAttrs = 1;
         SPAND_CUDA(cudaLaunchKernelEx(&cfg, qrcp_gslab_kernel_ptr<T>(), ctx_, (const DSpars*)W.items,
                                       (const DAsn*)pieces_, ws_, ws2_, jpvt_, ipvt_, tauws_, rank_, colcount_,
-                                      fallback_, tol, W.gsmem, qc_proj()));
+                                      fallback_, tol, W.gsmem, INT_MAX, qc_proj()));
     }
     void apply_conf(WaveDev& W, const QcConf& q) {
+        W.vec_rows = q.vec_rows;
         W.rpl = q.rpl;
         W.cs = q.cs;
         W.threads = q.threads;
@@ -4105,6 +4341,7 @@ class DeviceFactor : public DeviceFactorBase {
         launches_ += (int64_t)K;
     }
     void apply_conf_keep(WaveDev& W, const QcConf& q) {
+        W.vec_rows = q.vec_rows;
         W.rpl = q.rpl;
         W.cs = q.cs;
         W.threads = q.threads;
@@ -4127,7 +4364,7 @@ class DeviceFactor : public DeviceFactorBase {
             W.rpl > 0 && !force_global_ ? qrcp_blocked_kernel_ptr<T>(W.rpl) : qrcp_smem_kernel_ptr<T>(W.threads);
         SPAND_CUDA(cudaLaunchKernelEx(&cfg, fn, ctx_, (const DSpars*)W.items, (const DAsn*)pieces_, ws_, (T*)nullptr,
                                       jpvt_, ipvt_, tauws_, rank_, colcount_, fallback_, tol,
-                                      force_global_ ? 0 : W.smem, qc_proj()));
+                                      force_global_ ? 0 : W.smem, W.vec_rows, qc_proj()));
     }
     void launch_potrf(int* pivots, int* clusters, int n, int smem, const TrtriDev& tri, int pc_cs, int pc_smem) {
         if (pc_cs > 0) {
@@ -4387,8 +4624,8 @@ class DeviceFactor : public DeviceFactorBase {
                     ortho_mrhs_kernel<T><<<D.n_ortho, 256, D.ortho_mrhs_smem, s_>>>(ctx_, X, D.ortho, vstore_, tstore_,
                                                                                     trans);
                 else
-                    ortho_wyb_kernel<T><<<D.n_ortho * nrhs, 512, D.x_smem_ortho, s_>>>(ctx_, X, D.ortho, D.n_ortho,
-                                                                                      vstore_, tstore_, trans);
+                    ortho_wyb_kernel<T><<<D.n_ortho * nrhs, 512, D.x_smem_ortho, s_>>>(
+                        ctx_, X, D.ortho, D.n_ortho, vstore_, tstore_, trans, D.x_smem_ortho / (int)sizeof(T));
             });
         };
         auto merge = [&](const LevelDev& D, int fwd) {
@@ -4477,6 +4714,8 @@ class DeviceFactor : public DeviceFactorBase {
     T *vstore_ = nullptr, *taustore_ = nullptr, *tauws_ = nullptr, *ws_ = nullptr;
     T* ws2_ = nullptr;  // column slabs of the global-memory QRCP
     int *jpvt_ = nullptr, *ipvt_ = nullptr, *colcount_ = nullptr, *fallback_ = nullptr;
+    int64_t ws_len_ = 0, cols_len_ = 0;  // elements of ws_ / ws2_ and of jpvt_ / ipvt_
+    int items_len_ = 0;                  // entries of fallback_ / colcount_
     int* tv_count_ = nullptr;  // finished row tiles per cluster (triangular products)
     cudaStream_t s2_ = nullptr;  // side stream of the WY factors
     DStatus* h_status_ = nullptr;  // pinned copy of the status word, filled by factorize_enqueue
@@ -4504,6 +4743,8 @@ class DeviceFactor : public DeviceFactorBase {
     int* diag_ = nullptr;
     int n_diag_ = 0, diag_smem_ = 0;
     bool tuned_ = false;
+    // re-layered sparsification waves after the first factorization (SPAND_QC_RELAYER=0: the plan's)
+    bool relayer_on_ = !(getenv("SPAND_QC_RELAYER") && atoi(getenv("SPAND_QC_RELAYER")) == 0);
     // measured QRCP tuning: the factorization after tune_qrcp() times every wave's
     // candidates (SPAND_QC_TUNE=0: the launch model's choice only); the winners are kept per
     // plan fingerprint for the process (trees of the same plan skip the measurement)

@@ -50,6 +50,15 @@ __device__ __forceinline__ void qc_barrier(cooperative_groups::cluster_group& cl
 // sets fallback[item].  GS = true: the same algorithm with the slabs in global memory (the
 // second workspace gslab, L2-resident), for exactly the matrices flagged by the
 // shared-memory launch; the CTAs read other slabs' columns with L2-only loads.
+// the vectorised trailing update needs at least this many rows (two vectors per lane)
+constexpr int QC_VEC_ROWS = 64;
+
+// sixteen bytes of a column, loaded and stored as one shared-memory vector
+template <typename T>
+struct alignas(16) QcPack {
+    T e[16 / sizeof(T)];
+};
+
 // NT: the largest CTA this instantiation is launched with (QC_THREADS, or QC_WIDE_THREADS
 // for the waves whose shared memory admits one CTA per SM: twice the warps on each slab)
 template <typename T, bool GS, int NT>
@@ -57,7 +66,8 @@ __global__ void __launch_bounds__(NT) qrcp_cluster_kernel(Ctx<T> c, const DSpars
                                                                   const DAsn* __restrict__ pieces, T* ws, T* gslab,
                                                                   int* jpvt_ws, int* ipvt_ws, T* taus,
                                                                   int* rank_out, int* colcount, int* fallback,
-                                                                  double tol, int smem_bytes, QcProj<T> proj) {
+                                                                  double tol, int smem_bytes, int vec_rows,
+                                                                  QcProj<T> proj) {
     namespace cgx = cooperative_groups;
     cgx::cluster_group cl = cgx::this_cluster();
     const int CS = (int)cl.num_blocks();
@@ -79,7 +89,11 @@ __global__ void __launch_bounds__(NT) qrcp_cluster_kernel(Ctx<T> c, const DSpars
     for (int p = 0; p < it.count; p++) cols += c.csize[pieces[it.first + p].nbr];
     const int mn = min(rows, cols);
     const int cpc = (cols + CS - 1) / CS;
-    const int lda = GS ? c.cap[it.cluster] : (rows | 1);
+    // the vectorised update (16-byte shared-memory vectors, eight lanes per column) for
+    // slabs of at least vec_rows rows; the scalar update (odd leading dimension) below
+    constexpr int VW = 16 / (int)sizeof(T);
+    const bool vec = !GS && rows >= max(vec_rows, QC_VEC_ROWS);
+    const int lda = GS ? c.cap[it.cluster] : (vec ? (rows + VW - 1) / VW * VW : (rows | 1));
     const bool fits = GS ? qc_small_need(rows, cols, CS, (int)sizeof(T)) <= smem_bytes
                          : qc_need(rows, cols, CS, (int)sizeof(T)) <= smem_bytes;
     const int r1 = proj.q ? proj.rank1[it.cluster] : 0;
@@ -106,7 +120,7 @@ __global__ void __launch_bounds__(NT) qrcp_cluster_kernel(Ctx<T> c, const DSpars
     T* Aitem = gslab + it.ws_off;  // GS: the whole matrix, column j at Aitem + j * lda
     T* A = GS ? Aitem + (size_t)c0 * lda : reinterpret_cast<T*>(smem_raw);
     T* vsh = GS ? reinterpret_cast<T*>(smem_raw) : A + (size_t)lda * cpc;
-    T* vn1 = vsh + rows;
+    T* vn1 = vsh + (GS ? rows : lda);
     T* vn2 = vn1 + cpc;
     int* perm = reinterpret_cast<int*>(vn2 + cpc);
     int* pos = perm + cols;
@@ -116,6 +130,12 @@ __global__ void __launch_bounds__(NT) qrcp_cluster_kernel(Ctx<T> c, const DSpars
     const int lane = tid & 31, w = tid >> 5, nw = nth >> 5;
     // gather the slab of Asn = [A_sn | A_ns^T]
     qc_gather_slab(c, it, pieces, rows, c0, c1, A, lda);
+    if (vec) {
+        // the vectors' padding rows stay zero in every column and in the reflector
+        const int pad = lda - rows;
+        for (int idx = tid; idx < pad * nloc; idx += nth) A[rows + idx % pad + (size_t)(idx / pad) * lda] = T(0);
+        for (int r = rows + tid; r < lda; r += nth) vsh[r] = T(0);
+    }
     for (int p = tid; p < cols; p += nth) perm[p] = p;
     for (int j = tid; j < nloc; j += nth) pos[j] = c0 + j;
     __syncthreads();
@@ -148,6 +168,7 @@ __global__ void __launch_bounds__(NT) qrcp_cluster_kernel(Ctx<T> c, const DSpars
     // threads per column for the trailing update
     int G = 1;
     while (G < 8 && (nloc * G * 2 <= nth || rows >= 64 * G)) G *= 2;
+    if (vec) G = 8;
     const int gid = tid / G, gl = tid % G, ngroups = nth / G;
     const T tie = T(1) - qrcp_tie<T>();
     const T tol3z = dsqrt(sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-07));
@@ -246,13 +267,18 @@ __global__ void __launch_bounds__(NT) qrcp_cluster_kernel(Ctx<T> c, const DSpars
                           : (own == me ? A : cl.map_shared_rank(A, own)) + (size_t)lj * lda;
         T* apend = pend >= 0 ? A + (size_t)pend * lda : nullptr;
         T part = 0;
+        // vsh holds zeros from the start of row i's 16-byte vector through row i, so that the
+        // vectorised update can run over whole vectors (row i itself is updated apart)
+        const int rv = (i + 1) & ~(VW - 1);
         for (int r = tid; r < rows; r += nth) {
             if (apend && r > pend_i) apend[r] = vsh[r] * pend_sc;
             if (r >= i) {
                 const T v = GS ? __ldcg(src + r) : src[r];
-                vsh[r] = v;
+                vsh[r] = r == i ? T(0) : v;
                 if (r == i) s_alpha = v;
                 else part += v * v;
+            } else if (r >= rv) {
+                vsh[r] = T(0);
             }
         }
         if (apend && tid == 0) apend[pend_i] = pend_beta;
@@ -298,7 +324,21 @@ __global__ void __launch_bounds__(NT) qrcp_cluster_kernel(Ctx<T> c, const DSpars
             const bool active = j < nloc && ph != phys && pos[j] >= i;
             T* aj = A + (size_t)(active ? j : 0) * lda;
             T s = 0;
-            if (active && tu != T(0)) {
+            if (vec) {
+                if (active && tu != T(0)) {
+                    T s0 = 0, s1 = 0;
+                    for (int r = rv + VW * gl; r < rows; r += VW * 8) {
+                        const QcPack<T> a = *reinterpret_cast<const QcPack<T>*>(aj + r);
+                        const QcPack<T> v = *reinterpret_cast<const QcPack<T>*>(vsh + r);
+#pragma unroll
+                        for (int e = 0; e < VW; e += 2) {
+                            s0 += v.e[e] * a.e[e];
+                            s1 += v.e[e + 1] * a.e[e + 1];
+                        }
+                    }
+                    s = s0 + s1;
+                }
+            } else if (active && tu != T(0)) {
                 T s0 = 0, s1 = 0, s2 = 0, s3 = 0;
                 int r = i + 1 + gl;
                 for (; r + 3 * G < rows; r += 4 * G) {
@@ -312,7 +352,19 @@ __global__ void __launch_bounds__(NT) qrcp_cluster_kernel(Ctx<T> c, const DSpars
             }
             for (int o = G >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
             const T ai0 = __shfl_sync(0xffffffffu, (active && gl == 0) ? aj[i] : T(0), (lane / G) * G);
-            if (active && tu != T(0)) {
+            if (vec && active && tu != T(0)) {
+                const T coef = tu * (ai0 + sc * s);
+                const T cr = coef * sc;
+                for (int r = rv + VW * gl; r < rows; r += VW * 8) {
+                    QcPack<T> a = *reinterpret_cast<const QcPack<T>*>(aj + r);
+                    const QcPack<T> v = *reinterpret_cast<const QcPack<T>*>(vsh + r);
+#pragma unroll
+                    for (int e = 0; e < VW; e++) a.e[e] -= cr * v.e[e];
+                    *reinterpret_cast<QcPack<T>*>(aj + r) = a;
+                }
+                // after the vectors: the one holding row i (this lane's first) rewrote it unchanged
+                if (gl == 0) aj[i] = ai0 - coef;
+            } else if (active && tu != T(0)) {
                 const T coef = tu * (ai0 + sc * s);
                 const T cr = coef * sc;
                 if (gl == 0) aj[i] = ai0 - coef;

@@ -11,12 +11,21 @@ constexpr int QC_THREADS = 256;
 // the wide instantiation of the shared-memory QRCP (one CTA per SM, 16 warps per slab)
 constexpr int QC_WIDE_THREADS = 512;
 
-// Shared memory of one CTA holding a rows x ceil(cols/cs) column slab: the slab (ld =
-// rows | 1), the reflector, two partial-norm arrays, the replicated permutation and the
-// slab's column positions.
+// Leading dimension of a column slab in shared memory: rows | 1 (odd: the scalar update's
+// column groups fall on distinct banks) or rows rounded up to whole 16-byte vectors (the
+// vectorised update); the larger of the two is reserved.
+__host__ __device__ inline int qc_ld_bound(int rows, int elem) {
+    const int vw = 16 / elem;
+    return ((rows | 1) + vw - 1) / vw * vw;
+}
+
+// Shared memory of one CTA holding a rows x ceil(cols/cs) column slab: the slab, the
+// reflector (one leading dimension each), two partial-norm arrays, the replicated
+// permutation and the slab's column positions.
 __host__ __device__ inline long long qc_need(int rows, int cols, int cs, int elem) {
     const long long cpc = (cols + cs - 1) / cs;
-    return ((long long)(rows | 1) * cpc + rows + 2 * cpc) * elem + ((long long)cols + cpc) * 4;
+    const long long ld = qc_ld_bound(rows, elem);
+    return (ld * cpc + ld + 2 * cpc) * elem + ((long long)cols + cpc) * 4;
 }
 
 // Shared memory of one CTA of the global-slab variant: the reflector, the two norm
@@ -83,10 +92,11 @@ struct QcProj {
 };
 
 // (ctx, items, pieces, ws, gslab, jpvt, ipvt, tau, rank, colcount, fallback, tol,
-//  dynamic shared bytes, projection)
+//  dynamic shared bytes, vec_rows, projection); vec_rows: slabs of at least that many rows
+//  take the vectorised trailing update (INT_MAX: none)
 template <typename T>
 using QcKernel = void (*)(Ctx<T>, const DSpars*, const DAsn*, T*, T*, int*, int*, T*, int*, int*, int*, double,
-                          int, QcProj<T>);
+                          int, int, QcProj<T>);
 
 // column slabs in the cluster's shared memory, for CTAs of `threads` threads (at most
 // QC_THREADS, or at most QC_WIDE_THREADS)

@@ -64,9 +64,10 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_blocked_kernel(Ctx<T> c, cons
                                                                   const DAsn* __restrict__ pieces, T* ws, T* gslab,
                                                                   int* jpvt_ws, int* ipvt_ws, T* taus, int* rank_out,
                                                                   int* colcount, int* fallback, double tol,
-                                                                  int smem_bytes, QcProj<T> proj) {
+                                                                  int smem_bytes, int vec_rows, QcProj<T> proj) {
     namespace cgx = cooperative_groups;
     (void)gslab;
+    (void)vec_rows;
     (void)proj;
     cgx::cluster_group cl = cgx::this_cluster();
     const int CS = (int)cl.num_blocks();

@@ -88,6 +88,15 @@ def test_factor_parity_fp64_narrow_qrcp(threads, monkeypatch):
 
 
 @pytest.mark.parametrize("mode", ["0", "1"])
+def test_factor_parity_fp64_qrcp_vectorised(mode, monkeypatch):
+    """Every shared-memory QRCP launch with the scalar trailing update (0) or with the
+    vectorised one on the slabs of 128 rows or more (1)."""
+    monkeypatch.setenv("SPAND_QC_VEC", mode)
+    for case in [(32, 3, 8, 1e-2, 0, 2), (24, 3, 7, 1e-3, 0, 2), (16, 3, 6, 0.0, 0, 2), (64, 2, 7, 1e-2, 0, 2)]:
+        _check_parity(*case)
+
+
+@pytest.mark.parametrize("mode", ["0", "1"])
 def test_factor_parity_fp64_qrcp_kind(mode, monkeypatch):
     """Every shared-memory QRCP launch through the unblocked kernel (0) or through the
     blocked panel kernel (1, wherever the matrices fit it): the same bars, so the panel
@@ -383,3 +392,21 @@ def test_tolerance_change_after_tuning(graph, monkeypatch):
         assert np.array_equal(t.ranks(), o3.ranks())
         xt, xo = t.solve(b), o3.solve(b)
         assert np.linalg.norm(xt - xo) / np.linalg.norm(xo) < TOL_SOLVE
+
+
+def test_relayered_waves(monkeypatch):
+    """The sparsification waves re-layered after the first factorization (list scheduling
+    over the dependency graph, bounded by the co-resident clusters) against the plan's
+    waves: the same ranks and op list, M^{-1}b within 1e-12, and the oracle's parity."""
+    from spand_public_gb300 import problems as P
+    monkeypatch.setenv("SPAND_QC_RELAYER", "0")
+    A, t0, o = _build(32, 3, 8, 1e-2, factorizations=3)
+    monkeypatch.delenv("SPAND_QC_RELAYER")
+    _, t1, _ = _build(32, 3, 8, 1e-2, factorizations=3)
+    assert np.array_equal(t0.ranks(), t1.ranks())
+    assert np.array_equal(t1.ranks(), o.ranks())
+    assert np.array_equal(t0.ops(), t1.ops())
+    b = P.rhs(A.shape[0], 2, seed=4)
+    x0, x1, xo = t0.solve(b), t1.solve(b), o.solve(b)
+    assert np.linalg.norm(x1 - x0) / np.linalg.norm(x0) < TOL_SOLVE
+    assert np.linalg.norm(x1 - xo) / np.linalg.norm(xo) < TOL_SOLVE
