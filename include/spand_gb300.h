@@ -253,6 +253,16 @@ int spand_tree_profile_reset(spand_tree* t);
 /* Algorithmic bytes and flops per kernel class: which = 0 one factorization, 1 one solve. */
 int spand_tree_work_count(spand_tree* t, int which, int* n);
 int spand_tree_work_entry(spand_tree* t, int which, int idx, char* name64, double* bytes, double* flops);
+/* The QRCP launch of every sparsification wave, in launch order (after a factorization).
+ * conf9: level, wave, matrices, row capacity of the largest, blocked rows per lane (0: the
+ * unblocked kernel), CTAs per cluster, threads per CTA, dynamic shared memory bytes, rows
+ * from which the trailing update is vectorised (INT_MAX: never).  ncand: configurations
+ * the measuring factorization timed for the wave (0 where none was measured); conf5 of
+ * candidate k: blocked rows per lane, CTAs per cluster, threads, shared memory, vectorised
+ * rows, with its measured time in ms. */
+int spand_tree_qrcp_wave_count(spand_tree* t, int* n);
+int spand_tree_qrcp_wave(spand_tree* t, int idx, int* conf9, int* ncand);
+int spand_tree_qrcp_wave_candidate(spand_tree* t, int idx, int k, int* conf5, double* ms);
 
 #ifdef __cplusplus
 }

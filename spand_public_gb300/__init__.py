@@ -122,6 +122,10 @@ _PROTOS = {
     "spand_tree_profile_entry": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.POINTER(C.c_longlong),
                                            C.POINTER(C.c_double)]),
     "spand_tree_profile_reset": (C.c_int, [C.c_void_p]),
+    "spand_tree_qrcp_wave_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "spand_tree_qrcp_wave": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "spand_tree_qrcp_wave_candidate": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                                 C.POINTER(C.c_double)]),
     "spand_tree_work_count": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
     "spand_tree_work_entry": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_char_p, C.POINTER(C.c_double),
                                         C.POINTER(C.c_double)]),
@@ -447,6 +451,29 @@ class Tree:
             out[name.value.decode()] = dict(launches=la.value, ms=ms.value)
         if reset:
             _check(self.L.spand_tree_profile_reset(self.h))
+        return out
+
+    def qrcp_waves(self):
+        """The QRCP launch of every sparsification wave: a list of dicts (level, wave, items,
+        cap_rows, rpl, cs, threads, smem, vec_rows) with 'timed': [(conf dict, ms), ...], the
+        configurations the measuring factorization timed for the wave."""
+        n = C.c_int()
+        _check(self.L.spand_tree_qrcp_wave_count(self.h, C.byref(n)))
+        keys = ("level", "wave", "items", "cap_rows", "rpl", "cs", "threads", "smem", "vec_rows")
+        ckeys = ("rpl", "cs", "threads", "smem", "vec_rows")
+        out = []
+        for i in range(n.value):
+            conf = (C.c_int * 9)()
+            nc = C.c_int()
+            _check(self.L.spand_tree_qrcp_wave(self.h, i, conf, C.byref(nc)))
+            d = dict(zip(keys, list(conf)))
+            d["timed"] = []
+            for k in range(nc.value):
+                c5 = (C.c_int * 5)()
+                ms = C.c_double()
+                _check(self.L.spand_tree_qrcp_wave_candidate(self.h, i, k, c5, C.byref(ms)))
+                d["timed"].append((dict(zip(ckeys, list(c5))), ms.value))
+            out.append(d)
         return out
 
     def work(self, which: str = "factor"):

@@ -1,4 +1,5 @@
 // extern "C" boundary (include/spand_gb300.h) over spaND::Tree.
+#include <algorithm>
 #include <cstring>
 #include <exception>
 #include <string>
@@ -466,6 +467,34 @@ int spand_tree_profile_entry(spand_tree* t, int idx, char* name, long long* laun
 int spand_tree_profile_reset(spand_tree* t) {
     CHECK_T(t);
     if (t->t->device()) t->t->device()->profiler().clear();
+    return SPAND_OK;
+}
+int spand_tree_qrcp_wave_count(spand_tree* t, int* n) {
+    CHECK_T(t);
+    if (!n) return fail(SPAND_ERR_ARG, "null output");
+    if (!t->t->device()) return fail(SPAND_ERR_STATE, "before assemble");
+    *n = (int)t->t->device()->qrcp_waves().size();
+    return SPAND_OK;
+}
+int spand_tree_qrcp_wave(spand_tree* t, int idx, int* conf9, int* ncand) {
+    CHECK_T(t);
+    if (!conf9 || !ncand) return fail(SPAND_ERR_ARG, "null output");
+    if (!t->t->device()) return fail(SPAND_ERR_STATE, "before assemble");
+    const auto v = t->t->device()->qrcp_waves();
+    if (idx < 0 || idx >= (int)v.size()) return fail(SPAND_ERR_ARG, "index out of range");
+    std::copy(v[idx].conf, v[idx].conf + 9, conf9);
+    *ncand = (int)v[idx].cand.size();
+    return SPAND_OK;
+}
+int spand_tree_qrcp_wave_candidate(spand_tree* t, int idx, int k, int* conf5, double* ms) {
+    CHECK_T(t);
+    if (!conf5 || !ms) return fail(SPAND_ERR_ARG, "null output");
+    if (!t->t->device()) return fail(SPAND_ERR_STATE, "before assemble");
+    const auto v = t->t->device()->qrcp_waves();
+    if (idx < 0 || idx >= (int)v.size()) return fail(SPAND_ERR_ARG, "index out of range");
+    if (k < 0 || k >= (int)v[idx].cand.size()) return fail(SPAND_ERR_ARG, "candidate out of range");
+    std::copy(v[idx].cand[k].begin(), v[idx].cand[k].end(), conf5);
+    *ms = v[idx].ms[k];
     return SPAND_OK;
 }
 int spand_tree_work_count(spand_tree* t, int which, int* n) {

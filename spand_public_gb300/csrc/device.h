@@ -9,6 +9,7 @@
 
 #include <cuda_runtime.h>
 
+#include <array>
 #include <cstdint>
 #include <memory>
 #include <string>
@@ -157,6 +158,17 @@ class DeviceFactorBase {
     // ordering, host memory; copied) are kept by every sparsification of the following
     // factorizations; nphi = 0 turns it off
     virtual void set_phi(const double* phi, int n, int nphi) = 0;
+    // The QRCP launch of every sparsification wave, in launch order: level, wave, matrices,
+    // row capacity of its largest matrix, blocked rows per lane (0: the unblocked kernel),
+    // CTAs per cluster, threads per CTA, dynamic shared memory, and the row count from which
+    // the trailing update is vectorised (INT_MAX: never); with the configurations the
+    // measuring factorization timed and their times (empty where none was measured).
+    struct QrcpWave {
+        int conf[9];
+        std::vector<std::array<int, 5>> cand;  // rpl, cs, threads, smem, vec_rows
+        std::vector<double> ms;
+    };
+    virtual std::vector<QrcpWave> qrcp_waves() const { return {}; }
 
    protected:
     int failed_cluster_ = -1;

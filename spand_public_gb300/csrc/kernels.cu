@@ -258,7 +258,7 @@ __device__ bool chol_inv_smem(T* A, int n, int* bad) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) potrf3_kernel(Ctx<T> c, const int* __restrict__ pivots,
+__global__ void __launch_bounds__(256, 3) potrf3_kernel(Ctx<T> c, const int* __restrict__ pivots,
                                                      const int* __restrict__ clusters, int count, int smem_elems,
                                                      int strip_max_n, const int* __restrict__ only) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1425,6 +1425,80 @@ __device__ void larft_blocks(const T* V, int ldv, int rows, int k, const T* tau,
     }
 }
 
+// Off-diagonal blocks of the k x k factor T of Q = I - V T V^T over all k reflectors (the
+// form in which the one-right-hand-side Orthogonal op applies Q in three passes).  Block
+// column j (columns [c0, c0 + bw)) is T[0:c0, j] = -T[0:c0, 0:c0] (V[:, 0:c0]^T V_j) T_j:
+// Q_0 ... Q_{j-1} = I - V_A T_A V_A^T merged with Q_j, j ascending.  S = V_A^T V_j is summed
+// over the rows >= c0 (V_j is zero above) in 32 x 32 tiles staged in shared memory and
+// written into T's block column; M = S T_j replaces it row by row (a warp per row); then
+// -T_A M replaces M one 32-row chunk at a time in ascending order (chunk p reads rows >= p
+// of M only, so the rows it overwrites are read by no later chunk).  256 threads; sm holds
+// 3 x 32 x 33 elements; the diagonal blocks T_j are larft_blocks' (zero below the diagonal).
+template <typename T>
+__device__ void larft_offdiag(const T* V, int ldv, int rows, int k, T* Tm, int ldt, T* sm) {
+    const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, w = tid >> 5, nw = nth >> 5;
+    constexpr int L = QB + 1;
+    T* ta = sm;
+    T* tb = sm + QB * L;
+    T* tj = sm + 2 * QB * L;
+    const int nb = (k + QB - 1) / QB;
+    auto vval = [&](int r, int j) -> T { return r > j ? V[r + (size_t)j * ldv] : (r == j ? T(1) : T(0)); };
+    for (int jb = 1; jb < nb; jb++) {
+        const int c0 = jb * QB, bw = min(QB, k - c0);
+        for (int p0 = 0; p0 < c0; p0 += QB) {
+            T acc[4] = {T(0), T(0), T(0), T(0)};
+            for (int r0 = c0; r0 < rows; r0 += QB) {
+                __syncthreads();
+                for (int idx = tid; idx < QB * QB; idx += nth) {
+                    const int rr = idx % QB, cc = idx / QB, r = r0 + rr;
+                    ta[rr * L + cc] = r < rows ? vval(r, p0 + cc) : T(0);
+                    tb[rr * L + cc] = (r < rows && cc < bw) ? vval(r, c0 + cc) : T(0);
+                }
+                __syncthreads();
+                for (int rr = 0; rr < QB; rr++) {
+                    const T b = tb[rr * L + lane];
+                    for (int u = 0; u < 4 && w + nw * u < QB; u++) acc[u] += ta[rr * L + w + nw * u] * b;
+                }
+            }
+            if (lane < bw)
+                for (int u = 0; u < 4 && w + nw * u < QB; u++) Tm[(p0 + w + nw * u) + (size_t)(c0 + lane) * ldt] = acc[u];
+        }
+        for (int idx = tid; idx < QB * QB; idx += nth) {
+            const int l = idx % QB, q = idx / QB;
+            tj[l * L + q] = (l < bw && q < bw && l <= q) ? Tm[(c0 + l) + (size_t)(c0 + q) * ldt] : T(0);
+        }
+        __syncthreads();  // S in T's block column, T_j staged
+        for (int p = w; p < c0; p += nw) {
+            T* sp = Tm + p + (size_t)c0 * ldt;
+            const T sv = lane < bw ? sp[(size_t)lane * ldt] : T(0);
+            T m = T(0);
+            for (int l = 0; l < QB; l++) m += __shfl_sync(0xffffffffu, sv, l) * tj[l * L + lane];
+            if (lane < bw) sp[(size_t)lane * ldt] = m;
+        }
+        for (int p0 = 0; p0 < c0; p0 += QB) {
+            T acc[4] = {T(0), T(0), T(0), T(0)};
+            for (int l0 = p0; l0 < c0; l0 += QB) {
+                __syncthreads();
+                for (int idx = tid; idx < QB * QB; idx += nth) {
+                    const int pp = idx % QB, ll = idx / QB;
+                    ta[ll * L + pp] = p0 + pp <= l0 + ll ? Tm[(p0 + pp) + (size_t)(l0 + ll) * ldt] : T(0);
+                    tb[pp * L + ll] = ll < bw ? Tm[(l0 + pp) + (size_t)(c0 + ll) * ldt] : T(0);
+                }
+                __syncthreads();
+                for (int ll = 0; ll < QB; ll++) {
+                    const T b = tb[ll * L + lane];
+                    for (int u = 0; u < 4 && w + nw * u < QB; u++) acc[u] += ta[ll * L + w + nw * u] * b;
+                }
+            }
+            __syncthreads();  // every thread has read this chunk's rows of M
+            if (lane < bw)
+                for (int u = 0; u < 4 && w + nw * u < QB; u++)
+                    Tm[(p0 + w + nw * u) + (size_t)(c0 + lane) * ldt] = -acc[u];
+        }
+        __syncthreads();
+    }
+}
+
 // WY factors of a sparsified cluster's reflectors (for the Orthogonal op of the solve) and
 // its tau saved.  One CTA per cluster of the wave.  Reads only the persistent reflector
 // store (filled by sparsify_scatter_kernel) and the cluster's own tau slots, so it may
@@ -1443,6 +1517,8 @@ __global__ void __launch_bounds__(256) sparsify_wy_kernel(Ctx<T> c, const DSpars
     extern __shared__ __align__(16) unsigned char lb_raw[];
     T* sm = reinterpret_cast<T*>(lb_raw);
     larft_blocks(vstore + it.v_off, ld, rows, k, taus_ws + it.tau_off, tstore + it.v_off, ld, sm);
+    __syncthreads();  // the diagonal blocks written
+    larft_offdiag(vstore + it.v_off, ld, rows, k, tstore + it.v_off, ld, sm);
 }
 
 // Compressed edges AsnP = triu(R[:k,:]) P^T written back into the cluster's edge blocks,
@@ -1821,6 +1897,90 @@ __global__ void __launch_bounds__(TV_THREADS) trsv4_kernel(Ctx<T> c, XCtx<T> X, 
     if (threadIdx.x == 0) counters[cl] = 0;
 }
 
+// The triangular products (as trsv4_kernel) of clusters of at most 64 rows, one warp per
+// cluster, eight clusters per CTA: x in registers (rows lane and lane + 32), every x_k
+// reaches the lanes by shuffle.  Forward y_i = x_i / L_ii + sum_{k<i} L^{-1}[i][k] x_k with
+// lane i walking row i of L^{-1} (column i of the block, contiguous); backward
+// y_k = x_k / L_kk + sum_{i>k} L^{-1}[i][k] x_i with consecutive lanes on consecutive
+// entries of each column (coalesced).  In place: the warp holds all of x before it writes.
+constexpr int TS_WARPS = 8;
+template <typename T>
+__global__ void __launch_bounds__(32 * TS_WARPS) trsv_small_kernel(Ctx<T> c, XCtx<T> X,
+                                                                   const int* __restrict__ clusters,
+                                                                   const int* __restrict__ lblocks,
+                                                                   const int* __restrict__ idx, int count, int trans) {
+    const int lane = threadIdx.x & 31;
+    const int item = blockIdx.x * TS_WARPS + (threadIdx.x >> 5);
+    if (item >= count) return;
+    const int k = idx[item];
+    const int cl = clusters[k];
+    const int n = c.rows0[cl];
+    if (n == 0) return;
+    const T* __restrict__ L = bptr(c, lblocks[k]);
+    const int ld = c.blk[lblocks[k]].ld;
+    const int ia = lane, ib = lane + 32;
+    const T da = ia < n ? L[ia + (size_t)ia * ld] : T(1);
+    const T db = ib < n ? L[ib + (size_t)ib * ld] : T(1);
+    for (int rhs = 0; rhs < X.nrhs; rhs++) {
+        T* x = X.xs + X.xoff[cl] + (size_t)rhs * X.xld;
+        const T xa = ia < n ? x[ia] : T(0);
+        const T xb = ib < n ? x[ib] : T(0);
+        T sa0 = xa / da, sa1 = T(0), sb0 = xb / db, sb1 = T(0);
+        if (!trans) {
+            // row i of L^{-1} is read only for rows of the cluster (i < n) and only left of
+            // its diagonal (q < i)
+            const int ea = ia < n ? ia : 0, eb = ib < n ? ib : 0;
+            const T* la = L + (size_t)ea * ld;
+            const T* lb = L + (size_t)eb * ld;
+            int q = 0;
+            for (; q + 1 < n; q += 2) {
+                const T x0 = __shfl_sync(0xffffffffu, q < 32 ? xa : xb, q & 31);
+                const T x1 = __shfl_sync(0xffffffffu, q + 1 < 32 ? xa : xb, (q + 1) & 31);
+                if (q < ea) sa0 += la[q] * x0;
+                if (q + 1 < ea) sa1 += la[q + 1] * x1;
+                if (q < eb) sb0 += lb[q] * x0;
+                if (q + 1 < eb) sb1 += lb[q + 1] * x1;
+            }
+            if (q < n) {
+                const T x0 = __shfl_sync(0xffffffffu, q < 32 ? xa : xb, q & 31);
+                if (q < ea) sa0 += la[q] * x0;
+                if (q < eb) sb0 += lb[q] * x0;
+            }
+        } else {
+            int q = 1;
+            for (; q + 1 < n; q += 2) {
+                const T x0 = __shfl_sync(0xffffffffu, q < 32 ? xa : xb, q & 31);
+                const T x1 = __shfl_sync(0xffffffffu, q + 1 < 32 ? xa : xb, (q + 1) & 31);
+                const T* l0 = L + (size_t)q * ld;
+                const T* l1 = L + (size_t)(q + 1) * ld;
+                if (ia < q) sa0 += l0[ia] * x0;
+                if (ia < q + 1) sa1 += l1[ia] * x1;
+                if (ib < q) sb0 += l0[ib] * x0;
+                if (ib < q + 1) sb1 += l1[ib] * x1;
+            }
+            if (q < n) {
+                const T x0 = __shfl_sync(0xffffffffu, q < 32 ? xa : xb, q & 31);
+                const T* l0 = L + (size_t)q * ld;
+                if (ia < q) sa0 += l0[ia] * x0;
+                if (ib < q) sb0 += l0[ib] * x0;
+            }
+        }
+        if (ia < n) x[ia] = sa0 + sa1;
+        if (ib < n) x[ib] = sb0 + sb1;
+    }
+}
+
+// One Gemm op's operands as the solve kernels use them: the factor block, the solve
+// vector it multiplies, its length and the LDLT signs.
+template <typename T>
+struct GemmMeta {
+    const T* A;
+    const T* x;
+    const T* sg;
+    int ld, n, kind;
+};
+constexpr int GM_CHUNK = 64;
+
 // Forward Gemm ops grouped by neighbour n (operations.cpp:55-93): x_n -= sum over the
 // group's ops of A_ns x_s (GemmSymmOut) or A_sn^T x_s (GemmSymmIn), in op order.  One
 // block per (group, 64 rows of x_n); 4 threads per row split the columns, partial sums
@@ -1854,52 +2014,70 @@ __global__ void __launch_bounds__(256) gemm_fwd2_kernel(Ctx<T> c, XCtx<T> X, con
     constexpr int RPW = GF_ROWS / 8;  // rows per warp in the GemmSymmIn products
     const int i = i0 + li;
     if (threadIdx.x < GF_ROWS) racc[threadIdx.x] = T(0);
-    __syncthreads();
+    // the ops' operands, GM_CHUNK at a time, looked up by one thread each (the lookups are
+    // chains of dependent loads; done in parallel they cost one chain per chunk, not per op)
+    __shared__ GemmMeta<T> meta[GM_CHUNK];
     T acc = 0;
-    for (int o = 0; o < G.count; o++) {
-        const DGemmOp op = ops[G.first + o];
-        const int ns = c.csize[op.self];
-        const T* xs = X.xs + X.xoff[op.self] + r * X.xld;
-        const T* A = bptr(c, op.block);
-        const int ld = c.blk[op.block].ld;
-        const T* sg = signs ? signs + soff[op.self] : nullptr;
-        const int kind = op.kind & 15;
-        if (kind == 1) {
-            // A_ns x_s: a thread per row (consecutive rows read consecutive entries)
-            if (i < nn) {
-                T s0 = 0, s1 = 0, s2 = 0, s3 = 0;
-                int j = sp;
-                if (sg) {
-                    for (; j < ns; j += 4) s0 += A[i + (size_t)j * ld] * (sg[j] * xs[j]);
-                } else {
-                    for (; j + 12 < ns; j += 16) {
-                        s0 += A[i + (size_t)j * ld] * xs[j];
-                        s1 += A[i + (size_t)(j + 4) * ld] * xs[j + 4];
-                        s2 += A[i + (size_t)(j + 8) * ld] * xs[j + 8];
-                        s3 += A[i + (size_t)(j + 12) * ld] * xs[j + 12];
+    for (int o0 = 0; o0 < G.count; o0 += GM_CHUNK) {
+        const int cnt = min(GM_CHUNK, G.count - o0);
+        __syncthreads();
+        if (threadIdx.x < cnt) {
+            const DGemmOp op = ops[G.first + o0 + threadIdx.x];
+            GemmMeta<T> m;
+            m.n = c.csize[op.self];
+            m.x = X.xs + X.xoff[op.self] + r * X.xld;
+            m.A = bptr(c, op.block);
+            m.ld = c.blk[op.block].ld;
+            m.sg = signs ? signs + soff[op.self] : nullptr;
+            m.kind = op.kind & 15;
+            meta[threadIdx.x] = m;
+        }
+        __syncthreads();
+        for (int o = 0; o < cnt; o++) {
+            const GemmMeta<T> m = meta[o];
+            const int ns = m.n;
+            const T* xs = m.x;
+            const T* A = m.A;
+            const int ld = m.ld;
+            const T* sg = m.sg;
+            const int kind = m.kind;
+            if (kind == 1) {
+                // A_ns x_s: a thread per row (consecutive rows read consecutive entries)
+                if (i < nn) {
+                    T s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+                    int j = sp;
+                    if (sg) {
+                        for (; j < ns; j += 4) s0 += A[i + (size_t)j * ld] * (sg[j] * xs[j]);
+                    } else {
+                        for (; j + 12 < ns; j += 16) {
+                            s0 += A[i + (size_t)j * ld] * xs[j];
+                            s1 += A[i + (size_t)(j + 4) * ld] * xs[j + 4];
+                            s2 += A[i + (size_t)(j + 8) * ld] * xs[j + 8];
+                            s3 += A[i + (size_t)(j + 12) * ld] * xs[j + 12];
+                        }
+                        for (; j < ns; j += 4) s0 += A[i + (size_t)j * ld] * xs[j];
                     }
-                    for (; j < ns; j += 4) s0 += A[i + (size_t)j * ld] * xs[j];
+                    acc += (s0 + s1) + (s2 + s3);
                 }
-                acc += (s0 + s1) + (s2 + s3);
-            }
-        } else {
-            // A_sn^T x_s: row i is column i of A_sn; a warp per RPW rows, lanes over j
-            // (consecutive lanes read consecutive entries), the rows' sums in parallel
-            T sr[RPW];
+            } else {
+                // A_sn^T x_s: row i is column i of A_sn; a warp per RPW rows, lanes over j
+                // (consecutive lanes read consecutive entries), the rows' sums in parallel
+                T sr[RPW];
 #pragma unroll
-            for (int u = 0; u < RPW; u++) sr[u] = T(0);
-            for (int j = lane; j < ns; j += 32) {
-                const T xj = sg ? sg[j] * xs[j] : xs[j];
+                for (int u = 0; u < RPW; u++) sr[u] = T(0);
+                for (int j = lane; j < ns; j += 32) {
+                    const T xj = sg ? sg[j] * xs[j] : xs[j];
+#pragma unroll
+                    for (int u = 0; u < RPW; u++) {
+                        const int ii = i0 + wid * RPW + u;
+                        if (ii < nn) sr[u] += A[j + (size_t)ii * ld] * xj;
+                    }
+                }
 #pragma unroll
                 for (int u = 0; u < RPW; u++) {
-                    const int ii = i0 + wid * RPW + u;
-                    if (ii < nn) sr[u] += A[j + (size_t)ii * ld] * xj;
+                    const T v = warp_sum(sr[u]);
+                    if (lane == 0) racc[wid * RPW + u] += v;
                 }
-            }
-#pragma unroll
-            for (int u = 0; u < RPW; u++) {
-                const T v = warp_sum(sr[u]);
-                if (lane == 0) racc[wid * RPW + u] += v;
             }
         }
     }
@@ -1936,37 +2114,54 @@ __global__ void __launch_bounds__(256) gemm_bwd2_kernel(Ctx<T> c, XCtx<T> X, con
     T wsum[GB_ROWS / 8];
 #pragma unroll
     for (int u = 0; u < GB_ROWS / 8; u++) wsum[u] = T(0);
-    for (int o = 0; o < G.count; o++) {
-        const DGemmOp op = ops[G.first + o];
-        const int nn = (sib_mode || (op.kind & 16)) ? c.csize[op.nbr] : c.rows0[op.nbr];
-        const T* xn = X.xs + X.xoff[op.nbr] + r * X.xld;
-        const T* A = bptr(c, op.block);
-        const int ld = c.blk[op.block].ld;
-        if ((op.kind & 15) == 1) {
-            // A_ns^T x_n: entry i is column i of A_ns
+    __shared__ GemmMeta<T> meta[GM_CHUNK];  // as in gemm_fwd2_kernel
+    for (int o0 = 0; o0 < G.count; o0 += GM_CHUNK) {
+        const int cnt = min(GM_CHUNK, G.count - o0);
+        __syncthreads();
+        if (threadIdx.x < cnt) {
+            const DGemmOp op = ops[G.first + o0 + threadIdx.x];
+            GemmMeta<T> m;
+            m.n = (sib_mode || (op.kind & 16)) ? c.csize[op.nbr] : c.rows0[op.nbr];
+            m.x = X.xs + X.xoff[op.nbr] + r * X.xld;
+            m.A = bptr(c, op.block);
+            m.ld = c.blk[op.block].ld;
+            m.sg = nullptr;
+            m.kind = op.kind & 15;
+            meta[threadIdx.x] = m;
+        }
+        __syncthreads();
+        for (int o = 0; o < cnt; o++) {
+            const GemmMeta<T> m = meta[o];
+            const int nn = m.n;
+            const T* xn = m.x;
+            const T* A = m.A;
+            const int ld = m.ld;
+            if (m.kind == 1) {
+                // A_ns^T x_n: entry i is column i of A_ns
 #pragma unroll
-            for (int u = 0; u < GB_ROWS / 8; u++) {
-                const int ii = w + nw * u;
-                const int i = i0 + ii;
-                if (ii < GB_ROWS && i < ns) {
-                    const T* a = A + (size_t)i * ld;
-                    T s = 0;
-                    for (int j = lane; j < nn; j += 32) s += a[j] * xn[j];
-                    wsum[u] += s;
+                for (int u = 0; u < GB_ROWS / 8; u++) {
+                    const int ii = w + nw * u;
+                    const int i = i0 + ii;
+                    if (ii < GB_ROWS && i < ns) {
+                        const T* a = A + (size_t)i * ld;
+                        T s = 0;
+                        for (int j = lane; j < nn; j += 32) s += a[j] * xn[j];
+                        wsum[u] += s;
+                    }
                 }
-            }
-        } else {
-            // A_sn x_n: a thread per entry, column slices j = sp (mod 8)
-            const int i = i0 + li;
-            if (i < ns) {
-                T s0 = 0, s1 = 0;
-                int j = sp;
-                for (; j + 8 < nn; j += 16) {
-                    s0 += A[i + (size_t)j * ld] * xn[j];
-                    s1 += A[i + (size_t)(j + 8) * ld] * xn[j + 8];
+            } else {
+                // A_sn x_n: a thread per entry, column slices j = sp (mod 8)
+                const int i = i0 + li;
+                if (i < ns) {
+                    T s0 = 0, s1 = 0;
+                    int j = sp;
+                    for (; j + 8 < nn; j += 16) {
+                        s0 += A[i + (size_t)j * ld] * xn[j];
+                        s1 += A[i + (size_t)(j + 8) * ld] * xn[j + 8];
+                    }
+                    for (; j < nn; j += 8) s0 += A[i + (size_t)j * ld] * xn[j];
+                    pacc += s0 + s1;
                 }
-                for (; j < nn; j += 8) s0 += A[i + (size_t)j * ld] * xn[j];
-                pacc += s0 + s1;
             }
         }
     }
@@ -2074,18 +2269,110 @@ __global__ void __launch_bounds__(512) ortho_wyb_kernel(Ctx<T> c, XCtx<T> X, con
     for (int i = threadIdx.x; i < rows; i += blockDim.x) x[i] = xs[i];
 }
 
+// Orthogonal op with the whole compact WY factor (T: k x k upper triangular, off-diagonal
+// blocks from larft_offdiag): fwd x <- Q^T x = x - V T^T V^T x, bwd x <- Q x = x - V T V^T x
+// (operations.cpp:153-158) in three passes and two barriers whatever k: w = V^T x (a warp
+// per reflector, lanes down its column), y = T^T w (a warp per entry, lanes down T's
+// column) or T w (a thread per entry, consecutive threads on consecutive rows of T), then
+// x -= V y (a thread per row, consecutive threads on consecutive rows of V).  Every factor
+// read is coalesced; V is read twice and T once, straight from global memory.  One CTA per
+// (cluster, right-hand side); shared memory: x (rows), w and y (k each).
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) ortho_full_kernel(Ctx<T> c, XCtx<T> X, const DOrtho* __restrict__ items,
+                                                        int count, const T* __restrict__ vstore,
+                                                        const T* __restrict__ tstore, int trans) {
+    const int item = blockIdx.x % count;
+    const int r = blockIdx.x / count;
+    const DOrtho it = items[item];
+    const int rows = c.rows0[it.cluster];
+    const int k = c.csize[it.cluster];
+    if (k >= rows || k == 0) return;
+    const int ld = c.cap[it.cluster];
+    const T* __restrict__ V = vstore + it.v_off;
+    const T* __restrict__ Tm = tstore + it.v_off;
+    T* x = X.xs + X.xoff[it.cluster] + (size_t)r * X.xld;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* xs = reinterpret_cast<T*>(smem_raw);
+    T* wv = xs + rows;
+    T* yv = wv + k;
+    constexpr int NW = NT / 32;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    for (int i = tid; i < rows; i += NT) xs[i] = x[i];
+    __syncthreads();
+    for (int i = w; i < k; i += NW) {
+        const T* vi = V + (size_t)i * ld;
+        T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+        int q = i + 1 + lane;
+        for (; q + 96 < rows; q += 128) {
+            s0 += vi[q] * xs[q];
+            s1 += vi[q + 32] * xs[q + 32];
+            s2 += vi[q + 64] * xs[q + 64];
+            s3 += vi[q + 96] * xs[q + 96];
+        }
+        for (; q < rows; q += 32) s0 += vi[q] * xs[q];
+        const T s = warp_sum((s0 + s1) + (s2 + s3));
+        if (lane == 0) wv[i] = xs[i] + s;
+    }
+    __syncthreads();
+    if (trans) {
+        for (int i = w; i < k; i += NW) {
+            const T* ti = Tm + (size_t)i * ld;
+            T s0 = T(0), s1 = T(0);
+            int j = lane;
+            for (; j + 32 <= i; j += 64) {
+                s0 += ti[j] * wv[j];
+                s1 += ti[j + 32] * wv[j + 32];
+            }
+            if (j <= i) s0 += ti[j] * wv[j];
+            const T s = warp_sum(s0 + s1);
+            if (lane == 0) yv[i] = s;
+        }
+    } else {
+        for (int i = tid; i < k; i += NT) {
+            T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+            int j = i;
+            for (; j + 3 < k; j += 4) {
+                s0 += Tm[i + (size_t)j * ld] * wv[j];
+                s1 += Tm[i + (size_t)(j + 1) * ld] * wv[j + 1];
+                s2 += Tm[i + (size_t)(j + 2) * ld] * wv[j + 2];
+                s3 += Tm[i + (size_t)(j + 3) * ld] * wv[j + 3];
+            }
+            for (; j < k; j++) s0 += Tm[i + (size_t)j * ld] * wv[j];
+            yv[i] = (s0 + s1) + (s2 + s3);
+        }
+    }
+    __syncthreads();
+    for (int q = tid; q < rows; q += NT) {
+        const int iend = min(q, k);  // stored entries V[q][i], i < q; V[q][q] = 1 when q < k
+        T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+        int i = 0;
+        for (; i + 3 < iend; i += 4) {
+            s0 += V[q + (size_t)i * ld] * yv[i];
+            s1 += V[q + (size_t)(i + 1) * ld] * yv[i + 1];
+            s2 += V[q + (size_t)(i + 2) * ld] * yv[i + 2];
+            s3 += V[q + (size_t)(i + 3) * ld] * yv[i + 3];
+        }
+        for (; i < iend; i++) s0 += V[q + (size_t)i * ld] * yv[i];
+        if (q < k) s0 += yv[q];
+        x[q] = xs[q] - ((s0 + s1) + (s2 + s3));
+    }
+}
+
 // Merge op: parent x = children heads concatenated (fwd) and back (bwd)
 template <typename T>
 __global__ void merge_x_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ children, const int* __restrict__ parent_of,
                                int nchildren, const int* __restrict__ cpos, int fwd) {
-    const int k = blockIdx.x % nchildren;
-    const int r = blockIdx.x / nchildren;
+    // a warp per (child, right-hand side)
+    const int pair = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (pair >= nchildren * X.nrhs) return;
+    const int k = pair % nchildren;
+    const int r = pair / nchildren;
     const int ch = children[k];
     const int p = parent_of[k];
     const int n = c.csize[ch];
     T* xc = X.xs + X.xoff[ch] + r * X.xld;
     T* xp = X.xs + X.xoff[p] + cpos[ch] + r * X.xld;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int i = threadIdx.x & 31; i < n; i += 32) {
         if (fwd) xp[i] = xc[i];
         else xc[i] = xp[i];
     }
@@ -3105,6 +3392,10 @@ class DeviceFactor : public DeviceFactorBase {
                 {
                     const int64_t full = ((int64_t)mx + QB * (QB + 1) + (int64_t)QB * mx) * (int64_t)sizeof(T);
                     D.x_smem_ortho = full <= 200 * 1024 ? (int)full : mx * (int)sizeof(T);
+                    // the whole-T form: x, w and y (k <= rows <= capacity)
+                    const int64_t of = 3 * (int64_t)mx * (int64_t)sizeof(T);
+                    D.ortho_full_smem = of <= 200 * 1024 ? (int)of : 0;
+                    D.ortho_full_wide = mx >= 96;
                 }
                 const int64_t mr = (int64_t)mx * (MR_RB + 1) * (int64_t)sizeof(T);
                 D.ortho_mrhs_smem = mr <= 200 * 1024 ? (int)mr : 0;
@@ -3166,6 +3457,10 @@ class DeviceFactor : public DeviceFactorBase {
         SPAND_CUDA(cudaFuncSetAttribute(sparsify_wy_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         larft_smem_elems() * (int)sizeof(T)));
         SPAND_CUDA(cudaFuncSetAttribute(ortho_wyb_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SPAND_CUDA(cudaFuncSetAttribute(ortho_full_kernel<T, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        200 * 1024));
+        SPAND_CUDA(cudaFuncSetAttribute(ortho_full_kernel<T, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        200 * 1024));
         caps_h_ = P.c_cap;
     }
 
@@ -3729,6 +4024,7 @@ class DeviceFactor : public DeviceFactorBase {
         DSpars* items = nullptr;
         int maxcap = 1;
         std::vector<QcConf> cands;  // launch configurations the measuring factorization times
+        std::vector<std::pair<QcConf, float>> timed;  // what it measured (ms per candidate)
         int64_t cols = 0;           // Asn columns of all its matrices (pivot workspace)
         int rpl = 0;         // > 0: the blocked QRCP for up to 32 * rpl rows; 0: the unblocked kernel
         int vec_rows = INT_MAX;  // unblocked kernel: slabs of at least this many rows are vectorised
@@ -3803,6 +4099,8 @@ class DeviceFactor : public DeviceFactorBase {
         DTile* gf_tiles32 = nullptr;  // forward Gemm groups in 32-row tiles (many right-hand sides)
         int n_gf_tiles32 = 0;
         int ortho_mrhs_smem = 0;      // x of 32 right-hand sides (rows x 33); 0: one at a time
+        int ortho_full_smem = 0;      // the whole-T Orthogonal op's x, w, y (0: too large, blocked form)
+        bool ortho_full_wide = false; // its 512-thread instantiation (clusters of 96 rows or more)
         int2 *elim_tv = nullptr, *scale_tv = nullptr;  // (item, row tile) of the triangular products
         int n_elim_tv = 0, n_scale_tv = 0;
         int n_gf = 0, n_gb = 0;
@@ -3921,7 +4219,7 @@ class DeviceFactor : public DeviceFactorBase {
             // co-resident clusters of the launch the level's matrices would take together
             WaveDev probe;
             probe.n = n;
-            choose_cluster(probe, dims);
+            choose_cluster(probe, dims, false, false);  // the same waves whatever is forced
             const QcKernel<T> fn =
                 probe.rpl > 0 ? qrcp_blocked_kernel_ptr<T>(probe.rpl) : qrcp_smem_kernel_ptr<T>(probe.threads);
             // Levels whose matrices need clusters of 8 or 16 CTAs keep their waves: with so few
@@ -4147,18 +4445,19 @@ class DeviceFactor : public DeviceFactorBase {
     // 64-thread CTAs fit eight, which the many small matrices of the lower levels use); the
     // estimate is rounds x (per-step latency + passes over the largest slab by the CTA's
     // threads) and the smallest wins.
-    void choose_cluster(WaveDev& W, const std::vector<std::pair<int, int>>& dims, bool collect = false) {
+    void choose_cluster(WaveDev& W, const std::vector<std::pair<int, int>>& dims, bool collect = false,
+                        bool honour_force = true) {
         double best = 1e300;
         int bcs = 0, bsm = 0, bth = QC_THREADS, bvec = INT_MAX;
         std::vector<QcConf> all;  // every launchable configuration with its estimate
         int maxrows_ = 0;
         for (const auto& d : dims) maxrows_ = std::max(maxrows_, d.first);
         // SPAND_QC_VEC=0 / 1: never / always (where the slabs are tall enough) the vectorised update
-        const int force_vec = getenv("SPAND_QC_VEC") ? atoi(getenv("SPAND_QC_VEC")) : -1;
+        const int force_vec = (honour_force && getenv("SPAND_QC_VEC")) ? atoi(getenv("SPAND_QC_VEC")) : -1;
         // SPAND_QC_CS=<cs>, SPAND_QC_THREADS=<n>: that configuration wherever the matrices
         // fit (measurement aids)
-        const int force = getenv("SPAND_QC_CS") ? atoi(getenv("SPAND_QC_CS")) : 0;
-        const int force_th = getenv("SPAND_QC_THREADS") ? atoi(getenv("SPAND_QC_THREADS")) : 0;
+        const int force = (honour_force && getenv("SPAND_QC_CS")) ? atoi(getenv("SPAND_QC_CS")) : 0;
+        const int force_th = (honour_force && getenv("SPAND_QC_THREADS")) ? atoi(getenv("SPAND_QC_THREADS")) : 0;
         for (int cs = 1; cs <= qc_max_cs_; cs *= 2) {
             int64_t sm = 4096, work = 0;
             for (const auto& d : dims) {
@@ -4201,7 +4500,7 @@ class DeviceFactor : public DeviceFactorBase {
         // is bound by latency, not by shared-memory bandwidth), so it is taken only with
         // SPAND_QC_BLOCKED=1 (wherever the matrices fit it)
         int brpl = 0;
-        const char* fb = getenv("SPAND_QC_BLOCKED");
+        const char* fb = honour_force ? getenv("SPAND_QC_BLOCKED") : nullptr;
         const int force_b = fb ? atoi(fb) : 0;
         int maxrows = 0;
         for (const auto& d : dims) maxrows = std::max(maxrows, d.first);
@@ -4251,6 +4550,7 @@ class DeviceFactor : public DeviceFactorBase {
         W.smem = bsm;
         W.threads = bth;
         W.cands.clear();
+        W.timed.clear();
         if (collect && force_b == 0 && force <= 0 && force_th <= 0 && force_vec < 0) {
             // the measuring factorization times the model's best configurations of each
             // kernel variant (QC_TUNE_PER_KIND each: scalar, blocked, vectorised update; the
@@ -4264,6 +4564,21 @@ class DeviceFactor : public DeviceFactorBase {
                 taken[kind]++;
                 if (q.rpl == brpl && q.cs == bcs && q.threads == bth && q.vec_rows == bvec) continue;
                 W.cands.push_back(q);
+            }
+            // and the model pick's neighbours (twice the CTAs with half or the same threads,
+            // half the CTAs with twice the threads, half the threads): where the model errs
+            // the fastest launch was one of these at 64^3
+            const int nb[4][2] = {{2, -2}, {2, 1}, {-2, 2}, {1, -2}};
+            for (const auto& m : nb) {
+                const int cs = m[0] > 0 ? bcs * m[0] : bcs / -m[0];
+                const int th = m[1] > 0 ? bth * m[1] : bth / -m[1];
+                for (const QcConf& q : all) {
+                    if (q.rpl || q.cs != cs || q.threads != th || q.vec_rows != bvec) continue;
+                    bool dup = false;
+                    for (const QcConf& c : W.cands)
+                        dup |= c.rpl == q.rpl && c.cs == q.cs && c.threads == q.threads && c.vec_rows == q.vec_rows;
+                    if (!dup) W.cands.push_back(q);
+                }
             }
         }
     }
@@ -4299,6 +4614,22 @@ class DeviceFactor : public DeviceFactorBase {
         W.smem = q.smem;
         W.cands.clear();
     }
+    std::vector<QrcpWave> qrcp_waves() const override {
+        std::vector<QrcpWave> out;
+        for (size_t l = 0; l < levels_.size(); l++)
+            for (size_t w = 0; w < levels_[l].waves.size(); w++) {
+                const WaveDev& W = levels_[l].waves[w];
+                QrcpWave q;
+                const int c[9] = {(int)l, (int)w, W.n, W.maxcap, W.rpl, W.cs, W.threads, W.smem, W.vec_rows};
+                std::copy(c, c + 9, q.conf);
+                for (const auto& t : W.timed) {
+                    q.cand.push_back({t.first.rpl, t.first.cs, t.first.threads, t.first.smem, t.first.vec_rows});
+                    q.ms.push_back(t.second);
+                }
+                out.push_back(q);
+            }
+        return out;
+    }
     size_t n_waves() const {
         size_t n = 0;
         for (const LevelDev& D : levels_) n += D.waves.size();
@@ -4318,18 +4649,31 @@ class DeviceFactor : public DeviceFactorBase {
             SPAND_CUDA(cudaEventCreate(&e));
             tune_ev_.push_back(e);
         }
-        for (size_t k = 0; k < K; k++) {
-            apply_conf_keep(W, W.cands[k]);
-            SPAND_CUDA(cudaEventRecord(tune_ev_[2 * k], s_));
-            launch_qrcp_once(W, tol);
-            SPAND_CUDA(cudaEventRecord(tune_ev_[2 * k + 1], s_));
+        // one untimed launch first, so that every timed one finds the inputs in L2 alike;
+        // every candidate timed twice (rounds in the same order), the faster kept
+        apply_conf_keep(W, W.cands[0]);
+        launch_qrcp_once(W, tol);
+        std::vector<float> best_ms(K, 1e30f);
+        for (int round = 0; round < 2; round++) {
+            for (size_t k = 0; k < K; k++) {
+                apply_conf_keep(W, W.cands[k]);
+                SPAND_CUDA(cudaEventRecord(tune_ev_[2 * k], s_));
+                launch_qrcp_once(W, tol);
+                SPAND_CUDA(cudaEventRecord(tune_ev_[2 * k + 1], s_));
+            }
+            SPAND_CUDA(cudaEventSynchronize(tune_ev_[2 * K - 1]));
+            for (size_t k = 0; k < K; k++) {
+                float ms = 0;
+                SPAND_CUDA(cudaEventElapsedTime(&ms, tune_ev_[2 * k], tune_ev_[2 * k + 1]));
+                best_ms[k] = std::min(best_ms[k], ms);
+            }
         }
-        SPAND_CUDA(cudaEventSynchronize(tune_ev_[2 * K - 1]));
         size_t bk = 0;
         float bms = 1e30f;
+        W.timed.clear();
         for (size_t k = 0; k < K; k++) {
-            float ms = 0;
-            SPAND_CUDA(cudaEventElapsedTime(&ms, tune_ev_[2 * k], tune_ev_[2 * k + 1]));
+            const float ms = best_ms[k];
+            W.timed.push_back({W.cands[k], ms});
             if (ms < bms) {
                 bms = ms;
                 bk = k;
@@ -4338,7 +4682,7 @@ class DeviceFactor : public DeviceFactorBase {
         const QcConf q = W.cands[bk];
         apply_conf(W, q);
         launch_qrcp_once(W, tol);
-        launches_ += (int64_t)K;
+        launches_ += (int64_t)(2 * K + 1);
     }
     void apply_conf_keep(WaveDev& W, const QcConf& q) {
         W.vec_rows = q.vec_rows;
@@ -4610,6 +4954,29 @@ class DeviceFactor : public DeviceFactorBase {
                 });
                 return;
             }
+            if (!mr && trsv_small_on_ && cur_level_ >= 0) {
+                // clusters of at most 64 rows a warp each, the others in row tiles
+                const LevelDev& D = levels_[cur_level_];
+                const bool elim = clusters == D.elim_llt;
+                const bool scale = clusters == D.scale_llt;
+                if (elim || scale) {
+                    const int* small = elim ? D.elim_small : D.scale_small;
+                    const int nsmall = elim ? D.n_elim_small : D.n_scale_small;
+                    const int2* big = elim ? D.elim_big_tv : D.scale_big_tv;
+                    const int nbig = elim ? D.n_elim_big_tv : D.n_scale_big_tv;
+                    if (nsmall)
+                        launch("trsv", [&] {
+                            trsv_small_kernel<T><<<(nsmall + TS_WARPS - 1) / TS_WARPS, 32 * TS_WARPS, 0, s_>>>(
+                                ctx_, X, clusters, blks, small, nsmall, trans);
+                        });
+                    if (nbig)
+                        launch("trsv", [&] {
+                            trsv4_kernel<T><<<nbig, TV_THREADS, smem, s_>>>(ctx_, X, clusters, blks, big, trans, tmp,
+                                                                            tv_count_);
+                        });
+                    return;
+                }
+            }
             launch("trsv", [&] {
                 if (mr)
                     trsv_mrhs_kernel<T><<<ntv, 256, 0, s_>>>(ctx_, X, clusters, blks, tv, trans, tmp, tv_count_);
@@ -4623,7 +4990,14 @@ class DeviceFactor : public DeviceFactorBase {
                 if (mr && D.ortho_mrhs_smem)
                     ortho_mrhs_kernel<T><<<D.n_ortho, 256, D.ortho_mrhs_smem, s_>>>(ctx_, X, D.ortho, vstore_, tstore_,
                                                                                     trans);
-                else
+                else if (D.ortho_full_smem && ortho_full_on_) {
+                    if (D.ortho_full_wide)
+                        ortho_full_kernel<T, 512><<<D.n_ortho * nrhs, 512, D.ortho_full_smem, s_>>>(
+                            ctx_, X, D.ortho, D.n_ortho, vstore_, tstore_, trans);
+                    else
+                        ortho_full_kernel<T, 256><<<D.n_ortho * nrhs, 256, D.ortho_full_smem, s_>>>(
+                            ctx_, X, D.ortho, D.n_ortho, vstore_, tstore_, trans);
+                } else
                     ortho_wyb_kernel<T><<<D.n_ortho * nrhs, 512, D.x_smem_ortho, s_>>>(
                         ctx_, X, D.ortho, D.n_ortho, vstore_, tstore_, trans, D.x_smem_ortho / (int)sizeof(T));
             });
@@ -4634,8 +5008,9 @@ class DeviceFactor : public DeviceFactorBase {
                 if (mr)
                     merge_x_mrhs_kernel<T><<<D.n_children, 256, 0, s_>>>(ctx_, X, D.child_idx, D.child_parent, cpos_, fwd);
                 else
-                    merge_x_kernel<T><<<D.n_children * nrhs, 128, 0, s_>>>(ctx_, X, D.child_idx, D.child_parent,
-                                                                           D.n_children, cpos_, fwd);
+                    merge_x_kernel<T><<<(D.n_children * nrhs + 7) / 8, 256, 0, s_>>>(ctx_, X, D.child_idx,
+                                                                                     D.child_parent, D.n_children,
+                                                                                     cpos_, fwd);
             });
         };
         for (int l = 0; l < P.nlevels; l++) {
@@ -4745,6 +5120,10 @@ class DeviceFactor : public DeviceFactorBase {
     bool tuned_ = false;
     // re-layered sparsification waves after the first factorization (SPAND_QC_RELAYER=0: the plan's)
     bool relayer_on_ = !(getenv("SPAND_QC_RELAYER") && atoi(getenv("SPAND_QC_RELAYER")) == 0);
+    // SPAND_ORTHO_FULL=0: the Orthogonal op of one right-hand side in the blocked form
+    bool ortho_full_on_ = !(getenv("SPAND_ORTHO_FULL") && atoi(getenv("SPAND_ORTHO_FULL")) == 0);
+    // SPAND_TRSV_SMALL=0: the triangular products of small clusters in row tiles as well
+    bool trsv_small_on_ = !(getenv("SPAND_TRSV_SMALL") && atoi(getenv("SPAND_TRSV_SMALL")) == 0);
     // measured QRCP tuning: the factorization after tune_qrcp() times every wave's
     // candidates (SPAND_QC_TUNE=0: the launch model's choice only); the winners are kept per
     // plan fingerprint for the process (trees of the same plan skip the measurement)

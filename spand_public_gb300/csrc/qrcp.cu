@@ -168,7 +168,12 @@ __global__ void __launch_bounds__(NT) qrcp_cluster_kernel(Ctx<T> c, const DSpars
     // threads per column for the trailing update
     int G = 1;
     while (G < 8 && (nloc * G * 2 <= nth || rows >= 64 * G)) G *= 2;
-    if (vec) G = 8;
+    if (vec) {
+        // eight lanes per column, or four where that takes the slab's columns in fewer
+        // rounds (the same vectors per lane, one fixed round cost less)
+        const int g8 = nth / 8, g4 = nth / 4;
+        G = (nloc + g4 - 1) / g4 < (nloc + g8 - 1) / g8 ? 4 : 8;
+    }
     const int gid = tid / G, gl = tid % G, ngroups = nth / G;
     const T tie = T(1) - qrcp_tie<T>();
     const T tol3z = dsqrt(sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-07));
@@ -223,8 +228,13 @@ __global__ void __launch_bounds__(NT) qrcp_cluster_kernel(Ctx<T> c, const DSpars
     for (int i = 0; i < mn; i++) {
         const int par = i & 1;
         // (1) pivot, in every warp from the published entries
+        // (the entry loops unrolled over the slot bound: their loads issue together)
         T gmax = 0;
-        for (int e = lane; e < E; e += 32) gmax = fmax(gmax, pubm[par][e]);
+#pragma unroll
+        for (int q = 0; q < QC_SLOTS / 32; q++) {
+            const int e = lane + 32 * q;
+            if (e < E) gmax = fmax(gmax, pubm[par][e]);
+        }
         gmax = warp_max(gmax);
         const T thr = gmax * tie;
         int pvt = INT_MAX;
@@ -232,11 +242,17 @@ __global__ void __launch_bounds__(NT) qrcp_cluster_kernel(Ctx<T> c, const DSpars
         // a warp whose maximum reaches the global window published the first position of
         // its own (wider or equal) window; where that column also reaches the global
         // threshold it is the warp's first candidate, else the warp must search again
-        for (int e = lane; e < E; e += 32) {
-            const T m = pubm[par][e];
-            if (m >= thr) {
-                if (pubn[par][e] >= thr) pvt = min(pvt, pubf[par][e]);
-                else amb = true;
+#pragma unroll
+        for (int q = 0; q < QC_SLOTS / 32; q++) {
+            const int e = lane + 32 * q;
+            if (e < E) {
+                const T m = pubm[par][e];
+                const T fnm = pubn[par][e];
+                const int fpos = pubf[par][e];
+                if (m >= thr) {
+                    if (fnm >= thr) pvt = min(pvt, fpos);
+                    else amb = true;
+                }
             }
         }
         pvt = warp_min(pvt);
@@ -286,8 +302,7 @@ __global__ void __launch_bounds__(NT) qrcp_cluster_kernel(Ctx<T> c, const DSpars
         part = warp_sum(part);
         if (lane == 0) red[w] = part;
         __syncthreads();  // partial norms, alpha; every thread has read perm
-        T xnorm2 = 0;
-        for (int k = 0; k < nw; k++) xnorm2 += red[k];
+        const T xnorm2 = warp_sum(lane < nw ? red[lane] : T(0));
         const T alpha = s_alpha;
         const T xnorm = dsqrt(xnorm2);
         T beta, tu, sc;
@@ -327,7 +342,7 @@ __global__ void __launch_bounds__(NT) qrcp_cluster_kernel(Ctx<T> c, const DSpars
             if (vec) {
                 if (active && tu != T(0)) {
                     T s0 = 0, s1 = 0;
-                    for (int r = rv + VW * gl; r < rows; r += VW * 8) {
+                    for (int r = rv + VW * gl; r < rows; r += VW * G) {
                         const QcPack<T> a = *reinterpret_cast<const QcPack<T>*>(aj + r);
                         const QcPack<T> v = *reinterpret_cast<const QcPack<T>*>(vsh + r);
 #pragma unroll
@@ -355,7 +370,7 @@ __global__ void __launch_bounds__(NT) qrcp_cluster_kernel(Ctx<T> c, const DSpars
             if (vec && active && tu != T(0)) {
                 const T coef = tu * (ai0 + sc * s);
                 const T cr = coef * sc;
-                for (int r = rv + VW * gl; r < rows; r += VW * 8) {
+                for (int r = rv + VW * gl; r < rows; r += VW * G) {
                     QcPack<T> a = *reinterpret_cast<const QcPack<T>*>(aj + r);
                     const QcPack<T> v = *reinterpret_cast<const QcPack<T>*>(vsh + r);
 #pragma unroll
