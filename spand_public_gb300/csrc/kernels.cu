@@ -164,31 +164,38 @@ __device__ bool chol_inv_smem(T* A, int n, int* bad) {
         }
         // (2) diagonal block and its inverse (upper-triangle slots of the block)
         if (tid < 32) {
+            // the block in registers, lane i holding row i (a[k] = A[i][k], k <= i):
+            // right-looking Cholesky with the columns broadcast by shuffles (the same
+            // operations per element, in the same order, as a column-by-column update)
+            T a[PNB];
+#pragma unroll
+            for (int k = 0; k < PNB; k++) a[k] = (k <= lane && lane < w) ? A[(jb + lane) + (jb + k) * n] : T(0);
             int fail = 0;
-            for (int j = 0; j < w; j++) {
-                T* cj = A + (jb + j) * n + jb;
-                T d = 0;
-                if (lane == j) {
-                    d = cj[j];
+#pragma unroll
+            for (int j = 0; j < PNB; j++) {
+                if (j < w) {
+                    T d = __shfl_sync(0xffffffffu, a[j], j);
                     if (!(d > T(0))) {
                         fail = 1;
                         d = T(1);
                     } else {
                         d = dsqrt(d);
                     }
-                    cj[j] = d;
+                    if (lane == j) a[j] = d;
+                    else if (lane > j) a[j] /= d;
+                    const T lij = a[j];
+#pragma unroll
+                    for (int k = j + 1; k < PNB; k++) {
+                        const T lkj = __shfl_sync(0xffffffffu, a[j], k);
+                        if (lane > j && k <= lane) a[k] -= lij * lkj;
+                    }
                 }
-                d = __shfl_sync(0xffffffffu, d, j);
-                fail = __shfl_sync(0xffffffffu, fail, j);
-                if (fail) break;
-                if (lane > j && lane < w) cj[lane] /= d;
-                __syncwarp();
-                if (lane > j && lane < w) {
-                    const T lij = cj[lane];
-                    for (int kk = j + 1; kk <= lane; kk++) A[(jb + lane) + (jb + kk) * n] -= lij * cj[kk];
-                }
-                __syncwarp();
             }
+            if (lane < w)
+#pragma unroll
+                for (int k = 0; k < PNB; k++)
+                    if (k <= lane) A[(jb + lane) + (jb + k) * n] = a[k];
+            __syncwarp();
             if (lane == 0 && fail) *bad = 1;
             if (!fail) {
                 // column c = lane of D = L_pp^{-1} in registers (forward substitution on e_c,
@@ -258,9 +265,10 @@ __device__ bool chol_inv_smem(T* A, int n, int* bad) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256, 3) potrf3_kernel(Ctx<T> c, const int* __restrict__ pivots,
+__global__ void __launch_bounds__(256) potrf3_kernel(Ctx<T> c, const int* __restrict__ pivots,
                                                      const int* __restrict__ clusters, int count, int smem_elems,
-                                                     int strip_max_n, const int* __restrict__ only) {
+                                                     int strip_max_n, const int* __restrict__ only,
+                                                     int small_cap = 0) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
     const int item = blockIdx.x;
@@ -275,7 +283,7 @@ __global__ void __launch_bounds__(256, 3) potrf3_kernel(Ctx<T> c, const int* __r
     if (failed) return;
     const int cl = clusters[item];
     const int n = c.csize[cl];
-    if (n == 0) return;
+    if (n == 0 || c.cap[cl] <= small_cap) return;  // small pivots: potrf_small_kernel
     T* G = bptr(c, pivots[item]);
     const int gld = c.blk[pivots[item]].ld;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = blockDim.x >> 5;
@@ -295,6 +303,76 @@ __global__ void __launch_bounds__(256, 3) potrf3_kernel(Ctx<T> c, const int* __r
         if (!bad && n > strip_max_n) trtri_to_upper(G, gld, n);
     }
     if (bad && threadIdx.x == 0) atomicCAS(&c.status->not_spd, 0, cl + 1);
+}
+
+// Pivots of at most 32 rows, one warp each (eight per CTA), in registers: lane i holds row
+// i of the block (a[k] = A[i][k], k <= i); right-looking Cholesky with the columns
+// broadcast by shuffles (the same operations per element, in the same order, as
+// chol_inv_smem's diagonal block), then column c = lane of L^{-1} by forward substitution
+// with L's rows broadcast by shuffles.  Out: L in the lower triangle, L^{-1} transposed in
+// the strictly upper one (the layout of potrf3_kernel).  The thousands of small pivots of
+// the lowest levels otherwise take a 256-thread CTA each, two per SM (the large kernel's
+// registers), for a few hundred FMAs.
+constexpr int PS_WARPS = 8;
+template <typename T>
+__global__ void __launch_bounds__(32 * PS_WARPS) potrf_small_kernel(Ctx<T> c, const int* __restrict__ pivots,
+                                                                   const int* __restrict__ clusters, int count) {
+    const int lane = threadIdx.x & 31;
+    const int k = blockIdx.x * PS_WARPS + (threadIdx.x >> 5);
+    if (k >= count) return;
+    if (*(volatile int*)&c.status->not_spd) return;
+    const int item = k;
+    const int cl = clusters[item];
+    const int n = c.csize[cl];
+    if (n == 0 || n > 32) return;
+    T* G = bptr(c, pivots[item]);
+    const int ld = c.blk[pivots[item]].ld;
+    T a[32];
+#pragma unroll
+    for (int q = 0; q < 32; q++) a[q] = (q <= lane && lane < n) ? G[lane + (size_t)q * ld] : T(0);
+    int fail = 0;
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+        if (j < n) {
+            T d = __shfl_sync(0xffffffffu, a[j], j);
+            if (!(d > T(0))) {
+                fail = 1;
+                d = T(1);
+            } else {
+                d = dsqrt(d);
+            }
+            if (lane == j) a[j] = d;
+            else if (lane > j) a[j] /= d;
+            const T lij = a[j];
+#pragma unroll
+            for (int q = j + 1; q < 32; q++) {
+                const T lqj = __shfl_sync(0xffffffffu, a[j], q);
+                if (lane > j && q <= lane) a[q] -= lij * lqj;
+            }
+        }
+    }
+    if (__any_sync(0xffffffffu, fail)) {
+        if (lane == 0) atomicCAS(&c.status->not_spd, 0, cl + 1);
+        return;
+    }
+    // D = L^{-1}, column c = lane: D[r][c] = (delta_rc - sum_{c <= l < r} L[r][l] D[l][c]) / L[r][r]
+    T dcol[32];
+#pragma unroll
+    for (int r = 0; r < 32; r++) {
+        T acc = r == lane ? T(1) : T(0);
+#pragma unroll
+        for (int l = 0; l < r; l++) acc -= __shfl_sync(0xffffffffu, a[l], r) * dcol[l];
+        const T lrr = __shfl_sync(0xffffffffu, a[r], r);
+        dcol[r] = (r >= lane && r < n) ? acc / lrr : T(0);
+    }
+    if (lane < n) {
+#pragma unroll
+        for (int q = 0; q < 32; q++)
+            if (q <= lane) G[lane + (size_t)q * ld] = a[q];  // L, row lane
+#pragma unroll
+        for (int r = 0; r < 32; r++)
+            if (r > lane && r < n) G[lane + (size_t)r * ld] = dcol[r];  // L^{-1}[r][lane] at (lane, r)
+    }
 }
 
 // Cholesky factorization of pivot blocks too large for one CTA's shared memory, in the
@@ -699,6 +777,108 @@ __global__ void __launch_bounds__(256) trsm3_kernel(Ctx<T> c, const DTrsm* __res
                 xr[cc * sk] = s + xr[cc * sk] / L[cc + (size_t)cc * lld];
             }
         }
+    }
+}
+
+// The same panel products (LLT pivots, no row permutation) on the tensor cores, FP32 path:
+// out = X (L^{-1})^T for a 32-row tile X of the panel, with mma.sync m16n8k8 TF32 tiles and
+// FP32 accumulation.  Every operand is split into a TF32 head and a TF32 tail and the
+// product summed as head*head + head*tail + tail*head (the "3xTF32" scheme, Ootomo and
+// Yokota 2022): about 22 of FP32's 24 significand bits per product (measured 1-4x the SIMT
+// kernel's error against FP64).  The tensor core accumulates one 8-deep k-step at a time
+// (its internal additions are not rounded to nearest, which over a long inner dimension
+// costs accuracy) and the steps are added in FP32 registers.  The tile is staged in shared
+// memory with stride TC_XLD (conflict-free A-fragment loads); B fragments come straight
+// from the pivot block: B[k][cc] = (L^{-1})[cc][k], the block's column cc above the
+// diagonal, 1 / L_cc on it and zero below.  Warp w computes the 8-column blocks w, w + 8,
+// ..., each over the k-blocks up to its diagonal.
+constexpr int TC_XLD = TRB + 8;
+
+__device__ __forceinline__ uint32_t tf32_of(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ void mma_tf32_16x8x8(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__global__ void __launch_bounds__(256) trsm_tc_kernel(Ctx<float> c, const DTrsm* __restrict__ items,
+                                                      const DTile* __restrict__ tiles, int ntiles) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* X = reinterpret_cast<float*>(smem_raw);
+    const int t = blockIdx.x;
+    if (t >= ntiles || c.status->not_spd) return;
+    const DTrsm it = items[tiles[t].item];
+    const int n = c.csize[it.cluster];
+    if (n == 0) return;
+    const float* L = bptr(c, it.lblock);
+    const int lld = c.blk[it.lblock].ld;
+    float* B = bptr(c, it.block);
+    const int bld = c.blk[it.block].ld;
+    const int m = it.side == 1 ? c.csize[c.blk[it.block].rowc] : c.csize[c.blk[it.block].colc];
+    const int r0 = tiles[t].tile_i * TRB;
+    if (r0 >= m) return;
+    const int tr = min(TRB, m - r0);
+    const long long sq = it.side == 1 ? 1 : bld, sk = it.side == 1 ? bld : 1;
+    float* Bt = B + (it.side == 1 ? (size_t)r0 : (size_t)r0 * bld);
+    const int nc = (n + 7) & ~7;
+    for (int idx = threadIdx.x; idx < TRB * nc; idx += blockDim.x) {
+        int q, k;
+        if (it.side == 1) {
+            q = idx % TRB;
+            k = idx / TRB;
+        } else {
+            k = idx % nc;
+            q = idx / nc;
+        }
+        X[q + k * TC_XLD] = (q < tr && k < n) ? Bt[q * sq + (long long)k * sk] : 0.f;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, g = lane >> 2, tg = lane & 3;
+    for (int cb = w; cb < nc / 8; cb += 8) {
+        const int cc0 = cb * 8, cc = cc0 + g;
+        const bool live = cc < n;
+        const float* lcol = L + (size_t)(live ? cc : 0) * lld;
+        const float dinv = live ? 1.f / lcol[cc] : 0.f;
+        float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+        for (int k0 = 0; k0 <= cc0; k0 += 8) {
+            const int ka = k0 + tg, kb = ka + 4;
+            const float b0 = !live ? 0.f : (ka < cc ? lcol[ka] : (ka == cc ? dinv : 0.f));
+            const float b1 = !live ? 0.f : (kb < cc ? lcol[kb] : (kb == cc ? dinv : 0.f));
+            uint32_t bh[2] = {tf32_of(b0), tf32_of(b1)};
+            uint32_t bl[2] = {tf32_of(b0 - __uint_as_float(bh[0])), tf32_of(b1 - __uint_as_float(bh[1]))};
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const float* xa = X + 16 * h + g;
+                const float av[4] = {xa[ka * TC_XLD], xa[8 + ka * TC_XLD], xa[kb * TC_XLD], xa[8 + kb * TC_XLD]};
+                uint32_t ah[4], al[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    ah[i] = tf32_of(av[i]);
+                    al[i] = tf32_of(av[i] - __uint_as_float(ah[i]));
+                }
+                // one k-step per tensor-core accumulation (its internal sums are not rounded
+                // to nearest); the steps are added in FP32 outside it
+                float big[4] = {0.f, 0.f, 0.f, 0.f}, small[4] = {0.f, 0.f, 0.f, 0.f};
+                mma_tf32_16x8x8(small, al, bh);
+                mma_tf32_16x8x8(small, ah, bl);
+                mma_tf32_16x8x8(big, ah, bh);
+#pragma unroll
+                for (int e = 0; e < 4; e++) acc[h][e] += big[e] + small[e];
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++)
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int q = 16 * h + g + (i >= 2 ? 8 : 0), col = cc0 + 2 * tg + (i & 1);
+                if (q < tr && col < n) Bt[q * sq + (long long)col * sk] = acc[h][i];
+            }
     }
 }
 
@@ -1328,6 +1508,99 @@ __global__ void __launch_bounds__(256) schur_kernel(Ctx<T> c, const DTarget* __r
             int i = i0 + tx + 16 * a, j = j0 + ty + 16 * b;
             if (i < M && j < N && (!tg.syrk || i >= j)) C[i + (size_t)j * ldc] = acc[a][b];
         }
+}
+
+// The Schur updates on the tensor cores, FP32 path: the same 32x32 tiles of C, the same
+// staging of X and Y (SK entries of the inner dimension at a time, LDLT signs applied);
+// warp w owns the 16x8 piece (rows 16 (w mod 2), columns 8 (w / 2)) and accumulates
+// -X Y into it with mma.sync m16n8k8 TF32, each operand split into TF32 head and tail
+// (head*head + head*tail + tail*head, close to FP32 accuracy), two k-steps per staged
+// chunk.
+__global__ void __launch_bounds__(256) schur_tc_kernel(Ctx<float> c, const DTarget* __restrict__ targets,
+                                                       const DUpd* __restrict__ ups, const DTile* __restrict__ tiles,
+                                                       int ntiles, const float* __restrict__ signs = nullptr,
+                                                       const long long* __restrict__ soff = nullptr) {
+    const int t = blockIdx.x;
+    if (t >= ntiles || c.status->not_spd) return;
+    const DTarget tg = targets[tiles[t].item];
+    const DBlock cb = c.blk[tg.target];
+    const int M = c.csize[cb.rowc], N = c.csize[cb.colc];
+    const int i0 = tiles[t].tile_i * ST, j0 = tiles[t].tile_j * ST;
+    if (i0 >= M || j0 >= N) return;
+    if (tg.syrk && i0 + ST <= j0) return;  // strictly upper tile
+    __shared__ float Xs[ST][SK + 4];
+    __shared__ float Ys[SK][ST + 8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, g = lane >> 2, tq = lane & 3;
+    const int mh = 16 * (w & 1), nb = 8 * (w >> 1);
+    float* C = c.arena + cb.off;
+    const int ldc = cb.ld;
+    float acc[4];
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        const int i = i0 + mh + g + (e >= 2 ? 8 : 0), j = j0 + nb + 2 * tq + (e & 1);
+        acc[e] = (i < M && j < N) ? C[i + (size_t)j * ldc] : 0.f;
+    }
+    for (int u = 0; u < tg.count; u++) {
+        const DUpd up = ups[tg.first + u];
+        const int S = c.csize[up.s];
+        const float* B1 = bptr(c, up.b1);
+        const int ld1 = c.blk[up.b1].ld;
+        const float* B2 = bptr(c, up.b2);
+        const int ld2 = c.blk[up.b2].ld;
+        for (int k0 = 0; k0 < S; k0 += SK) {
+            for (int idx = threadIdx.x; idx < ST * SK; idx += 256) {
+                int ii, kk;
+                if (up.t1) { kk = idx % SK; ii = idx / SK; } else { ii = idx % ST; kk = idx / ST; }
+                const int i = i0 + ii, k = k0 + kk;
+                float v = 0.f;
+                if (i < M && k < S) {
+                    v = up.t1 ? B1[k + (size_t)i * ld1] : B1[i + (size_t)k * ld1];
+                    if (signs) v *= signs[soff[up.s] + k];
+                }
+                Xs[ii][kk] = v;
+            }
+            for (int idx = threadIdx.x; idx < ST * SK; idx += 256) {
+                int jj, kk;
+                if (up.t2) { jj = idx % ST; kk = idx / ST; } else { kk = idx % SK; jj = idx / SK; }
+                const int j = j0 + jj, k = k0 + kk;
+                float v = 0.f;
+                if (j < N && k < S) v = up.t2 ? B2[j + (size_t)k * ld2] : B2[k + (size_t)j * ld2];
+                Ys[kk][jj] = v;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int ks = 0; ks < SK; ks += 8) {
+                // A = -X (rows mh.., inner ks..), B = Y (inner ks.., columns nb..)
+                const float av[4] = {-Xs[mh + g][ks + tq], -Xs[mh + g + 8][ks + tq], -Xs[mh + g][ks + tq + 4],
+                                     -Xs[mh + g + 8][ks + tq + 4]};
+                const float bv[2] = {Ys[ks + tq][nb + g], Ys[ks + tq + 4][nb + g]};
+                uint32_t ah[4], al[4], bh[2], bl[2];
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    ah[e] = tf32_of(av[e]);
+                    al[e] = tf32_of(av[e] - __uint_as_float(ah[e]));
+                }
+#pragma unroll
+                for (int e = 0; e < 2; e++) {
+                    bh[e] = tf32_of(bv[e]);
+                    bl[e] = tf32_of(bv[e] - __uint_as_float(bh[e]));
+                }
+                // one k-step per tensor-core accumulation, the steps added in FP32 outside it
+                float big[4] = {0.f, 0.f, 0.f, 0.f}, small[4] = {0.f, 0.f, 0.f, 0.f};
+                mma_tf32_16x8x8(small, al, bh);
+                mma_tf32_16x8x8(small, ah, bl);
+                mma_tf32_16x8x8(big, ah, bh);
+#pragma unroll
+                for (int e = 0; e < 4; e++) acc[e] += big[e] + small[e];
+            }
+            __syncthreads();
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        const int i = i0 + mh + g + (e >= 2 ? 8 : 0), j = j0 + nb + 2 * tq + (e & 1);
+        if (i < M && j < N && (!tg.syrk || i >= j)) C[i + (size_t)j * ldc] = acc[e];
+    }
 }
 
 // ------------------------------------------------------------------------------------
@@ -2272,11 +2545,13 @@ __global__ void __launch_bounds__(512) ortho_wyb_kernel(Ctx<T> c, XCtx<T> X, con
 // Orthogonal op with the whole compact WY factor (T: k x k upper triangular, off-diagonal
 // blocks from larft_offdiag): fwd x <- Q^T x = x - V T^T V^T x, bwd x <- Q x = x - V T V^T x
 // (operations.cpp:153-158) in three passes and two barriers whatever k: w = V^T x (a warp
-// per reflector, lanes down its column), y = T^T w (a warp per entry, lanes down T's
-// column) or T w (a thread per entry, consecutive threads on consecutive rows of T), then
-// x -= V y (a thread per row, consecutive threads on consecutive rows of V).  Every factor
-// read is coalesced; V is read twice and T once, straight from global memory.  One CTA per
-// (cluster, right-hand side); shared memory: x (rows), w and y (k each).
+// per four reflectors, lanes down their columns), y = T^T w (a warp per four entries, lanes
+// down T's columns) or T w (a thread per entry, consecutive threads on consecutive rows of
+// T), then x -= V y (a thread per row, consecutive threads on consecutive rows of V).  Every
+// factor read is coalesced, and each thread keeps four to eight independent loads in
+// flight (the passes are bound by load latency, not bandwidth); V is read twice and T
+// once, straight from global memory.  One CTA per (cluster, right-hand side); shared
+// memory: x (rows), w and y (k each).
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT) ortho_full_kernel(Ctx<T> c, XCtx<T> X, const DOrtho* __restrict__ items,
                                                         int count, const T* __restrict__ vstore,
@@ -2296,66 +2571,219 @@ __global__ void __launch_bounds__(NT) ortho_full_kernel(Ctx<T> c, XCtx<T> X, con
     T* wv = xs + rows;
     T* yv = wv + k;
     constexpr int NW = NT / 32;
+    constexpr int C4 = 4;  // columns a warp sums at once (their loads in flight together)
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     for (int i = tid; i < rows; i += NT) xs[i] = x[i];
     __syncthreads();
-    for (int i = w; i < k; i += NW) {
-        const T* vi = V + (size_t)i * ld;
-        T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
-        int q = i + 1 + lane;
-        for (; q + 96 < rows; q += 128) {
-            s0 += vi[q] * xs[q];
-            s1 += vi[q + 32] * xs[q + 32];
-            s2 += vi[q + 64] * xs[q + 64];
-            s3 += vi[q + 96] * xs[q + 96];
+    // w_i = x_i + sum_{q>i} V[q][i] x_q
+    for (int i0 = w * C4; i0 < k; i0 += NW * C4) {
+        T s[C4];
+#pragma unroll
+        for (int u = 0; u < C4; u++) s[u] = T(0);
+        for (int q = i0 + 1 + lane; q < rows; q += 32) {
+            const T xq = xs[q];
+#pragma unroll
+            for (int u = 0; u < C4; u++)
+                if (i0 + u < k && q > i0 + u) s[u] += V[q + (size_t)(i0 + u) * ld] * xq;
         }
-        for (; q < rows; q += 32) s0 += vi[q] * xs[q];
-        const T s = warp_sum((s0 + s1) + (s2 + s3));
-        if (lane == 0) wv[i] = xs[i] + s;
+#pragma unroll
+        for (int u = 0; u < C4; u++) {
+            const T v = warp_sum(s[u]);
+            if (lane == 0 && i0 + u < k) wv[i0 + u] = xs[i0 + u] + v;
+        }
     }
     __syncthreads();
     if (trans) {
-        for (int i = w; i < k; i += NW) {
-            const T* ti = Tm + (size_t)i * ld;
-            T s0 = T(0), s1 = T(0);
-            int j = lane;
-            for (; j + 32 <= i; j += 64) {
-                s0 += ti[j] * wv[j];
-                s1 += ti[j + 32] * wv[j + 32];
+        // y_i = sum_{j<=i} T[j][i] w_j, lanes down column i of T
+        for (int i0 = w * C4; i0 < k; i0 += NW * C4) {
+            T s[C4];
+#pragma unroll
+            for (int u = 0; u < C4; u++) s[u] = T(0);
+            const int hi = min(i0 + C4 - 1, k - 1);
+            for (int j = lane; j <= hi; j += 32) {
+                const T wj = wv[j];
+#pragma unroll
+                for (int u = 0; u < C4; u++)
+                    if (j <= i0 + u && i0 + u < k) s[u] += Tm[j + (size_t)(i0 + u) * ld] * wj;
             }
-            if (j <= i) s0 += ti[j] * wv[j];
-            const T s = warp_sum(s0 + s1);
-            if (lane == 0) yv[i] = s;
+#pragma unroll
+            for (int u = 0; u < C4; u++) {
+                const T v = warp_sum(s[u]);
+                if (lane == 0 && i0 + u < k) yv[i0 + u] = v;
+            }
         }
     } else {
+        // y_i = sum_{j>=i} T[i][j] w_j, consecutive threads on consecutive rows of T
         for (int i = tid; i < k; i += NT) {
-            T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+            T s[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) s[u] = T(0);
             int j = i;
-            for (; j + 3 < k; j += 4) {
-                s0 += Tm[i + (size_t)j * ld] * wv[j];
-                s1 += Tm[i + (size_t)(j + 1) * ld] * wv[j + 1];
-                s2 += Tm[i + (size_t)(j + 2) * ld] * wv[j + 2];
-                s3 += Tm[i + (size_t)(j + 3) * ld] * wv[j + 3];
+            for (; j + 7 < k; j += 8) {
+#pragma unroll
+                for (int u = 0; u < 8; u++) s[u] += Tm[i + (size_t)(j + u) * ld] * wv[j + u];
             }
-            for (; j < k; j++) s0 += Tm[i + (size_t)j * ld] * wv[j];
-            yv[i] = (s0 + s1) + (s2 + s3);
+            for (; j < k; j++) s[0] += Tm[i + (size_t)j * ld] * wv[j];
+            yv[i] = ((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]));
         }
     }
     __syncthreads();
+    // x_q -= sum_{i <= min(q, k-1)} V[q][i] y_i (V[q][q] = 1), a thread per row
     for (int q = tid; q < rows; q += NT) {
-        const int iend = min(q, k);  // stored entries V[q][i], i < q; V[q][q] = 1 when q < k
-        T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+        const int iend = min(q, k);
+        T s[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) s[u] = T(0);
         int i = 0;
-        for (; i + 3 < iend; i += 4) {
-            s0 += V[q + (size_t)i * ld] * yv[i];
-            s1 += V[q + (size_t)(i + 1) * ld] * yv[i + 1];
-            s2 += V[q + (size_t)(i + 2) * ld] * yv[i + 2];
-            s3 += V[q + (size_t)(i + 3) * ld] * yv[i + 3];
+        for (; i + 7 < iend; i += 8) {
+#pragma unroll
+            for (int u = 0; u < 8; u++) s[u] += V[q + (size_t)(i + u) * ld] * yv[i + u];
         }
-        for (; i < iend; i++) s0 += V[q + (size_t)i * ld] * yv[i];
-        if (q < k) s0 += yv[q];
-        x[q] = xs[q] - ((s0 + s1) + (s2 + s3));
+        for (; i < iend; i++) s[0] += V[q + (size_t)i * ld] * yv[i];
+        if (q < k) s[0] += yv[q];
+        x[q] = xs[q] - (((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7])));
     }
+}
+
+// The same Orthogonal op for the large clusters of the top levels, on a thread-block
+// cluster of CS CTAs per (cluster, right-hand side): one CTA reads a fraction of V and T
+// only, so the op is spread over CS SMs' load bandwidth (one CTA alone is bound by the
+// loads it can keep in flight).  CTA r computes w and y for its slice of the k reflectors
+// and the update of its slice of the rows; the slices of w and of y are gathered through
+// distributed shared memory after a cluster barrier each.  Rows x reflectors of the
+// update are split over the warps (row blocks of 32 lanes x reflector chunks, partial
+// sums added in chunk order).  Shared memory: x, w, y and the partial sums.
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) ortho_cluster_kernel(Ctx<T> c, XCtx<T> X, const DOrtho* __restrict__ items,
+                                                           int count, const T* __restrict__ vstore,
+                                                           const T* __restrict__ tstore, int trans) {
+    namespace cgx = cooperative_groups;
+    cgx::cluster_group cl = cgx::this_cluster();
+    const int CS = (int)cl.num_blocks(), me = (int)cl.block_rank();
+    const int pair = blockIdx.x / CS;
+    const int item = pair % count, r = pair / count;
+    const DOrtho it = items[item];
+    const int rows = c.rows0[it.cluster];
+    const int k = c.csize[it.cluster];
+    if (k >= rows || k == 0) return;  // the same for every CTA of the cluster
+    const int ld = c.cap[it.cluster];
+    const T* __restrict__ V = vstore + it.v_off;
+    const T* __restrict__ Tm = tstore + it.v_off;
+    T* x = X.xs + X.xoff[it.cluster] + (size_t)r * X.xld;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* xs = reinterpret_cast<T*>(smem_raw);
+    T* wv = xs + rows;
+    T* yv = wv + k;
+    T* part = yv + k;  // NW x 32 partial sums
+    constexpr int NW = NT / 32;
+    constexpr int C4 = 4;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    auto lo = [&](int n, int q) { return (int)((long long)n * q / CS); };
+    // part holds 32 x max(NW, row blocks of a slice) partial sums
+    const int i_lo = lo(k, me), i_hi = lo(k, me + 1);
+    for (int i = tid; i < rows; i += NT) xs[i] = x[i];
+    __syncthreads();
+    for (int i0 = i_lo + w * C4; i0 < i_hi; i0 += NW * C4) {
+        T s4[C4];
+#pragma unroll
+        for (int u = 0; u < C4; u++) s4[u] = T(0);
+        for (int q = i0 + 1 + lane; q < rows; q += 32) {
+            const T xq = xs[q];
+#pragma unroll
+            for (int u = 0; u < C4; u++)
+                if (i0 + u < i_hi && q > i0 + u) s4[u] += V[q + (size_t)(i0 + u) * ld] * xq;
+        }
+#pragma unroll
+        for (int u = 0; u < C4; u++) {
+            const T v = warp_sum(s4[u]);
+            if (lane == 0 && i0 + u < i_hi) wv[i0 + u] = xs[i0 + u] + v;
+        }
+    }
+    // every reflector's w from the CTA that owns it
+    auto owner = [&](int i) {
+        int q = (int)(((long long)i * CS) / k);
+        while (q + 1 < CS && lo(k, q + 1) <= i) q++;
+        while (q > 0 && lo(k, q) > i) q--;
+        return q;
+    };
+    cl.sync();
+    for (int i = tid; i < k; i += NT) {
+        const int o = owner(i);
+        if (o != me) wv[i] = *cl.map_shared_rank(wv + i, o);
+    }
+    __syncthreads();
+    if (trans) {
+        for (int i0 = i_lo + w * C4; i0 < i_hi; i0 += NW * C4) {
+            T s4[C4];
+#pragma unroll
+            for (int u = 0; u < C4; u++) s4[u] = T(0);
+            const int hi = min(i0 + C4 - 1, i_hi - 1);
+            for (int j = lane; j <= hi; j += 32) {
+                const T wj = wv[j];
+#pragma unroll
+                for (int u = 0; u < C4; u++)
+                    if (j <= i0 + u && i0 + u < i_hi) s4[u] += Tm[j + (size_t)(i0 + u) * ld] * wj;
+            }
+#pragma unroll
+            for (int u = 0; u < C4; u++) {
+                const T v = warp_sum(s4[u]);
+                if (lane == 0 && i0 + u < i_hi) yv[i0 + u] = v;
+            }
+        }
+    } else {
+        for (int i = i_lo + tid; i < i_hi; i += NT) {
+            T s8[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) s8[u] = T(0);
+            int j = i;
+            for (; j + 7 < k; j += 8) {
+#pragma unroll
+                for (int u = 0; u < 8; u++) s8[u] += Tm[i + (size_t)(j + u) * ld] * wv[j + u];
+            }
+            for (; j < k; j++) s8[0] += Tm[i + (size_t)j * ld] * wv[j];
+            yv[i] = ((s8[0] + s8[1]) + (s8[2] + s8[3])) + ((s8[4] + s8[5]) + (s8[6] + s8[7]));
+        }
+    }
+    cl.sync();
+    for (int i = tid; i < k; i += NT) {
+        const int o = owner(i);
+        if (o != me) yv[i] = *cl.map_shared_rank(yv + i, o);
+    }
+    __syncthreads();
+    // x_q -= sum_{i <= min(q, k-1)} V[q][i] y_i for this CTA's rows: warp w takes row block
+    // w mod nrb (32 rows, a lane each) and reflector chunk w / nrb
+    const int q_lo = lo(rows, me), q_hi = lo(rows, me + 1);
+    const int nrb = (q_hi - q_lo + 31) / 32;
+    if (nrb > 0) {
+        const int nchunk = max(1, NW / nrb);
+        for (int vw = w; vw < nrb * nchunk; vw += NW) {  // more row blocks than warps: in turns
+            const int rb = vw % nrb, ch = vw / nrb;
+            const int q = q_lo + 32 * rb + lane;
+            const int iend = q < q_hi ? min(q, k) : 0;
+            const int c0 = (int)((long long)k * ch / nchunk), c1 = (int)((long long)k * (ch + 1) / nchunk);
+            const int e = min(c1, iend);
+            T s8[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) s8[u] = T(0);
+            int i = c0;
+            for (; i + 7 < e; i += 8) {
+#pragma unroll
+                for (int u = 0; u < 8; u++) s8[u] += V[q + (size_t)(i + u) * ld] * yv[i + u];
+            }
+            for (; i < e; i++) s8[0] += V[q + (size_t)i * ld] * yv[i];
+            if (q < k && q >= c0 && q < c1) s8[0] += yv[q];  // V[q][q] = 1
+            part[ch * (32 * nrb) + 32 * rb + lane] =
+                ((s8[0] + s8[1]) + (s8[2] + s8[3])) + ((s8[4] + s8[5]) + (s8[6] + s8[7]));
+        }
+        __syncthreads();
+        for (int qq = tid; qq < q_hi - q_lo; qq += NT) {
+            T sum = T(0);
+            for (int ch2 = 0; ch2 < nchunk; ch2++) sum += part[ch2 * (32 * nrb) + qq];
+            x[q_lo + qq] = xs[q_lo + qq] - sum;
+        }
+    }
+    // no CTA leaves while another may still read its w or y
+    cl.sync();
 }
 
 // Merge op: parent x = children heads concatenated (fwd) and back (bwd)
@@ -3043,6 +3471,21 @@ class DeviceFactor : public DeviceFactorBase {
             D.n_elim = (int)L.elim_clusters.size();
             D.elim_clusters = up(L.elim_clusters);
             D.elim_pivots = up(L.elim_pivots);
+            // LLT pivots of at most 32 rows: a warp each (potrf_small_kernel)
+            auto small_pivots = [&](const std::vector<int>& cl, const std::vector<int>& pv, int*& scl, int*& spv,
+                                    int& ns) {
+                std::vector<int> a, b;
+                if (!lu_ && !ldlt_)
+                    for (size_t q = 0; q < cl.size(); q++)
+                        if (P.c_cap[cl[q]] <= 32) {
+                            a.push_back(cl[q]);
+                            b.push_back(pv[q]);
+                        }
+                ns = (int)a.size();
+                scl = up(a);
+                spv = up(b);
+            };
+            small_pivots(L.elim_clusters, L.elim_pivots, D.elim_ps_cl, D.elim_ps_piv, D.n_elim_ps);
             D.elim_smem = smem_for(L.elim_clusters, P);
             D.elim_tri = build_trtri(L.elim_clusters, P);
             // PLU: the panels are products with the inverse block
@@ -3075,6 +3518,7 @@ class DeviceFactor : public DeviceFactorBase {
             D.n_scale = (int)L.scale_clusters.size();
             D.scale_clusters = up(L.scale_clusters);
             D.scale_pivots = up(L.scale_pivots);
+            small_pivots(L.scale_clusters, L.scale_pivots, D.scale_ps_cl, D.scale_ps_piv, D.n_scale_ps);
             D.scale_smem = smem_for(L.scale_clusters, P);
             D.scale_tri = build_trtri(L.scale_clusters, P);
             build_trsm(L.scale_trsm, lu_ ? L.scale_inv : L.scale_pivots, L.scale_clusters, P, D.scale_trsm0,
@@ -3396,6 +3840,14 @@ class DeviceFactor : public DeviceFactorBase {
                     const int64_t of = 3 * (int64_t)mx * (int64_t)sizeof(T);
                     D.ortho_full_smem = of <= 200 * 1024 ? (int)of : 0;
                     D.ortho_full_wide = mx >= 96;
+                    // the large clusters of the top levels: CS CTAs per cluster (at least 24
+                    // rows each, about eight CTAs per SM in all), 256 threads
+                    int cs = 1;
+                    while (cs < 8 && mx / (2 * cs) >= 24 && (int64_t)D.n_ortho * cs < 8 * (int64_t)num_sms_) cs *= 2;
+                    const int64_t oc = ((int64_t)3 * mx + 32 * std::max<int64_t>(8, (mx / cs + 31) / 32 + 1)) *
+                                       (int64_t)sizeof(T);
+                    D.ortho_cs = (mx >= 96 && cs > 1 && oc <= 200 * 1024) ? cs : 1;
+                    D.ortho_cs_smem = (int)oc;
                 }
                 const int64_t mr = (int64_t)mx * (MR_RB + 1) * (int64_t)sizeof(T);
                 D.ortho_mrhs_smem = mr <= 200 * 1024 ? (int)mr : 0;
@@ -3458,6 +3910,9 @@ class DeviceFactor : public DeviceFactorBase {
                                         larft_smem_elems() * (int)sizeof(T)));
         SPAND_CUDA(cudaFuncSetAttribute(ortho_wyb_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(ortho_full_kernel<T, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        200 * 1024));
+        SPAND_CUDA(cudaFuncSetAttribute(trsm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SPAND_CUDA(cudaFuncSetAttribute(ortho_cluster_kernel<T, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(ortho_full_kernel<T, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         200 * 1024));
@@ -3566,16 +4021,13 @@ class DeviceFactor : public DeviceFactorBase {
                     launch_trsm(D.elim_trsm0);
                     launch_trsm(D.elim_trsm1);
                 } else {
-                    launch_potrf(D.elim_pivots, D.elim_clusters, D.n_elim, D.elim_smem, D.elim_tri, D.elim_pc_cs,
+                    launch_potrf(D.elim_pivots, D.elim_clusters, D.n_elim, D.elim_ps_piv, D.elim_ps_cl, D.n_elim_ps,
+                                 D.elim_smem, D.elim_tri, D.elim_pc_cs,
                                  D.elim_pc_smem);
                     launch_trsm(D.elim_trsm0);
                     launch_trsm(D.elim_trsm1);
                 }
-                if (D.n_schur_tiles)
-                    launch("schur", [&] {
-                        schur_kernel<T><<<D.n_schur_tiles, 256, 0, s_>>>(ctx_, D.schur_targets, d_ups_, D.schur_tiles,
-                                                                         D.n_schur_tiles, signs_, d_xoff_);
-                    });
+                launch_schur(D.schur_targets, d_ups_, D.schur_tiles, D.n_schur_tiles);
             }
             if (D.scaled && D.n_scale) {
                 if (lu_) {
@@ -3587,7 +4039,8 @@ class DeviceFactor : public DeviceFactorBase {
                     launch_trsm(D.scale_trsm0);
                     launch_trsm(D.scale_trsm1);
                 } else {
-                    launch_potrf(D.scale_pivots, D.scale_clusters, D.n_scale, D.scale_smem, D.scale_tri,
+                    launch_potrf(D.scale_pivots, D.scale_clusters, D.n_scale, D.scale_ps_piv, D.scale_ps_cl,
+                                 D.n_scale_ps, D.scale_smem, D.scale_tri,
                                  D.scale_pc_cs, D.scale_pc_smem);
                     launch_trsm(D.scale_trsm0);
                     launch_trsm(D.scale_trsm1);
@@ -3653,11 +4106,7 @@ class DeviceFactor : public DeviceFactorBase {
                         lorasp_split<T>(ctx_, W.items, W.n, W.stiles, W.sib, W.orng, lr_splits_, vstore_, tstore_,
                                         rank_, s_);
                     });
-                    if (D.n_schur_tiles)
-                        launch("schur", [&] {
-                            schur_kernel<T><<<D.n_schur_tiles, 256, 0, s_>>>(ctx_, D.schur_targets, d_ups_, D.schur_tiles,
-                                                                             D.n_schur_tiles, signs_, d_xoff_);
-                        });
+                    launch_schur(D.schur_targets, d_ups_, D.schur_tiles, D.n_schur_tiles);
                 }
                 if (ldlt_) {
                     launch("pivot_split", [&] {
@@ -3666,11 +4115,7 @@ class DeviceFactor : public DeviceFactorBase {
                     });
                     launch_ldlt(W.sib_piv, W.sib, nullptr, W.n, W.ldlt_smem);
                     launch_trsm(W.sib_trsm);
-                    if (W.n_sib_tiles)
-                        launch("schur", [&] {
-                            schur_kernel<T><<<W.n_sib_tiles, 256, 0, s_>>>(ctx_, W.sib_targets, W.sib_ups, W.sib_tiles,
-                                                                           W.n_sib_tiles, signs_, d_xoff_);
-                        });
+                    launch_schur(W.sib_targets, W.sib_ups, W.sib_tiles, W.n_sib_tiles);
                 }
                 cur_wave_ = -1;
                 // WY factors: on the side stream beside the next wave's QRCP (on the main
@@ -4051,6 +4496,8 @@ class DeviceFactor : public DeviceFactorBase {
         int n_elim = 0;
         int* elim_clusters = nullptr;
         int* elim_pivots = nullptr;
+        int *elim_ps_cl = nullptr, *elim_ps_piv = nullptr, *scale_ps_cl = nullptr, *scale_ps_piv = nullptr;
+        int n_elim_ps = 0, n_scale_ps = 0;  // LLT pivots of at most 32 rows (a warp each)
         int elim_smem = 0;
         int elim_pc_cs = 0, elim_pc_smem = 0;   // cluster Cholesky (0: single-CTA kernel)
         TrsmDev elim_trsm0, elim_trsm1;
@@ -4101,6 +4548,8 @@ class DeviceFactor : public DeviceFactorBase {
         int ortho_mrhs_smem = 0;      // x of 32 right-hand sides (rows x 33); 0: one at a time
         int ortho_full_smem = 0;      // the whole-T Orthogonal op's x, w, y (0: too large, blocked form)
         bool ortho_full_wide = false; // its 512-thread instantiation (clusters of 96 rows or more)
+        int ortho_cs = 1;             // > 1: the thread-block-cluster form, CTAs per cluster
+        int ortho_cs_smem = 0;        // its shared memory
         int2 *elim_tv = nullptr, *scale_tv = nullptr;  // (item, row tile) of the triangular products
         int n_elim_tv = 0, n_scale_tv = 0;
         int n_gf = 0, n_gb = 0;
@@ -4710,7 +5159,15 @@ class DeviceFactor : public DeviceFactorBase {
                                       jpvt_, ipvt_, tauws_, rank_, colcount_, fallback_, tol,
                                       force_global_ ? 0 : W.smem, W.vec_rows, qc_proj()));
     }
-    void launch_potrf(int* pivots, int* clusters, int n, int smem, const TrtriDev& tri, int pc_cs, int pc_smem) {
+    void launch_potrf(int* pivots, int* clusters, int n, const int* ps_piv, const int* ps_cl, int n_ps, int smem,
+                      const TrtriDev& tri, int pc_cs, int pc_smem) {
+        // (not beside the cluster kernel or the strip inverse, which take every pivot of the list)
+        const bool small = n_ps > 0 && potrf_small_on_ && pc_cs == 0 && smem > 0;
+        if (small)
+            launch("potrf", [&] {
+                potrf_small_kernel<T><<<(n_ps + PS_WARPS - 1) / PS_WARPS, 32 * PS_WARPS, 0, s_>>>(ctx_, ps_piv, ps_cl,
+                                                                                              n_ps);
+            });
         if (pc_cs > 0) {
             launch("potrf_cluster", [&] {
                 cudaLaunchConfig_t cfg = {};
@@ -4736,7 +5193,7 @@ class DeviceFactor : public DeviceFactorBase {
         launch("potrf", [&] {
             potrf3_kernel<T><<<n, 256, smem, s_>>>(ctx_, pivots, clusters, n, smem / (int)sizeof(T),
                                                    strips ? tri.smem / (32 * (int)sizeof(T)) : 0,
-                                                   pc_cs > 0 ? (const int*)pc_fallback_ : nullptr);
+                                                   pc_cs > 0 ? (const int*)pc_fallback_ : nullptr, small ? 32 : 0);
         });
         if (strips)
             launch("trtri", [&] {
@@ -4780,8 +5237,33 @@ class DeviceFactor : public DeviceFactorBase {
         if (mx * (int64_t)sizeof(T) > 200 * 1024) throw DeviceError{SPAND_ERR_UNSUPPORTED, "pivot too large"};
         return (int)(mx * sizeof(T));
     }
+    void launch_schur(const DTarget* targets, const DUpd* ups, const DTile* tiles, int ntiles) {
+        if (!ntiles) return;
+        if constexpr (sizeof(T) == 4) {
+            if (schur_tc_on_) {
+                launch("schur", [&] {
+                    schur_tc_kernel<<<ntiles, 256, 0, s_>>>(ctx_, targets, ups, tiles, ntiles, signs_, d_xoff_);
+                });
+                return;
+            }
+        }
+        launch("schur", [&] {
+            schur_kernel<T><<<ntiles, 256, 0, s_>>>(ctx_, targets, ups, tiles, ntiles, signs_, d_xoff_);
+        });
+    }
     void launch_trsm(const TrsmDev& t) {
         if (!t.ntiles) return;
+        if constexpr (sizeof(T) == 4) {
+            // FP32 path, LLT pivots: the tensor-core kernel wherever its staged tile fits
+            const int nmax = t.smem / (TRB * (int)sizeof(T));
+            const int64_t tcs = (int64_t)TC_XLD * ((nmax + 7) & ~7) * (int64_t)sizeof(float);
+            if (trsm_tc_on_ && !ldlt_ && t.smem > 16 && tcs <= 200 * 1024) {
+                launch("trsm", [&] {
+                    trsm_tc_kernel<<<t.ntiles, 256, (size_t)tcs, s_>>>(ctx_, t.items, t.tiles, t.ntiles);
+                });
+                return;
+            }
+        }
         launch("trsm", [&] {
             trsm3_kernel<T><<<t.ntiles, 256, t.smem, s_>>>(ctx_, t.items, t.tiles, t.ntiles, t.smem / (int)sizeof(T),
                                                            ldlt_ ? lu_perm_ : nullptr, d_xoff_);
@@ -4990,7 +5472,22 @@ class DeviceFactor : public DeviceFactorBase {
                 if (mr && D.ortho_mrhs_smem)
                     ortho_mrhs_kernel<T><<<D.n_ortho, 256, D.ortho_mrhs_smem, s_>>>(ctx_, X, D.ortho, vstore_, tstore_,
                                                                                     trans);
-                else if (D.ortho_full_smem && ortho_full_on_) {
+                else if (D.ortho_cs > 1 && ortho_full_on_ && ortho_cluster_on_) {
+                    cudaLaunchConfig_t cfg = {};
+                    cfg.gridDim = dim3((unsigned)(D.n_ortho * nrhs * D.ortho_cs));
+                    cfg.blockDim = dim3(256);
+                    cfg.dynamicSmemBytes = (size_t)D.ortho_cs_smem;
+                    cfg.stream = s_;
+                    cudaLaunchAttribute attr[1];
+                    attr[0].id = cudaLaunchAttributeClusterDimension;
+                    attr[0].val.clusterDim.x = (unsigned)D.ortho_cs;
+                    attr[0].val.clusterDim.y = 1;
+                    attr[0].val.clusterDim.z = 1;
+                    cfg.attrs = attr;
+                    cfg.numAttrs = 1;
+                    SPAND_CUDA(cudaLaunchKernelEx(&cfg, ortho_cluster_kernel<T, 256>, ctx_, X, (const DOrtho*)D.ortho,
+                                                  D.n_ortho, (const T*)vstore_, (const T*)tstore_, trans));
+                } else if (D.ortho_full_smem && ortho_full_on_) {
                     if (D.ortho_full_wide)
                         ortho_full_kernel<T, 512><<<D.n_ortho * nrhs, 512, D.ortho_full_smem, s_>>>(
                             ctx_, X, D.ortho, D.n_ortho, vstore_, tstore_, trans);
@@ -5124,6 +5621,14 @@ class DeviceFactor : public DeviceFactorBase {
     bool ortho_full_on_ = !(getenv("SPAND_ORTHO_FULL") && atoi(getenv("SPAND_ORTHO_FULL")) == 0);
     // SPAND_TRSV_SMALL=0: the triangular products of small clusters in row tiles as well
     bool trsv_small_on_ = !(getenv("SPAND_TRSV_SMALL") && atoi(getenv("SPAND_TRSV_SMALL")) == 0);
+    // SPAND_TRSM_TC=0: the FP32 panel products on the SIMT kernel
+    bool trsm_tc_on_ = !(getenv("SPAND_TRSM_TC") && atoi(getenv("SPAND_TRSM_TC")) == 0);
+    // SPAND_SCHUR_TC=0: the FP32 Schur updates on the SIMT kernel
+    bool schur_tc_on_ = !(getenv("SPAND_SCHUR_TC") && atoi(getenv("SPAND_SCHUR_TC")) == 0);
+    // SPAND_ORTHO_CLUSTER=0: the Orthogonal op of the large clusters on one CTA each
+    bool ortho_cluster_on_ = !(getenv("SPAND_ORTHO_CLUSTER") && atoi(getenv("SPAND_ORTHO_CLUSTER")) == 0);
+    // SPAND_POTRF_SMALL=0: the pivots of at most 32 rows on the one-CTA kernel as well
+    bool potrf_small_on_ = !(getenv("SPAND_POTRF_SMALL") && atoi(getenv("SPAND_POTRF_SMALL")) == 0);
     // measured QRCP tuning: the factorization after tune_qrcp() times every wave's
     // candidates (SPAND_QC_TUNE=0: the launch model's choice only); the winners are kept per
     // plan fingerprint for the process (trees of the same plan skip the measurement)

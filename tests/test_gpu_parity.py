@@ -410,3 +410,72 @@ def test_relayered_waves(monkeypatch):
     x0, x1, xo = t0.solve(b), t1.solve(b), o.solve(b)
     assert np.linalg.norm(x1 - x0) / np.linalg.norm(x0) < TOL_SOLVE
     assert np.linalg.norm(x1 - xo) / np.linalg.norm(xo) < TOL_SOLVE
+
+
+@pytest.mark.parametrize("n,dim,nlevels", [(64, 2, 7), (32, 3, 8)])
+def test_tensor_cores_fp32(monkeypatch, n, dim, nlevels):
+    """The FP32 panel products and Schur updates on the tensor cores (TF32 head/tail
+    split, FP32 accumulation) against the SIMT kernels.  Without sparsification (every
+    level skipped) the factorization has no pivot decisions, and both FP32 factorizations
+    are compared with the FP64 oracle's: the tensor-core blocks (ScalingLLT and Gemm) and
+    M^{-1}b are within 8x the SIMT kernels' own FP32 error (plus 1e-6) -- a head/tail TF32
+    product carries about 22 of FP32's 24 significand bits (measured: 1-4x).  With sparsification at eps = 1e-2 the two FP32 factorizations
+    may take different (equally valid) QRCP pivots where two column norms sit at the edge
+    of the FP32 tie window, so there the bar is the mixed path's own: CG to 1e-10 within
+    the iteration budget of the FP64 factor."""
+    from spand_public_gb300 import problems as P
+
+    def pair(skip, tol):
+        monkeypatch.setenv("SPAND_TRSM_TC", "0")
+        monkeypatch.setenv("SPAND_SCHUR_TC", "0")
+        A, t0, o = _build(n, dim, nlevels, tol, skip=skip, fp32=True, factorizations=2)
+        monkeypatch.delenv("SPAND_TRSM_TC")
+        monkeypatch.delenv("SPAND_SCHUR_TC")
+        _, t1, _ = _build(n, dim, nlevels, tol, skip=skip, fp32=True, factorizations=2)
+        return A, t0, t1, o
+
+    def rel(a, b):
+        return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+    A, t0, t1, o = pair(nlevels, 1e-2)
+    ops0, ops1, opo = t0.ops(), t1.ops(), o.ops()
+    assert np.array_equal(ops0, ops1)
+    assert np.array_equal(ops0[:, :8], opo[:, :8])
+    e_simt, e_tc = 0.0, 0.0
+    for k in range(ops0.shape[0]):
+        kind, rows, cols = ops0[k, 0], ops0[k, 6], ops0[k, 7]
+        if kind not in (0, 1, 2) or rows * cols == 0:
+            continue
+        a, b, c = t1.op_matrix(k, rows, cols), t0.op_matrix(k, rows, cols), o.op_matrix(k, rows, cols)
+        if kind == 0:
+            a, b, c = np.tril(a), np.tril(b), np.tril(c)
+        e_tc, e_simt = max(e_tc, rel(a, c)), max(e_simt, rel(b, c))
+    assert e_tc <= 8 * e_simt + 1e-6, (e_tc, e_simt)
+    b = P.rhs(A.shape[0], 1, seed=5)[:, 0]
+    x0, x1, xo = t0.solve(b), t1.solve(b), o.solve(b)
+    assert rel(x1, xo) <= 8 * rel(x0, xo) + 1e-6, (rel(x1, xo), rel(x0, xo))
+
+    A, t0, t1, _ = pair(0, 1e-2)
+    _, t64, _ = _build(n, dim, nlevels, 1e-2, factorizations=1)
+    _, it64, _ = t64.cg(b, iters=200, tol=1e-10)
+    x1, it1, _ = t1.cg(b, iters=200, tol=1e-10)
+    assert np.linalg.norm(A @ x1 - b) / np.linalg.norm(b) < 1e-9
+    assert it1 <= max(it64 + 1, int(np.ceil(1.15 * it64))), (it1, it64)
+
+
+@pytest.mark.parametrize("form", [{"SPAND_ORTHO_FULL": "0"}, {"SPAND_ORTHO_CLUSTER": "0"}, {}])
+def test_orthogonal_op_forms(monkeypatch, form):
+    """The one-right-hand-side Orthogonal op in each of its forms (blocked WY, whole-T on one
+    CTA, whole-T on a thread-block cluster for the large clusters; the same for the
+    triangular products with and without the warp kernel): M^{-1}b against the oracle's
+    within 1e-12 relative, 3D (large top-level clusters) and 2D."""
+    from spand_public_gb300 import problems as P
+    for k, v in form.items():
+        monkeypatch.setenv(k, v)
+    if not form:
+        monkeypatch.setenv("SPAND_TRSV_SMALL", "0")
+    for n, dim, nlevels in ((32, 3, 8), (64, 2, 7)):
+        A, t, o = _build(n, dim, nlevels, 1e-2, factorizations=2)
+        b = P.rhs(A.shape[0], 2, seed=9)
+        xt, xo = t.solve(b), o.solve(b)
+        assert np.linalg.norm(xt - xo) / np.linalg.norm(xo) < TOL_SOLVE
