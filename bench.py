@@ -161,14 +161,19 @@ def peaks():
         return 6800.0, 1900.0, "fallback"
 
 
-def ncu_traffic(cls: str):
-    """DRAM bytes per launch of a kernel class from the committed ncu summary, if any."""
+def ncu_traffic(cls: str, bytes_per_launch: float):
+    """DRAM bytes per launch of a kernel class: the DRAM-to-algorithmic byte ratio of its
+    committed ncu capture (profiles/ncu_traffic.json, measured on a smaller case of the same
+    kernel) times this launch's algorithmic bytes, or None without a capture."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     try:
         with open(path) as f:
-            return json.load(f).get(cls)
+            e = json.load(f).get(cls)
     except Exception:
         return None
+    if isinstance(e, dict) and "dram_per_algorithmic" in e:
+        return round(e["dram_per_algorithmic"] * bytes_per_launch)
+    return None
 
 
 # --------------------------------------------------------------------------------------
@@ -370,7 +375,7 @@ def run_gb300(args, rank, world, local_rank):
     dom_launches = prof[dom]["launches"]
     dom_avg_ms = prof[dom]["ms"] / max(dom_launches, 1)
     achieved = (dom_by / max(dom_launches, 1)) / (dom_avg_ms * 1e-3) / 1e9 if dom_avg_ms > 0 else 0.0
-    traffic = ncu_traffic(dom)
+    traffic = ncu_traffic(dom, dom_by / max(dom_launches, 1))
     roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "peak_source": peak_kind,
                 "traffic": traffic, "bytes_per_launch": dom_by / max(dom_launches, 1),

@@ -1779,7 +1779,7 @@ __device__ void larft_offdiag(const T* V, int ldv, int rows, int k, T* Tm, int l
 template <typename T>
 __global__ void __launch_bounds__(256) sparsify_wy_kernel(Ctx<T> c, const DSpars* __restrict__ items,
                                                           const T* vstore, const int* __restrict__ rank_in,
-                                                          const T* taus_ws, T* taustore, T* tstore) {
+                                                          const T* taus_ws, T* taustore, T* tstore, int full_t) {
     if (c.status->not_spd) return;
     const DSpars it = items[blockIdx.x];
     const int rows = c.rows0[it.cluster];
@@ -1790,7 +1790,8 @@ __global__ void __launch_bounds__(256) sparsify_wy_kernel(Ctx<T> c, const DSpars
     extern __shared__ __align__(16) unsigned char lb_raw[];
     T* sm = reinterpret_cast<T*>(lb_raw);
     larft_blocks(vstore + it.v_off, ld, rows, k, taus_ws + it.tau_off, tstore + it.v_off, ld, sm);
-    __syncthreads();  // the diagonal blocks written
+    if (!full_t) return;  // the blocked Orthogonal op needs the diagonal blocks only
+    __syncthreads();      // the diagonal blocks written
     larft_offdiag(vstore + it.v_off, ld, rows, k, tstore + it.v_off, ld, sm);
 }
 
@@ -2201,41 +2202,54 @@ __global__ void __launch_bounds__(32 * TS_WARPS) trsv_small_kernel(Ctx<T> c, XCt
         T sa0 = xa / da, sa1 = T(0), sb0 = xb / db, sb1 = T(0);
         if (!trans) {
             // row i of L^{-1} is read only for rows of the cluster (i < n) and only left of
-            // its diagonal (q < i)
+            // its diagonal (q < i); eight columns at a time, their loads issued together
             const int ea = ia < n ? ia : 0, eb = ib < n ? ib : 0;
             const T* la = L + (size_t)ea * ld;
             const T* lb = L + (size_t)eb * ld;
-            int q = 0;
-            for (; q + 1 < n; q += 2) {
-                const T x0 = __shfl_sync(0xffffffffu, q < 32 ? xa : xb, q & 31);
-                const T x1 = __shfl_sync(0xffffffffu, q + 1 < 32 ? xa : xb, (q + 1) & 31);
-                if (q < ea) sa0 += la[q] * x0;
-                if (q + 1 < ea) sa1 += la[q + 1] * x1;
-                if (q < eb) sb0 += lb[q] * x0;
-                if (q + 1 < eb) sb1 += lb[q + 1] * x1;
-            }
-            if (q < n) {
-                const T x0 = __shfl_sync(0xffffffffu, q < 32 ? xa : xb, q & 31);
-                if (q < ea) sa0 += la[q] * x0;
-                if (q < eb) sb0 += lb[q] * x0;
+            for (int q0 = 0; q0 < n; q0 += 8) {
+                T va[8], vb[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    va[u] = q0 + u < ea ? la[q0 + u] : T(0);
+                    vb[u] = q0 + u < eb ? lb[q0 + u] : T(0);
+                }
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const int q = q0 + u;
+                    const T xq = __shfl_sync(0xffffffffu, q < 32 ? xa : xb, q & 31);
+                    if (u & 1) {
+                        sa1 += va[u] * xq;
+                        sb1 += vb[u] * xq;
+                    } else {
+                        sa0 += va[u] * xq;
+                        sb0 += vb[u] * xq;
+                    }
+                }
             }
         } else {
-            int q = 1;
-            for (; q + 1 < n; q += 2) {
-                const T x0 = __shfl_sync(0xffffffffu, q < 32 ? xa : xb, q & 31);
-                const T x1 = __shfl_sync(0xffffffffu, q + 1 < 32 ? xa : xb, (q + 1) & 31);
-                const T* l0 = L + (size_t)q * ld;
-                const T* l1 = L + (size_t)(q + 1) * ld;
-                if (ia < q) sa0 += l0[ia] * x0;
-                if (ia < q + 1) sa1 += l1[ia] * x1;
-                if (ib < q) sb0 += l0[ib] * x0;
-                if (ib < q + 1) sb1 += l1[ib] * x1;
-            }
-            if (q < n) {
-                const T x0 = __shfl_sync(0xffffffffu, q < 32 ? xa : xb, q & 31);
-                const T* l0 = L + (size_t)q * ld;
-                if (ia < q) sa0 += l0[ia] * x0;
-                if (ib < q) sb0 += l0[ib] * x0;
+            // y_k += sum_{q>k} L^{-1}[q][k] x_q: column q of the block, consecutive lanes on
+            // consecutive entries; eight columns at a time
+            for (int q0 = 1; q0 < n; q0 += 8) {
+                T va[8], vb[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const int q = q0 + u;
+                    const T* lq = L + (size_t)(q < n ? q : 0) * ld;
+                    va[u] = (q < n && ia < q) ? lq[ia] : T(0);
+                    vb[u] = (q < n && ib < q) ? lq[ib] : T(0);
+                }
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const int q = q0 + u;
+                    const T xq = __shfl_sync(0xffffffffu, q < 32 ? xa : xb, q & 31);
+                    if (u & 1) {
+                        sa1 += va[u] * xq;
+                        sb1 += vb[u] * xq;
+                    } else {
+                        sa0 += va[u] * xq;
+                        sb0 += vb[u] * xq;
+                    }
+                }
             }
         }
         if (ia < n) x[ia] = sa0 + sa1;
@@ -2306,6 +2320,8 @@ __global__ void __launch_bounds__(256) gemm_fwd2_kernel(Ctx<T> c, XCtx<T> X, con
             meta[threadIdx.x] = m;
         }
         __syncthreads();
+        // two ops per pass: the second op's loads issue while the first's are in flight
+#pragma unroll 2
         for (int o = 0; o < cnt; o++) {
             const GemmMeta<T> m = meta[o];
             const int ns = m.n;
@@ -2403,6 +2419,8 @@ __global__ void __launch_bounds__(256) gemm_bwd2_kernel(Ctx<T> c, XCtx<T> X, con
             meta[threadIdx.x] = m;
         }
         __syncthreads();
+        // two ops per pass: the second op's loads issue while the first's are in flight
+#pragma unroll 2
         for (int o = 0; o < cnt; o++) {
             const GemmMeta<T> m = meta[o];
             const int nn = m.n;
@@ -2410,30 +2428,37 @@ __global__ void __launch_bounds__(256) gemm_bwd2_kernel(Ctx<T> c, XCtx<T> X, con
             const T* A = m.A;
             const int ld = m.ld;
             if (m.kind == 1) {
-                // A_ns^T x_n: entry i is column i of A_ns
+                // A_ns^T x_n: entry i is column i of A_ns; the warp's entries side by side in
+                // one pass over j (their loads issue together)
+                const T* au[GB_ROWS / 8];
+                bool live[GB_ROWS / 8];
 #pragma unroll
                 for (int u = 0; u < GB_ROWS / 8; u++) {
                     const int ii = w + nw * u;
-                    const int i = i0 + ii;
-                    if (ii < GB_ROWS && i < ns) {
-                        const T* a = A + (size_t)i * ld;
-                        T s = 0;
-                        for (int j = lane; j < nn; j += 32) s += a[j] * xn[j];
-                        wsum[u] += s;
-                    }
+                    live[u] = ii < GB_ROWS && i0 + ii < ns;
+                    au[u] = A + (size_t)(live[u] ? i0 + ii : 0) * ld;
+                }
+                for (int j = lane; j < nn; j += 32) {
+                    const T xj = xn[j];
+#pragma unroll
+                    for (int u = 0; u < GB_ROWS / 8; u++)
+                        if (live[u]) wsum[u] += au[u][j] * xj;
                 }
             } else {
-                // A_sn x_n: a thread per entry, column slices j = sp (mod 8)
+                // A_sn x_n: a thread per entry, column slices j = sp (mod 8), four loads in
+                // flight
                 const int i = i0 + li;
                 if (i < ns) {
-                    T s0 = 0, s1 = 0;
+                    T s0 = 0, s1 = 0, s2 = 0, s3 = 0;
                     int j = sp;
-                    for (; j + 8 < nn; j += 16) {
+                    for (; j + 24 < nn; j += 32) {
                         s0 += A[i + (size_t)j * ld] * xn[j];
                         s1 += A[i + (size_t)(j + 8) * ld] * xn[j + 8];
+                        s2 += A[i + (size_t)(j + 16) * ld] * xn[j + 16];
+                        s3 += A[i + (size_t)(j + 24) * ld] * xn[j + 24];
                     }
                     for (; j < nn; j += 8) s0 += A[i + (size_t)j * ld] * xn[j];
-                    pacc += s0 + s1;
+                    pacc += (s0 + s1) + (s2 + s3);
                 }
             }
         }
@@ -4079,7 +4104,7 @@ class DeviceFactor : public DeviceFactorBase {
                     // the WY factors first: the Q^T application uses them
                     launch("sparsify_wy", [&] {
                         sparsify_wy_kernel<T><<<W.n, 256, larft_smem_elems() * sizeof(T), s_>>>(
-                            ctx_, W.items, vstore_, rank_, tauws_, taustore_, tstore_);
+                            ctx_, W.items, vstore_, rank_, tauws_, taustore_, tstore_, ortho_full_on_ ? 1 : 0);
                     });
                     launch("preserve_apply", [&] {
                         preserve_apply<T>(ctx_, phictx(), W.items, W.n, W.ptiles, pieces_, vstore_, tstore_, rank_, s_);
@@ -4100,7 +4125,7 @@ class DeviceFactor : public DeviceFactorBase {
                     // siblings' elimination: Schur updates between their neighbours
                     launch("sparsify_wy", [&] {
                         sparsify_wy_kernel<T><<<W.n, 256, larft_smem_elems() * sizeof(T), s_>>>(
-                            ctx_, W.items, vstore_, rank_, tauws_, taustore_, tstore_);
+                            ctx_, W.items, vstore_, rank_, tauws_, taustore_, tstore_, ortho_full_on_ ? 1 : 0);
                     });
                     launch("lorasp_split", [&] {
                         lorasp_split<T>(ctx_, W.items, W.n, W.stiles, W.sib, W.orng, lr_splits_, vstore_, tstore_,
@@ -4125,13 +4150,13 @@ class DeviceFactor : public DeviceFactorBase {
                 } else if (prof_.enabled() || check_launches_) {
                     launch("sparsify_wy", [&] {
                         sparsify_wy_kernel<T><<<W.n, 256, larft_smem_elems() * sizeof(T), s_>>>(
-                            ctx_, W.items, vstore_, rank_, tauws_, taustore_, tstore_);
+                            ctx_, W.items, vstore_, rank_, tauws_, taustore_, tstore_, ortho_full_on_ ? 1 : 0);
                     });
                 } else {
                     SPAND_CUDA(cudaEventRecord(ev_fork_, s_));
                     SPAND_CUDA(cudaStreamWaitEvent(s2_, ev_fork_, 0));
                     sparsify_wy_kernel<T><<<W.n, 256, larft_smem_elems() * sizeof(T), s2_>>>(
-                        ctx_, W.items, vstore_, rank_, tauws_, taustore_, tstore_);
+                        ctx_, W.items, vstore_, rank_, tauws_, taustore_, tstore_, ortho_full_on_ ? 1 : 0);
                     launches_ += 1;
                     side_used = true;
                 }
