@@ -60,6 +60,7 @@ struct DOrtho {
 // Status word: first failing cluster + 1 for a non-SPD pivot.
 struct DStatus {
     int not_spd;
+    int overflow;  // a sparsification matrix outgrew its wave's shared-memory QRCP launch
 };
 
 template <typename T>

@@ -265,7 +265,9 @@ __device__ bool chol_inv_smem(T* A, int n, int* bad) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) potrf3_kernel(Ctx<T> c, const int* __restrict__ pivots,
+// FP32: registers capped for three CTAs per SM (24 bytes of spills); FP64 keeps two
+// (its register-resident panels would spill hundreds of bytes)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) potrf3_kernel(Ctx<T> c, const int* __restrict__ pivots,
                                                      const int* __restrict__ clusters, int count, int smem_elems,
                                                      int strip_max_n, const int* __restrict__ only,
                                                      int small_cap = 0) {
@@ -4016,6 +4018,7 @@ class DeviceFactor : public DeviceFactorBase {
 
     void enqueue_factor(double tol) {
         const Plan& P = *P_;
+        gskip_used_ = false;
         // inputs: the assembled blocks (device copy) and the initial cluster sizes
         launch("restore", [&] {
             if (P.assembled_len)
@@ -4113,8 +4116,12 @@ class DeviceFactor : public DeviceFactorBase {
                     cur_wave_ = (int)wi;
                     launch("qrcp", [&] { launch_qrcp_cluster(W, tol); });
                     // matrices larger than the cluster's shared memory: the same algorithm with
-                    // the slabs in global memory (clusters of other matrices exit at once)
-                    launch("qrcp_global", [&] { launch_qrcp_global(W, tol); });
+                    // the slabs in global memory (clusters of other matrices exit at once).
+                    // Not queued where the tuned launch holds every matrix of the wave at the
+                    // sizes it was tuned for; a matrix that outgrew it raises the status's
+                    // overflow flag and the factorization runs again with the pass queued.
+                    if (!W.gskip) launch("qrcp_global", [&] { launch_qrcp_global(W, tol); });
+                    gskip_used_ |= W.gskip;
                     launch("sparsify_scatter", [&] {
                         sparsify_scatter_kernel<T><<<dim3((unsigned)W.n, (unsigned)W.ytiles), 256, 0, s_>>>(
                             ctx_, W.items, pieces_, ws_, ipvt_, rank_, vstore_);
@@ -4192,6 +4199,16 @@ class DeviceFactor : public DeviceFactorBase {
     void factorize_finish() override {
         SPAND_CUDA(cudaStreamSynchronize(s_));
         const DStatus st = *h_status_;
+        if (st.overflow && gskip_used_) {
+            // a matrix outgrew the tuned launch of its wave and its global-memory pass was not
+            // queued: everything after it is void; factor again with every pass queued
+            for (LevelDev& D : levels_)
+                for (WaveDev& W : D.waves) W.gskip = false;
+            drop_factor_graph();
+            factorize_enqueue(last_tol_);
+            factorize_finish();
+            return;
+        }
         failed_cluster_ = st.not_spd - 1;
         if (st.not_spd)
             throw DeviceError{SPAND_ERR_NOT_SPD, std::string(lu_ || ldlt_ ? "Error: Singular Pivot" : "Error: Non-SPD Pivot") +
@@ -4495,6 +4512,7 @@ class DeviceFactor : public DeviceFactorBase {
         int maxcap = 1;
         std::vector<QcConf> cands;  // launch configurations the measuring factorization times
         std::vector<std::pair<QcConf, float>> timed;  // what it measured (ms per candidate)
+        bool gskip = false;  // tuned launch holds every matrix: no global-memory pass queued
         int64_t cols = 0;           // Asn columns of all its matrices (pivot workspace)
         int rpl = 0;         // > 0: the blocked QRCP for up to 32 * rpl rows; 0: the unblocked kernel
         int vec_rows = INT_MAX;  // unblocked kernel: slabs of at least this many rows are vectorised
@@ -5010,6 +5028,7 @@ class DeviceFactor : public DeviceFactorBase {
                 }
             }
         }
+        W.gskip = false;
         if (!bcs) {  // matrices above the cap take the global-memory path
             W.rpl = 0;
             W.vec_rows = INT_MAX;
@@ -5025,6 +5044,8 @@ class DeviceFactor : public DeviceFactorBase {
         W.threads = bth;
         W.cands.clear();
         W.timed.clear();
+        // every candidate holds the matrices at these sizes: the global pass is not queued
+        W.gskip = gskip_on_ && !force_global_;
         if (collect && force_b == 0 && force <= 0 && force_th <= 0 && force_vec < 0) {
             // the measuring factorization times the model's best configurations of each
             // kernel variant (QC_TUNE_PER_KIND each: scalar, blocked, vectorised update; the
@@ -5652,6 +5673,9 @@ class DeviceFactor : public DeviceFactorBase {
     bool schur_tc_on_ = !(getenv("SPAND_SCHUR_TC") && atoi(getenv("SPAND_SCHUR_TC")) == 0);
     // SPAND_ORTHO_CLUSTER=0: the Orthogonal op of the large clusters on one CTA each
     bool ortho_cluster_on_ = !(getenv("SPAND_ORTHO_CLUSTER") && atoi(getenv("SPAND_ORTHO_CLUSTER")) == 0);
+    // SPAND_QC_GLOBAL_PASS=1: queue the global-memory QRCP pass after every wave
+    bool gskip_on_ = !(getenv("SPAND_QC_GLOBAL_PASS") && atoi(getenv("SPAND_QC_GLOBAL_PASS")) == 1);
+    bool gskip_used_ = false;  // the last factorization left a global pass out
     // SPAND_POTRF_SMALL=0: the pivots of at most 32 rows on the one-CTA kernel as well
     bool potrf_small_on_ = !(getenv("SPAND_POTRF_SMALL") && atoi(getenv("SPAND_POTRF_SMALL")) == 0);
     // measured QRCP tuning: the factorization after tune_qrcp() times every wave's

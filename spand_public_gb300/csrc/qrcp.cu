@@ -100,6 +100,7 @@ __global__ void __launch_bounds__(NT) qrcp_cluster_kernel(Ctx<T> c, const DSpars
     const bool spanned = proj.q && r1 >= rows;
     if (!GS && threadIdx.x == 0 && me == 0) {
         fallback[item] = (mn > 0 && tol < 1.0 && !fits && !spanned) ? 1 : 0;
+        if (fallback[item]) atomicOr(&c.status->overflow, 1);
         colcount[item] = cols;
     }
     int* jpg = jpvt_ws + it.col_off;

@@ -92,6 +92,7 @@ __global__ void __launch_bounds__(QC_THREADS) qrcp_blocked_kernel(Ctx<T> c, cons
     const bool fits = rows <= 32 * RPL && qb_need(rows, cols, CS, (int)sizeof(T)) <= smem_bytes;
     if (threadIdx.x == 0 && me == 0) {
         fallback[item] = (mn > 0 && tol < 1.0 && !fits) ? 1 : 0;
+        if (fallback[item]) atomicOr(&c.status->overflow, 1);
         colcount[item] = cols;
     }
     int* jpg = jpvt_ws + it.col_off;

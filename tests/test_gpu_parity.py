@@ -479,3 +479,27 @@ def test_orthogonal_op_forms(monkeypatch, form):
         b = P.rhs(A.shape[0], 2, seed=9)
         xt, xo = t.solve(b), o.solve(b)
         assert np.linalg.norm(xt - xo) / np.linalg.norm(xo) < TOL_SOLVE
+
+
+def test_outgrown_launches_refactor():
+    """A tree tuned at eps = 1e-2 (its waves' global-memory QRCP passes no longer queued)
+    factored at eps = 1e-8: the sparsification matrices outgrow the tuned launches, the
+    device status reports it, and the factorization runs again with every pass queued --
+    ranks and M^{-1}b equal to the oracle's at the new tolerance, then again once re-tuned."""
+    from oracle.oracle import OracleTree
+    from spand_public_gb300 import problems as P
+    A = P.neglapl(16, 3)
+    b = P.rhs(A.shape[0], 2, seed=10)
+    _, t, _ = _build(16, 3, 6, 1e-2, factorizations=3)
+    o = OracleTree(6)
+    o.set_Xcoo(P.linspace_nd(16, 3))
+    o.set_tol(1e-8)
+    o.partition(A)
+    o.assemble(A)
+    o.factorize()
+    t.set_tol(1e-8)
+    for _ in range(3):
+        t.factorize()
+        assert np.array_equal(t.ranks(), o.ranks())
+        xt, xo = t.solve(b), o.solve(b)
+        assert np.linalg.norm(xt - xo) / np.linalg.norm(xo) < TOL_SOLVE
