@@ -103,6 +103,16 @@ __device__ T block_sum(T v, T* red) {
     return s;
 }
 
+// Programmatic dependent launch (the solve sweep's kernels): wait until the previous
+// kernel of the stream has finished and its writes are visible -- a no-op for a kernel
+// launched without the attribute -- then let the next kernel's CTAs be scheduled while
+// this one runs (they wait in their own griddepcontrol.wait).  Called first, before any
+// read of data an earlier kernel wrote.
+__device__ __forceinline__ void pdl_wait_and_release() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 template <typename T>
 __device__ T warp_sum(T v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -2063,6 +2063,7 @@ __global__ void split_x_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ owne
 template <typename T>
 __global__ void perm_in_kernel(const double* __restrict__ x, int ldx, XCtx<T> X, const int* __restrict__ perm,
                                const long long* __restrict__ slot, int n) {
+    pdl_wait_and_release();
     long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (k >= (long long)n * X.nrhs) return;
     int p = (int)(k % n), r = (int)(k / n);
@@ -2072,6 +2073,7 @@ __global__ void perm_in_kernel(const double* __restrict__ x, int ldx, XCtx<T> X,
 template <typename T>
 __global__ void perm_out_kernel(double* __restrict__ x, int ldx, XCtx<T> X, const int* __restrict__ perm,
                                 const long long* __restrict__ slot, int n) {
+    pdl_wait_and_release();
     long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (k >= (long long)n * X.nrhs) return;
     int p = (int)(k % n), r = (int)(k / n);
@@ -2096,6 +2098,7 @@ __global__ void __launch_bounds__(TV_THREADS) trsv4_kernel(Ctx<T> c, XCtx<T> X, 
                                                           const int* __restrict__ lblocks,
                                                           const int2* __restrict__ tiles, int trans, T* tmp,
                                                           int* counters) {
+    pdl_wait_and_release();
     const int2 tl = tiles[blockIdx.x];
     const int item = tl.x, tile = tl.y;
     const int cl = clusters[item];
@@ -2185,6 +2188,7 @@ __global__ void __launch_bounds__(32 * TS_WARPS) trsv_small_kernel(Ctx<T> c, XCt
                                                                    const int* __restrict__ clusters,
                                                                    const int* __restrict__ lblocks,
                                                                    const int* __restrict__ idx, int count, int trans) {
+    pdl_wait_and_release();
     const int lane = threadIdx.x & 31;
     const int item = blockIdx.x * TS_WARPS + (threadIdx.x >> 5);
     if (item >= count) return;
@@ -2287,6 +2291,7 @@ __global__ void __launch_bounds__(256) gemm_fwd2_kernel(Ctx<T> c, XCtx<T> X, con
                                                         int ntiles, int rhs_stride, const T* __restrict__ signs = nullptr,
                                                         const long long* __restrict__ soff = nullptr,
                                                         int sib_mode = 0) {
+    pdl_wait_and_release();
     const int t = blockIdx.x % ntiles;
     const int r = blockIdx.x / ntiles;
     const DGroup G = groups[tiles[t].item];
@@ -2389,6 +2394,7 @@ __global__ void __launch_bounds__(256) gemm_bwd2_kernel(Ctx<T> c, XCtx<T> X, con
                                                         int ntiles, const T* __restrict__ signs = nullptr,
                                                         const long long* __restrict__ soff = nullptr,
                                                         int sib_mode = 0) {
+    pdl_wait_and_release();
     const int t = blockIdx.x % ntiles;
     const int r = blockIdx.x / ntiles;
     const DGroup G = groups[tiles[t].item];
@@ -2493,6 +2499,7 @@ template <typename T>
 __global__ void __launch_bounds__(512) ortho_wyb_kernel(Ctx<T> c, XCtx<T> X, const DOrtho* __restrict__ items,
                                                         int count, const T* vstore, const T* tstore, int trans,
                                                         int smem_elems) {
+    pdl_wait_and_release();
     const int item = blockIdx.x % count;
     const int r = blockIdx.x / count;
     const DOrtho it = items[item];
@@ -2583,6 +2590,7 @@ template <typename T, int NT>
 __global__ void __launch_bounds__(NT) ortho_full_kernel(Ctx<T> c, XCtx<T> X, const DOrtho* __restrict__ items,
                                                         int count, const T* __restrict__ vstore,
                                                         const T* __restrict__ tstore, int trans) {
+    pdl_wait_and_release();
     const int item = blockIdx.x % count;
     const int r = blockIdx.x / count;
     const DOrtho it = items[item];
@@ -2684,6 +2692,7 @@ template <typename T, int NT>
 __global__ void __launch_bounds__(NT) ortho_cluster_kernel(Ctx<T> c, XCtx<T> X, const DOrtho* __restrict__ items,
                                                            int count, const T* __restrict__ vstore,
                                                            const T* __restrict__ tstore, int trans) {
+    pdl_wait_and_release();
     namespace cgx = cooperative_groups;
     cgx::cluster_group cl = cgx::this_cluster();
     const int CS = (int)cl.num_blocks(), me = (int)cl.block_rank();
@@ -2817,6 +2826,7 @@ __global__ void __launch_bounds__(NT) ortho_cluster_kernel(Ctx<T> c, XCtx<T> X, 
 template <typename T>
 __global__ void merge_x_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ children, const int* __restrict__ parent_of,
                                int nchildren, const int* __restrict__ cpos, int fwd) {
+    pdl_wait_and_release();
     // a warp per (child, right-hand side)
     const int pair = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (pair >= nchildren * X.nrhs) return;
@@ -5283,6 +5293,35 @@ class DeviceFactor : public DeviceFactorBase {
         if (mx * (int64_t)sizeof(T) > 200 * 1024) throw DeviceError{SPAND_ERR_UNSUPPORTED, "pivot too large"};
         return (int)(mx * sizeof(T));
     }
+    // A kernel of the one-right-hand-side solve sweep, launched as a programmatic dependent of
+    // the previous one (its CTAs are scheduled while that one still runs and wait in
+    // pdl_wait_and_release for its completion): the sweep's ~130 dependent launches overlap
+    // their launch latency.  Off while the profiler times every launch or SPAND_PDL=0.
+    template <typename... KArgs, typename... Args>
+    void launch_sweep(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, int cluster, Args&&... args) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = grid;
+        cfg.blockDim = block;
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = s_;
+        cudaLaunchAttribute attr[2];
+        int na = 0;
+        if (cluster > 1) {
+            attr[na].id = cudaLaunchAttributeClusterDimension;
+            attr[na].val.clusterDim.x = (unsigned)cluster;
+            attr[na].val.clusterDim.y = 1;
+            attr[na].val.clusterDim.z = 1;
+            na++;
+        }
+        if (pdl_on_ && !prof_.enabled() && !check_launches_) {
+            attr[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            attr[na].val.programmaticStreamSerializationAllowed = 1;
+            na++;
+        }
+        cfg.attrs = attr;
+        cfg.numAttrs = na;
+        SPAND_CUDA(cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...));
+    }
     void launch_schur(const DTarget* targets, const DUpd* ups, const DTile* tiles, int ntiles) {
         if (!ntiles) return;
         if constexpr (sizeof(T) == 4) {
@@ -5447,7 +5486,8 @@ class DeviceFactor : public DeviceFactorBase {
             }
         };
         launch("perm", [&] {
-            perm_in_kernel<T><<<(unsigned)((tot + 255) / 256), 256, 0, s_>>>(x, ld, X, d_perm_, d_slot_, n);
+            launch_sweep(perm_in_kernel<T>, dim3((unsigned)((tot + 255) / 256)), dim3(256), 0, 1, (const double*)x, ld, X,
+                         (const int*)d_perm_, (const long long*)d_slot_, n);
         });
         auto trsv_mr = [&](const int* clusters, const int* blks, const int* small, int nsmall, const int2* big, int nbig,
                            int trans) {
@@ -5494,13 +5534,13 @@ class DeviceFactor : public DeviceFactorBase {
                     const int nbig = elim ? D.n_elim_big_tv : D.n_scale_big_tv;
                     if (nsmall)
                         launch("trsv", [&] {
-                            trsv_small_kernel<T><<<(nsmall + TS_WARPS - 1) / TS_WARPS, 32 * TS_WARPS, 0, s_>>>(
-                                ctx_, X, clusters, blks, small, nsmall, trans);
+                            launch_sweep(trsv_small_kernel<T>, dim3((nsmall + TS_WARPS - 1) / TS_WARPS),
+                                         dim3(32 * TS_WARPS), 0, 1, ctx_, X, clusters, blks, small, nsmall, trans);
                         });
                     if (nbig)
                         launch("trsv", [&] {
-                            trsv4_kernel<T><<<nbig, TV_THREADS, smem, s_>>>(ctx_, X, clusters, blks, big, trans, tmp,
-                                                                            tv_count_);
+                            launch_sweep(trsv4_kernel<T>, dim3(nbig), dim3(TV_THREADS), (size_t)smem, 1, ctx_, X,
+                                         clusters, blks, big, trans, tmp, tv_count_);
                         });
                     return;
                 }
@@ -5509,7 +5549,8 @@ class DeviceFactor : public DeviceFactorBase {
                 if (mr)
                     trsv_mrhs_kernel<T><<<ntv, 256, 0, s_>>>(ctx_, X, clusters, blks, tv, trans, tmp, tv_count_);
                 else
-                    trsv4_kernel<T><<<ntv, TV_THREADS, smem, s_>>>(ctx_, X, clusters, blks, tv, trans, tmp, tv_count_);
+                    launch_sweep(trsv4_kernel<T>, dim3(ntv), dim3(TV_THREADS), (size_t)smem, 1, ctx_, X, clusters, blks,
+                                 tv, trans, tmp, tv_count_);
             });
         };
         auto ortho = [&](const LevelDev& D, int trans) {
@@ -5518,31 +5559,23 @@ class DeviceFactor : public DeviceFactorBase {
                 if (mr && D.ortho_mrhs_smem)
                     ortho_mrhs_kernel<T><<<D.n_ortho, 256, D.ortho_mrhs_smem, s_>>>(ctx_, X, D.ortho, vstore_, tstore_,
                                                                                     trans);
-                else if (D.ortho_cs > 1 && ortho_full_on_ && ortho_cluster_on_) {
-                    cudaLaunchConfig_t cfg = {};
-                    cfg.gridDim = dim3((unsigned)(D.n_ortho * nrhs * D.ortho_cs));
-                    cfg.blockDim = dim3(256);
-                    cfg.dynamicSmemBytes = (size_t)D.ortho_cs_smem;
-                    cfg.stream = s_;
-                    cudaLaunchAttribute attr[1];
-                    attr[0].id = cudaLaunchAttributeClusterDimension;
-                    attr[0].val.clusterDim.x = (unsigned)D.ortho_cs;
-                    attr[0].val.clusterDim.y = 1;
-                    attr[0].val.clusterDim.z = 1;
-                    cfg.attrs = attr;
-                    cfg.numAttrs = 1;
-                    SPAND_CUDA(cudaLaunchKernelEx(&cfg, ortho_cluster_kernel<T, 256>, ctx_, X, (const DOrtho*)D.ortho,
-                                                  D.n_ortho, (const T*)vstore_, (const T*)tstore_, trans));
-                } else if (D.ortho_full_smem && ortho_full_on_) {
+                else if (D.ortho_cs > 1 && ortho_full_on_ && ortho_cluster_on_)
+                    launch_sweep(ortho_cluster_kernel<T, 256>, dim3((unsigned)(D.n_ortho * nrhs * D.ortho_cs)), dim3(256),
+                                 (size_t)D.ortho_cs_smem, D.ortho_cs, ctx_, X, (const DOrtho*)D.ortho, D.n_ortho,
+                                 (const T*)vstore_, (const T*)tstore_, trans);
+                else if (D.ortho_full_smem && ortho_full_on_) {
                     if (D.ortho_full_wide)
-                        ortho_full_kernel<T, 512><<<D.n_ortho * nrhs, 512, D.ortho_full_smem, s_>>>(
-                            ctx_, X, D.ortho, D.n_ortho, vstore_, tstore_, trans);
+                        launch_sweep(ortho_full_kernel<T, 512>, dim3(D.n_ortho * nrhs), dim3(512),
+                                     (size_t)D.ortho_full_smem, 1, ctx_, X, (const DOrtho*)D.ortho, D.n_ortho,
+                                     (const T*)vstore_, (const T*)tstore_, trans);
                     else
-                        ortho_full_kernel<T, 256><<<D.n_ortho * nrhs, 256, D.ortho_full_smem, s_>>>(
-                            ctx_, X, D.ortho, D.n_ortho, vstore_, tstore_, trans);
+                        launch_sweep(ortho_full_kernel<T, 256>, dim3(D.n_ortho * nrhs), dim3(256),
+                                     (size_t)D.ortho_full_smem, 1, ctx_, X, (const DOrtho*)D.ortho, D.n_ortho,
+                                     (const T*)vstore_, (const T*)tstore_, trans);
                 } else
-                    ortho_wyb_kernel<T><<<D.n_ortho * nrhs, 512, D.x_smem_ortho, s_>>>(
-                        ctx_, X, D.ortho, D.n_ortho, vstore_, tstore_, trans, D.x_smem_ortho / (int)sizeof(T));
+                    launch_sweep(ortho_wyb_kernel<T>, dim3(D.n_ortho * nrhs), dim3(512), (size_t)D.x_smem_ortho, 1,
+                                 ctx_, X, (const DOrtho*)D.ortho, D.n_ortho, (const T*)vstore_, (const T*)tstore_,
+                                 trans, D.x_smem_ortho / (int)sizeof(T));
             });
         };
         auto merge = [&](const LevelDev& D, int fwd) {
@@ -5551,9 +5584,9 @@ class DeviceFactor : public DeviceFactorBase {
                 if (mr)
                     merge_x_mrhs_kernel<T><<<D.n_children, 256, 0, s_>>>(ctx_, X, D.child_idx, D.child_parent, cpos_, fwd);
                 else
-                    merge_x_kernel<T><<<(D.n_children * nrhs + 7) / 8, 256, 0, s_>>>(ctx_, X, D.child_idx,
-                                                                                     D.child_parent, D.n_children,
-                                                                                     cpos_, fwd);
+                    launch_sweep(merge_x_kernel<T>, dim3((D.n_children * nrhs + 7) / 8), dim3(256), 0, 1, ctx_, X,
+                                 (const int*)D.child_idx, (const int*)D.child_parent, D.n_children,
+                                 (const int*)cpos_, fwd);
             });
         };
         for (int l = 0; l < P.nlevels; l++) {
@@ -5567,8 +5600,9 @@ class DeviceFactor : public DeviceFactorBase {
                     if (mr)
                         gemm_mrhs_kernel<T><<<D.n_gf_tiles32, 256, 0, s_>>>(ctx_, X, D.gf, D.gfo, D.gf_tiles32, 1);
                     else
-                        gemm_fwd2_kernel<T><<<D.n_gf_tiles * nrhs, 256, 0, s_>>>(ctx_, X, D.gf, D.gfo, D.gf_tiles,
-                                                                                 D.n_gf_tiles, 0, sg, d_xoff_);
+                        launch_sweep(gemm_fwd2_kernel<T>, dim3(D.n_gf_tiles * nrhs), dim3(256), 0, 1, ctx_, X,
+                                     (const DGroup*)D.gf, (const DGemmOp*)D.gfo, (const DTile*)D.gf_tiles,
+                                     D.n_gf_tiles, 0, sg, (const long long*)d_xoff_, 0);
                 });
             cur_count_ = D.n_scale_llt;
             permx(D.scale_llt, D.n_scale_llt, 1, D.x_smem_scale);
@@ -5597,8 +5631,9 @@ class DeviceFactor : public DeviceFactorBase {
                     if (mr)
                         gemm_mrhs_kernel<T><<<D.n_gb_tiles, 256, 0, s_>>>(ctx_, X, D.gb, D.gbo, D.gb_tiles, 0);
                     else
-                        gemm_bwd2_kernel<T><<<D.n_gb_tiles * nrhs, 256, 0, s_>>>(ctx_, X, D.gb, D.gbo, D.gb_tiles,
-                                                                                 D.n_gb_tiles, sg, d_xoff_);
+                        launch_sweep(gemm_bwd2_kernel<T>, dim3(D.n_gb_tiles * nrhs), dim3(256), 0, 1, ctx_, X,
+                                     (const DGroup*)D.gb, (const DGemmOp*)D.gbo, (const DTile*)D.gb_tiles,
+                                     D.n_gb_tiles, sg, (const long long*)d_xoff_, 0);
                 });
             cur_count_ = D.n_elim_llt;
             trsv(D.elim_llt, lu_ ? D.elim_inv : D.elim_llt_blk, D.elim_tv, D.n_elim_tv, D.x_smem_elim, 1);
@@ -5606,7 +5641,8 @@ class DeviceFactor : public DeviceFactorBase {
         }
         cur_level_ = -1;
         launch("perm", [&] {
-            perm_out_kernel<T><<<(unsigned)((tot + 255) / 256), 256, 0, s_>>>(x, ld, X, d_perm_, d_slot_, n);
+            launch_sweep(perm_out_kernel<T>, dim3((unsigned)((tot + 255) / 256)), dim3(256), 0, 1, x, ld, X,
+                         (const int*)d_perm_, (const long long*)d_slot_, n);
         });
         SPAND_CUDA(cudaGetLastError());
     }
@@ -5676,6 +5712,8 @@ class DeviceFactor : public DeviceFactorBase {
     // SPAND_QC_GLOBAL_PASS=1: queue the global-memory QRCP pass after every wave
     bool gskip_on_ = !(getenv("SPAND_QC_GLOBAL_PASS") && atoi(getenv("SPAND_QC_GLOBAL_PASS")) == 1);
     bool gskip_used_ = false;  // the last factorization left a global pass out
+    // SPAND_PDL=0: the solve sweep's kernels launched without programmatic dependence
+    bool pdl_on_ = !(getenv("SPAND_PDL") && atoi(getenv("SPAND_PDL")) == 0);
     // SPAND_POTRF_SMALL=0: the pivots of at most 32 rows on the one-CTA kernel as well
     bool potrf_small_on_ = !(getenv("SPAND_POTRF_SMALL") && atoi(getenv("SPAND_POTRF_SMALL")) == 0);
     // measured QRCP tuning: the factorization after tune_qrcp() times every wave's
