@@ -271,6 +271,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) potrf3_kernel(Ctx
                                                      const int* __restrict__ clusters, int count, int smem_elems,
                                                      int strip_max_n, const int* __restrict__ only,
                                                      int small_cap = 0) {
+    pdl_wait_and_release();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
     const int item = blockIdx.x;
@@ -319,6 +320,7 @@ constexpr int PS_WARPS = 8;
 template <typename T>
 __global__ void __launch_bounds__(32 * PS_WARPS) potrf_small_kernel(Ctx<T> c, const int* __restrict__ pivots,
                                                                    const int* __restrict__ clusters, int count) {
+    pdl_wait_and_release();
     const int lane = threadIdx.x & 31;
     const int k = blockIdx.x * PS_WARPS + (threadIdx.x >> 5);
     if (k >= count) return;
@@ -402,6 +404,7 @@ template <typename T>
 __global__ void __launch_bounds__(PC_THREADS) potrf_cluster_kernel(Ctx<T> c, const int* __restrict__ pivots,
                                                                    const int* __restrict__ clusters, int count,
                                                                    int smem_bytes, int* fallback) {
+    pdl_wait_and_release();
     namespace cgx = cooperative_groups;
     cgx::cluster_group cl = cgx::this_cluster();
     const int CS = (int)cl.num_blocks(), me = (int)cl.block_rank();
@@ -603,6 +606,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) trtri_kernel(Ctx<T> c, const int* __restrict__ pivots,
                                                     const int* __restrict__ clusters, const DTile* __restrict__ tiles,
                                                     int ntiles, int smem_elems, long long skip_n2) {
+    pdl_wait_and_release();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* Y = reinterpret_cast<T*>(smem_raw);  // Y[i + jj * n], rows i >= jb
     const int t = blockIdx.x;
@@ -708,6 +712,7 @@ __global__ void __launch_bounds__(256) trsm3_kernel(Ctx<T> c, const DTrsm* __res
                                                    const DTile* __restrict__ tiles, int ntiles, int smem_elems,
                                                    const int* __restrict__ perm_store = nullptr,
                                                    const long long* __restrict__ poff = nullptr) {
+    pdl_wait_and_release();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* X = reinterpret_cast<T*>(smem_raw);
     const int t = blockIdx.x;
@@ -811,6 +816,7 @@ __device__ __forceinline__ void mma_tf32_16x8x8(float (&d)[4], const uint32_t (&
 
 __global__ void __launch_bounds__(256) trsm_tc_kernel(Ctx<float> c, const DTrsm* __restrict__ items,
                                                       const DTile* __restrict__ tiles, int ntiles) {
+    pdl_wait_and_release();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* X = reinterpret_cast<float*>(smem_raw);
     const int t = blockIdx.x;
@@ -1440,6 +1446,7 @@ __global__ void __launch_bounds__(256) schur_kernel(Ctx<T> c, const DTarget* __r
                                                      const DUpd* __restrict__ ups, const DTile* __restrict__ tiles,
                                                      int ntiles, const T* __restrict__ signs = nullptr,
                                                      const long long* __restrict__ soff = nullptr) {
+    pdl_wait_and_release();
     const int t = blockIdx.x;
     if (t >= ntiles || c.status->not_spd) return;
     const DTarget tg = targets[tiles[t].item];
@@ -1522,6 +1529,7 @@ __global__ void __launch_bounds__(256) schur_tc_kernel(Ctx<float> c, const DTarg
                                                        const DUpd* __restrict__ ups, const DTile* __restrict__ tiles,
                                                        int ntiles, const float* __restrict__ signs = nullptr,
                                                        const long long* __restrict__ soff = nullptr) {
+    pdl_wait_and_release();
     const int t = blockIdx.x;
     if (t >= ntiles || c.status->not_spd) return;
     const DTarget tg = targets[tiles[t].item];
@@ -1808,6 +1816,7 @@ __global__ void __launch_bounds__(256) sparsify_scatter_kernel(Ctx<T> c, const D
                                                                const DAsn* __restrict__ pieces, const T* ws,
                                                                const int* __restrict__ ipvt_ws,
                                                                const int* __restrict__ rank_in, T* vstore) {
+    pdl_wait_and_release();
     __shared__ T tile[32][33];
     __shared__ int qs[32];
     if (c.status->not_spd) return;
@@ -1877,6 +1886,7 @@ __global__ void __launch_bounds__(256) sparsify_scatter_kernel(Ctx<T> c, const D
 // ------------------------------------------------------------------------------------
 __global__ void merge_sizes_kernel(int* csize, int* rows0, int* cpos, const int* __restrict__ parents, int np,
                                    const int* __restrict__ child_ptr, const int* __restrict__ child_idx) {
+    pdl_wait_and_release();
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= np) return;
     int pos = 0;
@@ -1894,6 +1904,7 @@ constexpr int MT = 32;
 template <typename T>
 __global__ void merge_copy_kernel(Ctx<T> c, const DMerge* __restrict__ items, const DTile* __restrict__ tiles,
                                   int ntiles, const int* __restrict__ cpos) {
+    pdl_wait_and_release();
     const int t = blockIdx.x;
     if (t >= ntiles || c.status->not_spd) return;
     const DMerge m = items[tiles[t].item];
@@ -1948,6 +1959,7 @@ __global__ void identity_kernel(Ctx<T> c, const int* __restrict__ blocks, const 
 }
 
 __global__ void snapshot_kernel(const int* csize, int* rows0, const int* __restrict__ clusters, int n) {
+    pdl_wait_and_release();
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n) rows0[clusters[k]] = csize[clusters[k]];
 }
@@ -4095,8 +4107,8 @@ class DeviceFactor : public DeviceFactorBase {
             }
             if (D.n_level)
                 launch("snapshot", [&] {
-                    snapshot_kernel<<<(D.n_level + 255) / 256, 256, 0, s_>>>(csize_, rows0_, D.level_clusters,
-                                                                             D.n_level);
+                    launch_pdl(snapshot_kernel, dim3((D.n_level + 255) / 256), dim3(256), 0, 1, (const int*)csize_,
+                               rows0_, (const int*)D.level_clusters, D.n_level);
                 });
             for (size_t wi = 0; wi < D.waves.size(); wi++) {
                 WaveDev& W = D.waves[wi];
@@ -4133,8 +4145,9 @@ class DeviceFactor : public DeviceFactorBase {
                     if (!W.gskip) launch("qrcp_global", [&] { launch_qrcp_global(W, tol); });
                     gskip_used_ |= W.gskip;
                     launch("sparsify_scatter", [&] {
-                        sparsify_scatter_kernel<T><<<dim3((unsigned)W.n, (unsigned)W.ytiles), 256, 0, s_>>>(
-                            ctx_, W.items, pieces_, ws_, ipvt_, rank_, vstore_);
+                        launch_pdl(sparsify_scatter_kernel<T>, dim3((unsigned)W.n, (unsigned)W.ytiles), dim3(256), 0, 1,
+                                   ctx_, (const DSpars*)W.items, (const DAsn*)pieces_, (const T*)ws_,
+                                   (const int*)ipvt_, (const int*)rank_, vstore_);
                     });
                 }
                 if (lorasp_) {
@@ -4180,14 +4193,15 @@ class DeviceFactor : public DeviceFactorBase {
             }
             if (D.merged && D.n_parents) {
                 launch("merge_sizes", [&] {
-                    merge_sizes_kernel<<<(D.n_parents + 127) / 128, 128, 0, s_>>>(csize_, rows0_, cpos_, D.parents,
-                                                                                    D.n_parents, D.child_ptr,
-                                                                                    D.child_idx);
+                    launch_pdl(merge_sizes_kernel, dim3((D.n_parents + 127) / 128), dim3(128), 0, 1, csize_, rows0_,
+                               cpos_, (const int*)D.parents, D.n_parents, (const int*)D.child_ptr,
+                               (const int*)D.child_idx);
                 });
                 if (D.n_merge_tiles)
                     launch("merge_copy", [&] {
-                        merge_copy_kernel<T><<<D.n_merge_tiles, 256, 0, s_>>>(ctx_, D.merge_items, D.merge_tiles,
-                                                                              D.n_merge_tiles, cpos_);
+                        launch_pdl(merge_copy_kernel<T>, dim3(D.n_merge_tiles), dim3(256), 0, 1, ctx_,
+                                   (const DMerge*)D.merge_items, (const DTile*)D.merge_tiles, D.n_merge_tiles,
+                                   (const int*)cpos_);
                     });
                 if (nphi_)
                     launch("preserve_merge", [&] {
@@ -5202,13 +5216,20 @@ class DeviceFactor : public DeviceFactorBase {
         cfg.blockDim = dim3((unsigned)W.threads);
         cfg.dynamicSmemBytes = force_global_ ? 0 : (size_t)W.smem;
         cfg.stream = s_;
-        cudaLaunchAttribute attr[1];
+        cudaLaunchAttribute attr[2];
         attr[0].id = cudaLaunchAttributeClusterDimension;
         attr[0].val.clusterDim.x = (unsigned)W.cs;
         attr[0].val.clusterDim.y = 1;
         attr[0].val.clusterDim.z = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
+        // a programmatic dependent of the previous launch (as launch_pdl) when the blocked
+        // kernel, whose body does not wait, is not the one launched
+        if (pdl_on_ && !prof_.enabled() && !check_launches_ && !measuring_ && !(W.rpl > 0 && !force_global_)) {
+            attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            attr[1].val.programmaticStreamSerializationAllowed = 1;
+            cfg.numAttrs = 2;
+        }
         const QcKernel<T> fn =
             W.rpl > 0 && !force_global_ ? qrcp_blocked_kernel_ptr<T>(W.rpl) : qrcp_smem_kernel_ptr<T>(W.threads);
         SPAND_CUDA(cudaLaunchKernelEx(&cfg, fn, ctx_, (const DSpars*)W.items, (const DAsn*)pieces_, ws_, (T*)nullptr,
@@ -5221,25 +5242,13 @@ class DeviceFactor : public DeviceFactorBase {
         const bool small = n_ps > 0 && potrf_small_on_ && pc_cs == 0 && smem > 0;
         if (small)
             launch("potrf", [&] {
-                potrf_small_kernel<T><<<(n_ps + PS_WARPS - 1) / PS_WARPS, 32 * PS_WARPS, 0, s_>>>(ctx_, ps_piv, ps_cl,
-                                                                                              n_ps);
+                launch_pdl(potrf_small_kernel<T>, dim3((n_ps + PS_WARPS - 1) / PS_WARPS), dim3(32 * PS_WARPS), 0, 1,
+                           ctx_, ps_piv, ps_cl, n_ps);
             });
         if (pc_cs > 0) {
             launch("potrf_cluster", [&] {
-                cudaLaunchConfig_t cfg = {};
-                cfg.gridDim = dim3((unsigned)(n * pc_cs));
-                cfg.blockDim = dim3(PC_THREADS);
-                cfg.dynamicSmemBytes = (size_t)pc_smem;
-                cfg.stream = s_;
-                cudaLaunchAttribute attr[1];
-                attr[0].id = cudaLaunchAttributeClusterDimension;
-                attr[0].val.clusterDim.x = (unsigned)pc_cs;
-                attr[0].val.clusterDim.y = 1;
-                attr[0].val.clusterDim.z = 1;
-                cfg.attrs = attr;
-                cfg.numAttrs = 1;
-                SPAND_CUDA(cudaLaunchKernelEx(&cfg, potrf_cluster_kernel<T>, ctx_, (const int*)pivots,
-                                              (const int*)clusters, n, pc_smem, pc_fallback_));
+                launch_pdl(potrf_cluster_kernel<T>, dim3((unsigned)(n * pc_cs)), dim3(PC_THREADS), (size_t)pc_smem,
+                           pc_cs, ctx_, (const int*)pivots, (const int*)clusters, n, pc_smem, pc_fallback_);
             });
         }
         // The strip-wise inverse runs only where pivots may miss the single-CTA kernel's shared
@@ -5247,15 +5256,15 @@ class DeviceFactor : public DeviceFactorBase {
         const bool strips = tri.ntiles > 0 && (smem == 0 || pc_cs > 0);
         // single-CTA kernel: every pivot, or (after the cluster kernel) those it could not hold
         launch("potrf", [&] {
-            potrf3_kernel<T><<<n, 256, smem, s_>>>(ctx_, pivots, clusters, n, smem / (int)sizeof(T),
-                                                   strips ? tri.smem / (32 * (int)sizeof(T)) : 0,
-                                                   pc_cs > 0 ? (const int*)pc_fallback_ : nullptr, small ? 32 : 0);
+            launch_pdl(potrf3_kernel<T>, dim3(n), dim3(256), (size_t)smem, 1, ctx_, (const int*)pivots,
+                       (const int*)clusters, n, smem / (int)sizeof(T), strips ? tri.smem / (32 * (int)sizeof(T)) : 0,
+                       pc_cs > 0 ? (const int*)pc_fallback_ : nullptr, small ? 32 : 0);
         });
         if (strips)
             launch("trtri", [&] {
-                trtri_kernel<T><<<tri.ntiles, 256, tri.smem, s_>>>(ctx_, pivots, clusters, tri.tiles, tri.ntiles,
-                                                                   tri.smem / (int)sizeof(T),
-                                                                   pc_cs > 0 ? 0LL : (long long)(smem / (int)sizeof(T)));
+                launch_pdl(trtri_kernel<T>, dim3(tri.ntiles), dim3(256), (size_t)tri.smem, 1, ctx_, (const int*)pivots,
+                           (const int*)clusters, (const DTile*)tri.tiles, tri.ntiles, tri.smem / (int)sizeof(T),
+                           pc_cs > 0 ? 0LL : (long long)(smem / (int)sizeof(T)));
             });
     }
     void launch_getrf(int* pivots, int* invs, int* clusters, int n, int smem) {
@@ -5293,12 +5302,13 @@ class DeviceFactor : public DeviceFactorBase {
         if (mx * (int64_t)sizeof(T) > 200 * 1024) throw DeviceError{SPAND_ERR_UNSUPPORTED, "pivot too large"};
         return (int)(mx * sizeof(T));
     }
-    // A kernel of the one-right-hand-side solve sweep, launched as a programmatic dependent of
-    // the previous one (its CTAs are scheduled while that one still runs and wait in
-    // pdl_wait_and_release for its completion): the sweep's ~130 dependent launches overlap
-    // their launch latency.  Off while the profiler times every launch or SPAND_PDL=0.
+    // A kernel of the factorization's main stream or of the one-right-hand-side solve sweep,
+    // launched as a programmatic dependent of the previous one (its CTAs are scheduled while
+    // that one still runs and wait in pdl_wait_and_release for its completion): chains of
+    // hundreds of dependent launches overlap their launch latency.  Off while the profiler
+    // or the measuring factorization times launches one by one, and with SPAND_PDL=0.
     template <typename... KArgs, typename... Args>
-    void launch_sweep(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, int cluster, Args&&... args) {
+    void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, int cluster, Args&&... args) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = grid;
         cfg.blockDim = block;
@@ -5313,7 +5323,7 @@ class DeviceFactor : public DeviceFactorBase {
             attr[na].val.clusterDim.z = 1;
             na++;
         }
-        if (pdl_on_ && !prof_.enabled() && !check_launches_) {
+        if (pdl_on_ && !prof_.enabled() && !check_launches_ && !measuring_) {
             attr[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
             attr[na].val.programmaticStreamSerializationAllowed = 1;
             na++;
@@ -5327,13 +5337,15 @@ class DeviceFactor : public DeviceFactorBase {
         if constexpr (sizeof(T) == 4) {
             if (schur_tc_on_) {
                 launch("schur", [&] {
-                    schur_tc_kernel<<<ntiles, 256, 0, s_>>>(ctx_, targets, ups, tiles, ntiles, signs_, d_xoff_);
+                    launch_pdl(schur_tc_kernel, dim3(ntiles), dim3(256), 0, 1, ctx_, targets, ups, tiles, ntiles,
+                               (const float*)signs_, (const long long*)d_xoff_);
                 });
                 return;
             }
         }
         launch("schur", [&] {
-            schur_kernel<T><<<ntiles, 256, 0, s_>>>(ctx_, targets, ups, tiles, ntiles, signs_, d_xoff_);
+            launch_pdl(schur_kernel<T>, dim3(ntiles), dim3(256), 0, 1, ctx_, targets, ups, tiles, ntiles,
+                       (const T*)signs_, (const long long*)d_xoff_);
         });
     }
     void launch_trsm(const TrsmDev& t) {
@@ -5344,14 +5356,16 @@ class DeviceFactor : public DeviceFactorBase {
             const int64_t tcs = (int64_t)TC_XLD * ((nmax + 7) & ~7) * (int64_t)sizeof(float);
             if (trsm_tc_on_ && !ldlt_ && t.smem > 16 && tcs <= 200 * 1024) {
                 launch("trsm", [&] {
-                    trsm_tc_kernel<<<t.ntiles, 256, (size_t)tcs, s_>>>(ctx_, t.items, t.tiles, t.ntiles);
+                    launch_pdl(trsm_tc_kernel, dim3(t.ntiles), dim3(256), (size_t)tcs, 1, ctx_, (const DTrsm*)t.items,
+                               (const DTile*)t.tiles, t.ntiles);
                 });
                 return;
             }
         }
         launch("trsm", [&] {
-            trsm3_kernel<T><<<t.ntiles, 256, t.smem, s_>>>(ctx_, t.items, t.tiles, t.ntiles, t.smem / (int)sizeof(T),
-                                                           ldlt_ ? lu_perm_ : nullptr, d_xoff_);
+            launch_pdl(trsm3_kernel<T>, dim3(t.ntiles), dim3(256), (size_t)t.smem, 1, ctx_, (const DTrsm*)t.items,
+                       (const DTile*)t.tiles, t.ntiles, t.smem / (int)sizeof(T),
+                       (const int*)(ldlt_ ? lu_perm_ : nullptr), (const long long*)d_xoff_);
         });
     }
     // Cluster Cholesky for pivots of up to nmax rows that one CTA's shared memory cannot
@@ -5486,7 +5500,7 @@ class DeviceFactor : public DeviceFactorBase {
             }
         };
         launch("perm", [&] {
-            launch_sweep(perm_in_kernel<T>, dim3((unsigned)((tot + 255) / 256)), dim3(256), 0, 1, (const double*)x, ld, X,
+            launch_pdl(perm_in_kernel<T>, dim3((unsigned)((tot + 255) / 256)), dim3(256), 0, 1, (const double*)x, ld, X,
                          (const int*)d_perm_, (const long long*)d_slot_, n);
         });
         auto trsv_mr = [&](const int* clusters, const int* blks, const int* small, int nsmall, const int2* big, int nbig,
@@ -5534,12 +5548,12 @@ class DeviceFactor : public DeviceFactorBase {
                     const int nbig = elim ? D.n_elim_big_tv : D.n_scale_big_tv;
                     if (nsmall)
                         launch("trsv", [&] {
-                            launch_sweep(trsv_small_kernel<T>, dim3((nsmall + TS_WARPS - 1) / TS_WARPS),
+                            launch_pdl(trsv_small_kernel<T>, dim3((nsmall + TS_WARPS - 1) / TS_WARPS),
                                          dim3(32 * TS_WARPS), 0, 1, ctx_, X, clusters, blks, small, nsmall, trans);
                         });
                     if (nbig)
                         launch("trsv", [&] {
-                            launch_sweep(trsv4_kernel<T>, dim3(nbig), dim3(TV_THREADS), (size_t)smem, 1, ctx_, X,
+                            launch_pdl(trsv4_kernel<T>, dim3(nbig), dim3(TV_THREADS), (size_t)smem, 1, ctx_, X,
                                          clusters, blks, big, trans, tmp, tv_count_);
                         });
                     return;
@@ -5549,7 +5563,7 @@ class DeviceFactor : public DeviceFactorBase {
                 if (mr)
                     trsv_mrhs_kernel<T><<<ntv, 256, 0, s_>>>(ctx_, X, clusters, blks, tv, trans, tmp, tv_count_);
                 else
-                    launch_sweep(trsv4_kernel<T>, dim3(ntv), dim3(TV_THREADS), (size_t)smem, 1, ctx_, X, clusters, blks,
+                    launch_pdl(trsv4_kernel<T>, dim3(ntv), dim3(TV_THREADS), (size_t)smem, 1, ctx_, X, clusters, blks,
                                  tv, trans, tmp, tv_count_);
             });
         };
@@ -5560,20 +5574,20 @@ class DeviceFactor : public DeviceFactorBase {
                     ortho_mrhs_kernel<T><<<D.n_ortho, 256, D.ortho_mrhs_smem, s_>>>(ctx_, X, D.ortho, vstore_, tstore_,
                                                                                     trans);
                 else if (D.ortho_cs > 1 && ortho_full_on_ && ortho_cluster_on_)
-                    launch_sweep(ortho_cluster_kernel<T, 256>, dim3((unsigned)(D.n_ortho * nrhs * D.ortho_cs)), dim3(256),
+                    launch_pdl(ortho_cluster_kernel<T, 256>, dim3((unsigned)(D.n_ortho * nrhs * D.ortho_cs)), dim3(256),
                                  (size_t)D.ortho_cs_smem, D.ortho_cs, ctx_, X, (const DOrtho*)D.ortho, D.n_ortho,
                                  (const T*)vstore_, (const T*)tstore_, trans);
                 else if (D.ortho_full_smem && ortho_full_on_) {
                     if (D.ortho_full_wide)
-                        launch_sweep(ortho_full_kernel<T, 512>, dim3(D.n_ortho * nrhs), dim3(512),
+                        launch_pdl(ortho_full_kernel<T, 512>, dim3(D.n_ortho * nrhs), dim3(512),
                                      (size_t)D.ortho_full_smem, 1, ctx_, X, (const DOrtho*)D.ortho, D.n_ortho,
                                      (const T*)vstore_, (const T*)tstore_, trans);
                     else
-                        launch_sweep(ortho_full_kernel<T, 256>, dim3(D.n_ortho * nrhs), dim3(256),
+                        launch_pdl(ortho_full_kernel<T, 256>, dim3(D.n_ortho * nrhs), dim3(256),
                                      (size_t)D.ortho_full_smem, 1, ctx_, X, (const DOrtho*)D.ortho, D.n_ortho,
                                      (const T*)vstore_, (const T*)tstore_, trans);
                 } else
-                    launch_sweep(ortho_wyb_kernel<T>, dim3(D.n_ortho * nrhs), dim3(512), (size_t)D.x_smem_ortho, 1,
+                    launch_pdl(ortho_wyb_kernel<T>, dim3(D.n_ortho * nrhs), dim3(512), (size_t)D.x_smem_ortho, 1,
                                  ctx_, X, (const DOrtho*)D.ortho, D.n_ortho, (const T*)vstore_, (const T*)tstore_,
                                  trans, D.x_smem_ortho / (int)sizeof(T));
             });
@@ -5584,7 +5598,7 @@ class DeviceFactor : public DeviceFactorBase {
                 if (mr)
                     merge_x_mrhs_kernel<T><<<D.n_children, 256, 0, s_>>>(ctx_, X, D.child_idx, D.child_parent, cpos_, fwd);
                 else
-                    launch_sweep(merge_x_kernel<T>, dim3((D.n_children * nrhs + 7) / 8), dim3(256), 0, 1, ctx_, X,
+                    launch_pdl(merge_x_kernel<T>, dim3((D.n_children * nrhs + 7) / 8), dim3(256), 0, 1, ctx_, X,
                                  (const int*)D.child_idx, (const int*)D.child_parent, D.n_children,
                                  (const int*)cpos_, fwd);
             });
@@ -5600,7 +5614,7 @@ class DeviceFactor : public DeviceFactorBase {
                     if (mr)
                         gemm_mrhs_kernel<T><<<D.n_gf_tiles32, 256, 0, s_>>>(ctx_, X, D.gf, D.gfo, D.gf_tiles32, 1);
                     else
-                        launch_sweep(gemm_fwd2_kernel<T>, dim3(D.n_gf_tiles * nrhs), dim3(256), 0, 1, ctx_, X,
+                        launch_pdl(gemm_fwd2_kernel<T>, dim3(D.n_gf_tiles * nrhs), dim3(256), 0, 1, ctx_, X,
                                      (const DGroup*)D.gf, (const DGemmOp*)D.gfo, (const DTile*)D.gf_tiles,
                                      D.n_gf_tiles, 0, sg, (const long long*)d_xoff_, 0);
                 });
@@ -5631,7 +5645,7 @@ class DeviceFactor : public DeviceFactorBase {
                     if (mr)
                         gemm_mrhs_kernel<T><<<D.n_gb_tiles, 256, 0, s_>>>(ctx_, X, D.gb, D.gbo, D.gb_tiles, 0);
                     else
-                        launch_sweep(gemm_bwd2_kernel<T>, dim3(D.n_gb_tiles * nrhs), dim3(256), 0, 1, ctx_, X,
+                        launch_pdl(gemm_bwd2_kernel<T>, dim3(D.n_gb_tiles * nrhs), dim3(256), 0, 1, ctx_, X,
                                      (const DGroup*)D.gb, (const DGemmOp*)D.gbo, (const DTile*)D.gb_tiles,
                                      D.n_gb_tiles, sg, (const long long*)d_xoff_, 0);
                 });
@@ -5641,7 +5655,7 @@ class DeviceFactor : public DeviceFactorBase {
         }
         cur_level_ = -1;
         launch("perm", [&] {
-            launch_sweep(perm_out_kernel<T>, dim3((unsigned)((tot + 255) / 256)), dim3(256), 0, 1, x, ld, X,
+            launch_pdl(perm_out_kernel<T>, dim3((unsigned)((tot + 255) / 256)), dim3(256), 0, 1, x, ld, X,
                          (const int*)d_perm_, (const long long*)d_slot_, n);
         });
         SPAND_CUDA(cudaGetLastError());

@@ -68,6 +68,7 @@ __global__ void __launch_bounds__(NT) qrcp_cluster_kernel(Ctx<T> c, const DSpars
                                                                   int* rank_out, int* colcount, int* fallback,
                                                                   double tol, int smem_bytes, int vec_rows,
                                                                   QcProj<T> proj) {
+    pdl_wait_and_release();
     namespace cgx = cooperative_groups;
     cgx::cluster_group cl = cgx::this_cluster();
     const int CS = (int)cl.num_blocks();
