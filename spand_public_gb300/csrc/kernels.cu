@@ -1519,12 +1519,13 @@ __global__ void __launch_bounds__(256) schur_kernel(Ctx<T> c, const DTarget* __r
         }
 }
 
-// The Schur updates on the tensor cores, FP32 path: the same 32x32 tiles of C, the same
-// staging of X and Y (SK entries of the inner dimension at a time, LDLT signs applied);
+// The Schur updates on the tensor cores, FP32 path: the same 32x32 tiles of C, X and Y
+// staged SKT = 32 entries of the inner dimension at a time (LDLT signs applied);
 // warp w owns the 16x8 piece (rows 16 (w mod 2), columns 8 (w / 2)) and accumulates
 // -X Y into it with mma.sync m16n8k8 TF32, each operand split into TF32 head and tail
-// (head*head + head*tail + tail*head, close to FP32 accuracy), two k-steps per staged
+// (head*head + head*tail + tail*head, close to FP32 accuracy), four k-steps per staged
 // chunk.
+constexpr int SKT = 32;
 __global__ void __launch_bounds__(256) schur_tc_kernel(Ctx<float> c, const DTarget* __restrict__ targets,
                                                        const DUpd* __restrict__ ups, const DTile* __restrict__ tiles,
                                                        int ntiles, const float* __restrict__ signs = nullptr,
@@ -1538,8 +1539,8 @@ __global__ void __launch_bounds__(256) schur_tc_kernel(Ctx<float> c, const DTarg
     const int i0 = tiles[t].tile_i * ST, j0 = tiles[t].tile_j * ST;
     if (i0 >= M || j0 >= N) return;
     if (tg.syrk && i0 + ST <= j0) return;  // strictly upper tile
-    __shared__ float Xs[ST][SK + 4];
-    __shared__ float Ys[SK][ST + 8];
+    __shared__ float Xs[ST][SKT + 4];
+    __shared__ float Ys[SKT][ST + 8];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, g = lane >> 2, tq = lane & 3;
     const int mh = 16 * (w & 1), nb = 8 * (w >> 1);
     float* C = c.arena + cb.off;
@@ -1557,10 +1558,10 @@ __global__ void __launch_bounds__(256) schur_tc_kernel(Ctx<float> c, const DTarg
         const int ld1 = c.blk[up.b1].ld;
         const float* B2 = bptr(c, up.b2);
         const int ld2 = c.blk[up.b2].ld;
-        for (int k0 = 0; k0 < S; k0 += SK) {
-            for (int idx = threadIdx.x; idx < ST * SK; idx += 256) {
+        for (int k0 = 0; k0 < S; k0 += SKT) {
+            for (int idx = threadIdx.x; idx < ST * SKT; idx += 256) {
                 int ii, kk;
-                if (up.t1) { kk = idx % SK; ii = idx / SK; } else { ii = idx % ST; kk = idx / ST; }
+                if (up.t1) { kk = idx % SKT; ii = idx / SKT; } else { ii = idx % ST; kk = idx / ST; }
                 const int i = i0 + ii, k = k0 + kk;
                 float v = 0.f;
                 if (i < M && k < S) {
@@ -1569,9 +1570,9 @@ __global__ void __launch_bounds__(256) schur_tc_kernel(Ctx<float> c, const DTarg
                 }
                 Xs[ii][kk] = v;
             }
-            for (int idx = threadIdx.x; idx < ST * SK; idx += 256) {
+            for (int idx = threadIdx.x; idx < ST * SKT; idx += 256) {
                 int jj, kk;
-                if (up.t2) { jj = idx % ST; kk = idx / ST; } else { kk = idx % SK; jj = idx / SK; }
+                if (up.t2) { jj = idx % ST; kk = idx / ST; } else { kk = idx % SKT; jj = idx / SKT; }
                 const int j = j0 + jj, k = k0 + kk;
                 float v = 0.f;
                 if (j < N && k < S) v = up.t2 ? B2[j + (size_t)k * ld2] : B2[k + (size_t)j * ld2];
@@ -1579,7 +1580,7 @@ __global__ void __launch_bounds__(256) schur_tc_kernel(Ctx<float> c, const DTarg
             }
             __syncthreads();
 #pragma unroll
-            for (int ks = 0; ks < SK; ks += 8) {
+            for (int ks = 0; ks < SKT; ks += 8) {
                 // A = -X (rows mh.., inner ks..), B = Y (inner ks.., columns nb..)
                 const float av[4] = {-Xs[mh + g][ks + tq], -Xs[mh + g + 8][ks + tq], -Xs[mh + g][ks + tq + 4],
                                      -Xs[mh + g + 8][ks + tq + 4]};
@@ -1899,7 +1900,7 @@ __global__ void merge_sizes_kernel(int* csize, int* rows0, int* cpos, const int*
     rows0[parents[p]] = pos;
 }
 
-constexpr int MT = 32;
+constexpr int MT = 64;  // a 64 x 64 tile per CTA: sixteen elements per thread
 
 template <typename T>
 __global__ void merge_copy_kernel(Ctx<T> c, const DMerge* __restrict__ items, const DTile* __restrict__ tiles,
