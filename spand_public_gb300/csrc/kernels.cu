@@ -890,6 +890,87 @@ __global__ void __launch_bounds__(256) trsm_tc_kernel(Ctx<float> c, const DTrsm*
     }
 }
 
+// The panel products of pivots of at most 32 rows (the thousands of small interface pivots
+// of the lowest levels), one warp per 32-row tile, eight tiles per CTA: the same TF32
+// head/tail tensor-core products as trsm_tc_kernel, each warp staging its own tile and
+// running all of its (at most four) 8-column blocks, so a tile is a warp's work instead of
+// a CTA's.
+constexpr int TSW = 8;  // tiles (warps) per CTA
+__global__ void __launch_bounds__(32 * TSW) trsm_tc_small_kernel(Ctx<float> c, const DTrsm* __restrict__ items,
+                                                                  const DTile* __restrict__ tiles, int ntiles) {
+    pdl_wait_and_release();
+    __shared__ float Xall[TSW][32 * TC_XLD];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int t = blockIdx.x * TSW + wid;
+    if (t >= ntiles || c.status->not_spd) return;
+    const DTrsm it = items[tiles[t].item];
+    const int n = c.csize[it.cluster];
+    if (n == 0 || n > 32) return;
+    const float* L = bptr(c, it.lblock);
+    const int lld = c.blk[it.lblock].ld;
+    float* B = bptr(c, it.block);
+    const int bld = c.blk[it.block].ld;
+    const int m = it.side == 1 ? c.csize[c.blk[it.block].rowc] : c.csize[c.blk[it.block].colc];
+    const int r0 = tiles[t].tile_i * TRB;
+    if (r0 >= m) return;
+    const int tr = min(TRB, m - r0);
+    const long long sq = it.side == 1 ? 1 : bld, sk = it.side == 1 ? bld : 1;
+    float* Bt = B + (it.side == 1 ? (size_t)r0 : (size_t)r0 * bld);
+    const int nc = (n + 7) & ~7;
+    float* X = Xall[wid];
+    for (int idx = lane; idx < TRB * nc; idx += 32) {
+        int q, k;
+        if (it.side == 1) {
+            q = idx % TRB;
+            k = idx / TRB;
+        } else {
+            k = idx % nc;
+            q = idx / nc;
+        }
+        X[q + k * TC_XLD] = (q < tr && k < n) ? Bt[q * sq + (long long)k * sk] : 0.f;
+    }
+    __syncwarp();
+    const int g = lane >> 2, tg = lane & 3;
+    for (int cb = 0; cb < nc / 8; cb++) {
+        const int cc0 = cb * 8, cc = cc0 + g;
+        const bool live = cc < n;
+        const float* lcol = L + (size_t)(live ? cc : 0) * lld;
+        const float dinv = live ? 1.f / lcol[cc] : 0.f;
+        float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+        for (int k0 = 0; k0 <= cc0; k0 += 8) {
+            const int ka = k0 + tg, kb = ka + 4;
+            const float b0 = !live ? 0.f : (ka < cc ? lcol[ka] : (ka == cc ? dinv : 0.f));
+            const float b1 = !live ? 0.f : (kb < cc ? lcol[kb] : (kb == cc ? dinv : 0.f));
+            uint32_t bh[2] = {tf32_of(b0), tf32_of(b1)};
+            uint32_t bl[2] = {tf32_of(b0 - __uint_as_float(bh[0])), tf32_of(b1 - __uint_as_float(bh[1]))};
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const float* xa = X + 16 * h + g;
+                const float av[4] = {xa[ka * TC_XLD], xa[8 + ka * TC_XLD], xa[kb * TC_XLD], xa[8 + kb * TC_XLD]};
+                uint32_t ah[4], al[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    ah[i] = tf32_of(av[i]);
+                    al[i] = tf32_of(av[i] - __uint_as_float(ah[i]));
+                }
+                float big[4] = {0.f, 0.f, 0.f, 0.f}, small[4] = {0.f, 0.f, 0.f, 0.f};
+                mma_tf32_16x8x8(small, al, bh);
+                mma_tf32_16x8x8(small, ah, bl);
+                mma_tf32_16x8x8(big, ah, bh);
+#pragma unroll
+                for (int e = 0; e < 4; e++) acc[h][e] += big[e] + small[e];
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++)
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int q = 16 * h + g + (i >= 2 ? 8 : 0), col = cc0 + 2 * tg + (i & 1);
+                if (q < tr && col < n) Bt[q * sq + (long long)col * sk] = acc[h][i];
+            }
+    }
+}
+
 // ------------------------------------------------------------------------------------
 // General (PLU) path.  Partial-pivot LU of a pivot block (tree.cpp:614-635; getf,
 // util.cpp:183-200, in the LAPACK dgetf2 order: the pivot is the first row of largest
@@ -3522,20 +3603,29 @@ class DeviceFactor : public DeviceFactorBase {
             D.elim_clusters = up(L.elim_clusters);
             D.elim_pivots = up(L.elim_pivots);
             // LLT pivots of at most 32 rows: a warp each (potrf_small_kernel)
+            // and the others, for the one-CTA kernel when the small ones go to the warp kernel
             auto small_pivots = [&](const std::vector<int>& cl, const std::vector<int>& pv, int*& scl, int*& spv,
-                                    int& ns) {
-                std::vector<int> a, b;
+                                    int& ns, int*& bcl, int*& bpv, int& nb) {
+                std::vector<int> a, b, c2, d2;
                 if (!lu_ && !ldlt_)
-                    for (size_t q = 0; q < cl.size(); q++)
+                    for (size_t q = 0; q < cl.size(); q++) {
                         if (P.c_cap[cl[q]] <= 32) {
                             a.push_back(cl[q]);
                             b.push_back(pv[q]);
+                        } else {
+                            c2.push_back(cl[q]);
+                            d2.push_back(pv[q]);
                         }
+                    }
                 ns = (int)a.size();
                 scl = up(a);
                 spv = up(b);
+                nb = (int)c2.size();
+                bcl = up(c2);
+                bpv = up(d2);
             };
-            small_pivots(L.elim_clusters, L.elim_pivots, D.elim_ps_cl, D.elim_ps_piv, D.n_elim_ps);
+            small_pivots(L.elim_clusters, L.elim_pivots, D.elim_ps_cl, D.elim_ps_piv, D.n_elim_ps, D.elim_pb_cl,
+                         D.elim_pb_piv, D.n_elim_pb);
             D.elim_smem = smem_for(L.elim_clusters, P);
             D.elim_tri = build_trtri(L.elim_clusters, P);
             // PLU: the panels are products with the inverse block
@@ -3568,7 +3658,8 @@ class DeviceFactor : public DeviceFactorBase {
             D.n_scale = (int)L.scale_clusters.size();
             D.scale_clusters = up(L.scale_clusters);
             D.scale_pivots = up(L.scale_pivots);
-            small_pivots(L.scale_clusters, L.scale_pivots, D.scale_ps_cl, D.scale_ps_piv, D.n_scale_ps);
+            small_pivots(L.scale_clusters, L.scale_pivots, D.scale_ps_cl, D.scale_ps_piv, D.n_scale_ps, D.scale_pb_cl,
+                         D.scale_pb_piv, D.n_scale_pb);
             D.scale_smem = smem_for(L.scale_clusters, P);
             D.scale_tri = build_trtri(L.scale_clusters, P);
             build_trsm(L.scale_trsm, lu_ ? L.scale_inv : L.scale_pivots, L.scale_clusters, P, D.scale_trsm0,
@@ -4073,6 +4164,7 @@ class DeviceFactor : public DeviceFactorBase {
                     launch_trsm(D.elim_trsm1);
                 } else {
                     launch_potrf(D.elim_pivots, D.elim_clusters, D.n_elim, D.elim_ps_piv, D.elim_ps_cl, D.n_elim_ps,
+                                 D.elim_pb_piv, D.elim_pb_cl, D.n_elim_pb,
                                  D.elim_smem, D.elim_tri, D.elim_pc_cs,
                                  D.elim_pc_smem);
                     launch_trsm(D.elim_trsm0);
@@ -4091,7 +4183,7 @@ class DeviceFactor : public DeviceFactorBase {
                     launch_trsm(D.scale_trsm1);
                 } else {
                     launch_potrf(D.scale_pivots, D.scale_clusters, D.n_scale, D.scale_ps_piv, D.scale_ps_cl,
-                                 D.n_scale_ps, D.scale_smem, D.scale_tri,
+                                 D.n_scale_ps, D.scale_pb_piv, D.scale_pb_cl, D.n_scale_pb, D.scale_smem, D.scale_tri,
                                  D.scale_pc_cs, D.scale_pc_smem);
                     launch_trsm(D.scale_trsm0);
                     launch_trsm(D.scale_trsm1);
@@ -4519,6 +4611,12 @@ class DeviceFactor : public DeviceFactorBase {
         int ntiles = 0;
         int side = 0;
         int smem = 0;
+        // the same tiles split by pivot size: at most 32 rows (a warp each on the tensor
+        // cores, FP32) and larger
+        DTile* stiles = nullptr;
+        int nstiles = 0;
+        DTile* btiles = nullptr;
+        int nbtiles = 0;
     };
     struct TrtriDev {
         DTile* tiles = nullptr;
@@ -4566,6 +4664,8 @@ class DeviceFactor : public DeviceFactorBase {
         int* elim_pivots = nullptr;
         int *elim_ps_cl = nullptr, *elim_ps_piv = nullptr, *scale_ps_cl = nullptr, *scale_ps_piv = nullptr;
         int n_elim_ps = 0, n_scale_ps = 0;  // LLT pivots of at most 32 rows (a warp each)
+        int *elim_pb_cl = nullptr, *elim_pb_piv = nullptr, *scale_pb_cl = nullptr, *scale_pb_piv = nullptr;
+        int n_elim_pb = 0, n_scale_pb = 0;  // the other LLT pivots
         int elim_smem = 0;
         int elim_pc_cs = 0, elim_pc_smem = 0;   // cluster Cholesky (0: single-CTA kernel)
         TrsmDev elim_trsm0, elim_trsm1;
@@ -4865,6 +4965,16 @@ class DeviceFactor : public DeviceFactorBase {
         auto t1 = tiles_1d(ext1, TRB);
         side0 = {up(it0), up(t0), (int)t0.size(), 0, trsm_smem(clusters, P)};
         side1 = {up(it1), up(t1), (int)t1.size(), 1, trsm_smem(clusters, P)};
+        auto split = [&](const std::vector<DTrsm>& it, const std::vector<DTile>& tl, TrsmDev& d) {
+            std::vector<DTile> sm, bg;
+            for (const DTile& x : tl) (P.c_cap[it[x.item].cluster] <= 32 ? sm : bg).push_back(x);
+            d.stiles = up(sm);
+            d.nstiles = (int)sm.size();
+            d.btiles = up(bg);
+            d.nbtiles = (int)bg.size();
+        };
+        split(it0, t0, side0);
+        split(it1, t1, side1);
     }
     // ---- QRCP launch configuration -------------------------------------------------
     int qc_smem_cap_ = 0;  // dynamic shared memory per CTA available to the QRCP kernel
@@ -5237,8 +5347,9 @@ class DeviceFactor : public DeviceFactorBase {
                                       jpvt_, ipvt_, tauws_, rank_, colcount_, fallback_, tol,
                                       force_global_ ? 0 : W.smem, W.vec_rows, qc_proj()));
     }
-    void launch_potrf(int* pivots, int* clusters, int n, const int* ps_piv, const int* ps_cl, int n_ps, int smem,
-                      const TrtriDev& tri, int pc_cs, int pc_smem) {
+    void launch_potrf(int* pivots, int* clusters, int n, const int* ps_piv, const int* ps_cl, int n_ps,
+                      const int* pb_piv, const int* pb_cl, int n_pb, int smem, const TrtriDev& tri, int pc_cs,
+                      int pc_smem) {
         // (not beside the cluster kernel or the strip inverse, which take every pivot of the list)
         const bool small = n_ps > 0 && potrf_small_on_ && pc_cs == 0 && smem > 0;
         if (small)
@@ -5255,12 +5366,22 @@ class DeviceFactor : public DeviceFactorBase {
         // The strip-wise inverse runs only where pivots may miss the single-CTA kernel's shared
         // memory (which inverts what it holds); without it potrf3 inverts every pivot itself.
         const bool strips = tri.ntiles > 0 && (smem == 0 || pc_cs > 0);
-        // single-CTA kernel: every pivot, or (after the cluster kernel) those it could not hold
-        launch("potrf", [&] {
-            launch_pdl(potrf3_kernel<T>, dim3(n), dim3(256), (size_t)smem, 1, ctx_, (const int*)pivots,
-                       (const int*)clusters, n, smem / (int)sizeof(T), strips ? tri.smem / (32 * (int)sizeof(T)) : 0,
-                       pc_cs > 0 ? (const int*)pc_fallback_ : nullptr, small ? 32 : 0);
-        });
+        // single-CTA kernel: every pivot, or (after the cluster kernel) those it could not hold,
+        // or (beside the warp kernel) the pivots of more than 32 rows only
+        if (small && n_pb == 0) {
+        } else if (small) {
+            launch("potrf", [&] {
+                launch_pdl(potrf3_kernel<T>, dim3(n_pb), dim3(256), (size_t)smem, 1, ctx_, pb_piv, pb_cl, n_pb,
+                           smem / (int)sizeof(T), 0, (const int*)nullptr, 0);
+            });
+        } else {
+            launch("potrf", [&] {
+                launch_pdl(potrf3_kernel<T>, dim3(n), dim3(256), (size_t)smem, 1, ctx_, (const int*)pivots,
+                           (const int*)clusters, n, smem / (int)sizeof(T),
+                           strips ? tri.smem / (32 * (int)sizeof(T)) : 0,
+                           pc_cs > 0 ? (const int*)pc_fallback_ : nullptr, 0);
+            });
+        }
         if (strips)
             launch("trtri", [&] {
                 launch_pdl(trtri_kernel<T>, dim3(tri.ntiles), dim3(256), (size_t)tri.smem, 1, ctx_, (const int*)pivots,
@@ -5356,10 +5477,19 @@ class DeviceFactor : public DeviceFactorBase {
             const int nmax = t.smem / (TRB * (int)sizeof(T));
             const int64_t tcs = (int64_t)TC_XLD * ((nmax + 7) & ~7) * (int64_t)sizeof(float);
             if (trsm_tc_on_ && !ldlt_ && t.smem > 16 && tcs <= 200 * 1024) {
-                launch("trsm", [&] {
-                    launch_pdl(trsm_tc_kernel, dim3(t.ntiles), dim3(256), (size_t)tcs, 1, ctx_, (const DTrsm*)t.items,
-                               (const DTile*)t.tiles, t.ntiles);
-                });
+                // pivots of at most 32 rows a warp per tile, the others a CTA per tile
+                const bool split = trsm_small_on_ && t.nstiles > 0;
+                if (split)
+                    launch("trsm", [&] {
+                        launch_pdl(trsm_tc_small_kernel, dim3((t.nstiles + TSW - 1) / TSW), dim3(32 * TSW), 0, 1, ctx_,
+                                   (const DTrsm*)t.items, (const DTile*)t.stiles, t.nstiles);
+                    });
+                const int nb = split ? t.nbtiles : t.ntiles;
+                if (nb)
+                    launch("trsm", [&] {
+                        launch_pdl(trsm_tc_kernel, dim3(nb), dim3(256), (size_t)tcs, 1, ctx_, (const DTrsm*)t.items,
+                                   (const DTile*)(split ? t.btiles : t.tiles), nb);
+                    });
                 return;
             }
         }
@@ -5720,6 +5850,8 @@ class DeviceFactor : public DeviceFactorBase {
     bool trsv_small_on_ = !(getenv("SPAND_TRSV_SMALL") && atoi(getenv("SPAND_TRSV_SMALL")) == 0);
     // SPAND_TRSM_TC=0: the FP32 panel products on the SIMT kernel
     bool trsm_tc_on_ = !(getenv("SPAND_TRSM_TC") && atoi(getenv("SPAND_TRSM_TC")) == 0);
+    // SPAND_TRSM_SMALL=0: the panel products of small pivots a CTA per tile as well
+    bool trsm_small_on_ = !(getenv("SPAND_TRSM_SMALL") && atoi(getenv("SPAND_TRSM_SMALL")) == 0);
     // SPAND_SCHUR_TC=0: the FP32 Schur updates on the SIMT kernel
     bool schur_tc_on_ = !(getenv("SPAND_SCHUR_TC") && atoi(getenv("SPAND_SCHUR_TC")) == 0);
     // SPAND_ORTHO_CLUSTER=0: the Orthogonal op of the large clusters on one CTA each
