@@ -57,7 +57,7 @@ __device__ void trtri_to_upper(T* A, int ld, int n) {
 // panels (dpotrf 'L', tree.cpp:582-593): the path of pivots too large for shared memory.
 // Per panel: (1) update by the factored columns, (2) the 32x32 diagonal block by one warp
 // with shuffles, (3) the rows below by a triangular solve, one row per thread.  Three
-// barriers per panel.  (Pivots that fit are factored and inverted by chol_inv_smem.)
+// barriers per panel.  (Pivots that fit are factored and inverted by chol_inv_tiled.)
 // ------------------------------------------------------------------------------------
 constexpr int PNB = 32;
 
@@ -127,17 +127,77 @@ __device__ bool chol_blocked(T* A, int ld, int n, int* bad) {
     return true;
 }
 
+// The 32x32 diagonal block of a panel (rows and columns jb..jb+w-1 of a block held in shared
+// memory, ld = n), by the first warp: Cholesky in registers, lane i holding row i (a[k] =
+// A[i][k], k <= i), right-looking with the columns broadcast by shuffles (the same
+// operations per element, in the same order, as a column-by-column update); then its
+// inverse D by forward substitution, column c = lane in registers: D[r][c] = (delta_rc -
+// sum_{l<r} L[r][l] D[l][c]) / L[r][r].  D goes transposed into the block's strictly upper
+// slots (A[(jb+c) + (jb+r)*n] = D[r][c], r > c) and row-major into Dpad (zero above the
+// diagonal and outside w) for the rows below.  Sets *bad on a non-positive pivot.
+template <typename T>
+__device__ void chol_diag32(T* A, int n, int jb, int w, T* Dpad, int* bad) {
+    const int lane = threadIdx.x & 31;
+    T a[PNB];
+#pragma unroll
+    for (int k = 0; k < PNB; k++) a[k] = (k <= lane && lane < w) ? A[(jb + lane) + (jb + k) * n] : T(0);
+    int fail = 0;
+#pragma unroll
+    for (int j = 0; j < PNB; j++) {
+        if (j < w) {
+            T d = __shfl_sync(0xffffffffu, a[j], j);
+            if (!(d > T(0))) {
+                fail = 1;
+                d = T(1);
+            } else {
+                d = dsqrt(d);
+            }
+            if (lane == j) a[j] = d;
+            else if (lane > j) a[j] /= d;
+            const T lij = a[j];
+#pragma unroll
+            for (int k = j + 1; k < PNB; k++) {
+                const T lkj = __shfl_sync(0xffffffffu, a[j], k);
+                if (lane > j && k <= lane) a[k] -= lij * lkj;
+            }
+        }
+    }
+    if (lane < w)
+#pragma unroll
+        for (int k = 0; k < PNB; k++)
+            if (k <= lane) A[(jb + lane) + (jb + k) * n] = a[k];
+    __syncwarp();
+    if (lane == 0 && fail) *bad = 1;
+    if (fail) return;
+    T d[PNB];
+#pragma unroll
+    for (int r = 0; r < PNB; r++) {
+        d[r] = T(0);
+        if (r < w) {
+            T acc = r == lane ? T(1) : T(0);
+#pragma unroll
+            for (int l = 0; l < r; l++) acc -= A[(jb + r) + (jb + l) * n] * d[l];
+            d[r] = acc / A[(jb + r) + (jb + r) * n];
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < PNB; r++) {
+        if (r < w && r > lane) A[(jb + lane) + (jb + r) * n] = d[r];
+        Dpad[r * (PNB + 1) + lane] = d[r];
+    }
+}
+
 // Cholesky and inverse of a pivot block held in shared memory (ld = n, lower triangle
 // in, L in the lower triangle and L^{-1} transposed in the strictly upper triangle out;
 // the diagonal of L^{-1}, 1 / L_ii, is not stored).  32-column panels: (1) update of the
-// panel by the factored columns (left-looking), (2) the 32x32 diagonal block by one warp
-// with shuffles, then its inverse D by forward substitution (lane = column, in
-// registers), (3) rows below: row x D^T, a warp per row.  Then L^{-1} block row by block row:
-// L^{-1}[I][J] = -D_I sum_{J <= K < I} L[I][K] L^{-1}[K][J], the sum written into the
-// block's upper-triangle slots first and multiplied by D_I per column.  256 threads.
+// panel by the factored columns (left-looking), (2) the 32x32 diagonal block and its
+// inverse D (chol_diag32), (3) rows below: row x D^T, a warp per row.  Then L^{-1} block row
+// by block row: L^{-1}[I][J] = -D_I sum_{J <= K < I} L[I][K] L^{-1}[K][J], the sum written
+// into the block's upper-triangle slots first and multiplied by D_I per column.  256
+// threads, one element per thread in the products (kept as the comparison path of
+// chol_inv_tiled).
 template <typename T>
-__device__ bool chol_inv_smem(T* A, int n, int* bad) {
-    __shared__ T Dpad[PNB * (PNB + 1)];  // inverse of the current diagonal block, padded rows
+__device__ bool chol_inv_smem(T* A, int n, int* bad, T* Dpad) {
     const int tid = threadIdx.x, lane = tid & 31, w8 = tid >> 5;
     constexpr int NWARP = 8;
     const int nb = (n + PNB - 1) / PNB;
@@ -163,63 +223,7 @@ __device__ bool chol_inv_smem(T* A, int n, int* bad) {
             __syncthreads();
         }
         // (2) diagonal block and its inverse (upper-triangle slots of the block)
-        if (tid < 32) {
-            // the block in registers, lane i holding row i (a[k] = A[i][k], k <= i):
-            // right-looking Cholesky with the columns broadcast by shuffles (the same
-            // operations per element, in the same order, as a column-by-column update)
-            T a[PNB];
-#pragma unroll
-            for (int k = 0; k < PNB; k++) a[k] = (k <= lane && lane < w) ? A[(jb + lane) + (jb + k) * n] : T(0);
-            int fail = 0;
-#pragma unroll
-            for (int j = 0; j < PNB; j++) {
-                if (j < w) {
-                    T d = __shfl_sync(0xffffffffu, a[j], j);
-                    if (!(d > T(0))) {
-                        fail = 1;
-                        d = T(1);
-                    } else {
-                        d = dsqrt(d);
-                    }
-                    if (lane == j) a[j] = d;
-                    else if (lane > j) a[j] /= d;
-                    const T lij = a[j];
-#pragma unroll
-                    for (int k = j + 1; k < PNB; k++) {
-                        const T lkj = __shfl_sync(0xffffffffu, a[j], k);
-                        if (lane > j && k <= lane) a[k] -= lij * lkj;
-                    }
-                }
-            }
-            if (lane < w)
-#pragma unroll
-                for (int k = 0; k < PNB; k++)
-                    if (k <= lane) A[(jb + lane) + (jb + k) * n] = a[k];
-            __syncwarp();
-            if (lane == 0 && fail) *bad = 1;
-            if (!fail) {
-                // column c = lane of D = L_pp^{-1} in registers (forward substitution on e_c,
-                // L read by broadcast): D[r][c] = (delta_rc - sum_{l<r} L[r][l] D[l][c]) / L[r][r]
-                T d[PNB];
-#pragma unroll
-                for (int r = 0; r < PNB; r++) {
-                    d[r] = T(0);
-                    if (r < w) {
-                        T acc = r == lane ? T(1) : T(0);
-#pragma unroll
-                        for (int l = 0; l < r; l++) acc -= A[(jb + r) + (jb + l) * n] * d[l];
-                        d[r] = acc / A[(jb + r) + (jb + r) * n];
-                    }
-                }
-                // D transposed into the block's upper slots (A[(jb+c) + (jb+r)*n] = D[r][c],
-                // r > c) and row-major into Dpad for the rows below
-#pragma unroll
-                for (int r = 0; r < PNB; r++) {
-                    if (r < w && r > lane) A[(jb + lane) + (jb + r) * n] = d[r];
-                    Dpad[r * (PNB + 1) + lane] = d[r];
-                }
-            }
-        }
+        if (tid < 32) chol_diag32(A, n, jb, w, Dpad, bad);
         __syncthreads();
         if (*bad) return false;
         // (3) rows below: L[i][jb+j] = sum_{l <= j} A[i][jb+l] D[j][l]
@@ -264,13 +268,213 @@ __device__ bool chol_inv_smem(T* A, int n, int* bad) {
     return true;
 }
 
+// The same factorization and inverse, same layout and results up to rounding, with every
+// product of the panels on register tiles: a thread holds 4 rows x 4 columns of the output
+// (8 column groups x 32 row groups over the 256 threads), so each pair of shared-memory
+// loads feeds four multiply-adds instead of one and sixteen independent sums are in flight.
+// (1) the panel's left-looking update, rows jb..n-1 in passes of 128; (3) the rows below
+// times D^T; then per block row I of L^{-1}: (a) E = L[I][0:i0] L^{-1}[0:i0][0:i0] on tiles
+// of E into the block's upper slots, (b) L^{-1}[I][0:i0] = -D_I E on tiles, read into
+// registers, a barrier, then written over E (the tiles of one pass cover disjoint column
+// groups from the next pass's).  Loads past the last row are clamped to row n-1 (or stay
+// inside the n x n block by construction) and never written back.
+template <typename T>
+__device__ bool chol_inv_tiled(T* A, int n, int* bad, T* Dpad) {
+    const int tid = threadIdx.x;
+    const int cq = tid & 7, rq = tid >> 3;  // the thread's 4-column group and 4-row group
+    const int c0 = 4 * cq;
+    const int nb = (n + PNB - 1) / PNB;
+    for (int pb = 0; pb < nb; pb++) {
+        const int jb = pb * PNB, w = min(PNB, n - jb);
+        // (1) A[i][jb+jj] -= sum_{k < jb} L[i][k] L[jb+jj][k], i >= jb + jj.  Rows r0+u <= n+2
+        // and columns jb+c0+v <= n+2 at k <= n-2 stay below n*n (n > 32 here).
+        if (jb > 0) {
+            for (int r0 = jb + 4 * rq; r0 < n; r0 += 128) {
+                if (r0 + 3 < jb + c0 || c0 >= w) continue;  // above the diagonal or right of the panel
+                T acc[4][4];
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int v = 0; v < 4; v++) acc[u][v] = T(0);
+                const T* pa = A + r0;
+                const T* pbk = A + jb + c0;
+#pragma unroll 2
+                for (int k = 0; k < jb; k++) {
+                    T a[4], b[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) a[u] = pa[u + k * n];
+#pragma unroll
+                    for (int v = 0; v < 4; v++) b[v] = pbk[v + k * n];
+#pragma unroll
+                    for (int u = 0; u < 4; u++)
+#pragma unroll
+                        for (int v = 0; v < 4; v++) acc[u][v] += a[u] * b[v];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int v = 0; v < 4; v++) {
+                        const int i = r0 + u, jj = c0 + v;
+                        if (i < n && jj < w && i >= jb + jj) A[i + (jb + jj) * n] -= acc[u][v];
+                    }
+            }
+            __syncthreads();
+        }
+        // (2) diagonal block and its inverse
+        if (tid < 32) chol_diag32(A, n, jb, w, Dpad, bad);
+        __syncthreads();
+        if (*bad) return false;
+        // (3) rows below: L[i][jb+c] = sum_{l <= c} A[i][jb+l] D[c][l] (Dpad zero above its
+        // diagonal); the eight threads of a row group share a warp, which has read all its rows
+        // before any of them is written
+        for (int base = jb + w; base < n; base += 128) {
+            const int r0 = base + 4 * rq;
+            const bool act = r0 < n && c0 < w;
+            T acc[4][4];
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++) acc[u][v] = T(0);
+            if (act) {
+                const int lmax = min(c0 + 3, w - 1);
+                int ro[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) ro[u] = min(r0 + u, n - 1);
+                for (int l = 0; l <= lmax; l++) {
+                    T a[4], d[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) a[u] = A[ro[u] + (jb + l) * n];
+#pragma unroll
+                    for (int v = 0; v < 4; v++) d[v] = Dpad[(c0 + v) * (PNB + 1) + l];
+#pragma unroll
+                    for (int u = 0; u < 4; u++)
+#pragma unroll
+                        for (int v = 0; v < 4; v++) acc[u][v] += a[u] * d[v];
+                }
+            }
+            __syncwarp();
+            if (act)
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int v = 0; v < 4; v++)
+                        if (r0 + u < n && c0 + v < w) A[(r0 + u) + (jb + c0 + v) * n] = acc[u][v];
+        }
+        __syncthreads();
+    }
+    // off-diagonal blocks of L^{-1}, block row by block row; tile t: row group t & 7 (rows
+    // i0+4(t&7)..+3 of the block), column group t >> 3 (columns 4(t>>3)..+3 < i0)
+    for (int ib = 1; ib < nb; ib++) {
+        const int i0 = ib * PNB, h = min(PNB, n - i0);
+        const int ntile = 2 * i0;  // 8 row groups x i0/4 column groups
+        // (a) E[ii][j] = sum_{j <= m < i0} L[i0+ii][m] Linv[m][j] -> A[j + (i0+ii)*n]
+        for (int t = tid; t < ntile; t += blockDim.x) {
+            const int q = 4 * (t & 7), j0 = 4 * (t >> 3);
+            int ro[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) ro[u] = min(i0 + q + u, n - 1);
+            T acc[4][4];
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++) acc[u][v] = T(0);
+            // m = j0..j0+3: Linv[m][j0+v] is 0 above its diagonal and 1 / L[m][m] on it
+#pragma unroll
+            for (int mm = 0; mm < 4; mm++) {
+                const int m = j0 + mm;
+                const T rd = T(1) / A[m + m * n];
+                T a[4], b[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) a[u] = A[ro[u] + m * n];
+#pragma unroll
+                for (int v = 0; v < 4; v++) b[v] = mm < v ? T(0) : (mm == v ? rd : A[(j0 + v) + m * n]);
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int v = 0; v < 4; v++) acc[u][v] += a[u] * b[v];
+            }
+#pragma unroll 2
+            for (int m = j0 + 4; m < i0; m++) {
+                T a[4], b[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) a[u] = A[ro[u] + m * n];
+#pragma unroll
+                for (int v = 0; v < 4; v++) b[v] = A[(j0 + v) + m * n];
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int v = 0; v < 4; v++) acc[u][v] += a[u] * b[v];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (q + u < h)
+#pragma unroll
+                    for (int v = 0; v < 4; v++) A[(j0 + v) + (i0 + q + u) * n] = acc[u][v];
+        }
+        __syncthreads();
+        // (b) Linv[i0+ii][j] = -(E[ii][j] / L[i0+ii][i0+ii] + sum_{l < ii} D[ii][l] E[l][j]),
+        // D[ii][l] = A[(i0+l) + (i0+ii)*n]
+        for (int t0 = 0; t0 < ntile; t0 += blockDim.x) {
+            const int t = t0 + tid;
+            const bool act = t < ntile;
+            const int q = 4 * (t & 7), j0 = 4 * (t >> 3);
+            T o[4][4];
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++) o[u][v] = T(0);
+            if (act && q < h) {
+                int co[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) co[u] = min(i0 + q + u, n - 1) * n;
+                for (int l = 0; l < q; l++) {  // below every row of the group: D[q+u][l] stored
+                    T d[4], e[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) d[u] = A[(i0 + l) + co[u]];
+#pragma unroll
+                    for (int v = 0; v < 4; v++) e[v] = A[(j0 + v) + (i0 + l) * n];
+#pragma unroll
+                    for (int u = 0; u < 4; u++)
+#pragma unroll
+                        for (int v = 0; v < 4; v++) o[u][v] += d[u] * e[v];
+                }
+#pragma unroll
+                for (int ll = 0; ll < 4; ll++) {  // l = q..q+3: the group's own triangle
+                    const int l = q + ll;
+                    if (l < h) {
+                        T d[4], e[4];
+#pragma unroll
+                        for (int u = 0; u < 4; u++)
+                            d[u] = ll < u ? A[(i0 + l) + co[u]] : (ll == u ? T(1) / A[(i0 + l) + (i0 + l) * n] : T(0));
+#pragma unroll
+                        for (int v = 0; v < 4; v++) e[v] = A[(j0 + v) + (i0 + l) * n];
+#pragma unroll
+                        for (int u = 0; u < 4; u++)
+#pragma unroll
+                            for (int v = 0; v < 4; v++) o[u][v] += d[u] * e[v];
+                    }
+                }
+            }
+            __syncthreads();
+            if (act)
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (q + u < h)
+#pragma unroll
+                        for (int v = 0; v < 4; v++) A[(j0 + v) + (i0 + q + u) * n] = -o[u][v];
+        }
+        __syncthreads();
+    }
+    return true;
+}
+
 template <typename T>
 // FP32: registers capped for three CTAs per SM (24 bytes of spills); FP64 keeps two
 // (its register-resident panels would spill hundreds of bytes)
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) potrf3_kernel(Ctx<T> c, const int* __restrict__ pivots,
                                                      const int* __restrict__ clusters, int count, int smem_elems,
                                                      int strip_max_n, const int* __restrict__ only,
-                                                     int small_cap = 0) {
+                                                     int small_cap, int tiled) {
     pdl_wait_and_release();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
@@ -295,7 +499,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) potrf3_kernel(Ctx
             for (int i = j + tx; i < n; i += 32) sm[i + j * n] = G[i + (size_t)j * gld];
         __syncthreads();
         // factor and inverse together; the whole block (L below, L^{-1} transposed above) back
-        if (chol_inv_smem(sm, n, &bad)) {
+        __shared__ T Dpad[PNB * (PNB + 1)];  // inverse of the current diagonal block, padded rows
+        if (tiled ? chol_inv_tiled(sm, n, &bad, Dpad) : chol_inv_smem(sm, n, &bad, Dpad)) {
             for (int j = ty; j < n; j += nty)
                 for (int i = tx; i < n; i += 32) G[i + (size_t)j * gld] = sm[i + j * n];
         }
@@ -5372,14 +5577,14 @@ class DeviceFactor : public DeviceFactorBase {
         } else if (small) {
             launch("potrf", [&] {
                 launch_pdl(potrf3_kernel<T>, dim3(n_pb), dim3(256), (size_t)smem, 1, ctx_, pb_piv, pb_cl, n_pb,
-                           smem / (int)sizeof(T), 0, (const int*)nullptr, 0);
+                           smem / (int)sizeof(T), 0, (const int*)nullptr, 0, potrf_tiled_on_ ? 1 : 0);
             });
         } else {
             launch("potrf", [&] {
                 launch_pdl(potrf3_kernel<T>, dim3(n), dim3(256), (size_t)smem, 1, ctx_, (const int*)pivots,
                            (const int*)clusters, n, smem / (int)sizeof(T),
                            strips ? tri.smem / (32 * (int)sizeof(T)) : 0,
-                           pc_cs > 0 ? (const int*)pc_fallback_ : nullptr, 0);
+                           pc_cs > 0 ? (const int*)pc_fallback_ : nullptr, 0, potrf_tiled_on_ ? 1 : 0);
             });
         }
         if (strips)
@@ -5863,6 +6068,9 @@ class DeviceFactor : public DeviceFactorBase {
     bool pdl_on_ = !(getenv("SPAND_PDL") && atoi(getenv("SPAND_PDL")) == 0);
     // SPAND_POTRF_SMALL=0: the pivots of at most 32 rows on the one-CTA kernel as well
     bool potrf_small_on_ = !(getenv("SPAND_POTRF_SMALL") && atoi(getenv("SPAND_POTRF_SMALL")) == 0);
+    // register-tiled products in the one-CTA Cholesky and inverse (SPAND_POTRF_TILED=0: one
+    // element per thread)
+    bool potrf_tiled_on_ = !(getenv("SPAND_POTRF_TILED") && atoi(getenv("SPAND_POTRF_TILED")) == 0);
     // measured QRCP tuning: the factorization after tune_qrcp() times every wave's
     // candidates (SPAND_QC_TUNE=0: the launch model's choice only); the winners are kept per
     // plan fingerprint for the process (trees of the same plan skip the measurement)
