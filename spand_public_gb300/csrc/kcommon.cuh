@@ -83,6 +83,27 @@ __device__ __forceinline__ T dsqrt(T x) {
     return sqrt(x);
 }
 
+// 1 / sqrt(x): the hardware reciprocal square root in FP32 (a few ulp), correctly rounded
+// sqrt and division in FP64
+__device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double rsqrt_t(double x) { return 1.0 / sqrt(x); }
+
+// four consecutive elements from shared memory, p aligned to four elements (16-byte loads)
+__device__ __forceinline__ void lds4(const float* p, float (&x)[4]) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    x[0] = v.x;
+    x[1] = v.y;
+    x[2] = v.z;
+    x[3] = v.w;
+}
+__device__ __forceinline__ void lds4(const double* p, double (&x)[4]) {
+    const double2 v0 = *reinterpret_cast<const double2*>(p), v1 = *reinterpret_cast<const double2*>(p + 2);
+    x[0] = v0.x;
+    x[1] = v0.y;
+    x[2] = v1.x;
+    x[3] = v1.y;
+}
+
 // ------------------------------------------------------------------------------------
 // Block reductions (fixed order, deterministic)
 // ------------------------------------------------------------------------------------

@@ -128,32 +128,36 @@ __device__ bool chol_blocked(T* A, int ld, int n, int* bad) {
 }
 
 // The 32x32 diagonal block of a panel (rows and columns jb..jb+w-1 of a block held in shared
-// memory, ld = n), by the first warp: Cholesky in registers, lane i holding row i (a[k] =
-// A[i][k], k <= i), right-looking with the columns broadcast by shuffles (the same
-// operations per element, in the same order, as a column-by-column update); then its
-// inverse D by forward substitution, column c = lane in registers: D[r][c] = (delta_rc -
-// sum_{l<r} L[r][l] D[l][c]) / L[r][r].  D goes transposed into the block's strictly upper
-// slots (A[(jb+c) + (jb+r)*n] = D[r][c], r > c) and row-major into Dpad (zero above the
-// diagonal and outside w) for the rows below.  Sets *bad on a non-positive pivot.
+// memory with leading dimension ld), by the first warp.  Cholesky in registers, lane i
+// holding row i (a[k] = A[i][k], k <= i), right-looking with the columns broadcast by
+// shuffles; each step scales by r = 1/sqrt(pivot) (L[j][j] = pivot * r, the column below
+// times r), and lane j keeps r = 1/L[j][j].  Then the inverse D, column c = lane in registers,
+// by forward substitution, D[r][c] = (delta_rc - sum_{l<r} L[r][l] D[l][c]) / L[r][r], each
+// sum in four interleaved partial sums (a quarter of the dependent chain; the L[r][l] are
+// broadcast loads) and the division a product with 1/L[r][r].  D goes transposed into the block's strictly upper slots (A[(jb+c) + (jb+r)*ld] = D[r][c],
+// r > c) and row-major into Dpad (zero above the diagonal and outside w) for the rows
+// below.  Sets *bad on a non-positive pivot.
 template <typename T>
-__device__ void chol_diag32(T* A, int n, int jb, int w, T* Dpad, int* bad) {
+__device__ void chol_diag32(T* A, int ld, int jb, int w, T* Dpad, int* bad) {
     const int lane = threadIdx.x & 31;
     T a[PNB];
 #pragma unroll
-    for (int k = 0; k < PNB; k++) a[k] = (k <= lane && lane < w) ? A[(jb + lane) + (jb + k) * n] : T(0);
+    for (int k = 0; k < PNB; k++) a[k] = (k <= lane && lane < w) ? A[(jb + lane) + (jb + k) * ld] : T(0);
     int fail = 0;
+    T rl = T(1);  // 1 / L[lane][lane]
 #pragma unroll
     for (int j = 0; j < PNB; j++) {
         if (j < w) {
-            T d = __shfl_sync(0xffffffffu, a[j], j);
-            if (!(d > T(0))) {
-                fail = 1;
-                d = T(1);
-            } else {
-                d = dsqrt(d);
+            const T t = __shfl_sync(0xffffffffu, a[j], j);
+            T r = T(1);
+            if (!(t > T(0))) fail = 1;
+            else r = rsqrt_t(t);
+            if (lane == j) {
+                a[j] = t * r;
+                rl = r;
+            } else if (lane > j) {
+                a[j] *= r;
             }
-            if (lane == j) a[j] = d;
-            else if (lane > j) a[j] /= d;
             const T lij = a[j];
 #pragma unroll
             for (int k = j + 1; k < PNB; k++) {
@@ -165,7 +169,7 @@ __device__ void chol_diag32(T* A, int n, int jb, int w, T* Dpad, int* bad) {
     if (lane < w)
 #pragma unroll
         for (int k = 0; k < PNB; k++)
-            if (k <= lane) A[(jb + lane) + (jb + k) * n] = a[k];
+            if (k <= lane) A[(jb + lane) + (jb + k) * ld] = a[k];
     __syncwarp();
     if (lane == 0 && fail) *bad = 1;
     if (fail) return;
@@ -174,15 +178,20 @@ __device__ void chol_diag32(T* A, int n, int jb, int w, T* Dpad, int* bad) {
     for (int r = 0; r < PNB; r++) {
         d[r] = T(0);
         if (r < w) {
-            T acc = r == lane ? T(1) : T(0);
+            T s0 = r == lane ? T(1) : T(0), s1 = T(0), s2 = T(0), s3 = T(0);
 #pragma unroll
-            for (int l = 0; l < r; l++) acc -= A[(jb + r) + (jb + l) * n] * d[l];
-            d[r] = acc / A[(jb + r) + (jb + r) * n];
+            for (int l = 0; l < r; l += 4) {
+                s0 -= A[(jb + r) + (jb + l) * ld] * d[l];
+                if (l + 1 < r) s1 -= A[(jb + r) + (jb + l + 1) * ld] * d[l + 1];
+                if (l + 2 < r) s2 -= A[(jb + r) + (jb + l + 2) * ld] * d[l + 2];
+                if (l + 3 < r) s3 -= A[(jb + r) + (jb + l + 3) * ld] * d[l + 3];
+            }
+            d[r] = ((s0 + s1) + (s2 + s3)) * __shfl_sync(0xffffffffu, rl, r);
         }
     }
 #pragma unroll
     for (int r = 0; r < PNB; r++) {
-        if (r < w && r > lane) A[(jb + lane) + (jb + r) * n] = d[r];
+        if (r < w && r > lane) A[(jb + lane) + (jb + r) * ld] = d[r];
         Dpad[r * (PNB + 1) + lane] = d[r];
     }
 }
@@ -268,26 +277,34 @@ __device__ bool chol_inv_smem(T* A, int n, int* bad, T* Dpad) {
     return true;
 }
 
-// The same factorization and inverse, same layout and results up to rounding, with every
-// product of the panels on register tiles: a thread holds 4 rows x 4 columns of the output
-// (8 column groups x 32 row groups over the 256 threads), so each pair of shared-memory
-// loads feeds four multiply-adds instead of one and sixteen independent sums are in flight.
-// (1) the panel's left-looking update, rows jb..n-1 in passes of 128; (3) the rows below
-// times D^T; then per block row I of L^{-1}: (a) E = L[I][0:i0] L^{-1}[0:i0][0:i0] on tiles
-// of E into the block's upper slots, (b) L^{-1}[I][0:i0] = -D_I E on tiles, read into
-// registers, a barrier, then written over E (the tiles of one pass cover disjoint column
-// groups from the next pass's).  Loads past the last row are clamped to row n-1 (or stay
-// inside the n x n block by construction) and never written back.
+// Elements of a pivot block of n rows held in shared memory by chol_inv_tiled: leading
+// dimension n rounded up to a multiple of four, so that four consecutive rows starting at a
+// multiple of four are one 16-byte load
+__host__ __device__ inline int potrf_ld(int n) { return (n + 3) & ~3; }
+constexpr int POTRF_SMEM_MAX = 216 * 1024;  // dynamic shared memory of potrf3_kernel at most
+__host__ __device__ inline long long potrf_held(int n) { return (long long)potrf_ld(n) * n; }
+
+// The same factorization and inverse, same layout (leading dimension ld = potrf_ld(n)) and
+// results up to rounding, with every product of the panels on register tiles: a thread
+// holds 4 rows x 4 columns of the output (8 column groups x 32 row groups over the 256
+// threads) and reads each group of four rows or columns as one 16-byte load, so two loads
+// feed sixteen multiply-adds and sixteen independent sums are in flight.  (1) the panel's
+// left-looking update, rows jb..n-1 in passes of 128; (3) the rows below times D^T; then per
+// block row I of L^{-1}: (a) E = L[I][0:i0] L^{-1}[0:i0][0:i0] on tiles of E into the block's
+// upper slots, a thread taking column group g and, past 32 groups, its mirror (the sums
+// shorten with the column, so the pair's work is even); (b) L^{-1}[I][0:i0] = -D_I E on
+// tiles, read into registers, a barrier, then written over E (the tiles of one pass cover
+// disjoint column groups from the next pass's).  Rows between n and ld are read as padding
+// and never written back.
 template <typename T>
-__device__ bool chol_inv_tiled(T* A, int n, int* bad, T* Dpad) {
+__device__ bool chol_inv_tiled(T* A, int n, int ld, int* bad, T* Dpad) {
     const int tid = threadIdx.x;
     const int cq = tid & 7, rq = tid >> 3;  // the thread's 4-column group and 4-row group
     const int c0 = 4 * cq;
     const int nb = (n + PNB - 1) / PNB;
     for (int pb = 0; pb < nb; pb++) {
         const int jb = pb * PNB, w = min(PNB, n - jb);
-        // (1) A[i][jb+jj] -= sum_{k < jb} L[i][k] L[jb+jj][k], i >= jb + jj.  Rows r0+u <= n+2
-        // and columns jb+c0+v <= n+2 at k <= n-2 stay below n*n (n > 32 here).
+        // (1) A[i][jb+jj] -= sum_{k < jb} L[i][k] L[jb+jj][k], i >= jb + jj
         if (jb > 0) {
             for (int r0 = jb + 4 * rq; r0 < n; r0 += 128) {
                 if (r0 + 3 < jb + c0 || c0 >= w) continue;  // above the diagonal or right of the panel
@@ -301,10 +318,8 @@ __device__ bool chol_inv_tiled(T* A, int n, int* bad, T* Dpad) {
 #pragma unroll 2
                 for (int k = 0; k < jb; k++) {
                     T a[4], b[4];
-#pragma unroll
-                    for (int u = 0; u < 4; u++) a[u] = pa[u + k * n];
-#pragma unroll
-                    for (int v = 0; v < 4; v++) b[v] = pbk[v + k * n];
+                    lds4(pa + k * ld, a);
+                    lds4(pbk + k * ld, b);
 #pragma unroll
                     for (int u = 0; u < 4; u++)
 #pragma unroll
@@ -315,13 +330,13 @@ __device__ bool chol_inv_tiled(T* A, int n, int* bad, T* Dpad) {
 #pragma unroll
                     for (int v = 0; v < 4; v++) {
                         const int i = r0 + u, jj = c0 + v;
-                        if (i < n && jj < w && i >= jb + jj) A[i + (jb + jj) * n] -= acc[u][v];
+                        if (i < n && jj < w && i >= jb + jj) A[i + (jb + jj) * ld] -= acc[u][v];
                     }
             }
             __syncthreads();
         }
         // (2) diagonal block and its inverse
-        if (tid < 32) chol_diag32(A, n, jb, w, Dpad, bad);
+        if (tid < 32) chol_diag32(A, ld, jb, w, Dpad, bad);
         __syncthreads();
         if (*bad) return false;
         // (3) rows below: L[i][jb+c] = sum_{l <= c} A[i][jb+l] D[c][l] (Dpad zero above its
@@ -337,13 +352,9 @@ __device__ bool chol_inv_tiled(T* A, int n, int* bad, T* Dpad) {
                 for (int v = 0; v < 4; v++) acc[u][v] = T(0);
             if (act) {
                 const int lmax = min(c0 + 3, w - 1);
-                int ro[4];
-#pragma unroll
-                for (int u = 0; u < 4; u++) ro[u] = min(r0 + u, n - 1);
                 for (int l = 0; l <= lmax; l++) {
                     T a[4], d[4];
-#pragma unroll
-                    for (int u = 0; u < 4; u++) a[u] = A[ro[u] + (jb + l) * n];
+                    lds4(A + r0 + (jb + l) * ld, a);
 #pragma unroll
                     for (int v = 0; v < 4; v++) d[v] = Dpad[(c0 + v) * (PNB + 1) + l];
 #pragma unroll
@@ -358,81 +369,80 @@ __device__ bool chol_inv_tiled(T* A, int n, int* bad, T* Dpad) {
                 for (int u = 0; u < 4; u++)
 #pragma unroll
                     for (int v = 0; v < 4; v++)
-                        if (r0 + u < n && c0 + v < w) A[(r0 + u) + (jb + c0 + v) * n] = acc[u][v];
+                        if (r0 + u < n && c0 + v < w) A[(r0 + u) + (jb + c0 + v) * ld] = acc[u][v];
         }
         __syncthreads();
     }
-    // off-diagonal blocks of L^{-1}, block row by block row; tile t: row group t & 7 (rows
-    // i0+4(t&7)..+3 of the block), column group t >> 3 (columns 4(t>>3)..+3 < i0)
+    // off-diagonal blocks of L^{-1}, block row by block row; a tile is a row group q = 4 *
+    // (0..7) (rows i0+q..+3 of the block) and a column group j0 = 4 * g (columns j0..j0+3 < i0)
     for (int ib = 1; ib < nb; ib++) {
         const int i0 = ib * PNB, h = min(PNB, n - i0);
-        const int ntile = 2 * i0;  // 8 row groups x i0/4 column groups
-        // (a) E[ii][j] = sum_{j <= m < i0} L[i0+ii][m] Linv[m][j] -> A[j + (i0+ii)*n]
-        for (int t = tid; t < ntile; t += blockDim.x) {
-            const int q = 4 * (t & 7), j0 = 4 * (t >> 3);
-            int ro[4];
-#pragma unroll
-            for (int u = 0; u < 4; u++) ro[u] = min(i0 + q + u, n - 1);
-            T acc[4][4];
-#pragma unroll
-            for (int u = 0; u < 4; u++)
-#pragma unroll
-                for (int v = 0; v < 4; v++) acc[u][v] = T(0);
-            // m = j0..j0+3: Linv[m][j0+v] is 0 above its diagonal and 1 / L[m][m] on it
-#pragma unroll
-            for (int mm = 0; mm < 4; mm++) {
-                const int m = j0 + mm;
-                const T rd = T(1) / A[m + m * n];
-                T a[4], b[4];
-#pragma unroll
-                for (int u = 0; u < 4; u++) a[u] = A[ro[u] + m * n];
-#pragma unroll
-                for (int v = 0; v < 4; v++) b[v] = mm < v ? T(0) : (mm == v ? rd : A[(j0 + v) + m * n]);
+        const int ng = i0 / 4;  // column groups
+        const int q = 4 * (tid & 7);
+        // (a) E[ii][j] = sum_{j <= m < i0} L[i0+ii][m] Linv[m][j] -> A[j + (i0+ii)*ld]
+        if (q < h) {
+            for (int pass = 0; pass < 2; pass++) {
+                const int g = pass == 0 ? (tid >> 3) : ng - 1 - (tid >> 3);
+                if (g >= ng || (pass == 1 && g < 32)) break;
+                const int j0 = 4 * g;
+                T acc[4][4];
 #pragma unroll
                 for (int u = 0; u < 4; u++)
 #pragma unroll
-                    for (int v = 0; v < 4; v++) acc[u][v] += a[u] * b[v];
-            }
+                    for (int v = 0; v < 4; v++) acc[u][v] = T(0);
+                // m = j0..j0+3: Linv[m][j0+v] is 0 above its diagonal and 1 / L[m][m] on it
+#pragma unroll
+                for (int mm = 0; mm < 4; mm++) {
+                    const int m = j0 + mm;
+                    const T rd = T(1) / A[m + m * ld];
+                    T a[4], b[4];
+                    lds4(A + i0 + q + m * ld, a);
+#pragma unroll
+                    for (int v = 0; v < 4; v++) b[v] = mm < v ? T(0) : (mm == v ? rd : A[(j0 + v) + m * ld]);
+#pragma unroll
+                    for (int u = 0; u < 4; u++)
+#pragma unroll
+                        for (int v = 0; v < 4; v++) acc[u][v] += a[u] * b[v];
+                }
 #pragma unroll 2
-            for (int m = j0 + 4; m < i0; m++) {
-                T a[4], b[4];
+                for (int m = j0 + 4; m < i0; m++) {
+                    T a[4], b[4];
+                    lds4(A + i0 + q + m * ld, a);
+                    lds4(A + j0 + m * ld, b);
 #pragma unroll
-                for (int u = 0; u < 4; u++) a[u] = A[ro[u] + m * n];
+                    for (int u = 0; u < 4; u++)
 #pragma unroll
-                for (int v = 0; v < 4; v++) b[v] = A[(j0 + v) + m * n];
+                        for (int v = 0; v < 4; v++) acc[u][v] += a[u] * b[v];
+                }
 #pragma unroll
                 for (int u = 0; u < 4; u++)
+                    if (q + u < h)
 #pragma unroll
-                    for (int v = 0; v < 4; v++) acc[u][v] += a[u] * b[v];
+                        for (int v = 0; v < 4; v++) A[(j0 + v) + (i0 + q + u) * ld] = acc[u][v];
             }
-#pragma unroll
-            for (int u = 0; u < 4; u++)
-                if (q + u < h)
-#pragma unroll
-                    for (int v = 0; v < 4; v++) A[(j0 + v) + (i0 + q + u) * n] = acc[u][v];
         }
         __syncthreads();
         // (b) Linv[i0+ii][j] = -(E[ii][j] / L[i0+ii][i0+ii] + sum_{l < ii} D[ii][l] E[l][j]),
-        // D[ii][l] = A[(i0+l) + (i0+ii)*n]
+        // D[ii][l] = A[(i0+l) + (i0+ii)*ld]; column group g = t >> 3 of tile t
+        const int ntile = 8 * ng;
         for (int t0 = 0; t0 < ntile; t0 += blockDim.x) {
             const int t = t0 + tid;
-            const bool act = t < ntile;
-            const int q = 4 * (t & 7), j0 = 4 * (t >> 3);
+            const bool act = t < ntile && q < h;
+            const int j0 = 4 * (t >> 3);
             T o[4][4];
 #pragma unroll
             for (int u = 0; u < 4; u++)
 #pragma unroll
                 for (int v = 0; v < 4; v++) o[u][v] = T(0);
-            if (act && q < h) {
+            if (act) {
                 int co[4];
 #pragma unroll
-                for (int u = 0; u < 4; u++) co[u] = min(i0 + q + u, n - 1) * n;
+                for (int u = 0; u < 4; u++) co[u] = min(i0 + q + u, n - 1) * ld;
                 for (int l = 0; l < q; l++) {  // below every row of the group: D[q+u][l] stored
                     T d[4], e[4];
 #pragma unroll
                     for (int u = 0; u < 4; u++) d[u] = A[(i0 + l) + co[u]];
-#pragma unroll
-                    for (int v = 0; v < 4; v++) e[v] = A[(j0 + v) + (i0 + l) * n];
+                    lds4(A + j0 + (i0 + l) * ld, e);
 #pragma unroll
                     for (int u = 0; u < 4; u++)
 #pragma unroll
@@ -445,9 +455,8 @@ __device__ bool chol_inv_tiled(T* A, int n, int* bad, T* Dpad) {
                         T d[4], e[4];
 #pragma unroll
                         for (int u = 0; u < 4; u++)
-                            d[u] = ll < u ? A[(i0 + l) + co[u]] : (ll == u ? T(1) / A[(i0 + l) + (i0 + l) * n] : T(0));
-#pragma unroll
-                        for (int v = 0; v < 4; v++) e[v] = A[(j0 + v) + (i0 + l) * n];
+                            d[u] = ll < u ? A[(i0 + l) + co[u]] : (ll == u ? T(1) / A[(i0 + l) + (i0 + l) * ld] : T(0));
+                        lds4(A + j0 + (i0 + l) * ld, e);
 #pragma unroll
                         for (int u = 0; u < 4; u++)
 #pragma unroll
@@ -461,7 +470,7 @@ __device__ bool chol_inv_tiled(T* A, int n, int* bad, T* Dpad) {
                 for (int u = 0; u < 4; u++)
                     if (q + u < h)
 #pragma unroll
-                        for (int v = 0; v < 4; v++) A[(j0 + v) + (i0 + q + u) * n] = -o[u][v];
+                        for (int v = 0; v < 4; v++) A[(j0 + v) + (i0 + q + u) * ld] = -o[u][v];
         }
         __syncthreads();
     }
@@ -494,15 +503,16 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) potrf3_kernel(Ctx
     T* G = bptr(c, pivots[item]);
     const int gld = c.blk[pivots[item]].ld;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = blockDim.x >> 5;
-    if ((long long)n * n <= smem_elems) {
+    if (potrf_held(n) <= smem_elems) {
+        const int ld = tiled ? potrf_ld(n) : n;
         for (int j = ty; j < n; j += nty)
-            for (int i = j + tx; i < n; i += 32) sm[i + j * n] = G[i + (size_t)j * gld];
+            for (int i = j + tx; i < n; i += 32) sm[i + j * ld] = G[i + (size_t)j * gld];
         __syncthreads();
         // factor and inverse together; the whole block (L below, L^{-1} transposed above) back
         __shared__ T Dpad[PNB * (PNB + 1)];  // inverse of the current diagonal block, padded rows
-        if (tiled ? chol_inv_tiled(sm, n, &bad, Dpad) : chol_inv_smem(sm, n, &bad, Dpad)) {
+        if (tiled ? chol_inv_tiled(sm, n, ld, &bad, Dpad) : chol_inv_smem(sm, n, &bad, Dpad)) {
             for (int j = ty; j < n; j += nty)
-                for (int i = tx; i < n; i += 32) G[i + (size_t)j * gld] = sm[i + j * n];
+                for (int i = tx; i < n; i += 32) G[i + (size_t)j * gld] = sm[i + j * ld];
         }
     } else {
         chol_blocked(G, gld, n, &bad);
@@ -654,58 +664,9 @@ __global__ void __launch_bounds__(PC_THREADS) potrf_cluster_kernel(Ctx<T> c, con
         const int r0 = 32 * p, ldp = n - r0, w = min(32, n - r0);
         if (owner == me) {
             T* P = sm + poff(p);
-            if (tid < 32) {
-                // the diagonal block in registers, lane i holding row i (a[k] = A[i][k], k <= i):
-                // right-looking Cholesky with the columns broadcast by shuffles, then
-                // D = L^{-1} by forward substitution, lane = column (L read back from P)
-                T a[32];
-#pragma unroll
-                for (int k = 0; k < 32; k++) a[k] = (k <= tid && tid < w) ? P[tid + (size_t)k * ldp] : T(0);
-                int fail = 0;
-#pragma unroll
-                for (int j = 0; j < 32; j++) {
-                    if (j < w) {
-                        T d = __shfl_sync(0xffffffffu, a[j], j);
-                        if (!(d > T(0))) {
-                            fail = 1;
-                            d = T(1);
-                        } else {
-                            d = dsqrt(d);
-                        }
-                        if (tid == j) a[j] = d;
-                        else if (tid > j) a[j] /= d;
-                        const T lij = a[j];
-#pragma unroll
-                        for (int k = j + 1; k < 32; k++) {
-                            const T lkj = __shfl_sync(0xffffffffu, a[j], k);
-                            if (tid > j && k <= tid) a[k] -= lij * lkj;
-                        }
-                    }
-                }
-                if (tid < w)
-#pragma unroll
-                    for (int k = 0; k < 32; k++)
-                        if (k <= tid) P[tid + (size_t)k * ldp] = a[k];
-                __syncwarp();
-                // column c = tid of D: D[r][c] = (delta_rc - sum_{c <= l < r} L[r][l] D[l][c]) / L[r][r]
-                T dcol[32];
-#pragma unroll
-                for (int r = 0; r < 32; r++) {
-                    dcol[r] = T(0);
-                    if (r < w && r >= tid) {
-                        T acc0 = r == tid ? T(1) : T(0), acc1 = T(0);
-#pragma unroll
-                        for (int l = 0; l < r; l += 2) {
-                            if (l >= tid) acc0 -= P[r + (size_t)l * ldp] * dcol[l];
-                            if (l + 1 < r && l + 1 >= tid) acc1 -= P[r + (size_t)(l + 1) * ldp] * dcol[l + 1];
-                        }
-                        dcol[r] = (acc0 + acc1) / P[r + (size_t)r * ldp];
-                    }
-                }
-#pragma unroll
-                for (int r = 0; r < 32; r++) Dpc[r * 33 + tid] = dcol[r];  // Dpc[r][c] = D[r][c]
-                if (tid == 0 && fail) bad = 1;
-            }
+            // the diagonal block and its inverse D (into Dpc; D^T also lands in the panel's
+            // upper slots, which are not copied back)
+            if (tid < 32) chol_diag32(P, ldp, 0, w, Dpc, &bad);
             __syncthreads();
             // rows below: L[t][j] = sum_{l <= j} A[t][l] D[j][l], a warp per four rows, lane = j
             if (!bad) {
@@ -820,9 +781,9 @@ __global__ void __launch_bounds__(256) trtri_kernel(Ctx<T> c, const int* __restr
     const int cl = clusters[item];
     const int n = c.csize[cl];
     const int jb = tiles[t].tile_i * 32;
-    // pivots inverted by potrf3_kernel: those it held in shared memory (n^2 <= skip_n2) and
-    // the large ones
-    if (jb >= n || (long long)n * n <= skip_n2 || (long long)n * 32 > smem_elems) return;
+    // pivots inverted by potrf3_kernel: those it held in shared memory (potrf_held(n) <=
+    // skip_n2) and the large ones
+    if (jb >= n || potrf_held(n) <= skip_n2 || (long long)n * 32 > smem_elems) return;
     const int w = min(32, n - jb);
     T* A = bptr(c, pivots[item]);
     const int ld = c.blk[pivots[item]].ld;
@@ -4226,7 +4187,7 @@ class DeviceFactor : public DeviceFactorBase {
             d_perm_ = up(perm_h_);
         }
         ctx_ = Ctx<T>{arena_, d_blk_, csize_, rows0_, d_cap_, status_};
-        SPAND_CUDA(cudaFuncSetAttribute(potrf3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SPAND_CUDA(cudaFuncSetAttribute(potrf3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, POTRF_SMEM_MAX));
         SPAND_CUDA(cudaFuncSetAttribute(trtri_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(trsm3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         if (ldlt_) {
@@ -4378,6 +4339,7 @@ class DeviceFactor : public DeviceFactorBase {
                 launch_schur(D.schur_targets, d_ups_, D.schur_tiles, D.n_schur_tiles);
             }
             if (D.scaled && D.n_scale) {
+                scale_phase_ = true;
                 if (lu_) {
                     launch_getrf(D.scale_pivots, D.scale_inv, D.scale_clusters, D.n_scale, D.scale_lu_smem);
                     launch_lu_trsm(D.scale_trsm0);
@@ -4402,6 +4364,7 @@ class DeviceFactor : public DeviceFactorBase {
                         preserve_scale<T>(ctx_, phictx(), phitmp_, D.scale_clusters, D.scale_pivots, D.n_scale,
                                           ldlt_ ? lu_perm_ : nullptr, d_xoff_, s_);
                     });
+                scale_phase_ = false;
             }
             if (D.n_level)
                 launch("snapshot", [&] {
@@ -5109,7 +5072,7 @@ class DeviceFactor : public DeviceFactorBase {
     template <typename F>
     void launch(const char* cls, F&& f, int kernels = 1) {
         if (prof_.enabled() && per_level_ && cur_level_ >= 0) {
-            std::string name = std::string(cls) + "@L" + std::to_string(cur_level_);
+            std::string name = std::string(cls) + (scale_phase_ ? "@S" : "@L") + std::to_string(cur_level_);
             if (per_wave_ && cur_wave_ >= 0) name += "w" + std::to_string(cur_wave_);
             prof_.begin(s_, name.c_str());
         } else {
@@ -5744,8 +5707,8 @@ class DeviceFactor : public DeviceFactorBase {
     }
     // shared memory of the POTRF kernel for pivots of size up to nmax: whole block, else one panel
     static int potrf_smem_n(int nmax) {
-        int64_t full = (int64_t)nmax * nmax * sizeof(T);
-        return full <= 200 * 1024 ? (int)std::max<int64_t>(full, 16) : 0;
+        int64_t full = potrf_held(nmax) * (int64_t)sizeof(T);
+        return full <= POTRF_SMEM_MAX ? (int)std::max<int64_t>(full, 16) : 0;
     }
     // the strip (32 columns) and, where it fits, the staged row-block tile (33 columns)
     static int trtri_smem_n(int nmax) {
@@ -6095,6 +6058,7 @@ class DeviceFactor : public DeviceFactorBase {
     double fgraph_tol_ = -1.0;
     int fgraph_nphi_ = -1;
     int cur_level_ = -1;
+    bool scale_phase_ = false;  // the level's scaling pivots (per-level profile names "@S")
     // in-kernel phase timing of the QRCP of one level (SPAND_QC_PROBE=<level>)
     // per-level kernel classes in the profile (SPAND_PROFILE_LEVELS=1)
     bool per_level_ = getenv("SPAND_PROFILE_LEVELS") != nullptr;
