@@ -649,9 +649,20 @@ __global__ void __launch_bounds__(PC_THREADS) potrf_cluster_kernel(Ctx<T> c, con
     for (int p = me; p < np; p += CS) {
         T* P = sm + own;
         const int r0 = 32 * p, ldp = n - r0, w = min(32, n - r0);
-        for (int idx = tid; idx < ldp * w; idx += PC_THREADS) {
-            const int t = idx % ldp, j = idx / ldp;
-            if (t >= j) P[t + (size_t)j * ldp] = G[(r0 + t) + (size_t)(r0 + j) * gld];
+        // the panel's rows x w columns (the entries above the diagonal block's diagonal are
+        // scratch), eight loads in flight per thread before their stores
+        for (int base = 0; base < ldp * w; base += 8 * PC_THREADS) {
+            T v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int idx = base + tid + PC_THREADS * u;
+                v[u] = idx < ldp * w ? G[(r0 + idx % ldp) + (size_t)(r0 + idx / ldp) * gld] : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int idx = base + tid + PC_THREADS * u;
+                if (idx < ldp * w) P[idx] = v[u];  // P[t + j * ldp] with idx = t + j * ldp
+            }
         }
         own += (long long)ldp * 32;
     }
@@ -697,9 +708,24 @@ __global__ void __launch_bounds__(PC_THREADS) potrf_cluster_kernel(Ctx<T> c, con
         if (rs >= n) continue;
         const int ls = n - rs;
         const T* Pp = cl.map_shared_rank(sm, owner) + poff(p);
-        for (int idx = tid; idx < ls * w; idx += PC_THREADS) {
-            const int t = idx % ls, k = idx / ls;
-            S[t + (size_t)k * ls] = Pp[(rs - r0 + t) + (size_t)k * ldp];
+        // eight distributed-shared-memory loads in flight per thread before their stores (the
+        // compiler keeps a load behind an earlier store it cannot tell apart from it)
+        for (int base = 0; base < ls * w; base += 8 * PC_THREADS) {
+            T v[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const int idx = base + tid + PC_THREADS * j;
+                v[j] = T(0);
+                if (idx < ls * w) {
+                    const int t = idx % ls, k = idx / ls;
+                    v[j] = Pp[(rs - r0 + t) + (size_t)k * ldp];
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const int idx = base + tid + PC_THREADS * j;
+                if (idx < ls * w) S[idx] = v[j];  // S[t + k * ls] with idx = t + k * ls
+            }
         }
         __syncthreads();
         const int rg = tid >> 3, cg = tid & 7;
@@ -799,9 +825,19 @@ __global__ void __launch_bounds__(256) trtri_kernel(Ctx<T> c, const int* __restr
         // L[i][k] once for its TRI_COLS columns jj = ty + nty u; the tile is first copied to
         // shared memory by the whole CTA (coalesced, many loads in flight)
         if (stage && kw > 0) {
-            for (int idx = threadIdx.x; idx < 32 * kw; idx += blockDim.x) {
-                const int r = idx & 31, k = idx >> 5;
-                Lt[r + 33 * k] = r < h ? A[(ib + r) + (size_t)(jb + k) * ld] : T(0);
+            // eight loads in flight per thread before their stores
+            for (int base = 0; base < 32 * kw; base += 8 * 256) {
+                T v[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const int idx = base + threadIdx.x + 256 * u, r = idx & 31, k = idx >> 5;
+                    v[u] = (idx < 32 * kw && r < h) ? A[(ib + r) + (size_t)(jb + k) * ld] : T(0);
+                }
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const int idx = base + threadIdx.x + 256 * u;
+                    if (idx < 32 * kw) Lt[(idx & 31) + 33 * (idx >> 5)] = v[u];
+                }
             }
             __syncthreads();
         }
@@ -831,7 +867,7 @@ __global__ void __launch_bounds__(256) trtri_kernel(Ctx<T> c, const int* __restr
 #pragma unroll
         for (int r = 0; r < 32; r++)
             lrow[r] = (tx < h && r < tx) ? A[(ib + tx) + (size_t)(ib + r) * ld] : T(0);
-        const T dii = tx < h ? A[(ib + tx) + (size_t)(ib + tx) * ld] : T(1);
+        const T rdii = tx < h ? T(1) / A[(ib + tx) + (size_t)(ib + tx) * ld] : T(1);
         T acc[TRI_COLS];
 #pragma unroll
         for (int u = 0; u < TRI_COLS; u++) {
@@ -843,7 +879,7 @@ __global__ void __launch_bounds__(256) trtri_kernel(Ctx<T> c, const int* __restr
             if (r < h) {
 #pragma unroll
                 for (int u = 0; u < TRI_COLS; u++) {
-                    const T yr = __shfl_sync(0xffffffffu, acc[u] / dii, r);
+                    const T yr = __shfl_sync(0xffffffffu, acc[u] * rdii, r);
                     if (tx == r) acc[u] = yr;
                     else acc[u] -= lrow[r] * yr;
                 }
