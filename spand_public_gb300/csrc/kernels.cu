@@ -282,6 +282,9 @@ __device__ bool chol_inv_smem(T* A, int n, int* bad, T* Dpad) {
 // multiple of four are one 16-byte load
 __host__ __device__ inline int potrf_ld(int n) { return (n + 3) & ~3; }
 constexpr int POTRF_SMEM_MAX = 216 * 1024;  // dynamic shared memory of potrf3_kernel at most
+// above this, a level's one-CTA Cholesky is launched per size class (three CTAs of 256
+// threads per SM fit beside it)
+constexpr int POTRF_MID_SMEM = 68 * 1024;
 __host__ __device__ inline long long potrf_held(int n) { return (long long)potrf_ld(n) * n; }
 
 // The same factorization and inverse, same layout (leading dimension ld = potrf_ld(n)) and
@@ -483,7 +486,7 @@ template <typename T>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) potrf3_kernel(Ctx<T> c, const int* __restrict__ pivots,
                                                      const int* __restrict__ clusters, int count, int smem_elems,
                                                      int strip_max_n, const int* __restrict__ only,
-                                                     int small_cap, int tiled) {
+                                                     int small_cap, int tiled, int n_lo, int n_hi) {
     pdl_wait_and_release();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
@@ -500,6 +503,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) potrf3_kernel(Ctx
     const int cl = clusters[item];
     const int n = c.csize[cl];
     if (n == 0 || c.cap[cl] <= small_cap) return;  // small pivots: potrf_small_kernel
+    if (n <= n_lo || n > n_hi) return;              // the other size class's launch
     T* G = bptr(c, pivots[item]);
     const int gld = c.blk[pivots[item]].ld;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = blockDim.x >> 5;
@@ -4368,7 +4372,7 @@ class DeviceFactor : public DeviceFactorBase {
                     launch_potrf(D.elim_pivots, D.elim_clusters, D.n_elim, D.elim_ps_piv, D.elim_ps_cl, D.n_elim_ps,
                                  D.elim_pb_piv, D.elim_pb_cl, D.n_elim_pb,
                                  D.elim_smem, D.elim_tri, D.elim_pc_cs,
-                                 D.elim_pc_smem);
+                                 D.elim_pc_smem, D.elim_split);
                     launch_trsm(D.elim_trsm0);
                     launch_trsm(D.elim_trsm1);
                 }
@@ -4387,7 +4391,7 @@ class DeviceFactor : public DeviceFactorBase {
                 } else {
                     launch_potrf(D.scale_pivots, D.scale_clusters, D.n_scale, D.scale_ps_piv, D.scale_ps_cl,
                                  D.n_scale_ps, D.scale_pb_piv, D.scale_pb_cl, D.n_scale_pb, D.scale_smem, D.scale_tri,
-                                 D.scale_pc_cs, D.scale_pc_smem);
+                                 D.scale_pc_cs, D.scale_pc_smem, D.scale_split);
                     launch_trsm(D.scale_trsm0);
                     launch_trsm(D.scale_trsm1);
                     if (lorasp_)
@@ -4603,6 +4607,8 @@ class DeviceFactor : public DeviceFactorBase {
             int ne = nmax(L.elim_clusters), ns = nmax(L.scale_clusters);
             D.elim_smem = potrf_smem_n(ne);
             D.scale_smem = potrf_smem_n(ns);
+            D.elim_split = potrf_split_pays(L.elim_clusters, r0, D.elim_smem);
+            D.scale_split = potrf_split_pays(L.scale_clusters, r0, D.scale_smem);
             choose_potrf_cluster(ne, D.elim_smem, D.n_elim, D.elim_pc_cs, D.elim_pc_smem);
             choose_potrf_cluster(ns, D.scale_smem, D.n_scale, D.scale_pc_cs, D.scale_pc_smem);
             // the strip inverse must take every pivot the cluster Cholesky holds: its shared
@@ -4872,6 +4878,7 @@ class DeviceFactor : public DeviceFactorBase {
         int n_elim_pb = 0, n_scale_pb = 0;  // the other LLT pivots
         int elim_smem = 0;
         int elim_pc_cs = 0, elim_pc_smem = 0;   // cluster Cholesky (0: single-CTA kernel)
+        bool elim_split = false;                 // one-CTA Cholesky launched per size class
         TrsmDev elim_trsm0, elim_trsm1;
         TrtriDev elim_tri, scale_tri;
         DTarget* schur_targets = nullptr;
@@ -4883,6 +4890,7 @@ class DeviceFactor : public DeviceFactorBase {
         int* scale_pivots = nullptr;
         int scale_smem = 0;
         int scale_pc_cs = 0, scale_pc_smem = 0;
+        bool scale_split = false;
         TrsmDev scale_trsm0, scale_trsm1;
         int n_level = 0;
         int* level_clusters = nullptr;
@@ -5553,7 +5561,7 @@ class DeviceFactor : public DeviceFactorBase {
     }
     void launch_potrf(int* pivots, int* clusters, int n, const int* ps_piv, const int* ps_cl, int n_ps,
                       const int* pb_piv, const int* pb_cl, int n_pb, int smem, const TrtriDev& tri, int pc_cs,
-                      int pc_smem) {
+                      int pc_smem, bool split_pays) {
         // (not beside the cluster kernel or the strip inverse, which take every pivot of the list)
         const bool small = n_ps > 0 && potrf_small_on_ && pc_cs == 0 && smem > 0;
         if (small)
@@ -5572,18 +5580,36 @@ class DeviceFactor : public DeviceFactorBase {
         const bool strips = tri.ntiles > 0 && (smem == 0 || pc_cs > 0);
         // single-CTA kernel: every pivot, or (after the cluster kernel) those it could not hold,
         // or (beside the warp kernel) the pivots of more than 32 rows only
+        // Where a few large pivots set the level's shared memory (potrf_split_pays), the pivots
+        // of at most mid_n rows run first in a launch sized for them, more CTAs per SM, then
+        // the larger ones (each launch skips the other class's pivots at once).
+        const int mid_n = potrf_mid_n();
+        const bool split = split_pays && potrf_split_on_ && pc_cs == 0 && smem > POTRF_MID_SMEM;
+        const int mid_smem = (int)(potrf_held(mid_n) * (int64_t)sizeof(T));
+        const int tiled = potrf_tiled_on_ ? 1 : 0;
         if (small && n_pb == 0) {
         } else if (small) {
+            if (split)
+                launch("potrf", [&] {
+                    launch_pdl(potrf3_kernel<T>, dim3(n_pb), dim3(256), (size_t)mid_smem, 1, ctx_, pb_piv, pb_cl, n_pb,
+                               mid_smem / (int)sizeof(T), 0, (const int*)nullptr, 0, tiled, 0, mid_n);
+                });
             launch("potrf", [&] {
                 launch_pdl(potrf3_kernel<T>, dim3(n_pb), dim3(256), (size_t)smem, 1, ctx_, pb_piv, pb_cl, n_pb,
-                           smem / (int)sizeof(T), 0, (const int*)nullptr, 0, potrf_tiled_on_ ? 1 : 0);
+                           smem / (int)sizeof(T), 0, (const int*)nullptr, 0, tiled, split ? mid_n : 0, INT_MAX);
             });
         } else {
+            const int strip_max_n = strips ? tri.smem / (32 * (int)sizeof(T)) : 0;
+            if (split)
+                launch("potrf", [&] {
+                    launch_pdl(potrf3_kernel<T>, dim3(n), dim3(256), (size_t)mid_smem, 1, ctx_, (const int*)pivots,
+                               (const int*)clusters, n, mid_smem / (int)sizeof(T), strip_max_n, (const int*)nullptr, 0,
+                               tiled, 0, mid_n);
+                });
             launch("potrf", [&] {
                 launch_pdl(potrf3_kernel<T>, dim3(n), dim3(256), (size_t)smem, 1, ctx_, (const int*)pivots,
-                           (const int*)clusters, n, smem / (int)sizeof(T),
-                           strips ? tri.smem / (32 * (int)sizeof(T)) : 0,
-                           pc_cs > 0 ? (const int*)pc_fallback_ : nullptr, 0, potrf_tiled_on_ ? 1 : 0);
+                           (const int*)clusters, n, smem / (int)sizeof(T), strip_max_n,
+                           pc_cs > 0 ? (const int*)pc_fallback_ : nullptr, 0, tiled, split ? mid_n : 0, INT_MAX);
             });
         }
         if (strips)
@@ -5742,6 +5768,35 @@ class DeviceFactor : public DeviceFactorBase {
         }
     }
     // shared memory of the POTRF kernel for pivots of size up to nmax: whole block, else one panel
+    // CTAs of the one-CTA Cholesky per SM at `smem` bytes of dynamic shared memory (its
+    // register bound: three in FP32, two in FP64)
+    int potrf_ctas_per_sm(int smem) const {
+        const int per = smem + PNB * (PNB + 1) * (int)sizeof(T) + 1024;
+        return std::max(1, std::min(sizeof(T) == 4 ? 3 : 2, (228 * 1024) / per));
+    }
+    // Size classes pay where at most eight pivots (by their sizes in the first factorization)
+    // exceed mid_n rows and the others would take fewer waves of CTAs at the smaller launch's
+    // occupancy; otherwise the second launch only adds its length (measured at 64^3: the
+    // lowest level's elimination 0.35 -> 0.27 ms; levels with tens of large pivots slower).
+    bool potrf_split_pays(const std::vector<int>& cl, const std::vector<int>& r0, int smem) const {
+        const int mid_n = potrf_mid_n();
+        int big = 0, mid = 0;
+        for (int c0 : cl) {
+            if (P_->c_cap[c0] <= 32) continue;  // the warp kernel's
+            if (r0[c0] > mid_n) big++;
+            else mid++;
+        }
+        if (big > 8 || smem <= POTRF_MID_SMEM) return false;
+        const long long full = (long long)num_sms_ * potrf_ctas_per_sm(smem);
+        const long long part = (long long)num_sms_ * potrf_ctas_per_sm((int)(potrf_held(mid_n) * (int64_t)sizeof(T)));
+        return (mid + full - 1) / full > (mid + part - 1) / part;
+    }
+    // largest pivot the size-class launch of the one-CTA Cholesky holds in POTRF_MID_SMEM
+    static int potrf_mid_n() {
+        int m = 32;
+        while (potrf_held(m + 1) * (int64_t)sizeof(T) <= POTRF_MID_SMEM) m++;
+        return m;
+    }
     static int potrf_smem_n(int nmax) {
         int64_t full = potrf_held(nmax) * (int64_t)sizeof(T);
         return full <= POTRF_SMEM_MAX ? (int)std::max<int64_t>(full, 16) : 0;
@@ -6070,6 +6125,8 @@ class DeviceFactor : public DeviceFactorBase {
     // register-tiled products in the one-CTA Cholesky and inverse (SPAND_POTRF_TILED=0: one
     // element per thread)
     bool potrf_tiled_on_ = !(getenv("SPAND_POTRF_TILED") && atoi(getenv("SPAND_POTRF_TILED")) == 0);
+    // size-class launches of the one-CTA Cholesky (SPAND_POTRF_SPLIT=0: one launch per level)
+    bool potrf_split_on_ = !(getenv("SPAND_POTRF_SPLIT") && atoi(getenv("SPAND_POTRF_SPLIT")) == 0);
     // measured QRCP tuning: the factorization after tune_qrcp() times every wave's
     // candidates (SPAND_QC_TUNE=0: the launch model's choice only); the winners are kept per
     // plan fingerprint for the process (trees of the same plan skip the measurement)
