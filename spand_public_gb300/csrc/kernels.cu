@@ -2394,12 +2394,10 @@ constexpr int TV_ROWS = 32;
 constexpr int TV_THREADS = 256;
 
 template <typename T>
-__global__ void __launch_bounds__(TV_THREADS) trsv4_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ clusters,
-                                                          const int* __restrict__ lblocks,
-                                                          const int2* __restrict__ tiles, int trans, T* tmp,
-                                                          int* counters) {
-    pdl_wait_and_release();
-    const int2 tl = tiles[blockIdx.x];
+__device__ __forceinline__ void trsv4_body(Ctx<T> c, XCtx<T> X, const int* __restrict__ clusters,
+                                           const int* __restrict__ lblocks, const int2* __restrict__ tiles,
+                                           int trans, T* tmp, int* counters, int bid) {
+    const int2 tl = tiles[bid];
     const int item = tl.x, tile = tl.y;
     const int cl = clusters[item];
     const int n = c.rows0[cl];
@@ -2476,6 +2474,15 @@ __global__ void __launch_bounds__(TV_THREADS) trsv4_kernel(Ctx<T> c, XCtx<T> X, 
     if (threadIdx.x == 0) counters[cl] = 0;
 }
 
+template <typename T>
+__global__ void __launch_bounds__(TV_THREADS) trsv4_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ clusters,
+                                                          const int* __restrict__ lblocks,
+                                                          const int2* __restrict__ tiles, int trans, T* tmp,
+                                                          int* counters) {
+    pdl_wait_and_release();
+    trsv4_body<T>(c, X, clusters, lblocks, tiles, trans, tmp, counters, blockIdx.x);
+}
+
 // The triangular products (as trsv4_kernel) of clusters of at most 64 rows, one warp per
 // cluster, eight clusters per CTA: x in registers (rows lane and lane + 32), every x_k
 // reaches the lanes by shuffle.  Forward y_i = x_i / L_ii + sum_{k<i} L^{-1}[i][k] x_k with
@@ -2484,13 +2491,11 @@ __global__ void __launch_bounds__(TV_THREADS) trsv4_kernel(Ctx<T> c, XCtx<T> X, 
 // entries of each column (coalesced).  In place: the warp holds all of x before it writes.
 constexpr int TS_WARPS = 8;
 template <typename T>
-__global__ void __launch_bounds__(32 * TS_WARPS) trsv_small_kernel(Ctx<T> c, XCtx<T> X,
-                                                                   const int* __restrict__ clusters,
-                                                                   const int* __restrict__ lblocks,
-                                                                   const int* __restrict__ idx, int count, int trans) {
-    pdl_wait_and_release();
+__device__ __forceinline__ void trsv_small_body(Ctx<T> c, XCtx<T> X, const int* __restrict__ clusters,
+                                                const int* __restrict__ lblocks, const int* __restrict__ idx,
+                                                int count, int trans, int bid) {
     const int lane = threadIdx.x & 31;
-    const int item = blockIdx.x * TS_WARPS + (threadIdx.x >> 5);
+    const int item = bid * TS_WARPS + (threadIdx.x >> 5);
     if (item >= count) return;
     const int k = idx[item];
     const int cl = clusters[k];
@@ -2561,6 +2566,31 @@ __global__ void __launch_bounds__(32 * TS_WARPS) trsv_small_kernel(Ctx<T> c, XCt
         if (ia < n) x[ia] = sa0 + sa1;
         if (ib < n) x[ib] = sb0 + sb1;
     }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32 * TS_WARPS) trsv_small_kernel(Ctx<T> c, XCtx<T> X,
+                                                                   const int* __restrict__ clusters,
+                                                                   const int* __restrict__ lblocks,
+                                                                   const int* __restrict__ idx, int count, int trans) {
+    pdl_wait_and_release();
+    trsv_small_body<T>(c, X, clusters, lblocks, idx, count, trans, blockIdx.x);
+}
+
+// Both of a phase's triangular products in one launch: the first nsb CTAs take the small
+// clusters a warp each (trsv_small_body), the others the row tiles of the larger ones
+// (trsv4_body).  The two sets of clusters are disjoint, so the halves need no order
+// between them, and the phase costs one launch instead of two.
+static_assert(32 * TS_WARPS == TV_THREADS, "one block shape for both halves");
+template <typename T>
+__global__ void __launch_bounds__(TV_THREADS) trsv_fused_kernel(Ctx<T> c, XCtx<T> X, const int* __restrict__ clusters,
+                                                               const int* __restrict__ lblocks,
+                                                               const int* __restrict__ idx, int count, int nsb,
+                                                               const int2* __restrict__ tiles, int trans, T* tmp,
+                                                               int* counters) {
+    pdl_wait_and_release();
+    if ((int)blockIdx.x < nsb) trsv_small_body<T>(c, X, clusters, lblocks, idx, count, trans, blockIdx.x);
+    else trsv4_body<T>(c, X, clusters, lblocks, tiles, trans, tmp, counters, (int)blockIdx.x - nsb);
 }
 
 // One Gemm op's operands as the solve kernels use them: the factor block, the solve
@@ -4242,6 +4272,7 @@ class DeviceFactor : public DeviceFactorBase {
         fallback_ = alloc<int>(max_items);
         items_len_ = max_items;
         SPAND_CUDA(cudaFuncSetAttribute(trsv4_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SPAND_CUDA(cudaFuncSetAttribute(trsv_fused_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(ortho_mrhs_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SPAND_CUDA(cudaFuncSetAttribute(trsv_mrhs_small_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         MRS_WARPS * MR_MAXROWS * (MR_RB + 1) * (int)sizeof(T)));
@@ -5936,10 +5967,19 @@ class DeviceFactor : public DeviceFactorBase {
                     const int nsmall = elim ? D.n_elim_small : D.n_scale_small;
                     const int2* big = elim ? D.elim_big_tv : D.scale_big_tv;
                     const int nbig = elim ? D.n_elim_big_tv : D.n_scale_big_tv;
+                    const int nsb = (nsmall + TS_WARPS - 1) / TS_WARPS;
+                    if (nsmall && nbig && trsv_fuse_on_) {
+                        launch("trsv", [&] {
+                            launch_pdl(trsv_fused_kernel<T>, dim3((unsigned)(nsb + nbig)), dim3(TV_THREADS),
+                                         (size_t)smem, 1, ctx_, X, clusters, blks, small, nsmall, nsb, big, trans, tmp,
+                                         tv_count_);
+                        });
+                        return;
+                    }
                     if (nsmall)
                         launch("trsv", [&] {
-                            launch_pdl(trsv_small_kernel<T>, dim3((nsmall + TS_WARPS - 1) / TS_WARPS),
-                                         dim3(32 * TS_WARPS), 0, 1, ctx_, X, clusters, blks, small, nsmall, trans);
+                            launch_pdl(trsv_small_kernel<T>, dim3(nsb), dim3(32 * TS_WARPS), 0, 1, ctx_, X, clusters,
+                                         blks, small, nsmall, trans);
                         });
                     if (nbig)
                         launch("trsv", [&] {
@@ -6122,6 +6162,8 @@ class DeviceFactor : public DeviceFactorBase {
     bool pdl_on_ = !(getenv("SPAND_PDL") && atoi(getenv("SPAND_PDL")) == 0);
     // SPAND_POTRF_SMALL=0: the pivots of at most 32 rows on the one-CTA kernel as well
     bool potrf_small_on_ = !(getenv("SPAND_POTRF_SMALL") && atoi(getenv("SPAND_POTRF_SMALL")) == 0);
+    // a phase's small-cluster and row-tile triangular products in one launch (SPAND_TRSV_FUSE=0: two)
+    bool trsv_fuse_on_ = !(getenv("SPAND_TRSV_FUSE") && atoi(getenv("SPAND_TRSV_FUSE")) == 0);
     // register-tiled products in the one-CTA Cholesky and inverse (SPAND_POTRF_TILED=0: one
     // element per thread)
     bool potrf_tiled_on_ = !(getenv("SPAND_POTRF_TILED") && atoi(getenv("SPAND_POTRF_TILED")) == 0);
