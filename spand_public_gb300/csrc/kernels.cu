@@ -509,8 +509,32 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) potrf3_kernel(Ctx
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = blockDim.x >> 5;
     if (potrf_held(n) <= smem_elems) {
         const int ld = tiled ? potrf_ld(n) : n;
-        for (int j = ty; j < n; j += nty)
-            for (int i = j + tx; i < n; i += 32) sm[i + j * ld] = G[i + (size_t)j * gld];
+        // the lower triangle, two columns per warp at a time with up to sixteen loads in flight
+        // per lane before their stores (a load behind a shared-memory store it may alias would
+        // otherwise wait out the previous load: one HBM latency per element a lane copies)
+        for (int j0 = ty; j0 < n; j0 += 2 * nty) {
+            for (int r = 0; r < n - j0; r += 256) {
+                T v[2][8];
+#pragma unroll
+                for (int cc = 0; cc < 2; cc++) {
+                    const int j = j0 + cc * nty;
+#pragma unroll
+                    for (int m = 0; m < 8; m++) {
+                        const int i = j + r + tx + 32 * m;
+                        v[cc][m] = (j < n && i < n) ? G[i + (size_t)j * gld] : T(0);
+                    }
+                }
+#pragma unroll
+                for (int cc = 0; cc < 2; cc++) {
+                    const int j = j0 + cc * nty;
+#pragma unroll
+                    for (int m = 0; m < 8; m++) {
+                        const int i = j + r + tx + 32 * m;
+                        if (j < n && i < n) sm[i + j * ld] = v[cc][m];
+                    }
+                }
+            }
+        }
         __syncthreads();
         // factor and inverse together; the whole block (L below, L^{-1} transposed above) back
         __shared__ T Dpad[PNB * (PNB + 1)];  // inverse of the current diagonal block, padded rows
