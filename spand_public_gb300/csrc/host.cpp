@@ -152,7 +152,7 @@ bool partition_modified_nd_metis(const Csc& A, int nlevels, std::vector<ClusterI
         return false;
     }
     dlclose(h);
-    err = "algebraic ordering through METIS is not wired in this build; pass grid coordinates (set_Xcoo)";
+    err = "algebraic ordering through METIS is not available in this library; pass grid coordinates (set_Xcoo)";
     (void)A;
     (void)nlevels;
     (void)out;
