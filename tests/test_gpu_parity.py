@@ -505,6 +505,23 @@ def test_outgrown_launches_refactor():
         assert np.linalg.norm(xt - xo) / np.linalg.norm(xo) < TOL_SOLVE
 
 
+def test_trsv_fused_identical(monkeypatch):
+    """A solve phase's small-cluster and row-tile triangular products in one launch give
+    bit for bit the solve of the two separate launches (the two sets of clusters are
+    disjoint and each cluster runs the same code), direct and inside the CG's graph."""
+    from spand_public_gb300 import problems as P
+    monkeypatch.setenv("SPAND_TRSV_FUSE", "0")
+    A, t0, _ = _build(32, 3, 8, 1e-2, factorizations=2)
+    monkeypatch.delenv("SPAND_TRSV_FUSE")
+    _, t1, _ = _build(32, 3, 8, 1e-2, factorizations=2)
+    b = P.rhs(A.shape[0], 2, seed=13)
+    assert np.array_equal(t0.solve(b), t1.solve(b))
+    x0, it0, _ = t0.cg(b[:, 0], iters=200, tol=1e-10)
+    x1, it1, _ = t1.cg(b[:, 0], iters=200, tol=1e-10)
+    assert it0 == it1
+    assert np.array_equal(x0, x1)
+
+
 def test_pdl_sweep_identical(monkeypatch):
     """The solve sweep's kernels launched as programmatic dependents (each waits for its
     predecessor inside the kernel) give bit for bit the solve of plain stream order, direct
